@@ -1,0 +1,341 @@
+#!/usr/bin/env python
+"""FT-CCSD solves/s on GB300 (libkvft) or on the host cores (reference arm).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl kvft|reference]
+                    [--workload ueg38|ueg114] [--precision fp64|fp64_tc|mixed]
+
+A step is one complete FT-CCSD solve (Kelvin's damped amplitude iteration
+from the first-order guess to convergence) of a seeded synthetic uniform
+electron gas.  ``value`` times K solves with integrals and buffers already
+resident in HBM; ``e2e`` times K solves through the public drop-in API
+(``kelvin_gb300.ccsd.ccsd(sys, ...).run()``) from host arrays, including the
+host->device upload of the integrals and the read-back of the amplitudes.
+With N > 1 (torchrun) every rank runs an independent replica: the path has no
+exchange step at N = 1 granularity, so only timings are reduced (gloo).
+One JSON line is printed by rank 0.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "FT-CCSD solves/s"
+UNIT = "solves/s"
+
+# Workloads (uniform electron gas, Kelvin's 'lin' Simpson tau grid).
+# iters: iterations of the FP64 solve to convergence, used to scale the
+# CPU reference's per-iteration sample to solves/s.
+WORKLOADS = {
+    "ueg38": dict(N=14, rs=4.0, norb=19, theta=0.5, ng=10, damp=0.5, econv=1e-10,
+                  max_iter=100, iters=None,
+                  label="UEG 14 e-, rs=4, 19 plane waves (38 spin orbitals), Theta=0.5, "
+                        "ng=10, damping 0.5, econv 1e-10"),
+    "ueg114": dict(N=38, rs=1.0, norb=57, theta=0.25, ng=20, damp=0.5, econv=1e-10,
+                   max_iter=100, iters=None,
+                   label="UEG 38 e-, rs=1, 57 plane waves (114 spin orbitals), Theta=0.25, "
+                         "ng=20, damping 0.5, econv 1e-10"),
+}
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return d, "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, \
+        "fallback"
+
+
+class ClockSampler(object):
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for ln in self.lines:
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 8:
+                continue
+            try:
+                sm.append(float(p[0]))
+                smax.append(float(p[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, p[4:8]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax),
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def build_system(w):
+    from kelvin_gb300 import systems
+    return systems.ueg_recipe(w["N"], w["rs"], w["norb"], w["theta"])
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    return ws, rank, local
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(ws, x):
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(x)], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ---------------------------------------------------------------------------
+# CPU reference (numpy port of Kelvin's path, the oracle) on the host cores
+# ---------------------------------------------------------------------------
+def cpu_iteration_seconds(w, sysobj, reps=1):
+    """Seconds per amplitude iteration of the numpy FP64 path (Kelvin's
+    ccsd_stanton + int_tbar + ft_cc_energy + damping) on this workload."""
+    import numpy
+    from oracle import ft_ccsd, ft_utils, quadrature
+    beta = 1.0 / sysobj.T
+    en = sysobj.g_energies_tot()
+    ti, g, G = quadrature.ft_quad(w["ng"], beta, "lin")
+    F, I = ft_ccsd.ft_integrals(sysobj.g_fock_tot(), sysobj.g_aint_tot(), en, beta, sysobj.mu)
+    D1, D2 = ft_utils.D1(en, en), ft_utils.D2(en, en)
+    ng, n = w["ng"], en.shape[0]
+    T1 = numpy.zeros((ng, n, n))
+    T2 = numpy.zeros((ng, n, n, n, n))
+    best = None
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        T1n, T2n = ft_ccsd.ccsd_stanton(F, I, T1, T2, D1, D2, ti, ng, G)
+        T1 = w["damp"] * T1 + (1 - w["damp"]) * T1n
+        T2 = w["damp"] * T2 + (1 - w["damp"]) * T2n
+        ft_ccsd.ft_cc_energy(T1, T2, F.ov, I.oovv, g, beta)
+        dt = time.perf_counter() - t0
+        best = dt if best is None else min(best, dt)
+    return best
+
+
+def run_reference(args, w):
+    ws, rank, _ = dist_setup()
+    if rank != 0:
+        return 0
+    sysobj = build_system(w)
+    cores = os.cpu_count()
+    for _ in range(max(args.warmup, 0) and 1):
+        cpu_iteration_seconds(w, sysobj, 1)
+    times = [cpu_iteration_seconds(w, sysobj, 1) for _ in range(args.steps)]
+    t_iter = statistics.median(times)
+    iters = w["iters"] or 30
+    value = 1.0 / (t_iter * iters)
+    sample = ("%d steps x 1 amplitude iteration (numpy FP64, %d BLAS threads); "
+              "solves/s = 1 / (median s/iteration x %d iterations of the converged solve)"
+              % (args.steps, cores, iters))
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": t_iter * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": w["label"], "impl": "oracle numpy port of Kelvin's path"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+def run_gpu(args, w):
+    ws, rank, local = dist_setup()
+    import numpy
+    from kelvin_gb300 import _lib, ccsd
+    from kelvin_gb300.cc_utils import DeviceSolver, iterate
+    from kelvin_gb300.quadrature import ft_quad
+
+    ctx = _lib.context(local)
+    prec, digits = ccsd.PRECISIONS[args.precision]
+    if args.digits:
+        digits = args.digits
+    ctx.set_precision(prec, digits)
+    sysobj = build_system(w)
+    beta = 1.0 / sysobj.T
+    en = sysobj.g_energies_tot()
+    fock, eri = sysobj.g_fock_tot(), sysobj.g_aint_tot()
+    ti, g, G = ft_quad(w["ng"], beta, "lin")
+    conv = {"econv": w["econv"], "tconv": 1000.0 * w["econv"], "max_iter": w["max_iter"],
+            "damp": w["damp"]}
+    n = en.shape[0]
+    ng = w["ng"]
+
+    # ---- device-resident solves (value) --------------------------------------
+    solver = DeviceSolver.from_system(ctx, en, fock, eri, beta, sysobj.mu, ti, g, G)
+
+    def one_solve():
+        solver.guess(1)
+        E = iterate(solver, conv)
+        return E, solver.iterations
+
+    for _ in range(args.warmup):
+        E, iters = one_solve()
+    ctx.sync()
+    barrier(ws)
+    clocks = ClockSampler(local)
+    clocks.start()
+    l0 = ctx.launches()
+    ctx.profile_begin()
+    ctx.record(0)
+    results = []
+    for _ in range(args.steps):
+        results.append(one_solve())
+    ctx.record(1)
+    ctx.sync()
+    prof = ctx.profile_end()
+    launches = ctx.launches() - l0
+    ms = ctx.elapsed_ms(0, 1)
+    clk = clocks.stop()
+    barrier(ws)
+    ms = max_over_ranks(ws, ms)
+    value = ws * args.steps / (ms / 1e3)
+    E, iters = results[-1]
+    solver.close()
+
+    # ---- end-to-end through the public API (e2e) -----------------------------
+    barrier(ws)
+    ctx.sync()
+    t0 = time.perf_counter()
+    ctx.record(2)
+    e2e_omega = None
+    for _ in range(args.steps):
+        cc = ccsd.ccsd(sysobj, T=sysobj.T, mu=sysobj.mu, max_iter=w["max_iter"],
+                       damp=w["damp"], ngrid=ng, econv=w["econv"], precision=args.precision,
+                       digits=digits, ctx=ctx)
+        e2e_omega = cc.run()[1]
+        cc.release()
+    ctx.record(3)
+    ctx.sync()
+    e2e_ms = max(ctx.elapsed_ms(2, 3), (time.perf_counter() - t0) * 1e3)
+    e2e_ms = max_over_ranks(ws, e2e_ms)
+    e2e_value = ws * args.steps / (e2e_ms / 1e3)
+    h2d = 8 * (n + n * n + n ** 4 + 2 * ng + ng * ng)
+    d2h = 8 * ng * (n * n + n ** 4) + 8 * 7 * (iters + 2)
+
+    if rank != 0:
+        return 0
+    peaks, peak_src = load_peaks()
+    # dominant kernel category by device time over the timed region
+    dom = max(prof, key=lambda c: prof[c][1])
+    nl, dms, work = prof[dom]
+    if dom in ("gemm6", "gemm"):
+        achieved = work / (dms / 1e3) / 1e12
+        if args.precision == "fp64":
+            peak, unit, bound = 1.25, "TFLOP/s", "tensor"
+            psrc = "nominal GB300 FP64 1.25 TFLOP/s (no FP64 figure in MEASURED_PEAKS.json)"
+        else:
+            peak, unit, bound = peaks["bf16_tflops_sustained"], "TFLOP/s", "tensor"
+            psrc = "bf16_tflops_sustained of %s peaks" % peak_src
+    else:
+        achieved = work / (dms / 1e3) / 1e9
+        peak, unit, bound = peaks["hbm_gbs"], "GB/s", "hbm"
+        psrc = "hbm_gbs of %s peaks" % peak_src
+    roofline = {"bound": bound, "kernel": dom, "achieved": achieved, "peak": peak,
+                "unit": unit, "frac": achieved / peak, "traffic": None,
+                "launches": nl, "avg_launch_ms": dms / max(nl, 1), "peak_source": psrc,
+                "breakdown_ms": {c: round(prof[c][1], 3) for c in prof}}
+
+    # CPU baseline: one numpy iteration of the same workload on the host cores
+    t_iter = cpu_iteration_seconds(w, sysobj, 1)
+    cpu_val = 1.0 / (t_iter * iters)
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64" if args.precision != "mixed" else "bf16-digits/f64",
+            "data": "synthetic",
+            "config": {"workload": w["label"], "precision": args.precision,
+                       "digits": digits if args.precision != "fp64" else None,
+                       "iterations_per_solve": iters, "omega_cc": E, "e2e_omega_cc": e2e_omega,
+                       "l2": "per-iteration working set > 129 MB L2; no flush",
+                       "parallelism": "replicas" if ws > 1 else "single GPU"},
+            "roofline": roofline,
+            "cpu_baseline": {"value": cpu_val, "unit": UNIT, "cores": os.cpu_count(),
+                             "kind": "port",
+                             "sample": "1 amplitude iteration of the same workload (numpy "
+                                       "FP64 oracle port, %.2f s) x %d iterations" % (t_iter, iters)},
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h},
+            "gpu_launches": launches,
+            "clocks": clk}
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="kvft", choices=["kvft", "reference"])
+    ap.add_argument("--workload", default="ueg38", choices=sorted(WORKLOADS))
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "fp64_tc", "mixed"])
+    ap.add_argument("--digits", type=int, default=0)
+    args = ap.parse_args()
+    w = WORKLOADS[args.workload]
+    if args.impl == "reference":
+        return run_reference(args, w)
+    return run_gpu(args, w)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,187 @@
+/*
+ * kvft -- GB300-native finite-temperature CCSD amplitude iteration.
+ *
+ * C ABI of libkvft.so.  Plain pointers and sizes only.  Unless a name ends in
+ * "_host", array arguments are DEVICE pointers (allocate them with kvft_alloc
+ * or any CUDA allocator on the context's device); "_host" variants take host
+ * pointers and copy in/out on the context's stream.  All arrays are C-ordered
+ * float64 with Kelvin's index order:
+ *     T1[ng][nv][no]          (t_i^a at tau point y is T1[y][a][i])
+ *     T2[ng][nv][nv][no][no]  (t_ij^ab)
+ *     F blocks oo[no][no], ov[no][nv], vo[nv][no], vv[nv][nv]
+ *     I blocks <pq||rs> with the block's o/v letters, e.g. oovv[i][j][a][b]
+ *
+ * Every call returns a kvft_status.  Errors never abort the process; the
+ * message of the last failure on a context is kvft_last_error(ctx).
+ * A context owns one CUDA stream; calls on one context are not thread-safe,
+ * calls on different contexts are.
+ */
+#ifndef KVFT_H
+#define KVFT_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    KVFT_OK = 0,
+    KVFT_EINVAL = 1,    /* bad argument (Kelvin raises Exception here) */
+    KVFT_ENOMEM = 2,    /* device allocation failed */
+    KVFT_EDIVERGE = 3,  /* non-finite energy or residual */
+    KVFT_ETIMEOUT = 4,  /* a bounded device wait gave up */
+    KVFT_EDEVICE = 5,   /* CUDA runtime error */
+    KVFT_ENOTCONV = 6   /* iteration limit reached (Kelvin logs a warning) */
+} kvft_status;
+
+/* Arithmetic used for the n^6/n^5 contractions.  Quadrature, energy,
+ * damping and norms are FP64 in every mode. */
+typedef enum {
+    KVFT_PREC_FP64 = 0,      /* FP64 FMA (SIMT) contractions */
+    KVFT_PREC_FP64_TC = 1,   /* FP64-accurate: digit-sliced BF16 tcgen05 GEMM */
+    KVFT_PREC_MIXED = 2      /* few-digit BF16 tcgen05 GEMM, FP32-level */
+} kvft_precision;
+
+typedef struct kvft_ctx kvft_ctx;
+typedef struct kvft_solver kvft_solver;
+
+/* ---- context, memory, timing ------------------------------------------ */
+int kvft_ctx_create(int device, void *stream, kvft_ctx **out);
+int kvft_ctx_destroy(kvft_ctx *ctx);
+const char *kvft_last_error(const kvft_ctx *ctx);
+const char *kvft_status_string(int status);
+int kvft_set_precision(kvft_ctx *ctx, int precision, int digits);
+int kvft_alloc(kvft_ctx *ctx, size_t bytes, void **dptr);
+int kvft_free(kvft_ctx *ctx, void *dptr);
+int kvft_h2d(kvft_ctx *ctx, void *dst, const void *src, size_t bytes);
+int kvft_d2h(kvft_ctx *ctx, void *dst, const void *src, size_t bytes);
+int kvft_memset(kvft_ctx *ctx, void *dptr, int value, size_t bytes);
+int kvft_sync(kvft_ctx *ctx);
+int kvft_event_record(kvft_ctx *ctx, int slot);            /* slot < 64 */
+int kvft_event_elapsed_ms(kvft_ctx *ctx, int s0, int s1, float *ms);
+int kvft_launch_count(kvft_ctx *ctx, uint64_t *count);     /* own kernels */
+int kvft_flush_l2(kvft_ctx *ctx);                          /* writes 256 MB */
+
+/* Live launch timing: between begin and end every library launch of the
+ * categories below is bracketed by CUDA events on the context's stream.
+ * work = algorithmic flops (GEMM categories) or bytes (the others). */
+enum {
+    KVFT_CAT_GEMM6 = 0,   /* n^6-class contractions (M, N, K all >= n^2) */
+    KVFT_CAT_GEMM = 1,    /* the other contractions */
+    KVFT_CAT_QUAD = 2,    /* tau integration (+ fused damping) */
+    KVFT_CAT_ENERGY = 3,
+    KVFT_CAT_ELEM = 4,    /* element-wise tensor passes */
+    KVFT_CAT_PACK = 5     /* tensor-core operand packing */
+};
+typedef struct {
+    uint64_t launches[6];
+    double ms[6];
+    double work[6];
+} kvft_profile_stats;
+int kvft_profile_begin(kvft_ctx *ctx);
+int kvft_profile_end(kvft_ctx *ctx, kvft_profile_stats *out);
+
+/* ---- quadrature: replaces kelvin/quadrature.py:292-317 ------------------
+ * out[y] = sum_x G[y][x] exp(dt D) tbar[x], dt = ti[x]-ti[y] for x < y and 0
+ * otherwise (full != 0: for every x).  D has the shape of one tau slice
+ * (D1[nv][no] / D2[nv][nv][no][no]); ti[ng], G[ng][ng]. */
+int kvft_int_tbar1(kvft_ctx *ctx, int ng, int nv, int no, const double *t1bar,
+                   const double *ti, const double *D1, const double *G,
+                   int full, double *t1out);
+int kvft_int_tbar2(kvft_ctx *ctx, int ng, int nv, int no, const double *t2bar,
+                   const double *ti, const double *D2, const double *G,
+                   int full, double *t2out);
+/* single grid point ig: replaces quadrature.py:348-369 */
+int kvft_int_tbar1_single(kvft_ctx *ctx, int ng, int ig, int nv, int no,
+                          const double *t1bar, const double *ti,
+                          const double *D1, const double *G, double *t1out);
+int kvft_int_tbar2_single(kvft_ctx *ctx, int ng, int ig, int nv, int no,
+                          const double *t2bar, const double *ti,
+                          const double *D2, const double *G, double *t2out);
+
+/* ---- energy: replaces kelvin/ft_cc_energy.py:7-32 -----------------------
+ * omega_host receives (1/beta)[sum t1n.f + sum t2n.eri]; f = F.ov[no][nv],
+ * eri = I.oovv[no][no][nv][nv], g[ng]. */
+int kvft_ft_cc_energy(kvft_ctx *ctx, int ng, int nv, int no, const double *T1,
+                      const double *T2, const double *f, const double *eri,
+                      const double *g, double beta, int qterm,
+                      double *omega_host);
+
+/* ---- CCSD update: replaces kelvin/ft_cc_equations.py:96-113 -------------
+ * F[4] = {oo, ov, vo, vv}; I[9] = {vvvv, vvvo, vovv, vvoo, vovo, oovv, vooo,
+ * ooov, oooo}.  T1new/T2new receive the integrated amplitudes. */
+int kvft_ccsd_stanton(kvft_ctx *ctx, int ng, int nv, int no,
+                      const double *const F[4], const double *const I[9],
+                      const double *T1old, const double *T2old,
+                      const double *D1, const double *D2, const double *ti,
+                      const double *G, int full, double *T1new, double *T2new);
+/* The tau-point residual alone (cqcpy _Stanton with fac, called at
+ * ft_cc_equations.py:106-107): T1 += fac R1(t1,t2), T2 += fac R2, batched
+ * over nb tau points. */
+int kvft_stanton_residual(kvft_ctx *ctx, int nb, int nv, int no,
+                          const double *const F[4], const double *const I[9],
+                          const double *t1, const double *t2, double fac,
+                          double *T1, double *T2);
+
+/* ---- Fermi-scaled integrals: replaces kelvin/cc_utils.py:569-602 ---------
+ * eps[n], fock[n][n] (System.g_fock_tot), eri[n]^4 (System.g_aint_tot) and
+ * the outputs F[4] (n x n), I[9] (n^4) are device pointers. */
+int kvft_ft_integrals(kvft_ctx *ctx, int n, const double *eps,
+                      const double *fock, const double *eri, double beta,
+                      double mu, double *const F[4], double *const I[9]);
+
+/* ---- device-resident solver: replaces kelvin/ccsd.py:595-712 with
+ * cc_utils.ft_integrals (569-602) and cc_utils.ft_cc_iter (111-173) -------
+ * eps[n] orbital energies, fock[n][n] (System.g_fock_tot), eri[n][n][n][n]
+ * (System.g_aint_tot), all HOST pointers; grid ti/g/G host pointers. */
+typedef struct {
+    double econv;     /* |dE| threshold */
+    double tconv;     /* res1+res2 threshold */
+    double damp;      /* alpha in T_old = alpha T_old + (1-alpha) T */
+    int max_iter;
+    int full;         /* dense-G exponential convention */
+    int guess;        /* 0: zero amplitudes, 1: Kelvin's first-order guess,
+                         2: the amplitudes currently held (warm start) */
+    int verbose;
+} kvft_solve_opts;
+
+typedef struct {
+    double omega_cc;  /* Gcc */
+    double e_guess;   /* energy of the initial amplitudes, Qterm = false */
+    double res;       /* last res1 + res2 */
+    int iterations;
+    int converged;
+} kvft_result;
+
+int kvft_solver_create(kvft_ctx *ctx, int n, int ng, const double *eps,
+                       const double *fock, const double *eri, double beta,
+                       double mu, const double *ti, const double *g,
+                       const double *G, kvft_solver **out);
+/* Solver over given Fermi-scaled blocks and explicit denominators (host
+ * pointers), the inputs of kelvin/cc_utils.py:111 ft_cc_iter. */
+int kvft_solver_create_blocks(kvft_ctx *ctx, int nv, int no, int ng,
+                              const double *const F[4],
+                              const double *const I[9], const double *D1,
+                              const double *D2, double beta, const double *ti,
+                              const double *g, const double *G,
+                              kvft_solver **out);
+int kvft_solver_destroy(kvft_solver *s);
+int kvft_solver_run(kvft_solver *s, const kvft_solve_opts *opts,
+                    kvft_result *res);
+/* one amplitude iteration (update + damping + norms + energy) */
+int kvft_solver_step(kvft_solver *s, double damp, double *energy,
+                     double *res);
+int kvft_solver_get_amplitudes(kvft_solver *s, double *T1_host,
+                               double *T2_host);
+int kvft_solver_set_amplitudes(kvft_solver *s, const double *T1_host,
+                               const double *T2_host);
+/* Device pointers of the solver's resident amplitudes (T1, T2). */
+int kvft_solver_device_amplitudes(kvft_solver *s, double **T1, double **T2);
+size_t kvft_solver_footprint(int n, int ng, int precision);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* KVFT_H */

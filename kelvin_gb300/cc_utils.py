@@ -1,0 +1,182 @@
+"""Iteration and integral plumbing, drop-in for the FT general-spin parts of
+kelvin/cc_utils.py.
+
+* ``ft_integrals(sys, en, beta, mu)`` -- Fermi-scaled blocks, computed on the
+  GPU (cc_utils.py:569-602);
+* ``form_new_ampl`` -- method dispatch (cc_utils.py:17-49; CCSD only);
+* ``ft_cc_iter`` -- the damped fixed-point loop (cc_utils.py:111-173) with
+  every array resident on the device: each iteration is one libkvft call
+  (update + integration + damping + norms + energy) and a 5-double read back.
+"""
+import ctypes
+import logging
+import time
+
+import numpy
+
+from . import _lib
+from .ft_cc_equations import F_ORDER, I_ORDER, ccsd_stanton
+
+
+class one_e_blocks(object):
+    """Attribute container .oo .ov .vo .vv."""
+
+    def __init__(self, oo, ov, vo, vv):
+        self.oo, self.ov, self.vo, self.vv = oo, ov, vo, vv
+
+
+class two_e_blocks(object):
+    """Attribute container for the nine antisymmetrised ERI blocks."""
+
+    def __init__(self, vvvv=None, vvvo=None, vovv=None, vvoo=None, vovo=None,
+                 oovv=None, vooo=None, ooov=None, oooo=None):
+        self.vvvv, self.vvvo, self.vovv = vvvv, vvvo, vovv
+        self.vvoo, self.vovo, self.oovv = vvoo, vovo, oovv
+        self.vooo, self.ooov, self.oooo = vooo, ooov, oooo
+
+
+def ft_integrals(sys, en, beta, mu, ctx=None):
+    """One- and two-electron integrals scaled by sqrt(f) / sqrt(1-f)."""
+    ctx = ctx or _lib.context()
+    en = numpy.ascontiguousarray(en, dtype=float)
+    n = en.shape[0]
+    deps = _lib.DeviceArray.from_host(ctx, en)
+    dfock = _lib.DeviceArray.from_host(ctx, sys.g_fock_tot())
+    deri = _lib.DeviceArray.from_host(ctx, sys.g_aint_tot())
+    F = [_lib.DeviceArray(ctx, (n, n)) for _ in range(4)]
+    I = [_lib.DeviceArray(ctx, (n, n, n, n)) for _ in range(9)]
+    ctx.check(ctx.L.kvft_ft_integrals(ctx.h, n, deps.ptr, dfock.ptr, deri.ptr, float(beta),
+                                      float(mu), _lib.ptr_array(F), _lib.ptr_array(I)),
+              "ft_integrals")
+    return (one_e_blocks(**{b: a.to_host() for b, a in zip(F_ORDER, F)}),
+            two_e_blocks(**{b: a.to_host() for b, a in zip(I_ORDER, I)}))
+
+
+def form_new_ampl(method, F, I, T1old, T2old, D1, D2, ti, ng, G):
+    """New amplitudes for ``method`` (only "CCSD" is on this path)."""
+    if method == "CCSD":
+        return ccsd_stanton(F, I, T1old, T2old, D1, D2, ti, ng, G)
+    raise Exception("Unrecognized method keyword")
+
+
+class DeviceSolver(object):
+    """A kvft_solver: integrals, grid and amplitudes resident in HBM."""
+
+    def __init__(self, ctx, handle, ng, nv, no):
+        self.ctx = ctx
+        self.h = handle
+        self.ng, self.nv, self.no = ng, nv, no
+
+    @classmethod
+    def from_system(cls, ctx, en, fock, eri, beta, mu, ti, g, G):
+        en, fock, eri, ti, g, G = (numpy.ascontiguousarray(a, dtype=float)
+                                   for a in (en, fock, eri, ti, g, G))
+        n, ng = en.shape[0], ti.shape[0]
+        h = _lib.vp()
+        ctx.check(ctx.L.kvft_solver_create(
+            ctx.h, n, ng, en.ctypes.data_as(_lib.vp), fock.ctypes.data_as(_lib.vp),
+            eri.ctypes.data_as(_lib.vp), float(beta), float(mu), ti.ctypes.data_as(_lib.vp),
+            g.ctypes.data_as(_lib.vp), G.ctypes.data_as(_lib.vp), ctypes.byref(h)),
+            "kvft_solver_create")
+        return cls(ctx, h, ng, n, n)
+
+    @classmethod
+    def from_blocks(cls, ctx, F, I, D1, D2, beta, ti, g, G):
+        Fa = [numpy.ascontiguousarray(getattr(F, b), dtype=float) for b in F_ORDER]
+        Ia = [numpy.ascontiguousarray(getattr(I, b), dtype=float) for b in I_ORDER]
+        D1, D2, ti, g, G = (numpy.ascontiguousarray(a, dtype=float) for a in (D1, D2, ti, g, G))
+        nv, no = Fa[2].shape
+        ng = ti.shape[0]
+        Fp = (_lib.vp * 4)(*[a.ctypes.data_as(_lib.vp) for a in Fa])
+        Ip = (_lib.vp * 9)(*[a.ctypes.data_as(_lib.vp) for a in Ia])
+        h = _lib.vp()
+        ctx.check(ctx.L.kvft_solver_create_blocks(
+            ctx.h, nv, no, ng, Fp, Ip, D1.ctypes.data_as(_lib.vp), D2.ctypes.data_as(_lib.vp),
+            float(beta), ti.ctypes.data_as(_lib.vp), g.ctypes.data_as(_lib.vp),
+            G.ctypes.data_as(_lib.vp), ctypes.byref(h)), "kvft_solver_create_blocks")
+        return cls(ctx, h, ng, nv, no)
+
+    def set_amplitudes(self, T1, T2):
+        T1 = numpy.ascontiguousarray(T1, dtype=float)
+        T2 = numpy.ascontiguousarray(T2, dtype=float)
+        self.ctx.check(self.ctx.L.kvft_solver_set_amplitudes(
+            self.h, T1.ctypes.data_as(_lib.vp), T2.ctypes.data_as(_lib.vp)),
+            "kvft_solver_set_amplitudes")
+
+    def amplitudes(self):
+        T1 = numpy.empty((self.ng, self.nv, self.no))
+        T2 = numpy.empty((self.ng, self.nv, self.nv, self.no, self.no))
+        self.ctx.check(self.ctx.L.kvft_solver_get_amplitudes(
+            self.h, T1.ctypes.data_as(_lib.vp), T2.ctypes.data_as(_lib.vp)),
+            "kvft_solver_get_amplitudes")
+        return T1, T2
+
+    def guess(self, kind, damp=0.0):
+        """kind 0: zeros, 1: Kelvin's first-order guess, 2: keep.  Runs zero
+        iterations and returns the guess energy (Qterm = False)."""
+        o = _lib.SolveOpts(econv=0.0, tconv=0.0, damp=damp, max_iter=0, full=0,
+                           guess=int(kind), verbose=0)
+        r = _lib.Result()
+        st = self.ctx.L.kvft_solver_run(self.h, ctypes.byref(o), ctypes.byref(r))
+        if st not in (0, 6):
+            self.ctx.check(st, "kvft_solver_run(guess)")
+        return r.e_guess
+
+    def step(self, damp):
+        E = ctypes.c_double()
+        res = ctypes.c_double()
+        self.ctx.check(self.ctx.L.kvft_solver_step(self.h, float(damp), ctypes.byref(E),
+                                                   ctypes.byref(res)), "kvft_solver_step")
+        return E.value, res.value
+
+    def close(self):
+        if self.h:
+            self.ctx.L.kvft_solver_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def iterate(solver, conv_options, method="CCSD"):
+    """The loop of cc_utils.py:131-173 on a DeviceSolver; returns Eold."""
+    tbeg = time.time()
+    ethresh = conv_options["econv"]
+    tthresh = conv_options["tconv"]
+    max_iter = conv_options["max_iter"]
+    alpha = conv_options["damp"]
+    converged = False
+    Eold = 888888888.888888888
+    i = 0
+    while i < max_iter and not converged:
+        E, res = solver.step(alpha)
+        logging.info(' %2d  %.10f   %.4E' % (i + 1, E, res))
+        i += 1
+        if numpy.abs(E - Eold) < ethresh and res < tthresh:
+            converged = True
+        Eold = E
+    if not converged:
+        logging.warning("{} did not converge!".format(method))
+    logging.info("Total {} time: {:.4f} s".format(method, time.time() - tbeg))
+    solver.iterations = i
+    solver.converged = converged
+    return Eold
+
+
+def ft_cc_iter(method, T1old, T2old, F, I, D1, D2, g, G, beta, ng, ti, iprint,
+               conv_options, ctx=None):
+    """Damped FT-CC iteration (cc_utils.py:111-173); returns (E, T1, T2)."""
+    if method != "CCSD":
+        raise Exception("Unrecognized method keyword")
+    ctx = ctx or _lib.context()
+    solver = DeviceSolver.from_blocks(ctx, F, I, D1, D2, beta, ti, g, G)
+    try:
+        solver.set_amplitudes(T1old, T2old)
+        E = iterate(solver, conv_options, method)
+        T1, T2 = solver.amplitudes()
+    finally:
+        solver.close()
+    return E, T1, T2

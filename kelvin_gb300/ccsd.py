@@ -1,0 +1,113 @@
+"""Finite-temperature CCSD driver, drop-in for kelvin.ccsd.ccsd (the FT
+general-spin path, kelvin/ccsd.py:43-126 and 595-712).
+
+    cc = ccsd(sys, T=T, mu=mu, damp=0.2, ngrid=10)
+    Omega, Omega_cc = cc.run()
+
+The system's integrals are uploaded once; integrals, tau grid and amplitudes
+stay resident in HBM for the whole solve, and each iteration is one libkvft
+call.  ``precision`` selects the contraction arithmetic ('fp64', 'fp64_tc',
+'mixed'); quadrature, energy and damping are FP64 in every mode.
+"""
+import logging
+
+import numpy
+
+from . import _lib
+from .cc_utils import DeviceSolver, iterate
+from .quadrature import ft_quad
+from .systems import grand_potential0
+
+PRECISIONS = {'fp64': (_lib.PREC_FP64, 7), 'fp64_tc': (_lib.PREC_FP64_TC, 7),
+              'mixed': (_lib.PREC_MIXED, 3)}
+
+
+class ccsd(object):
+    """Coupled cluster singles and doubles (CCSD) driver, T > 0."""
+
+    def __init__(self, sys, T=0.0, mu=0.0, iprint=0, singles=True, econv=1e-8,
+                 tconv=None, max_iter=40, damp=0.0, ngrid=10, realtime=False,
+                 athresh=0.0, quad='lin', rt_iter="all", precision='fp64',
+                 digits=None, device=0, ctx=None):
+        self.T = T
+        self.mu = mu
+        self.finite_T = T != 0
+        self.iprint = iprint
+        self.singles = singles
+        self.econv = econv
+        self.tconv = tconv if tconv is not None else 1000.0 * econv
+        self.max_iter = max_iter
+        self.damp = damp
+        self.ngrid = ngrid
+        self.realtime = True if self.finite_T else realtime
+        self.athresh = athresh
+        self.quad = quad
+        self.rt_iter = rt_iter
+        if precision not in PRECISIONS:
+            raise Exception("Unrecognized precision: {}".format(precision))
+        self.precision = precision
+        self.digits = digits if digits is not None else PRECISIONS[precision][1]
+        if not sys.verify(self.T, self.mu):
+            raise Exception("Sytem temperature inconsistent with CC temp")
+        if not self.finite_T:
+            raise Exception("kelvin_gb300.ccsd: only the finite-temperature path is built")
+        if not singles:
+            raise Exception("kelvin_gb300.ccsd: only CCSD (singles=True) is built")
+        if athresh > 0.0:
+            raise Exception("kelvin_gb300.ccsd: active-space thresholds are not built")
+        self.beta = 1.0 / T
+        self.beta_max = self.beta
+        self.ti, self.g, self.G = ft_quad(self.ngrid, self.beta_max, self.quad)
+        self.sys = sys
+        self.ctx = ctx or _lib.context(device)
+        self.T1 = None
+        self.T2 = None
+        self.solver = None
+
+    def run(self, T1=None, T2=None):
+        """Solve; returns (Omega_total, Omega_cc) like Kelvin."""
+        logging.info('Running CCSD at an electronic temperature of %f K'
+                     % (self.T * 315775.13))
+        return self._ft_ccsd(T1in=T1, T2in=T2)
+
+    def _ft_ccsd(self, T1in=None, T2in=None):
+        beta = self.beta
+        mu = self.mu
+        en = self.sys.g_energies_tot()
+        E0 = grand_potential0(beta, en, mu) + self.sys.const_energy()
+        E1 = self.sys.get_mp1()
+        if self.quad == 'gl':
+            raise Exception("the dense Gauss-Legendre G needs the full exp convention, "
+                            "which the resident solver does not run")
+        prec, digits = PRECISIONS[self.precision][0], self.digits
+        self.ctx.set_precision(prec, digits)
+        solver = DeviceSolver.from_system(self.ctx, en, self.sys.g_fock_tot(),
+                                          self.sys.g_aint_tot(), beta, mu, self.ti, self.g,
+                                          self.G)
+        self.solver = solver
+        if self.rt_iter[0] != 'a' and T2in is None:
+            logging.warning("Convergence scheme ({}) is not built; using 'all'"
+                            .format(self.rt_iter))
+        if T1in is not None and T2in is not None:
+            solver.set_amplitudes(T1in, T2in)
+            E2 = solver.guess(2)
+        else:
+            E2 = solver.guess(1)
+        logging.info('MP2 Energy: {:.10f}'.format(E2))
+        conv = {"econv": self.econv, "tconv": self.tconv, "max_iter": self.max_iter,
+                "damp": self.damp}
+        Eccn = iterate(solver, conv, "CCSD")
+        self.iterations = solver.iterations
+        self.converged = solver.converged
+        self.T1, self.T2 = solver.amplitudes()
+        self.G0 = E0
+        self.G1 = E1
+        self.Gcc = Eccn
+        self.Gtot = E0 + E1 + Eccn
+        return (Eccn + E0 + E1, Eccn)
+
+    def release(self):
+        """Free the device buffers of the last solve."""
+        if self.solver is not None:
+            self.solver.close()
+            self.solver = None

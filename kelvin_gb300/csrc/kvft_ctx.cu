@@ -1,0 +1,247 @@
+// Context, memory, timing and error plumbing of libkvft.
+#include "kvft_internal.h"
+
+#include <cstdio>
+#include <cstring>
+#include <new>
+
+int kv_fail(kvft_ctx *ctx, int code, const std::string &msg) {
+    if (ctx) ctx->err = msg;
+    return code;
+}
+
+int kv_cuda(kvft_ctx *ctx, cudaError_t e, const char *what) {
+    std::string m = std::string(what) + ": " + cudaGetErrorString(e);
+    int code = (e == cudaErrorMemoryAllocation) ? KVFT_ENOMEM : KVFT_EDEVICE;
+    return kv_fail(ctx, code, m);
+}
+
+int kv_launch_check(kvft_ctx *ctx, const char *what) {
+    ctx->launches++;
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return kv_cuda(ctx, e, what);
+    return KVFT_OK;
+}
+
+int kv_scratch(kvft_ctx *ctx, const char *key, size_t bytes, void **p) {
+    auto it = ctx->scratch.find(key);
+    if (it != ctx->scratch.end() && it->second.second >= bytes) {
+        *p = it->second.first;
+        return KVFT_OK;
+    }
+    if (it != ctx->scratch.end()) {
+        KV_CHECK(ctx, cudaStreamSynchronize(ctx->stream));
+        cudaFree(it->second.first);
+        ctx->scratch.erase(it);
+    }
+    void *q = nullptr;
+    size_t b = bytes ? bytes : 256;
+    KV_CHECK(ctx, cudaMalloc(&q, b));
+    ctx->scratch[key] = {q, b};
+    *p = q;
+    return KVFT_OK;
+}
+
+extern "C" {
+
+const char *kvft_status_string(int s) {
+    switch (s) {
+    case KVFT_OK: return "ok";
+    case KVFT_EINVAL: return "invalid argument";
+    case KVFT_ENOMEM: return "device memory exhausted";
+    case KVFT_EDIVERGE: return "iteration diverged";
+    case KVFT_ETIMEOUT: return "device wait timed out";
+    case KVFT_EDEVICE: return "CUDA error";
+    case KVFT_ENOTCONV: return "not converged";
+    default: return "unknown status";
+    }
+}
+
+int kvft_ctx_create(int device, void *stream, kvft_ctx **out) {
+    if (!out) return KVFT_EINVAL;
+    *out = nullptr;
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || ndev == 0) return KVFT_EDEVICE;
+    if (device < 0 || device >= ndev) return KVFT_EINVAL;
+    kvft_ctx *c = new (std::nothrow) kvft_ctx();
+    if (!c) return KVFT_ENOMEM;
+    c->device = device;
+    if (cudaSetDevice(device) != cudaSuccess) { delete c; return KVFT_EDEVICE; }
+    cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device);
+    if (stream) {
+        c->stream = (cudaStream_t)stream;
+    } else {
+        if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+            delete c;
+            return KVFT_EDEVICE;
+        }
+        c->own_stream = true;
+    }
+    for (int i = 0; i < 64; i++) cudaEventCreate(&c->ev[i]);
+    if (cudaMalloc(&c->dflag, 64 * sizeof(int)) != cudaSuccess) {
+        delete c;
+        return KVFT_ENOMEM;
+    }
+    cudaMemsetAsync(c->dflag, 0, 64 * sizeof(int), c->stream);
+    *out = c;
+    return KVFT_OK;
+}
+
+int kvft_ctx_destroy(kvft_ctx *c) {
+    if (!c) return KVFT_OK;
+    cudaSetDevice(c->device);
+    cudaStreamSynchronize(c->stream);
+    for (auto &kv : c->scratch) cudaFree(kv.second.first);
+    if (c->prof) {
+        for (auto e : c->prof->pool) cudaEventDestroy(e);
+        delete c->prof;
+    }
+    if (c->l2buf) cudaFree(c->l2buf);
+    if (c->dflag) cudaFree(c->dflag);
+    for (int i = 0; i < 64; i++) cudaEventDestroy(c->ev[i]);
+    if (c->own_stream) cudaStreamDestroy(c->stream);
+    delete c;
+    return KVFT_OK;
+}
+
+const char *kvft_last_error(const kvft_ctx *c) { return c ? c->err.c_str() : "null context"; }
+
+int kvft_set_precision(kvft_ctx *c, int precision, int digits) {
+    if (!c) return KVFT_EINVAL;
+    if (precision < KVFT_PREC_FP64 || precision > KVFT_PREC_MIXED)
+        return kv_fail(c, KVFT_EINVAL, "unknown precision");
+    if (precision != KVFT_PREC_FP64 && (digits < 2 || digits > 9))
+        return kv_fail(c, KVFT_EINVAL, "digit levels must be in [2, 9]");
+    c->precision = precision;
+    c->digits = digits;
+    return KVFT_OK;
+}
+
+int kvft_alloc(kvft_ctx *c, size_t bytes, void **p) {
+    if (!c || !p) return KVFT_EINVAL;
+    cudaSetDevice(c->device);
+    KV_CHECK(c, cudaMalloc(p, bytes ? bytes : 16));
+    return KVFT_OK;
+}
+
+int kvft_free(kvft_ctx *c, void *p) {
+    if (!c) return KVFT_EINVAL;
+    KV_CHECK(c, cudaStreamSynchronize(c->stream));
+    KV_CHECK(c, cudaFree(p));
+    return KVFT_OK;
+}
+
+int kvft_h2d(kvft_ctx *c, void *dst, const void *src, size_t bytes) {
+    if (!c) return KVFT_EINVAL;
+    KV_CHECK(c, cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, c->stream));
+    return KVFT_OK;
+}
+
+int kvft_d2h(kvft_ctx *c, void *dst, const void *src, size_t bytes) {
+    if (!c) return KVFT_EINVAL;
+    KV_CHECK(c, cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, c->stream));
+    KV_CHECK(c, cudaStreamSynchronize(c->stream));
+    return KVFT_OK;
+}
+
+int kvft_memset(kvft_ctx *c, void *p, int v, size_t bytes) {
+    if (!c) return KVFT_EINVAL;
+    KV_CHECK(c, cudaMemsetAsync(p, v, bytes, c->stream));
+    return KVFT_OK;
+}
+
+int kvft_sync(kvft_ctx *c) {
+    if (!c) return KVFT_EINVAL;
+    KV_CHECK(c, cudaStreamSynchronize(c->stream));
+    return KVFT_OK;
+}
+
+int kvft_event_record(kvft_ctx *c, int slot) {
+    if (!c || slot < 0 || slot >= 64) return KVFT_EINVAL;
+    KV_CHECK(c, cudaEventRecord(c->ev[slot], c->stream));
+    return KVFT_OK;
+}
+
+int kvft_event_elapsed_ms(kvft_ctx *c, int s0, int s1, float *ms) {
+    if (!c || s0 < 0 || s0 >= 64 || s1 < 0 || s1 >= 64 || !ms) return KVFT_EINVAL;
+    KV_CHECK(c, cudaEventSynchronize(c->ev[s1]));
+    KV_CHECK(c, cudaEventElapsedTime(ms, c->ev[s0], c->ev[s1]));
+    return KVFT_OK;
+}
+
+int kvft_launch_count(kvft_ctx *c, uint64_t *count) {
+    if (!c || !count) return KVFT_EINVAL;
+    *count = c->launches;
+    return KVFT_OK;
+}
+
+}  // extern "C"
+
+// ---- live launch timing ------------------------------------------------------
+int kv_prof_mark(kvft_ctx *ctx, size_t *slot) {
+    KvProf *p = ctx->prof;
+    if (p->used == p->pool.size()) {
+        cudaEvent_t e;
+        KV_CHECK(ctx, cudaEventCreate(&e));
+        p->pool.push_back(e);
+    }
+    *slot = p->used++;
+    KV_CHECK(ctx, cudaEventRecord(p->pool[*slot], ctx->stream));
+    return KVFT_OK;
+}
+
+void kv_prof_add(kvft_ctx *ctx, int cat, size_t e0, size_t e1, double work) {
+    ctx->prof->recs.push_back({cat, e0, e1, work});
+}
+
+KvProfScope::KvProfScope(kvft_ctx *c, int k, double w)
+    : ctx(c), cat(k), work(w), e0(0), on(c->prof && c->prof->on) {
+    if (on && kv_prof_mark(ctx, &e0) != KVFT_OK) on = false;
+}
+
+KvProfScope::~KvProfScope() {
+    size_t e1;
+    if (on && kv_prof_mark(ctx, &e1) == KVFT_OK) kv_prof_add(ctx, cat, e0, e1, work);
+}
+
+extern "C" int kvft_profile_begin(kvft_ctx *c) {
+    if (!c) return KVFT_EINVAL;
+    if (!c->prof) c->prof = new KvProf();
+    c->prof->on = true;
+    c->prof->used = 0;
+    c->prof->recs.clear();
+    return KVFT_OK;
+}
+
+extern "C" int kvft_profile_end(kvft_ctx *c, kvft_profile_stats *out) {
+    if (!c || !c->prof || !out) return KVFT_EINVAL;
+    KV_CHECK(c, cudaStreamSynchronize(c->stream));
+    memset(out, 0, sizeof(*out));
+    for (auto &r : c->prof->recs) {
+        float ms = 0.f;
+        KV_CHECK(c, cudaEventElapsedTime(&ms, c->prof->pool[r.e0], c->prof->pool[r.e1]));
+        out->launches[r.cat] += 1;
+        out->ms[r.cat] += ms;
+        out->work[r.cat] += r.work;
+    }
+    c->prof->on = false;
+    c->prof->recs.clear();
+    c->prof->used = 0;
+    return KVFT_OK;
+}
+
+__global__ void kv_flush_kernel(uint4 *p, size_t n, unsigned salt) {
+    size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (; i < n; i += stride) p[i] = make_uint4(salt, (unsigned)i, salt, 0u);
+}
+
+extern "C" int kvft_flush_l2(kvft_ctx *c) {
+    if (!c) return KVFT_EINVAL;
+    const size_t bytes = 256ull << 20;  // twice the 129 MB L2
+    if (!c->l2buf) KV_CHECK(c, cudaMalloc(&c->l2buf, bytes));
+    static unsigned salt = 1;
+    kv_flush_kernel<<<c->sm_count * 4, 512, 0, c->stream>>>((uint4 *)c->l2buf, bytes / 16, salt++);
+    return kv_launch_check(c, "flush_l2");
+}

@@ -1,0 +1,173 @@
+// Element-wise kernels of the CCSD update: permuted axpby, tau amplitudes,
+// W_mbej helper, the antisymmetrised T2 assembly and batch broadcast.  All are
+// HBM-bound grid-stride loops over a tau batch of n^4 tensors.
+#include "kvft_internal.h"
+
+namespace {
+
+inline int grid_for(kvft_ctx *ctx, long long total, int threads) {
+    long long b = (total + threads - 1) / threads;
+    long long cap = (long long)ctx->sm_count * 8;
+    return (int)std::max(1LL, std::min(b, cap));
+}
+
+struct Dims4 {
+    int d[4];
+    long long ss[4], ds[4];
+    long long sbst, dbst;
+};
+
+__global__ void axpby4_kernel(long long total, Dims4 g, double alpha,
+                              const double *__restrict__ src, double beta,
+                              double *__restrict__ dst) {
+    for (long long x = blockIdx.x * (long long)blockDim.x + threadIdx.x; x < total;
+         x += (long long)gridDim.x * blockDim.x) {
+        long long r = x;
+        int i3 = (int)(r % g.d[3]); r /= g.d[3];
+        int i2 = (int)(r % g.d[2]); r /= g.d[2];
+        int i1 = (int)(r % g.d[1]); r /= g.d[1];
+        int i0 = (int)(r % g.d[0]); r /= g.d[0];
+        long long b = r;
+        long long so = b * g.sbst + i0 * g.ss[0] + i1 * g.ss[1] + i2 * g.ss[2] + i3 * g.ss[3];
+        long long dof = b * g.dbst + i0 * g.ds[0] + i1 * g.ds[1] + i2 * g.ds[2] + i3 * g.ds[3];
+        double v = alpha * src[so];
+        dst[dof] = (beta != 0.0) ? v + beta * dst[dof] : v;
+    }
+}
+
+// out[y,a,b,i,j] = t2 + c (t1[a,i] t1[b,j] - t1[b,i] t1[a,j])
+__global__ void make_tau_kernel(long long total, int nv, int no,
+                                const double *__restrict__ t1,
+                                const double *__restrict__ t2, double c,
+                                double *__restrict__ out) {
+    const long long s4 = (long long)nv * nv * no * no;
+    for (long long x = blockIdx.x * (long long)blockDim.x + threadIdx.x; x < total;
+         x += (long long)gridDim.x * blockDim.x) {
+        long long y = x / s4;
+        long long r = x - y * s4;
+        int j = (int)(r % no); r /= no;
+        int i = (int)(r % no); r /= no;
+        int b = (int)(r % nv);
+        int a = (int)(r / nv);
+        const double *u = t1 + y * nv * no;
+        out[x] = t2[x] + c * (u[a * no + i] * u[b * no + j] - u[b * no + i] * u[a * no + j]);
+    }
+}
+
+// out[y,f,b,j,n] = 0.5 t2[y,f,b,j,n] + t1[y,f,j] t1[y,b,n]
+__global__ void wmbej_tmp_kernel(long long total, int nv, int no,
+                                 const double *__restrict__ t1,
+                                 const double *__restrict__ t2,
+                                 double *__restrict__ out) {
+    const long long s4 = (long long)nv * nv * no * no;
+    for (long long x = blockIdx.x * (long long)blockDim.x + threadIdx.x; x < total;
+         x += (long long)gridDim.x * blockDim.x) {
+        long long y = x / s4;
+        long long r = x - y * s4;
+        int n = (int)(r % no); r /= no;
+        int j = (int)(r % no); r /= no;
+        int b = (int)(r % nv);
+        int f = (int)(r / nv);
+        const double *u = t1 + y * nv * no;
+        out[x] = 0.5 * t2[x] + u[f * no + j] * u[b * no + n];
+    }
+}
+
+__global__ void assemble_t2_kernel(long long total, int nv, int no, double fac,
+                                   const double *__restrict__ Zab,
+                                   const double *__restrict__ Zij,
+                                   const double *__restrict__ Zabij,
+                                   double *__restrict__ T2) {
+    const long long s4 = (long long)nv * nv * no * no;
+    const long long sa = (long long)nv * no * no, sb = (long long)no * no, si = no;
+    for (long long x = blockIdx.x * (long long)blockDim.x + threadIdx.x; x < total;
+         x += (long long)gridDim.x * blockDim.x) {
+        long long y = x / s4;
+        long long r = x - y * s4;
+        int j = (int)(r % no); r /= no;
+        int i = (int)(r % no); r /= no;
+        int b = (int)(r % nv);
+        int a = (int)(r / nv);
+        long long base = y * s4;
+        long long abij = base + a * sa + b * sb + i * si + j;
+        long long baij = base + b * sa + a * sb + i * si + j;
+        long long abji = base + a * sa + b * sb + j * si + i;
+        long long baji = base + b * sa + a * sb + j * si + i;
+        double v = 0.0;
+        if (Zab) v += Zab[abij] - Zab[baij];
+        if (Zij) v += Zij[abij] - Zij[abji];
+        if (Zabij) v += Zabij[abij] - Zabij[baij] - Zabij[abji] + Zabij[baji];
+        T2[x] += fac * v;
+    }
+}
+
+__global__ void bcast_kernel(long long total, long long count,
+                             const double *__restrict__ src,
+                             double *__restrict__ dst) {
+    for (long long x = blockIdx.x * (long long)blockDim.x + threadIdx.x; x < total;
+         x += (long long)gridDim.x * blockDim.x)
+        dst[x] = src[x % count];
+}
+
+}  // namespace
+
+int kv_axpby4(kvft_ctx *ctx, int batch, const int dims[4], double alpha,
+              const double *src, const long long ss[4], long long sbst,
+              double beta, double *dst, const long long ds[4], long long dbst) {
+    Dims4 g;
+    long long total = batch;
+    for (int k = 0; k < 4; k++) {
+        g.d[k] = dims[k];
+        g.ss[k] = ss[k];
+        g.ds[k] = ds[k];
+        total *= dims[k];
+    }
+    g.sbst = sbst;
+    g.dbst = dbst;
+    if (total == 0) return KVFT_OK;
+    KvProfScope prof(ctx, KV_CAT_ELEM, 8.0 * total * (beta != 0.0 ? 3 : 2));
+    axpby4_kernel<<<grid_for(ctx, total, 256), 256, 0, ctx->stream>>>(total, g, alpha, src,
+                                                                      beta, dst);
+    return kv_launch_check(ctx, "axpby4");
+}
+
+int kv_make_tau(kvft_ctx *ctx, int batch, int nv, int no, const double *t1,
+                const double *t2, double c, double *out) {
+    long long total = (long long)batch * nv * nv * no * no;
+    if (total == 0) return KVFT_OK;
+    KvProfScope prof(ctx, KV_CAT_ELEM, 16.0 * total);
+    make_tau_kernel<<<grid_for(ctx, total, 256), 256, 0, ctx->stream>>>(total, nv, no, t1,
+                                                                        t2, c, out);
+    return kv_launch_check(ctx, "make_tau");
+}
+
+int kv_make_wmbej_tmp(kvft_ctx *ctx, int batch, int nv, int no,
+                      const double *t1, const double *t2, double *out) {
+    long long total = (long long)batch * nv * nv * no * no;
+    if (total == 0) return KVFT_OK;
+    KvProfScope prof(ctx, KV_CAT_ELEM, 16.0 * total);
+    wmbej_tmp_kernel<<<grid_for(ctx, total, 256), 256, 0, ctx->stream>>>(total, nv, no, t1,
+                                                                         t2, out);
+    return kv_launch_check(ctx, "wmbej_tmp");
+}
+
+int kv_assemble_t2(kvft_ctx *ctx, int batch, int nv, int no, double fac,
+                   const double *Zab, const double *Zij, const double *Zabij,
+                   double *T2) {
+    long long total = (long long)batch * nv * nv * no * no;
+    if (total == 0) return KVFT_OK;
+    KvProfScope prof(ctx, KV_CAT_ELEM, 8.0 * total * 5);
+    assemble_t2_kernel<<<grid_for(ctx, total, 256), 256, 0, ctx->stream>>>(
+        total, nv, no, fac, Zab, Zij, Zabij, T2);
+    return kv_launch_check(ctx, "assemble_t2");
+}
+
+int kv_bcast(kvft_ctx *ctx, int batch, size_t count, const double *src,
+             double *dst) {
+    long long total = (long long)batch * count;
+    if (total == 0) return KVFT_OK;
+    KvProfScope prof(ctx, KV_CAT_ELEM, 8.0 * total);
+    bcast_kernel<<<grid_for(ctx, total, 256), 256, 0, ctx->stream>>>(total, (long long)count,
+                                                                     src, dst);
+    return kv_launch_check(ctx, "bcast");
+}

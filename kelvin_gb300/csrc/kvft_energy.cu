@@ -1,0 +1,129 @@
+// FT-CC grand potential (kelvin/ft_cc_energy.py:7-32):
+//   Omega = (1/beta) [ sum_ai t1n[a,i] f[i,a] + sum_abij t2n[a,b,i,j] eri[i,j,a,b] ]
+//   t1n = sum_y g_y T1_y,  t2n = sum_y g_y (T2_y/4 + [Qterm] T1_y[a,i] T1_y[b,j]/2)
+// One pass over T2 (HBM-bound apart from GB300's slow FP64 FMAs); eri is read
+// through a shared-memory transpose so both streams stay coalesced.  Partial
+// sums are reduced in a fixed order, so the result is deterministic.
+#include "kvft_internal.h"
+
+namespace {
+
+constexpr int TILE = 32;
+
+__global__ void __launch_bounds__(256)
+energy2_kernel(int ng, int nv, int no, const double *__restrict__ T1,
+               const double *__restrict__ T2, const double *__restrict__ eri,
+               const double *__restrict__ g, int qterm, double *__restrict__ partial) {
+    __shared__ double E[TILE][TILE + 1];     // [ij][ab]
+    __shared__ double red[256];
+    const long long V2 = (long long)nv * nv, O2 = (long long)no * no;
+    const long long ab0 = (long long)blockIdx.y * TILE, ij0 = (long long)blockIdx.x * TILE;
+    const int t = threadIdx.x, tx = t % TILE, ty = t / TILE;   // ty in [0, 8)
+    for (int r = ty; r < TILE; r += 8) {
+        long long ij = ij0 + r, ab = ab0 + tx;
+        E[r][tx] = (ij < O2 && ab < V2) ? eri[ij * V2 + ab] : 0.0;
+    }
+    __syncthreads();
+    double acc = 0.0;
+    const long long ij = ij0 + tx;
+    if (ij < O2) {
+        const int i = (int)(ij / no), j = (int)(ij % no);
+        for (int r = ty; r < TILE; r += 8) {
+            const long long ab = ab0 + r;
+            if (ab >= V2) break;
+            const int a = (int)(ab / nv), b = (int)(ab % nv);
+            double s = 0.0;
+            for (int y = 0; y < ng; y++) {
+                double v = 0.25 * T2[((long long)y * V2 + ab) * O2 + ij];
+                if (qterm) {
+                    const double *u = T1 + (long long)y * nv * no;
+                    v = fma(0.5 * u[a * no + i], u[b * no + j], v);
+                }
+                s = fma(g[y], v, s);
+            }
+            acc = fma(s, E[tx][r], acc);
+        }
+    }
+    red[t] = acc;
+    __syncthreads();
+    for (int s = 128; s > 0; s >>= 1) {
+        if (t < s) red[t] += red[t + s];
+        __syncthreads();
+    }
+    if (t == 0) partial[blockIdx.y * gridDim.x + blockIdx.x] = red[0];
+}
+
+__global__ void energy1_kernel(int ng, int nv, int no, const double *__restrict__ T1,
+                               const double *__restrict__ f, const double *__restrict__ g,
+                               double *__restrict__ out) {
+    __shared__ double red[256];
+    double acc = 0.0;
+    for (int k = threadIdx.x; k < nv * no; k += 256) {
+        const int a = k / no, i = k % no;
+        double s = 0.0;
+        for (int y = 0; y < ng; y++) s = fma(g[y], T1[(long long)y * nv * no + k], s);
+        acc = fma(s, f[i * nv + a], acc);
+    }
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    for (int s = 128; s > 0; s >>= 1) {
+        if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *out = red[0];
+}
+
+__global__ void energy_final_kernel(const double *__restrict__ partial, int n,
+                                    const double *__restrict__ e1, double inv_beta,
+                                    double *__restrict__ res) {
+    __shared__ double red[256];
+    double acc = 0.0;
+    for (int k = threadIdx.x; k < n; k += 256) acc += partial[k];
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    for (int s = 128; s > 0; s >>= 1) {
+        if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *res = (e1[0] + red[0]) * inv_beta;
+}
+
+}  // namespace
+
+// Writes Omega to dres[0] (device).  Uses context scratch.
+int kv_energy(kvft_ctx *ctx, int ng, int nv, int no, const double *T1, const double *T2,
+              const double *f, const double *eri, const double *g, double beta, int qterm,
+              double *dres) {
+    const long long V2 = (long long)nv * nv, O2 = (long long)no * no;
+    dim3 grid((unsigned)((O2 + TILE - 1) / TILE), (unsigned)((V2 + TILE - 1) / TILE));
+    long long nblk = (long long)grid.x * grid.y;
+    void *part = nullptr;
+    KV_TRY(kv_scratch(ctx, "energy_partial", sizeof(double) * (nblk + 1), &part));
+    double *pp = (double *)part;
+    // algorithmic bytes: T2 (all tau points) + eri + T1
+    KvProfScope prof(ctx, KV_CAT_ENERGY,
+                     8.0 * ((double)ng * V2 * O2 + (double)V2 * O2 + (double)ng * nv * no));
+    energy2_kernel<<<grid, 256, 0, ctx->stream>>>(ng, nv, no, T1, T2, eri, g, qterm, pp);
+    KV_TRY(kv_launch_check(ctx, "energy2"));
+    energy1_kernel<<<1, 256, 0, ctx->stream>>>(ng, nv, no, T1, f, g, pp + nblk);
+    KV_TRY(kv_launch_check(ctx, "energy1"));
+    energy_final_kernel<<<1, 256, 0, ctx->stream>>>(pp, (int)nblk, pp + nblk, 1.0 / beta, dres);
+    return kv_launch_check(ctx, "energy_final");
+}
+
+extern "C" int kvft_ft_cc_energy(kvft_ctx *ctx, int ng, int nv, int no, const double *T1,
+                                 const double *T2, const double *f, const double *eri,
+                                 const double *g, double beta, int qterm,
+                                 double *omega_host) {
+    if (!ctx || ng < 1 || nv <= 0 || no <= 0 || !T1 || !T2 || !f || !eri || !g || !omega_host ||
+        beta == 0.0)
+        return kv_fail(ctx, KVFT_EINVAL, "ft_cc_energy: bad argument");
+    cudaSetDevice(ctx->device);
+    void *res = nullptr;
+    KV_TRY(kv_scratch(ctx, "energy_result", sizeof(double), &res));
+    KV_TRY(kv_energy(ctx, ng, nv, no, T1, T2, f, eri, g, beta, qterm, (double *)res));
+    KV_CHECK(ctx, cudaMemcpyAsync(omega_host, res, sizeof(double), cudaMemcpyDeviceToHost,
+                                  ctx->stream));
+    KV_CHECK(ctx, cudaStreamSynchronize(ctx->stream));
+    return KVFT_OK;
+}

@@ -1,0 +1,162 @@
+// FP64 (DFMA) strided, batched GEMM for the CCSD contractions.
+//
+// C[b](m,n) = alpha * sum_k A[b](m,k) B[b](k,n) + beta * C[b](m,n), where every
+// index is a composite of up to three tensor indices with their own strides
+// (KIdx), so permuted views of the n^4 amplitude/integral tensors are read in
+// place.  GB300 issues only ~2 FP64 FMAs per clock per SM, so the kernel keeps
+// every SM busy (split-K with FP64 atomics when the tile count is small) and
+// spends integer work freely on index decoding.
+#include "kvft_internal.h"
+
+namespace {
+
+constexpr int BM = 64, BN = 64, BK = 16, NT = 256;
+
+__global__ void __launch_bounds__(NT)
+gemm_f64_kernel(int M, int N, int K, int nsplit, int klen, double alpha,
+                KMat A, KMat B, double beta, KOut C, int atomic) {
+    __shared__ double As[BK][BM + 1];
+    __shared__ double Bs[BK][BN + 1];
+    const int tid = threadIdx.x;
+    const int bz = blockIdx.z;
+    const int batch = bz / nsplit;
+    const int ks = bz - batch * nsplit;
+    const int bm = blockIdx.y * BM;
+    const int bn = blockIdx.x * BN;
+    const int kbeg = ks * klen;
+    const int kend = min(K, kbeg + klen);
+
+    const double *Ap = A.p + (long long)batch * A.bst;
+    const double *Bp = B.p + (long long)batch * B.bst;
+
+    // load mapping: k fastest across threads when k is the contiguous index
+    const bool a_kfast = (A.c.st[2] == 1);
+    const bool b_kfast = (B.r.st[2] == 1);
+    int am[4], ak[4], bk[4], bnn[4];
+    long long aoff_m[4], boff_n[4];
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+        if (a_kfast) { ak[r] = tid % BK; am[r] = tid / BK + 16 * r; }
+        else { am[r] = tid % BM; ak[r] = tid / BM + 4 * r; }
+        if (b_kfast) { bk[r] = tid % BK; bnn[r] = tid / BK + 16 * r; }
+        else { bnn[r] = tid % BN; bk[r] = tid / BN + 4 * r; }
+        int m = bm + am[r];
+        int n = bn + bnn[r];
+        aoff_m[r] = (m < M) ? A.r.off(m) : -1;
+        boff_n[r] = (n < N) ? B.c.off(n) : -1;
+    }
+
+    const int tx = tid % 16, ty = tid / 16;
+    double acc[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; i++)
+#pragma unroll
+        for (int j = 0; j < 4; j++) acc[i][j] = 0.0;
+
+    for (int k0 = kbeg; k0 < kend; k0 += BK) {
+#pragma unroll
+        for (int r = 0; r < 4; r++) {
+            int k = k0 + ak[r];
+            double v = 0.0;
+            if (aoff_m[r] >= 0 && k < kend) v = Ap[aoff_m[r] + A.c.off(k)];
+            As[ak[r]][am[r]] = v;
+            k = k0 + bk[r];
+            v = 0.0;
+            if (boff_n[r] >= 0 && k < kend) v = Bp[boff_n[r] + B.r.off(k)];
+            Bs[bk[r]][bnn[r]] = v;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int kk = 0; kk < BK; kk++) {
+            double a[4], b[4];
+#pragma unroll
+            for (int i = 0; i < 4; i++) a[i] = As[kk][ty + 16 * i];
+#pragma unroll
+            for (int j = 0; j < 4; j++) b[j] = Bs[kk][tx + 16 * j];
+#pragma unroll
+            for (int i = 0; i < 4; i++)
+#pragma unroll
+                for (int j = 0; j < 4; j++) acc[i][j] = fma(a[i], b[j], acc[i][j]);
+        }
+        __syncthreads();
+    }
+
+    double *Cp = C.p + (long long)batch * C.bst;
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        int m = bm + ty + 16 * i;
+        if (m >= M) continue;
+        long long ro = C.r.off(m);
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            int n = bn + tx + 16 * j;
+            if (n >= N) continue;
+            double *dst = Cp + ro + C.c.off(n);
+            double v = alpha * acc[i][j];
+            if (atomic) atomicAdd(dst, v);
+            else *dst = (beta != 0.0) ? v + beta * (*dst) : v;
+        }
+    }
+}
+
+__global__ void scale_view_kernel(int M, int N, int batch, double beta, KOut C) {
+    long long total = (long long)M * N * batch;
+    for (long long x = blockIdx.x * (long long)blockDim.x + threadIdx.x; x < total;
+         x += (long long)gridDim.x * blockDim.x) {
+        int n = (int)(x % N);
+        long long r = x / N;
+        int m = (int)(r % M);
+        int b = (int)(r / M);
+        double *d = C.p + (long long)b * C.bst + C.r.off(m) + C.c.off(n);
+        *d = (beta == 0.0) ? 0.0 : beta * (*d);
+    }
+}
+
+}  // namespace
+
+int kv_gemm_f64(kvft_ctx *ctx, int M, int N, int K, int batch, double alpha,
+                const KMat &A, const KMat &B, double beta, const KOut &C) {
+    if (M <= 0 || N <= 0 || batch <= 0) return KVFT_OK;
+    if (K <= 0) {
+        if (beta == 1.0) return KVFT_OK;
+        int blocks = ctx->sm_count * 4;
+        scale_view_kernel<<<blocks, 256, 0, ctx->stream>>>(M, N, batch, beta, C);
+        return kv_launch_check(ctx, "scale_view");
+    }
+    long long tiles = (long long)((M + BM - 1) / BM) * ((N + BN - 1) / BN) * batch;
+    int nsplit = 1;
+    long long want = 2LL * ctx->sm_count;
+    if (tiles < want && K > 4 * BK) {
+        long long s = (want + tiles - 1) / tiles;
+        long long smax = (K + 4 * BK - 1) / (4 * BK);
+        nsplit = (int)std::min(s, smax);
+        while ((long long)batch * nsplit > 65535) nsplit--;
+        if (nsplit < 1) nsplit = 1;
+    }
+    int klen = (K + nsplit - 1) / nsplit;
+    klen = (klen + BK - 1) / BK * BK;
+    nsplit = (K + klen - 1) / klen;
+    int atomic = nsplit > 1;
+    if (atomic && beta != 1.0) {
+        int blocks = ctx->sm_count * 4;
+        scale_view_kernel<<<blocks, 256, 0, ctx->stream>>>(M, N, batch, beta, C);
+        KV_TRY(kv_launch_check(ctx, "scale_view"));
+    }
+    if ((long long)batch * nsplit > 65535)
+        return kv_fail(ctx, KVFT_EINVAL, "gemm batch too large");
+    dim3 grid((N + BN - 1) / BN, (M + BM - 1) / BM, batch * nsplit);
+    gemm_f64_kernel<<<grid, NT, 0, ctx->stream>>>(M, N, K, nsplit, klen, alpha, A, B,
+                                                   beta, C, atomic);
+    return kv_launch_check(ctx, "gemm_f64");
+}
+
+int kv_gemm(kvft_ctx *ctx, int M, int N, int K, int batch, double alpha,
+            const KMat &A, const KMat &B, double beta, const KOut &C) {
+    // n^6-class: every GEMM dimension is a pair of orbital indices or more
+    const long long mn = std::min(std::min(M, N), K), mx = std::max(std::max(M, N), K);
+    const int cat = (mn * mn > mx) ? KV_CAT_GEMM6 : KV_CAT_GEMM;
+    KvProfScope prof(ctx, cat, 2.0 * M * N * (double)K * batch);
+    if (ctx->precision == KVFT_PREC_FP64)
+        return kv_gemm_f64(ctx, M, N, K, batch, alpha, A, B, beta, C);
+    return kv_gemm_tc(ctx, M, N, K, batch, alpha, A, B, beta, C, ctx->digits);
+}

@@ -1,0 +1,159 @@
+// Internal definitions shared by the libkvft translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <algorithm>
+#include <stdint.h>
+#include <string>
+#include <vector>
+#include <map>
+
+#include "../../include/kvft.h"
+
+// ---------------------------------------------------------------------------
+// Strided views.  A contraction operand is a matrix whose row and column
+// indices are each a composite of up to three tensor indices, every one with
+// its own element stride, plus a stride between tau points (batch).  This is
+// how index permutations of the n^4 tensors enter the GEMMs without copies.
+// ---------------------------------------------------------------------------
+struct KIdx {
+    int size[3];        // slow -> fast; unused entries have size 1
+    long long st[3];    // element strides
+    __host__ __device__ int total() const { return size[0] * size[1] * size[2]; }
+    __host__ __device__ long long off(int x) const {
+        int i2 = x % size[2];
+        int r = x / size[2];
+        int i1 = r % size[1];
+        int i0 = r / size[1];
+        return (long long)i0 * st[0] + (long long)i1 * st[1] + (long long)i2 * st[2];
+    }
+};
+
+struct KMat {
+    const double *p;
+    KIdx r, c;
+    long long bst;      // stride between batch entries (0: shared operand)
+};
+
+struct KOut {
+    double *p;
+    KIdx r, c;
+    long long bst;
+};
+
+inline KIdx kidx1(int s0, long long t0) { return KIdx{{1, 1, s0}, {0, 0, t0}}; }
+inline KIdx kidx2(int s0, long long t0, int s1, long long t1) {
+    return KIdx{{1, s0, s1}, {0, t0, t1}};
+}
+inline KIdx kidx3(int s0, long long t0, int s1, long long t1, int s2, long long t2) {
+    return KIdx{{s0, s1, s2}, {t0, t1, t2}};
+}
+
+// ---------------------------------------------------------------------------
+// Context
+// ---------------------------------------------------------------------------
+struct kvft_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    int sm_count = 0;
+    int precision = KVFT_PREC_FP64;
+    int digits = 7;                  // digit levels for the tensor-core GEMM
+    std::string err;
+    cudaEvent_t ev[64] = {};
+    uint64_t launches = 0;
+    void *l2buf = nullptr;
+    // cached scratch buffers keyed by purpose
+    std::map<std::string, std::pair<void *, size_t>> scratch;
+    int *dflag = nullptr;            // device status word for bounded waits
+    struct KvProf *prof = nullptr;
+};
+
+// Live per-launch timing (enabled by kvft_profile_begin): event pairs around
+// launches of each category, with the algorithmic work they carry.
+enum KvCat { KV_CAT_GEMM6 = 0, KV_CAT_GEMM = 1, KV_CAT_QUAD = 2, KV_CAT_ENERGY = 3,
+             KV_CAT_ELEM = 4, KV_CAT_PACK = 5, KV_NCAT = 6 };
+struct KvProf {
+    bool on = false;
+    std::vector<cudaEvent_t> pool;
+    size_t used = 0;
+    struct Rec { int cat; size_t e0, e1; double work; };
+    std::vector<Rec> recs;
+};
+int kv_prof_mark(kvft_ctx *ctx, size_t *slot);            // record one event
+void kv_prof_add(kvft_ctx *ctx, int cat, size_t e0, size_t e1, double work);
+struct KvProfScope {                                      // RAII helper
+    kvft_ctx *ctx; int cat; double work; size_t e0; bool on;
+    KvProfScope(kvft_ctx *c, int k, double w);
+    ~KvProfScope();
+};
+
+// error helpers --------------------------------------------------------------
+int kv_fail(kvft_ctx *ctx, int code, const std::string &msg);
+int kv_cuda(kvft_ctx *ctx, cudaError_t e, const char *what);
+#define KV_CHECK(ctx, call)                                   \
+    do {                                                      \
+        cudaError_t _e = (call);                              \
+        if (_e != cudaSuccess) return kv_cuda(ctx, _e, #call); \
+    } while (0)
+#define KV_TRY(expr)                 \
+    do {                             \
+        int _s = (expr);             \
+        if (_s != KVFT_OK) return _s; \
+    } while (0)
+int kv_launch_check(kvft_ctx *ctx, const char *what);
+
+// scratch memory owned by the context (grows, never shrinks until destroy)
+int kv_scratch(kvft_ctx *ctx, const char *key, size_t bytes, void **p);
+
+// ---------------------------------------------------------------------------
+// Kernel launchers (each returns a kvft_status)
+// ---------------------------------------------------------------------------
+// C = alpha * A * B + beta * C, batched over `batch` tau points.
+int kv_gemm(kvft_ctx *ctx, int M, int N, int K, int batch, double alpha,
+            const KMat &A, const KMat &B, double beta, const KOut &C);
+int kv_gemm_f64(kvft_ctx *ctx, int M, int N, int K, int batch, double alpha,
+                const KMat &A, const KMat &B, double beta, const KOut &C);
+int kv_gemm_tc(kvft_ctx *ctx, int M, int N, int K, int batch, double alpha,
+               const KMat &A, const KMat &B, double beta, const KOut &C,
+               int digits);
+
+// 4-index strided axpby: dst = beta*dst + alpha*src over a [b][d0][d1][d2][d3]
+// index space; each side gives element strides for the 4 indices + batch.
+struct K4 {
+    int d[4];
+    long long s[4];
+    long long bst;
+};
+int kv_axpby4(kvft_ctx *ctx, int batch, const int dims[4], double alpha,
+              const double *src, const long long ss[4], long long sbst,
+              double beta, double *dst, const long long ds[4], long long dbst);
+
+// tau-type amplitudes: out = t2 + c * (t1[a,i] t1[b,j] - t1[b,i] t1[a,j])
+int kv_make_tau(kvft_ctx *ctx, int batch, int nv, int no, const double *t1,
+                const double *t2, double c, double *out);
+// tmp[f,b,j,n] = 0.5 t2[f,b,j,n] + t1[f,j] t1[b,n]
+int kv_make_wmbej_tmp(kvft_ctx *ctx, int batch, int nv, int no,
+                      const double *t1, const double *t2, double *out);
+// T2 += fac * [Zab - P(ab) Zab + Zij - P(ij) Zij + (1 - P(ab))(1 - P(ij)) Zabij]
+int kv_assemble_t2(kvft_ctx *ctx, int batch, int nv, int no, double fac,
+                   const double *Zab, const double *Zij, const double *Zabij,
+                   double *T2);
+// broadcast a tau-independent block over the batch: dst[b] = src
+int kv_bcast(kvft_ctx *ctx, int batch, size_t count, const double *src,
+             double *dst);
+
+int kv_int_tbar(kvft_ctx *ctx, int ng, size_t P, const double *tbar,
+                const double *ti, const double *D, const double *eps_v,
+                const double *eps_o, int nv, int no, int rank,
+                const double *G, int full, double *out);
+
+int kv_energy(kvft_ctx *ctx, int ng, int nv, int no, const double *T1,
+              const double *T2, const double *f, const double *eri,
+              const double *g, double beta, int qterm, double *dres);
+
+int kv_stanton(kvft_ctx *ctx, int nb, int nv, int no,
+               const double *const F[4], const double *const I[9],
+               const double *t1, const double *t2, double fac, double *T1,
+               double *T2);
+size_t kv_stanton_workspace(int nb, int nv, int no);

@@ -1,0 +1,379 @@
+// Exp-weighted cumulative tau integrals (kelvin/quadrature.py:292-317,
+// 348-369) and the fused "integrate + damp + norms" pass of the solver.
+//
+// For every amplitude element p with denominator d:
+//     T_y = sum_x G[y,x] w(y,x) tbar_x,
+//     w(y,x) = exp((ti[x]-ti[y]) d) for x < y (all x if `full`), else 1.
+// GB300 issues about two FP64 FMAs per clock per SM, so exp evaluations are
+// the cost to cut, not HBM bytes:
+//   * w(y,x) is built as a running product of step factors
+//     r_k = exp((ti[k]-ti[k+1]) d), one exp per grid step -- and a single exp
+//     when the grid is uniform (Kelvin's default 'lin' rule);
+//   * when G has the structure of Kelvin's Simpson/midpoint/left rules
+//     (G[y,x] == G[y-s,x] for x < y-s, zero above the diagonal), rows are
+//     chained: T_y = w(y,y-s) (T_{y-s} - G[y-s,y-s] tbar_{y-s})
+//                    + sum_{x=y-s}^{y} G[y,x] w(y,x) tbar_x,
+//     which is O(ng) per element instead of O(ng^2).
+// The product of <= ng correctly rounded factors differs from a direct exp
+// by at most ~ng ulp (relative), far inside the 1e-10 parity tolerance.
+#include "kvft_internal.h"
+
+#include <cmath>
+
+namespace {
+
+constexpr int QT = 128;      // threads per block
+constexpr int MAXNG = 64;
+
+struct QuadParams {
+    int ng;
+    long long P;             // elements per tau slice
+    int rank;                // 1: [nv][no], 2: [nv][nv][no][no]
+    int nv, no;
+    int step;                // recurrence step (0: general path)
+    int uniform;             // all ti[k+1]-ti[k] equal
+    int full;
+    double alpha;            // damping (fused update only)
+};
+
+__device__ __forceinline__ double denom(const QuadParams &q, long long p,
+                                        const double *D, const double *ev,
+                                        const double *eo) {
+    if (D) return D[p];
+    if (q.rank == 1) {
+        int i = (int)(p % q.no);
+        int a = (int)(p / q.no);
+        return ev[a] - eo[i];
+    }
+    long long r = p;
+    int j = (int)(r % q.no); r /= q.no;
+    int i = (int)(r % q.no); r /= q.no;
+    int b = (int)(r % q.nv);
+    int a = (int)(r / q.nv);
+    return ev[a] + ev[b] - eo[i] - eo[j];
+}
+
+// Shared memory: ti[ng], G[ng*ng], then per-thread columns r[ng][QT] and
+// tb[ng][QT] (general path).
+// MODE 0: out = T.  MODE 1 (fused solver update): Told = alpha Told + (1-alpha) T,
+// with block partial sums of |T - Told|^2 and |Told_new|^2.
+template <int MODE>
+__global__ void __launch_bounds__(QT)
+quad_kernel(QuadParams q, const double *__restrict__ tbar, const double *__restrict__ ti_g,
+            const double *__restrict__ G_g, const double *__restrict__ D,
+            const double *__restrict__ ev, const double *__restrict__ eo,
+            double *out, double *__restrict__ partial) {
+    extern __shared__ double sm[];
+    const int ng = q.ng;
+    double *ti = sm;
+    double *G = ti + ng;
+    double *rk = G + ng * ng;                 // [ng][QT]
+    double *tb = rk + ng * QT;                // [ng][QT]
+    for (int k = threadIdx.x; k < ng; k += QT) ti[k] = ti_g[k];
+    for (int k = threadIdx.x; k < ng * ng; k += QT) G[k] = G_g[k];
+    __syncthreads();
+
+    double s_diff = 0.0, s_norm = 0.0;
+    const int t = threadIdx.x;
+    for (long long p = blockIdx.x * (long long)QT + t; p < q.P;
+         p += (long long)gridDim.x * QT) {
+        const double d = denom(q, p, D, ev, eo);
+        // step factors r_k = exp((ti[k]-ti[k+1]) d)
+        double r0 = 1.0;
+        if (q.uniform) {
+            r0 = (ng > 1) ? exp((ti[0] - ti[1]) * d) : 1.0;
+        } else {
+            for (int k = 0; k + 1 < ng; k++) rk[k * QT + t] = exp((ti[k] - ti[k + 1]) * d);
+        }
+#define RK(k) (q.uniform ? r0 : rk[(k) * QT + t])
+        if (q.step > 0) {
+            // chained rows; keep the last `step` outputs and inputs in registers
+            double Tm1 = 0.0, Tm2 = 0.0, tbm1 = 0.0, tbm2 = 0.0;
+            for (int y = 0; y < ng; y++) {
+                const double tby = tbar[(long long)y * q.P + p];
+                double Ty;
+                if (y < q.step) {
+                    // direct: x in [0, y]
+                    Ty = G[y * ng + y] * tby;
+                    double w = 1.0;
+                    double tbx = tbm1;
+                    for (int x = y - 1; x >= 0; x--) {
+                        w *= RK(x);
+                        double v = (x == y - 1) ? tbm1 : tbm2;
+                        (void)tbx;
+                        Ty = fma(G[y * ng + x] * w, v, Ty);
+                    }
+                } else if (q.step == 1) {
+                    const double w1 = RK(y - 1);
+                    Ty = w1 * (Tm1 - G[(y - 1) * ng + (y - 1)] * tbm1) +
+                         G[y * ng + (y - 1)] * w1 * tbm1 + G[y * ng + y] * tby;
+                } else {  // step 2
+                    const double w1 = RK(y - 1);
+                    const double w2 = w1 * RK(y - 2);
+                    Ty = w2 * (Tm2 - G[(y - 2) * ng + (y - 2)] * tbm2) +
+                         G[y * ng + (y - 2)] * w2 * tbm2 + G[y * ng + (y - 1)] * w1 * tbm1 +
+                         G[y * ng + y] * tby;
+                }
+                if (MODE == 0) {
+                    out[(long long)y * q.P + p] = Ty;
+                } else {
+                    double *o = out + (long long)y * q.P + p;
+                    const double told = *o;
+                    const double df = Ty - told;
+                    s_diff = fma(df, df, s_diff);
+                    const double nt = q.alpha * told + (1.0 - q.alpha) * Ty;
+                    s_norm = fma(nt, nt, s_norm);
+                    *o = nt;
+                }
+                Tm2 = Tm1; Tm1 = Ty;
+                tbm2 = tbm1; tbm1 = tby;
+            }
+        } else {
+            for (int x = 0; x < ng; x++) tb[x * QT + t] = tbar[(long long)x * q.P + p];
+            for (int y = 0; y < ng; y++) {
+                double Ty = 0.0;
+                // x <= y: running product downward from x = y
+                double w = 1.0;
+                for (int x = y; x >= 0; x--) {
+                    if (x < y) w *= RK(x);
+                    const double gyx = G[y * ng + x];
+                    if (gyx != 0.0) Ty = fma(gyx * w, tb[x * QT + t], Ty);
+                }
+                // x > y: factor 1 (reference) or exp((ti[x]-ti[y]) d) (full)
+                double wu = 1.0;
+                for (int x = y + 1; x < ng; x++) {
+                    if (q.full) wu /= RK(x - 1);
+                    const double gyx = G[y * ng + x];
+                    if (gyx != 0.0) Ty = fma(gyx * wu, tb[x * QT + t], Ty);
+                }
+                if (MODE == 0) {
+                    out[(long long)y * q.P + p] = Ty;
+                } else {
+                    double *o = out + (long long)y * q.P + p;
+                    const double told = *o;
+                    const double df = Ty - told;
+                    s_diff = fma(df, df, s_diff);
+                    const double nt = q.alpha * told + (1.0 - q.alpha) * Ty;
+                    s_norm = fma(nt, nt, s_norm);
+                    *o = nt;
+                }
+            }
+        }
+#undef RK
+    }
+    if (MODE == 1) {
+        // block reduction of the two sums (fixed order: deterministic)
+        __shared__ double red[2][QT];
+        red[0][t] = s_diff;
+        red[1][t] = s_norm;
+        __syncthreads();
+        for (int s = QT / 2; s > 0; s >>= 1) {
+            if (t < s) {
+                red[0][t] += red[0][t + s];
+                red[1][t] += red[1][t + s];
+            }
+            __syncthreads();
+        }
+        if (t == 0) {
+            partial[2 * blockIdx.x] = red[0][0];
+            partial[2 * blockIdx.x + 1] = red[1][0];
+        }
+    }
+}
+
+// one grid point: out = sum_x G[ig,x] w(ig,x) tbar_x (quadrature.py:348-369)
+__global__ void quad_single_kernel(QuadParams q, int ig, const double *__restrict__ tbar,
+                                   const double *__restrict__ ti,
+                                   const double *__restrict__ G,
+                                   const double *__restrict__ D,
+                                   double *__restrict__ out) {
+    for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < q.P;
+         p += (long long)gridDim.x * blockDim.x) {
+        const double d = D[p];
+        double acc = 0.0;
+        for (int x = 0; x < q.ng; x++) {
+            const double g = G[ig * q.ng + x];
+            if (g == 0.0) continue;
+            const double dt = (x < ig) ? (ti[x] - ti[ig]) : 0.0;
+            acc = fma(g * exp(dt * d), tbar[(long long)x * q.P + p], acc);
+        }
+        out[p] = acc;
+    }
+}
+
+__global__ void reduce_pairs_kernel(const double *__restrict__ partial, int n,
+                                    double *__restrict__ res) {
+    __shared__ double red[2][256];
+    double a = 0.0, b = 0.0;
+    for (int k = threadIdx.x; k < n; k += 256) {
+        a += partial[2 * k];
+        b += partial[2 * k + 1];
+    }
+    red[0][threadIdx.x] = a;
+    red[1][threadIdx.x] = b;
+    __syncthreads();
+    for (int s = 128; s > 0; s >>= 1) {
+        if (threadIdx.x < s) {
+            red[0][threadIdx.x] += red[0][threadIdx.x + s];
+            red[1][threadIdx.x] += red[1][threadIdx.x + s];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        res[0] = red[0][0];
+        res[1] = red[1][0];
+    }
+}
+
+// Host-side analysis of the grid: recurrence step and uniform spacing.
+void analyse_grid(int ng, const double *ti, const double *G, int full, int *step,
+                  int *uniform) {
+    *uniform = 1;
+    for (int k = 1; k + 1 < ng; k++) {
+        double d0 = ti[1] - ti[0], dk = ti[k + 1] - ti[k];
+        if (std::fabs(dk - d0) > 1e-14 * std::max(std::fabs(d0), 1e-300)) *uniform = 0;
+    }
+    *step = 0;
+    if (full) return;
+    for (int y = 0; y < ng; y++)
+        for (int x = y + 1; x < ng; x++)
+            if (G[y * ng + x] != 0.0) return;   // not lower-triangular
+    for (int s = 1; s <= 2; s++) {
+        bool ok = true;
+        for (int y = s; y < ng && ok; y++)
+            for (int x = 0; x < y - s && ok; x++)
+                if (G[y * ng + x] != G[(y - s) * ng + x]) ok = false;
+        if (ok) { *step = s; return; }
+    }
+}
+
+size_t quad_smem(int ng) { return sizeof(double) * (ng + ng * ng + 2 * ng * QT); }
+
+}  // namespace
+
+// Shared launcher.  ti/G are DEVICE pointers; hti/hG are host copies used for
+// the grid analysis.  MODE 1 requires `partial` (2 doubles per block) and
+// `res` (2 doubles) device buffers.
+int kv_quad_launch(kvft_ctx *ctx, int mode, int ng, long long P, int rank, int nv,
+                   int no, const double *tbar, const double *ti, const double *hti,
+                   const double *G, const double *hG, const double *D,
+                   const double *ev, const double *eo, int full, double alpha,
+                   double *out, double *res) {
+    if (ng < 1 || ng > MAXNG) return kv_fail(ctx, KVFT_EINVAL, "ng must be in [1, 64]");
+    if (P == 0) return KVFT_OK;
+    QuadParams q;
+    q.ng = ng;
+    q.P = P;
+    q.rank = rank;
+    q.nv = nv;
+    q.no = no;
+    q.full = full;
+    q.alpha = alpha;
+    analyse_grid(ng, hti, hG, full, &q.step, &q.uniform);
+    size_t smem = quad_smem(ng);
+    long long blocks = (P + QT - 1) / QT;
+    long long cap = (long long)ctx->sm_count * 8;
+    int grid = (int)std::min(blocks, cap);
+    static bool attr_done[2] = {false, false};
+    if (!attr_done[mode]) {
+        if (mode == 0)
+            cudaFuncSetAttribute(quad_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)quad_smem(MAXNG));
+        else
+            cudaFuncSetAttribute(quad_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)quad_smem(MAXNG));
+        attr_done[mode] = true;
+    }
+    // algorithmic bytes: tbar in, T out (mode 0); tbar + T_old in, T_old out (mode 1)
+    KvProfScope prof(ctx, KV_CAT_QUAD, 8.0 * ng * (double)P * (mode == 0 ? 2 : 3));
+    if (mode == 0) {
+        quad_kernel<0><<<grid, QT, smem, ctx->stream>>>(q, tbar, ti, G, D, ev, eo, out, nullptr);
+        return kv_launch_check(ctx, "quad_kernel");
+    }
+    void *part = nullptr;
+    KV_TRY(kv_scratch(ctx, "quad_partial", sizeof(double) * 2 * grid, &part));
+    quad_kernel<1><<<grid, QT, smem, ctx->stream>>>(q, tbar, ti, G, D, ev, eo, out,
+                                                    (double *)part);
+    KV_TRY(kv_launch_check(ctx, "quad_update_kernel"));
+    reduce_pairs_kernel<<<1, 256, 0, ctx->stream>>>((const double *)part, grid, res);
+    return kv_launch_check(ctx, "reduce_pairs");
+}
+
+namespace {
+
+int int_tbar_entry(kvft_ctx *ctx, int rank, int ng, int nv, int no, const double *tbar,
+                   const double *ti, const double *D, const double *G, int full,
+                   double *out) {
+    if (!ctx || ng < 1 || ng > MAXNG || nv <= 0 || no <= 0 || !tbar || !ti || !D || !G || !out)
+        return kv_fail(ctx, KVFT_EINVAL, "int_tbar: bad argument (ng must be 1..64)");
+    if (tbar == out) return kv_fail(ctx, KVFT_EINVAL, "int_tbar: output must not alias input");
+    cudaSetDevice(ctx->device);
+    std::vector<double> hti(ng), hG((size_t)ng * ng);
+    KV_CHECK(ctx, cudaMemcpyAsync(hti.data(), ti, sizeof(double) * ng, cudaMemcpyDeviceToHost,
+                                  ctx->stream));
+    KV_CHECK(ctx, cudaMemcpyAsync(hG.data(), G, sizeof(double) * ng * ng,
+                                  cudaMemcpyDeviceToHost, ctx->stream));
+    KV_CHECK(ctx, cudaStreamSynchronize(ctx->stream));
+    long long P = (long long)nv * no * (rank == 2 ? (long long)nv * no : 1LL);
+    return kv_quad_launch(ctx, 0, ng, P, rank, nv, no, tbar, ti, hti.data(), G, hG.data(), D,
+                          nullptr, nullptr, full, 0.0, out, nullptr);
+}
+
+int int_tbar_single_entry(kvft_ctx *ctx, int rank, int ng, int ig, int nv, int no,
+                          const double *tbar, const double *ti, const double *D,
+                          const double *G, double *out) {
+    if (!ctx || ng < 1 || ig < 0 || ig >= ng || nv <= 0 || no <= 0 || !tbar || !ti || !D ||
+        !G || !out)
+        return kv_fail(ctx, KVFT_EINVAL, "int_tbar_single: bad argument");
+    cudaSetDevice(ctx->device);
+    QuadParams q{};
+    q.ng = ng;
+    q.P = (long long)nv * no * (rank == 2 ? (long long)nv * no : 1LL);
+    long long blocks = (q.P + 255) / 256;
+    int grid = (int)std::min(blocks, (long long)ctx->sm_count * 8);
+    quad_single_kernel<<<grid, 256, 0, ctx->stream>>>(q, ig, tbar, ti, G, D, out);
+    return kv_launch_check(ctx, "quad_single");
+}
+
+}  // namespace
+
+int kv_int_tbar(kvft_ctx *ctx, int ng, size_t P, const double *tbar, const double *ti,
+                const double *D, const double *eps_v, const double *eps_o, int nv, int no,
+                int rank, const double *G, int full, double *out) {
+    std::vector<double> hti(ng), hG((size_t)ng * ng);
+    KV_CHECK(ctx, cudaMemcpyAsync(hti.data(), ti, sizeof(double) * ng, cudaMemcpyDeviceToHost,
+                                  ctx->stream));
+    KV_CHECK(ctx, cudaMemcpyAsync(hG.data(), G, sizeof(double) * ng * ng,
+                                  cudaMemcpyDeviceToHost, ctx->stream));
+    KV_CHECK(ctx, cudaStreamSynchronize(ctx->stream));
+    return kv_quad_launch(ctx, 0, ng, (long long)P, rank, nv, no, tbar, ti, hti.data(), G,
+                          hG.data(), D, eps_v, eps_o, full, 0.0, out, nullptr);
+}
+
+extern "C" {
+
+int kvft_int_tbar1(kvft_ctx *ctx, int ng, int nv, int no, const double *t1bar,
+                   const double *ti, const double *D1, const double *G, int full,
+                   double *t1out) {
+    return int_tbar_entry(ctx, 1, ng, nv, no, t1bar, ti, D1, G, full, t1out);
+}
+
+int kvft_int_tbar2(kvft_ctx *ctx, int ng, int nv, int no, const double *t2bar,
+                   const double *ti, const double *D2, const double *G, int full,
+                   double *t2out) {
+    return int_tbar_entry(ctx, 2, ng, nv, no, t2bar, ti, D2, G, full, t2out);
+}
+
+int kvft_int_tbar1_single(kvft_ctx *ctx, int ng, int ig, int nv, int no,
+                          const double *t1bar, const double *ti, const double *D1,
+                          const double *G, double *t1out) {
+    return int_tbar_single_entry(ctx, 1, ng, ig, nv, no, t1bar, ti, D1, G, t1out);
+}
+
+int kvft_int_tbar2_single(kvft_ctx *ctx, int ng, int ig, int nv, int no,
+                          const double *t2bar, const double *ti, const double *D2,
+                          const double *G, double *t2out) {
+    return int_tbar_single_entry(ctx, 2, ng, ig, nv, no, t2bar, ti, D2, G, t2out);
+}
+
+}  // extern "C"

@@ -1,0 +1,534 @@
+// Device-resident FT-CCSD solve: Fermi-scaled integrals (kelvin/cc_utils.py:
+// 569-602), the damped amplitude iteration (kelvin/cc_utils.py:111-173) and
+// the one-call CCSD update (kelvin/ft_cc_equations.py:96-113).
+//
+// HBM layout of a solver (nv virtual / no occupied indices, ng tau points;
+// for a system built from orbital energies nv = no = n), all FP64:
+//   F blocks oo/ov/vo/vv; nine I blocks; eps[n] or explicit D1/D2
+//   T1[ng][nv][no], T2[ng][nv][nv][no][no]   damped amplitudes (Kelvin's T_old)
+//   T1b, T2b (same shapes)                   tbar = -F.vo - R1, -I.vvoo - R2
+//   Stanton workspace for a chunk of tau points (context scratch).
+// The fused quadrature pass integrates tbar and damps T in place, so the
+// undamped T never touches HBM.
+#include "kvft_internal.h"
+
+#include <cmath>
+#include <cstdio>
+#include <vector>
+
+int kv_quad_launch(kvft_ctx *ctx, int mode, int ng, long long P, int rank, int nv, int no,
+                   const double *tbar, const double *ti, const double *hti, const double *G,
+                   const double *hG, const double *D, const double *ev, const double *eo,
+                   int full, double alpha, double *out, double *res);
+
+namespace {
+
+__device__ __forceinline__ void fermi_sqrt(double beta, double e, double mu, double *so,
+                                           double *sv) {
+    const double x = beta * (e - mu);
+    const double ex = exp(-fabs(x));
+    const double f = (x > 0) ? ex / (1.0 + ex) : 1.0 / (1.0 + ex);      // occupation
+    const double fv = (x > 0) ? 1.0 / (1.0 + ex) : ex / (1.0 + ex);     // vacancy
+    *so = sqrt(f);
+    *sv = sqrt(fv);
+}
+
+__global__ void fermi_kernel(int n, double beta, double mu, const double *__restrict__ eps,
+                             double *__restrict__ sfo, double *__restrict__ sfv) {
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x)
+        fermi_sqrt(beta, eps[p], mu, &sfo[p], &sfv[p]);
+}
+
+// F_xy[p,q] = (fock - diag eps)[p,q] s_x[p] s_y[q], s_o = sqrt(f), s_v = sqrt(1-f)
+__global__ void scale_fock_kernel(int n, const double *__restrict__ fock,
+                                  const double *__restrict__ eps,
+                                  const double *__restrict__ sfo,
+                                  const double *__restrict__ sfv, double *oo, double *ov,
+                                  double *vo, double *vv) {
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n * n; k += gridDim.x * blockDim.x) {
+        const int p = k / n, q = k % n;
+        const double f = fock[k] - (p == q ? eps[p] : 0.0);
+        oo[k] = f * sfo[p] * sfo[q];
+        ov[k] = f * sfo[p] * sfv[q];
+        vo[k] = f * sfv[p] * sfo[q];
+        vv[k] = f * sfv[p] * sfv[q];
+    }
+}
+
+struct Blk9 {
+    double *p[9];
+};
+
+// I_wxyz[p,q,r,s] = eri[p,q,r,s] s_w[p] s_x[q] s_y[r] s_z[s]; one read of eri,
+// nine writes, block order vvvv vvvo vovv vvoo vovo oovv vooo ooov oooo
+__global__ void scale_eri_kernel(int n, const double *__restrict__ eri,
+                                 const double *__restrict__ sfo,
+                                 const double *__restrict__ sfv, Blk9 out) {
+    const long long n4 = (long long)n * n * n * n;
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n4;
+         k += (long long)gridDim.x * blockDim.x) {
+        long long r = k;
+        const int s = (int)(r % n); r /= n;
+        const int q2 = (int)(r % n); r /= n;
+        const int q = (int)(r % n);
+        const int p = (int)(r / n);
+        const double e = eri[k];
+        const double op = sfo[p], vp = sfv[p], oq = sfo[q], vq = sfv[q];
+        const double orr = sfo[q2], vr = sfv[q2], os = sfo[s], vs = sfv[s];
+        out.p[0][k] = e * vp * vq * vr * vs;
+        out.p[1][k] = e * vp * vq * vr * os;
+        out.p[2][k] = e * vp * oq * vr * vs;
+        out.p[3][k] = e * vp * vq * orr * os;
+        out.p[4][k] = e * vp * oq * vr * os;
+        out.p[5][k] = e * op * oq * vr * vs;
+        out.p[6][k] = e * vp * oq * orr * os;
+        out.p[7][k] = e * op * oq * orr * vs;
+        out.p[8][k] = e * op * oq * orr * os;
+    }
+}
+
+__global__ void sumsq_kernel(long long n, const double *__restrict__ x, double *__restrict__ part) {
+    __shared__ double red[256];
+    double a = 0.0;
+    for (long long k = blockIdx.x * 256LL + threadIdx.x; k < n; k += (long long)gridDim.x * 256)
+        a = fma(x[k], x[k], a);
+    red[threadIdx.x] = a;
+    __syncthreads();
+    for (int s = 128; s > 0; s >>= 1) {
+        if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) part[blockIdx.x] = red[0];
+}
+
+__global__ void sum_kernel(const double *__restrict__ part, int n, double *__restrict__ out) {
+    __shared__ double red[256];
+    double a = 0.0;
+    for (int k = threadIdx.x; k < n; k += 256) a += part[k];
+    red[threadIdx.x] = a;
+    __syncthreads();
+    for (int s = 128; s > 0; s >>= 1) {
+        if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *out = red[0];
+}
+
+int sumsq(kvft_ctx *ctx, long long n, const double *x, double *dout) {
+    int grid = (int)std::max(1LL, std::min((long long)ctx->sm_count * 4, (n + 255) / 256));
+    void *part = nullptr;
+    KV_TRY(kv_scratch(ctx, "sumsq_partial", sizeof(double) * grid, &part));
+    sumsq_kernel<<<grid, 256, 0, ctx->stream>>>(n, x, (double *)part);
+    KV_TRY(kv_launch_check(ctx, "sumsq"));
+    sum_kernel<<<1, 256, 0, ctx->stream>>>((double *)part, grid, dout);
+    return kv_launch_check(ctx, "sum");
+}
+
+// tbar seed: dst[b] = -blk for every tau point b
+int seed_neg(kvft_ctx *ctx, int nb, long long count, const double *blk, double *dst) {
+    int d[4] = {1, 1, 1, (int)count};
+    long long ss[4] = {0, 0, 0, 1}, ds[4] = {0, 0, 0, 1};
+    return kv_axpby4(ctx, nb, d, -1.0, blk, ss, 0, 0.0, dst, ds, count);
+}
+
+}  // namespace
+
+struct kvft_solver {
+    kvft_ctx *ctx = nullptr;
+    int nv = 0, no = 0, ng = 0, chunk = 1;
+    double beta = 0, mu = 0;
+    double *eps = nullptr, *sfo = nullptr, *sfv = nullptr;   // orbital-energy form
+    double *D1 = nullptr, *D2 = nullptr;                     // explicit-denominator form
+    double *F[4] = {};
+    double *I[9] = {};
+    double *ti = nullptr, *g = nullptr, *G = nullptr;
+    std::vector<double> hti, hg, hG;
+    double *T1 = nullptr, *T2 = nullptr, *T1b = nullptr, *T2b = nullptr;
+    double *dsc = nullptr;      // device scalars
+    std::vector<void *> allocs;
+    double nl1 = 0.1, nl2 = 0.1;
+    bool norms_valid = false;
+    long long s1() const { return (long long)nv * no; }
+    long long s2() const { return s1() * s1(); }
+};
+
+namespace {
+
+int salloc(kvft_solver *s, size_t bytes, double **p) {
+    void *q = nullptr;
+    KV_CHECK(s->ctx, cudaMalloc(&q, bytes ? bytes : 16));
+    s->allocs.push_back(q);
+    *p = (double *)q;
+    return KVFT_OK;
+}
+
+int alloc_common(kvft_solver *s) {
+    const size_t n1 = s->s1(), n2 = s->s2();
+    const size_t no = s->no, nv = s->nv;
+    const size_t bsz[4] = {no * no, no * nv, nv * no, nv * nv};
+    for (int k = 0; k < 4; k++) KV_TRY(salloc(s, sizeof(double) * bsz[k], &s->F[k]));
+    // vvvv vvvo vovv vvoo vovo oovv vooo ooov oooo
+    const size_t isz[9] = {nv * nv * nv * nv, nv * nv * nv * no, nv * no * nv * nv,
+                           nv * nv * no * no, nv * no * nv * no, no * no * nv * nv,
+                           nv * no * no * no, no * no * no * nv, no * no * no * no};
+    for (int k = 0; k < 9; k++) KV_TRY(salloc(s, sizeof(double) * isz[k], &s->I[k]));
+    KV_TRY(salloc(s, sizeof(double) * s->ng, &s->ti));
+    KV_TRY(salloc(s, sizeof(double) * s->ng, &s->g));
+    KV_TRY(salloc(s, sizeof(double) * s->ng * s->ng, &s->G));
+    KV_TRY(salloc(s, sizeof(double) * s->ng * n1, &s->T1));
+    KV_TRY(salloc(s, sizeof(double) * s->ng * n2, &s->T2));
+    KV_TRY(salloc(s, sizeof(double) * s->ng * n1, &s->T1b));
+    KV_TRY(salloc(s, sizeof(double) * s->ng * n2, &s->T2b));
+    KV_TRY(salloc(s, sizeof(double) * 16, &s->dsc));
+    return KVFT_OK;
+}
+
+int upload_grid(kvft_solver *s, const double *ti, const double *g, const double *G) {
+    const int ng = s->ng;
+    s->hti.assign(ti, ti + ng);
+    s->hg.assign(g, g + ng);
+    s->hG.assign(G, G + (size_t)ng * ng);
+    cudaStream_t str = s->ctx->stream;
+    KV_CHECK(s->ctx, cudaMemcpyAsync(s->ti, ti, sizeof(double) * ng, cudaMemcpyHostToDevice, str));
+    KV_CHECK(s->ctx, cudaMemcpyAsync(s->g, g, sizeof(double) * ng, cudaMemcpyHostToDevice, str));
+    KV_CHECK(s->ctx, cudaMemcpyAsync(s->G, G, sizeof(double) * ng * ng, cudaMemcpyHostToDevice,
+                                     str));
+    KV_CHECK(s->ctx, cudaMemsetAsync(s->T1, 0, sizeof(double) * ng * s->s1(), str));
+    KV_CHECK(s->ctx, cudaMemsetAsync(s->T2, 0, sizeof(double) * ng * s->s2(), str));
+    return KVFT_OK;
+}
+
+int pick_chunk(kvft_solver *s) {
+    size_t fr = 0, tot = 0;
+    KV_CHECK(s->ctx, cudaMemGetInfo(&fr, &tot));
+    size_t per = kv_stanton_workspace(1, s->nv, s->no);
+    size_t budget = (size_t)(0.6 * (double)fr);
+    long long c = per ? (long long)(budget / per) : s->ng;
+    s->chunk = (int)std::max(1LL, std::min((long long)s->ng, c));
+    return KVFT_OK;
+}
+
+// tbar = -F.vo - R1, -I.vvoo - R2 for all tau points
+int form_tbar(kvft_solver *s) {
+    kvft_ctx *ctx = s->ctx;
+    const long long n1 = s->s1(), n2 = s->s2();
+    KV_TRY(seed_neg(ctx, s->ng, n1, s->F[2], s->T1b));
+    KV_TRY(seed_neg(ctx, s->ng, n2, s->I[3], s->T2b));
+    const double *Fc[4] = {s->F[0], s->F[1], s->F[2], s->F[3]};
+    const double *Ic[9];
+    for (int k = 0; k < 9; k++) Ic[k] = s->I[k];
+    for (int y0 = 0; y0 < s->ng; y0 += s->chunk) {
+        int nb = std::min(s->chunk, s->ng - y0);
+        KV_TRY(kv_stanton(ctx, nb, s->nv, s->no, Fc, Ic, s->T1 + y0 * n1, s->T2 + y0 * n2, -1.0,
+                          s->T1b + y0 * n1, s->T2b + y0 * n2));
+    }
+    return KVFT_OK;
+}
+
+int integrate(kvft_solver *s, int mode, double damp, const double *t1b, const double *t2b,
+              double *o1, double *o2, double *r1, double *r2) {
+    KV_TRY(kv_quad_launch(s->ctx, mode, s->ng, s->s1(), 1, s->nv, s->no, t1b, s->ti,
+                          s->hti.data(), s->G, s->hG.data(), s->D1, s->eps, s->eps, 0, damp, o1,
+                          r1));
+    return kv_quad_launch(s->ctx, mode, s->ng, s->s2(), 2, s->nv, s->no, t2b, s->ti,
+                          s->hti.data(), s->G, s->hG.data(), s->D2, s->eps, s->eps, 0, damp, o2,
+                          r2);
+}
+
+int read_scalars(kvft_solver *s, int count, double *h) {
+    KV_CHECK(s->ctx, cudaMemcpyAsync(h, s->dsc, sizeof(double) * count, cudaMemcpyDeviceToHost,
+                                     s->ctx->stream));
+    KV_CHECK(s->ctx, cudaStreamSynchronize(s->ctx->stream));
+    return KVFT_OK;
+}
+
+int refresh_norms(kvft_solver *s) {
+    KV_TRY(sumsq(s->ctx, s->ng * s->s1(), s->T1, s->dsc + 8));
+    KV_TRY(sumsq(s->ctx, s->ng * s->s2(), s->T2, s->dsc + 9));
+    double h[10];
+    KV_TRY(read_scalars(s, 10, h));
+    s->nl1 = std::sqrt(h[8]) + 0.1;
+    s->nl2 = std::sqrt(h[9]) + 0.1;
+    s->norms_valid = true;
+    return KVFT_OK;
+}
+
+int finish_create(kvft_solver *s, kvft_solver **out) {
+    if (cudaStreamSynchronize(s->ctx->stream) != cudaSuccess)
+        return kv_fail(s->ctx, KVFT_EDEVICE, "solver set-up kernels failed");
+    KV_TRY(pick_chunk(s));
+    *out = s;
+    return KVFT_OK;
+}
+
+void destroy(kvft_solver *s) {
+    for (void *p : s->allocs) cudaFree(p);
+    delete s;
+}
+
+}  // namespace
+
+extern "C" {
+
+size_t kvft_solver_footprint(int n, int ng, int precision) {
+    (void)precision;
+    size_t n2 = (size_t)n * n, n4 = n2 * n2;
+    size_t fixed = sizeof(double) * (9 * n4 + 4 * n2 + 3 * n + 2 * (size_t)ng * (n2 + n4) + n4);
+    return fixed + kv_stanton_workspace(1, n, n);
+}
+
+int kvft_solver_create(kvft_ctx *ctx, int n, int ng, const double *eps, const double *fock,
+                       const double *eri, double beta, double mu, const double *ti,
+                       const double *g, const double *G, kvft_solver **out) {
+    if (!ctx || !out || n <= 0 || ng < 1 || ng > 64 || !eps || !fock || !eri || !ti || !g ||
+        !G || !(beta > 0.0))
+        return kv_fail(ctx, KVFT_EINVAL, "solver_create: bad argument");
+    cudaSetDevice(ctx->device);
+    *out = nullptr;
+    kvft_solver *s = new kvft_solver();
+    s->ctx = ctx;
+    s->nv = s->no = n;
+    s->ng = ng;
+    s->beta = beta;
+    s->mu = mu;
+    const size_t n2 = (size_t)n * n, n4 = n2 * n2;
+    double *dfock = nullptr, *deri = nullptr;
+    int st = alloc_common(s);
+    if (st == KVFT_OK) st = salloc(s, sizeof(double) * n, &s->eps);
+    if (st == KVFT_OK) st = salloc(s, sizeof(double) * n, &s->sfo);
+    if (st == KVFT_OK) st = salloc(s, sizeof(double) * n, &s->sfv);
+    if (st == KVFT_OK) st = upload_grid(s, ti, g, G);
+    if (st == KVFT_OK && (cudaMalloc(&dfock, sizeof(double) * n2) != cudaSuccess ||
+                          cudaMalloc(&deri, sizeof(double) * n4) != cudaSuccess))
+        st = kv_fail(ctx, KVFT_ENOMEM, "solver_create: no room for the raw integrals");
+    if (st == KVFT_OK) {
+        cudaStream_t str = ctx->stream;
+        if (cudaMemcpyAsync(s->eps, eps, sizeof(double) * n, cudaMemcpyHostToDevice, str) ||
+            cudaMemcpyAsync(dfock, fock, sizeof(double) * n2, cudaMemcpyHostToDevice, str) ||
+            cudaMemcpyAsync(deri, eri, sizeof(double) * n4, cudaMemcpyHostToDevice, str))
+            st = kv_fail(ctx, KVFT_EDEVICE, "solver_create: upload failed");
+    }
+    if (st == KVFT_OK) {
+        cudaStream_t str = ctx->stream;
+        fermi_kernel<<<1, 256, 0, str>>>(n, beta, mu, s->eps, s->sfo, s->sfv);
+        st = kv_launch_check(ctx, "fermi");
+        if (st == KVFT_OK) {
+            int gb = (int)std::max<size_t>(1, std::min<size_t>((n2 + 255) / 256, 1024));
+            scale_fock_kernel<<<gb, 256, 0, str>>>(n, dfock, s->eps, s->sfo, s->sfv, s->F[0],
+                                                   s->F[1], s->F[2], s->F[3]);
+            st = kv_launch_check(ctx, "scale_fock");
+        }
+        if (st == KVFT_OK) {
+            Blk9 b;
+            for (int k = 0; k < 9; k++) b.p[k] = s->I[k];
+            scale_eri_kernel<<<ctx->sm_count * 8, 256, 0, str>>>(n, deri, s->sfo, s->sfv, b);
+            st = kv_launch_check(ctx, "scale_eri");
+        }
+    }
+    if (st == KVFT_OK) st = finish_create(s, out);
+    cudaStreamSynchronize(ctx->stream);
+    if (dfock) cudaFree(dfock);
+    if (deri) cudaFree(deri);
+    if (st != KVFT_OK) destroy(s);
+    return st;
+}
+
+// Solver over given blocks (host pointers) and explicit denominators, for
+// Kelvin's cc_utils.ft_cc_iter signature: F[4], I[9] in the kvft.h order,
+// D1[nv][no], D2[nv][nv][no][no].
+int kvft_solver_create_blocks(kvft_ctx *ctx, int nv, int no, int ng, const double *const F[4],
+                              const double *const I[9], const double *D1, const double *D2,
+                              double beta, const double *ti, const double *g, const double *G,
+                              kvft_solver **out) {
+    if (!ctx || !out || nv <= 0 || no <= 0 || ng < 1 || ng > 64 || !F || !I || !D1 || !D2 ||
+        !ti || !g || !G || beta == 0.0)
+        return kv_fail(ctx, KVFT_EINVAL, "solver_create_blocks: bad argument");
+    cudaSetDevice(ctx->device);
+    *out = nullptr;
+    kvft_solver *s = new kvft_solver();
+    s->ctx = ctx;
+    s->nv = nv;
+    s->no = no;
+    s->ng = ng;
+    s->beta = beta;
+    const size_t n1 = s->s1(), n2 = s->s2();
+    int st = alloc_common(s);
+    if (st == KVFT_OK) st = salloc(s, sizeof(double) * n1, &s->D1);
+    if (st == KVFT_OK) st = salloc(s, sizeof(double) * n2, &s->D2);
+    if (st == KVFT_OK) st = upload_grid(s, ti, g, G);
+    if (st == KVFT_OK) {
+        const size_t sv = nv, so = no;
+        const size_t bsz[4] = {so * so, so * sv, sv * so, sv * sv};
+        const size_t isz[9] = {sv * sv * sv * sv, sv * sv * sv * so, sv * so * sv * sv,
+                               sv * sv * so * so, sv * so * sv * so, so * so * sv * sv,
+                               sv * so * so * so, so * so * so * sv, so * so * so * so};
+        cudaStream_t str = ctx->stream;
+        for (int k = 0; k < 4 && st == KVFT_OK; k++)
+            if (!F[k] || cudaMemcpyAsync(s->F[k], F[k], sizeof(double) * bsz[k],
+                                         cudaMemcpyHostToDevice, str))
+                st = kv_fail(ctx, KVFT_EINVAL, "solver_create_blocks: F upload");
+        for (int k = 0; k < 9 && st == KVFT_OK; k++)
+            if (!I[k] || cudaMemcpyAsync(s->I[k], I[k], sizeof(double) * isz[k],
+                                         cudaMemcpyHostToDevice, str))
+                st = kv_fail(ctx, KVFT_EINVAL, "solver_create_blocks: I upload");
+        if (st == KVFT_OK &&
+            (cudaMemcpyAsync(s->D1, D1, sizeof(double) * n1, cudaMemcpyHostToDevice, str) ||
+             cudaMemcpyAsync(s->D2, D2, sizeof(double) * n2, cudaMemcpyHostToDevice, str)))
+            st = kv_fail(ctx, KVFT_EDEVICE, "solver_create_blocks: D upload");
+    }
+    if (st == KVFT_OK) st = finish_create(s, out);
+    if (st != KVFT_OK) destroy(s);
+    return st;
+}
+
+int kvft_solver_destroy(kvft_solver *s) {
+    if (!s) return KVFT_OK;
+    cudaSetDevice(s->ctx->device);
+    cudaStreamSynchronize(s->ctx->stream);
+    destroy(s);
+    return KVFT_OK;
+}
+
+int kvft_solver_step(kvft_solver *s, double damp, double *energy, double *res) {
+    if (!s) return KVFT_EINVAL;
+    kvft_ctx *ctx = s->ctx;
+    cudaSetDevice(ctx->device);
+    if (!s->norms_valid) KV_TRY(refresh_norms(s));
+    KV_TRY(form_tbar(s));
+    // integrate + damp in place: T <- damp T + (1-damp) int(tbar)
+    KV_TRY(integrate(s, 1, damp, s->T1b, s->T2b, s->T1, s->T2, s->dsc + 0, s->dsc + 2));
+    KV_TRY(kv_energy(ctx, s->ng, s->nv, s->no, s->T1, s->T2, s->F[1], s->I[5], s->g, s->beta, 1,
+                     s->dsc + 4));
+    double h[5];
+    KV_TRY(read_scalars(s, 5, h));
+    const double res1 = std::sqrt(h[0]) / s->nl1;
+    const double res2 = std::sqrt(h[2]) / s->nl2;
+    s->nl1 = std::sqrt(h[1]) + 0.1;
+    s->nl2 = std::sqrt(h[3]) + 0.1;
+    if (energy) *energy = h[4];
+    if (res) *res = res1 + res2;
+    if (!std::isfinite(h[4]) || !std::isfinite(res1 + res2))
+        return kv_fail(ctx, KVFT_EDIVERGE, "non-finite energy or residual");
+    return KVFT_OK;
+}
+
+int kvft_solver_run(kvft_solver *s, const kvft_solve_opts *o, kvft_result *r) {
+    if (!s || !o || !r) return KVFT_EINVAL;
+    kvft_ctx *ctx = s->ctx;
+    cudaSetDevice(ctx->device);
+    if (o->full) return kv_fail(ctx, KVFT_EINVAL, "solver: dense-G convention not supported");
+    if (o->guess == 0) {
+        KV_CHECK(ctx, cudaMemsetAsync(s->T1, 0, sizeof(double) * s->ng * s->s1(), ctx->stream));
+        KV_CHECK(ctx, cudaMemsetAsync(s->T2, 0, sizeof(double) * s->ng * s->s2(), ctx->stream));
+    } else if (o->guess == 1) {
+        KV_TRY(seed_neg(ctx, s->ng, s->s1(), s->F[2], s->T1b));
+        KV_TRY(seed_neg(ctx, s->ng, s->s2(), s->I[3], s->T2b));
+        KV_TRY(integrate(s, 0, 0.0, s->T1b, s->T2b, s->T1, s->T2, nullptr, nullptr));
+    }
+    KV_TRY(kv_energy(ctx, s->ng, s->nv, s->no, s->T1, s->T2, s->F[1], s->I[5], s->g, s->beta, 0,
+                     s->dsc + 6));
+    double h[7];
+    KV_TRY(read_scalars(s, 7, h));
+    r->e_guess = h[6];
+    KV_TRY(refresh_norms(s));
+    double Eold = 888888888.888888888;
+    r->converged = 0;
+    r->iterations = 0;
+    r->res = 0.0;
+    int i = 0;
+    while (i < o->max_iter && !r->converged) {
+        double E = 0.0, res = 0.0;
+        KV_TRY(kvft_solver_step(s, o->damp, &E, &res));
+        if (o->verbose) fprintf(stderr, " %2d  %.10f   %.4E\n", i + 1, E, res);
+        i++;
+        r->res = res;
+        if (std::fabs(E - Eold) < o->econv && res < o->tconv) r->converged = 1;
+        Eold = E;
+    }
+    r->iterations = i;
+    r->omega_cc = Eold;
+    return r->converged ? KVFT_OK : KVFT_ENOTCONV;
+}
+
+int kvft_solver_get_amplitudes(kvft_solver *s, double *T1h, double *T2h) {
+    if (!s) return KVFT_EINVAL;
+    if (T1h)
+        KV_CHECK(s->ctx, cudaMemcpyAsync(T1h, s->T1, sizeof(double) * s->ng * s->s1(),
+                                         cudaMemcpyDeviceToHost, s->ctx->stream));
+    if (T2h)
+        KV_CHECK(s->ctx, cudaMemcpyAsync(T2h, s->T2, sizeof(double) * s->ng * s->s2(),
+                                         cudaMemcpyDeviceToHost, s->ctx->stream));
+    KV_CHECK(s->ctx, cudaStreamSynchronize(s->ctx->stream));
+    return KVFT_OK;
+}
+
+int kvft_solver_set_amplitudes(kvft_solver *s, const double *T1h, const double *T2h) {
+    if (!s || !T1h || !T2h) return KVFT_EINVAL;
+    KV_CHECK(s->ctx, cudaMemcpyAsync(s->T1, T1h, sizeof(double) * s->ng * s->s1(),
+                                     cudaMemcpyHostToDevice, s->ctx->stream));
+    KV_CHECK(s->ctx, cudaMemcpyAsync(s->T2, T2h, sizeof(double) * s->ng * s->s2(),
+                                     cudaMemcpyHostToDevice, s->ctx->stream));
+    s->norms_valid = false;
+    return KVFT_OK;
+}
+
+int kvft_solver_device_amplitudes(kvft_solver *s, double **T1, double **T2) {
+    if (!s) return KVFT_EINVAL;
+    if (T1) *T1 = s->T1;
+    if (T2) *T2 = s->T2;
+    return KVFT_OK;
+}
+
+// Fermi-scaled blocks from device eps[n], fock[n][n], eri[n]^4 into device
+// F[4] (n x n each) and I[9] (n^4 each): kelvin/cc_utils.py:569-602.
+int kvft_ft_integrals(kvft_ctx *ctx, int n, const double *eps, const double *fock,
+                      const double *eri, double beta, double mu, double *const F[4],
+                      double *const I[9]) {
+    if (!ctx || n <= 0 || !eps || !fock || !eri || !F || !I || !(beta > 0.0))
+        return kv_fail(ctx, KVFT_EINVAL, "ft_integrals: bad argument");
+    cudaSetDevice(ctx->device);
+    void *sf = nullptr;
+    KV_TRY(kv_scratch(ctx, "fermi_sqrt", sizeof(double) * 2 * n, &sf));
+    double *sfo = (double *)sf, *sfv = sfo + n;
+    fermi_kernel<<<1, 256, 0, ctx->stream>>>(n, beta, mu, eps, sfo, sfv);
+    KV_TRY(kv_launch_check(ctx, "fermi"));
+    const size_t n2 = (size_t)n * n;
+    int gb = (int)std::max<size_t>(1, std::min<size_t>((n2 + 255) / 256, 1024));
+    scale_fock_kernel<<<gb, 256, 0, ctx->stream>>>(n, fock, eps, sfo, sfv, F[0], F[1], F[2],
+                                                   F[3]);
+    KV_TRY(kv_launch_check(ctx, "scale_fock"));
+    Blk9 b;
+    for (int k = 0; k < 9; k++) b.p[k] = I[k];
+    scale_eri_kernel<<<ctx->sm_count * 8, 256, 0, ctx->stream>>>(n, eri, sfo, sfv, b);
+    return kv_launch_check(ctx, "scale_eri");
+}
+
+// One CCSD update for all tau points (ft_cc_equations.ccsd_stanton).
+int kvft_ccsd_stanton(kvft_ctx *ctx, int ng, int nv, int no, const double *const F[4],
+                      const double *const I[9], const double *T1old, const double *T2old,
+                      const double *D1, const double *D2, const double *ti, const double *G,
+                      int full, double *T1new, double *T2new) {
+    if (!ctx || ng < 1 || ng > 64 || nv <= 0 || no <= 0 || !F || !I || !T1old || !T2old ||
+        !D1 || !D2 || !ti || !G || !T1new || !T2new)
+        return kv_fail(ctx, KVFT_EINVAL, "ccsd_stanton: bad argument");
+    cudaSetDevice(ctx->device);
+    const long long s1 = (long long)nv * no, s2 = s1 * s1;
+    void *tb = nullptr;
+    KV_TRY(kv_scratch(ctx, "stanton_tbar", sizeof(double) * ng * (s1 + s2), &tb));
+    double *T1b = (double *)tb, *T2b = T1b + ng * s1;
+    KV_TRY(seed_neg(ctx, ng, s1, F[2], T1b));
+    KV_TRY(seed_neg(ctx, ng, s2, I[3], T2b));
+    size_t fr = 0, tot = 0;
+    KV_CHECK(ctx, cudaMemGetInfo(&fr, &tot));
+    size_t per = kv_stanton_workspace(1, nv, no);
+    int chunk = (int)std::max<long long>(1, std::min<long long>(ng, (long long)(0.6 * fr / per)));
+    for (int y0 = 0; y0 < ng; y0 += chunk) {
+        int nb = std::min(chunk, ng - y0);
+        KV_TRY(kv_stanton(ctx, nb, nv, no, F, I, T1old + y0 * s1, T2old + y0 * s2, -1.0,
+                          T1b + y0 * s1, T2b + y0 * s2));
+    }
+    KV_TRY(kvft_int_tbar1(ctx, ng, nv, no, T1b, ti, D1, G, full, T1new));
+    return kvft_int_tbar2(ctx, ng, nv, no, T2b, ti, D2, G, full, T2new);
+}
+
+}  // extern "C"

@@ -1,0 +1,304 @@
+// The spin-orbital CCSD residual with Stanton-Gauss intermediates, evaluated
+// for a batch of tau points on the device (the arithmetic Kelvin delegates to
+// cqcpy.cc_equations._Stanton at kelvin/ft_cc_equations.py:105-107).
+//
+// Every contraction is one strided GEMM (kv_gemm) whose operands are permuted
+// views of the amplitude / integral tensors; tau-independent integrals are
+// shared across the batch (batch stride 0) and, where the other operand is per
+// tau point, the tau index is folded into the GEMM's N dimension so that one
+// launch covers the whole batch.  Ten n^6 flops per tau point remain:
+//   X     = <mn||ef> tau_ef^ij                 (folded over tau)
+//   T2   += 1/2 tau_ab^mn W'_mnij, W' = W_mnij + X/4   (the W_abef tau-tau
+//           term is carried by X, saving the explicit 1/4 tau <mn||ef> GEMM)
+//   T2   += 1/2 W'_abef tau_ef^ij, W'_abef = <ab||ef> - P(ab) t_m^b <am||ef>
+//   W_mbej -= <mn||ef> (t_jn^fb / 2 + t_j^f t_n^b)  (folded over tau)
+//   Z    += t_im^ae W_mbej, then T2 += P(ij)P(ab) Z
+// and about thirty n^5 terms.
+#include "kvft_internal.h"
+
+namespace {
+
+struct Sizes {
+    long long v, o;
+    long long vo, oo, vv, v2o2, o4, v4, vo3;
+};
+
+inline KIdx X1(int s, long long t) { return kidx1(s, t); }
+inline KIdx X2(int s0, long long t0, int s1, long long t1) { return kidx2(s0, t0, s1, t1); }
+inline KIdx X3(int s0, long long t0, int s1, long long t1, int s2, long long t2) {
+    return kidx3(s0, t0, s1, t1, s2, t2);
+}
+inline KMat MA(const double *p, KIdx r, KIdx c, long long bst) { return KMat{p, r, c, bst}; }
+inline KOut MO(double *p, KIdx r, KIdx c, long long bst) { return KOut{p, r, c, bst}; }
+
+// workspace layout (per tau point, doubles)
+struct WS {
+    double *tau, *ttau, *Fae, *Fmi, *Fme, *Xbe, *Xmj, *Wmnij, *Wabef, *Wmbej,
+        *tmp4, *Q, *Zab, *Zij, *Zabij;
+};
+
+size_t ws_per_tau(long long v, long long o) {
+    long long v2o2 = v * v * o * o, o4 = o * o * o * o, v4 = v * v * v * v;
+    long long big = std::max(std::max(v4, o4), v2o2);
+    // tau ttau Wmbej Zab Zij Zabij (v2o2 each) + Wmnij (o4) + Wabef (v4)
+    // + tmp4 (max) + Q (v o^3) + five small matrices
+    return (size_t)(6 * v2o2 + o4 + v4 + big + v * o * o * o + 2 * v * v + 3 * o * o + 2 * o * v);
+}
+
+WS carve(double *base, int nb, long long v, long long o) {
+    WS w;
+    long long v2o2 = v * v * o * o, o4 = o * o * o * o, v4 = v * v * v * v;
+    long long big = std::max(std::max(v4, o4), v2o2);
+    double *p = base;
+    auto take = [&](long long per) { double *q = p; p += per * nb; return q; };
+    w.tau = take(v2o2);
+    w.ttau = take(v2o2);
+    w.Wmbej = take(v2o2);
+    w.Zab = take(v2o2);
+    w.Zij = take(v2o2);
+    w.Zabij = take(v2o2);
+    w.Wmnij = take(o4);
+    w.Wabef = take(v4);
+    w.tmp4 = take(big);
+    w.Q = take(v * o * o * o);
+    w.Fae = take(v * v);
+    w.Xbe = take(v * v);
+    w.Fmi = take(o * o);
+    w.Xmj = take(o * o);
+    w.Fme = take(o * v);
+    (void)take(o * v);
+    (void)take(o * o);
+    return w;
+}
+
+}  // namespace
+
+size_t kv_stanton_workspace(int nb, int nv, int no) {
+    return ws_per_tau(nv, no) * (size_t)nb * sizeof(double);
+}
+
+int kv_stanton(kvft_ctx *ctx, int nb, int nv, int no, const double *const F[4],
+               const double *const I[9], const double *t1, const double *t2,
+               double fac, double *T1, double *T2) {
+    if (nb <= 0) return KVFT_OK;
+    const long long v = nv, o = no;
+    const long long vo = v * o, oo = o * o, vv = v * v;
+    const long long v2o2 = vv * oo, o4 = oo * oo, v4 = vv * vv, vo2 = v * oo;
+    const long long vo3 = v * o * oo;
+    // F.vo and I.vvoo enter only through the caller's seed of T1/T2
+    const double *Foo = F[0], *Fov = F[1], *Fvv = F[3];
+    const double *vvvv = I[0], *vvvo = I[1], *vovv = I[2], *vovo = I[4],
+                 *oovv = I[5], *vooo = I[6], *ooov = I[7], *oooo = I[8];
+
+    void *wsp = nullptr;
+    KV_TRY(kv_scratch(ctx, "stanton", kv_stanton_workspace(nb, nv, no), &wsp));
+    WS w = carve((double *)wsp, nb, v, o);
+    const int B = nb;
+    const KIdx one = X1(1, 0);
+
+    // ---- tau, tau-tilde --------------------------------------------------
+    KV_TRY(kv_make_tau(ctx, B, nv, no, t1, t2, 1.0, w.tau));
+    KV_TRY(kv_make_tau(ctx, B, nv, no, t1, t2, 0.5, w.ttau));
+
+    // ---- F_ae ------------------------------------------------------------
+    KV_TRY(kv_bcast(ctx, B, vv, Fvv, w.Fae));
+    // -1/2 t1[a,m] Fov[m,e]
+    KV_TRY(kv_gemm(ctx, nv, nv, no, B, -0.5, MA(t1, X1(nv, o), X1(no, 1), vo),
+                   MA(Fov, X1(no, v), X1(nv, 1), 0), 1.0,
+                   MO(w.Fae, X1(nv, v), X1(nv, 1), vv)));
+    // - vovv[a,m,f,e] t1[f,m]    (M=(a,e), K=(m,f), N=tau)
+    KV_TRY(kv_gemm(ctx, nv * nv, B, no * nv, 1, -1.0,
+                   MA(vovv, X2(nv, o * vv, nv, 1), X2(no, vv, nv, v), 0),
+                   MA(t1, X2(no, 1, nv, o), X1(B, vo), 0), 1.0,
+                   MO(w.Fae, X2(nv, v, nv, 1), X1(B, vv), 0)));
+    // -1/2 ttau[a,f,m,n] oovv[m,n,e,f]
+    KV_TRY(kv_gemm(ctx, nv, nv, nv * no * no, B, -0.5,
+                   MA(w.ttau, X1(nv, vo2), X3(nv, oo, no, o, no, 1), v2o2),
+                   MA(oovv, X3(nv, 1, no, o * vv, no, vv), X1(nv, v), 0), 1.0,
+                   MO(w.Fae, X1(nv, v), X1(nv, 1), vv)));
+
+    // ---- F_mi ------------------------------------------------------------
+    KV_TRY(kv_bcast(ctx, B, oo, Foo, w.Fmi));
+    // +1/2 Fov[m,e] t1[e,i]
+    KV_TRY(kv_gemm(ctx, no, no, nv, B, 0.5, MA(Fov, X1(no, v), X1(nv, 1), 0),
+                   MA(t1, X1(nv, o), X1(no, 1), vo), 1.0,
+                   MO(w.Fmi, X1(no, o), X1(no, 1), oo)));
+    // + ooov[m,n,i,e] t1[e,n]    (M=(m,i), K=(n,e), N=tau)
+    KV_TRY(kv_gemm(ctx, no * no, B, no * nv, 1, 1.0,
+                   MA(ooov, X2(no, oo * v, no, v), X2(no, vo, nv, 1), 0),
+                   MA(t1, X2(no, 1, nv, o), X1(B, vo), 0), 1.0,
+                   MO(w.Fmi, X2(no, o, no, 1), X1(B, oo), 0)));
+    // +1/2 oovv[m,n,e,f] ttau[e,f,i,n]
+    KV_TRY(kv_gemm(ctx, no, no, no * nv * nv, B, 0.5,
+                   MA(oovv, X1(no, o * vv), X3(no, vv, nv, v, nv, 1), 0),
+                   MA(w.ttau, X3(no, 1, nv, vo2, nv, oo), X1(no, o), v2o2), 1.0,
+                   MO(w.Fmi, X1(no, o), X1(no, 1), oo)));
+
+    // ---- F_me ------------------------------------------------------------
+    KV_TRY(kv_bcast(ctx, B, vo, Fov, w.Fme));
+    // + oovv[m,n,e,f] t1[f,n]    (M=(m,e), K=(n,f), N=tau)
+    KV_TRY(kv_gemm(ctx, no * nv, B, no * nv, 1, 1.0,
+                   MA(oovv, X2(no, o * vv, nv, v), X2(no, vv, nv, 1), 0),
+                   MA(t1, X2(no, 1, nv, o), X1(B, vo), 0), 1.0,
+                   MO(w.Fme, X2(no, v, nv, 1), X1(B, vo), 0)));
+
+    // ---- R1 ----------------------------------------------------------------
+    const KOut T1o = MO(T1, X1(nv, o), X1(no, 1), vo);
+    KV_TRY(kv_gemm(ctx, nv, no, nv, B, fac, MA(w.Fae, X1(nv, v), X1(nv, 1), vv),
+                   MA(t1, X1(nv, o), X1(no, 1), vo), 1.0, T1o));
+    KV_TRY(kv_gemm(ctx, nv, no, no, B, -fac, MA(t1, X1(nv, o), X1(no, 1), vo),
+                   MA(w.Fmi, X1(no, o), X1(no, 1), oo), 1.0, T1o));
+    // t2[a,e,i,m] Fme[m,e]   (M=(a,i), K=(m,e), N=1)
+    KV_TRY(kv_gemm(ctx, nv * no, 1, no * nv, B, fac,
+                   MA(t2, X2(nv, vo2, no, o), X2(no, 1, nv, oo), v2o2),
+                   MA(w.Fme, X2(no, v, nv, 1), one, vo), 1.0,
+                   MO(T1, X2(nv, o, no, 1), one, vo)));
+    // - vovo[a,n,f,i] t1[f,n]   (M=(a,i), K=(n,f), N=tau)
+    KV_TRY(kv_gemm(ctx, nv * no, B, no * nv, 1, -fac,
+                   MA(vovo, X2(nv, vo2, no, 1), X2(no, vo, nv, o), 0),
+                   MA(t1, X2(no, 1, nv, o), X1(B, vo), 0), 1.0,
+                   MO(T1, X2(nv, o, no, 1), X1(B, vo), 0)));
+    // +1/2 vovv[a,m,e,f] t2[e,f,i,m]
+    KV_TRY(kv_gemm(ctx, nv, no, no * nv * nv, B, 0.5 * fac,
+                   MA(vovv, X1(nv, o * vv), X3(no, vv, nv, v, nv, 1), 0),
+                   MA(t2, X3(no, 1, nv, vo2, nv, oo), X1(no, o), v2o2), 1.0, T1o));
+    // +1/2 t2[a,e,m,n] ooov[n,m,i,e]
+    KV_TRY(kv_gemm(ctx, nv, no, nv * no * no, B, 0.5 * fac,
+                   MA(t2, X1(nv, vo2), X3(nv, oo, no, o, no, 1), v2o2),
+                   MA(ooov, X3(nv, 1, no, vo, no, oo * v), X1(no, v), 0), 1.0, T1o));
+
+    // ---- W_mnij' = oooo + P(ij) ooov t1 + X/2 --------------------------------
+    KV_TRY(kv_bcast(ctx, B, o4, oooo, w.Wmnij));
+    // tmp[m,n,i,j] = ooov[m,n,i,e] t1[e,j]
+    KV_TRY(kv_gemm(ctx, no * no * no, no, nv, B, 1.0,
+                   MA(ooov, X3(no, oo * v, no, vo, no, v), X1(nv, 1), 0),
+                   MA(t1, X1(nv, o), X1(no, 1), vo), 0.0,
+                   MO(w.tmp4, X3(no, o * oo, no, oo, no, o), X1(no, 1), o4)));
+    {
+        int d[4] = {no, no, no, no};
+        long long s_id[4] = {o * oo, oo, o, 1}, s_tr[4] = {o * oo, oo, 1, o};
+        KV_TRY(kv_axpby4(ctx, B, d, 1.0, w.tmp4, s_id, o4, 1.0, w.Wmnij, s_id, o4));
+        KV_TRY(kv_axpby4(ctx, B, d, -1.0, w.tmp4, s_tr, o4, 1.0, w.Wmnij, s_id, o4));
+    }
+    // X: + 1/2 oovv[m,n,e,f] tau[e,f,i,j]   (M=(m,n), K=(e,f), N=(tau,i,j))
+    KV_TRY(kv_gemm(ctx, no * no, B * no * no, nv * nv, 1, 0.5,
+                   MA(oovv, X2(no, o * vv, no, vv), X2(nv, v, nv, 1), 0),
+                   MA(w.tau, X2(nv, vo2, nv, oo), X3(B, v2o2, no, o, no, 1), 0), 1.0,
+                   MO(w.Wmnij, X2(no, o * oo, no, oo), X3(B, o4, no, o, no, 1), 0)));
+    // T2 += fac/2 tau[a,b,m,n] Wmnij[m,n,i,j]
+    const KOut T2o = MO(T2, X2(nv, vo2, nv, oo), X2(no, o, no, 1), v2o2);
+    KV_TRY(kv_gemm(ctx, nv * nv, no * no, no * no, B, 0.5 * fac,
+                   MA(w.tau, X2(nv, vo2, nv, oo), X2(no, o, no, 1), v2o2),
+                   MA(w.Wmnij, X2(no, o * oo, no, oo), X2(no, o, no, 1), o4), 1.0, T2o));
+
+    // ---- W_abef' = vvvv - P(ab) t1[b,m] vovv[a,m,e,f] ------------------------
+    KV_TRY(kv_bcast(ctx, B, v4, vvvv, w.Wabef));
+    // tmp[a,b,e,f] = t1[b,m] vovv[a,m,e,f]   (M=b, K=m, N=(a,e,f))
+    KV_TRY(kv_gemm(ctx, nv, nv * nv * nv, no, B, 1.0,
+                   MA(t1, X1(nv, o), X1(no, 1), vo),
+                   MA(vovv, X1(no, vv), X3(nv, o * vv, nv, v, nv, 1), 0), 0.0,
+                   MO(w.tmp4, X1(nv, vv), X3(nv, v * vv, nv, v, nv, 1), v4)));
+    {
+        int d[4] = {nv, nv, nv, nv};
+        long long s_id[4] = {v * vv, vv, v, 1}, s_tr[4] = {vv, v * vv, v, 1};
+        KV_TRY(kv_axpby4(ctx, B, d, -1.0, w.tmp4, s_id, v4, 1.0, w.Wabef, s_id, v4));
+        KV_TRY(kv_axpby4(ctx, B, d, 1.0, w.tmp4, s_tr, v4, 1.0, w.Wabef, s_id, v4));
+    }
+    // T2 += fac/2 Wabef[a,b,e,f] tau[e,f,i,j]
+    KV_TRY(kv_gemm(ctx, nv * nv, no * no, nv * nv, B, 0.5 * fac,
+                   MA(w.Wabef, X2(nv, v * vv, nv, vv), X2(nv, v, nv, 1), v4),
+                   MA(w.tau, X2(nv, vo2, nv, oo), X2(no, o, no, 1), v2o2), 1.0, T2o));
+
+    // ---- W_mbej (layout [m][b][e][j]) ----------------------------------------
+    const long long wm = vv * o, wb = vo, we = o;
+    {
+        int d[4] = {no, nv, nv, no};
+        long long ss[4] = {vo, vo2, o, 1};          // vovo[b,m,e,j]
+        long long ds[4] = {wm, wb, we, 1};
+        KV_TRY(kv_axpby4(ctx, B, d, -1.0, vovo, ss, 0, 0.0, w.Wmbej, ds, v2o2));
+    }
+    // - vovv[b,m,e,f] t1[f,j]    (M=(m,b,e), K=f, N=j)
+    KV_TRY(kv_gemm(ctx, no * nv * nv, no, nv, B, -1.0,
+                   MA(vovv, X3(no, vv, nv, o * vv, nv, v), X1(nv, 1), 0),
+                   MA(t1, X1(nv, o), X1(no, 1), vo), 1.0,
+                   MO(w.Wmbej, X3(no, wm, nv, wb, nv, we), X1(no, 1), v2o2)));
+    // + t1[b,n] ooov[m,n,j,e]    (M=b, K=n, N=(m,e,j))
+    KV_TRY(kv_gemm(ctx, nv, no * nv * no, no, B, 1.0,
+                   MA(t1, X1(nv, o), X1(no, 1), vo),
+                   MA(ooov, X1(no, vo), X3(no, oo * v, nv, 1, no, v), 0), 1.0,
+                   MO(w.Wmbej, X1(nv, wb), X3(no, wm, nv, we, no, 1), v2o2)));
+    // - oovv[m,n,e,f] (t2[f,b,j,n]/2 + t1[f,j] t1[b,n])  (M=(m,e), K=(n,f), N=(tau,b,j))
+    KV_TRY(kv_make_wmbej_tmp(ctx, B, nv, no, t1, t2, w.tmp4));
+    {
+        // tmp4 holds [tau][f][b][j][n] with per-tau stride v2o2 (tmp4 is sized
+        // for the largest block, so index it with the v2o2 layout directly)
+        KV_TRY(kv_gemm(ctx, no * nv, B * nv * no, no * nv, 1, -1.0,
+                       MA(oovv, X2(no, o * vv, nv, v), X2(no, vv, nv, 1), 0),
+                       MA(w.tmp4, X2(no, 1, nv, vo2), X3(B, v2o2, nv, oo, no, o), 0),
+                       1.0, MO(w.Wmbej, X2(no, wm, nv, we), X3(B, v2o2, nv, wb, no, 1), 0)));
+    }
+    // Zabij[a,b,i,j] = t2[a,e,i,m] Wmbej[m,b,e,j]   (M=(a,i), K=(m,e), N=(b,j))
+    KV_TRY(kv_gemm(ctx, nv * no, nv * no, no * nv, B, 1.0,
+                   MA(t2, X2(nv, vo2, no, o), X2(no, 1, nv, oo), v2o2),
+                   MA(w.Wmbej, X2(no, wm, nv, we), X2(nv, wb, no, 1), v2o2), 0.0,
+                   MO(w.Zabij, X2(nv, vo2, no, o), X2(nv, oo, no, 1), v2o2)));
+    // Q[b,m,i,j] = vovo[b,m,e,j] t1[e,i]   (M=(b,m,j), K=e, N=i)
+    KV_TRY(kv_gemm(ctx, nv * no * no, no, nv, B, 1.0,
+                   MA(vovo, X3(nv, vo2, no, vo, no, 1), X1(nv, o), 0),
+                   MA(t1, X1(nv, o), X1(no, 1), vo), 0.0,
+                   MO(w.Q, X3(nv, o * oo, no, oo, no, 1), X1(no, o), vo3)));
+    // Zabij += t1[a,m] Q[b,m,i,j]   (M=a, K=m, N=(b,i,j))
+    KV_TRY(kv_gemm(ctx, nv, nv * no * no, no, B, 1.0,
+                   MA(t1, X1(nv, o), X1(no, 1), vo),
+                   MA(w.Q, X1(no, oo), X3(nv, o * oo, no, o, no, 1), vo3), 1.0,
+                   MO(w.Zabij, X1(nv, vo2), X3(nv, oo, no, o, no, 1), v2o2)));
+
+    // ---- Zab: t2 (F_be - 1/2 t1 F_me) and t1 vooo -----------------------------
+    KV_TRY(kv_bcast(ctx, 1, vv * B, w.Fae, w.Xbe));
+    KV_TRY(kv_gemm(ctx, nv, nv, no, B, -0.5, MA(t1, X1(nv, o), X1(no, 1), vo),
+                   MA(w.Fme, X1(no, v), X1(nv, 1), vo), 1.0,
+                   MO(w.Xbe, X1(nv, v), X1(nv, 1), vv)));
+    // Zab[a,b,i,j] = t2[a,e,i,j] Xbe[b,e]   (M=(a,i,j), K=e, N=b)
+    KV_TRY(kv_gemm(ctx, nv * no * no, nv, nv, B, 1.0,
+                   MA(t2, X3(nv, vo2, no, o, no, 1), X1(nv, oo), v2o2),
+                   MA(w.Xbe, X1(nv, 1), X1(nv, v), vv), 0.0,
+                   MO(w.Zab, X3(nv, vo2, no, o, no, 1), X1(nv, oo), v2o2)));
+    // Zab += t1[a,m] vooo[b,m,i,j]   (M=a, K=m, N=(b,i,j))
+    KV_TRY(kv_gemm(ctx, nv, nv * no * no, no, B, 1.0,
+                   MA(t1, X1(nv, o), X1(no, 1), vo),
+                   MA(vooo, X1(no, oo), X3(nv, o * oo, no, o, no, 1), 0), 1.0,
+                   MO(w.Zab, X1(nv, vo2), X3(nv, oo, no, o, no, 1), v2o2)));
+
+    // ---- Zij: -t2 (F_mj + 1/2 t1 F_me) and vvvo t1 ------------------------------
+    KV_TRY(kv_bcast(ctx, 1, oo * B, w.Fmi, w.Xmj));
+    KV_TRY(kv_gemm(ctx, no, no, nv, B, 0.5, MA(w.Fme, X1(no, v), X1(nv, 1), vo),
+                   MA(t1, X1(nv, o), X1(no, 1), vo), 1.0,
+                   MO(w.Xmj, X1(no, o), X1(no, 1), oo)));
+    // Zij[a,b,i,j] = - t2[a,b,i,m] Xmj[m,j]   (M=(a,b,i), K=m, N=j)
+    KV_TRY(kv_gemm(ctx, nv * nv * no, no, no, B, -1.0,
+                   MA(t2, X3(nv, vo2, nv, oo, no, o), X1(no, 1), v2o2),
+                   MA(w.Xmj, X1(no, o), X1(no, 1), oo), 0.0,
+                   MO(w.Zij, X3(nv, vo2, nv, oo, no, o), X1(no, 1), v2o2)));
+    // Zij += vvvo[a,b,e,j] t1[e,i]   (M=(a,b,j), K=e, N=i)
+    KV_TRY(kv_gemm(ctx, nv * nv * no, no, nv, B, 1.0,
+                   MA(vvvo, X3(nv, vv * o, nv, vo, no, 1), X1(nv, o), 0),
+                   MA(t1, X1(nv, o), X1(no, 1), vo), 1.0,
+                   MO(w.Zij, X3(nv, vo2, nv, oo, no, 1), X1(no, o), v2o2)));
+
+    // ---- T2 += fac [P(ab) Zab + P(ij) Zij + P(ab)P(ij) Zabij] -------------------
+    return kv_assemble_t2(ctx, B, nv, no, fac, w.Zab, w.Zij, w.Zabij, T2);
+}
+
+extern "C" int kvft_stanton_residual(kvft_ctx *ctx, int nb, int nv, int no,
+                                     const double *const F[4], const double *const I[9],
+                                     const double *t1, const double *t2, double fac,
+                                     double *T1, double *T2) {
+    if (!ctx || nb < 0 || nv <= 0 || no <= 0 || !F || !I || !t1 || !t2 || !T1 || !T2)
+        return kv_fail(ctx, KVFT_EINVAL, "kvft_stanton_residual: bad argument");
+    for (int k = 0; k < 4; k++)
+        if (!F[k]) return kv_fail(ctx, KVFT_EINVAL, "kvft_stanton_residual: null F block");
+    for (int k = 0; k < 9; k++)
+        if (!I[k]) return kv_fail(ctx, KVFT_EINVAL, "kvft_stanton_residual: null I block");
+    cudaSetDevice(ctx->device);
+    return kv_stanton(ctx, nb, nv, no, F, I, t1, t2, fac, T1, T2);
+}

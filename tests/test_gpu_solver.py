@@ -1,0 +1,95 @@
+"""End-to-end parity of the device-resident FT-CCSD solve (FP64) with
+Kelvin: grand potential within 1e-10 Ha, amplitudes within 1e-8 max-abs."""
+import json
+import os
+
+import numpy
+import pytest
+
+from conftest import GOLDEN, golden, unpack_blocks
+from kelvin_gb300 import cc_utils, ccsd, quadrature, systems
+from oracle import ft_ccsd as oft
+
+pytestmark = pytest.mark.gpu
+
+OMEGA_TOL = 1e-10
+AMP_TOL = 1e-8
+
+
+def test_ueg7_vs_kelvin(ctx):
+    """kelvin/tests/test_ft_ccsd.py:119-133 (-0.010750238811) and Kelvin's
+    own amplitudes for that run."""
+    meta = json.load(open(os.path.join(GOLDEN, "ueg7.json")))
+    d = golden("ueg7.npz")
+    s = systems.UEGSystem(meta["T"], meta["L"], meta["cutoff"], mu=meta["mu"], norb=7)
+    cc = ccsd.ccsd(s, T=meta["T"], mu=meta["mu"], max_iter=50, damp=meta["damp"], ngrid=10)
+    Et, Ecc = cc.run()
+    assert abs(Ecc - meta["Omega_cc"]) < OMEGA_TOL
+    assert abs(Et - meta["Omega_total"]) < OMEGA_TOL
+    assert abs(Ecc - meta["kelvin_test_golden"]) < 1e-9
+    assert cc.iterations == len(meta["iterations"])
+    assert abs(cc.T1 - d["T1"]).max() < AMP_TOL
+    assert abs(cc.T2.reshape(-1)[d["T2_sample_idx"]] - d["T2_sample"]).max() < AMP_TOL
+    assert abs(numpy.linalg.norm(cc.T2) - meta["T2_norm"]) < AMP_TOL
+
+
+def test_uegscf7_ng40_vs_kelvin(ctx):
+    """UEG with HF-shifted energies, 40 tau points (examples/ueg_ft_cc_compare)."""
+    meta = json.load(open(os.path.join(GOLDEN, "uegscf7.json")))
+    s = systems.UEGSystem(meta["T"], meta["L"], meta["cutoff"], mu=meta["mu"], norb=7,
+                          hf_shift=True)
+    cc = ccsd.ccsd(s, T=meta["T"], mu=meta["mu"], max_iter=50, damp=meta["damp"],
+                   ngrid=meta["ngrid"], tconv=meta["tconv"])
+    Et, Ecc = cc.run()
+    assert abs(Ecc - meta["Omega_cc"]) < OMEGA_TOL
+    assert abs(Ecc - meta["kelvin_example_golden_u"]) < 1e-11
+
+
+def test_ueg19_vs_kelvin_example(ctx):
+    """examples/ueg_ft_ccsd2.out: 19 plane waves (38 spin orbitals, the
+    benchmark size), Omega_cc = -0.015646626108, Omega = -0.3086530556."""
+    s = systems.UEGSystem(0.1, 2 * numpy.pi, 1.2, mu=0.1, norb=19)
+    cc = ccsd.ccsd(s, T=0.1, mu=0.1, max_iter=50, damp=0.2, ngrid=10)
+    Et, Ecc = cc.run()
+    assert abs(Ecc - (-0.015646626108)) < 2e-12
+    assert abs(Et - (-0.3086530556)) < 1e-10
+
+
+def test_ft_cc_iter_dropin_vs_oracle(ctx):
+    d = golden("stanton.npz")
+    F, I = unpack_blocks(d, "ft_")
+    ti, G = d["ft_ti"], d["ft_G"]
+    ng = ti.shape[0]
+    beta = float(d["ft_beta"])
+    g = quadrature.ft_quad(ng, beta, "lin")[1]
+    conv = {"econv": 1e-10, "tconv": 1e-8, "max_iter": 60, "damp": 0.3}
+    T1 = numpy.zeros((ng, 6, 6))
+    T2 = numpy.zeros((ng, 6, 6, 6, 6))
+    Er, T1r, T2r = oft.ft_cc_iter("CCSD", T1, T2, F, I, d["ft_D1"], d["ft_D2"], g, G, beta,
+                                  ng, ti, 0, conv)
+    Eg, T1g, T2g = cc_utils.ft_cc_iter("CCSD", T1, T2, F, I, d["ft_D1"], d["ft_D2"], g, G,
+                                       beta, ng, ti, 0, conv)
+    assert abs(Eg - Er) < OMEGA_TOL
+    assert abs(T1g - T1r).max() < AMP_TOL
+    assert abs(T2g - T2r).max() < AMP_TOL
+
+
+def test_hubbard_ring_vs_oracle(ctx):
+    h = systems.hubbard_recipe(4, 1.0, 2.0, 2.0)
+    kw = dict(ngrid=12, damp=0.3, econv=1e-11, max_iter=80)
+    cc = ccsd.ccsd(h, T=h.T, mu=h.mu, **kw)
+    Et, Ecc = cc.run()
+    Etr, Eccr = oft.ft_ccsd(h.g_energies_tot(), h.g_fock_tot(), h.g_aint_tot(), h.T, h.mu,
+                            E1=h.get_mp1(), **kw)
+    assert abs(Ecc - Eccr) < OMEGA_TOL
+    assert abs(Et - Etr) < OMEGA_TOL
+
+
+def test_warm_start_reproduces(ctx):
+    s = systems.UEGSystem(0.1, 2 * numpy.pi, 1.2, mu=0.1, norb=7)
+    cc = ccsd.ccsd(s, T=0.1, mu=0.1, max_iter=50, damp=0.2, ngrid=10, econv=1e-11)
+    E1 = cc.run()[1]
+    cc2 = ccsd.ccsd(s, T=0.1, mu=0.1, max_iter=50, damp=0.2, ngrid=10, econv=1e-11)
+    E2 = cc2.run(T1=cc.T1, T2=cc.T2)[1]
+    assert abs(E1 - E2) < 1e-10
+    assert cc2.iterations <= 3
