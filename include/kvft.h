@@ -125,6 +125,14 @@ int kvft_stanton_residual(kvft_ctx *ctx, int nb, int nv, int no,
                           const double *t1, const double *t2, double fac,
                           double *T1, double *T2);
 
+/* ---- contraction engine: the GEMM under every einsum of the path --------
+ * (Kelvin's pyscf.lib.einsum -> BLAS dgemm).  C[b] = A[b] B[b] for `batch`
+ * consecutive row-major matrices A[M][K], B[K][N], C[M][N] (device).
+ * precision KVFT_PREC_FP64 uses FP64 FMAs; the tensor-core precisions use
+ * `digits` BF16 digit levels (7: FP64-accurate, 3..5: mixed). */
+int kvft_gemm(kvft_ctx *ctx, int M, int N, int K, int batch, int precision,
+              int digits, const double *A, const double *B, double *C);
+
 /* ---- Fermi-scaled integrals: replaces kelvin/cc_utils.py:569-602 ---------
  * eps[n], fock[n][n] (System.g_fock_tot), eri[n]^4 (System.g_aint_tot) and
  * the outputs F[4] (n x n), I[9] (n^4) are device pointers. */

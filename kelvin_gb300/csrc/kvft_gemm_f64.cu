@@ -156,7 +156,10 @@ int kv_gemm(kvft_ctx *ctx, int M, int N, int K, int batch, double alpha,
     const long long mn = std::min(std::min(M, N), K), mx = std::max(std::max(M, N), K);
     const int cat = (mn * mn > mx) ? KV_CAT_GEMM6 : KV_CAT_GEMM;
     KvProfScope prof(ctx, cat, 2.0 * M * N * (double)K * batch);
-    if (ctx->precision == KVFT_PREC_FP64)
-        return kv_gemm_f64(ctx, M, N, K, batch, alpha, A, B, beta, C);
+    // Tensor cores for everything but matrix-vector shapes and tiny products,
+    // which stay on the FP64 pipe.
+    const bool tc = ctx->precision != KVFT_PREC_FP64 && M >= 16 && N >= 16 && K >= 16 &&
+                    2.0 * M * N * (double)K * batch >= 2.0e6;
+    if (!tc) return kv_gemm_f64(ctx, M, N, K, batch, alpha, A, B, beta, C);
     return kv_gemm_tc(ctx, M, N, K, batch, alpha, A, B, beta, C, ctx->digits);
 }

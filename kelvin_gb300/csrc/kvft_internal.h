@@ -117,6 +117,8 @@ int kv_gemm_f64(kvft_ctx *ctx, int M, int N, int K, int batch, double alpha,
 int kv_gemm_tc(kvft_ctx *ctx, int M, int N, int K, int batch, double alpha,
                const KMat &A, const KMat &B, double beta, const KOut &C,
                int digits);
+// Reads (and clears) the device status word set by bounded waits; syncs.
+int kv_device_status(kvft_ctx *ctx);
 
 // 4-index strided axpby: dst = beta*dst + alpha*src over a [b][d0][d1][d2][d3]
 // index space; each side gives element strides for the 4 indices + batch.

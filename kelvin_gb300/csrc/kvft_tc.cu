@@ -1,9 +1,549 @@
-// Tensor-core contraction path (digit-sliced BF16 tcgen05 GEMM).
+// FP64-accurate contractions on the 5th-generation tensor cores.
+//
+// GB300 issues ~2 FP64 FMAs per clock per SM but ~3600 BF16 MACs, so an FP64
+// GEMM is rebuilt from exact BF16 digit products (an Ozaki-style error-free
+// splitting):
+//
+//   * packing: every row r of A (and every column of B) is scaled by 2^-e_r
+//     so that |y| < 1/2, then y = 2^-7 sum_{s=1..S} P_s with balanced base-128
+//     digits P_s = d_s 2^-7(s-1), d_s in [-64, 64] -- exact in BF16.  The
+//     digits are extracted with integer arithmetic from the FP64 bit pattern.
+//   * products: A B = 2^(e_m + e_n - 14) sum_{s,t} P_s^A P_t^B.  Pair (s,t)
+//     carries the weight 2^-7(s+t-2); pairs with s + t <= D are kept.  Each
+//     digit product is an integer below 2^12 (times a power of two), so an
+//     FP32 accumulator over K <= 2048 terms and two pairs is exact.
+//     tcgen05.mma accumulates level 2 (pair 1,1) and level 3 (pairs 1,2 2,1)
+//     exactly in separate TMEM accumulators and levels >= 4 in a third one
+//     (rounding there is 2^-24 of a 2^-14-relative term).
+//   * epilogue: the three accumulators are read from TMEM (tcgen05.ld),
+//     combined in FP64, scaled by 2^(e_m + e_n - 14) alpha and added to the
+//     FP64 output view.  K > 2048 is split into sequential launches.
+// With D = 7 (21 pair products, six digits) the norm-wise relative error is
+// ~1e-11, far inside the 1e-8 amplitude / 1e-10 Ha parity bounds; D = 3..5 is
+// the mixed-precision form.
+//
+// Kernel: one CTA per 128x128 output tile and K chunk; warp 0 = TMA producer,
+// warp 1 = MMA issuer (and TMEM owner), warps 2..5 = epilogue.  Operands are
+// staged by TMA (64-byte swizzle, 32-element k-blocks, every digit plane of a
+// k-block per pipeline stage).  Every mbarrier wait is bounded by
+// %globaltimer; on expiry the kernel records an error word and unwinds.
 #include "kvft_internal.h"
+
+#include <cuda.h>
+#include <cuda_bf16.h>
+
+#include <cstring>
+#include <mutex>
+
+namespace {
+
+constexpr int TM = 128, TN = 128, KB = 32;
+constexpr int PLANE_BYTES = TM * KB * 2;      // one digit plane of a k-block: 8 KB
+constexpr int MAXS = 6;
+constexpr int KCHUNK = 2048;                  // exactness bound of the level-3 sum
+constexpr int NTHREADS = 192;
+constexpr unsigned long long WAIT_NS = 2000000000ull;   // 2 s per wait
+
+struct TcParams {
+    int M, N;             // output extent of this launch
+    int k0, nkb;          // k-block range [k0, k0 + nkb*KB)
+    int S, D, NS;         // digit planes, levels, pipeline stages
+    int Mp, Np;           // padded rows per plane of A / B
+    int a_batch_rows, b_batch_rows;   // row offset between batch entries (0: shared)
+    const int *ea, *eb;   // row exponents of A / column exponents of B
+    int ea_bst, eb_bst;
+    double alpha, beta;
+    KOut C;
+    int *err;
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ unsigned long long gtime() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t a, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(a), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint32_t a, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(a), "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try(uint32_t a, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(ok)
+        : "r"(a), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// bounded wait: false after WAIT_NS of wall time
+__device__ __forceinline__ bool mbar_wait(uint32_t a, uint32_t parity) {
+    if (mbar_try(a, parity)) return true;
+    const unsigned long long t0 = gtime();
+    while (true) {
+        if (mbar_try(a, parity)) return true;
+        if (gtime() - t0 > WAIT_NS) return false;
+    }
+}
+
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *map, int x, int y,
+                                            uint32_t mbar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes"
+        " [%0], [%1, {%2, %3}], [%4];" ::"r"(dst),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(mbar)
+        : "memory");
+}
+
+// UMMA shared-memory descriptor: K-major, 64-byte swizzle, 8-row groups 512 B apart
+__device__ __forceinline__ uint64_t desc_sw64(uint32_t saddr) {
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr & 0x3FFFF) >> 4);
+    d |= (uint64_t)1 << 16;              // leading byte offset (unused, K-major swizzled)
+    d |= (uint64_t)(512 >> 4) << 32;     // stride byte offset
+    d |= (uint64_t)1 << 46;              // descriptor version
+    d |= (uint64_t)4 << 61;              // SWIZZLE_64B
+    return d;
+}
+
+// kind::f16 instruction descriptor: BF16 x BF16 -> FP32, K-major A and B
+constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(TN >> 3) << 17) |
+                           ((uint32_t)(TM >> 4) << 24);
+
+__device__ __forceinline__ void umma(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t acc) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(tmem_d),
+        "l"(a), "l"(b), "r"(IDESC), "r"(acc)
+        : "memory");
+}
+
+__device__ __forceinline__ void umma_commit(uint32_t mbar) {
+    asm volatile(
+        "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar)
+        : "memory");
+}
+
+__device__ __forceinline__ void fence_before() {
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void fence_after() {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+
+#define TMEM_LD32(taddr, r)                                                                   \
+    asm volatile(                                                                             \
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13," \
+        "%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"   \
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]),              \
+          "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]),           \
+          "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]),       \
+          "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),       \
+          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]),       \
+          "=r"(r[30]), "=r"(r[31])                                                          \
+        : "r"(taddr))
+
+__device__ __forceinline__ void tmem_wait_ld() {
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+__device__ __forceinline__ int level_acc(int l) { return l >= 4 ? 2 : l - 2; }
+
+__global__ void __launch_bounds__(NTHREADS, 1)
+tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+               TcParams p) {
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    const int S = p.S, NS = p.NS;
+    uint8_t *sA = smem;
+    uint8_t *sB = smem + (size_t)NS * S * PLANE_BYTES;
+    uint64_t *bars = (uint64_t *)(sB + (size_t)NS * S * PLANE_BYTES);
+    uint64_t *full = bars, *empty = bars + NS, *accf = bars + 2 * NS;
+    uint32_t *tmem_slot = (uint32_t *)(accf + 1);
+    __shared__ int s_fail;
+
+    const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+    const int m0 = blockIdx.y * TM, n0 = blockIdx.x * TN, b = blockIdx.z;
+    // TMEM columns: one 128-column FP32 accumulator per level group, power of two
+    const int nacc_used = p.D >= 4 ? 3 : p.D - 1;
+    const uint32_t tcols = nacc_used == 1 ? 128u : (nacc_used == 2 ? 256u : 512u);
+
+    if (threadIdx.x == 0) {
+        s_fail = 0;
+        for (int i = 0; i < NS; i++) {
+            mbar_init(smem_u32(&full[i]), 1);
+            mbar_init(smem_u32(&empty[i]), 1);
+        }
+        mbar_init(smem_u32(accf), 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                         smem_u32(tmem_slot)),
+                     "r"(tcols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    fence_before();
+    __syncthreads();
+    fence_after();
+    const uint32_t tmem = *tmem_slot;
+
+    if (warp == 0) {
+        if (lane == 0) {
+            // ---- TMA producer ----
+            const uint32_t bytes = 2u * S * PLANE_BYTES;
+            const int ya = b * p.a_batch_rows, yb = b * p.b_batch_rows;
+            int issued = 0;
+            for (int kb = 0; kb < p.nkb; kb++) {
+                const int st = kb % NS;
+                const uint32_t ph = (kb / NS) & 1;
+                if (!mbar_wait(smem_u32(&empty[st]), ph ^ 1)) {
+                    atomicExch(p.err, 1);
+                    s_fail = 1;
+                    break;
+                }
+                if (s_fail) break;
+                const uint32_t fb = smem_u32(&full[st]);
+                mbar_expect_tx(fb, bytes);
+                const int x = p.k0 + kb * KB;
+                for (int s = 0; s < S; s++) {
+                    tma_load_2d(smem_u32(sA + ((size_t)st * S + s) * PLANE_BYTES), &tmA, x,
+                                ya + s * p.Mp + m0, fb);
+                    tma_load_2d(smem_u32(sB + ((size_t)st * S + s) * PLANE_BYTES), &tmB, x,
+                                yb + s * p.Np + n0, fb);
+                }
+                issued = kb + 1;
+            }
+            // drain: every issued stage must have landed before the CTA exits
+            for (int kb = (issued > NS ? issued - NS : 0); kb < issued; kb++) {
+                const int st = kb % NS;
+                if (!mbar_wait(smem_u32(&full[st]), (kb / NS) & 1)) atomicExch(p.err, 2);
+            }
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {
+            // ---- MMA issuer ----
+            bool started[3] = {false, false, false};
+            bool ok = true;
+            for (int kb = 0; kb < p.nkb; kb++) {
+                const int st = kb % NS;
+                if (!mbar_wait(smem_u32(&full[st]), (kb / NS) & 1)) {
+                    atomicExch(p.err, 3);
+                    s_fail = 1;
+                    ok = false;
+                    break;
+                }
+                fence_after();
+                const uint32_t a0 = smem_u32(sA + (size_t)st * S * PLANE_BYTES);
+                const uint32_t b0 = smem_u32(sB + (size_t)st * S * PLANE_BYTES);
+                for (int l = 2; l <= p.D; l++) {
+                    const int acc = level_acc(l);
+                    for (int s = 1; s < l; s++) {
+                        const int t = l - s;
+                        if (s > S || t > S) continue;
+                        for (int kk = 0; kk < KB / 16; kk++) {
+                            const uint64_t da = desc_sw64(a0 + (s - 1) * PLANE_BYTES + kk * 32);
+                            const uint64_t db = desc_sw64(b0 + (t - 1) * PLANE_BYTES + kk * 32);
+                            umma(tmem + acc * TN, da, db, started[acc] ? 1u : 0u);
+                            started[acc] = true;
+                        }
+                    }
+                }
+                umma_commit(smem_u32(&empty[st]));
+            }
+            if (ok) umma_commit(smem_u32(accf));
+        }
+    } else {
+        // ---- epilogue: warps 2..5, TMEM lane quadrant = warp % 4 ----
+        const int q = warp % 4;
+        const int row = q * 32 + lane;
+        const bool okw = __all_sync(0xffffffffu, mbar_wait(smem_u32(accf), 0));
+        if (!okw && lane == 0) atomicExch(p.err, 4);
+        fence_after();
+        __syncwarp();
+        if (okw && !s_fail) {
+            const int m = m0 + row;
+            const int nacc = p.D >= 4 ? 3 : p.D - 1;
+            const int em = (m < p.M) ? p.ea[(long long)b * p.ea_bst + m] : 0;
+            double *Cb = p.C.p + (long long)b * p.C.bst;
+            const long long roff = (m < p.M) ? p.C.r.off(m) : 0;
+            for (int c = 0; c < TN / 32; c++) {
+                uint32_t r0[32], r1[32], r2[32];
+                const uint32_t tbase = tmem + ((uint32_t)(q * 32) << 16) + c * 32;
+                TMEM_LD32(tbase, r0);
+                if (nacc > 1) TMEM_LD32(tbase + TN, r1);
+                if (nacc > 2) TMEM_LD32(tbase + 2 * TN, r2);
+                tmem_wait_ld();
+                if (m < p.M) {
+#pragma unroll
+                    for (int j = 0; j < 32; j++) {
+                        const int n = n0 + c * 32 + j;
+                        if (n >= p.N) continue;
+                        double v = (double)__uint_as_float(r0[j]);
+                        if (nacc > 1) v += (double)__uint_as_float(r1[j]);
+                        if (nacc > 2) v += (double)__uint_as_float(r2[j]);
+                        const int en = p.eb[(long long)b * p.eb_bst + n];
+                        const double sc = ldexp(p.alpha, em + en - 14);
+                        double *dst = Cb + roff + p.C.c.off(n);
+                        *dst = (p.beta != 0.0) ? fma(sc, v, p.beta * (*dst)) : sc * v;
+                    }
+                }
+            }
+        }
+    }
+    fence_before();
+    __syncthreads();
+    if (warp == 1) {
+        __syncwarp();
+        fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(tcols)
+                     : "memory");
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Digit packing: FP64 strided view (rows x K) -> S BF16 planes [b][s][Rp][Kp]
+// and row exponents [b][Rp].
+// ---------------------------------------------------------------------------
+struct PackView {
+    const double *p;
+    KIdx r, c;
+    long long bst;
+};
+
+// e_r = (max over k of the binary exponent of |x|) + 2, so |x| 2^-e_r < 1/2
+__global__ void pack_exp_kernel(PackView v, int R, int K, int Rp, int *__restrict__ ex) {
+    const int b = blockIdx.y;
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) / 32;
+    const int lane = threadIdx.x % 32;
+    if (warp >= Rp) return;
+    int emax = -2000;
+    if (warp < R) {
+        const double *base = v.p + (long long)b * v.bst + v.r.off(warp);
+        for (int k = lane; k < K; k += 32) {
+            const unsigned long long bits = __double_as_longlong(base[v.c.off(k)]);
+            const int e = (int)((bits >> 52) & 0x7FF);
+            if ((bits & 0x7FFFFFFFFFFFFFFFull) != 0) emax = max(emax, e - 1023);
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, o));
+    if (lane == 0) ex[(long long)b * Rp + warp] = (emax == -2000) ? 0 : emax + 2;
+}
+
+__global__ void pack_digits_kernel(PackView v, int R, int K, int Rp, int Kp, int S,
+                                   const int *__restrict__ ex, __nv_bfloat16 *__restrict__ out) {
+    const int b = blockIdx.y;
+    const size_t plane = (size_t)Rp * Kp;
+    for (int row = blockIdx.x; row < Rp; row += gridDim.x) {
+    __nv_bfloat16 *ob = out + (size_t)b * S * plane + (size_t)row * Kp;
+    const int e = ex[(long long)b * Rp + row];
+    const double *base = (row < R) ? v.p + (long long)b * v.bst + v.r.off(row) : nullptr;
+    for (int k = threadIdx.x; k < Kp; k += blockDim.x) {
+        int d[MAXS] = {0, 0, 0, 0, 0, 0};
+        if (row < R && k < K) {
+            const unsigned long long bits = __double_as_longlong(base[v.c.off(k)]);
+            const int be = (int)((bits >> 52) & 0x7FF);
+            if (be != 0) {   // zero and subnormals (< 2^-1022) pack as zero
+                const long long mant = (long long)((bits & 0xFFFFFFFFFFFFFull) | (1ull << 52));
+                // |x| 2^-e 2^(7S) = mant 2^(be - 1023 - 52 - e + 7S), rounded to an integer
+                const int sh = be - 1023 - 52 - e + 7 * S;
+                long long Y;
+                if (sh >= 0) Y = mant << sh;                 // sh <= 7S - 54 + ... keeps Y < 2^(7S-1)
+                else if (sh > -63) Y = (mant + (1ll << (-sh - 1))) >> (-sh);
+                else Y = 0;
+                // balanced base-128 digits in [-64, 63], least significant first;
+                // the top digit takes the remainder, which is in [0, 64]
+                for (int s = S - 1; s >= 1; s--) {
+                    int dd = (int)(Y & 127);
+                    if (dd >= 64) dd -= 128;
+                    d[s] = dd;
+                    Y = (Y - dd) >> 7;
+                }
+                d[0] = (int)Y;
+                if (bits >> 63)
+                    for (int s = 0; s < S; s++) d[s] = -d[s];
+            }
+        }
+        for (int s = 0; s < S; s++) {
+            // P_s = d_s 2^-7s (stored pre-scaled; exact in BF16)
+            ob[(size_t)s * plane + k] = __float2bfloat16_rn(ldexpf((float)d[s], -7 * s));
+        }
+    }
+    }
+}
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
+                                  const cuuint64_t *, const cuuint64_t *, const cuuint32_t *,
+                                  const cuuint32_t *, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_fn() {
+    static EncodeTiledFn fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000,
+                                             cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (EncodeTiledFn)p;
+    });
+    return fn;
+}
+
+int make_map(kvft_ctx *ctx, CUtensorMap *map, void *base, int Kp, long long rows) {
+    EncodeTiledFn fn = encode_fn();
+    if (!fn) return kv_fail(ctx, KVFT_EDEVICE, "cuTensorMapEncodeTiled unavailable");
+    cuuint64_t dims[2] = {(cuuint64_t)Kp, (cuuint64_t)rows};
+    cuuint64_t strides[1] = {(cuuint64_t)Kp * 2};
+    cuuint32_t box[2] = {KB, TM};
+    cuuint32_t estr[2] = {1, 1};
+    CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, base, dims, strides, box, estr,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
+                    CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return kv_fail(ctx, KVFT_EDEVICE, "cuTensorMapEncodeTiled failed");
+    return KVFT_OK;
+}
+
+struct Packed {
+    __nv_bfloat16 *planes;
+    int *ex;
+    int Rp, Kp, nb;
+};
+
+int pack(kvft_ctx *ctx, const char *key, const PackView &v, int R, int K, int nb, int S,
+         Packed *out) {
+    const int Rp = (R + TM - 1) / TM * TM;
+    const int Kp = (K + KB - 1) / KB * KB;
+    const size_t plane_bytes = (size_t)Rp * Kp * 2;
+    const size_t bytes = (size_t)nb * S * plane_bytes + 1024 + (size_t)nb * Rp * sizeof(int);
+    void *buf = nullptr;
+    KV_TRY(kv_scratch(ctx, key, bytes, &buf));
+    out->planes = (__nv_bfloat16 *)buf;
+    out->ex = (int *)((uint8_t *)buf + (size_t)nb * S * plane_bytes + 1024);
+    out->Rp = Rp;
+    out->Kp = Kp;
+    out->nb = nb;
+    KvProfScope prof(ctx, KV_CAT_PACK, 8.0 * nb * (double)R * K * 2 + (double)nb * S * plane_bytes);
+    {
+        const int warps = Rp;
+        dim3 g((warps * 32 + 255) / 256, nb);
+        pack_exp_kernel<<<g, 256, 0, ctx->stream>>>(v, R, K, Rp, out->ex);
+        KV_TRY(kv_launch_check(ctx, "pack_exp"));
+    }
+    {
+        if (nb > 65535) return kv_fail(ctx, KVFT_EINVAL, "pack: batch too large");
+        const int threads = Kp >= 256 ? 256 : 128;
+        dim3 g(std::min(Rp, ctx->sm_count * 16), nb);
+        pack_digits_kernel<<<g, threads, 0, ctx->stream>>>(v, R, K, Rp, Kp, S, out->ex,
+                                                           out->planes);
+        KV_TRY(kv_launch_check(ctx, "pack_digits"));
+    }
+    return KVFT_OK;
+}
+
+size_t tc_smem(int S, int NS) { return 1024 + (size_t)2 * NS * S * PLANE_BYTES + 8 * (2 * NS + 2) + 64; }
+
+}  // namespace
 
 int kv_gemm_tc(kvft_ctx *ctx, int M, int N, int K, int batch, double alpha, const KMat &A,
                const KMat &B, double beta, const KOut &C, int digits) {
-    (void)M; (void)N; (void)K; (void)batch; (void)alpha; (void)A; (void)B; (void)beta;
-    (void)C; (void)digits;
-    return kv_fail(ctx, KVFT_EINVAL, "tensor-core contraction path is not built");
+    const int D = digits;
+    const int S = std::min(D - 1, MAXS);
+    if (D < 2 || D > MAXS + 1) return kv_fail(ctx, KVFT_EINVAL, "tensor-core digits out of range");
+    if (M <= 0 || N <= 0 || batch <= 0) return KVFT_OK;
+    if (K <= 0) return kv_gemm_f64(ctx, M, N, K, batch, alpha, A, B, beta, C);
+    const int nbA = A.bst ? batch : 1, nbB = B.bst ? batch : 1;
+    Packed pa, pb;
+    KV_TRY(pack(ctx, "tc_pack_a", PackView{A.p, A.r, A.c, A.bst}, M, K, nbA, S, &pa));
+    // B is K x N; its K-major form has rows = N (B's column index), cols = K
+    KV_TRY(pack(ctx, "tc_pack_b", PackView{B.p, B.c, B.r, B.bst}, N, K, nbB, S, &pb));
+    CUtensorMap ma, mb;
+    KV_TRY(make_map(ctx, &ma, pa.planes, pa.Kp, (long long)nbA * S * pa.Rp));
+    KV_TRY(make_map(ctx, &mb, pb.planes, pb.Kp, (long long)nbB * S * pb.Rp));
+    int NS = 2;
+    while (NS < 6 && tc_smem(S, NS + 1) <= 225 * 1024) NS++;
+    const size_t smem = tc_smem(S, NS);
+    static bool attr = false;
+    if (!attr) {
+        cudaFuncSetAttribute(tc_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             225 * 1024);
+        attr = true;
+    }
+    if (batch > 65535) return kv_fail(ctx, KVFT_EINVAL, "tensor-core gemm: batch too large");
+    dim3 grid((N + TN - 1) / TN, (M + TM - 1) / TM, batch);
+    const int nkb_total = pa.Kp / KB;
+    const int chunk_kb = KCHUNK / KB;
+    for (int kb0 = 0; kb0 < nkb_total; kb0 += chunk_kb) {
+        TcParams p;
+        p.M = M;
+        p.N = N;
+        p.k0 = kb0 * KB;
+        p.nkb = std::min(chunk_kb, nkb_total - kb0);
+        p.S = S;
+        p.D = D;
+        p.NS = NS;
+        p.Mp = pa.Rp;
+        p.Np = pb.Rp;
+        p.a_batch_rows = (nbA > 1) ? S * pa.Rp : 0;
+        p.b_batch_rows = (nbB > 1) ? S * pb.Rp : 0;
+        p.ea = pa.ex;
+        p.eb = pb.ex;
+        p.ea_bst = (nbA > 1) ? pa.Rp : 0;
+        p.eb_bst = (nbB > 1) ? pb.Rp : 0;
+        p.alpha = alpha;
+        p.beta = (kb0 == 0) ? beta : 1.0;
+        p.C = C;
+        p.err = ctx->dflag;
+        tc_gemm_kernel<<<grid, NTHREADS, smem, ctx->stream>>>(ma, mb, p);
+        KV_TRY(kv_launch_check(ctx, "tc_gemm"));
+    }
+    return KVFT_OK;
+}
+
+// Device status word written by bounded waits (0 = fine).
+int kv_device_status(kvft_ctx *ctx) {
+    int h = 0;
+    KV_CHECK(ctx, cudaMemcpyAsync(&h, ctx->dflag, sizeof(int), cudaMemcpyDeviceToHost,
+                                  ctx->stream));
+    KV_CHECK(ctx, cudaStreamSynchronize(ctx->stream));
+    if (h != 0) {
+        cudaMemsetAsync(ctx->dflag, 0, sizeof(int), ctx->stream);
+        return kv_fail(ctx, KVFT_ETIMEOUT,
+                       "tensor-core GEMM: a bounded device wait expired (code " +
+                           std::to_string(h) + ")");
+    }
+    return KVFT_OK;
+}
+
+// Plain row-major GEMM through the selected engine (test and measurement hook):
+// C[M][N] = A[M][K] B[K][N] for `batch` consecutive matrices, device pointers.
+extern "C" int kvft_gemm(kvft_ctx *ctx, int M, int N, int K, int batch, int precision,
+                         int digits, const double *A, const double *B, double *C) {
+    if (!ctx || M <= 0 || N <= 0 || K <= 0 || batch <= 0 || !A || !B || !C)
+        return kv_fail(ctx, KVFT_EINVAL, "kvft_gemm: bad argument");
+    cudaSetDevice(ctx->device);
+    KMat a{A, kidx1(M, K), kidx1(K, 1), (long long)M * K};
+    KMat b{B, kidx1(K, N), kidx1(N, 1), (long long)K * N};
+    KOut c{C, kidx1(M, N), kidx1(N, 1), (long long)M * N};
+    int st;
+    if (precision == KVFT_PREC_FP64)
+        st = kv_gemm_f64(ctx, M, N, K, batch, 1.0, a, b, 0.0, c);
+    else
+        st = kv_gemm_tc(ctx, M, N, K, batch, 1.0, a, b, 0.0, c, digits);
+    if (st != KVFT_OK) return st;
+    return kv_device_status(ctx);
 }
