@@ -321,8 +321,46 @@ def run_gpu(args, w):
     return 0
 
 
+def run_gemm(args):
+    """Time one contraction shape through kvft_gemm (device-resident operands)."""
+    import numpy
+    from kelvin_gb300 import _lib, ccsd
+    M, N, K, B = (int(x) for x in args.gemm.split(","))
+    ctx = _lib.context(0)
+    prec, digits = ccsd.PRECISIONS[args.precision]
+    digits = args.digits or digits
+    rng = numpy.random.default_rng(0)
+    A = _lib.DeviceArray.from_host(ctx, rng.standard_normal((B, M, K)))
+    Bm = _lib.DeviceArray.from_host(ctx, rng.standard_normal((B, K, N)))
+    C = _lib.DeviceArray(ctx, (B, M, N))
+
+    def once():
+        ctx.check(ctx.L.kvft_gemm(ctx.h, M, N, K, B, prec, digits, A.ptr, Bm.ptr, C.ptr),
+                  "kvft_gemm")
+
+    for _ in range(max(args.warmup, 1)):
+        once()
+    ctx.sync()
+    ctx.profile_begin()
+    ctx.record(0)
+    for _ in range(args.steps):
+        once()
+    ctx.record(1)
+    ctx.sync()
+    prof = ctx.profile_end()
+    ms = ctx.elapsed_ms(0, 1) / args.steps
+    flops = 2.0 * M * N * K * B
+    pairs = sum(l - 1 for l in range(2, digits + 1)) if args.precision != "fp64" else 1
+    print(json.dumps({"gemm": [M, N, K, B], "precision": args.precision, "digits": digits,
+                      "ms": ms, "fp64_equiv_tflops": flops / ms / 1e9,
+                      "bf16_tflops_issued": flops * pairs / ms / 1e9 if pairs > 1 else None,
+                      "breakdown_ms": {c: round(v[1] / args.steps, 4) for c, v in prof.items()}}))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
+    ap.add_argument("--gemm", default="", help="M,N,K,batch: time one contraction shape")
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
@@ -332,6 +370,8 @@ def main():
     ap.add_argument("--digits", type=int, default=0)
     args = ap.parse_args()
     w = WORKLOADS[args.workload]
+    if args.gemm:
+        return run_gemm(args)
     if args.impl == "reference":
         return run_reference(args, w)
     return run_gpu(args, w)

@@ -114,6 +114,12 @@ __global__ void scale_view_kernel(int M, int N, int batch, double beta, KOut C) 
 
 }  // namespace
 
+int kv_scale_view(kvft_ctx *ctx, int M, int N, int batch, double beta, const KOut &C) {
+    if (beta == 1.0 || M <= 0 || N <= 0 || batch <= 0) return KVFT_OK;
+    scale_view_kernel<<<ctx->sm_count * 4, 256, 0, ctx->stream>>>(M, N, batch, beta, C);
+    return kv_launch_check(ctx, "scale_view");
+}
+
 int kv_gemm_f64(kvft_ctx *ctx, int M, int N, int K, int batch, double alpha,
                 const KMat &A, const KMat &B, double beta, const KOut &C) {
     if (M <= 0 || N <= 0 || batch <= 0) return KVFT_OK;

@@ -117,6 +117,8 @@ int kv_gemm_f64(kvft_ctx *ctx, int M, int N, int K, int batch, double alpha,
 int kv_gemm_tc(kvft_ctx *ctx, int M, int N, int K, int batch, double alpha,
                const KMat &A, const KMat &B, double beta, const KOut &C,
                int digits);
+// C = beta * C over a strided output view (beta == 0 writes zeros).
+int kv_scale_view(kvft_ctx *ctx, int M, int N, int batch, double beta, const KOut &C);
 // Reads (and clears) the device status word set by bounded waits; syncs.
 int kv_device_status(kvft_ctx *ctx);
 

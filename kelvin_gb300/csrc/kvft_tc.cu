@@ -47,9 +47,13 @@ constexpr unsigned long long WAIT_NS = 2000000000ull;   // 2 s per wait
 
 struct TcParams {
     int M, N;             // output extent of this launch
-    int k0, nkb;          // k-block range [k0, k0 + nkb*KB)
+    int kb_base;          // first k-block of this launch
+    int chunk_kb;         // k-blocks per K chunk (exactness bound)
+    int nkb_total;        // k-blocks of the padded K extent
+    int nsplit;           // K chunks run side by side (grid z = batch * nsplit)
+    int atomic;           // 1: chunks add into C with FP64 atomics
     int S, D, NS;         // digit planes, levels, pipeline stages
-    int Mp, Np;           // padded rows per plane of A / B
+    int Mp, Np;           // rows per digit plane of A / B
     int a_batch_rows, b_batch_rows;   // row offset between batch entries (0: shared)
     const int *ea, *eb;   // row exponents of A / column exponents of B
     int ea_bst, eb_bst;
@@ -57,6 +61,14 @@ struct TcParams {
     KOut C;
     int *err;
 };
+
+// Raw row exponents are reduced with atomicMax into an array preset to
+// 0x80808080 (below any binary exponent); exp_of turns a raw maximum into the
+// packing exponent e_r = max + 2 (|x| 2^-e_r < 1/2), or 0 for an all-zero row.
+constexpr int EXP_RAW_FLOOR = -1100;
+__host__ __device__ __forceinline__ int exp_of(int raw) {
+    return raw < EXP_RAW_FLOOR ? 0 : raw + 2;
+}
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
     return static_cast<uint32_t>(__cvta_generic_to_shared(p));
@@ -188,7 +200,10 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
     __shared__ int s_fail;
 
     const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
-    const int m0 = blockIdx.y * TM, n0 = blockIdx.x * TN, b = blockIdx.z;
+    const int m0 = blockIdx.y * TM, n0 = blockIdx.x * TN;
+    const int b = blockIdx.z / p.nsplit, split = blockIdx.z % p.nsplit;
+    const int kb_begin = p.kb_base + split * p.chunk_kb;
+    const int nkb = min(p.chunk_kb, p.nkb_total - kb_begin);
     // TMEM columns: one 128-column FP32 accumulator per level group, power of two
     const int nacc_used = n_acc(p.D);
     const uint32_t tcols = nacc_used == 1 ? 128u : (nacc_used == 2 ? 256u : 512u);
@@ -221,7 +236,7 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
             const uint32_t bytes = 2u * S * PLANE_BYTES;
             const int ya = b * p.a_batch_rows, yb = b * p.b_batch_rows;
             int issued = 0;
-            for (int kb = 0; kb < p.nkb; kb++) {
+            for (int kb = 0; kb < nkb; kb++) {
                 const int st = kb % NS;
                 const uint32_t ph = (kb / NS) & 1;
                 if (!mbar_wait(smem_u32(&empty[st]), ph ^ 1)) {
@@ -232,7 +247,7 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
                 if (s_fail) break;
                 const uint32_t fb = smem_u32(&full[st]);
                 mbar_expect_tx(fb, bytes);
-                const int x = p.k0 + kb * KB;
+                const int x = (kb_begin + kb) * KB;
                 for (int s = 0; s < S; s++) {
                     tma_load_2d(smem_u32(sA + ((size_t)st * S + s) * PLANE_BYTES), &tmA, x,
                                 ya + s * p.Mp + m0, fb);
@@ -252,7 +267,7 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
             // ---- MMA issuer ----
             bool started[4] = {false, false, false, false};
             bool ok = true;
-            for (int kb = 0; kb < p.nkb; kb++) {
+            for (int kb = 0; kb < nkb; kb++) {
                 const int st = kb % NS;
                 if (!mbar_wait(smem_u32(&full[st]), (kb / NS) & 1)) {
                     atomicExch(p.err, 3);
@@ -291,7 +306,7 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
         if (okw && !s_fail) {
             const int m = m0 + row;
             const int nacc = n_acc(p.D);
-            const int em = (m < p.M) ? p.ea[(long long)b * p.ea_bst + m] : 0;
+            const int em = (m < p.M) ? exp_of(p.ea[(long long)b * p.ea_bst + m]) : 0;
             double *Cb = p.C.p + (long long)b * p.C.bst;
             const long long roff = (m < p.M) ? p.C.r.off(m) : 0;
             for (int c = 0; c < TN / 16; c++) {
@@ -313,10 +328,11 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
                         if (nacc > 2) v += (double)__uint_as_float(r2[j]);
                         if (nacc > 1) v += (double)__uint_as_float(r1[j]);
                         v += (double)__uint_as_float(r0[j]);
-                        const int en = p.eb[(long long)b * p.eb_bst + n];
+                        const int en = exp_of(p.eb[(long long)b * p.eb_bst + n]);
                         const double sc = ldexp(p.alpha, em + en - 14);
                         double *dst = Cb + roff + p.C.c.off(n);
-                        *dst = (p.beta != 0.0) ? fma(sc, v, p.beta * (*dst)) : sc * v;
+                        if (p.atomic) atomicAdd(dst, sc * v);
+                        else *dst = (p.beta != 0.0) ? fma(sc, v, p.beta * (*dst)) : sc * v;
                     }
                 }
             }
@@ -342,64 +358,78 @@ struct PackView {
     long long bst;
 };
 
-// e_r = (max over k of the binary exponent of |x|) + 2, so |x| 2^-e_r < 1/2
-__global__ void pack_exp_kernel(PackView v, int R, int K, int Rp, int *__restrict__ ex) {
+constexpr int EXP_SEG = 2048;   // K elements reduced by one warp
+
+__global__ void pack_exp_kernel(PackView v, int R, int K, int nseg, int *__restrict__ ex) {
     const int b = blockIdx.y;
-    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) / 32;
     const int lane = threadIdx.x % 32;
-    if (warp >= Rp) return;
-    int emax = -2000;
-    if (warp < R) {
-        const double *base = v.p + (long long)b * v.bst + v.r.off(warp);
-        for (int k = lane; k < K; k += 32) {
+    const long long nwarps = (long long)gridDim.x * blockDim.x / 32;
+    for (long long item = (blockIdx.x * (long long)blockDim.x + threadIdx.x) / 32;
+         item < (long long)R * nseg; item += nwarps) {
+        const int row = (int)(item / nseg), sg = (int)(item % nseg);
+        const double *base = v.p + (long long)b * v.bst + v.r.off(row);
+        const int kend = min(K, (sg + 1) * EXP_SEG);
+        int emax = -2000;
+        for (int k = sg * EXP_SEG + lane; k < kend; k += 32) {
             const unsigned long long bits = __double_as_longlong(base[v.c.off(k)]);
-            const int e = (int)((bits >> 52) & 0x7FF);
-            if ((bits & 0x7FFFFFFFFFFFFFFFull) != 0) emax = max(emax, e - 1023);
+            if ((bits & 0x7FFFFFFFFFFFFFFFull) != 0)
+                emax = max(emax, (int)((bits >> 52) & 0x7FF) - 1023);
         }
+        for (int o = 16; o > 0; o >>= 1) emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, o));
+        if (lane == 0 && emax > -2000) atomicMax(&ex[(long long)b * R + row], emax);
     }
-    for (int o = 16; o > 0; o >>= 1) emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, o));
-    if (lane == 0) ex[(long long)b * Rp + warp] = (emax == -2000) ? 0 : emax + 2;
 }
 
-__global__ void pack_digits_kernel(PackView v, int R, int K, int Rp, int Kp, int S,
+// Balanced base-128 digits of x 2^-e (|x 2^-e| < 1/2), most significant
+// first, from the FP64 bit pattern with integer arithmetic only.
+__device__ __forceinline__ void digits_of(unsigned long long bits, int e, int S, int *d) {
+    for (int s = 0; s < MAXS; s++) d[s] = 0;
+    const int be = (int)((bits >> 52) & 0x7FF);
+    if (be == 0) return;                        // zero / subnormal (< 2^-1022): zero
+    const long long mant = (long long)((bits & 0xFFFFFFFFFFFFFull) | (1ull << 52));
+    // |x| 2^-e 2^(7S) = mant 2^(be - 1023 - 52 - e + 7S), rounded to an integer
+    const int sh = be - 1023 - 52 - e + 7 * S;
+    long long Y;
+    if (sh >= 0) Y = mant << sh;
+    else if (sh > -63) Y = (mant + (1ll << (-sh - 1))) >> (-sh);
+    else Y = 0;
+    // digits in [-64, 63], least significant first; the top one takes the
+    // remainder, which is in [0, 64]
+    for (int s = S - 1; s >= 1; s--) {
+        int dd = (int)(Y & 127);
+        if (dd >= 64) dd -= 128;
+        d[s] = dd;
+        Y = (Y - dd) >> 7;
+    }
+    d[0] = (int)Y;
+    if (bits >> 63)
+        for (int s = 0; s < S; s++) d[s] = -d[s];
+}
+
+// planes[b][s][row][k] (row stride ld) = d_s 2^-7s, two k per thread
+template <int S>
+__global__ void pack_digits_kernel(PackView v, int R, int K, int ld,
                                    const int *__restrict__ ex, __nv_bfloat16 *__restrict__ out) {
     const int b = blockIdx.y;
-    const size_t plane = (size_t)Rp * Kp;
-    for (int row = blockIdx.x; row < Rp; row += gridDim.x) {
-    __nv_bfloat16 *ob = out + (size_t)b * S * plane + (size_t)row * Kp;
-    const int e = ex[(long long)b * Rp + row];
-    const double *base = (row < R) ? v.p + (long long)b * v.bst + v.r.off(row) : nullptr;
-    for (int k = threadIdx.x; k < Kp; k += blockDim.x) {
-        int d[MAXS] = {0, 0, 0, 0, 0, 0};
-        if (row < R && k < K) {
-            const unsigned long long bits = __double_as_longlong(base[v.c.off(k)]);
-            const int be = (int)((bits >> 52) & 0x7FF);
-            if (be != 0) {   // zero and subnormals (< 2^-1022) pack as zero
-                const long long mant = (long long)((bits & 0xFFFFFFFFFFFFFull) | (1ull << 52));
-                // |x| 2^-e 2^(7S) = mant 2^(be - 1023 - 52 - e + 7S), rounded to an integer
-                const int sh = be - 1023 - 52 - e + 7 * S;
-                long long Y;
-                if (sh >= 0) Y = mant << sh;                 // sh <= 7S - 54 + ... keeps Y < 2^(7S-1)
-                else if (sh > -63) Y = (mant + (1ll << (-sh - 1))) >> (-sh);
-                else Y = 0;
-                // balanced base-128 digits in [-64, 63], least significant first;
-                // the top digit takes the remainder, which is in [0, 64]
-                for (int s = S - 1; s >= 1; s--) {
-                    int dd = (int)(Y & 127);
-                    if (dd >= 64) dd -= 128;
-                    d[s] = dd;
-                    Y = (Y - dd) >> 7;
-                }
-                d[0] = (int)Y;
-                if (bits >> 63)
-                    for (int s = 0; s < S; s++) d[s] = -d[s];
+    const size_t plane = (size_t)R * ld;
+    for (int row = blockIdx.x; row < R; row += gridDim.x) {
+        __nv_bfloat16 *ob = out + (size_t)b * S * plane + (size_t)row * ld;
+        const int e = exp_of(ex[(long long)b * R + row]);
+        const double *base = v.p + (long long)b * v.bst + v.r.off(row);
+        for (int k = 2 * threadIdx.x; k < K; k += 2 * blockDim.x) {
+            int d0[MAXS], d1[MAXS];
+            digits_of(__double_as_longlong(base[v.c.off(k)]), e, S, d0);
+            if (k + 1 < K) digits_of(__double_as_longlong(base[v.c.off(k + 1)]), e, S, d1);
+            else
+                for (int s = 0; s < MAXS; s++) d1[s] = 0;
+            for (int s = 0; s < S; s++) {
+                // P_s = d_s 2^-7s (pre-scaled; exact in BF16)
+                __nv_bfloat162 w;
+                w.x = __float2bfloat16_rn(ldexpf((float)d0[s], -7 * s));
+                w.y = __float2bfloat16_rn(ldexpf((float)d1[s], -7 * s));
+                *reinterpret_cast<__nv_bfloat162 *>(ob + (size_t)s * plane + k) = w;
             }
         }
-        for (int s = 0; s < S; s++) {
-            // P_s = d_s 2^-7s (stored pre-scaled; exact in BF16)
-            ob[(size_t)s * plane + k] = __float2bfloat16_rn(ldexpf((float)d[s], -7 * s));
-        }
-    }
     }
 }
 
@@ -422,11 +452,11 @@ EncodeTiledFn encode_fn() {
     return fn;
 }
 
-int make_map(kvft_ctx *ctx, CUtensorMap *map, void *base, int Kp, long long rows) {
+int make_map(kvft_ctx *ctx, CUtensorMap *map, void *base, int K, int ld, long long rows) {
     EncodeTiledFn fn = encode_fn();
     if (!fn) return kv_fail(ctx, KVFT_EDEVICE, "cuTensorMapEncodeTiled unavailable");
-    cuuint64_t dims[2] = {(cuuint64_t)Kp, (cuuint64_t)rows};
-    cuuint64_t strides[1] = {(cuuint64_t)Kp * 2};
+    cuuint64_t dims[2] = {(cuuint64_t)K, (cuuint64_t)rows};
+    cuuint64_t strides[1] = {(cuuint64_t)ld * 2};
     cuuint32_t box[2] = {KB, TM};
     cuuint32_t estr[2] = {1, 1};
     CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, base, dims, strides, box, estr,
@@ -439,35 +469,53 @@ int make_map(kvft_ctx *ctx, CUtensorMap *map, void *base, int Kp, long long rows
 struct Packed {
     __nv_bfloat16 *planes;
     int *ex;
-    int Rp, Kp, nb;
+    int R, ld, K, nb;
 };
 
+// Digit planes [nb][S][R][ld] (ld = K rounded up to 8 for the 16-byte TMA row
+// stride) and exponents [nb][R].  No row or K padding is written: the tensor
+// map's extent is (K, nb S R) and TMA fills out-of-range boxes with zeros;
+// rows past R inside a 128-row box belong to the next plane and only reach
+// output rows/columns that the epilogue discards.
 int pack(kvft_ctx *ctx, const char *key, const PackView &v, int R, int K, int nb, int S,
          Packed *out) {
-    const int Rp = (R + TM - 1) / TM * TM;
-    const int Kp = (K + KB - 1) / KB * KB;
-    const size_t plane_bytes = (size_t)Rp * Kp * 2;
-    const size_t bytes = (size_t)nb * S * plane_bytes + 1024 + (size_t)nb * Rp * sizeof(int);
+    const int ld = (K + 7) / 8 * 8;
+    const size_t plane_bytes = (size_t)R * ld * 2;
+    const size_t pbytes = ((size_t)nb * S * plane_bytes + 1023) / 1024 * 1024;
+    const size_t bytes = pbytes + (size_t)nb * R * sizeof(int);
     void *buf = nullptr;
     KV_TRY(kv_scratch(ctx, key, bytes, &buf));
     out->planes = (__nv_bfloat16 *)buf;
-    out->ex = (int *)((uint8_t *)buf + (size_t)nb * S * plane_bytes + 1024);
-    out->Rp = Rp;
-    out->Kp = Kp;
+    out->ex = (int *)((uint8_t *)buf + pbytes);
+    out->R = R;
+    out->ld = ld;
+    out->K = K;
     out->nb = nb;
-    KvProfScope prof(ctx, KV_CAT_PACK, 8.0 * nb * (double)R * K * 2 + (double)nb * S * plane_bytes);
+    if (nb > 65535) return kv_fail(ctx, KVFT_EINVAL, "pack: batch too large");
+    KvProfScope prof(ctx, KV_CAT_PACK, 8.0 * nb * (double)R * K + (double)nb * S * plane_bytes);
+    KV_CHECK(ctx, cudaMemsetAsync(out->ex, 0x80, (size_t)nb * R * sizeof(int), ctx->stream));
     {
-        const int warps = Rp;
-        dim3 g((warps * 32 + 255) / 256, nb);
-        pack_exp_kernel<<<g, 256, 0, ctx->stream>>>(v, R, K, Rp, out->ex);
+        const int nseg = (K + EXP_SEG - 1) / EXP_SEG;
+        const long long warps = (long long)R * nseg;
+        const int blocks = (int)std::min<long long>((warps * 32 + 255) / 256, ctx->sm_count * 32);
+        pack_exp_kernel<<<dim3(blocks, nb), 256, 0, ctx->stream>>>(v, R, K, nseg, out->ex);
         KV_TRY(kv_launch_check(ctx, "pack_exp"));
     }
     {
-        if (nb > 65535) return kv_fail(ctx, KVFT_EINVAL, "pack: batch too large");
-        const int threads = Kp >= 256 ? 256 : 128;
-        dim3 g(std::min(Rp, ctx->sm_count * 16), nb);
-        pack_digits_kernel<<<g, threads, 0, ctx->stream>>>(v, R, K, Rp, Kp, S, out->ex,
-                                                           out->planes);
+        const int threads = 32 * std::max(1, std::min(8, (K / 2 + 31) / 32));
+        const int blocks = std::min(R, ctx->sm_count * 64);
+        const dim3 g(blocks, nb);
+        switch (S) {
+#define KV_PACK_CASE(s_)                                                                    \
+    case s_:                                                                                \
+        pack_digits_kernel<s_><<<g, threads, 0, ctx->stream>>>(v, R, K, ld, out->ex,        \
+                                                               out->planes);                \
+        break;
+            KV_PACK_CASE(1) KV_PACK_CASE(2) KV_PACK_CASE(3) KV_PACK_CASE(4) KV_PACK_CASE(5)
+            KV_PACK_CASE(6)
+#undef KV_PACK_CASE
+        default: return kv_fail(ctx, KVFT_EINVAL, "pack: digit count out of range");
+        }
         KV_TRY(kv_launch_check(ctx, "pack_digits"));
     }
     return KVFT_OK;
@@ -490,8 +538,8 @@ int kv_gemm_tc(kvft_ctx *ctx, int M, int N, int K, int batch, double alpha, cons
     // B is K x N; its K-major form has rows = N (B's column index), cols = K
     KV_TRY(pack(ctx, "tc_pack_b", PackView{B.p, B.c, B.r, B.bst}, N, K, nbB, S, &pb));
     CUtensorMap ma, mb;
-    KV_TRY(make_map(ctx, &ma, pa.planes, pa.Kp, (long long)nbA * S * pa.Rp));
-    KV_TRY(make_map(ctx, &mb, pb.planes, pb.Kp, (long long)nbB * S * pb.Rp));
+    KV_TRY(make_map(ctx, &ma, pa.planes, pa.K, pa.ld, (long long)nbA * S * pa.R));
+    KV_TRY(make_map(ctx, &mb, pb.planes, pb.K, pb.ld, (long long)nbB * S * pb.R));
     int NS = 2;
     while (NS < 6 && tc_smem(S, NS + 1) <= 225 * 1024) NS++;
     const size_t smem = tc_smem(S, NS);
@@ -502,30 +550,50 @@ int kv_gemm_tc(kvft_ctx *ctx, int M, int N, int K, int batch, double alpha, cons
         attr = true;
     }
     if (batch > 65535) return kv_fail(ctx, KVFT_EINVAL, "tensor-core gemm: batch too large");
-    dim3 grid((N + TN - 1) / TN, (M + TM - 1) / TM, batch);
-    const int nkb_total = pa.Kp / KB;
-    const int chunk_kb = KCHUNK / KB;
-    for (int kb0 = 0; kb0 < nkb_total; kb0 += chunk_kb) {
-        TcParams p;
-        p.M = M;
-        p.N = N;
-        p.k0 = kb0 * KB;
-        p.nkb = std::min(chunk_kb, nkb_total - kb0);
-        p.S = S;
-        p.D = D;
-        p.NS = NS;
-        p.Mp = pa.Rp;
-        p.Np = pb.Rp;
-        p.a_batch_rows = (nbA > 1) ? S * pa.Rp : 0;
-        p.b_batch_rows = (nbB > 1) ? S * pb.Rp : 0;
-        p.ea = pa.ex;
-        p.eb = pb.ex;
-        p.ea_bst = (nbA > 1) ? pa.Rp : 0;
-        p.eb_bst = (nbB > 1) ? pb.Rp : 0;
-        p.alpha = alpha;
-        p.beta = (kb0 == 0) ? beta : 1.0;
-        p.C = C;
-        p.err = ctx->dflag;
+    const int mt = (M + TM - 1) / TM, nt = (N + TN - 1) / TN;
+    const int nkb_total = (K + KB - 1) / KB;
+    const int nchunks = (nkb_total + KCHUNK / KB - 1) / (KCHUNK / KB);
+    const int chunk_kb = (nkb_total + nchunks - 1) / nchunks;     // balanced chunks
+    const long long tiles = (long long)mt * nt * batch;
+    // few output tiles and several K chunks: run the chunks side by side and
+    // add them into C with FP64 atomics (C pre-scaled by beta)
+    const bool par = nchunks > 1 && tiles < 2LL * ctx->sm_count &&
+                     (long long)batch * nchunks <= 65535;
+    if (par && beta != 1.0) KV_TRY(kv_scale_view(ctx, M, N, batch, beta, C));
+    TcParams p;
+    p.M = M;
+    p.N = N;
+    p.chunk_kb = chunk_kb;
+    p.nkb_total = nkb_total;
+    p.S = S;
+    p.D = D;
+    p.NS = NS;
+    p.Mp = pa.R;
+    p.Np = pb.R;
+    p.a_batch_rows = (nbA > 1) ? S * pa.R : 0;
+    p.b_batch_rows = (nbB > 1) ? S * pb.R : 0;
+    p.ea = pa.ex;
+    p.eb = pb.ex;
+    p.ea_bst = (nbA > 1) ? pa.R : 0;
+    p.eb_bst = (nbB > 1) ? pb.R : 0;
+    p.alpha = alpha;
+    p.C = C;
+    p.err = ctx->dflag;
+    if (par) {
+        p.kb_base = 0;
+        p.nsplit = nchunks;
+        p.atomic = 1;
+        p.beta = 1.0;
+        dim3 grid(nt, mt, batch * nchunks);
+        tc_gemm_kernel<<<grid, NTHREADS, smem, ctx->stream>>>(ma, mb, p);
+        return kv_launch_check(ctx, "tc_gemm");
+    }
+    p.nsplit = 1;
+    p.atomic = 0;
+    dim3 grid(nt, mt, batch);
+    for (int c = 0; c < nchunks; c++) {
+        p.kb_base = c * chunk_kb;
+        p.beta = (c == 0) ? beta : 1.0;
         tc_gemm_kernel<<<grid, NTHREADS, smem, ctx->stream>>>(ma, mb, p);
         KV_TRY(kv_launch_check(ctx, "tc_gemm"));
     }
