@@ -33,6 +33,7 @@
 #include <cuda.h>
 #include <cuda_bf16.h>
 
+#include <cmath>
 #include <cstring>
 #include <mutex>
 
@@ -58,9 +59,32 @@ struct TcParams {
     const int *ea, *eb;   // row exponents of A / column exponents of B
     int ea_bst, eb_bst;
     double alpha, beta;
+    int alpha_pow2;       // alpha = +-2^alpha_exp: folded into the exponent field
+    int alpha_exp;
+    unsigned long long alpha_sign;   // sign bit of alpha (FP64 position)
     KOut C;
     int *err;
 };
+
+// Knuth's error-free sum: s + e == a + b exactly (round-to-nearest FP32)
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
+    s = a + b;
+    const float bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+}
+
+// FP64 value of x 2^k with sign flipped by `sgn`, built from the FP32 bit
+// pattern (exact; FP32 subnormals, below 2^-126 of the accumulator, give 0)
+__device__ __forceinline__ double f32_scaled(float x, int k, unsigned long long sgn) {
+    const uint32_t u = __float_as_uint(x);
+    const int E = (int)((u >> 23) & 0xFF);
+    const int e64 = E - 127 + 1023 + k;
+    if (E == 0 || e64 <= 0) return 0.0;
+    const unsigned long long bits = (((unsigned long long)(u >> 31) << 63) ^ sgn) |
+                                    ((unsigned long long)e64 << 52) |
+                                    ((unsigned long long)(u & 0x7FFFFFu) << 29);
+    return __longlong_as_double(bits);
+}
 
 // Raw row exponents are reduced with atomicMax into an array preset to
 // 0x80808080 (below any binary exponent); exp_of turns a raw maximum into the
@@ -198,6 +222,8 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
     uint64_t *full = bars, *empty = bars + NS, *accf = bars + 2 * NS;
     uint32_t *tmem_slot = (uint32_t *)(accf + 1);
     __shared__ int s_fail;
+    __shared__ long long s_coff[4][16];   // epilogue: per-warp column offsets
+    __shared__ int s_cexp[4][16];         // and column exponents
 
     const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
     const int m0 = blockIdx.y * TM, n0 = blockIdx.x * TN;
@@ -304,12 +330,24 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
         fence_after();
         __syncwarp();
         if (okw && !s_fail) {
+            // GB300's FP64 pipe is ~1/1500 of its BF16 tensor rate, so the
+            // levels are combined with error-free FP32 two-sums and the FP64
+            // result is assembled from bit patterns, the scale
+            // 2^(e_m + e_n - 14) (and a power-of-two alpha) going straight into
+            // the exponent field: at most two FP64 operations per element.
             const int m = m0 + row;
             const int nacc = n_acc(p.D);
+            const int ew = warp - 2;
             const int em = (m < p.M) ? exp_of(p.ea[(long long)b * p.ea_bst + m]) : 0;
+            const int krow = em - 14 + p.alpha_exp;
             double *Cb = p.C.p + (long long)b * p.C.bst;
             const long long roff = (m < p.M) ? p.C.r.off(m) : 0;
             for (int c = 0; c < TN / 16; c++) {
+                if (lane < 16) {
+                    const int n = n0 + c * 16 + lane;
+                    s_coff[ew][lane] = (n < p.N) ? p.C.c.off(n) : 0;
+                    s_cexp[ew][lane] = (n < p.N) ? exp_of(p.eb[(long long)b * p.eb_bst + n]) : 0;
+                }
                 uint32_t r0[16], r1[16], r2[16], r3[16];
                 const uint32_t tbase = tmem + ((uint32_t)(q * 32) << 16) + c * 16;
                 TMEM_LD16(tbase, r0);
@@ -317,24 +355,30 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
                 if (nacc > 2) TMEM_LD16(tbase + 2 * TN, r2);
                 if (nacc > 3) TMEM_LD16(tbase + 3 * TN, r3);
                 tmem_wait_ld();
+                __syncwarp();
                 if (m < p.M) {
 #pragma unroll
                     for (int j = 0; j < 16; j++) {
                         const int n = n0 + c * 16 + j;
                         if (n >= p.N) continue;
-                        // smallest level first; every term is exact in FP64
-                        double v = 0.0;
-                        if (nacc > 3) v = (double)__uint_as_float(r3[j]);
-                        if (nacc > 2) v += (double)__uint_as_float(r2[j]);
-                        if (nacc > 1) v += (double)__uint_as_float(r1[j]);
-                        v += (double)__uint_as_float(r0[j]);
-                        const int en = exp_of(p.eb[(long long)b * p.eb_bst + n]);
-                        const double sc = ldexp(p.alpha, em + en - 14);
-                        double *dst = Cb + roff + p.C.c.off(n);
-                        if (p.atomic) atomicAdd(dst, sc * v);
-                        else *dst = (p.beta != 0.0) ? fma(sc, v, p.beta * (*dst)) : sc * v;
+                        float hi = __uint_as_float(r0[j]), lo = 0.f, e = 0.f;
+                        if (nacc > 1) two_sum(hi, __uint_as_float(r1[j]), hi, lo);
+                        if (nacc > 2) {
+                            two_sum(hi, __uint_as_float(r2[j]), hi, e);
+                            lo += e;
+                        }
+                        if (nacc > 3) lo += __uint_as_float(r3[j]);
+                        const int k = krow + s_cexp[ew][j];
+                        double v = f32_scaled(hi, k, p.alpha_sign) + f32_scaled(lo, k, p.alpha_sign);
+                        if (!p.alpha_pow2) v *= p.alpha;
+                        double *dst = Cb + roff + s_coff[ew][j];
+                        if (p.atomic) atomicAdd(dst, v);
+                        else if (p.beta == 0.0) *dst = v;
+                        else if (p.beta == 1.0) *dst += v;
+                        else *dst = fma(p.beta, *dst, v);
                     }
                 }
+                __syncwarp();
             }
         }
     }
@@ -577,6 +621,13 @@ int kv_gemm_tc(kvft_ctx *ctx, int M, int N, int K, int batch, double alpha, cons
     p.ea_bst = (nbA > 1) ? pa.R : 0;
     p.eb_bst = (nbB > 1) ? pb.R : 0;
     p.alpha = alpha;
+    {
+        int ex2 = 0;
+        const double fr = std::frexp(alpha, &ex2);
+        p.alpha_pow2 = (std::fabs(fr) == 0.5) ? 1 : 0;
+        p.alpha_exp = p.alpha_pow2 ? ex2 - 1 : 0;
+        p.alpha_sign = (p.alpha_pow2 && alpha < 0) ? (1ull << 63) : 0ull;
+    }
     p.C = C;
     p.err = ctx->dflag;
     if (par) {
