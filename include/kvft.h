@@ -109,6 +109,24 @@ int kvft_ft_cc_energy(kvft_ctx *ctx, int ng, int nv, int no, const double *T1,
                       const double *g, double beta, int qterm,
                       double *omega_host);
 
+/* ---- allocation-free energy (no counterpart in the reference) ------------
+ * For callers that must not let a library allocate device memory (a host
+ * whose memory pool owns the device, a latency-bound serving loop that cannot
+ * absorb cudaMalloc's synchronisation, a plugin host that forbids foreign
+ * allocations): the same value as kvft_ft_cc_energy, written to the DEVICE
+ * double *omega_dev on `stream` (NULL: the legacy default stream; any stream
+ * of the current device), with no context and no allocation.  Scratch is a
+ * fixed 256 KiB static device array held by every GPU that loads the library
+ * until exit.  The first call on a device looks up that array's address (do it
+ * before any stream capture).  Calls share the array: calls that overlap on
+ * the GPU race.  Limit: ceil(no*no/32) * ceil(nv*nv/32) <= 32767 tiles (up
+ * to nv = no = 76); larger problems return KVFT_EINVAL without launching. */
+int kvft_ft_cc_energy_noalloc(void *stream, int ng, int nv, int no,
+                              const double *T1, const double *T2,
+                              const double *f, const double *eri,
+                              const double *g, double beta, int qterm,
+                              double *omega_dev);
+
 /* ---- CCSD update: replaces kelvin/ft_cc_equations.py:96-113 -------------
  * F[4] = {oo, ov, vo, vv}; I[9] = {vvvv, vvvo, vovv, vvoo, vovo, oovv, vooo,
  * ooov, oooo}.  T1new/T2new receive the integrated amplitudes. */

@@ -92,6 +92,9 @@ _SIGS = {
                                              ctypes.c_int, ctypes.POINTER(vp),
                                              ctypes.POINTER(vp), vp, vp,
                                              ctypes.c_double, vp, vp]),
+    "kvft_ft_cc_energy_noalloc": (ctypes.c_int, [vp, ctypes.c_int, ctypes.c_int,
+                                                 ctypes.c_int, vp, vp, vp, vp, vp,
+                                                 ctypes.c_double, ctypes.c_int, vp]),
     "kvft_gemm": (ctypes.c_int, [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                  ctypes.c_int, ctypes.c_int, vp, vp, vp]),
     "kvft_ft_integrals": (ctypes.c_int, [vp, ctypes.c_int, vp, vp, vp, ctypes.c_double,

@@ -127,3 +127,63 @@ extern "C" int kvft_ft_cc_energy(kvft_ctx *ctx, int ng, int nv, int no, const do
     KV_CHECK(ctx, cudaStreamSynchronize(ctx->stream));
     return KVFT_OK;
 }
+
+// ---------------------------------------------------------------------------
+// Allocation-free energy reduction.
+//
+// Some callers cannot let a library call cudaMalloc: a host process that has
+// handed (nearly) all device memory to its own pool, a serving loop whose
+// latency budget has no room for the device-wide synchronisation cudaMalloc
+// and cudaFree can imply, or a plugin host that forbids allocations outside
+// its allocator.  kvft_ft_cc_energy_noalloc computes the same grand
+// potential as kvft_ft_cc_energy without any allocation: the per-tile
+// partial sums live in the file-scope array below, which every GPU that loads
+// libkvft holds (256 KiB) until the process exits.  Its device address is
+// looked up with cudaGetSymbolAddress once per device, on that device's first
+// call, so that first call should come before any stream capture.  All calls
+// on a device share the array and every call overwrites the slots it reads,
+// so nothing has to be cleared between calls; two calls that overlap on the
+// GPU (different streams, no ordering) race on it.
+// ---------------------------------------------------------------------------
+#include <mutex>
+
+namespace {
+constexpr int NOALLOC_MAX_TILES = 32767;   // 32 x 32 tiles of (a,b) x (i,j)
+__device__ __align__(256) double g_energy_scratch[NOALLOC_MAX_TILES + 1];
+std::mutex g_energy_scratch_mu;
+double *g_energy_scratch_ptr[64] = {};     // device address of the array, per device
+}  // namespace
+
+extern "C" int kvft_ft_cc_energy_noalloc(void *stream, int ng, int nv, int no,
+                                         const double *T1, const double *T2,
+                                         const double *f, const double *eri,
+                                         const double *g, double beta, int qterm,
+                                         double *omega_dev) {
+    if (ng < 1 || nv <= 0 || no <= 0 || !T1 || !T2 || !f || !eri || !g || !omega_dev ||
+        beta == 0.0)
+        return KVFT_EINVAL;
+    const long long V2 = (long long)nv * nv, O2 = (long long)no * no;
+    const long long gx = (O2 + TILE - 1) / TILE, gy = (V2 + TILE - 1) / TILE;
+    if (gx * gy > NOALLOC_MAX_TILES) return KVFT_EINVAL;   // beyond the static scratch
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return KVFT_EDEVICE;
+    double *scratch = nullptr;
+    {
+        std::lock_guard<std::mutex> lock(g_energy_scratch_mu);
+        if (!g_energy_scratch_ptr[dev]) {
+            void *p = nullptr;
+            if (cudaGetSymbolAddress(&p, g_energy_scratch) != cudaSuccess || !p)
+                return KVFT_EDEVICE;
+            g_energy_scratch_ptr[dev] = (double *)p;
+        }
+        scratch = g_energy_scratch_ptr[dev];
+    }
+    cudaStream_t st = (cudaStream_t)stream;
+    const int nblk = (int)(gx * gy);
+    energy2_kernel<<<dim3((unsigned)gx, (unsigned)gy), 256, 0, st>>>(ng, nv, no, T1, T2, eri, g,
+                                                                      qterm, scratch);
+    energy1_kernel<<<1, 256, 0, st>>>(ng, nv, no, T1, f, g, scratch + nblk);
+    energy_final_kernel<<<1, 256, 0, st>>>(scratch, nblk, scratch + nblk, 1.0 / beta,
+                                           omega_dev);
+    return cudaGetLastError() == cudaSuccess ? KVFT_OK : KVFT_EDEVICE;
+}
