@@ -2,17 +2,27 @@
 """FT-CCSD solves/s on GB300 (libkvft) or on the host cores (reference arm).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl kvft|reference]
-                    [--workload ueg38|ueg114] [--precision fp64|fp64_tc|mixed]
+                    [--workload ueg114|ueg38] [--precision mixed|fp64_tc|fp64]
+    python bench.py --gemm M,N,K,batch [--precision ...]      # one contraction shape
 
-A step is one complete FT-CCSD solve (Kelvin's damped amplitude iteration
-from the first-order guess to convergence) of a seeded synthetic uniform
-electron gas.  ``value`` times K solves with integrals and buffers already
-resident in HBM; ``e2e`` times K solves through the public drop-in API
+Workloads are seeded synthetic uniform electron gases (the benchmark configs):
+
+* ueg114 (default): 38 electrons, rs = 1, the 57 lowest plane waves (114 spin
+  orbitals), Theta = 0.25, ng = 20, damping 0.5, econv 1e-10.  A full solve
+  takes minutes, so a step is ONE amplitude iteration (CCSD update of all tau
+  points + integration + damping + norms + energy) and
+  solves/s = iterations/s / iterations_per_solve.
+* ueg38: 14 electrons, rs = 4, 19 plane waves (38 spin orbitals), Theta = 0.5,
+  ng = 10: a step is a complete solve (first-order guess to convergence).
+
+``value`` times K steps with the integrals and buffers already resident in HBM;
+``e2e`` times the same through the public drop-in API
 (``kelvin_gb300.ccsd.ccsd(sys, ...).run()``) from host arrays, including the
 host->device upload of the integrals and the read-back of the amplitudes.
-With N > 1 (torchrun) every rank runs an independent replica: the path has no
-exchange step at N = 1 granularity, so only timings are reduced (gloo).
-One JSON line is printed by rank 0.
+The headline precision is 'mixed' (three BF16 digit levels on tensor cores;
+FP64 quadrature, damping and energy); one FP64-accurate step is timed beside
+it.  With N > 1 (torchrun) every rank runs an independent replica: only the
+timings are reduced (gloo).  One JSON line is printed by rank 0.
 """
 import argparse
 import json
@@ -29,26 +39,24 @@ sys.path.insert(0, ROOT)
 METRIC = "FT-CCSD solves/s"
 UNIT = "solves/s"
 
-# Workloads (uniform electron gas, Kelvin's 'lin' Simpson tau grid).
-# iters: iterations of the FP64 solve to convergence, used to scale the
-# CPU reference's per-iteration sample to solves/s.
+# iters: amplitude iterations of the converged solve (FP64 path, guess 1).
 WORKLOADS = {
-    "ueg38": dict(N=14, rs=4.0, norb=19, theta=0.5, ng=10, damp=0.5, econv=1e-10,
-                  max_iter=100, iters=None,
-                  label="UEG 14 e-, rs=4, 19 plane waves (38 spin orbitals), Theta=0.5, "
-                        "ng=10, damping 0.5, econv 1e-10"),
     "ueg114": dict(N=38, rs=1.0, norb=57, theta=0.25, ng=20, damp=0.5, econv=1e-10,
-                   max_iter=100, iters=None,
+                   max_iter=100, iters=None, step="iteration",
                    label="UEG 38 e-, rs=1, 57 plane waves (114 spin orbitals), Theta=0.25, "
                          "ng=20, damping 0.5, econv 1e-10"),
+    "ueg38": dict(N=14, rs=4.0, norb=19, theta=0.5, ng=10, damp=0.5, econv=1e-10,
+                  max_iter=100, iters=30, step="solve",
+                  label="UEG 14 e-, rs=4, 19 plane waves (38 spin orbitals), Theta=0.5, "
+                        "ng=10, damping 0.5, econv 1e-10"),
 }
+ITERS_FALLBACK = 30
 
 
 def load_peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
-        d = json.load(open(p))
-        return d, "measured"
+        return json.load(open(p)), "measured"
     return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, \
         "fallback"
 
@@ -71,8 +79,7 @@ class ClockSampler(object):
                 ["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
                  "--format=csv,noheader,nounits", "-lms", "200"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
-            self.t = threading.Thread(target=self._read, daemon=True)
-            self.t.start()
+            threading.Thread(target=self._read, daemon=True).start()
         except Exception:
             self.proc = None
 
@@ -140,31 +147,47 @@ def max_over_ranks(ws, x):
 
 
 # ---------------------------------------------------------------------------
-# CPU reference (numpy port of Kelvin's path, the oracle) on the host cores
+# CPU reference: the oracle (numpy FP64 port of Kelvin's path) on host cores
 # ---------------------------------------------------------------------------
-def cpu_iteration_seconds(w, sysobj, reps=1):
-    """Seconds per amplitude iteration of the numpy FP64 path (Kelvin's
-    ccsd_stanton + int_tbar + ft_cc_energy + damping) on this workload."""
+def cpu_iteration_seconds(w, sysobj):
+    """(seconds per amplitude iteration of the numpy FP64 path, sample text).
+
+    n <= 40: one full iteration (ccsd_stanton over all tau points, int_tbar,
+    damping, ft_cc_energy).  Larger n (a numpy iteration is many minutes):
+    the W_abef ladder contraction of one tau point (2 n^6 flops, Kelvin's
+    einsum 'efij,abef->abij'), scaled by the iteration's 10 n^6 ng flops."""
     import numpy
     from oracle import ft_ccsd, ft_utils, quadrature
     beta = 1.0 / sysobj.T
     en = sysobj.g_energies_tot()
-    ti, g, G = quadrature.ft_quad(w["ng"], beta, "lin")
-    F, I = ft_ccsd.ft_integrals(sysobj.g_fock_tot(), sysobj.g_aint_tot(), en, beta, sysobj.mu)
-    D1, D2 = ft_utils.D1(en, en), ft_utils.D2(en, en)
-    ng, n = w["ng"], en.shape[0]
-    T1 = numpy.zeros((ng, n, n))
-    T2 = numpy.zeros((ng, n, n, n, n))
-    best = None
-    for _ in range(reps):
+    n, ng = en.shape[0], w["ng"]
+    threads = os.cpu_count()
+    if n <= 40:
+        ti, g, G = quadrature.ft_quad(ng, beta, "lin")
+        F, I = ft_ccsd.ft_integrals(sysobj.g_fock_tot(), sysobj.g_aint_tot(), en, beta,
+                                    sysobj.mu)
+        D1, D2 = ft_utils.D1(en, en), ft_utils.D2(en, en)
+        T1 = numpy.zeros((ng, n, n))
+        T2 = numpy.zeros((ng, n, n, n, n))
         t0 = time.perf_counter()
         T1n, T2n = ft_ccsd.ccsd_stanton(F, I, T1, T2, D1, D2, ti, ng, G)
         T1 = w["damp"] * T1 + (1 - w["damp"]) * T1n
         T2 = w["damp"] * T2 + (1 - w["damp"]) * T2n
         ft_ccsd.ft_cc_energy(T1, T2, F.ov, I.oovv, g, beta)
         dt = time.perf_counter() - t0
-        best = dt if best is None else min(best, dt)
-    return best
+        return dt, "1 full amplitude iteration (numpy FP64 oracle port, %d threads, %.2f s)" % (
+            threads, dt)
+    rng = numpy.random.default_rng(0)
+    W = rng.standard_normal((n * n, n * n))
+    tau = rng.standard_normal((n * n, n * n))
+    t0 = time.perf_counter()
+    W @ tau
+    dt = time.perf_counter() - t0
+    it = dt * 5.0 * ng
+    return it, ("one n^6 contraction of the iteration (W_abef ladder of one tau point, "
+                "%d^2 x %d^2 x %d^2 FP64 BLAS via numpy, %d threads, %.2f s) scaled by "
+                "10 n^6 ng / 2 n^6 = %d (n^5 terms and quadrature not counted: a lower "
+                "bound on the CPU time)" % (n, n, n, threads, dt, 5 * ng))
 
 
 def run_reference(args, w):
@@ -172,23 +195,26 @@ def run_reference(args, w):
     if rank != 0:
         return 0
     sysobj = build_system(w)
-    cores = os.cpu_count()
-    for _ in range(max(args.warmup, 0) and 1):
-        cpu_iteration_seconds(w, sysobj, 1)
-    times = [cpu_iteration_seconds(w, sysobj, 1) for _ in range(args.steps)]
+    iters = w["iters"] or ITERS_FALLBACK
+    cpu_iteration_seconds(w, sysobj)                      # warm-up sample
+    times, sample = [], ""
+    for _ in range(args.steps):
+        t, sample = cpu_iteration_seconds(w, sysobj)
+        times.append(t)
     t_iter = statistics.median(times)
-    iters = w["iters"] or 30
     value = 1.0 / (t_iter * iters)
-    sample = ("%d steps x 1 amplitude iteration (numpy FP64, %d BLAS threads); "
-              "solves/s = 1 / (median s/iteration x %d iterations of the converged solve)"
-              % (args.steps, cores, iters))
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": t_iter * 1e3, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": w["label"], "impl": "oracle numpy port of Kelvin's path"},
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-                             "sample": sample},
+            "ms_per_step": t_iter * 1e3 * (iters if w["step"] == "solve" else 1),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic",
+            "config": {"workload": w["label"], "step": w["step"],
+                       "iterations_per_solve": iters,
+                       "impl": "oracle numpy FP64 port of Kelvin's path (Kelvin is pure "
+                               "Python and cannot run on the GPU host)"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": os.cpu_count(),
+                             "kind": "port", "sample": "%d x %s; solves/s = 1 / (median "
+                             "s/iteration x %d iterations)" % (args.steps, sample, iters)},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
@@ -200,7 +226,6 @@ def run_reference(args, w):
 # ---------------------------------------------------------------------------
 def run_gpu(args, w):
     ws, rank, local = dist_setup()
-    import numpy
     from kelvin_gb300 import _lib, ccsd
     from kelvin_gb300.cc_utils import DeviceSolver, iterate
     from kelvin_gb300.quadrature import ft_quad
@@ -209,7 +234,6 @@ def run_gpu(args, w):
     prec, digits = ccsd.PRECISIONS[args.precision]
     if args.digits:
         digits = args.digits
-    ctx.set_precision(prec, digits)
     sysobj = build_system(w)
     beta = 1.0 / sysobj.T
     en = sysobj.g_energies_tot()
@@ -217,19 +241,22 @@ def run_gpu(args, w):
     ti, g, G = ft_quad(w["ng"], beta, "lin")
     conv = {"econv": w["econv"], "tconv": 1000.0 * w["econv"], "max_iter": w["max_iter"],
             "damp": w["damp"]}
-    n = en.shape[0]
-    ng = w["ng"]
+    n, ng = en.shape[0], w["ng"]
+    per_solve = w["step"] == "solve"
+    iters = w["iters"] or ITERS_FALLBACK
 
-    # ---- device-resident solves (value) --------------------------------------
+    ctx.set_precision(prec, digits)
     solver = DeviceSolver.from_system(ctx, en, fock, eri, beta, sysobj.mu, ti, g, G)
+    solver.guess(1)
 
-    def one_solve():
-        solver.guess(1)
-        E = iterate(solver, conv)
-        return E, solver.iterations
+    def one_step():
+        if per_solve:
+            solver.guess(1)
+            return iterate(solver, conv), solver.iterations
+        return solver.step(w["damp"])[0], 1
 
     for _ in range(args.warmup):
-        E, iters = one_solve()
+        one_step()
     ctx.sync()
     barrier(ws)
     clocks = ClockSampler(local)
@@ -237,86 +264,107 @@ def run_gpu(args, w):
     l0 = ctx.launches()
     ctx.profile_begin()
     ctx.record(0)
-    results = []
-    for _ in range(args.steps):
-        results.append(one_solve())
+    results = [one_step() for _ in range(args.steps)]
     ctx.record(1)
     ctx.sync()
     prof = ctx.profile_end()
     launches = ctx.launches() - l0
-    ms = ctx.elapsed_ms(0, 1)
+    ms = max_over_ranks(ws, ctx.elapsed_ms(0, 1))
     clk = clocks.stop()
-    barrier(ws)
-    ms = max_over_ranks(ws, ms)
-    value = ws * args.steps / (ms / 1e3)
-    E, iters = results[-1]
+    step_ms = ms / args.steps
+    value = ws / (step_ms / 1e3) / (1 if per_solve else iters)
+    if per_solve:
+        iters = results[-1][1]
+
+    # one FP64-accurate step beside the headline precision (mixed vs FP64)
+    fp64_step_ms = None
+    if args.precision == "mixed":
+        ctx.set_precision(_lib.PREC_FP64_TC, 7)
+        one_step()
+        ctx.sync()
+        ctx.record(4)
+        one_step()
+        ctx.record(5)
+        ctx.sync()
+        fp64_step_ms = ctx.elapsed_ms(4, 5)
+        ctx.set_precision(prec, digits)
     solver.close()
 
-    # ---- end-to-end through the public API (e2e) -----------------------------
+    # ---- end to end through the public API (e2e) -----------------------------
     barrier(ws)
     ctx.sync()
     t0 = time.perf_counter()
     ctx.record(2)
-    e2e_omega = None
-    for _ in range(args.steps):
-        cc = ccsd.ccsd(sysobj, T=sysobj.T, mu=sysobj.mu, max_iter=w["max_iter"],
-                       damp=w["damp"], ngrid=ng, econv=w["econv"], precision=args.precision,
-                       digits=digits, ctx=ctx)
-        e2e_omega = cc.run()[1]
+    for _ in range(1 if not per_solve else args.steps):
+        cc = ccsd.ccsd(sysobj, T=sysobj.T, mu=sysobj.mu, max_iter=(
+            w["max_iter"] if per_solve else args.steps), damp=w["damp"], ngrid=ng,
+            econv=w["econv"], precision=args.precision, digits=digits, refine_sweeps=0, ctx=ctx)
+        cc.run()
+        e2e_iters = cc.iterations
         cc.release()
     ctx.record(3)
     ctx.sync()
     e2e_ms = max(ctx.elapsed_ms(2, 3), (time.perf_counter() - t0) * 1e3)
     e2e_ms = max_over_ranks(ws, e2e_ms)
-    e2e_value = ws * args.steps / (e2e_ms / 1e3)
+    if per_solve:
+        e2e_value = ws * args.steps / (e2e_ms / 1e3)
+    else:
+        e2e_value = ws * e2e_iters / (e2e_ms / 1e3) / iters
     h2d = 8 * (n + n * n + n ** 4 + 2 * ng + ng * ng)
-    d2h = 8 * ng * (n * n + n ** 4) + 8 * 7 * (iters + 2)
+    d2h = 8 * ng * (n * n + n ** 4) + 8 * 7 * (e2e_iters + 2)
 
     if rank != 0:
         return 0
     peaks, peak_src = load_peaks()
-    # dominant kernel category by device time over the timed region
     dom = max(prof, key=lambda c: prof[c][1])
     nl, dms, work = prof[dom]
     if dom in ("gemm6", "gemm"):
         achieved = work / (dms / 1e3) / 1e12
+        unit, bound = "TFLOP/s", "tensor"
         if args.precision == "fp64":
-            peak, unit, bound = 1.25, "TFLOP/s", "tensor"
-            psrc = "nominal GB300 FP64 1.25 TFLOP/s (no FP64 figure in MEASURED_PEAKS.json)"
+            peak = 1.25
+            psrc = "nominal GB300 FP64 1.25 TFLOP/s (MEASURED_PEAKS.json has no FP64 figure)"
+            kernel = "gemm_f64_kernel (%s contractions)" % dom
         else:
-            peak, unit, bound = peaks["bf16_tflops_sustained"], "TFLOP/s", "tensor"
-            psrc = "bf16_tflops_sustained of %s peaks" % peak_src
+            pairs = sum(l - 1 for l in range(2, digits + 1))
+            achieved *= pairs          # BF16 tensor flops issued per FP64-equivalent flop
+            peak = peaks["bf16_tflops_sustained"]
+            psrc = "bf16_tflops_sustained of %s peaks; achieved = algorithmic 2MNK flops x " \
+                   "%d digit-pair products" % (peak_src, pairs)
+            kernel = "tc_gemm_kernel (%s contractions)" % dom
     else:
         achieved = work / (dms / 1e3) / 1e9
         peak, unit, bound = peaks["hbm_gbs"], "GB/s", "hbm"
         psrc = "hbm_gbs of %s peaks" % peak_src
-    roofline = {"bound": bound, "kernel": dom, "achieved": achieved, "peak": peak,
-                "unit": unit, "frac": achieved / peak, "traffic": None,
-                "launches": nl, "avg_launch_ms": dms / max(nl, 1), "peak_source": psrc,
-                "breakdown_ms": {c: round(prof[c][1], 3) for c in prof}}
+        kernel = dom
+    roofline = {"bound": bound, "kernel": kernel, "achieved": achieved, "peak": peak,
+                "unit": unit, "frac": achieved / peak, "traffic": None, "launches": nl,
+                "avg_launch_ms": dms / max(nl, 1), "peak_source": psrc,
+                "breakdown_ms_per_step": {c: round(prof[c][1] / args.steps, 3) for c in prof}}
 
-    # CPU baseline: one numpy iteration of the same workload on the host cores
-    t_iter = cpu_iteration_seconds(w, sysobj, 1)
+    t_iter, sample = cpu_iteration_seconds(w, sysobj)
     cpu_val = 1.0 / (t_iter * iters)
+    cfg = {"workload": w["label"], "step": w["step"], "precision": args.precision,
+           "digits": digits if args.precision != "fp64" else None,
+           "iterations_per_solve": iters, "omega_cc_last_step": results[-1][0],
+           "l2": "per-step working set > 129 MB L2 (no flush)",
+           "parallelism": "replicas" if ws > 1 else "single GPU"}
+    if w["iters"] is None and not per_solve:
+        cfg["iterations_per_solve_note"] = "not yet measured for this workload; %d assumed" % iters
+    if fp64_step_ms is not None:
+        cfg["fp64_tc_step_ms"] = fp64_step_ms
+        cfg["fp64_tc_solves_per_s"] = ws / (fp64_step_ms / 1e3) / (1 if per_solve else iters)
+        cfg["mixed_over_fp64_tc"] = fp64_step_ms / step_ms
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f64" if args.precision != "mixed" else "bf16-digits/f64",
-            "data": "synthetic",
-            "config": {"workload": w["label"], "precision": args.precision,
-                       "digits": digits if args.precision != "fp64" else None,
-                       "iterations_per_solve": iters, "omega_cc": E, "e2e_omega_cc": e2e_omega,
-                       "l2": "per-iteration working set > 129 MB L2; no flush",
-                       "parallelism": "replicas" if ws > 1 else "single GPU"},
-            "roofline": roofline,
+            "dtype": "f64" if args.precision != "mixed" else "bf16x3-digits/f32acc + f64",
+            "data": "synthetic", "config": cfg, "roofline": roofline,
             "cpu_baseline": {"value": cpu_val, "unit": UNIT, "cores": os.cpu_count(),
-                             "kind": "port",
-                             "sample": "1 amplitude iteration of the same workload (numpy "
-                                       "FP64 oracle port, %.2f s) x %d iterations" % (t_iter, iters)},
+                             "kind": "port", "sample": sample + "; x %d iterations" % iters},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
-            "gpu_launches": launches,
-            "clocks": clk}
+            "gpu_launches": launches, "clocks": clk}
     print(json.dumps(line))
     return 0
 
@@ -365,8 +413,8 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="kvft", choices=["kvft", "reference"])
-    ap.add_argument("--workload", default="ueg38", choices=sorted(WORKLOADS))
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "fp64_tc", "mixed"])
+    ap.add_argument("--workload", default="ueg114", choices=sorted(WORKLOADS))
+    ap.add_argument("--precision", default="mixed", choices=["fp64", "fp64_tc", "mixed"])
     ap.add_argument("--digits", type=int, default=0)
     args = ap.parse_args()
     w = WORKLOADS[args.workload]

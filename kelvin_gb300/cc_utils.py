@@ -141,8 +141,9 @@ class DeviceSolver(object):
             pass
 
 
-def iterate(solver, conv_options, method="CCSD"):
-    """The loop of cc_utils.py:131-173 on a DeviceSolver; returns Eold."""
+def iterate(solver, conv_options, method="CCSD", min_iter=0):
+    """The loop of cc_utils.py:131-173 on a DeviceSolver; returns Eold.
+    ``min_iter`` forces at least that many sweeps (refinement)."""
     tbeg = time.time()
     ethresh = conv_options["econv"]
     tthresh = conv_options["tconv"]
@@ -151,7 +152,7 @@ def iterate(solver, conv_options, method="CCSD"):
     converged = False
     Eold = 888888888.888888888
     i = 0
-    while i < max_iter and not converged:
+    while i < max_iter and (not converged or i < min_iter):
         E, res = solver.step(alpha)
         logging.info(' %2d  %.10f   %.4E' % (i + 1, E, res))
         i += 1

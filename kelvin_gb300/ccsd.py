@@ -28,7 +28,7 @@ class ccsd(object):
     def __init__(self, sys, T=0.0, mu=0.0, iprint=0, singles=True, econv=1e-8,
                  tconv=None, max_iter=40, damp=0.0, ngrid=10, realtime=False,
                  athresh=0.0, quad='lin', rt_iter="all", precision='fp64',
-                 digits=None, device=0, ctx=None):
+                 digits=None, refine_sweeps=2, device=0, ctx=None):
         self.T = T
         self.mu = mu
         self.finite_T = T != 0
@@ -47,6 +47,9 @@ class ccsd(object):
             raise Exception("Unrecognized precision: {}".format(precision))
         self.precision = precision
         self.digits = digits if digits is not None else PRECISIONS[precision][1]
+        # mixed form: sweeps re-evaluated with FP64-accurate contractions once
+        # the few-digit iteration has converged (0: none)
+        self.refine_sweeps = refine_sweeps
         if not sys.verify(self.T, self.mu):
             raise Exception("Sytem temperature inconsistent with CC temp")
         if not self.finite_T:
@@ -99,6 +102,18 @@ class ccsd(object):
         Eccn = iterate(solver, conv, "CCSD")
         self.iterations = solver.iterations
         self.converged = solver.converged
+        self.iterations_refine = 0
+        if self.precision == 'mixed' and self.refine_sweeps > 0:
+            # FP64-accurate refinement: re-evaluate the update with seven digit
+            # levels from the low-precision fixed point
+            self.omega_low = Eccn
+            self.ctx.set_precision(_lib.PREC_FP64_TC, 7)
+            try:
+                Eccn = iterate(solver, conv, "CCSD", min_iter=self.refine_sweeps)
+            finally:
+                self.ctx.set_precision(prec, digits)
+            self.iterations_refine = solver.iterations
+            self.converged = solver.converged
         self.T1, self.T2 = solver.amplitudes()
         self.G0 = E0
         self.G1 = E1

@@ -161,3 +161,4 @@ int kv_stanton(kvft_ctx *ctx, int nb, int nv, int no,
                const double *t1, const double *t2, double fac, double *T1,
                double *T2);
 size_t kv_stanton_workspace(int nb, int nv, int no);
+size_t kv_chunk_bytes_per_tau(kvft_ctx *ctx, int nv, int no);

@@ -136,6 +136,7 @@ int seed_neg(kvft_ctx *ctx, int nb, long long count, const double *blk, double *
 struct kvft_solver {
     kvft_ctx *ctx = nullptr;
     int nv = 0, no = 0, ng = 0, chunk = 1;
+    int chunk_prec = -1;        // precision/digits the chunk was sized for
     double beta = 0, mu = 0;
     double *eps = nullptr, *sfo = nullptr, *sfv = nullptr;   // orbital-energy form
     double *D1 = nullptr, *D2 = nullptr;                     // explicit-denominator form
@@ -198,19 +199,25 @@ int upload_grid(kvft_solver *s, const double *ti, const double *g, const double 
     return KVFT_OK;
 }
 
+// tau points per Stanton call: workspace plus (tensor-core precisions) digit
+// planes of two operands must fit in 60% of the memory not held by the solver
 int pick_chunk(kvft_solver *s) {
     size_t fr = 0, tot = 0;
     KV_CHECK(s->ctx, cudaMemGetInfo(&fr, &tot));
-    size_t per = kv_stanton_workspace(1, s->nv, s->no);
-    size_t budget = (size_t)(0.6 * (double)fr);
+    size_t held = 0;
+    for (auto &kv : s->ctx->scratch) held += kv.second.second;
+    size_t per = kv_chunk_bytes_per_tau(s->ctx, s->nv, s->no);
+    size_t budget = (size_t)(0.6 * (double)(fr + held));
     long long c = per ? (long long)(budget / per) : s->ng;
     s->chunk = (int)std::max(1LL, std::min((long long)s->ng, c));
+    s->chunk_prec = s->ctx->precision * 16 + s->ctx->digits;
     return KVFT_OK;
 }
 
 // tbar = -F.vo - R1, -I.vvoo - R2 for all tau points
 int form_tbar(kvft_solver *s) {
     kvft_ctx *ctx = s->ctx;
+    if (s->chunk_prec != ctx->precision * 16 + ctx->digits) KV_TRY(pick_chunk(s));
     const long long n1 = s->s1(), n2 = s->s2();
     KV_TRY(seed_neg(ctx, s->ng, n1, s->F[2], s->T1b));
     KV_TRY(seed_neg(ctx, s->ng, n2, s->I[3], s->T2b));
@@ -520,8 +527,11 @@ int kvft_ccsd_stanton(kvft_ctx *ctx, int ng, int nv, int no, const double *const
     KV_TRY(seed_neg(ctx, ng, s2, I[3], T2b));
     size_t fr = 0, tot = 0;
     KV_CHECK(ctx, cudaMemGetInfo(&fr, &tot));
-    size_t per = kv_stanton_workspace(1, nv, no);
-    int chunk = (int)std::max<long long>(1, std::min<long long>(ng, (long long)(0.6 * fr / per)));
+    size_t held = 0;
+    for (auto &kv : ctx->scratch) held += kv.second.second;
+    size_t per = kv_chunk_bytes_per_tau(ctx, nv, no);
+    int chunk = (int)std::max<long long>(
+        1, std::min<long long>(ng, (long long)(0.6 * (double)(fr + held) / per)));
     for (int y0 = 0; y0 < ng; y0 += chunk) {
         int nb = std::min(chunk, ng - y0);
         KV_TRY(kv_stanton(ctx, nb, nv, no, F, I, T1old + y0 * s1, T2old + y0 * s2, -1.0,

@@ -77,6 +77,19 @@ size_t kv_stanton_workspace(int nb, int nv, int no) {
     return ws_per_tau(nv, no) * (size_t)nb * sizeof(double);
 }
 
+// Device bytes one tau point of a Stanton call needs: the workspace and, on
+// the tensor-core path, BF16 digit planes of two n^4-sized operands.
+size_t kv_chunk_bytes_per_tau(kvft_ctx *ctx, int nv, int no) {
+    size_t per = kv_stanton_workspace(1, nv, no);
+    if (ctx->precision != KVFT_PREC_FP64) {
+        const size_t big = std::max(std::max((size_t)nv * nv * nv * nv, (size_t)no * no * no * no),
+                                    (size_t)nv * nv * no * no);
+        const size_t S = (size_t)std::min(ctx->digits - 1, 6);
+        per += 2 * S * 2 * big;
+    }
+    return per;
+}
+
 int kv_stanton(kvft_ctx *ctx, int nb, int nv, int no, const double *const F[4],
                const double *const I[9], const double *t1, const double *t2,
                double fac, double *T1, double *T2) {

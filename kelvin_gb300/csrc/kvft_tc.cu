@@ -402,25 +402,59 @@ struct PackView {
     long long bst;
 };
 
-constexpr int EXP_SEG = 2048;   // K elements reduced by one warp
+// Operand tiles of 32 rows x 64 k go through shared memory so that global
+// reads are coalesced along whichever operand index is contiguous in memory
+// (the row index for some permuted views, k for others) and plane writes are
+// coalesced along k.
+constexpr int PT_R = 32, PT_K = 64;
 
-__global__ void pack_exp_kernel(PackView v, int R, int K, int nseg, int *__restrict__ ex) {
-    const int b = blockIdx.y;
-    const int lane = threadIdx.x % 32;
-    const long long nwarps = (long long)gridDim.x * blockDim.x / 32;
-    for (long long item = (blockIdx.x * (long long)blockDim.x + threadIdx.x) / 32;
-         item < (long long)R * nseg; item += nwarps) {
-        const int row = (int)(item / nseg), sg = (int)(item % nseg);
-        const double *base = v.p + (long long)b * v.bst + v.r.off(row);
-        const int kend = min(K, (sg + 1) * EXP_SEG);
+__device__ __forceinline__ void load_tile(const PackView &v, int b, int r0, int k0, int R, int K,
+                                          bool rows_fast,
+                                          unsigned long long (*tile)[PT_K + 1]) {
+    const int tx = threadIdx.x % 32, ty = threadIdx.x / 32;
+    const double *base = v.p + (long long)b * v.bst;
+    if (rows_fast) {
+        const int row = r0 + tx;
+        const long long ro = (row < R) ? v.r.off(row) : 0;
+        for (int kk = ty; kk < PT_K; kk += 8) {
+            const int k = k0 + kk;
+            tile[tx][kk] =
+                (row < R && k < K) ? (unsigned long long)__double_as_longlong(base[ro + v.c.off(k)])
+                                   : 0ull;
+        }
+    } else {
+        for (int rr = ty; rr < PT_R; rr += 8) {
+            const int row = r0 + rr;
+            const long long ro = (row < R) ? v.r.off(row) : 0;
+            for (int h = 0; h < 2; h++) {
+                const int k = k0 + tx + 32 * h;
+                tile[rr][tx + 32 * h] =
+                    (row < R && k < K)
+                        ? (unsigned long long)__double_as_longlong(base[ro + v.c.off(k)])
+                        : 0ull;
+            }
+        }
+    }
+}
+
+// raw row exponents: max binary exponent over each tile row, atomicMax'ed
+__global__ void __launch_bounds__(256)
+pack_exp_kernel(PackView v, int R, int K, int rows_fast, int *__restrict__ ex) {
+    __shared__ unsigned long long tile[PT_R][PT_K + 1];
+    const int b = blockIdx.z, r0 = blockIdx.y * PT_R, k0 = blockIdx.x * PT_K;
+    load_tile(v, b, r0, k0, R, K, rows_fast, tile);
+    __syncthreads();
+    const int lane = threadIdx.x % 32, w = threadIdx.x / 32;
+    for (int rr = w; rr < PT_R; rr += 8) {
         int emax = -2000;
-        for (int k = sg * EXP_SEG + lane; k < kend; k += 32) {
-            const unsigned long long bits = __double_as_longlong(base[v.c.off(k)]);
+        for (int h = 0; h < 2; h++) {
+            const unsigned long long bits = tile[rr][lane + 32 * h];
             if ((bits & 0x7FFFFFFFFFFFFFFFull) != 0)
                 emax = max(emax, (int)((bits >> 52) & 0x7FF) - 1023);
         }
         for (int o = 16; o > 0; o >>= 1) emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, o));
-        if (lane == 0 && emax > -2000) atomicMax(&ex[(long long)b * R + row], emax);
+        const int row = r0 + rr;
+        if (lane == 0 && emax > -2000 && row < R) atomicMax(&ex[(long long)b * R + row], emax);
     }
 }
 
@@ -450,29 +484,33 @@ __device__ __forceinline__ void digits_of(unsigned long long bits, int e, int S,
         for (int s = 0; s < S; s++) d[s] = -d[s];
 }
 
-// planes[b][s][row][k] (row stride ld) = d_s 2^-7s, two k per thread
+// planes[b][s][row][k] (row stride ld) = d_s 2^-7s; each thread packs two k
 template <int S>
-__global__ void pack_digits_kernel(PackView v, int R, int K, int ld,
-                                   const int *__restrict__ ex, __nv_bfloat16 *__restrict__ out) {
-    const int b = blockIdx.y;
+__global__ void __launch_bounds__(256)
+pack_digits_kernel(PackView v, int R, int K, int ld, int rows_fast, const int *__restrict__ ex,
+                   __nv_bfloat16 *__restrict__ out) {
+    __shared__ unsigned long long tile[PT_R][PT_K + 1];
+    const int b = blockIdx.z, r0 = blockIdx.y * PT_R, k0 = blockIdx.x * PT_K;
+    load_tile(v, b, r0, k0, R, K, rows_fast, tile);
+    __syncthreads();
     const size_t plane = (size_t)R * ld;
-    for (int row = blockIdx.x; row < R; row += gridDim.x) {
-        __nv_bfloat16 *ob = out + (size_t)b * S * plane + (size_t)row * ld;
+    const int tx = threadIdx.x % 32, ty = threadIdx.x / 32;
+    const int k = k0 + 2 * tx;
+    if (k >= K) return;
+    for (int rr = ty; rr < PT_R; rr += 8) {
+        const int row = r0 + rr;
+        if (row >= R) break;
         const int e = exp_of(ex[(long long)b * R + row]);
-        const double *base = v.p + (long long)b * v.bst + v.r.off(row);
-        for (int k = 2 * threadIdx.x; k < K; k += 2 * blockDim.x) {
-            int d0[MAXS], d1[MAXS];
-            digits_of(__double_as_longlong(base[v.c.off(k)]), e, S, d0);
-            if (k + 1 < K) digits_of(__double_as_longlong(base[v.c.off(k + 1)]), e, S, d1);
-            else
-                for (int s = 0; s < MAXS; s++) d1[s] = 0;
-            for (int s = 0; s < S; s++) {
-                // P_s = d_s 2^-7s (pre-scaled; exact in BF16)
-                __nv_bfloat162 w;
-                w.x = __float2bfloat16_rn(ldexpf((float)d0[s], -7 * s));
-                w.y = __float2bfloat16_rn(ldexpf((float)d1[s], -7 * s));
-                *reinterpret_cast<__nv_bfloat162 *>(ob + (size_t)s * plane + k) = w;
-            }
+        int d0[MAXS], d1[MAXS];
+        digits_of(tile[rr][2 * tx], e, S, d0);
+        digits_of(tile[rr][2 * tx + 1], e, S, d1);    // zero beyond K (tile fill)
+        __nv_bfloat16 *ob = out + (size_t)b * S * plane + (size_t)row * ld + k;
+#pragma unroll
+        for (int s = 0; s < S; s++) {
+            __nv_bfloat162 w2;
+            w2.x = __float2bfloat16_rn(ldexpf((float)d0[s], -7 * s));
+            w2.y = __float2bfloat16_rn(ldexpf((float)d1[s], -7 * s));
+            *reinterpret_cast<__nv_bfloat162 *>(ob + (size_t)s * plane) = w2;
         }
     }
 }
@@ -538,30 +576,25 @@ int pack(kvft_ctx *ctx, const char *key, const PackView &v, int R, int K, int nb
     if (nb > 65535) return kv_fail(ctx, KVFT_EINVAL, "pack: batch too large");
     KvProfScope prof(ctx, KV_CAT_PACK, 8.0 * nb * (double)R * K + (double)nb * S * plane_bytes);
     KV_CHECK(ctx, cudaMemsetAsync(out->ex, 0x80, (size_t)nb * R * sizeof(int), ctx->stream));
-    {
-        const int nseg = (K + EXP_SEG - 1) / EXP_SEG;
-        const long long warps = (long long)R * nseg;
-        const int blocks = (int)std::min<long long>((warps * 32 + 255) / 256, ctx->sm_count * 32);
-        pack_exp_kernel<<<dim3(blocks, nb), 256, 0, ctx->stream>>>(v, R, K, nseg, out->ex);
-        KV_TRY(kv_launch_check(ctx, "pack_exp"));
-    }
-    {
-        const int threads = 32 * std::max(1, std::min(8, (K / 2 + 31) / 32));
-        const int blocks = std::min(R, ctx->sm_count * 64);
-        const dim3 g(blocks, nb);
-        switch (S) {
+    // coalesce global reads along the contiguous index
+    const int rows_fast = (v.r.st[2] == 1 && v.c.st[2] != 1) ? 1 : 0;
+    const long long rtiles = (R + PT_R - 1) / PT_R;
+    if (rtiles > 65535) return kv_fail(ctx, KVFT_EINVAL, "pack: too many rows");
+    const dim3 g((K + PT_K - 1) / PT_K, (unsigned)rtiles, nb);
+    pack_exp_kernel<<<g, 256, 0, ctx->stream>>>(v, R, K, rows_fast, out->ex);
+    KV_TRY(kv_launch_check(ctx, "pack_exp"));
+    switch (S) {
 #define KV_PACK_CASE(s_)                                                                    \
     case s_:                                                                                \
-        pack_digits_kernel<s_><<<g, threads, 0, ctx->stream>>>(v, R, K, ld, out->ex,        \
-                                                               out->planes);                \
+        pack_digits_kernel<s_><<<g, 256, 0, ctx->stream>>>(v, R, K, ld, rows_fast, out->ex, \
+                                                           out->planes);                    \
         break;
-            KV_PACK_CASE(1) KV_PACK_CASE(2) KV_PACK_CASE(3) KV_PACK_CASE(4) KV_PACK_CASE(5)
-            KV_PACK_CASE(6)
+        KV_PACK_CASE(1) KV_PACK_CASE(2) KV_PACK_CASE(3) KV_PACK_CASE(4) KV_PACK_CASE(5)
+        KV_PACK_CASE(6)
 #undef KV_PACK_CASE
-        default: return kv_fail(ctx, KVFT_EINVAL, "pack: digit count out of range");
-        }
-        KV_TRY(kv_launch_check(ctx, "pack_digits"));
+    default: return kv_fail(ctx, KVFT_EINVAL, "pack: digit count out of range");
     }
+    KV_TRY(kv_launch_check(ctx, "pack_digits"));
     return KVFT_OK;
 }
 
@@ -576,6 +609,14 @@ int kv_gemm_tc(kvft_ctx *ctx, int M, int N, int K, int batch, double alpha, cons
     if (D < 2 || D > MAXS + 1) return kv_fail(ctx, KVFT_EINVAL, "tensor-core digits out of range");
     if (M <= 0 || N <= 0 || batch <= 0) return KVFT_OK;
     if (K <= 0) return kv_gemm_f64(ctx, M, N, K, batch, alpha, A, B, beta, C);
+    if (M < N) {
+        // C^T = B^T A^T: the larger extent goes to the 128 TMEM lanes, which are
+        // the epilogue's rows (a small M would leave most epilogue warps idle)
+        const KMat At{B.p, B.c, B.r, B.bst};
+        const KMat Bt{A.p, A.c, A.r, A.bst};
+        const KOut Ct{C.p, C.c, C.r, C.bst};
+        return kv_gemm_tc(ctx, N, M, K, batch, alpha, At, Bt, beta, Ct, digits);
+    }
     const int nbA = A.bst ? batch : 1, nbB = B.bst ? batch : 1;
     Packed pa, pb;
     KV_TRY(pack(ctx, "tc_pack_a", PackView{A.p, A.r, A.c, A.bst}, M, K, nbA, S, &pa));
