@@ -51,6 +51,7 @@ WORKLOADS = {
                         "ng=10, damping 0.5, econv 1e-10"),
 }
 ITERS_FALLBACK = 30
+REFINE = 2          # FP64-accurate refinement sweeps that end a mixed solve
 
 
 def load_peaks():
@@ -227,7 +228,7 @@ def run_reference(args, w):
 def run_gpu(args, w):
     ws, rank, local = dist_setup()
     from kelvin_gb300 import _lib, ccsd
-    from kelvin_gb300.cc_utils import DeviceSolver, iterate
+    from kelvin_gb300.cc_utils import DeviceSolver
     from kelvin_gb300.quadrature import ft_quad
 
     ctx = _lib.context(local)
@@ -252,7 +253,8 @@ def run_gpu(args, w):
     def one_step():
         if per_solve:
             solver.guess(1)
-            return iterate(solver, conv), solver.iterations
+            E, info = ccsd.converge(solver, ctx, conv, args.precision, digits, REFINE)
+            return E, info["iterations"] + info["iterations_refine"]
         return solver.step(w["damp"])[0], 1
 
     for _ in range(args.warmup):
@@ -288,6 +290,9 @@ def run_gpu(args, w):
         ctx.sync()
         fp64_step_ms = ctx.elapsed_ms(4, 5)
         ctx.set_precision(prec, digits)
+        if not per_solve:
+            # a mixed solve = iterations at few digits + FP64-accurate refinement sweeps
+            value = ws / ((iters * step_ms + REFINE * fp64_step_ms) / 1e3)
     solver.close()
 
     # ---- end to end through the public API (e2e) -----------------------------
@@ -298,7 +303,8 @@ def run_gpu(args, w):
     for _ in range(1 if not per_solve else args.steps):
         cc = ccsd.ccsd(sysobj, T=sysobj.T, mu=sysobj.mu, max_iter=(
             w["max_iter"] if per_solve else args.steps), damp=w["damp"], ngrid=ng,
-            econv=w["econv"], precision=args.precision, digits=digits, refine_sweeps=0, ctx=ctx)
+            econv=w["econv"], precision=args.precision, digits=digits,
+            refine_sweeps=REFINE if per_solve else 0, ctx=ctx)
         cc.run()
         e2e_iters = cc.iterations
         cc.release()

@@ -167,6 +167,7 @@ class Context(object):
     def set_precision(self, precision, digits=7):
         self.check(self.L.kvft_set_precision(self.h, int(precision), int(digits)),
                    "kvft_set_precision")
+        self._precision = (int(precision), int(digits))
 
     def sync(self):
         self.check(self.L.kvft_sync(self.h), "kvft_sync")

@@ -141,29 +141,41 @@ class DeviceSolver(object):
             pass
 
 
-def iterate(solver, conv_options, method="CCSD", min_iter=0):
+def iterate(solver, conv_options, method="CCSD", stall=0, quiet=False):
     """The loop of cc_utils.py:131-173 on a DeviceSolver; returns Eold.
-    ``min_iter`` forces at least that many sweeps (refinement)."""
+
+    ``stall`` > 0 also stops when the residual has not fallen below 0.9 of
+    its best value for that many sweeps (a low-precision noise floor);
+    ``quiet`` drops the non-convergence warning (fixed sweep counts)."""
     tbeg = time.time()
     ethresh = conv_options["econv"]
     tthresh = conv_options["tconv"]
     max_iter = conv_options["max_iter"]
     alpha = conv_options["damp"]
     converged = False
+    stalled = False
+    best, since = float("inf"), 0
     Eold = 888888888.888888888
     i = 0
-    while i < max_iter and (not converged or i < min_iter):
+    while i < max_iter and not converged and not stalled:
         E, res = solver.step(alpha)
         logging.info(' %2d  %.10f   %.4E' % (i + 1, E, res))
         i += 1
         if numpy.abs(E - Eold) < ethresh and res < tthresh:
             converged = True
+        if stall:
+            if res < 0.9 * best:
+                best, since = res, 0
+            else:
+                since += 1
+                stalled = since >= stall
         Eold = E
-    if not converged:
+    if not converged and not stalled and not quiet:
         logging.warning("{} did not converge!".format(method))
     logging.info("Total {} time: {:.4f} s".format(method, time.time() - tbeg))
     solver.iterations = i
     solver.converged = converged
+    solver.stalled = stalled
     return Eold
 
 

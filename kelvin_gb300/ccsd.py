@@ -22,6 +22,42 @@ PRECISIONS = {'fp64': (_lib.PREC_FP64, 7), 'fp64_tc': (_lib.PREC_FP64_TC, 7),
               'mixed': (_lib.PREC_MIXED, 3)}
 
 
+def converge(solver, ctx, conv, precision, digits, refine_sweeps=2):
+    """Iterate a DeviceSolver to convergence; returns (Omega_cc, info).
+
+    FP64 forms use Kelvin's test (|dE| < econv and res < tconv).  The mixed
+    form's few-digit update is a slightly discontinuous map (digit rounding),
+    so its iteration settles at a noise floor instead of meeting econv: it
+    stops at Kelvin's test or when the residual has stopped falling for three
+    sweeps, then runs `refine_sweeps` sweeps with FP64-accurate contractions
+    from that point."""
+    if precision != 'mixed':
+        E = iterate(solver, conv, "CCSD")
+        return E, {"iterations": solver.iterations, "iterations_refine": 0,
+                   "converged": solver.converged, "omega_low": None}
+    E_low = iterate(solver, conv, "CCSD", stall=3)
+    info = {"iterations": solver.iterations, "iterations_refine": 0,
+            "converged": solver.converged or getattr(solver, "stalled", False),
+            "omega_low": E_low}
+    E = E_low
+    if refine_sweeps > 0:
+        prec = ctx_precision(ctx)
+        ctx.set_precision(_lib.PREC_FP64_TC, 7)
+        try:
+            ref = dict(conv)
+            ref["max_iter"] = refine_sweeps
+            E = iterate(solver, ref, "CCSD refinement", quiet=True)
+        finally:
+            ctx.set_precision(*prec)
+        info["iterations_refine"] = solver.iterations
+    return E, info
+
+
+def ctx_precision(ctx):
+    """(precision, digits) last set on a context through set_precision."""
+    return getattr(ctx, "_precision", (_lib.PREC_FP64, 7))
+
+
 class ccsd(object):
     """Coupled cluster singles and doubles (CCSD) driver, T > 0."""
 
@@ -99,21 +135,12 @@ class ccsd(object):
         logging.info('MP2 Energy: {:.10f}'.format(E2))
         conv = {"econv": self.econv, "tconv": self.tconv, "max_iter": self.max_iter,
                 "damp": self.damp}
-        Eccn = iterate(solver, conv, "CCSD")
-        self.iterations = solver.iterations
-        self.converged = solver.converged
-        self.iterations_refine = 0
-        if self.precision == 'mixed' and self.refine_sweeps > 0:
-            # FP64-accurate refinement: re-evaluate the update with seven digit
-            # levels from the low-precision fixed point
-            self.omega_low = Eccn
-            self.ctx.set_precision(_lib.PREC_FP64_TC, 7)
-            try:
-                Eccn = iterate(solver, conv, "CCSD", min_iter=self.refine_sweeps)
-            finally:
-                self.ctx.set_precision(prec, digits)
-            self.iterations_refine = solver.iterations
-            self.converged = solver.converged
+        Eccn, info = converge(solver, self.ctx, conv, self.precision, digits,
+                              self.refine_sweeps)
+        self.iterations = info["iterations"]
+        self.iterations_refine = info["iterations_refine"]
+        self.converged = info["converged"]
+        self.omega_low = info["omega_low"]
         self.T1, self.T2 = solver.amplitudes()
         self.G0 = E0
         self.G1 = E1

@@ -17,6 +17,20 @@ struct Dims4 {
     long long sbst, dbst;
 };
 
+// ---- antisymmetric pair compression ------------------------------------------
+// A tensor antisymmetric in an index pair is stored over p < q only; pair
+// index x = p (2n - p - 1) / 2 + (q - p - 1).
+__device__ __forceinline__ int pair_start(int p, int n) { return p * (2 * n - p - 1) / 2; }
+
+__device__ __forceinline__ void pair_of(int x, int n, int &p, int &q) {
+    const float b = 2.0f * n - 1.0f;
+    p = (int)((b - sqrtf(b * b - 8.0f * x)) * 0.5f);
+    p = max(0, min(p, n - 2));
+    while (p > 0 && pair_start(p, n) > x) p--;
+    while (p < n - 2 && pair_start(p + 1, n) <= x) p++;
+    q = x - pair_start(p, n) + p + 1;
+}
+
 __global__ void axpby4_kernel(long long total, Dims4 g, double alpha,
                               const double *__restrict__ src, double beta,
                               double *__restrict__ dst) {
@@ -77,6 +91,7 @@ __global__ void assemble_t2_kernel(long long total, int nv, int no, double fac,
                                    const double *__restrict__ Zab,
                                    const double *__restrict__ Zij,
                                    const double *__restrict__ Zabij,
+                                   const double *__restrict__ Lc,
                                    double *__restrict__ T2) {
     const long long s4 = (long long)nv * nv * no * no;
     const long long sa = (long long)nv * no * no, sb = (long long)no * no, si = no;
@@ -97,6 +112,15 @@ __global__ void assemble_t2_kernel(long long total, int nv, int no, double fac,
         if (Zab) v += Zab[abij] - Zab[baij];
         if (Zij) v += Zij[abij] - Zij[abji];
         if (Zabij) v += Zabij[abij] - Zabij[baij] - Zabij[abji] + Zabij[baji];
+        if (Lc && a != b && i != j) {
+            // ladder terms, stored over a<b, i<j: antisymmetric expansion
+            const int pv = nv * (nv - 1) / 2, po = no * (no - 1) / 2;
+            const int p = min(a, b), q = max(a, b), r = min(i, j), t = max(i, j);
+            const double sg = ((a < b) == (i < j)) ? 1.0 : -1.0;
+            v += sg * Lc[y * (long long)pv * po +
+                         (long long)(pair_start(p, nv) + q - p - 1) * po +
+                         pair_start(r, no) + t - r - 1];
+        }
         T2[x] += fac * v;
     }
 }
@@ -107,6 +131,57 @@ __global__ void bcast_kernel(long long total, long long count,
     for (long long x = blockIdx.x * (long long)blockDim.x + threadIdx.x; x < total;
          x += (long long)gridDim.x * blockDim.x)
         dst[x] = src[x % count];
+}
+
+// tau_c[y][(e<f)][(i<j)] = t2[y,e,f,i,j] + t1[y,e,i] t1[y,f,j] - t1[y,f,i] t1[y,e,j]
+__global__ void make_tau_pairs_kernel(long long total, int nv, int no, int pv, int po,
+                                      const double *__restrict__ t1,
+                                      const double *__restrict__ t2,
+                                      double *__restrict__ out) {
+    const long long per = (long long)pv * po;
+    const long long s4 = (long long)nv * nv * no * no;
+    for (long long x = blockIdx.x * (long long)blockDim.x + threadIdx.x; x < total;
+         x += (long long)gridDim.x * blockDim.x) {
+        const long long y = x / per;
+        const long long r = x - y * per;
+        int e, f, i, j;
+        pair_of((int)(r / po), nv, e, f);
+        pair_of((int)(r % po), no, i, j);
+        const double *u = t1 + y * nv * no;
+        const long long off = y * s4 + (((long long)e * nv + f) * no + i) * no + j;
+        out[x] = t2[off] + u[e * no + i] * u[f * no + j] - u[f * no + i] * u[e * no + j];
+    }
+}
+
+struct PairGather {
+    int n1, n2, P1, P2;          // pair ranges: (p<q) over n1 rows, (r<s) over n2 columns
+    const double *A;             // shared term, ca * A[p,q,r,s]
+    long long sa[4];
+    double ca;
+    const double *B;             // per-batch terms c1 B[p,q,r,s] + c2 B[with strides sb2]
+    long long sb1[4], sb2[4], bst;
+    double c1, c2;
+};
+
+__global__ void pair_gather_kernel(long long total, PairGather g, double *__restrict__ out) {
+    const long long per = (long long)g.P1 * g.P2;
+    for (long long x = blockIdx.x * (long long)blockDim.x + threadIdx.x; x < total;
+         x += (long long)gridDim.x * blockDim.x) {
+        const long long y = x / per;
+        const long long r = x - y * per;
+        int p, q, a, b;
+        pair_of((int)(r / g.P2), g.n1, p, q);
+        pair_of((int)(r % g.P2), g.n2, a, b);
+        double v = 0.0;
+        if (g.A) v = g.ca * g.A[p * g.sa[0] + q * g.sa[1] + a * g.sa[2] + b * g.sa[3]];
+        if (g.B) {
+            const double *Bb = g.B + y * g.bst;
+            v += g.c1 * Bb[p * g.sb1[0] + q * g.sb1[1] + a * g.sb1[2] + b * g.sb1[3]];
+            if (g.c2 != 0.0)
+                v += g.c2 * Bb[p * g.sb2[0] + q * g.sb2[1] + a * g.sb2[2] + b * g.sb2[3]];
+        }
+        out[x] = v;
+    }
 }
 
 }  // namespace
@@ -153,13 +228,50 @@ int kv_make_wmbej_tmp(kvft_ctx *ctx, int batch, int nv, int no,
 
 int kv_assemble_t2(kvft_ctx *ctx, int batch, int nv, int no, double fac,
                    const double *Zab, const double *Zij, const double *Zabij,
-                   double *T2) {
+                   const double *Lc, double *T2) {
     long long total = (long long)batch * nv * nv * no * no;
     if (total == 0) return KVFT_OK;
-    KvProfScope prof(ctx, KV_CAT_ELEM, 8.0 * total * 5);
+    KvProfScope prof(ctx, KV_CAT_ELEM, 8.0 * total * 6);
     assemble_t2_kernel<<<grid_for(ctx, total, 256), 256, 0, ctx->stream>>>(
-        total, nv, no, fac, Zab, Zij, Zabij, T2);
+        total, nv, no, fac, Zab, Zij, Zabij, Lc, T2);
     return kv_launch_check(ctx, "assemble_t2");
+}
+
+int kv_make_tau_pairs(kvft_ctx *ctx, int batch, int nv, int no, const double *t1,
+                      const double *t2, double *out) {
+    const int pv = nv * (nv - 1) / 2, po = no * (no - 1) / 2;
+    long long total = (long long)batch * pv * po;
+    if (total == 0) return KVFT_OK;
+    KvProfScope prof(ctx, KV_CAT_ELEM, 16.0 * total);
+    make_tau_pairs_kernel<<<grid_for(ctx, total, 256), 256, 0, ctx->stream>>>(total, nv, no, pv,
+                                                                              po, t1, t2, out);
+    return kv_launch_check(ctx, "make_tau_pairs");
+}
+
+int kv_pair_gather(kvft_ctx *ctx, int batch, int n1, int n2, const double *A,
+                   const long long sa[4], double ca, const double *B, const long long sb1[4],
+                   double c1, const long long sb2[4], double c2, long long bst, double *out) {
+    PairGather g;
+    g.n1 = n1;
+    g.n2 = n2;
+    g.P1 = n1 * (n1 - 1) / 2;
+    g.P2 = n2 * (n2 - 1) / 2;
+    g.A = A;
+    g.ca = ca;
+    g.B = B;
+    g.c1 = c1;
+    g.c2 = c2;
+    g.bst = bst;
+    for (int k = 0; k < 4; k++) {
+        g.sa[k] = sa ? sa[k] : 0;
+        g.sb1[k] = sb1 ? sb1[k] : 0;
+        g.sb2[k] = sb2 ? sb2[k] : 0;
+    }
+    long long total = (long long)batch * g.P1 * g.P2;
+    if (total == 0) return KVFT_OK;
+    KvProfScope prof(ctx, KV_CAT_ELEM, 8.0 * total * (B ? 3 : 2));
+    pair_gather_kernel<<<grid_for(ctx, total, 256), 256, 0, ctx->stream>>>(total, g, out);
+    return kv_launch_check(ctx, "pair_gather");
 }
 
 int kv_bcast(kvft_ctx *ctx, int batch, size_t count, const double *src,

@@ -142,7 +142,15 @@ int kv_make_wmbej_tmp(kvft_ctx *ctx, int batch, int nv, int no,
 // T2 += fac * [Zab - P(ab) Zab + Zij - P(ij) Zij + (1 - P(ab))(1 - P(ij)) Zabij]
 int kv_assemble_t2(kvft_ctx *ctx, int batch, int nv, int no, double fac,
                    const double *Zab, const double *Zij, const double *Zabij,
-                   double *T2);
+                   const double *Lc, double *T2);
+// Antisymmetric pair compression (pairs p < q, x = p(2n-p-1)/2 + q-p-1):
+// tau_c[y][(e<f)][(i<j)] from t1, t2
+int kv_make_tau_pairs(kvft_ctx *ctx, int batch, int nv, int no, const double *t1,
+                      const double *t2, double *out);
+// out[y][(p<q) over n1][(r<s) over n2] = ca A[p,q,r,s] + c1 B[y][p,q,r,s] + c2 B[y](sb2)
+int kv_pair_gather(kvft_ctx *ctx, int batch, int n1, int n2, const double *A,
+                   const long long sa[4], double ca, const double *B, const long long sb1[4],
+                   double c1, const long long sb2[4], double c2, long long bst, double *out);
 // broadcast a tau-independent block over the batch: dst[b] = src
 int kv_bcast(kvft_ctx *ctx, int batch, size_t count, const double *src,
              double *dst);

@@ -6,14 +6,16 @@
 // views of the amplitude / integral tensors; tau-independent integrals are
 // shared across the batch (batch stride 0) and, where the other operand is per
 // tau point, the tau index is folded into the GEMM's N dimension so that one
-// launch covers the whole batch.  Ten n^6 flops per tau point remain:
-//   X     = <mn||ef> tau_ef^ij                 (folded over tau)
-//   T2   += 1/2 tau_ab^mn W'_mnij, W' = W_mnij + X/4   (the W_abef tau-tau
-//           term is carried by X, saving the explicit 1/4 tau <mn||ef> GEMM)
-//   T2   += 1/2 W'_abef tau_ef^ij, W'_abef = <ab||ef> - P(ab) t_m^b <am||ef>
-//   W_mbej -= <mn||ef> (t_jn^fb / 2 + t_j^f t_n^b)  (folded over tau)
-//   Z    += t_im^ae W_mbej, then T2 += P(ij)P(ab) Z
-// and about thirty n^5 terms.
+// launch covers the whole batch.  The n^6 work per tau point is
+//   X      = <mn||ef> tau_ef^ij                        (folded over tau)
+//   T2    += 1/2 tau_ab^mn W'_mnij, W' = W_mnij + X/4   (the W_abef tau-tau
+//            term is carried by X, saving the explicit 1/4 tau <mn||ef> GEMM)
+//   T2    += 1/2 W'_abef tau_ef^ij, W'_abef = <ab||ef> - P(ab) t_m^b <am||ef>
+//   W_mbej -= <mn||ef> (t_jn^fb / 2 + t_j^f t_n^b)     (folded over tau)
+//   Z      = t_im^ae W_mbej, then T2 += P(ij)P(ab) Z
+// where the first three run over antisymmetric index pairs p < q only
+// (n^6/4 flops each instead of 2 n^6), so 4.75 n^6 flops per tau point remain
+// besides about thirty n^5 terms.
 #include "kvft_internal.h"
 
 namespace {
@@ -34,15 +36,15 @@ inline KOut MO(double *p, KIdx r, KIdx c, long long bst) { return KOut{p, r, c, 
 // workspace layout (per tau point, doubles)
 struct WS {
     double *tau, *ttau, *Fae, *Fmi, *Fme, *Xbe, *Xmj, *Wmnij, *Wabef, *Wmbej,
-        *tmp4, *Q, *Zab, *Zij, *Zabij;
+        *tmp4, *Q, *Zab, *Zij, *Zabij, *Lc;
 };
 
 size_t ws_per_tau(long long v, long long o) {
     long long v2o2 = v * v * o * o, o4 = o * o * o * o, v4 = v * v * v * v;
     long long big = std::max(std::max(v4, o4), v2o2);
-    // tau ttau Wmbej Zab Zij Zabij (v2o2 each) + Wmnij (o4) + Wabef (v4)
+    // tau_c ttau Wmbej Zab Zij Zabij Lc (v2o2 each) + W'_mnij_c (o4) + W'_abef_c (v4)
     // + tmp4 (max) + Q (v o^3) + five small matrices
-    return (size_t)(6 * v2o2 + o4 + v4 + big + v * o * o * o + 2 * v * v + 3 * o * o + 2 * o * v);
+    return (size_t)(7 * v2o2 + o4 + v4 + big + v * o * o * o + 2 * v * v + 3 * o * o + 2 * o * v);
 }
 
 WS carve(double *base, int nb, long long v, long long o) {
@@ -57,6 +59,7 @@ WS carve(double *base, int nb, long long v, long long o) {
     w.Zab = take(v2o2);
     w.Zij = take(v2o2);
     w.Zabij = take(v2o2);
+    w.Lc = take(v2o2);
     w.Wmnij = take(o4);
     w.Wabef = take(v4);
     w.tmp4 = take(big);
@@ -109,8 +112,7 @@ int kv_stanton(kvft_ctx *ctx, int nb, int nv, int no, const double *const F[4],
     const int B = nb;
     const KIdx one = X1(1, 0);
 
-    // ---- tau, tau-tilde --------------------------------------------------
-    KV_TRY(kv_make_tau(ctx, B, nv, no, t1, t2, 1.0, w.tau));
+    // ---- tau-tilde (tau itself is only needed pair-compressed) --------------
     KV_TRY(kv_make_tau(ctx, B, nv, no, t1, t2, 0.5, w.ttau));
 
     // ---- F_ae ------------------------------------------------------------
@@ -180,47 +182,56 @@ int kv_stanton(kvft_ctx *ctx, int nb, int nv, int no, const double *const F[4],
                    MA(t2, X1(nv, vo2), X3(nv, oo, no, o, no, 1), v2o2),
                    MA(ooov, X3(nv, 1, no, vo, no, oo * v), X1(no, v), 0), 1.0, T1o));
 
-    // ---- W_mnij' = oooo + P(ij) ooov t1 + X/2 --------------------------------
-    KV_TRY(kv_bcast(ctx, B, o4, oooo, w.Wmnij));
-    // tmp[m,n,i,j] = ooov[m,n,i,e] t1[e,j]
-    KV_TRY(kv_gemm(ctx, no * no * no, no, nv, B, 1.0,
-                   MA(ooov, X3(no, oo * v, no, vo, no, v), X1(nv, 1), 0),
-                   MA(t1, X1(nv, o), X1(no, 1), vo), 0.0,
-                   MO(w.tmp4, X3(no, o * oo, no, oo, no, o), X1(no, 1), o4)));
-    {
-        int d[4] = {no, no, no, no};
-        long long s_id[4] = {o * oo, oo, o, 1}, s_tr[4] = {o * oo, oo, 1, o};
-        KV_TRY(kv_axpby4(ctx, B, d, 1.0, w.tmp4, s_id, o4, 1.0, w.Wmnij, s_id, o4));
-        KV_TRY(kv_axpby4(ctx, B, d, -1.0, w.tmp4, s_tr, o4, 1.0, w.Wmnij, s_id, o4));
+    // ---- ladder terms over antisymmetric pairs ---------------------------------
+    // tau, W'_mnij, W'_abef and <mn||ef> are antisymmetric in each index pair,
+    // so the three ladder contractions run over p < q only (8x fewer flops):
+    //   W'_c[mn,ij] = oooo + P(ij) ooov t1 + sum_{e<f} oovv[mn,ef] tau[ef,ij]
+    //   Lc[ab,ij]   = sum_{m<n} tau[ab,mn] W'_c[mn,ij] + sum_{e<f} W'_c[ab,ef] tau[ef,ij]
+    // (the 1/2 of each full-range sum cancels the factor 2 of the pair sum; the
+    // X/4 of W_mnij plus the tau <mn||ef>/4 of W_abef make the X/2 in W'_mnij),
+    // and T2 += fac Lc, expanded with signs, in the final assembly.
+    const int pv = nv * (nv - 1) / 2, po = no * (no - 1) / 2;
+    const long long pvo = (long long)pv * po, poo = (long long)po * po, pvv = (long long)pv * pv;
+    const bool ladders = pv > 0 && po > 0;
+    if (ladders) {
+        KV_TRY(kv_make_tau_pairs(ctx, B, nv, no, t1, t2, w.tau));      // tau_c[y][ef][ij]
+        void *oc = nullptr;
+        KV_TRY(kv_scratch(ctx, "oovv_pairs", sizeof(double) * (size_t)po * pv, &oc));
+        const long long sov[4] = {o * vv, vv, v, 1};
+        KV_TRY(kv_pair_gather(ctx, 1, no, nv, oovv, sov, 1.0, nullptr, nullptr, 0.0, nullptr,
+                              0.0, 0, (double *)oc));
+        // Z[m,n,i,j] = ooov[m,n,i,e] t1[e,j]
+        KV_TRY(kv_gemm(ctx, no * no * no, no, nv, B, 1.0,
+                       MA(ooov, X3(no, oo * v, no, vo, no, v), X1(nv, 1), 0),
+                       MA(t1, X1(nv, o), X1(no, 1), vo), 0.0,
+                       MO(w.tmp4, X3(no, o * oo, no, oo, no, o), X1(no, 1), o4)));
+        // W'_c = oooo + Z - Z^(ij)
+        const long long s4o[4] = {o * oo, oo, o, 1}, s4t[4] = {o * oo, oo, 1, o};
+        KV_TRY(kv_pair_gather(ctx, B, no, no, oooo, s4o, 1.0, w.tmp4, s4o, 1.0, s4t, -1.0, o4,
+                              w.Wmnij));
+        // W'_c += oovv_c tau_c   (M = mn pairs, K = ef pairs, N = (tau, ij pairs))
+        KV_TRY(kv_gemm(ctx, po, B * po, pv, 1, 1.0,
+                       MA((const double *)oc, X1(po, pv), X1(pv, 1), 0),
+                       MA(w.tau, X1(pv, po), X2(B, pvo, po, 1), 0), 1.0,
+                       MO(w.Wmnij, X1(po, po), X2(B, poo, po, 1), 0)));
+        // Lc = tau_c W'_c        (M = ab pairs, K = mn pairs, N = ij pairs)
+        KV_TRY(kv_gemm(ctx, pv, po, po, B, 1.0, MA(w.tau, X1(pv, po), X1(po, 1), pvo),
+                       MA(w.Wmnij, X1(po, po), X1(po, 1), poo), 0.0,
+                       MO(w.Lc, X1(pv, po), X1(po, 1), pvo)));
+        // Y[a,b,e,f] = t1[b,m] vovv[a,m,e,f]   (M=b, K=m, N=(a,e,f))
+        KV_TRY(kv_gemm(ctx, nv, nv * nv * nv, no, B, 1.0,
+                       MA(t1, X1(nv, o), X1(no, 1), vo),
+                       MA(vovv, X1(no, vv), X3(nv, o * vv, nv, v, nv, 1), 0), 0.0,
+                       MO(w.tmp4, X1(nv, vv), X3(nv, v * vv, nv, v, nv, 1), v4)));
+        // W'_abef_c = vvvv - Y + Y^(ab)
+        const long long s4v[4] = {v * vv, vv, v, 1}, s4s[4] = {vv, v * vv, v, 1};
+        KV_TRY(kv_pair_gather(ctx, B, nv, nv, vvvv, s4v, 1.0, w.tmp4, s4v, -1.0, s4s, 1.0, v4,
+                              w.Wabef));
+        // Lc += W'_abef_c tau_c   (M = ab pairs, K = ef pairs, N = ij pairs)
+        KV_TRY(kv_gemm(ctx, pv, po, pv, B, 1.0, MA(w.Wabef, X1(pv, pv), X1(pv, 1), pvv),
+                       MA(w.tau, X1(pv, po), X1(po, 1), pvo), 1.0,
+                       MO(w.Lc, X1(pv, po), X1(po, 1), pvo)));
     }
-    // X: + 1/2 oovv[m,n,e,f] tau[e,f,i,j]   (M=(m,n), K=(e,f), N=(tau,i,j))
-    KV_TRY(kv_gemm(ctx, no * no, B * no * no, nv * nv, 1, 0.5,
-                   MA(oovv, X2(no, o * vv, no, vv), X2(nv, v, nv, 1), 0),
-                   MA(w.tau, X2(nv, vo2, nv, oo), X3(B, v2o2, no, o, no, 1), 0), 1.0,
-                   MO(w.Wmnij, X2(no, o * oo, no, oo), X3(B, o4, no, o, no, 1), 0)));
-    // T2 += fac/2 tau[a,b,m,n] Wmnij[m,n,i,j]
-    const KOut T2o = MO(T2, X2(nv, vo2, nv, oo), X2(no, o, no, 1), v2o2);
-    KV_TRY(kv_gemm(ctx, nv * nv, no * no, no * no, B, 0.5 * fac,
-                   MA(w.tau, X2(nv, vo2, nv, oo), X2(no, o, no, 1), v2o2),
-                   MA(w.Wmnij, X2(no, o * oo, no, oo), X2(no, o, no, 1), o4), 1.0, T2o));
-
-    // ---- W_abef' = vvvv - P(ab) t1[b,m] vovv[a,m,e,f] ------------------------
-    KV_TRY(kv_bcast(ctx, B, v4, vvvv, w.Wabef));
-    // tmp[a,b,e,f] = t1[b,m] vovv[a,m,e,f]   (M=b, K=m, N=(a,e,f))
-    KV_TRY(kv_gemm(ctx, nv, nv * nv * nv, no, B, 1.0,
-                   MA(t1, X1(nv, o), X1(no, 1), vo),
-                   MA(vovv, X1(no, vv), X3(nv, o * vv, nv, v, nv, 1), 0), 0.0,
-                   MO(w.tmp4, X1(nv, vv), X3(nv, v * vv, nv, v, nv, 1), v4)));
-    {
-        int d[4] = {nv, nv, nv, nv};
-        long long s_id[4] = {v * vv, vv, v, 1}, s_tr[4] = {vv, v * vv, v, 1};
-        KV_TRY(kv_axpby4(ctx, B, d, -1.0, w.tmp4, s_id, v4, 1.0, w.Wabef, s_id, v4));
-        KV_TRY(kv_axpby4(ctx, B, d, 1.0, w.tmp4, s_tr, v4, 1.0, w.Wabef, s_id, v4));
-    }
-    // T2 += fac/2 Wabef[a,b,e,f] tau[e,f,i,j]
-    KV_TRY(kv_gemm(ctx, nv * nv, no * no, nv * nv, B, 0.5 * fac,
-                   MA(w.Wabef, X2(nv, v * vv, nv, vv), X2(nv, v, nv, 1), v4),
-                   MA(w.tau, X2(nv, vo2, nv, oo), X2(no, o, no, 1), v2o2), 1.0, T2o));
 
     // ---- W_mbej (layout [m][b][e][j]) ----------------------------------------
     const long long wm = vv * o, wb = vo, we = o;
@@ -299,7 +310,8 @@ int kv_stanton(kvft_ctx *ctx, int nb, int nv, int no, const double *const F[4],
                    MO(w.Zij, X3(nv, vo2, nv, oo, no, 1), X1(no, o), v2o2)));
 
     // ---- T2 += fac [P(ab) Zab + P(ij) Zij + P(ab)P(ij) Zabij] -------------------
-    return kv_assemble_t2(ctx, B, nv, no, fac, w.Zab, w.Zij, w.Zabij, T2);
+    return kv_assemble_t2(ctx, B, nv, no, fac, w.Zab, w.Zij, w.Zabij, ladders ? w.Lc : nullptr,
+                          T2);
 }
 
 extern "C" int kvft_stanton_residual(kvft_ctx *ctx, int nb, int nv, int no,

@@ -103,6 +103,20 @@ def test_ueg19_fp64_tc_vs_kelvin_example(tc_ctx):
     assert abs(Ecc - (-0.015646626108)) < 1e-10
 
 
+def test_mixed_vs_fp64_on_benchmark_system(tc_ctx):
+    """UEG 14 e-, rs=4, 38 spin orbitals, ng=10: three digit levels plus two
+    FP64-accurate refinement sweeps stay within 1e-6 Ha per electron of FP64."""
+    s = systems.ueg_recipe(14, 4.0, 19, 0.5)
+    kw = dict(T=s.T, mu=s.mu, max_iter=100, damp=0.5, ngrid=10, econv=1e-10, ctx=tc_ctx)
+    ref = ccsd.ccsd(s, precision="fp64_tc", **kw)
+    E64 = ref.run()[1]
+    mix = ccsd.ccsd(s, precision="mixed", **kw)
+    Emx = mix.run()[1]
+    assert mix.iterations_refine == 2
+    assert abs(Emx - E64) < 1e-6 * s.N
+    assert abs(mix.omega_low - E64) < 1e-6 * s.N
+
+
 def test_ueg19_mixed_within_tolerance(tc_ctx):
     """Mixed form (5 digit levels): |dOmega| <= 1e-6 Ha per electron."""
     s = systems.UEGSystem(0.1, 2 * numpy.pi, 1.2, mu=0.1, norb=19)
