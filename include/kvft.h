@@ -196,6 +196,12 @@ int kvft_solver_create_blocks(kvft_ctx *ctx, int nv, int no, int ng,
 int kvft_solver_destroy(kvft_solver *s);
 int kvft_solver_run(kvft_solver *s, const kvft_solve_opts *opts,
                     kvft_result *res);
+/* Kelvin's tau-pointwise schedule (rt_iter = "point"; cc_utils.py:176-242):
+ * converge grid point by grid point from a linear extrapolation, then
+ * res->omega_cc = ft_cc_energy of the result.  Uses opts damp, tconv,
+ * max_iter (per point). */
+int kvft_solver_run_point(kvft_solver *s, const kvft_solve_opts *opts,
+                          kvft_result *res);
 /* one amplitude iteration (update + damping + norms + energy) */
 int kvft_solver_step(kvft_solver *s, double damp, double *energy,
                      double *res);

@@ -112,6 +112,8 @@ _SIGS = {
     "kvft_solver_run": (ctypes.c_int, [vp, ctypes.POINTER(SolveOpts),
                                        ctypes.POINTER(Result)]),
     "kvft_solver_step": (ctypes.c_int, [vp, ctypes.c_double, c_double_p, c_double_p]),
+    "kvft_solver_run_point": (ctypes.c_int, [vp, ctypes.POINTER(SolveOpts),
+                                             ctypes.POINTER(Result)]),
     "kvft_solver_get_amplitudes": (ctypes.c_int, [vp, vp, vp]),
     "kvft_solver_set_amplitudes": (ctypes.c_int, [vp, vp, vp]),
     "kvft_solver_device_amplitudes": (ctypes.c_int, [vp, ctypes.POINTER(vp),

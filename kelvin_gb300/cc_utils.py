@@ -122,6 +122,22 @@ class DeviceSolver(object):
             self.ctx.check(st, "kvft_solver_run(guess)")
         return r.e_guess
 
+    def run_point(self, conv_options, verbose=False):
+        """Kelvin's tau-pointwise schedule on the device; returns the Result."""
+        o = _lib.SolveOpts(econv=float(conv_options["econv"]), tconv=float(conv_options["tconv"]),
+                           damp=float(conv_options["damp"]),
+                           max_iter=int(conv_options["max_iter"]), full=0, guess=0,
+                           verbose=int(bool(verbose)))
+        r = _lib.Result()
+        st = self.ctx.L.kvft_solver_run_point(self.h, ctypes.byref(o), ctypes.byref(r))
+        if st not in (0, 6):
+            self.ctx.check(st, "kvft_solver_run_point")
+        self.iterations = r.iterations
+        self.converged = bool(r.converged)
+        if not r.converged:
+            logging.warning("CCSD did not converge!")
+        return r
+
     def step(self, damp):
         E = ctypes.c_double()
         res = ctypes.c_double()
@@ -193,3 +209,19 @@ def ft_cc_iter(method, T1old, T2old, F, I, D1, D2, g, G, beta, ng, ti, iprint,
     finally:
         solver.close()
     return E, T1, T2
+
+
+def ft_cc_iter_extrap(method, F, I, D1, D2, g, G, beta, ng, ti, iprint, conv_options,
+                      ctx=None):
+    """Grid-point-by-grid-point convergence (cc_utils.py:176-242) on the
+    device; returns (T1, T2)."""
+    if method != "CCSD":
+        raise Exception("Unrecognized method keyword")
+    ctx = ctx or _lib.context()
+    solver = DeviceSolver.from_blocks(ctx, F, I, D1, D2, beta, ti, g, G)
+    try:
+        solver.run_point(conv_options)
+        T1, T2 = solver.amplitudes()
+    finally:
+        solver.close()
+    return T1, T2

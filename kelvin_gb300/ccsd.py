@@ -124,17 +124,27 @@ class ccsd(object):
                                           self.sys.g_aint_tot(), beta, mu, self.ti, self.g,
                                           self.G)
         self.solver = solver
+        conv = {"econv": self.econv, "tconv": self.tconv, "max_iter": self.max_iter,
+                "damp": self.damp}
         if self.rt_iter[0] != 'a' and T2in is None:
-            logging.warning("Convergence scheme ({}) is not built; using 'all'"
-                            .format(self.rt_iter))
+            # tau-pointwise schedule (ccsd.py:697-702 -> cc_utils.py:176-242)
+            r = solver.run_point(conv)
+            self.iterations = r.iterations
+            self.iterations_refine = 0
+            self.converged = bool(r.converged)
+            self.omega_low = None
+            self.T1, self.T2 = solver.amplitudes()
+            Eccn = r.omega_cc
+            self.G0, self.G1, self.Gcc, self.Gtot = E0, E1, Eccn, E0 + E1 + Eccn
+            return (Eccn + E0 + E1, Eccn)
+        if self.rt_iter[0] != 'a':
+            logging.warning("Convergence scheme ({}) is ignored when amplitudes are given.".format(self.rt_iter))
         if T1in is not None and T2in is not None:
             solver.set_amplitudes(T1in, T2in)
             E2 = solver.guess(2)
         else:
             E2 = solver.guess(1)
         logging.info('MP2 Energy: {:.10f}'.format(E2))
-        conv = {"econv": self.econv, "tconv": self.tconv, "max_iter": self.max_iter,
-                "damp": self.damp}
         Eccn, info = converge(solver, self.ctx, conv, self.precision, digits,
                               self.refine_sweeps)
         self.iterations = info["iterations"]

@@ -186,10 +186,12 @@ __global__ void quad_single_kernel(QuadParams q, int ig, const double *__restric
                                    const double *__restrict__ ti,
                                    const double *__restrict__ G,
                                    const double *__restrict__ D,
+                                   const double *__restrict__ ev,
+                                   const double *__restrict__ eo,
                                    double *__restrict__ out) {
     for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < q.P;
          p += (long long)gridDim.x * blockDim.x) {
-        const double d = D[p];
+        const double d = denom(q, p, D, ev, eo);
         double acc = 0.0;
         for (int x = 0; x < q.ng; x++) {
             const double g = G[ig * q.ng + x];
@@ -331,11 +333,28 @@ int int_tbar_single_entry(kvft_ctx *ctx, int rank, int ng, int ig, int nv, int n
     q.P = (long long)nv * no * (rank == 2 ? (long long)nv * no : 1LL);
     long long blocks = (q.P + 255) / 256;
     int grid = (int)std::min(blocks, (long long)ctx->sm_count * 8);
-    quad_single_kernel<<<grid, 256, 0, ctx->stream>>>(q, ig, tbar, ti, G, D, out);
+    quad_single_kernel<<<grid, 256, 0, ctx->stream>>>(q, ig, tbar, ti, G, D, nullptr, nullptr,
+                                                      out);
     return kv_launch_check(ctx, "quad_single");
 }
 
 }  // namespace
+
+// one grid point ig of the tau integral for the solver (D or eps form)
+int kv_quad_single(kvft_ctx *ctx, int ng, int ig, long long P, int rank, int nv, int no,
+                   const double *tbar, const double *ti, const double *G, const double *D,
+                   const double *ev, const double *eo, double *out) {
+    QuadParams q{};
+    q.ng = ng;
+    q.P = P;
+    q.rank = rank;
+    q.nv = nv;
+    q.no = no;
+    const int grid = (int)std::min((P + 255) / 256, (long long)ctx->sm_count * 8);
+    KvProfScope prof(ctx, KV_CAT_QUAD, 8.0 * (double)P * (ng + 1));
+    quad_single_kernel<<<grid, 256, 0, ctx->stream>>>(q, ig, tbar, ti, G, D, ev, eo, out);
+    return kv_launch_check(ctx, "quad_single");
+}
 
 int kv_int_tbar(kvft_ctx *ctx, int ng, size_t P, const double *tbar, const double *ti,
                 const double *D, const double *eps_v, const double *eps_o, int nv, int no,

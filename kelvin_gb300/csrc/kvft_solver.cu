@@ -20,6 +20,9 @@ int kv_quad_launch(kvft_ctx *ctx, int mode, int ng, long long P, int rank, int n
                    const double *tbar, const double *ti, const double *hti, const double *G,
                    const double *hG, const double *D, const double *ev, const double *eo,
                    int full, double alpha, double *out, double *res);
+int kv_quad_single(kvft_ctx *ctx, int ng, int ig, long long P, int rank, int nv, int no,
+                   const double *tbar, const double *ti, const double *G, const double *D,
+                   const double *ev, const double *eo, double *out);
 
 namespace {
 
@@ -120,6 +123,38 @@ int sumsq(kvft_ctx *ctx, long long n, const double *x, double *dout) {
     KV_TRY(kv_scratch(ctx, "sumsq_partial", sizeof(double) * grid, &part));
     sumsq_kernel<<<grid, 256, 0, ctx->stream>>>(n, x, (double *)part);
     KV_TRY(kv_launch_check(ctx, "sumsq"));
+    sum_kernel<<<1, 256, 0, ctx->stream>>>((double *)part, grid, dout);
+    return kv_launch_check(ctx, "sum");
+}
+
+// T = alpha T + (1 - alpha) u with a block partial of |u - T_old|^2
+__global__ void damp_norm_kernel(long long n, double alpha, const double *__restrict__ u,
+                                 double *__restrict__ T, double *__restrict__ part) {
+    __shared__ double red[256];
+    double a = 0.0;
+    for (long long k = blockIdx.x * 256LL + threadIdx.x; k < n; k += (long long)gridDim.x * 256) {
+        const double told = T[k];
+        const double d = u[k] - told;
+        a = fma(d, d, a);
+        T[k] = alpha * told + (1.0 - alpha) * u[k];
+    }
+    red[threadIdx.x] = a;
+    __syncthreads();
+    for (int s = 128; s > 0; s >>= 1) {
+        if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) part[blockIdx.x] = red[0];
+}
+
+int damp_norm(kvft_ctx *ctx, long long n, double alpha, const double *u, double *T,
+              double *dout) {
+    const int grid = (int)std::max(1LL, std::min((long long)ctx->sm_count * 4, (n + 255) / 256));
+    void *part = nullptr;
+    KV_TRY(kv_scratch(ctx, "damp_norm_partial", sizeof(double) * grid, &part));
+    KvProfScope prof(ctx, KV_CAT_ELEM, 24.0 * n);
+    damp_norm_kernel<<<grid, 256, 0, ctx->stream>>>(n, alpha, u, T, (double *)part);
+    KV_TRY(kv_launch_check(ctx, "damp_norm"));
     sum_kernel<<<1, 256, 0, ctx->stream>>>((double *)part, grid, dout);
     return kv_launch_check(ctx, "sum");
 }
@@ -455,6 +490,88 @@ int kvft_solver_run(kvft_solver *s, const kvft_solve_opts *o, kvft_result *r) {
     r->iterations = i;
     r->omega_cc = Eold;
     return r->converged ? KVFT_OK : KVFT_ENOTCONV;
+}
+
+// Kelvin's tau-pointwise schedule (cc_utils.py:176-242, rt_iter = "point"):
+// grid point by grid point, start from the linear extrapolation of the two
+// previous points and iterate the single-point update (ft_cc_equations.py:
+// 116-127) to res1 + res2 < tconv; the integrals of later points see the
+// converged tbar of the earlier ones.  Omega = ft_cc_energy of the result.
+int kvft_solver_run_point(kvft_solver *s, const kvft_solve_opts *o, kvft_result *r) {
+    if (!s || !o || !r) return KVFT_EINVAL;
+    kvft_ctx *ctx = s->ctx;
+    cudaSetDevice(ctx->device);
+    const long long n1 = s->s1(), n2 = s->s2();
+    const int ng = s->ng;
+    if (s->chunk_prec != ctx->precision * 16 + ctx->digits) KV_TRY(pick_chunk(s));
+    KV_CHECK(ctx, cudaMemsetAsync(s->T1, 0, sizeof(double) * ng * n1, ctx->stream));
+    KV_CHECK(ctx, cudaMemsetAsync(s->T2, 0, sizeof(double) * ng * n2, ctx->stream));
+    KV_CHECK(ctx, cudaMemsetAsync(s->T1b, 0, sizeof(double) * ng * n1, ctx->stream));
+    KV_CHECK(ctx, cudaMemsetAsync(s->T2b, 0, sizeof(double) * ng * n2, ctx->stream));
+    void *tmp = nullptr;
+    KV_TRY(kv_scratch(ctx, "point_tmp", sizeof(double) * (n1 + n2), &tmp));
+    double *u1 = (double *)tmp, *u2 = u1 + n1;
+    const double *Fc[4] = {s->F[0], s->F[1], s->F[2], s->F[3]};
+    const double *Ic[9];
+    for (int k = 0; k < 9; k++) Ic[k] = s->I[k];
+    const double nl1 = std::sqrt((double)n1), nl2 = std::sqrt((double)n2);
+    int total = 0, all_conv = 1;
+    double res = 0.0;
+    for (int ig = 0; ig < ng; ig++) {
+        double *t1b = s->T1b + ig * n1, *t2b = s->T2b + ig * n2;
+        double *T1g = s->T1 + ig * n1, *T2g = s->T2 + ig * n2;
+        KV_TRY(seed_neg(ctx, 1, n1, s->F[2], t1b));
+        KV_TRY(seed_neg(ctx, 1, n2, s->I[3], t2b));
+        if (ig == 0) continue;
+        if (ig == 1) {
+            KV_TRY(kv_quad_single(ctx, ng, ig, n1, 1, s->nv, s->no, s->T1b, s->ti, s->G, s->D1,
+                                  s->eps, s->eps, T1g));
+            KV_TRY(kv_quad_single(ctx, ng, ig, n2, 2, s->nv, s->no, s->T2b, s->ti, s->G, s->D2,
+                                  s->eps, s->eps, T2g));
+        } else {
+            // linear extrapolation from the two previous grid points
+            const double c = (s->hti[ig] - s->hti[ig - 1]) / (s->hti[ig - 2] - s->hti[ig - 1]);
+            int d1[4] = {1, 1, 1, (int)n1}, d2[4] = {1, 1, 1, (int)n2};
+            long long one[4] = {0, 0, 0, 1};
+            KV_TRY(kv_axpby4(ctx, 1, d1, 1.0 - c, T1g - n1, one, 0, 0.0, T1g, one, 0));
+            KV_TRY(kv_axpby4(ctx, 1, d1, c, T1g - 2 * n1, one, 0, 1.0, T1g, one, 0));
+            KV_TRY(kv_axpby4(ctx, 1, d2, 1.0 - c, T2g - n2, one, 0, 0.0, T2g, one, 0));
+            KV_TRY(kv_axpby4(ctx, 1, d2, c, T2g - 2 * n2, one, 0, 1.0, T2g, one, 0));
+        }
+        bool conv = false;
+        int i = 0;
+        while (i < o->max_iter && !conv) {
+            KV_TRY(seed_neg(ctx, 1, n1, s->F[2], t1b));
+            KV_TRY(seed_neg(ctx, 1, n2, s->I[3], t2b));
+            KV_TRY(kv_stanton(ctx, 1, s->nv, s->no, Fc, Ic, T1g, T2g, -1.0, t1b, t2b));
+            KV_TRY(kv_quad_single(ctx, ng, ig, n1, 1, s->nv, s->no, s->T1b, s->ti, s->G, s->D1,
+                                  s->eps, s->eps, u1));
+            KV_TRY(kv_quad_single(ctx, ng, ig, n2, 2, s->nv, s->no, s->T2b, s->ti, s->G, s->D2,
+                                  s->eps, s->eps, u2));
+            KV_TRY(damp_norm(ctx, n1, o->damp, u1, T1g, s->dsc + 0));
+            KV_TRY(damp_norm(ctx, n2, o->damp, u2, T2g, s->dsc + 1));
+            double h[2];
+            KV_TRY(read_scalars(s, 2, h));
+            res = std::sqrt(h[0]) / nl1 + std::sqrt(h[1]) / nl2;
+            if (!std::isfinite(res)) return kv_fail(ctx, KVFT_EDIVERGE, "non-finite residual");
+            if (o->verbose) fprintf(stderr, " point %d  %2d  %.4E\n", ig, i + 1, res);
+            i++;
+            conv = res < o->tconv;
+        }
+        total += i;
+        if (!conv) all_conv = 0;
+    }
+    KV_TRY(kv_energy(ctx, s->ng, s->nv, s->no, s->T1, s->T2, s->F[1], s->I[5], s->g, s->beta, 1,
+                     s->dsc + 4));
+    double h[5];
+    KV_TRY(read_scalars(s, 5, h));
+    r->omega_cc = h[4];
+    r->e_guess = 0.0;
+    r->res = res;
+    r->iterations = total;
+    r->converged = all_conv;
+    s->norms_valid = false;
+    return all_conv ? KVFT_OK : KVFT_ENOTCONV;
 }
 
 int kvft_solver_get_amplitudes(kvft_solver *s, double *T1h, double *T2h) {

@@ -93,3 +93,29 @@ def test_warm_start_reproduces(ctx):
     E2 = cc2.run(T1=cc.T1, T2=cc.T2)[1]
     assert abs(E1 - E2) < 1e-10
     assert cc2.iterations <= 3
+
+
+def test_pointwise_schedule_matches_all_at_once(ctx):
+    """kelvin/tests/test_ft_ccsd.py:135-149: rt_iter='point' and 'all' agree to
+    1e-8 (tconv 1e-8)."""
+    s = systems.UEGSystem(0.1, 2 * numpy.pi, 1.2, mu=0.1, norb=7)
+    kw = dict(T=0.1, mu=0.1, max_iter=50, damp=0.2, tconv=1e-8, ngrid=10)
+    E1 = ccsd.ccsd(s, **kw).run()[1]
+    E2 = ccsd.ccsd(s, rt_iter="point", **kw).run()[1]
+    assert abs(E1 - E2) < 1e-8
+
+
+def test_ft_cc_iter_extrap_dropin_vs_oracle(ctx):
+    d = golden("stanton.npz")
+    F, I = unpack_blocks(d, "ft_")
+    ti, G = d["ft_ti"], d["ft_G"]
+    ng = ti.shape[0]
+    beta = float(d["ft_beta"])
+    g = quadrature.ft_quad(ng, beta, "lin")[1]
+    conv = {"econv": 1e-10, "tconv": 1e-9, "max_iter": 80, "damp": 0.3}
+    T1r, T2r = oft.ft_cc_iter_extrap("CCSD", F, I, d["ft_D1"], d["ft_D2"], g, G, beta, ng, ti,
+                                     0, conv)
+    T1g, T2g = cc_utils.ft_cc_iter_extrap("CCSD", F, I, d["ft_D1"], d["ft_D2"], g, G, beta, ng,
+                                          ti, 0, conv)
+    assert abs(T1g - T1r).max() < AMP_TOL
+    assert abs(T2g - T2r).max() < AMP_TOL
