@@ -162,9 +162,11 @@ int kv_gemm(kvft_ctx *ctx, int M, int N, int K, int batch, double alpha,
     const long long mn = std::min(std::min(M, N), K), mx = std::max(std::max(M, N), K);
     const int cat = (mn * mn > mx) ? KV_CAT_GEMM6 : KV_CAT_GEMM;
     KvProfScope prof(ctx, cat, 2.0 * M * N * (double)K * batch);
-    // Tensor cores for everything but matrix-vector shapes and tiny products,
-    // which stay on the FP64 pipe.
-    const bool tc = ctx->precision != KVFT_PREC_FP64 && M >= 16 && N >= 16 && K >= 16 &&
+    // Tensor cores for everything but short sums and tiny products, which stay
+    // on the FP64 pipe.  Skinny shapes (a few columns against a long K) go to
+    // the tensor cores too: even with most of a 128-wide tile idle they beat
+    // GB300's FP64 pipe by an order of magnitude.
+    const bool tc = ctx->precision != KVFT_PREC_FP64 && K >= 16 &&
                     2.0 * M * N * (double)K * batch >= 2.0e6;
     if (!tc) return kv_gemm_f64(ctx, M, N, K, batch, alpha, A, B, beta, C);
     return kv_gemm_tc(ctx, M, N, K, batch, alpha, A, B, beta, C, ctx->digits);

@@ -12,22 +12,26 @@
 //     carries the weight 2^-7(s+t-2); pairs with s + t <= D are kept.  Each
 //     digit product is an integer below 2^12 (times a power of two), so an
 //     FP32 accumulator over K <= 2048 terms and two pairs is exact.
-//     tcgen05.mma accumulates level 2 (pair 1,1), level 3 (pairs 1,2 2,1) and
-//     level 4 in separate TMEM accumulators and levels >= 5 in a fourth one:
-//     the tensor core's FP32 adds truncate, and keeping every merged term
-//     2^-21 below the leading level holds their error under ~1e-13.
-//   * epilogue: the accumulators are read from TMEM (tcgen05.ld),
-//     combined in FP64, scaled by 2^(e_m + e_n - 14) alpha and added to the
-//     FP64 output view.  K > 2048 is split into sequential launches.
+//     Every level l = s + t has its own TMEM accumulator, at column
+//     (l - 2) TN of the set, and the digit planes of a B tile lie one after
+//     another in shared memory, so a single tcgen05.mma of A plane s against
+//     B planes t0..t0+k-1 (N = k TN <= 256) adds each product into its own
+//     level: 8 MMAs per 16-deep k-step for D = 7 instead of 21 pair MMAs,
+//     which keeps the tensor core's shared-memory reads of A below the SM's
+//     shared-memory bandwidth.
+//   * epilogue: the accumulators are read from TMEM (tcgen05.ld), the K
+//     chunks (K > 2048) are summed in registers, and the tile is scaled by
+//     2^(e_m + e_n - 14) alpha and written to the FP64 output view once.
 // With D = 7 (21 pair products, six digits) the norm-wise relative error is
 // ~1e-11, far inside the 1e-8 amplitude / 1e-10 Ha parity bounds; D = 3..5 is
 // the mixed-precision form.
 //
-// Kernel: one CTA per 128x128 output tile and K chunk; warp 0 = TMA producer,
-// warp 1 = MMA issuer (and TMEM owner), warps 2..5 = epilogue.  Operands are
-// staged by TMA (64-byte swizzle, 32-element k-blocks, every digit plane of a
-// k-block per pipeline stage).  Every mbarrier wait is bounded by
-// %globaltimer; on expiry the kernel records an error word and unwinds.
+// Kernel: persistent, one CTA per SM walking output tiles; warp 0 = TMA
+// producer, warp 1 = MMA issuer (and TMEM owner), warps 2..9 = epilogue; the
+// epilogue of one tile overlaps the MMAs of the next.  Operands are staged by TMA (64-byte swizzle, 32-element k-blocks,
+// every digit plane of a k-block per pipeline stage).  Every mbarrier wait is
+// bounded by %globaltimer; on expiry the kernel records an error word and
+// unwinds.
 #include "kvft_internal.h"
 
 #include <cuda.h>
@@ -39,20 +43,23 @@
 
 namespace {
 
-constexpr int TM = 128, TN = 128, KB = 32;
-constexpr int PLANE_BYTES = TM * KB * 2;      // one digit plane of a k-block: 8 KB
+constexpr int TM = 128, KB = 32;
+constexpr int PLANE_BYTES = TM * KB * 2;      // one digit plane of an A k-block: 8 KB
 constexpr int MAXS = 6;
 constexpr int KCHUNK = 2048;                  // exactness bound of the level-3 sum
-constexpr int NTHREADS = 192;
+constexpr int NEPI = 8;                       // epilogue warps: two per TMEM lane quadrant
+constexpr int NTHREADS = 64 + 32 * NEPI;      // + TMA producer warp + MMA warp
+constexpr int TMEM_COLS = 512;               // all of an SM's TMEM (one CTA per SM)
+constexpr int GROUP_M = 8;                    // m-tiles per raster group (L2 reuse)
 constexpr unsigned long long WAIT_NS = 2000000000ull;   // 2 s per wait
 
 struct TcParams {
-    int M, N;             // output extent of this launch
-    int kb_base;          // first k-block of this launch
+    int M, N;             // output extent
+    int mt, nt;           // output tiles along M and N
+    int units;            // work units: mt * nt * batch * nsplit
+    int nsplit;           // >1: each K chunk is its own unit, added into C by FP64 atomics
     int chunk_kb;         // k-blocks per K chunk (exactness bound)
     int nkb_total;        // k-blocks of the padded K extent
-    int nsplit;           // K chunks run side by side (grid z = batch * nsplit)
-    int atomic;           // 1: chunks add into C with FP64 atomics
     int S, D, NS;         // digit planes, levels, pipeline stages
     int Mp, Np;           // rows per digit plane of A / B
     int a_batch_rows, b_batch_rows;   // row offset between batch entries (0: shared)
@@ -65,6 +72,38 @@ struct TcParams {
     KOut C;
     int *err;
 };
+
+// A work unit: one output tile of one batch entry over a k-block range.
+struct Unit {
+    int b, m0, n0, kb0, kb1;
+};
+
+// Units are numbered split-fastest, then in raster groups of GROUP_M m-tiles
+// (n-tiles walk inside a group), then by batch entry, so the CTAs that run
+// at the same time share a few A row panels and sweep B once per group.
+__device__ __forceinline__ Unit unit_of(const TcParams &p, int u, int tn) {
+    Unit w;
+    const int split = u % p.nsplit;
+    const int t = u / p.nsplit;
+    const int per_b = p.mt * p.nt;
+    w.b = t / per_b;
+    const int r = t - w.b * per_b;
+    const int gsz = GROUP_M * p.nt;
+    const int g = r / gsz;
+    const int first = g * GROUP_M;
+    const int gm = min(GROUP_M, p.mt - first);
+    const int rr = r - g * gsz;
+    w.m0 = (first + rr % gm) * TM;
+    w.n0 = (rr / gm) * tn;
+    if (p.nsplit > 1) {
+        w.kb0 = split * p.chunk_kb;
+        w.kb1 = min(w.kb0 + p.chunk_kb, p.nkb_total);
+    } else {
+        w.kb0 = 0;
+        w.kb1 = p.nkb_total;
+    }
+    return w;
+}
 
 // Knuth's error-free sum: s + e == a + b exactly (round-to-nearest FP32)
 __device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
@@ -154,16 +193,24 @@ __device__ __forceinline__ uint64_t desc_sw64(uint32_t saddr) {
     return d;
 }
 
-// kind::f16 instruction descriptor: BF16 x BF16 -> FP32, K-major A and B
-constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(TN >> 3) << 17) |
-                           ((uint32_t)(TM >> 4) << 24);
+// kind::f16 instruction descriptor: BF16 x BF16 -> FP32, K-major A and B,
+// M = 128, N = tn
+__host__ __device__ constexpr uint32_t idesc_of(int tn) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(tn >> 3) << 17) |
+           ((uint32_t)(TM >> 4) << 24);
+}
 
-__device__ __forceinline__ void umma(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t acc) {
+__device__ __forceinline__ void umma(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t idesc,
+                                     uint32_t acc) {
     asm volatile(
         "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
         " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(tmem_d),
-        "l"(a), "l"(b), "r"(IDESC), "r"(acc)
+        "l"(a), "l"(b), "r"(idesc), "r"(acc)
         : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint32_t a) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(a) : "memory");
 }
 
 __device__ __forceinline__ void umma_commit(uint32_t mbar) {
@@ -179,18 +226,6 @@ __device__ __forceinline__ void fence_after() {
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 }
 
-#define TMEM_LD32(taddr, r)                                                                   \
-    asm volatile(                                                                             \
-        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13," \
-        "%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"   \
-        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]),              \
-          "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]),           \
-          "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]),       \
-          "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),       \
-          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]),       \
-          "=r"(r[30]), "=r"(r[31])                                                          \
-        : "r"(taddr))
-
 #define TMEM_LD16(taddr, r)                                                                   \
     asm volatile(                                                                             \
         "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13," \
@@ -200,54 +235,114 @@ __device__ __forceinline__ void fence_after() {
           "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])                                  \
         : "r"(taddr))
 
+#define TMEM_LD8(taddr, r)                                                                    \
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"     \
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]),     \
+                   "=r"(r[6]), "=r"(r[7])                                                     \
+                 : "r"(taddr))
+
+#define TMEM_LD4(taddr, r)                                                                    \
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0,%1,%2,%3}, [%4];"                 \
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])                             \
+                 : "r"(taddr))
+
+// 32 lanes x LW consecutive columns of TMEM
+template <int LW>
+__device__ __forceinline__ void tmem_ld(uint32_t taddr, uint32_t *r) {
+    static_assert(LW == 16 || LW == 8 || LW == 4, "TMEM load width");
+    if constexpr (LW == 16) {
+        TMEM_LD16(taddr, r);
+    } else if constexpr (LW == 8) {
+        TMEM_LD8(taddr, r);
+    } else {
+        TMEM_LD4(taddr, r);
+    }
+}
+
 __device__ __forceinline__ void tmem_wait_ld() {
     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
-// TMEM accumulator of digit level l: levels 2, 3, 4 each have their own
-// (exact sums); levels >= 5 share the fourth, 2^-21 below the leading level,
-// so the truncating FP32 adds of the tensor core stay below 2^-45 relative.
-__device__ __forceinline__ int level_acc(int l) { return l >= 5 ? 3 : l - 2; }
-__host__ __device__ __forceinline__ int n_acc(int D) { return D >= 5 ? 4 : D - 1; }
+// Shared-memory bytes of the kernel: 1 KB alignment slack, NS pipeline stages
+// (S digit planes of A and of B per stage), the barriers, the epilogue's
+// per-warp column tables and two words (TMEM base, failure flag).
+__host__ __device__ constexpr size_t tc_smem(int S, int NS, int tn) {
+    return 1024 + (size_t)NS * S * (PLANE_BYTES + tn * KB * 2) + 8 * (2 * NS + 5) +
+           (size_t)NEPI * (tn / 2) * 12 + 16;
+}
 
+// Persistent kernel: each CTA walks the units blockIdx.x, blockIdx.x +
+// gridDim.x, ...; the stage ring and the TMEM accumulator sets run on across
+// units, so TMA, tensor core and epilogue of different units overlap.
+//
+//   warp 0      TMA producer: all S digit planes of A and B of one k-block per
+//               stage.
+//   warp 1      TMEM owner and MMA issuer: the level products of K chunk c
+//               (at most KCHUNK deep, so each level sum is exact in FP32) go
+//               to accumulator set c % NSET; a commit marks the set full.
+//   warps 2-9   epilogue: warp w reads TMEM lanes 32 (w % 4).. of column half
+//               (w - 2) / 4, frees the set, and carries the sum over the
+//               unit's K chunks in registers -- one FP32 value per element
+//               when D <= 3 (the few-digit form), an unevaluated FP32 pair
+//               (error-free two-sums) otherwise.  After the last chunk the
+//               tile goes to C once: FP64 built from bit patterns with the
+//               scale 2^(e_m + e_n - 14) (and a power-of-two alpha) in the
+//               exponent field, old values of C loaded 8 at a time.
+//
+// D <= 3: TN = 128, two levels (256 columns) per set, two sets, so the MMAs
+// of one chunk run while the epilogue drains the other.  D >= 4: TN = 64, up
+// to six levels (384 columns), one set; the epilogue frees it as soon as the
+// levels are in registers (a few percent of a chunk's MMA time), and writes
+// the tile while the next chunk accumulates.
+template <int TN, bool FF>
 __global__ void __launch_bounds__(NTHREADS, 1)
 tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                TcParams p) {
+    constexpr int BPLANE = TN * KB * 2;      // one digit plane of a B k-block
+    constexpr int WCOLS = TN / 2;            // columns per epilogue warp
+    constexpr int LW = FF ? 4 : 16;          // columns per TMEM load (<= 32 registers in flight)
+    constexpr int NG = WCOLS / LW;           // TMEM loads per level
+    constexpr int WG = 8;                    // columns per store group
+    constexpr int MAXL = FF ? 6 : 2;         // levels per set
+    constexpr int NSET = FF ? 1 : 2;         // accumulator sets
+    constexpr int SET_COLS = MAXL * TN;      // 384 or 256 TMEM columns
+    constexpr int PMAX = 256 / TN;           // B planes per MMA (N <= 256)
+    static_assert(NSET * SET_COLS <= TMEM_COLS, "accumulator sets exceed TMEM");
+    constexpr uint32_t IDESC = idesc_of(TN);
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     const int S = p.S, NS = p.NS;
+    const size_t stage_a = (size_t)S * PLANE_BYTES, stage_b = (size_t)S * BPLANE;
     uint8_t *sA = smem;
-    uint8_t *sB = smem + (size_t)NS * S * PLANE_BYTES;
-    uint64_t *bars = (uint64_t *)(sB + (size_t)NS * S * PLANE_BYTES);
-    uint64_t *full = bars, *empty = bars + NS, *accf = bars + 2 * NS;
-    uint32_t *tmem_slot = (uint32_t *)(accf + 1);
-    __shared__ int s_fail;
-    __shared__ long long s_coff[4][16];   // epilogue: per-warp column offsets
-    __shared__ int s_cexp[4][16];         // and column exponents
+    uint8_t *sB = smem + NS * stage_a;
+    uint64_t *bars = (uint64_t *)(sB + NS * stage_b);
+    uint64_t *full = bars, *empty = bars + NS;
+    uint64_t *accf = bars + 2 * NS, *acce = accf + 2, *done = acce + 2;
+    long long *s_coff = (long long *)(done + 1);            // [NEPI][WCOLS]
+    int *s_cexp = (int *)(s_coff + NEPI * WCOLS);           // [NEPI][WCOLS]
+    uint32_t *tmem_slot = (uint32_t *)(s_cexp + NEPI * WCOLS);
+    volatile int *s_fail = (volatile int *)(tmem_slot + 1);
 
     const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
-    const int m0 = blockIdx.y * TM, n0 = blockIdx.x * TN;
-    const int b = blockIdx.z / p.nsplit, split = blockIdx.z % p.nsplit;
-    const int kb_begin = p.kb_base + split * p.chunk_kb;
-    const int nkb = min(p.chunk_kb, p.nkb_total - kb_begin);
-    // TMEM columns: one 128-column FP32 accumulator per level group, power of two
-    const int nacc_used = n_acc(p.D);
-    const uint32_t tcols = nacc_used == 1 ? 128u : (nacc_used == 2 ? 256u : 512u);
 
     if (threadIdx.x == 0) {
-        s_fail = 0;
+        *s_fail = 0;
         for (int i = 0; i < NS; i++) {
             mbar_init(smem_u32(&full[i]), 1);
             mbar_init(smem_u32(&empty[i]), 1);
         }
-        mbar_init(smem_u32(accf), 1);
+        for (int i = 0; i < NSET; i++) {
+            mbar_init(smem_u32(&accf[i]), 1);
+            mbar_init(smem_u32(&acce[i]), NEPI);
+        }
+        mbar_init(smem_u32(done), 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     }
     if (warp == 1) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                          smem_u32(tmem_slot)),
-                     "r"(tcols)
+                     "r"(TMEM_COLS)
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
@@ -259,127 +354,230 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
     if (warp == 0) {
         if (lane == 0) {
             // ---- TMA producer ----
-            const uint32_t bytes = 2u * S * PLANE_BYTES;
-            const int ya = b * p.a_batch_rows, yb = b * p.b_batch_rows;
-            int issued = 0;
-            for (int kb = 0; kb < nkb; kb++) {
-                const int st = kb % NS;
-                const uint32_t ph = (kb / NS) & 1;
-                if (!mbar_wait(smem_u32(&empty[st]), ph ^ 1)) {
-                    atomicExch(p.err, 1);
-                    s_fail = 1;
-                    break;
+            const uint32_t bytes = (uint32_t)(stage_a + stage_b);
+            int st = 0, issued = 0;
+            uint32_t ph = 0;
+            bool ok = true;
+            for (int u = blockIdx.x; u < p.units && ok; u += gridDim.x) {
+                const Unit w = unit_of(p, u, TN);
+                const int ya = w.b * p.a_batch_rows + w.m0, yb = w.b * p.b_batch_rows + w.n0;
+                for (int kb = w.kb0; kb < w.kb1; kb++) {
+                    if (!mbar_wait(smem_u32(&empty[st]), ph ^ 1) || *s_fail) {
+                        atomicExch(p.err, 1);
+                        *s_fail = 1;
+                        ok = false;
+                        break;
+                    }
+                    const uint32_t fb = smem_u32(&full[st]);
+                    mbar_expect_tx(fb, bytes);
+                    const int x = kb * KB;
+                    for (int s = 0; s < S; s++) {
+                        tma_load_2d(smem_u32(sA + st * stage_a + s * PLANE_BYTES), &tmA, x,
+                                    ya + s * p.Mp, fb);
+                        tma_load_2d(smem_u32(sB + st * stage_b + s * BPLANE), &tmB, x,
+                                    yb + s * p.Np, fb);
+                    }
+                    issued++;
+                    if (++st == NS) {
+                        st = 0;
+                        ph ^= 1;
+                    }
                 }
-                if (s_fail) break;
-                const uint32_t fb = smem_u32(&full[st]);
-                mbar_expect_tx(fb, bytes);
-                const int x = (kb_begin + kb) * KB;
-                for (int s = 0; s < S; s++) {
-                    tma_load_2d(smem_u32(sA + ((size_t)st * S + s) * PLANE_BYTES), &tmA, x,
-                                ya + s * p.Mp + m0, fb);
-                    tma_load_2d(smem_u32(sB + ((size_t)st * S + s) * PLANE_BYTES), &tmB, x,
-                                yb + s * p.Np + n0, fb);
-                }
-                issued = kb + 1;
             }
             // drain: every issued stage must have landed before the CTA exits
-            for (int kb = (issued > NS ? issued - NS : 0); kb < issued; kb++) {
-                const int st = kb % NS;
-                if (!mbar_wait(smem_u32(&full[st]), (kb / NS) & 1)) atomicExch(p.err, 2);
+            for (int i = 0; i < min(issued, NS); i++) {
+                if (st == 0) {
+                    st = NS - 1;
+                    ph ^= 1;
+                } else {
+                    st--;
+                }
+                if (!mbar_wait(smem_u32(&full[st]), ph)) atomicExch(p.err, 2);
             }
         }
     } else if (warp == 1) {
         if (lane == 0) {
             // ---- MMA issuer ----
-            bool started[4] = {false, false, false, false};
+            int st = 0, gc = 0;
+            uint32_t ph = 0;
             bool ok = true;
-            for (int kb = 0; kb < nkb; kb++) {
-                const int st = kb % NS;
-                if (!mbar_wait(smem_u32(&full[st]), (kb / NS) & 1)) {
-                    atomicExch(p.err, 3);
-                    s_fail = 1;
+            for (int u = blockIdx.x; u < p.units && ok; u += gridDim.x) {
+                const Unit w = unit_of(p, u, TN);
+                for (int c0 = w.kb0; c0 < w.kb1 && ok; c0 += p.chunk_kb) {
+                    const int c1 = min(c0 + p.chunk_kb, w.kb1);
+                    const int set = gc % NSET;
+                    if (!mbar_wait(smem_u32(&acce[set]), ((gc / NSET) & 1) ^ 1) || *s_fail) {
+                        atomicExch(p.err, 3);
+                        *s_fail = 1;
+                        ok = false;
+                        break;
+                    }
+                    fence_after();
+                    const uint32_t tacc = tmem + set * SET_COLS;
+                    for (int kb = c0; kb < c1; kb++) {
+                        if (!mbar_wait(smem_u32(&full[st]), ph) || *s_fail) {
+                            atomicExch(p.err, 4);
+                            *s_fail = 1;
+                            ok = false;
+                            break;
+                        }
+                        fence_after();
+                        const uint32_t a0 = smem_u32(sA + st * stage_a);
+                        const uint32_t b0 = smem_u32(sB + st * stage_b);
+                        // A plane s against B planes t0.. (adjacent in shared
+                        // memory) into levels s + t0.. (adjacent in TMEM); the
+                        // first k-step of a chunk starts every level (s = 1
+                        // reaches all of them) and later ones accumulate
+#pragma unroll
+                        for (int kk = 0; kk < KB / 16; kk++) {
+                            for (int s = 1; s <= S && s < p.D; s++) {
+                                const int tmax = min(S, p.D - s);
+                                const uint64_t da =
+                                    desc_sw64(a0 + (s - 1) * PLANE_BYTES + kk * 32);
+                                const uint32_t acc = (kb > c0 || kk > 0 || s > 1) ? 1u : 0u;
+                                for (int t0 = 1; t0 <= tmax; t0 += PMAX) {
+                                    const int np = min(PMAX, tmax - t0 + 1);
+                                    const uint64_t db =
+                                        desc_sw64(b0 + (t0 - 1) * BPLANE + kk * 32);
+                                    umma(tacc + (s + t0 - 2) * TN, da, db, idesc_of(np * TN),
+                                         acc);
+                                }
+                            }
+                        }
+                        umma_commit(smem_u32(&empty[st]));
+                        if (++st == NS) {
+                            st = 0;
+                            ph ^= 1;
+                        }
+                    }
+                    if (!ok) break;
+                    umma_commit(smem_u32(&accf[set]));
+                    gc++;
+                }
+            }
+            // every MMA issued by this thread completes before TMEM is freed
+            umma_commit(smem_u32(done));
+            if (!mbar_wait(smem_u32(done), 0)) atomicExch(p.err, 5);
+        }
+    } else {
+        // ---- epilogue ----
+        const int ew = warp - 2, q = warp & 3, h = ew >> 2;
+        const int row = q * 32 + lane;
+        const int nl = p.D - 1;                     // levels 2..D
+        long long *coff = s_coff + ew * WCOLS;
+        int *cexp = s_cexp + ew * WCOLS;
+        float rhi[WCOLS];
+        float rlo[FF ? WCOLS : 1];
+        int gc = 0;
+        bool ok = true;
+        for (int u = blockIdx.x; u < p.units && ok; u += gridDim.x) {
+            const Unit w = unit_of(p, u, TN);
+            if (w.kb0 >= w.kb1) continue;
+            for (int c0 = w.kb0; c0 < w.kb1; c0 += p.chunk_kb) {
+                const int set = gc % NSET;
+                const bool got = mbar_wait(smem_u32(&accf[set]), (gc / NSET) & 1);
+                // one verdict per warp: tcgen05.ld below needs every lane
+                if (__any_sync(0xffffffffu, !got || *s_fail)) {
+                    if (lane == 0) {
+                        atomicExch(p.err, 6);
+                        *s_fail = 1;
+                    }
                     ok = false;
                     break;
                 }
                 fence_after();
-                const uint32_t a0 = smem_u32(sA + (size_t)st * S * PLANE_BYTES);
-                const uint32_t b0 = smem_u32(sB + (size_t)st * S * PLANE_BYTES);
-                for (int l = 2; l <= p.D; l++) {
-                    const int acc = level_acc(l);
-                    for (int s = 1; s < l; s++) {
-                        const int t = l - s;
-                        if (s > S || t > S) continue;
-                        for (int kk = 0; kk < KB / 16; kk++) {
-                            const uint64_t da = desc_sw64(a0 + (s - 1) * PLANE_BYTES + kk * 32);
-                            const uint64_t db = desc_sw64(b0 + (t - 1) * PLANE_BYTES + kk * 32);
-                            umma(tmem + acc * TN, da, db, started[acc] ? 1u : 0u);
-                            started[acc] = true;
-                        }
-                    }
-                }
-                umma_commit(smem_u32(&empty[st]));
-            }
-            if (ok) umma_commit(smem_u32(accf));
-        }
-    } else {
-        // ---- epilogue: warps 2..5, TMEM lane quadrant = warp % 4 ----
-        const int q = warp % 4;
-        const int row = q * 32 + lane;
-        const bool okw = __all_sync(0xffffffffu, mbar_wait(smem_u32(accf), 0));
-        if (!okw && lane == 0) atomicExch(p.err, 4);
-        fence_after();
-        __syncwarp();
-        if (okw && !s_fail) {
-            // GB300's FP64 pipe is ~1/1500 of its BF16 tensor rate, so the
-            // levels are combined with error-free FP32 two-sums and the FP64
-            // result is assembled from bit patterns, the scale
-            // 2^(e_m + e_n - 14) (and a power-of-two alpha) going straight into
-            // the exponent field: at most two FP64 operations per element.
-            const int m = m0 + row;
-            const int nacc = n_acc(p.D);
-            const int ew = warp - 2;
-            const int em = (m < p.M) ? exp_of(p.ea[(long long)b * p.ea_bst + m]) : 0;
-            const int krow = em - 14 + p.alpha_exp;
-            double *Cb = p.C.p + (long long)b * p.C.bst;
-            const long long roff = (m < p.M) ? p.C.r.off(m) : 0;
-            for (int c = 0; c < TN / 16; c++) {
-                if (lane < 16) {
-                    const int n = n0 + c * 16 + lane;
-                    s_coff[ew][lane] = (n < p.N) ? p.C.c.off(n) : 0;
-                    s_cexp[ew][lane] = (n < p.N) ? exp_of(p.eb[(long long)b * p.eb_bst + n]) : 0;
-                }
-                uint32_t r0[16], r1[16], r2[16], r3[16];
-                const uint32_t tbase = tmem + ((uint32_t)(q * 32) << 16) + c * 16;
-                TMEM_LD16(tbase, r0);
-                if (nacc > 1) TMEM_LD16(tbase + TN, r1);
-                if (nacc > 2) TMEM_LD16(tbase + 2 * TN, r2);
-                if (nacc > 3) TMEM_LD16(tbase + 3 * TN, r3);
-                tmem_wait_ld();
-                __syncwarp();
-                if (m < p.M) {
+                const bool first = (c0 == w.kb0);
+                const uint32_t tb =
+                    tmem + ((uint32_t)(q * 32) << 16) + set * SET_COLS + h * WCOLS;
 #pragma unroll
-                    for (int j = 0; j < 16; j++) {
-                        const int n = n0 + c * 16 + j;
-                        if (n >= p.N) continue;
-                        float hi = __uint_as_float(r0[j]), lo = 0.f, e = 0.f;
-                        if (nacc > 1) two_sum(hi, __uint_as_float(r1[j]), hi, lo);
-                        if (nacc > 2) {
-                            two_sum(hi, __uint_as_float(r2[j]), hi, e);
-                            lo += e;
+                for (int g = 0; g < NG; g++) {
+                    uint32_t r[MAXL][LW];
+#pragma unroll
+                    for (int l = 0; l < MAXL; l++)
+                        if (l < nl) tmem_ld<LW>(tb + l * TN + g * LW, r[l]);
+                    tmem_wait_ld();
+#pragma unroll
+                    for (int j = 0; j < LW; j++) {
+                        const int i = g * LW + j;
+                        float hi = __uint_as_float(r[0][j]);
+                        if constexpr (!FF) {
+                            if (nl > 1) hi += __uint_as_float(r[1][j]);
+                            rhi[i] = first ? hi : rhi[i] + hi;
+                        } else {
+                            // exact level sums, leading first: an FP32 pair
+                            float lo = 0.f, e;
+#pragma unroll
+                            for (int l = 1; l < MAXL; l++) {
+                                if (l < nl) {
+                                    two_sum(hi, __uint_as_float(r[l][j]), hi, e);
+                                    lo += e;
+                                }
+                            }
+                            if (first) {
+                                rhi[i] = hi;
+                                rlo[i] = lo;
+                            } else {
+                                float sm;
+                                two_sum(rhi[i], hi, sm, e);
+                                rlo[i] += lo + e;
+                                rhi[i] = sm;
+                            }
                         }
-                        if (nacc > 3) lo += __uint_as_float(r3[j]);
-                        const int k = krow + s_cexp[ew][j];
-                        double v = f32_scaled(hi, k, p.alpha_sign) + f32_scaled(lo, k, p.alpha_sign);
-                        if (!p.alpha_pow2) v *= p.alpha;
-                        double *dst = Cb + roff + s_coff[ew][j];
-                        if (p.atomic) atomicAdd(dst, v);
-                        else if (p.beta == 0.0) *dst = v;
-                        else if (p.beta == 1.0) *dst += v;
-                        else *dst = fma(p.beta, *dst, v);
                     }
                 }
+                fence_before();
                 __syncwarp();
+                if (lane == 0) mbar_arrive(smem_u32(&acce[set]));
+                gc++;
             }
+            if (!ok) break;
+            // ---- the tile to C ----
+            const int nw = w.n0 + h * WCOLS;          // first column of this warp
+            for (int i = lane; i < WCOLS; i += 32) {
+                const int n = nw + i;
+                coff[i] = (n < p.N) ? p.C.c.off(n) : 0;
+                cexp[i] = (n < p.N) ? exp_of(p.eb[(long long)w.b * p.eb_bst + n]) : 0;
+            }
+            __syncwarp();
+            const int m = w.m0 + row;
+            if (m < p.M) {
+                const int krow = exp_of(p.ea[(long long)w.b * p.ea_bst + m]) - 14 + p.alpha_exp;
+                double *Cr = p.C.p + (long long)w.b * p.C.bst + p.C.r.off(m);
+                const int nlim = p.N - nw;
+#pragma unroll
+                for (int g = 0; g < WCOLS / WG; g++) {
+                    double out[WG];
+#pragma unroll
+                    for (int j = 0; j < WG; j++) {
+                        const int i = g * WG + j;
+                        const int k = krow + cexp[i];
+                        double v = f32_scaled(rhi[i], k, p.alpha_sign);
+                        if constexpr (FF) v += f32_scaled(rlo[i], k, p.alpha_sign);
+                        if (!p.alpha_pow2) v *= p.alpha;
+                        out[j] = v;
+                    }
+                    if (p.nsplit > 1) {
+#pragma unroll
+                        for (int j = 0; j < WG; j++)
+                            if (g * WG + j < nlim) atomicAdd(Cr + coff[g * WG + j], out[j]);
+                    } else {
+                        if (p.beta != 0.0) {
+                            double old[WG];
+#pragma unroll
+                            for (int j = 0; j < WG; j++)
+                                old[j] = (g * WG + j < nlim) ? Cr[coff[g * WG + j]] : 0.0;
+#pragma unroll
+                            for (int j = 0; j < WG; j++)
+                                out[j] = (p.beta == 1.0) ? old[j] + out[j]
+                                                         : fma(p.beta, old[j], out[j]);
+                        }
+#pragma unroll
+                        for (int j = 0; j < WG; j++)
+                            if (g * WG + j < nlim) Cr[coff[g * WG + j]] = out[j];
+                    }
+                }
+            }
+            __syncwarp();
         }
     }
     fence_before();
@@ -387,7 +585,8 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
     if (warp == 1) {
         __syncwarp();
         fence_after();
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(tcols)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                     "r"(TMEM_COLS)
                      : "memory");
     }
 }
@@ -534,12 +733,15 @@ EncodeTiledFn encode_fn() {
     return fn;
 }
 
-int make_map(kvft_ctx *ctx, CUtensorMap *map, void *base, int K, int ld, long long rows) {
+// 2D map over digit planes (K x rows, row stride ld elements); one box is a
+// k-block of box_rows rows
+int make_map(kvft_ctx *ctx, CUtensorMap *map, void *base, int K, int ld, long long rows,
+             int box_rows) {
     EncodeTiledFn fn = encode_fn();
     if (!fn) return kv_fail(ctx, KVFT_EDEVICE, "cuTensorMapEncodeTiled unavailable");
     cuuint64_t dims[2] = {(cuuint64_t)K, (cuuint64_t)rows};
     cuuint64_t strides[1] = {(cuuint64_t)ld * 2};
-    cuuint32_t box[2] = {KB, TM};
+    cuuint32_t box[2] = {KB, (cuuint32_t)box_rows};
     cuuint32_t estr[2] = {1, 1};
     CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, base, dims, strides, box, estr,
                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
@@ -598,61 +800,76 @@ int pack(kvft_ctx *ctx, const char *key, const PackView &v, int R, int K, int nb
     return KVFT_OK;
 }
 
-size_t tc_smem(int S, int NS) { return 1024 + (size_t)2 * NS * S * PLANE_BYTES + 8 * (2 * NS + 2) + 64; }
+// The stride-1 index of a view: its fastest dimension of extent > 1 has
+// element stride 1.
+bool unit_stride(const KIdx &x) {
+    for (int d = 2; d >= 0; d--)
+        if (x.size[d] > 1) return x.st[d] == 1;
+    return true;
+}
 
-}  // namespace
+constexpr size_t SMEM_CAP = 225 * 1024;
+// Below half of an SM's shared memory two CTAs could share an SM and the
+// second one's 512-column TMEM allocation would block: always take more.
+constexpr size_t SMEM_FLOOR = 120 * 1024;
 
-int kv_gemm_tc(kvft_ctx *ctx, int M, int N, int K, int batch, double alpha, const KMat &A,
-               const KMat &B, double beta, const KOut &C, int digits) {
-    const int D = digits;
-    const int S = std::min(D - 1, MAXS);
-    if (D < 2 || D > MAXS + 1) return kv_fail(ctx, KVFT_EINVAL, "tensor-core digits out of range");
-    if (M <= 0 || N <= 0 || batch <= 0) return KVFT_OK;
-    if (K <= 0) return kv_gemm_f64(ctx, M, N, K, batch, alpha, A, B, beta, C);
-    if (M < N) {
-        // C^T = B^T A^T: the larger extent goes to the 128 TMEM lanes, which are
-        // the epilogue's rows (a small M would leave most epilogue warps idle)
-        const KMat At{B.p, B.c, B.r, B.bst};
-        const KMat Bt{A.p, A.c, A.r, A.bst};
-        const KOut Ct{C.p, C.c, C.r, C.bst};
-        return kv_gemm_tc(ctx, N, M, K, batch, alpha, At, Bt, beta, Ct, digits);
+template <int TN, bool FF>
+int launch_tc(kvft_ctx *ctx, const CUtensorMap &ma, const CUtensorMap &mb, TcParams &p) {
+    int NS = 2;
+    while (NS < 8 && tc_smem(p.S, NS + 1, TN) <= SMEM_CAP) NS++;
+    if (tc_smem(p.S, NS, TN) > SMEM_CAP)
+        return kv_fail(ctx, KVFT_EINVAL, "tensor-core gemm: stages exceed shared memory");
+    p.NS = NS;
+    const size_t smem = std::max(tc_smem(p.S, NS, TN), SMEM_FLOOR);
+    static bool attr = false;
+    if (!attr) {
+        KV_CHECK(ctx, cudaFuncSetAttribute(tc_gemm_kernel<TN, FF>,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)SMEM_CAP));
+        attr = true;
     }
+    const int grid = std::min(p.units, ctx->sm_count);
+    tc_gemm_kernel<TN, FF><<<grid, NTHREADS, smem, ctx->stream>>>(ma, mb, p);
+    return kv_launch_check(ctx, "tc_gemm");
+}
+
+int gemm_tc_run(kvft_ctx *ctx, int M, int N, int K, int batch, double alpha, const KMat &A,
+                const KMat &B, double beta, const KOut &C, int D) {
+    const int S = std::min(D - 1, MAXS);
+    const bool ff = D >= 4;            // three or four accumulators: FP32 pairs, TN = 64
+    const int tn = ff ? 64 : 128;
     const int nbA = A.bst ? batch : 1, nbB = B.bst ? batch : 1;
     Packed pa, pb;
     KV_TRY(pack(ctx, "tc_pack_a", PackView{A.p, A.r, A.c, A.bst}, M, K, nbA, S, &pa));
     // B is K x N; its K-major form has rows = N (B's column index), cols = K
     KV_TRY(pack(ctx, "tc_pack_b", PackView{B.p, B.c, B.r, B.bst}, N, K, nbB, S, &pb));
     CUtensorMap ma, mb;
-    KV_TRY(make_map(ctx, &ma, pa.planes, pa.K, pa.ld, (long long)nbA * S * pa.R));
-    KV_TRY(make_map(ctx, &mb, pb.planes, pb.K, pb.ld, (long long)nbB * S * pb.R));
-    int NS = 2;
-    while (NS < 6 && tc_smem(S, NS + 1) <= 225 * 1024) NS++;
-    const size_t smem = tc_smem(S, NS);
-    static bool attr = false;
-    if (!attr) {
-        cudaFuncSetAttribute(tc_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             225 * 1024);
-        attr = true;
-    }
-    if (batch > 65535) return kv_fail(ctx, KVFT_EINVAL, "tensor-core gemm: batch too large");
-    const int mt = (M + TM - 1) / TM, nt = (N + TN - 1) / TN;
+    KV_TRY(make_map(ctx, &ma, pa.planes, pa.K, pa.ld, (long long)nbA * S * pa.R, TM));
+    KV_TRY(make_map(ctx, &mb, pb.planes, pb.K, pb.ld, (long long)nbB * S * pb.R, tn));
+    const int mt = (M + TM - 1) / TM, nt = (N + tn - 1) / tn;
     const int nkb_total = (K + KB - 1) / KB;
     const int nchunks = (nkb_total + KCHUNK / KB - 1) / (KCHUNK / KB);
     const int chunk_kb = (nkb_total + nchunks - 1) / nchunks;     // balanced chunks
     const long long tiles = (long long)mt * nt * batch;
-    // few output tiles and several K chunks: run the chunks side by side and
-    // add them into C with FP64 atomics (C pre-scaled by beta)
-    const bool par = nchunks > 1 && tiles < 2LL * ctx->sm_count &&
-                     (long long)batch * nchunks <= 65535;
+    // fewer output tiles than two waves of SMs and several K chunks: every
+    // chunk becomes a unit of its own and adds into C with FP64 atomics
+    // (C pre-scaled by beta)
+    const bool par = nchunks > 1 && tiles < 2LL * ctx->sm_count;
+    const long long units = tiles * (par ? nchunks : 1);
+    if (units > 0x7FFFFFFFLL) return kv_fail(ctx, KVFT_EINVAL, "tensor-core gemm: too many tiles");
     if (par && beta != 1.0) KV_TRY(kv_scale_view(ctx, M, N, batch, beta, C));
     TcParams p;
     p.M = M;
     p.N = N;
+    p.mt = mt;
+    p.nt = nt;
+    p.units = (int)units;
+    p.nsplit = par ? nchunks : 1;
     p.chunk_kb = chunk_kb;
     p.nkb_total = nkb_total;
     p.S = S;
     p.D = D;
-    p.NS = NS;
+    p.NS = 0;
     p.Mp = pa.R;
     p.Np = pb.R;
     p.a_batch_rows = (nbA > 1) ? S * pa.R : 0;
@@ -662,6 +879,7 @@ int kv_gemm_tc(kvft_ctx *ctx, int M, int N, int K, int batch, double alpha, cons
     p.ea_bst = (nbA > 1) ? pa.R : 0;
     p.eb_bst = (nbB > 1) ? pb.R : 0;
     p.alpha = alpha;
+    p.beta = par ? 1.0 : beta;
     {
         int ex2 = 0;
         const double fr = std::frexp(alpha, &ex2);
@@ -671,25 +889,35 @@ int kv_gemm_tc(kvft_ctx *ctx, int M, int N, int K, int batch, double alpha, cons
     }
     p.C = C;
     p.err = ctx->dflag;
-    if (par) {
-        p.kb_base = 0;
-        p.nsplit = nchunks;
-        p.atomic = 1;
-        p.beta = 1.0;
-        dim3 grid(nt, mt, batch * nchunks);
-        tc_gemm_kernel<<<grid, NTHREADS, smem, ctx->stream>>>(ma, mb, p);
-        return kv_launch_check(ctx, "tc_gemm");
+    return ff ? launch_tc<64, true>(ctx, ma, mb, p) : launch_tc<128, false>(ctx, ma, mb, p);
+}
+
+}  // namespace
+
+int kv_gemm_tc(kvft_ctx *ctx, int M, int N, int K, int batch, double alpha, const KMat &A,
+               const KMat &B, double beta, const KOut &C, int digits) {
+    const int D = digits;
+    if (D < 2 || D > MAXS + 1) return kv_fail(ctx, KVFT_EINVAL, "tensor-core digits out of range");
+    if (M <= 0 || N <= 0 || batch <= 0) return KVFT_OK;
+    if (K <= 0) return kv_gemm_f64(ctx, M, N, K, batch, alpha, A, B, beta, C);
+    // C^T = B^T A^T costs nothing but the operand roles.  The epilogue's lanes
+    // are the tile rows, so the stride-1 index of C goes to the rows (each
+    // store then covers 32 consecutive doubles) unless that extent is short
+    // and K long (the unused TMEM lanes would cost MMA time); otherwise the
+    // larger extent goes to the rows.
+    bool swap = M < N;
+    const bool rc = unit_stride(C.r), cc = unit_stride(C.c);
+    if (rc != cc) {
+        const int ext = cc ? N : M;
+        if (ext >= 64 || K <= 512) swap = cc;
     }
-    p.nsplit = 1;
-    p.atomic = 0;
-    dim3 grid(nt, mt, batch);
-    for (int c = 0; c < nchunks; c++) {
-        p.kb_base = c * chunk_kb;
-        p.beta = (c == 0) ? beta : 1.0;
-        tc_gemm_kernel<<<grid, NTHREADS, smem, ctx->stream>>>(ma, mb, p);
-        KV_TRY(kv_launch_check(ctx, "tc_gemm"));
+    if (swap) {
+        const KMat At{B.p, B.c, B.r, B.bst};
+        const KMat Bt{A.p, A.c, A.r, A.bst};
+        const KOut Ct{C.p, C.c, C.r, C.bst};
+        return gemm_tc_run(ctx, N, M, K, batch, alpha, At, Bt, beta, Ct, D);
     }
-    return KVFT_OK;
+    return gemm_tc_run(ctx, M, N, K, batch, alpha, A, B, beta, C, D);
 }
 
 // Device status word written by bounded waits (0 = fine).

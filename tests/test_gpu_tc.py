@@ -59,6 +59,22 @@ def test_tc_gemm_accuracy(ctx, M, N, K, batch, digits):
     assert normwise(C, A, B) < TOL[digits]
 
 
+# Unit schedules of the persistent kernel: K chunks summed inside one unit
+# (>= two waves of tiles), K chunks as separate units added by atomics (few
+# tiles), C's contiguous index kept on the columns (narrow N, long K), and
+# skinny products (N = 1, 8) against a long K.
+@pytest.mark.parametrize("M,N,K,batch", [(2048, 2560, 4200, 1), (640, 640, 2500, 8),
+                                         (300, 40, 1000, 1), (3000, 8, 5000, 1),
+                                         (1444, 1, 1444, 6)])
+@pytest.mark.parametrize("digits", [3, 7])
+def test_tc_gemm_unit_schedules(ctx, M, N, K, batch, digits):
+    rng = numpy.random.default_rng(M + 3 * N + K + digits)
+    A = rng.standard_normal((batch, M, K)) * numpy.exp(rng.standard_normal((batch, M, 1)))
+    B = rng.standard_normal((batch, K, N))
+    C = gemm(ctx, A, B, _lib.PREC_FP64_TC, digits)
+    assert normwise(C, A, B) < TOL[digits]
+
+
 def test_tc_gemm_matches_fp64_engine(ctx):
     rng = numpy.random.default_rng(3)
     A = rng.standard_normal((1, 96, 777))
