@@ -68,60 +68,100 @@ __global__ void make_tau_kernel(long long total, int nv, int no,
     }
 }
 
-// out[y,f,b,j,n] = 0.5 t2[y,f,b,j,n] + t1[y,f,j] t1[y,b,n]
-__global__ void wmbej_tmp_kernel(long long total, int nv, int no,
-                                 const double *__restrict__ t1,
-                                 const double *__restrict__ t2,
-                                 double *__restrict__ out) {
-    const long long s4 = (long long)nv * nv * no * no;
-    for (long long x = blockIdx.x * (long long)blockDim.x + threadIdx.x; x < total;
-         x += (long long)gridDim.x * blockDim.x) {
-        long long y = x / s4;
-        long long r = x - y * s4;
-        int n = (int)(r % no); r /= no;
-        int j = (int)(r % no); r /= no;
-        int b = (int)(r % nv);
-        int f = (int)(r / nv);
-        const double *u = t1 + y * nv * no;
-        out[x] = 0.5 * t2[x] + u[f * no + j] * u[b * no + n];
+// out[y][b][j][n][f] = 0.5 t2[y][f][b][j][n] + t1[y][f][j] t1[y][b][n]: the
+// contraction index (n, f) ends up contiguous, matching <mn||ef> of the W_mbej
+// product.  32 x 32 (f, n) tiles go through shared memory so the reads are
+// coalesced along n and the writes along f.
+__global__ void __launch_bounds__(256)
+wmbej_tmp_kernel(int nv, int no, const double *__restrict__ t1, const double *__restrict__ t2,
+                 double *__restrict__ out) {
+    __shared__ double tile[32][33];
+    const int tx = threadIdx.x % 32, ty = threadIdx.x / 32;
+    const int ntn = (no + 31) / 32;
+    const int f0 = (blockIdx.x / ntn) * 32, n0 = (blockIdx.x % ntn) * 32;
+    const long long y = blockIdx.z;
+    const long long oo = (long long)no * no;
+    const double *u = t1 + y * nv * no;
+    for (int bj = blockIdx.y; bj < nv * no; bj += gridDim.y) {
+        const int b = bj / no, j = bj % no;
+        __syncthreads();
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            const int f = f0 + ty + 8 * i, n = n0 + tx;
+            if (f < nv && n < no)
+                tile[ty + 8 * i][tx] = t2[((y * nv + f) * nv + b) * oo + (long long)j * no + n];
+        }
+        __syncthreads();
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            const int n = n0 + ty + 8 * i, f = f0 + tx;
+            if (f < nv && n < no)
+                out[(((y * nv + b) * no + j) * no + n) * nv + f] =
+                    0.5 * tile[tx][ty + 8 * i] + u[f * no + j] * u[b * no + n];
+        }
     }
 }
 
-__global__ void assemble_t2_kernel(long long total, int nv, int no, double fac,
-                                   const double *__restrict__ Zab,
-                                   const double *__restrict__ Zij,
-                                   const double *__restrict__ Zabij,
-                                   const double *__restrict__ Lc,
-                                   double *__restrict__ T2) {
-    const long long s4 = (long long)nv * nv * no * no;
-    const long long sa = (long long)nv * no * no, sb = (long long)no * no, si = no;
-    for (long long x = blockIdx.x * (long long)blockDim.x + threadIdx.x; x < total;
-         x += (long long)gridDim.x * blockDim.x) {
-        long long y = x / s4;
-        long long r = x - y * s4;
-        int j = (int)(r % no); r /= no;
-        int i = (int)(r % no); r /= no;
-        int b = (int)(r % nv);
-        int a = (int)(r / nv);
-        long long base = y * s4;
-        long long abij = base + a * sa + b * sb + i * si + j;
-        long long baij = base + b * sa + a * sb + i * si + j;
-        long long abji = base + a * sa + b * sb + j * si + i;
-        long long baji = base + b * sa + a * sb + j * si + i;
-        double v = 0.0;
-        if (Zab) v += Zab[abij] - Zab[baij];
-        if (Zij) v += Zij[abij] - Zij[abji];
-        if (Zabij) v += Zabij[abij] - Zabij[baij] - Zabij[abji] + Zabij[baji];
-        if (Lc && a != b && i != j) {
-            // ladder terms, stored over a<b, i<j: antisymmetric expansion
-            const int pv = nv * (nv - 1) / 2, po = no * (no - 1) / 2;
-            const int p = min(a, b), q = max(a, b), r = min(i, j), t = max(i, j);
-            const double sg = ((a < b) == (i < j)) ? 1.0 : -1.0;
-            v += sg * Lc[y * (long long)pv * po +
-                         (long long)(pair_start(p, nv) + q - p - 1) * po +
-                         pair_start(r, no) + t - r - 1];
+// T2[y,a,b,i,j] += fac (1 - P(ab))(1 - P(ij)) (Z + L)[y,a,b,i,j], L = the
+// ladder sum stored over a < b, i < j and zero elsewhere.  One block per
+// (a < b) pair and pair of 32 x 32 (i, j) tiles (a tile and its mirror):
+// Q = Z[a,b] - Z[b,a] of both tiles goes through shared memory, so every Z
+// element is read once, coalesced, and R = Q - Q^T + (L - L^T) is added to
+// T2[a,b] and subtracted from T2[b,a].  The a = b blocks of T2 get nothing.
+__global__ void __launch_bounds__(256)
+assemble_t2_kernel(int nv, int no, double fac, const double *__restrict__ Z,
+                   const double *__restrict__ Lc, double *__restrict__ T2) {
+    __shared__ double qa[32][33], qb[32][33];
+    const int tx = threadIdx.x % 32, ty = threadIdx.x / 32;
+    const int nt = (no + 31) / 32;
+    int it = 0, rem = blockIdx.x;           // tile pair (it <= jt)
+    while (rem >= nt - it) {
+        rem -= nt - it;
+        it++;
+    }
+    const int jt = it + rem;
+    const int i0 = it * 32, j0 = jt * 32;
+    const long long y = blockIdx.z;
+    const int pv = nv * (nv - 1) / 2, po = no * (no - 1) / 2;
+    const long long oo = (long long)no * no, s4 = (long long)nv * nv * oo;
+    for (int pab = blockIdx.y; pab < pv; pab += gridDim.y) {
+        int a, b;
+        pair_of(pab, nv, a, b);
+        const long long oab = y * s4 + ((long long)a * nv + b) * oo;
+        const long long oba = y * s4 + ((long long)b * nv + a) * oo;
+        const double *L = Lc ? Lc + (y * pv + pab) * (long long)po : nullptr;
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            const int r = ty + 8 * k;
+            int i = i0 + r, j = j0 + tx;
+            qa[r][tx] = (i < no && j < no) ? Z[oab + i * no + j] - Z[oba + i * no + j] : 0.0;
+            i = j0 + r;
+            j = i0 + tx;
+            qb[r][tx] = (i < no && j < no) ? Z[oab + i * no + j] - Z[oba + i * no + j] : 0.0;
         }
-        T2[x] += fac * v;
+        __syncthreads();
+        auto ladder = [&](int i, int j) -> double {
+            if (!L || i == j) return 0.0;
+            return i < j ? L[pair_start(i, no) + j - i - 1] : -L[pair_start(j, no) + i - j - 1];
+        };
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            const int r = ty + 8 * k;
+            int i = i0 + r, j = j0 + tx;
+            if (i < no && j < no) {
+                const double R = fac * (qa[r][tx] - qb[tx][r] + ladder(i, j));
+                T2[oab + i * no + j] += R;
+                T2[oba + i * no + j] -= R;
+            }
+            i = j0 + r;
+            j = i0 + tx;
+            if (it != jt && i < no && j < no) {
+                const double R = fac * (qb[r][tx] - qa[tx][r] + ladder(i, j));
+                T2[oab + i * no + j] += R;
+                T2[oba + i * no + j] -= R;
+            }
+        }
     }
 }
 
@@ -220,20 +260,23 @@ int kv_make_wmbej_tmp(kvft_ctx *ctx, int batch, int nv, int no,
                       const double *t1, const double *t2, double *out) {
     long long total = (long long)batch * nv * nv * no * no;
     if (total == 0) return KVFT_OK;
+    if (batch > 65535) return kv_fail(ctx, KVFT_EINVAL, "wmbej_tmp: batch too large");
     KvProfScope prof(ctx, KV_CAT_ELEM, 16.0 * total);
-    wmbej_tmp_kernel<<<grid_for(ctx, total, 256), 256, 0, ctx->stream>>>(total, nv, no, t1,
-                                                                         t2, out);
+    const dim3 grid(((nv + 31) / 32) * ((no + 31) / 32), std::min(nv * no, 65535), batch);
+    wmbej_tmp_kernel<<<grid, 256, 0, ctx->stream>>>(nv, no, t1, t2, out);
     return kv_launch_check(ctx, "wmbej_tmp");
 }
 
-int kv_assemble_t2(kvft_ctx *ctx, int batch, int nv, int no, double fac,
-                   const double *Zab, const double *Zij, const double *Zabij,
+int kv_assemble_t2(kvft_ctx *ctx, int batch, int nv, int no, double fac, const double *Z,
                    const double *Lc, double *T2) {
-    long long total = (long long)batch * nv * nv * no * no;
-    if (total == 0) return KVFT_OK;
-    KvProfScope prof(ctx, KV_CAT_ELEM, 8.0 * total * 6);
-    assemble_t2_kernel<<<grid_for(ctx, total, 256), 256, 0, ctx->stream>>>(
-        total, nv, no, fac, Zab, Zij, Zabij, Lc, T2);
+    const long long total = (long long)batch * nv * nv * no * no;
+    if (total == 0 || nv < 2) return KVFT_OK;
+    if (batch > 65535) return kv_fail(ctx, KVFT_EINVAL, "assemble_t2: batch too large");
+    KvProfScope prof(ctx, KV_CAT_ELEM, 8.0 * total * (Lc ? 3.25 : 3.0));
+    const int nt = (no + 31) / 32;
+    const int pv = nv * (nv - 1) / 2;
+    const dim3 grid(nt * (nt + 1) / 2, std::min(pv, 65535), batch);
+    assemble_t2_kernel<<<grid, 256, 0, ctx->stream>>>(nv, no, fac, Z, Lc, T2);
     return kv_launch_check(ctx, "assemble_t2");
 }
 

@@ -156,8 +156,56 @@ int kv_gemm_f64(kvft_ctx *ctx, int M, int N, int K, int batch, double alpha,
     return kv_launch_check(ctx, "gemm_f64");
 }
 
+namespace {
+
+// Moves K component p of both operands' K indices to the fastest position,
+// keeping the order of the others (the contraction is the same sum).
+void k_to_fast(KIdx &a, KIdx &b, int p) {
+    KIdx na = a, nb = b;
+    int q = 0;
+    for (int d = 0; d < 3; d++)
+        if (d != p) {
+            na.size[q] = a.size[d];
+            na.st[q] = a.st[d];
+            nb.size[q] = b.size[d];
+            nb.st[q] = b.st[d];
+            q++;
+        }
+    na.size[2] = a.size[p];
+    na.st[2] = a.st[p];
+    nb.size[2] = b.size[p];
+    nb.st[2] = b.st[p];
+    a = na;
+    b = nb;
+}
+
+// The order of the contraction index's components is free.  Operands are read
+// in tiles coalesced along their row index or along K, whichever is contiguous
+// in memory; when an operand's rows are not, the K component that is
+// contiguous in it (if any) is made the fastest, for the larger operand first.
+void order_k(int M, int N, int batch, KMat &A, KMat &B) {
+    const long long sa = (long long)M * (A.bst ? batch : 1);
+    const long long sb = (long long)N * (B.bst ? batch : 1);
+    for (int pass = 0; pass < 2; pass++) {
+        const bool a_turn = (pass == 0) == (sa >= sb);
+        const KIdx &rows = a_turn ? A.r : B.c;      // rows of the packed form
+        const KIdx &k = a_turn ? A.c : B.r;
+        if (kidx_fast_stride(rows) == 1) continue;
+        if (kidx_fast_stride(k) == 1) return;        // already contiguous along K
+        for (int d = 0; d < 3; d++)
+            if (k.size[d] > 1 && k.st[d] == 1) {
+                k_to_fast(A.c, B.r, d);
+                return;
+            }
+    }
+}
+
+}  // namespace
+
 int kv_gemm(kvft_ctx *ctx, int M, int N, int K, int batch, double alpha,
-            const KMat &A, const KMat &B, double beta, const KOut &C) {
+            const KMat &A_in, const KMat &B_in, double beta, const KOut &C) {
+    KMat A = A_in, B = B_in;
+    order_k(M, N, batch, A, B);
     // n^6-class: every GEMM dimension is a pair of orbital indices or more
     const long long mn = std::min(std::min(M, N), K), mx = std::max(std::max(M, N), K);
     const int cat = (mn * mn > mx) ? KV_CAT_GEMM6 : KV_CAT_GEMM;

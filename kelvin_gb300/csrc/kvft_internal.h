@@ -48,6 +48,13 @@ inline KIdx kidx2(int s0, long long t0, int s1, long long t1) {
 inline KIdx kidx3(int s0, long long t0, int s1, long long t1, int s2, long long t2) {
     return KIdx{{s0, s1, s2}, {t0, t1, t2}};
 }
+// Element stride of the fastest component of extent > 1 (0 for one element):
+// consecutive index values are adjacent in memory when it is 1.
+inline long long kidx_fast_stride(const KIdx &x) {
+    for (int d = 2; d >= 0; d--)
+        if (x.size[d] > 1) return x.st[d];
+    return 0;
+}
 
 // ---------------------------------------------------------------------------
 // Context
@@ -136,12 +143,12 @@ int kv_axpby4(kvft_ctx *ctx, int batch, const int dims[4], double alpha,
 // tau-type amplitudes: out = t2 + c * (t1[a,i] t1[b,j] - t1[b,i] t1[a,j])
 int kv_make_tau(kvft_ctx *ctx, int batch, int nv, int no, const double *t1,
                 const double *t2, double c, double *out);
-// tmp[f,b,j,n] = 0.5 t2[f,b,j,n] + t1[f,j] t1[b,n]
+// tmp[b,j,n,f] = 0.5 t2[f,b,j,n] + t1[f,j] t1[b,n]
 int kv_make_wmbej_tmp(kvft_ctx *ctx, int batch, int nv, int no,
                       const double *t1, const double *t2, double *out);
-// T2 += fac * [Zab - P(ab) Zab + Zij - P(ij) Zij + (1 - P(ab))(1 - P(ij)) Zabij]
-int kv_assemble_t2(kvft_ctx *ctx, int batch, int nv, int no, double fac,
-                   const double *Zab, const double *Zij, const double *Zabij,
+// T2 += fac (1 - P(ab))(1 - P(ij)) (Z + L), L = the ladder sum stored over
+// a < b, i < j (Lc, or nullptr), zero elsewhere
+int kv_assemble_t2(kvft_ctx *ctx, int batch, int nv, int no, double fac, const double *Z,
                    const double *Lc, double *T2);
 // Antisymmetric pair compression (pairs p < q, x = p(2n-p-1)/2 + q-p-1):
 // tau_c[y][(e<f)][(i<j)] from t1, t2

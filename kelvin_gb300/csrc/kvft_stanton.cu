@@ -12,7 +12,8 @@
 //            term is carried by X, saving the explicit 1/4 tau <mn||ef> GEMM)
 //   T2    += 1/2 W'_abef tau_ef^ij, W'_abef = <ab||ef> - P(ab) t_m^b <am||ef>
 //   W_mbej -= <mn||ef> (t_jn^fb / 2 + t_j^f t_n^b)     (folded over tau)
-//   Z      = t_im^ae W_mbej, then T2 += P(ij)P(ab) Z
+//   Z      = t_im^ae W_mbej, then T2 += P(ij)P(ab) Z (with the n^5 Zab and
+//            Zij terms folded into the same array, see the assembly)
 // where the first three run over antisymmetric index pairs p < q only
 // (n^6/4 flops each instead of 2 n^6), so 4.75 n^6 flops per tau point remain
 // besides about thirty n^5 terms.
@@ -36,15 +37,15 @@ inline KOut MO(double *p, KIdx r, KIdx c, long long bst) { return KOut{p, r, c, 
 // workspace layout (per tau point, doubles)
 struct WS {
     double *tau, *ttau, *Fae, *Fmi, *Fme, *Xbe, *Xmj, *Wmnij, *Wabef, *Wmbej,
-        *tmp4, *Q, *Zab, *Zij, *Zabij, *Lc;
+        *tmp4, *Q, *Z, *Lc;
 };
 
 size_t ws_per_tau(long long v, long long o) {
     long long v2o2 = v * v * o * o, o4 = o * o * o * o, v4 = v * v * v * v;
     long long big = std::max(std::max(v4, o4), v2o2);
-    // tau_c ttau Wmbej Zab Zij Zabij Lc (v2o2 each) + W'_mnij_c (o4) + W'_abef_c (v4)
+    // tau_c ttau Wmbej Z Lc (v2o2 each) + W'_mnij_c (o4) + W'_abef_c (v4)
     // + tmp4 (max) + Q (v o^3) + five small matrices
-    return (size_t)(7 * v2o2 + o4 + v4 + big + v * o * o * o + 2 * v * v + 3 * o * o + 2 * o * v);
+    return (size_t)(5 * v2o2 + o4 + v4 + big + v * o * o * o + 2 * v * v + 3 * o * o + 2 * o * v);
 }
 
 WS carve(double *base, int nb, long long v, long long o) {
@@ -56,9 +57,7 @@ WS carve(double *base, int nb, long long v, long long o) {
     w.tau = take(v2o2);
     w.ttau = take(v2o2);
     w.Wmbej = take(v2o2);
-    w.Zab = take(v2o2);
-    w.Zij = take(v2o2);
-    w.Zabij = take(v2o2);
+    w.Z = take(v2o2);
     w.Lc = take(v2o2);
     w.Wmnij = take(o4);
     w.Wabef = take(v4);
@@ -254,18 +253,24 @@ int kv_stanton(kvft_ctx *ctx, int nb, int nv, int no, const double *const F[4],
     // - oovv[m,n,e,f] (t2[f,b,j,n]/2 + t1[f,j] t1[b,n])  (M=(m,e), K=(n,f), N=(tau,b,j))
     KV_TRY(kv_make_wmbej_tmp(ctx, B, nv, no, t1, t2, w.tmp4));
     {
-        // tmp4 holds [tau][f][b][j][n] with per-tau stride v2o2 (tmp4 is sized
-        // for the largest block, so index it with the v2o2 layout directly)
+        // tmp4 holds [tau][b][j][n][f] with per-tau stride v2o2 (tmp4 is sized
+        // for the largest block, so index it with the v2o2 layout directly);
+        // the contraction index (n, f) is contiguous in both operands
         KV_TRY(kv_gemm(ctx, no * nv, B * nv * no, no * nv, 1, -1.0,
                        MA(oovv, X2(no, o * vv, nv, v), X2(no, vv, nv, 1), 0),
-                       MA(w.tmp4, X2(no, 1, nv, vo2), X3(B, v2o2, nv, oo, no, o), 0),
+                       MA(w.tmp4, X2(no, v, nv, 1), X3(B, v2o2, nv, vo2, no, vo), 0),
                        1.0, MO(w.Wmbej, X2(no, wm, nv, we), X3(B, v2o2, nv, wb, no, 1), 0)));
     }
+    // The three doubles terms share one array Z:
+    //   T2 += P(ab) Zab + P(ij) Zij + P(ab)P(ij) Zabij
+    //       = (1 - P(ab))(1 - P(ij)) (Zabij + Zab/2 + Zij/2)
+    // because Zab is antisymmetric in (i,j) and Zij in (a,b) (as t2 and the
+    // antisymmetrised integrals are), so the assembly reads one n^4 array.
     // Zabij[a,b,i,j] = t2[a,e,i,m] Wmbej[m,b,e,j]   (M=(a,i), K=(m,e), N=(b,j))
     KV_TRY(kv_gemm(ctx, nv * no, nv * no, no * nv, B, 1.0,
                    MA(t2, X2(nv, vo2, no, o), X2(no, 1, nv, oo), v2o2),
                    MA(w.Wmbej, X2(no, wm, nv, we), X2(nv, wb, no, 1), v2o2), 0.0,
-                   MO(w.Zabij, X2(nv, vo2, no, o), X2(nv, oo, no, 1), v2o2)));
+                   MO(w.Z, X2(nv, vo2, no, o), X2(nv, oo, no, 1), v2o2)));
     // Q[b,m,i,j] = vovo[b,m,e,j] t1[e,i]   (M=(b,m,j), K=e, N=i)
     KV_TRY(kv_gemm(ctx, nv * no * no, no, nv, B, 1.0,
                    MA(vovo, X3(nv, vo2, no, vo, no, 1), X1(nv, o), 0),
@@ -275,43 +280,42 @@ int kv_stanton(kvft_ctx *ctx, int nb, int nv, int no, const double *const F[4],
     KV_TRY(kv_gemm(ctx, nv, nv * no * no, no, B, 1.0,
                    MA(t1, X1(nv, o), X1(no, 1), vo),
                    MA(w.Q, X1(no, oo), X3(nv, o * oo, no, o, no, 1), vo3), 1.0,
-                   MO(w.Zabij, X1(nv, vo2), X3(nv, oo, no, o, no, 1), v2o2)));
+                   MO(w.Z, X1(nv, vo2), X3(nv, oo, no, o, no, 1), v2o2)));
 
-    // ---- Zab: t2 (F_be - 1/2 t1 F_me) and t1 vooo -----------------------------
+    // ---- Z += Zab/2: t2 (F_be - 1/2 t1 F_me) and t1 vooo ----------------------
     KV_TRY(kv_bcast(ctx, 1, vv * B, w.Fae, w.Xbe));
     KV_TRY(kv_gemm(ctx, nv, nv, no, B, -0.5, MA(t1, X1(nv, o), X1(no, 1), vo),
                    MA(w.Fme, X1(no, v), X1(nv, 1), vo), 1.0,
                    MO(w.Xbe, X1(nv, v), X1(nv, 1), vv)));
     // Zab[a,b,i,j] = t2[a,e,i,j] Xbe[b,e]   (M=(a,i,j), K=e, N=b)
-    KV_TRY(kv_gemm(ctx, nv * no * no, nv, nv, B, 1.0,
+    KV_TRY(kv_gemm(ctx, nv * no * no, nv, nv, B, 0.5,
                    MA(t2, X3(nv, vo2, no, o, no, 1), X1(nv, oo), v2o2),
-                   MA(w.Xbe, X1(nv, 1), X1(nv, v), vv), 0.0,
-                   MO(w.Zab, X3(nv, vo2, no, o, no, 1), X1(nv, oo), v2o2)));
+                   MA(w.Xbe, X1(nv, 1), X1(nv, v), vv), 1.0,
+                   MO(w.Z, X3(nv, vo2, no, o, no, 1), X1(nv, oo), v2o2)));
     // Zab += t1[a,m] vooo[b,m,i,j]   (M=a, K=m, N=(b,i,j))
-    KV_TRY(kv_gemm(ctx, nv, nv * no * no, no, B, 1.0,
+    KV_TRY(kv_gemm(ctx, nv, nv * no * no, no, B, 0.5,
                    MA(t1, X1(nv, o), X1(no, 1), vo),
                    MA(vooo, X1(no, oo), X3(nv, o * oo, no, o, no, 1), 0), 1.0,
-                   MO(w.Zab, X1(nv, vo2), X3(nv, oo, no, o, no, 1), v2o2)));
+                   MO(w.Z, X1(nv, vo2), X3(nv, oo, no, o, no, 1), v2o2)));
 
-    // ---- Zij: -t2 (F_mj + 1/2 t1 F_me) and vvvo t1 ------------------------------
+    // ---- Z += Zij/2: -t2 (F_mj + 1/2 t1 F_me) and vvvo t1 -----------------------
     KV_TRY(kv_bcast(ctx, 1, oo * B, w.Fmi, w.Xmj));
     KV_TRY(kv_gemm(ctx, no, no, nv, B, 0.5, MA(w.Fme, X1(no, v), X1(nv, 1), vo),
                    MA(t1, X1(nv, o), X1(no, 1), vo), 1.0,
                    MO(w.Xmj, X1(no, o), X1(no, 1), oo)));
     // Zij[a,b,i,j] = - t2[a,b,i,m] Xmj[m,j]   (M=(a,b,i), K=m, N=j)
-    KV_TRY(kv_gemm(ctx, nv * nv * no, no, no, B, -1.0,
+    KV_TRY(kv_gemm(ctx, nv * nv * no, no, no, B, -0.5,
                    MA(t2, X3(nv, vo2, nv, oo, no, o), X1(no, 1), v2o2),
-                   MA(w.Xmj, X1(no, o), X1(no, 1), oo), 0.0,
-                   MO(w.Zij, X3(nv, vo2, nv, oo, no, o), X1(no, 1), v2o2)));
+                   MA(w.Xmj, X1(no, o), X1(no, 1), oo), 1.0,
+                   MO(w.Z, X3(nv, vo2, nv, oo, no, o), X1(no, 1), v2o2)));
     // Zij += vvvo[a,b,e,j] t1[e,i]   (M=(a,b,j), K=e, N=i)
-    KV_TRY(kv_gemm(ctx, nv * nv * no, no, nv, B, 1.0,
+    KV_TRY(kv_gemm(ctx, nv * nv * no, no, nv, B, 0.5,
                    MA(vvvo, X3(nv, vv * o, nv, vo, no, 1), X1(nv, o), 0),
                    MA(t1, X1(nv, o), X1(no, 1), vo), 1.0,
-                   MO(w.Zij, X3(nv, vo2, nv, oo, no, 1), X1(no, o), v2o2)));
+                   MO(w.Z, X3(nv, vo2, nv, oo, no, 1), X1(no, o), v2o2)));
 
-    // ---- T2 += fac [P(ab) Zab + P(ij) Zij + P(ab)P(ij) Zabij] -------------------
-    return kv_assemble_t2(ctx, B, nv, no, fac, w.Zab, w.Zij, w.Zabij, ladders ? w.Lc : nullptr,
-                          T2);
+    // ---- T2 += fac (1 - P(ab))(1 - P(ij)) (Z + ladders) -------------------------
+    return kv_assemble_t2(ctx, B, nv, no, fac, w.Z, ladders ? w.Lc : nullptr, T2);
 }
 
 extern "C" int kvft_stanton_residual(kvft_ctx *ctx, int nb, int nv, int no,

@@ -28,10 +28,10 @@
 //
 // Kernel: persistent, one CTA per SM walking output tiles; warp 0 = TMA
 // producer, warp 1 = MMA issuer (and TMEM owner), warps 2..9 = epilogue; the
-// epilogue of one tile overlaps the MMAs of the next.  Operands are staged by TMA (64-byte swizzle, 32-element k-blocks,
-// every digit plane of a k-block per pipeline stage).  Every mbarrier wait is
-// bounded by %globaltimer; on expiry the kernel records an error word and
-// unwinds.
+// epilogue of one tile overlaps the MMAs of the next.  Operands are staged by
+// TMA (64-byte swizzle, 32-element k-blocks, every digit plane of a k-block
+// per pipeline stage).  Every mbarrier wait is bounded by %globaltimer; on
+// expiry the kernel records an error word and unwinds.
 #include "kvft_internal.h"
 
 #include <cuda.h>
@@ -43,8 +43,7 @@
 
 namespace {
 
-constexpr int TM = 128, KB = 32;
-constexpr int PLANE_BYTES = TM * KB * 2;      // one digit plane of an A k-block: 8 KB
+constexpr int TM = 128;
 constexpr int MAXS = 6;
 constexpr int KCHUNK = 2048;                  // exactness bound of the level-3 sum
 constexpr int NEPI = 8;                       // epilogue warps: two per TMEM lane quadrant
@@ -182,14 +181,18 @@ __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *map
         : "memory");
 }
 
-// UMMA shared-memory descriptor: K-major, 64-byte swizzle, 8-row groups 512 B apart
-__device__ __forceinline__ uint64_t desc_sw64(uint32_t saddr) {
+// UMMA shared-memory descriptor of a K-major operand tile whose rows are one
+// k-block of KBT BF16 values: KBT = 32 -> 64-byte swizzle (8-row groups 512 B
+// apart), KBT = 64 -> 128-byte swizzle (8-row groups 1024 B apart)
+template <int KBT>
+__device__ __forceinline__ uint64_t desc_of(uint32_t saddr) {
+    static_assert(KBT == 32 || KBT == 64, "k-block of 32 or 64");
     uint64_t d = 0;
     d |= (uint64_t)((saddr & 0x3FFFF) >> 4);
-    d |= (uint64_t)1 << 16;              // leading byte offset (unused, K-major swizzled)
-    d |= (uint64_t)(512 >> 4) << 32;     // stride byte offset
-    d |= (uint64_t)1 << 46;              // descriptor version
-    d |= (uint64_t)4 << 61;              // SWIZZLE_64B
+    d |= (uint64_t)1 << 16;                         // leading byte offset (unused)
+    d |= (uint64_t)((8 * KBT * 2) >> 4) << 32;      // stride byte offset
+    d |= (uint64_t)1 << 46;                         // descriptor version
+    d |= (uint64_t)(KBT == 32 ? 4 : 2) << 61;       // SWIZZLE_64B / SWIZZLE_128B
     return d;
 }
 
@@ -266,8 +269,8 @@ __device__ __forceinline__ void tmem_wait_ld() {
 // Shared-memory bytes of the kernel: 1 KB alignment slack, NS pipeline stages
 // (S digit planes of A and of B per stage), the barriers, the epilogue's
 // per-warp column tables and two words (TMEM base, failure flag).
-__host__ __device__ constexpr size_t tc_smem(int S, int NS, int tn) {
-    return 1024 + (size_t)NS * S * (PLANE_BYTES + tn * KB * 2) + 8 * (2 * NS + 5) +
+__host__ __device__ constexpr size_t tc_smem(int S, int NS, int tn, int kb) {
+    return 1024 + (size_t)NS * S * (TM + tn) * kb * 2 + 8 * (2 * NS + 5) +
            (size_t)NEPI * (tn / 2) * 12 + 16;
 }
 
@@ -294,11 +297,12 @@ __host__ __device__ constexpr size_t tc_smem(int S, int NS, int tn) {
 // to six levels (384 columns), one set; the epilogue frees it as soon as the
 // levels are in registers (a few percent of a chunk's MMA time), and writes
 // the tile while the next chunk accumulates.
-template <int TN, bool FF>
+template <int TN, bool FF, int KBT>
 __global__ void __launch_bounds__(NTHREADS, 1)
 tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                TcParams p) {
-    constexpr int BPLANE = TN * KB * 2;      // one digit plane of a B k-block
+    constexpr int PLANE_BYTES = TM * KBT * 2;    // one digit plane of an A k-block
+    constexpr int BPLANE = TN * KBT * 2;         // one digit plane of a B k-block
     constexpr int WCOLS = TN / 2;            // columns per epilogue warp
     constexpr int LW = FF ? 4 : 16;          // columns per TMEM load (<= 32 registers in flight)
     constexpr int NG = WCOLS / LW;           // TMEM loads per level
@@ -370,7 +374,7 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
                     }
                     const uint32_t fb = smem_u32(&full[st]);
                     mbar_expect_tx(fb, bytes);
-                    const int x = kb * KB;
+                    const int x = kb * KBT;
                     for (int s = 0; s < S; s++) {
                         tma_load_2d(smem_u32(sA + st * stage_a + s * PLANE_BYTES), &tmA, x,
                                     ya + s * p.Mp, fb);
@@ -429,16 +433,16 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
                         // first k-step of a chunk starts every level (s = 1
                         // reaches all of them) and later ones accumulate
 #pragma unroll
-                        for (int kk = 0; kk < KB / 16; kk++) {
+                        for (int kk = 0; kk < KBT / 16; kk++) {
                             for (int s = 1; s <= S && s < p.D; s++) {
                                 const int tmax = min(S, p.D - s);
                                 const uint64_t da =
-                                    desc_sw64(a0 + (s - 1) * PLANE_BYTES + kk * 32);
+                                    desc_of<KBT>(a0 + (s - 1) * PLANE_BYTES + kk * 32);
                                 const uint32_t acc = (kb > c0 || kk > 0 || s > 1) ? 1u : 0u;
                                 for (int t0 = 1; t0 <= tmax; t0 += PMAX) {
                                     const int np = min(PMAX, tmax - t0 + 1);
                                     const uint64_t db =
-                                        desc_sw64(b0 + (t0 - 1) * BPLANE + kk * 32);
+                                        desc_of<KBT>(b0 + (t0 - 1) * BPLANE + kk * 32);
                                     umma(tacc + (s + t0 - 2) * TN, da, db, idesc_of(np * TN),
                                          acc);
                                 }
@@ -473,6 +477,23 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
         for (int u = blockIdx.x; u < p.units && ok; u += gridDim.x) {
             const Unit w = unit_of(p, u, TN);
             if (w.kb0 >= w.kb1) continue;
+            // C addresses of this unit; with beta != 0 the old values are
+            // prefetched into L2 now, while the MMAs run, so the read-modify-
+            // write below is not bound by the few loads a warp keeps in flight
+            const int nw = w.n0 + h * WCOLS;          // first column of this warp
+            for (int i = lane; i < WCOLS; i += 32) {
+                const int n = nw + i;
+                coff[i] = (n < p.N) ? p.C.c.off(n) : 0;
+                cexp[i] = (n < p.N) ? exp_of(p.eb[(long long)w.b * p.eb_bst + n]) : 0;
+            }
+            __syncwarp();
+            const int m = w.m0 + row;
+            const int nlim = p.N - nw;
+            double *Cr = p.C.p + (long long)w.b * p.C.bst + (m < p.M ? p.C.r.off(m) : 0);
+            if (m < p.M && p.nsplit == 1 && p.beta != 0.0) {
+                for (int i = 0; i < min(WCOLS, nlim); i++)
+                    asm volatile("prefetch.global.L2 [%0];" ::"l"(Cr + coff[i]));
+            }
             for (int c0 = w.kb0; c0 < w.kb1; c0 += p.chunk_kb) {
                 const int set = gc % NSET;
                 const bool got = mbar_wait(smem_u32(&accf[set]), (gc / NSET) & 1);
@@ -532,18 +553,8 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
             }
             if (!ok) break;
             // ---- the tile to C ----
-            const int nw = w.n0 + h * WCOLS;          // first column of this warp
-            for (int i = lane; i < WCOLS; i += 32) {
-                const int n = nw + i;
-                coff[i] = (n < p.N) ? p.C.c.off(n) : 0;
-                cexp[i] = (n < p.N) ? exp_of(p.eb[(long long)w.b * p.eb_bst + n]) : 0;
-            }
-            __syncwarp();
-            const int m = w.m0 + row;
             if (m < p.M) {
                 const int krow = exp_of(p.ea[(long long)w.b * p.ea_bst + m]) - 14 + p.alpha_exp;
-                double *Cr = p.C.p + (long long)w.b * p.C.bst + p.C.r.off(m);
-                const int nlim = p.N - nw;
 #pragma unroll
                 for (int g = 0; g < WCOLS / WG; g++) {
                     double out[WG];
@@ -604,56 +615,89 @@ struct PackView {
 // Operand tiles of 32 rows x 64 k go through shared memory so that global
 // reads are coalesced along whichever operand index is contiguous in memory
 // (the row index for some permuted views, k for others) and plane writes are
-// coalesced along k.
+// coalesced along k.  The composite-index offsets of the tile's rows and k
+// columns are computed once per tile (96 divisions instead of one per
+// element) and kept in shared memory; -1 marks a row or column outside the
+// view.
 constexpr int PT_R = 32, PT_K = 64;
 
+struct PackTile {
+    unsigned long long v[PT_R][PT_K + 1];
+    long long roff[PT_R];
+    long long koff[PT_K];
+};
+
 __device__ __forceinline__ void load_tile(const PackView &v, int b, int r0, int k0, int R, int K,
-                                          bool rows_fast,
-                                          unsigned long long (*tile)[PT_K + 1]) {
-    const int tx = threadIdx.x % 32, ty = threadIdx.x / 32;
+                                          bool rows_fast, PackTile &t) {
+    const int tid = threadIdx.x, tx = tid % 32, ty = tid / 32;
+    if (tid < PT_R) {
+        const int row = r0 + tid;
+        t.roff[tid] = (row < R) ? v.r.off(row) : -1;
+    } else if (tid < PT_R + PT_K) {
+        const int k = k0 + tid - PT_R;
+        t.koff[tid - PT_R] = (k < K) ? v.c.off(k) : -1;
+    }
+    __syncthreads();
     const double *base = v.p + (long long)b * v.bst;
     if (rows_fast) {
-        const int row = r0 + tx;
-        const long long ro = (row < R) ? v.r.off(row) : 0;
-        for (int kk = ty; kk < PT_K; kk += 8) {
-            const int k = k0 + kk;
-            tile[tx][kk] =
-                (row < R && k < K) ? (unsigned long long)__double_as_longlong(base[ro + v.c.off(k)])
-                                   : 0ull;
+        const long long ro = t.roff[tx];
+#pragma unroll
+        for (int i = 0; i < PT_K / 8; i++) {
+            const int kk = ty + 8 * i;
+            const long long ko = t.koff[kk];
+            t.v[tx][kk] = (ro >= 0 && ko >= 0)
+                              ? (unsigned long long)__double_as_longlong(__ldg(base + ro + ko))
+                              : 0ull;
         }
     } else {
-        for (int rr = ty; rr < PT_R; rr += 8) {
-            const int row = r0 + rr;
-            const long long ro = (row < R) ? v.r.off(row) : 0;
-            for (int h = 0; h < 2; h++) {
-                const int k = k0 + tx + 32 * h;
-                tile[rr][tx + 32 * h] =
-                    (row < R && k < K)
-                        ? (unsigned long long)__double_as_longlong(base[ro + v.c.off(k)])
-                        : 0ull;
-            }
+        const long long ko0 = t.koff[tx], ko1 = t.koff[tx + 32];
+#pragma unroll
+        for (int i = 0; i < PT_R / 8; i++) {
+            const int rr = ty + 8 * i;
+            const long long ro = t.roff[rr];
+            t.v[rr][tx] = (ro >= 0 && ko0 >= 0)
+                              ? (unsigned long long)__double_as_longlong(__ldg(base + ro + ko0))
+                              : 0ull;
+            t.v[rr][tx + 32] = (ro >= 0 && ko1 >= 0)
+                                   ? (unsigned long long)__double_as_longlong(__ldg(base + ro + ko1))
+                                   : 0ull;
         }
     }
 }
 
-// raw row exponents: max binary exponent over each tile row, atomicMax'ed
+// raw row exponents: max binary exponent over each row of `ktiles`
+// consecutive 64-wide k tiles, one atomicMax per row and block
 __global__ void __launch_bounds__(256)
-pack_exp_kernel(PackView v, int R, int K, int rows_fast, int *__restrict__ ex) {
-    __shared__ unsigned long long tile[PT_R][PT_K + 1];
-    const int b = blockIdx.z, r0 = blockIdx.y * PT_R, k0 = blockIdx.x * PT_K;
-    load_tile(v, b, r0, k0, R, K, rows_fast, tile);
-    __syncthreads();
+pack_exp_kernel(PackView v, int R, int K, int rows_fast, int ktiles, int *__restrict__ ex) {
+    __shared__ PackTile tile;
+    const int b = blockIdx.z, r0 = blockIdx.y * PT_R;
     const int lane = threadIdx.x % 32, w = threadIdx.x / 32;
-    for (int rr = w; rr < PT_R; rr += 8) {
-        int emax = -2000;
-        for (int h = 0; h < 2; h++) {
-            const unsigned long long bits = tile[rr][lane + 32 * h];
-            if ((bits & 0x7FFFFFFFFFFFFFFFull) != 0)
-                emax = max(emax, (int)((bits >> 52) & 0x7FF) - 1023);
+    int emax[PT_R / 8];
+#pragma unroll
+    for (int i = 0; i < PT_R / 8; i++) emax[i] = -2000;
+    for (int t = 0; t < ktiles; t++) {
+        const int k0 = (blockIdx.x * ktiles + t) * PT_K;
+        if (k0 >= K) break;
+        // the barrier inside load_tile orders these tile writes after the
+        // previous tile's reads
+        load_tile(v, b, r0, k0, R, K, rows_fast, tile);
+        __syncthreads();
+#pragma unroll
+        for (int i = 0; i < PT_R / 8; i++) {
+            const int rr = w + 8 * i;
+            for (int h = 0; h < 2; h++) {
+                const unsigned long long bits = tile.v[rr][lane + 32 * h];
+                if ((bits & 0x7FFFFFFFFFFFFFFFull) != 0)
+                    emax[i] = max(emax[i], (int)((bits >> 52) & 0x7FF) - 1023);
+            }
         }
-        for (int o = 16; o > 0; o >>= 1) emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, o));
-        const int row = r0 + rr;
-        if (lane == 0 && emax > -2000 && row < R) atomicMax(&ex[(long long)b * R + row], emax);
+    }
+#pragma unroll
+    for (int i = 0; i < PT_R / 8; i++) {
+        int e = emax[i];
+        for (int o = 16; o > 0; o >>= 1) e = max(e, __shfl_xor_sync(0xffffffffu, e, o));
+        const int row = r0 + w + 8 * i;
+        if (lane == 0 && e > -2000 && row < R) atomicMax(&ex[(long long)b * R + row], e);
     }
 }
 
@@ -688,7 +732,7 @@ template <int S>
 __global__ void __launch_bounds__(256)
 pack_digits_kernel(PackView v, int R, int K, int ld, int rows_fast, const int *__restrict__ ex,
                    __nv_bfloat16 *__restrict__ out) {
-    __shared__ unsigned long long tile[PT_R][PT_K + 1];
+    __shared__ PackTile tile;
     const int b = blockIdx.z, r0 = blockIdx.y * PT_R, k0 = blockIdx.x * PT_K;
     load_tile(v, b, r0, k0, R, K, rows_fast, tile);
     __syncthreads();
@@ -701,14 +745,15 @@ pack_digits_kernel(PackView v, int R, int K, int ld, int rows_fast, const int *_
         if (row >= R) break;
         const int e = exp_of(ex[(long long)b * R + row]);
         int d0[MAXS], d1[MAXS];
-        digits_of(tile[rr][2 * tx], e, S, d0);
-        digits_of(tile[rr][2 * tx + 1], e, S, d1);    // zero beyond K (tile fill)
+        digits_of(tile.v[rr][2 * tx], e, S, d0);
+        digits_of(tile.v[rr][2 * tx + 1], e, S, d1);    // zero beyond K (tile fill)
         __nv_bfloat16 *ob = out + (size_t)b * S * plane + (size_t)row * ld + k;
 #pragma unroll
         for (int s = 0; s < S; s++) {
+            const float sc = __int_as_float((127 - 7 * s) << 23);    // 2^-7s, exact
             __nv_bfloat162 w2;
-            w2.x = __float2bfloat16_rn(ldexpf((float)d0[s], -7 * s));
-            w2.y = __float2bfloat16_rn(ldexpf((float)d1[s], -7 * s));
+            w2.x = __float2bfloat16_rn((float)d0[s] * sc);
+            w2.y = __float2bfloat16_rn((float)d1[s] * sc);
             *reinterpret_cast<__nv_bfloat162 *>(ob + (size_t)s * plane) = w2;
         }
     }
@@ -734,17 +779,18 @@ EncodeTiledFn encode_fn() {
 }
 
 // 2D map over digit planes (K x rows, row stride ld elements); one box is a
-// k-block of box_rows rows
-int make_map(kvft_ctx *ctx, CUtensorMap *map, void *base, int K, int ld, long long rows,
+// k-block of kb values (swizzled by its 2 kb bytes) by box_rows rows
+int make_map(kvft_ctx *ctx, CUtensorMap *map, void *base, int K, int ld, long long rows, int kb,
              int box_rows) {
     EncodeTiledFn fn = encode_fn();
     if (!fn) return kv_fail(ctx, KVFT_EDEVICE, "cuTensorMapEncodeTiled unavailable");
     cuuint64_t dims[2] = {(cuuint64_t)K, (cuuint64_t)rows};
     cuuint64_t strides[1] = {(cuuint64_t)ld * 2};
-    cuuint32_t box[2] = {KB, (cuuint32_t)box_rows};
+    cuuint32_t box[2] = {(cuuint32_t)kb, (cuuint32_t)box_rows};
     cuuint32_t estr[2] = {1, 1};
     CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, base, dims, strides, box, estr,
-                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE,
+                    kb == 64 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B,
                     CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) return kv_fail(ctx, KVFT_EDEVICE, "cuTensorMapEncodeTiled failed");
     return KVFT_OK;
@@ -779,11 +825,16 @@ int pack(kvft_ctx *ctx, const char *key, const PackView &v, int R, int K, int nb
     KvProfScope prof(ctx, KV_CAT_PACK, 8.0 * nb * (double)R * K + (double)nb * S * plane_bytes);
     KV_CHECK(ctx, cudaMemsetAsync(out->ex, 0x80, (size_t)nb * R * sizeof(int), ctx->stream));
     // coalesce global reads along the contiguous index
-    const int rows_fast = (v.r.st[2] == 1 && v.c.st[2] != 1) ? 1 : 0;
+    const int rows_fast = (kidx_fast_stride(v.r) == 1 && kidx_fast_stride(v.c) != 1) ? 1 : 0;
     const long long rtiles = (R + PT_R - 1) / PT_R;
     if (rtiles > 65535) return kv_fail(ctx, KVFT_EINVAL, "pack: too many rows");
     const dim3 g((K + PT_K - 1) / PT_K, (unsigned)rtiles, nb);
-    pack_exp_kernel<<<g, 256, 0, ctx->stream>>>(v, R, K, rows_fast, out->ex);
+    // long rows: each exponent block walks up to 16 k tiles, so that about
+    // 32 blocks per SM remain and the atomics per row drop accordingly
+    const long long tiles = (long long)g.x * g.y * g.z;
+    const int ktiles = (int)std::max(1LL, std::min(16LL, tiles / (32LL * ctx->sm_count)));
+    const dim3 ge((g.x + ktiles - 1) / ktiles, g.y, g.z);
+    pack_exp_kernel<<<ge, 256, 0, ctx->stream>>>(v, R, K, rows_fast, ktiles, out->ex);
     KV_TRY(kv_launch_check(ctx, "pack_exp"));
     switch (S) {
 #define KV_PACK_CASE(s_)                                                                    \
@@ -801,11 +852,10 @@ int pack(kvft_ctx *ctx, const char *key, const PackView &v, int R, int K, int nb
 }
 
 // The stride-1 index of a view: its fastest dimension of extent > 1 has
-// element stride 1.
+// element stride 1 (or the index has a single value).
 bool unit_stride(const KIdx &x) {
-    for (int d = 2; d >= 0; d--)
-        if (x.size[d] > 1) return x.st[d] == 1;
-    return true;
+    const long long f = kidx_fast_stride(x);
+    return f == 1 || f == 0;
 }
 
 constexpr size_t SMEM_CAP = 225 * 1024;
@@ -813,42 +863,46 @@ constexpr size_t SMEM_CAP = 225 * 1024;
 // second one's 512-column TMEM allocation would block: always take more.
 constexpr size_t SMEM_FLOOR = 120 * 1024;
 
-template <int TN, bool FF>
+template <int TN, bool FF, int KBT>
 int launch_tc(kvft_ctx *ctx, const CUtensorMap &ma, const CUtensorMap &mb, TcParams &p) {
     int NS = 2;
-    while (NS < 8 && tc_smem(p.S, NS + 1, TN) <= SMEM_CAP) NS++;
-    if (tc_smem(p.S, NS, TN) > SMEM_CAP)
+    while (NS < 8 && tc_smem(p.S, NS + 1, TN, KBT) <= SMEM_CAP) NS++;
+    if (tc_smem(p.S, NS, TN, KBT) > SMEM_CAP)
         return kv_fail(ctx, KVFT_EINVAL, "tensor-core gemm: stages exceed shared memory");
     p.NS = NS;
-    const size_t smem = std::max(tc_smem(p.S, NS, TN), SMEM_FLOOR);
+    const size_t smem = std::max(tc_smem(p.S, NS, TN, KBT), SMEM_FLOOR);
     static bool attr = false;
     if (!attr) {
-        KV_CHECK(ctx, cudaFuncSetAttribute(tc_gemm_kernel<TN, FF>,
+        KV_CHECK(ctx, cudaFuncSetAttribute(tc_gemm_kernel<TN, FF, KBT>,
                                            cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            (int)SMEM_CAP));
         attr = true;
     }
     const int grid = std::min(p.units, ctx->sm_count);
-    tc_gemm_kernel<TN, FF><<<grid, NTHREADS, smem, ctx->stream>>>(ma, mb, p);
+    tc_gemm_kernel<TN, FF, KBT><<<grid, NTHREADS, smem, ctx->stream>>>(ma, mb, p);
     return kv_launch_check(ctx, "tc_gemm");
 }
 
 int gemm_tc_run(kvft_ctx *ctx, int M, int N, int K, int batch, double alpha, const KMat &A,
                 const KMat &B, double beta, const KOut &C, int D) {
     const int S = std::min(D - 1, MAXS);
-    const bool ff = D >= 4;            // three or four accumulators: FP32 pairs, TN = 64
+    // D >= 4: three to six levels, FP32 pairs, TN = 64, and 32-deep k-blocks
+    // (six digit planes per stage); D <= 3: 64-deep k-blocks, so that every
+    // TMA box row is a full 128-byte line
+    const bool ff = D >= 4;
     const int tn = ff ? 64 : 128;
+    const int kb = ff ? 32 : 64;
     const int nbA = A.bst ? batch : 1, nbB = B.bst ? batch : 1;
     Packed pa, pb;
     KV_TRY(pack(ctx, "tc_pack_a", PackView{A.p, A.r, A.c, A.bst}, M, K, nbA, S, &pa));
     // B is K x N; its K-major form has rows = N (B's column index), cols = K
     KV_TRY(pack(ctx, "tc_pack_b", PackView{B.p, B.c, B.r, B.bst}, N, K, nbB, S, &pb));
     CUtensorMap ma, mb;
-    KV_TRY(make_map(ctx, &ma, pa.planes, pa.K, pa.ld, (long long)nbA * S * pa.R, TM));
-    KV_TRY(make_map(ctx, &mb, pb.planes, pb.K, pb.ld, (long long)nbB * S * pb.R, tn));
+    KV_TRY(make_map(ctx, &ma, pa.planes, pa.K, pa.ld, (long long)nbA * S * pa.R, kb, TM));
+    KV_TRY(make_map(ctx, &mb, pb.planes, pb.K, pb.ld, (long long)nbB * S * pb.R, kb, tn));
     const int mt = (M + TM - 1) / TM, nt = (N + tn - 1) / tn;
-    const int nkb_total = (K + KB - 1) / KB;
-    const int nchunks = (nkb_total + KCHUNK / KB - 1) / (KCHUNK / KB);
+    const int nkb_total = (K + kb - 1) / kb;
+    const int nchunks = (nkb_total + KCHUNK / kb - 1) / (KCHUNK / kb);
     const int chunk_kb = (nkb_total + nchunks - 1) / nchunks;     // balanced chunks
     const long long tiles = (long long)mt * nt * batch;
     // fewer output tiles than two waves of SMs and several K chunks: every
@@ -889,7 +943,7 @@ int gemm_tc_run(kvft_ctx *ctx, int M, int N, int K, int batch, double alpha, con
     }
     p.C = C;
     p.err = ctx->dflag;
-    return ff ? launch_tc<64, true>(ctx, ma, mb, p) : launch_tc<128, false>(ctx, ma, mb, p);
+    return ff ? launch_tc<64, true, 32>(ctx, ma, mb, p) : launch_tc<128, false, 64>(ctx, ma, mb, p);
 }
 
 }  // namespace
