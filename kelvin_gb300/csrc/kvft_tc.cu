@@ -297,10 +297,15 @@ __host__ __device__ constexpr size_t tc_smem(int S, int NS, int tn, int kb) {
 // to six levels (384 columns), one set; the epilogue frees it as soon as the
 // levels are in registers (a few percent of a chunk's MMA time), and writes
 // the tile while the next chunk accumulates.
-template <int TN, bool FF, int KBT>
+//
+// DL (the digit levels D) is a template parameter: the MMA issue loop is then
+// straight-line code whose descriptors are per-stage bases plus constant
+// offsets, so the single issuing thread keeps up with the tensor core.
+template <int TN, bool FF, int KBT, int DL>
 __global__ void __launch_bounds__(NTHREADS, 1)
 tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                TcParams p) {
+    constexpr int SD = DL - 1 < MAXS ? DL - 1 : MAXS;   // digit planes
     constexpr int PLANE_BYTES = TM * KBT * 2;    // one digit plane of an A k-block
     constexpr int BPLANE = TN * KBT * 2;         // one digit plane of a B k-block
     constexpr int WCOLS = TN / 2;            // columns per epilogue warp
@@ -315,8 +320,9 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
     constexpr uint32_t IDESC = idesc_of(TN);
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-    const int S = p.S, NS = p.NS;
-    const size_t stage_a = (size_t)S * PLANE_BYTES, stage_b = (size_t)S * BPLANE;
+    constexpr int S = SD;
+    const int NS = p.NS;
+    constexpr uint32_t stage_a = S * PLANE_BYTES, stage_b = S * BPLANE;
     uint8_t *sA = smem;
     uint8_t *sB = smem + NS * stage_a;
     uint64_t *bars = (uint64_t *)(sB + NS * stage_b);
@@ -402,6 +408,10 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
     } else if (warp == 1) {
         if (lane == 0) {
             // ---- MMA issuer ----
+            // descriptors of stage 0's first planes; a stage or plane offset
+            // adds (offset >> 4) to the address field (all of shared memory
+            // fits its 14 bits)
+            const uint64_t dA0 = desc_of<KBT>(smem_u32(sA)), dB0 = desc_of<KBT>(smem_u32(sB));
             int st = 0, gc = 0;
             uint32_t ph = 0;
             bool ok = true;
@@ -426,23 +436,26 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
                             break;
                         }
                         fence_after();
-                        const uint32_t a0 = smem_u32(sA + st * stage_a);
-                        const uint32_t b0 = smem_u32(sB + st * stage_b);
                         // A plane s against B planes t0.. (adjacent in shared
                         // memory) into levels s + t0.. (adjacent in TMEM); the
                         // first k-step of a chunk starts every level (s = 1
                         // reaches all of them) and later ones accumulate
+                        const uint64_t dA = dA0 + ((st * stage_a) >> 4);
+                        const uint64_t dB = dB0 + ((st * stage_b) >> 4);
+                        const uint32_t later = (kb > c0) ? 1u : 0u;
 #pragma unroll
                         for (int kk = 0; kk < KBT / 16; kk++) {
-                            for (int s = 1; s <= S && s < p.D; s++) {
-                                const int tmax = min(S, p.D - s);
-                                const uint64_t da =
-                                    desc_of<KBT>(a0 + (s - 1) * PLANE_BYTES + kk * 32);
-                                const uint32_t acc = (kb > c0 || kk > 0 || s > 1) ? 1u : 0u;
+#pragma unroll
+                            for (int s = 1; s <= S; s++) {
+                                if (s >= DL) continue;
+                                const int tmax = min(S, DL - s);
+                                const uint32_t acc = (kk > 0 || s > 1) ? 1u : later;
+                                const uint64_t da = dA + (((s - 1) * PLANE_BYTES + kk * 32) >> 4);
+#pragma unroll
                                 for (int t0 = 1; t0 <= tmax; t0 += PMAX) {
                                     const int np = min(PMAX, tmax - t0 + 1);
                                     const uint64_t db =
-                                        desc_of<KBT>(b0 + (t0 - 1) * BPLANE + kk * 32);
+                                        dB + (((t0 - 1) * BPLANE + kk * 32) >> 4);
                                     umma(tacc + (s + t0 - 2) * TN, da, db, idesc_of(np * TN),
                                          acc);
                                 }
@@ -467,7 +480,7 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
         // ---- epilogue ----
         const int ew = warp - 2, q = warp & 3, h = ew >> 2;
         const int row = q * 32 + lane;
-        const int nl = p.D - 1;                     // levels 2..D
+        constexpr int nl = DL - 1;                  // levels 2..D
         long long *coff = s_coff + ew * WCOLS;
         int *cexp = s_cexp + ew * WCOLS;
         float rhi[WCOLS];
@@ -863,8 +876,10 @@ constexpr size_t SMEM_CAP = 225 * 1024;
 // second one's 512-column TMEM allocation would block: always take more.
 constexpr size_t SMEM_FLOOR = 120 * 1024;
 
-template <int TN, bool FF, int KBT>
+// Launches the persistent kernel, one CTA per SM.
+template <int TN, bool FF, int KBT, int DL>
 int launch_tc(kvft_ctx *ctx, const CUtensorMap &ma, const CUtensorMap &mb, TcParams &p) {
+    auto kern = tc_gemm_kernel<TN, FF, KBT, DL>;
     int NS = 2;
     while (NS < 8 && tc_smem(p.S, NS + 1, TN, KBT) <= SMEM_CAP) NS++;
     if (tc_smem(p.S, NS, TN, KBT) > SMEM_CAP)
@@ -873,13 +888,12 @@ int launch_tc(kvft_ctx *ctx, const CUtensorMap &ma, const CUtensorMap &mb, TcPar
     const size_t smem = std::max(tc_smem(p.S, NS, TN, KBT), SMEM_FLOOR);
     static bool attr = false;
     if (!attr) {
-        KV_CHECK(ctx, cudaFuncSetAttribute(tc_gemm_kernel<TN, FF, KBT>,
-                                           cudaFuncAttributeMaxDynamicSharedMemorySize,
+        KV_CHECK(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            (int)SMEM_CAP));
         attr = true;
     }
     const int grid = std::min(p.units, ctx->sm_count);
-    tc_gemm_kernel<TN, FF, KBT><<<grid, NTHREADS, smem, ctx->stream>>>(ma, mb, p);
+    kern<<<grid, NTHREADS, smem, ctx->stream>>>(ma, mb, p);
     return kv_launch_check(ctx, "tc_gemm");
 }
 
@@ -943,7 +957,14 @@ int gemm_tc_run(kvft_ctx *ctx, int M, int N, int K, int batch, double alpha, con
     }
     p.C = C;
     p.err = ctx->dflag;
-    return ff ? launch_tc<64, true, 32>(ctx, ma, mb, p) : launch_tc<128, false, 64>(ctx, ma, mb, p);
+    switch (D) {
+    case 2: return launch_tc<128, false, 64, 2>(ctx, ma, mb, p);
+    case 3: return launch_tc<128, false, 64, 3>(ctx, ma, mb, p);
+    case 4: return launch_tc<64, true, 32, 4>(ctx, ma, mb, p);
+    case 5: return launch_tc<64, true, 32, 5>(ctx, ma, mb, p);
+    case 6: return launch_tc<64, true, 32, 6>(ctx, ma, mb, p);
+    default: return launch_tc<64, true, 32, 7>(ctx, ma, mb, p);
+    }
 }
 
 }  // namespace

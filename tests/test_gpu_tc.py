@@ -61,11 +61,12 @@ def test_tc_gemm_accuracy(ctx, M, N, K, batch, digits):
 
 # Unit schedules of the persistent kernel: K chunks summed inside one unit
 # (>= two waves of tiles), K chunks as separate units added by atomics (few
-# tiles), C's contiguous index kept on the columns (narrow N, long K), and
-# skinny products (N = 1, 8) against a long K.
+# tiles), C's contiguous index kept on the columns (narrow N, long K), skinny
+# products (N = 1, 8) against a long K, and many waves of persistent tiles
+# with ragged edges in both directions (31 m-tiles, 24 or 47 n-tiles).
 @pytest.mark.parametrize("M,N,K,batch", [(2048, 2560, 4200, 1), (640, 640, 2500, 8),
                                          (300, 40, 1000, 1), (3000, 8, 5000, 1),
-                                         (1444, 1, 1444, 6)])
+                                         (1444, 1, 1444, 6), (3900, 3000, 2100, 1)])
 @pytest.mark.parametrize("digits", [3, 7])
 def test_tc_gemm_unit_schedules(ctx, M, N, K, batch, digits):
     rng = numpy.random.default_rng(M + 3 * N + K + digits)
@@ -73,6 +74,18 @@ def test_tc_gemm_unit_schedules(ctx, M, N, K, batch, digits):
     B = rng.standard_normal((batch, K, N))
     C = gemm(ctx, A, B, _lib.PREC_FP64_TC, digits)
     assert normwise(C, A, B) < TOL[digits]
+
+
+@pytest.mark.parametrize("digits", [2, 3, 4, 5, 6, 7])
+def test_tc_gemm_every_digit_count(ctx, digits):
+    """Each digit count is its own kernel instance (levels fixed at compile
+    time); the error falls by ~2^-7 per level."""
+    rng = numpy.random.default_rng(100 + digits)
+    A = rng.standard_normal((2, 300, 2500))
+    B = rng.standard_normal((2, 2500, 260))
+    C = gemm(ctx, A, B, _lib.PREC_FP64_TC, digits)
+    tol = TOL.get(digits, 5e-11 if digits == 6 else None)
+    assert normwise(C, A, B) < tol
 
 
 def test_tc_gemm_matches_fp64_engine(ctx):
