@@ -503,6 +503,8 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
             const int m = w.m0 + row;
             const int nlim = p.N - nw;
             double *Cr = p.C.p + (long long)w.b * p.C.bst + (m < p.M ? p.C.r.off(m) : 0);
+            const int krow =
+                (m < p.M) ? exp_of(p.ea[(long long)w.b * p.ea_bst + m]) - 14 + p.alpha_exp : 0;
             if (m < p.M && p.nsplit == 1 && p.beta != 0.0) {
                 for (int i = 0; i < min(WCOLS, nlim); i++)
                     asm volatile("prefetch.global.L2 [%0];" ::"l"(Cr + coff[i]));
@@ -567,37 +569,55 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
             if (!ok) break;
             // ---- the tile to C ----
             if (m < p.M) {
-                const int krow = exp_of(p.ea[(long long)w.b * p.ea_bst + m]) - 14 + p.alpha_exp;
+                // value of column i of this thread's row
+                auto value = [&](int i) -> double {
+                    const int k = krow + cexp[i];
+                    double v = f32_scaled(rhi[i], k, p.alpha_sign);
+                    if constexpr (FF) v += f32_scaled(rlo[i], k, p.alpha_sign);
+                    if (!p.alpha_pow2) v *= p.alpha;
+                    return v;
+                };
+                if (p.nsplit > 1 || p.beta == 1.0) {
+                    // C += value: each element gets exactly one addition in
+                    // this launch unless K chunks run as separate units, so a
+                    // fire-and-forget reduction at L2 gives old + value
+                    // rounded once, like a load-add-store, without the
+                    // thread waiting for the old value
 #pragma unroll
-                for (int g = 0; g < WCOLS / WG; g++) {
-                    double out[WG];
+                    for (int i = 0; i < WCOLS; i++)
+                        if (i < nlim) atomicAdd(Cr + coff[i], value(i));
+                } else if (p.beta == 0.0) {
 #pragma unroll
-                    for (int j = 0; j < WG; j++) {
-                        const int i = g * WG + j;
-                        const int k = krow + cexp[i];
-                        double v = f32_scaled(rhi[i], k, p.alpha_sign);
-                        if constexpr (FF) v += f32_scaled(rlo[i], k, p.alpha_sign);
-                        if (!p.alpha_pow2) v *= p.alpha;
-                        out[j] = v;
-                    }
-                    if (p.nsplit > 1) {
+                    for (int i = 0; i < WCOLS; i++)
+                        if (i < nlim) Cr[coff[i]] = value(i);
+                } else {
+                    // read-modify-write: the old values of the next RING
+                    // groups of WG columns are in flight while one group is
+                    // combined and stored
+                    constexpr int NGW = WCOLS / WG, RING = FF ? 3 : 2;
+                    double old[RING][WG];
+#pragma unroll
+                    for (int q = 0; q < RING; q++)
 #pragma unroll
                         for (int j = 0; j < WG; j++)
-                            if (g * WG + j < nlim) atomicAdd(Cr + coff[g * WG + j], out[j]);
-                    } else {
-                        if (p.beta != 0.0) {
-                            double old[WG];
+                            old[q][j] = (q < NGW && q * WG + j < nlim) ? Cr[coff[q * WG + j]] : 0.0;
 #pragma unroll
-                            for (int j = 0; j < WG; j++)
-                                old[j] = (g * WG + j < nlim) ? Cr[coff[g * WG + j]] : 0.0;
+                    for (int g = 0; g < NGW; g++) {
+                        const int q = g % RING;
 #pragma unroll
-                            for (int j = 0; j < WG; j++)
-                                out[j] = (p.beta == 1.0) ? old[j] + out[j]
-                                                         : fma(p.beta, old[j], out[j]);
+                        for (int j = 0; j < WG; j++) {
+                            const int i = g * WG + j;
+                            const double v = (p.beta == 1.0) ? old[q][j] + value(i)
+                                                             : fma(p.beta, old[q][j], value(i));
+                            if (i < nlim) Cr[coff[i]] = v;
                         }
+                        if (g + RING < NGW) {
 #pragma unroll
-                        for (int j = 0; j < WG; j++)
-                            if (g * WG + j < nlim) Cr[coff[g * WG + j]] = out[j];
+                            for (int j = 0; j < WG; j++) {
+                                const int i = (g + RING) * WG + j;
+                                old[q][j] = (i < nlim) ? Cr[coff[i]] : 0.0;
+                            }
+                        }
                     }
                 }
             }
