@@ -31,40 +31,55 @@ __device__ __forceinline__ void pair_of(int x, int n, int &p, int &q) {
     q = x - pair_start(p, n) + p + 1;
 }
 
-__global__ void axpby4_kernel(long long total, Dims4 g, double alpha,
-                              const double *__restrict__ src, double beta,
-                              double *__restrict__ dst) {
-    for (long long x = blockIdx.x * (long long)blockDim.x + threadIdx.x; x < total;
-         x += (long long)gridDim.x * blockDim.x) {
-        long long r = x;
-        int i3 = (int)(r % g.d[3]); r /= g.d[3];
-        int i2 = (int)(r % g.d[2]); r /= g.d[2];
-        int i1 = (int)(r % g.d[1]); r /= g.d[1];
-        int i0 = (int)(r % g.d[0]); r /= g.d[0];
-        long long b = r;
-        long long so = b * g.sbst + i0 * g.ss[0] + i1 * g.ss[1] + i2 * g.ss[2] + i3 * g.ss[3];
-        long long dof = b * g.dbst + i0 * g.ds[0] + i1 * g.ds[1] + i2 * g.ds[2] + i3 * g.ds[3];
-        double v = alpha * src[so];
-        dst[dof] = (beta != 0.0) ? v + beta * dst[dof] : v;
+// One block per (batch, i0, i1, chunk of AX_CHUNK (i2, i3) positions); its
+// threads walk (i2, i3), the innermost index fastest, so only a 32-bit
+// division per element remains.
+constexpr int AX_CHUNK = 2048;
+
+__global__ void __launch_bounds__(256)
+axpby4_kernel(long long nblk, Dims4 g, double alpha, const double *__restrict__ src,
+              double beta, double *__restrict__ dst) {
+    const long long n23 = (long long)g.d[2] * g.d[3];
+    const long long nch = (n23 + AX_CHUNK - 1) / AX_CHUNK;
+    for (long long blk = blockIdx.x; blk < nblk; blk += gridDim.x) {
+        const long long row = blk / nch;
+        const long long e0 = (blk - row * nch) * AX_CHUNK;
+        const long long b = row / ((long long)g.d[0] * g.d[1]);
+        const int r = (int)(row - b * g.d[0] * g.d[1]);
+        const int i0 = r / g.d[1], i1 = r % g.d[1];
+        const double *s = src + b * g.sbst + i0 * g.ss[0] + i1 * g.ss[1];
+        double *d = dst + b * g.dbst + i0 * g.ds[0] + i1 * g.ds[1];
+        const int cnt = (int)min((long long)AX_CHUNK, n23 - e0);
+        const long long i2s = e0 / g.d[3];
+        const int i3s = (int)(e0 - i2s * g.d[3]);
+        for (int k = threadIdx.x; k < cnt; k += blockDim.x) {
+            const int t = i3s + k;               // < d3 + AX_CHUNK: 32-bit
+            const long long i2 = i2s + t / g.d[3];
+            const int i3 = t % g.d[3];
+            const double v = alpha * s[i2 * g.ss[2] + i3 * g.ss[3]];
+            double *o = d + i2 * g.ds[2] + i3 * g.ds[3];
+            *o = (beta != 0.0) ? fma(beta, *o, v) : v;
+        }
     }
 }
 
-// out[y,a,b,i,j] = t2 + c (t1[a,i] t1[b,j] - t1[b,i] t1[a,j])
-__global__ void make_tau_kernel(long long total, int nv, int no,
-                                const double *__restrict__ t1,
-                                const double *__restrict__ t2, double c,
-                                double *__restrict__ out) {
-    const long long s4 = (long long)nv * nv * no * no;
-    for (long long x = blockIdx.x * (long long)blockDim.x + threadIdx.x; x < total;
-         x += (long long)gridDim.x * blockDim.x) {
-        long long y = x / s4;
-        long long r = x - y * s4;
-        int j = (int)(r % no); r /= no;
-        int i = (int)(r % no); r /= no;
-        int b = (int)(r % nv);
-        int a = (int)(r / nv);
+// out[y,a,b,i,j] = t2 + c (t1[a,i] t1[b,j] - t1[b,i] t1[a,j]); one block per
+// (y, a, b), threads over (i, j)
+__global__ void __launch_bounds__(256)
+make_tau_kernel(long long nblk, int nv, int no, const double *__restrict__ t1,
+                const double *__restrict__ t2, double c, double *__restrict__ out) {
+    const int oo = no * no;
+    for (long long blk = blockIdx.x; blk < nblk; blk += gridDim.x) {
+        const long long y = blk / ((long long)nv * nv);
+        const int ab = (int)(blk - y * nv * nv);
+        const int a = ab / nv, b = ab % nv;
         const double *u = t1 + y * nv * no;
-        out[x] = t2[x] + c * (u[a * no + i] * u[b * no + j] - u[b * no + i] * u[a * no + j]);
+        const double *ua = u + a * no, *ub = u + b * no;
+        const long long base = blk * oo;
+        for (int e = threadIdx.x; e < oo; e += blockDim.x) {
+            const int i = e / no, j = e % no;
+            out[base + e] = t2[base + e] + c * (ua[i] * ub[j] - ub[i] * ua[j]);
+        }
     }
 }
 
@@ -108,6 +123,8 @@ wmbej_tmp_kernel(int nv, int no, const double *__restrict__ t1, const double *__
 // Q = Z[a,b] - Z[b,a] of both tiles goes through shared memory, so every Z
 // element is read once, coalesced, and R = Q - Q^T + (L - L^T) is added to
 // T2[a,b] and subtracted from T2[b,a].  The a = b blocks of T2 get nothing.
+// Every other element of T2 receives exactly one addition, issued as a
+// fire-and-forget reduction at L2 (one rounding, like load-add-store).
 __global__ void __launch_bounds__(256)
 assemble_t2_kernel(int nv, int no, double fac, const double *__restrict__ Z,
                    const double *__restrict__ Lc, double *__restrict__ T2) {
@@ -151,15 +168,15 @@ assemble_t2_kernel(int nv, int no, double fac, const double *__restrict__ Z,
             int i = i0 + r, j = j0 + tx;
             if (i < no && j < no) {
                 const double R = fac * (qa[r][tx] - qb[tx][r] + ladder(i, j));
-                T2[oab + i * no + j] += R;
-                T2[oba + i * no + j] -= R;
+                atomicAdd(T2 + oab + i * no + j, R);
+                atomicAdd(T2 + oba + i * no + j, -R);
             }
             i = j0 + r;
             j = i0 + tx;
             if (it != jt && i < no && j < no) {
                 const double R = fac * (qb[r][tx] - qa[tx][r] + ladder(i, j));
-                T2[oab + i * no + j] += R;
-                T2[oba + i * no + j] -= R;
+                atomicAdd(T2 + oab + i * no + j, R);
+                atomicAdd(T2 + oba + i * no + j, -R);
             }
         }
     }
@@ -173,23 +190,25 @@ __global__ void bcast_kernel(long long total, long long count,
         dst[x] = src[x % count];
 }
 
-// tau_c[y][(e<f)][(i<j)] = t2[y,e,f,i,j] + t1[y,e,i] t1[y,f,j] - t1[y,f,i] t1[y,e,j]
-__global__ void make_tau_pairs_kernel(long long total, int nv, int no, int pv, int po,
-                                      const double *__restrict__ t1,
-                                      const double *__restrict__ t2,
-                                      double *__restrict__ out) {
-    const long long per = (long long)pv * po;
+// tau_c[y][(e<f)][(i<j)] = t2[y,e,f,i,j] + t1[y,e,i] t1[y,f,j] - t1[y,f,i] t1[y,e,j];
+// one block per (y, e<f), threads over the (i<j) pairs
+__global__ void __launch_bounds__(256)
+make_tau_pairs_kernel(long long nblk, int nv, int no, int pv, int po,
+                      const double *__restrict__ t1, const double *__restrict__ t2,
+                      double *__restrict__ out) {
     const long long s4 = (long long)nv * nv * no * no;
-    for (long long x = blockIdx.x * (long long)blockDim.x + threadIdx.x; x < total;
-         x += (long long)gridDim.x * blockDim.x) {
-        const long long y = x / per;
-        const long long r = x - y * per;
-        int e, f, i, j;
-        pair_of((int)(r / po), nv, e, f);
-        pair_of((int)(r % po), no, i, j);
+    for (long long blk = blockIdx.x; blk < nblk; blk += gridDim.x) {
+        const long long y = blk / pv;
+        int e, f;
+        pair_of((int)(blk - y * pv), nv, e, f);
         const double *u = t1 + y * nv * no;
-        const long long off = y * s4 + (((long long)e * nv + f) * no + i) * no + j;
-        out[x] = t2[off] + u[e * no + i] * u[f * no + j] - u[f * no + i] * u[e * no + j];
+        const double *src = t2 + y * s4 + ((long long)e * nv + f) * no * no;
+        double *dst = out + blk * po;
+        for (int x = threadIdx.x; x < po; x += blockDim.x) {
+            int i, j;
+            pair_of(x, no, i, j);
+            dst[x] = src[i * no + j] + u[e * no + i] * u[f * no + j] - u[f * no + i] * u[e * no + j];
+        }
     }
 }
 
@@ -203,24 +222,29 @@ struct PairGather {
     double c1, c2;
 };
 
-__global__ void pair_gather_kernel(long long total, PairGather g, double *__restrict__ out) {
-    const long long per = (long long)g.P1 * g.P2;
-    for (long long x = blockIdx.x * (long long)blockDim.x + threadIdx.x; x < total;
-         x += (long long)gridDim.x * blockDim.x) {
-        const long long y = x / per;
-        const long long r = x - y * per;
-        int p, q, a, b;
-        pair_of((int)(r / g.P2), g.n1, p, q);
-        pair_of((int)(r % g.P2), g.n2, a, b);
-        double v = 0.0;
-        if (g.A) v = g.ca * g.A[p * g.sa[0] + q * g.sa[1] + a * g.sa[2] + b * g.sa[3]];
-        if (g.B) {
-            const double *Bb = g.B + y * g.bst;
-            v += g.c1 * Bb[p * g.sb1[0] + q * g.sb1[1] + a * g.sb1[2] + b * g.sb1[3]];
-            if (g.c2 != 0.0)
-                v += g.c2 * Bb[p * g.sb2[0] + q * g.sb2[1] + a * g.sb2[2] + b * g.sb2[3]];
+// one block per (batch, p<q), threads over the (a<b) pairs
+__global__ void __launch_bounds__(256)
+pair_gather_kernel(long long nblk, PairGather g, double *__restrict__ out) {
+    for (long long blk = blockIdx.x; blk < nblk; blk += gridDim.x) {
+        const long long y = blk / g.P1;
+        int p, q;
+        pair_of((int)(blk - y * g.P1), g.n1, p, q);
+        const double *Ar = g.A ? g.A + p * g.sa[0] + q * g.sa[1] : nullptr;
+        const double *Bb = g.B ? g.B + y * g.bst : nullptr;
+        const double *B1 = Bb ? Bb + p * g.sb1[0] + q * g.sb1[1] : nullptr;
+        const double *B2 = Bb ? Bb + p * g.sb2[0] + q * g.sb2[1] : nullptr;
+        double *o = out + blk * g.P2;
+        for (int x = threadIdx.x; x < g.P2; x += blockDim.x) {
+            int a, b;
+            pair_of(x, g.n2, a, b);
+            double v = 0.0;
+            if (Ar) v = g.ca * Ar[a * g.sa[2] + b * g.sa[3]];
+            if (Bb) {
+                v += g.c1 * B1[a * g.sb1[2] + b * g.sb1[3]];
+                if (g.c2 != 0.0) v += g.c2 * B2[a * g.sb2[2] + b * g.sb2[3]];
+            }
+            o[x] = v;
         }
-        out[x] = v;
     }
 }
 
@@ -241,8 +265,10 @@ int kv_axpby4(kvft_ctx *ctx, int batch, const int dims[4], double alpha,
     g.dbst = dbst;
     if (total == 0) return KVFT_OK;
     KvProfScope prof(ctx, KV_CAT_ELEM, 8.0 * total * (beta != 0.0 ? 3 : 2));
-    axpby4_kernel<<<grid_for(ctx, total, 256), 256, 0, ctx->stream>>>(total, g, alpha, src,
-                                                                      beta, dst);
+    const long long nblk = (long long)batch * dims[0] * dims[1] *
+                           (((long long)dims[2] * dims[3] + AX_CHUNK - 1) / AX_CHUNK);
+    axpby4_kernel<<<(unsigned)std::min(nblk, (long long)ctx->sm_count * 16), 256, 0,
+                    ctx->stream>>>(nblk, g, alpha, src, beta, dst);
     return kv_launch_check(ctx, "axpby4");
 }
 
@@ -251,8 +277,9 @@ int kv_make_tau(kvft_ctx *ctx, int batch, int nv, int no, const double *t1,
     long long total = (long long)batch * nv * nv * no * no;
     if (total == 0) return KVFT_OK;
     KvProfScope prof(ctx, KV_CAT_ELEM, 16.0 * total);
-    make_tau_kernel<<<grid_for(ctx, total, 256), 256, 0, ctx->stream>>>(total, nv, no, t1,
-                                                                        t2, c, out);
+    const long long nblk = (long long)batch * nv * nv;
+    make_tau_kernel<<<(unsigned)std::min(nblk, (long long)ctx->sm_count * 16), 256, 0,
+                      ctx->stream>>>(nblk, nv, no, t1, t2, c, out);
     return kv_launch_check(ctx, "make_tau");
 }
 
@@ -286,8 +313,9 @@ int kv_make_tau_pairs(kvft_ctx *ctx, int batch, int nv, int no, const double *t1
     long long total = (long long)batch * pv * po;
     if (total == 0) return KVFT_OK;
     KvProfScope prof(ctx, KV_CAT_ELEM, 16.0 * total);
-    make_tau_pairs_kernel<<<grid_for(ctx, total, 256), 256, 0, ctx->stream>>>(total, nv, no, pv,
-                                                                              po, t1, t2, out);
+    const long long nblk = (long long)batch * pv;
+    make_tau_pairs_kernel<<<(unsigned)std::min(nblk, (long long)ctx->sm_count * 16), 256, 0,
+                            ctx->stream>>>(nblk, nv, no, pv, po, t1, t2, out);
     return kv_launch_check(ctx, "make_tau_pairs");
 }
 
@@ -313,7 +341,9 @@ int kv_pair_gather(kvft_ctx *ctx, int batch, int n1, int n2, const double *A,
     long long total = (long long)batch * g.P1 * g.P2;
     if (total == 0) return KVFT_OK;
     KvProfScope prof(ctx, KV_CAT_ELEM, 8.0 * total * (B ? 3 : 2));
-    pair_gather_kernel<<<grid_for(ctx, total, 256), 256, 0, ctx->stream>>>(total, g, out);
+    const long long nblk = (long long)batch * g.P1;
+    pair_gather_kernel<<<(unsigned)std::min(nblk, (long long)ctx->sm_count * 16), 256, 0,
+                         ctx->stream>>>(nblk, g, out);
     return kv_launch_check(ctx, "pair_gather");
 }
 

@@ -53,8 +53,10 @@ __device__ __forceinline__ double denom(const QuadParams &q, long long p,
     return ev[a] + ev[b] - eo[i] - eo[j];
 }
 
-// Shared memory: ti[ng], G[ng*ng], then per-thread columns r[ng][QT] and
-// tb[ng][QT] (general path).
+// Shared memory: ti[ng], G[ng*ng], the chained-row coefficients cs[ng]
+// (G[y,y-s] - G[y-s,y-s]), g1[ng] (G[y,y-1]) and gd[ng] (G[y,y]), then the
+// per-thread columns r[ng][QT] (non-uniform grids) and tb[ng][QT] (general
+// path).
 // MODE 0: out = T.  MODE 1 (fused solver update): Told = alpha Told + (1-alpha) T,
 // with block partial sums of |T - Told|^2 and |Told_new|^2.
 template <int MODE>
@@ -67,11 +69,19 @@ quad_kernel(QuadParams q, const double *__restrict__ tbar, const double *__restr
     const int ng = q.ng;
     double *ti = sm;
     double *G = ti + ng;
-    double *rk = G + ng * ng;                 // [ng][QT]
-    double *tb = rk + ng * QT;                // [ng][QT]
+    double *cs = G + ng * ng, *g1 = cs + ng, *gd = g1 + ng;
+    double *rk = gd + ng;                                  // [ng][QT]
+    double *tb = rk + (q.uniform ? 0 : ng * QT);           // [ng][QT]
     for (int k = threadIdx.x; k < ng; k += QT) ti[k] = ti_g[k];
     for (int k = threadIdx.x; k < ng * ng; k += QT) G[k] = G_g[k];
+    for (int y = threadIdx.x; y < ng; y += QT) {
+        const int sy = q.step > 0 ? q.step : 1;
+        cs[y] = (y >= sy) ? G_g[y * ng + y - sy] - G_g[(y - sy) * ng + y - sy] : 0.0;
+        g1[y] = (y >= 1) ? G_g[y * ng + y - 1] : 0.0;
+        gd[y] = G_g[y * ng + y];
+    }
     __syncthreads();
+    const double oma = 1.0 - q.alpha;
 
     double s_diff = 0.0, s_norm = 0.0;
     const int t = threadIdx.x;
@@ -96,32 +106,29 @@ quad_kernel(QuadParams q, const double *__restrict__ tbar, const double *__restr
                     // direct: x in [0, y]
                     Ty = G[y * ng + y] * tby;
                     double w = 1.0;
-                    double tbx = tbm1;
                     for (int x = y - 1; x >= 0; x--) {
                         w *= RK(x);
-                        double v = (x == y - 1) ? tbm1 : tbm2;
-                        (void)tbx;
+                        const double v = (x == y - 1) ? tbm1 : tbm2;
                         Ty = fma(G[y * ng + x] * w, v, Ty);
                     }
                 } else if (q.step == 1) {
-                    const double w1 = RK(y - 1);
-                    Ty = w1 * (Tm1 - G[(y - 1) * ng + (y - 1)] * tbm1) +
-                         G[y * ng + (y - 1)] * w1 * tbm1 + G[y * ng + y] * tby;
+                    // T_y = w (T_{y-1} - G[y-1,y-1] tb_{y-1}) + G[y,y-1] w tb_{y-1}
+                    //       + G[y,y] tb_y
+                    Ty = fma(gd[y], tby, RK(y - 1) * fma(cs[y], tbm1, Tm1));
                 } else {  // step 2
                     const double w1 = RK(y - 1);
                     const double w2 = w1 * RK(y - 2);
-                    Ty = w2 * (Tm2 - G[(y - 2) * ng + (y - 2)] * tbm2) +
-                         G[y * ng + (y - 2)] * w2 * tbm2 + G[y * ng + (y - 1)] * w1 * tbm1 +
-                         G[y * ng + y] * tby;
+                    Ty = fma(gd[y], tby, fma(g1[y] * w1, tbm1, w2 * fma(cs[y], tbm2, Tm2)));
                 }
                 if (MODE == 0) {
                     out[(long long)y * q.P + p] = Ty;
                 } else {
+                    // damped update Told + (1 - alpha)(T - Told) and the norms
                     double *o = out + (long long)y * q.P + p;
                     const double told = *o;
                     const double df = Ty - told;
                     s_diff = fma(df, df, s_diff);
-                    const double nt = q.alpha * told + (1.0 - q.alpha) * Ty;
+                    const double nt = fma(oma, df, told);
                     s_norm = fma(nt, nt, s_norm);
                     *o = nt;
                 }
@@ -153,7 +160,7 @@ quad_kernel(QuadParams q, const double *__restrict__ tbar, const double *__restr
                     const double told = *o;
                     const double df = Ty - told;
                     s_diff = fma(df, df, s_diff);
-                    const double nt = q.alpha * told + (1.0 - q.alpha) * Ty;
+                    const double nt = fma(oma, df, told);
                     s_norm = fma(nt, nt, s_norm);
                     *o = nt;
                 }
@@ -249,7 +256,10 @@ void analyse_grid(int ng, const double *ti, const double *G, int full, int *step
     }
 }
 
-size_t quad_smem(int ng) { return sizeof(double) * (ng + ng * ng + 2 * ng * QT); }
+size_t quad_smem(int ng, int uniform, int step) {
+    return sizeof(double) *
+           (4 * ng + ng * ng + (uniform ? 0 : ng * QT) + (step > 0 ? 0 : ng * QT));
+}
 
 }  // namespace
 
@@ -272,18 +282,18 @@ int kv_quad_launch(kvft_ctx *ctx, int mode, int ng, long long P, int rank, int n
     q.full = full;
     q.alpha = alpha;
     analyse_grid(ng, hti, hG, full, &q.step, &q.uniform);
-    size_t smem = quad_smem(ng);
+    size_t smem = quad_smem(ng, q.uniform, q.step);
     long long blocks = (P + QT - 1) / QT;
-    long long cap = (long long)ctx->sm_count * 8;
+    long long cap = (long long)ctx->sm_count * 16;
     int grid = (int)std::min(blocks, cap);
     static bool attr_done[2] = {false, false};
     if (!attr_done[mode]) {
         if (mode == 0)
             cudaFuncSetAttribute(quad_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)quad_smem(MAXNG));
+                                 (int)quad_smem(MAXNG, 0, 0));
         else
             cudaFuncSetAttribute(quad_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)quad_smem(MAXNG));
+                                 (int)quad_smem(MAXNG, 0, 0));
         attr_done[mode] = true;
     }
     // algorithmic bytes: tbar in, T out (mode 0); tbar + T_old in, T_old out (mode 1)
