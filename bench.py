@@ -4,6 +4,10 @@
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl kvft|reference]
                     [--workload ueg114|ueg38] [--precision mixed|fp64_tc|fp64]
     python bench.py --gemm M,N,K,batch [--precision ...]      # one contraction shape
+    python bench.py --profile-step [--workload ...] [--precision ...]
+        # one warm-up iteration, then one iteration; prints the library's
+        # kernel-launch counts so that a profiler's launch list can be cut to
+        # exactly the second iteration
 
 Workloads are seeded synthetic uniform electron gases (the benchmark configs):
 
@@ -375,6 +379,32 @@ def run_gpu(args, w):
     return 0
 
 
+def run_profile_step(args, w):
+    """One warm-up iteration and one profiled iteration of the solver."""
+    from kelvin_gb300 import _lib, ccsd
+    from kelvin_gb300.cc_utils import DeviceSolver
+    from kelvin_gb300.quadrature import ft_quad
+    ctx = _lib.context(0)
+    prec, digits = ccsd.PRECISIONS[args.precision]
+    ctx.set_precision(prec, args.digits or digits)
+    s = build_system(w)
+    beta = 1.0 / s.T
+    ti, g, G = ft_quad(w["ng"], beta, "lin")
+    solver = DeviceSolver.from_system(ctx, s.g_energies_tot(), s.g_fock_tot(), s.g_aint_tot(),
+                                      beta, s.mu, ti, g, G)
+    solver.guess(1)
+    solver.step(w["damp"])
+    ctx.sync()
+    l0 = ctx.launches()
+    E, res = solver.step(w["damp"])
+    ctx.sync()
+    print(json.dumps({"profile_step": args.workload, "precision": args.precision,
+                      "launches_before": l0, "launches_in_step": ctx.launches() - l0,
+                      "omega_cc": E, "res": res}))
+    solver.close()
+    return 0
+
+
 def run_gemm(args):
     """Time one contraction shape through kvft_gemm (device-resident operands)."""
     import numpy
@@ -415,6 +445,8 @@ def run_gemm(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gemm", default="", help="M,N,K,batch: time one contraction shape")
+    ap.add_argument("--profile-step", action="store_true",
+                    help="one warm-up and one profiled solver iteration")
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
@@ -426,6 +458,8 @@ def main():
     w = WORKLOADS[args.workload]
     if args.gemm:
         return run_gemm(args)
+    if args.profile_step:
+        return run_profile_step(args, w)
     if args.impl == "reference":
         return run_reference(args, w)
     return run_gpu(args, w)
