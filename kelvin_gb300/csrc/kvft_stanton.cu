@@ -87,7 +87,7 @@ size_t kv_chunk_bytes_per_tau(kvft_ctx *ctx, int nv, int no) {
         const size_t big = std::max(std::max((size_t)nv * nv * nv * nv, (size_t)no * no * no * no),
                                     (size_t)nv * nv * no * no);
         const size_t S = (size_t)std::min(ctx->digits - 1, 6);
-        per += 2 * S * 2 * big;
+        per += 2 * S * 2 * big / 8 * 9;       // plane rows are padded to 64 k values
     }
     return per;
 }

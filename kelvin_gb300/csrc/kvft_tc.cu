@@ -835,14 +835,15 @@ struct Packed {
     int R, ld, K, nb;
 };
 
-// Digit planes [nb][S][R][ld] (ld = K rounded up to 8 for the 16-byte TMA row
-// stride) and exponents [nb][R].  No row or K padding is written: the tensor
-// map's extent is (K, nb S R) and TMA fills out-of-range boxes with zeros;
-// rows past R inside a 128-row box belong to the next plane and only reach
-// output rows/columns that the epilogue discards.
+// Digit planes [nb][S][R][ld] and exponents [nb][R].  ld = K rounded up to 64
+// elements, so that every row starts on a 128-byte line and a TMA box row
+// (one k-block of one row) touches one line, not two.  No row or K padding is
+// written: the tensor map's extent is (K, nb S R) and TMA fills out-of-range
+// boxes with zeros; rows past R inside a 128-row box belong to the next plane
+// and only reach output rows/columns that the epilogue discards.
 int pack(kvft_ctx *ctx, const char *key, const PackView &v, int R, int K, int nb, int S,
          Packed *out) {
-    const int ld = (K + 7) / 8 * 8;
+    const int ld = (K + 63) / 64 * 64;
     const size_t plane_bytes = (size_t)R * ld * 2;
     const size_t pbytes = ((size_t)nb * S * plane_bytes + 1023) / 1024 * 1024;
     const size_t bytes = pbytes + (size_t)nb * R * sizeof(int);
