@@ -16,6 +16,11 @@ int kv_cuda(kvft_ctx *ctx, cudaError_t e, const char *what) {
     return kv_fail(ctx, code, m);
 }
 
+void kv_pack_cache_clear(kvft_ctx *ctx) {
+    for (auto &kv : ctx->pack_cache) cudaFree(kv.second.first);
+    ctx->pack_cache.clear();
+}
+
 int kv_launch_check(kvft_ctx *ctx, const char *what) {
     ctx->launches++;
     cudaError_t e = cudaGetLastError();
@@ -93,6 +98,7 @@ int kvft_ctx_destroy(kvft_ctx *c) {
     cudaSetDevice(c->device);
     cudaStreamSynchronize(c->stream);
     for (auto &kv : c->scratch) cudaFree(kv.second.first);
+    kv_pack_cache_clear(c);
     if (c->prof) {
         for (auto e : c->prof->pool) cudaEventDestroy(e);
         delete c->prof;

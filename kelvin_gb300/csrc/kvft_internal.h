@@ -33,6 +33,7 @@ struct KMat {
     const double *p;
     KIdx r, c;
     long long bst;      // stride between batch entries (0: shared operand)
+    int stable = 0;     // contents fixed for the solver's lifetime (integral blocks)
 };
 
 struct KOut {
@@ -74,6 +75,21 @@ struct kvft_ctx {
     std::map<std::string, std::pair<void *, size_t>> scratch;
     int *dflag = nullptr;            // device status word for bounded waits
     struct KvProf *prof = nullptr;
+    // Digit planes of stable operands (the integral blocks), kept across the
+    // residual evaluations of one solver: on only inside solver-driven
+    // evaluations, emptied when a solver is destroyed.
+    bool pack_cache_on = false;
+    std::map<std::string, std::pair<void *, size_t>> pack_cache;
+};
+void kv_pack_cache_clear(kvft_ctx *ctx);
+// Turns the pack cache on for the lifetime of the guard.
+struct KvPackCacheScope {
+    kvft_ctx *ctx;
+    bool prev;
+    explicit KvPackCacheScope(kvft_ctx *c) : ctx(c), prev(c->pack_cache_on) {
+        c->pack_cache_on = true;
+    }
+    ~KvPackCacheScope() { ctx->pack_cache_on = prev; }
 };
 
 // Live per-launch timing (enabled by kvft_profile_begin): event pairs around

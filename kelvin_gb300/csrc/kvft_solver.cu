@@ -259,6 +259,7 @@ int form_tbar(kvft_solver *s) {
     const double *Fc[4] = {s->F[0], s->F[1], s->F[2], s->F[3]};
     const double *Ic[9];
     for (int k = 0; k < 9; k++) Ic[k] = s->I[k];
+    KvPackCacheScope cache(ctx);          // the integral blocks are the solver's own
     for (int y0 = 0; y0 < s->ng; y0 += s->chunk) {
         int nb = std::min(s->chunk, s->ng - y0);
         KV_TRY(kv_stanton(ctx, nb, s->nv, s->no, Fc, Ic, s->T1 + y0 * n1, s->T2 + y0 * n2, -1.0,
@@ -427,6 +428,9 @@ int kvft_solver_destroy(kvft_solver *s) {
     if (!s) return KVFT_OK;
     cudaSetDevice(s->ctx->device);
     cudaStreamSynchronize(s->ctx->stream);
+    // cached digit planes of this solver's integrals (their addresses may be
+    // reused by later allocations)
+    kv_pack_cache_clear(s->ctx);
     destroy(s);
     return KVFT_OK;
 }
@@ -543,7 +547,10 @@ int kvft_solver_run_point(kvft_solver *s, const kvft_solve_opts *o, kvft_result 
         while (i < o->max_iter && !conv) {
             KV_TRY(seed_neg(ctx, 1, n1, s->F[2], t1b));
             KV_TRY(seed_neg(ctx, 1, n2, s->I[3], t2b));
-            KV_TRY(kv_stanton(ctx, 1, s->nv, s->no, Fc, Ic, T1g, T2g, -1.0, t1b, t2b));
+            {
+                KvPackCacheScope cache(ctx);
+                KV_TRY(kv_stanton(ctx, 1, s->nv, s->no, Fc, Ic, T1g, T2g, -1.0, t1b, t2b));
+            }
             KV_TRY(kv_quad_single(ctx, ng, ig, n1, 1, s->nv, s->no, s->T1b, s->ti, s->G, s->D1,
                                   s->eps, s->eps, u1));
             KV_TRY(kv_quad_single(ctx, ng, ig, n2, 2, s->nv, s->no, s->T2b, s->ti, s->G, s->D2,

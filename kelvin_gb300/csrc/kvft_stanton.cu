@@ -32,6 +32,8 @@ inline KIdx X3(int s0, long long t0, int s1, long long t1, int s2, long long t2)
     return kidx3(s0, t0, s1, t1, s2, t2);
 }
 inline KMat MA(const double *p, KIdx r, KIdx c, long long bst) { return KMat{p, r, c, bst}; }
+// an integral block: shared by the batch and fixed for the solver's lifetime
+inline KMat MAI(const double *p, KIdx r, KIdx c) { return KMat{p, r, c, 0, 1}; }
 inline KOut MO(double *p, KIdx r, KIdx c, long long bst) { return KOut{p, r, c, bst}; }
 
 // workspace layout (per tau point, doubles)
@@ -122,13 +124,13 @@ int kv_stanton(kvft_ctx *ctx, int nb, int nv, int no, const double *const F[4],
                    MO(w.Fae, X1(nv, v), X1(nv, 1), vv)));
     // - vovv[a,m,f,e] t1[f,m]    (M=(a,e), K=(m,f), N=tau)
     KV_TRY(kv_gemm(ctx, nv * nv, B, no * nv, 1, -1.0,
-                   MA(vovv, X2(nv, o * vv, nv, 1), X2(no, vv, nv, v), 0),
+                   MAI(vovv, X2(nv, o * vv, nv, 1), X2(no, vv, nv, v)),
                    MA(t1, X2(no, 1, nv, o), X1(B, vo), 0), 1.0,
                    MO(w.Fae, X2(nv, v, nv, 1), X1(B, vv), 0)));
     // -1/2 ttau[a,f,m,n] oovv[m,n,e,f]
     KV_TRY(kv_gemm(ctx, nv, nv, nv * no * no, B, -0.5,
                    MA(w.ttau, X1(nv, vo2), X3(nv, oo, no, o, no, 1), v2o2),
-                   MA(oovv, X3(nv, 1, no, o * vv, no, vv), X1(nv, v), 0), 1.0,
+                   MAI(oovv, X3(nv, 1, no, o * vv, no, vv), X1(nv, v)), 1.0,
                    MO(w.Fae, X1(nv, v), X1(nv, 1), vv)));
 
     // ---- F_mi ------------------------------------------------------------
@@ -139,12 +141,12 @@ int kv_stanton(kvft_ctx *ctx, int nb, int nv, int no, const double *const F[4],
                    MO(w.Fmi, X1(no, o), X1(no, 1), oo)));
     // + ooov[m,n,i,e] t1[e,n]    (M=(m,i), K=(n,e), N=tau)
     KV_TRY(kv_gemm(ctx, no * no, B, no * nv, 1, 1.0,
-                   MA(ooov, X2(no, oo * v, no, v), X2(no, vo, nv, 1), 0),
+                   MAI(ooov, X2(no, oo * v, no, v), X2(no, vo, nv, 1)),
                    MA(t1, X2(no, 1, nv, o), X1(B, vo), 0), 1.0,
                    MO(w.Fmi, X2(no, o, no, 1), X1(B, oo), 0)));
     // +1/2 oovv[m,n,e,f] ttau[e,f,i,n]
     KV_TRY(kv_gemm(ctx, no, no, no * nv * nv, B, 0.5,
-                   MA(oovv, X1(no, o * vv), X3(no, vv, nv, v, nv, 1), 0),
+                   MAI(oovv, X1(no, o * vv), X3(no, vv, nv, v, nv, 1)),
                    MA(w.ttau, X3(no, 1, nv, vo2, nv, oo), X1(no, o), v2o2), 1.0,
                    MO(w.Fmi, X1(no, o), X1(no, 1), oo)));
 
@@ -152,7 +154,7 @@ int kv_stanton(kvft_ctx *ctx, int nb, int nv, int no, const double *const F[4],
     KV_TRY(kv_bcast(ctx, B, vo, Fov, w.Fme));
     // + oovv[m,n,e,f] t1[f,n]    (M=(m,e), K=(n,f), N=tau)
     KV_TRY(kv_gemm(ctx, no * nv, B, no * nv, 1, 1.0,
-                   MA(oovv, X2(no, o * vv, nv, v), X2(no, vv, nv, 1), 0),
+                   MAI(oovv, X2(no, o * vv, nv, v), X2(no, vv, nv, 1)),
                    MA(t1, X2(no, 1, nv, o), X1(B, vo), 0), 1.0,
                    MO(w.Fme, X2(no, v, nv, 1), X1(B, vo), 0)));
 
@@ -169,17 +171,17 @@ int kv_stanton(kvft_ctx *ctx, int nb, int nv, int no, const double *const F[4],
                    MO(T1, X2(nv, o, no, 1), one, vo)));
     // - vovo[a,n,f,i] t1[f,n]   (M=(a,i), K=(n,f), N=tau)
     KV_TRY(kv_gemm(ctx, nv * no, B, no * nv, 1, -fac,
-                   MA(vovo, X2(nv, vo2, no, 1), X2(no, vo, nv, o), 0),
+                   MAI(vovo, X2(nv, vo2, no, 1), X2(no, vo, nv, o)),
                    MA(t1, X2(no, 1, nv, o), X1(B, vo), 0), 1.0,
                    MO(T1, X2(nv, o, no, 1), X1(B, vo), 0)));
     // +1/2 vovv[a,m,e,f] t2[e,f,i,m]
     KV_TRY(kv_gemm(ctx, nv, no, no * nv * nv, B, 0.5 * fac,
-                   MA(vovv, X1(nv, o * vv), X3(no, vv, nv, v, nv, 1), 0),
+                   MAI(vovv, X1(nv, o * vv), X3(no, vv, nv, v, nv, 1)),
                    MA(t2, X3(no, 1, nv, vo2, nv, oo), X1(no, o), v2o2), 1.0, T1o));
     // +1/2 t2[a,e,m,n] ooov[n,m,i,e]
     KV_TRY(kv_gemm(ctx, nv, no, nv * no * no, B, 0.5 * fac,
                    MA(t2, X1(nv, vo2), X3(nv, oo, no, o, no, 1), v2o2),
-                   MA(ooov, X3(nv, 1, no, vo, no, oo * v), X1(no, v), 0), 1.0, T1o));
+                   MAI(ooov, X3(nv, 1, no, vo, no, oo * v), X1(no, v)), 1.0, T1o));
 
     // ---- ladder terms over antisymmetric pairs ---------------------------------
     // tau, W'_mnij, W'_abef and <mn||ef> are antisymmetric in each index pair,
@@ -201,7 +203,7 @@ int kv_stanton(kvft_ctx *ctx, int nb, int nv, int no, const double *const F[4],
                               0.0, 0, (double *)oc));
         // Z[m,n,i,j] = ooov[m,n,i,e] t1[e,j]
         KV_TRY(kv_gemm(ctx, no * no * no, no, nv, B, 1.0,
-                       MA(ooov, X3(no, oo * v, no, vo, no, v), X1(nv, 1), 0),
+                       MAI(ooov, X3(no, oo * v, no, vo, no, v), X1(nv, 1)),
                        MA(t1, X1(nv, o), X1(no, 1), vo), 0.0,
                        MO(w.tmp4, X3(no, o * oo, no, oo, no, o), X1(no, 1), o4)));
         // W'_c = oooo + Z - Z^(ij)
@@ -220,7 +222,7 @@ int kv_stanton(kvft_ctx *ctx, int nb, int nv, int no, const double *const F[4],
         // Y[a,b,e,f] = t1[b,m] vovv[a,m,e,f]   (M=b, K=m, N=(a,e,f))
         KV_TRY(kv_gemm(ctx, nv, nv * nv * nv, no, B, 1.0,
                        MA(t1, X1(nv, o), X1(no, 1), vo),
-                       MA(vovv, X1(no, vv), X3(nv, o * vv, nv, v, nv, 1), 0), 0.0,
+                       MAI(vovv, X1(no, vv), X3(nv, o * vv, nv, v, nv, 1)), 0.0,
                        MO(w.tmp4, X1(nv, vv), X3(nv, v * vv, nv, v, nv, 1), v4)));
         // W'_abef_c = vvvv - Y + Y^(ab)
         const long long s4v[4] = {v * vv, vv, v, 1}, s4s[4] = {vv, v * vv, v, 1};
@@ -242,13 +244,13 @@ int kv_stanton(kvft_ctx *ctx, int nb, int nv, int no, const double *const F[4],
     }
     // - vovv[b,m,e,f] t1[f,j]    (M=(m,b,e), K=f, N=j)
     KV_TRY(kv_gemm(ctx, no * nv * nv, no, nv, B, -1.0,
-                   MA(vovv, X3(no, vv, nv, o * vv, nv, v), X1(nv, 1), 0),
+                   MAI(vovv, X3(no, vv, nv, o * vv, nv, v), X1(nv, 1)),
                    MA(t1, X1(nv, o), X1(no, 1), vo), 1.0,
                    MO(w.Wmbej, X3(no, wm, nv, wb, nv, we), X1(no, 1), v2o2)));
     // + t1[b,n] ooov[m,n,j,e]    (M=b, K=n, N=(m,e,j))
     KV_TRY(kv_gemm(ctx, nv, no * nv * no, no, B, 1.0,
                    MA(t1, X1(nv, o), X1(no, 1), vo),
-                   MA(ooov, X1(no, vo), X3(no, oo * v, nv, 1, no, v), 0), 1.0,
+                   MAI(ooov, X1(no, vo), X3(no, oo * v, nv, 1, no, v)), 1.0,
                    MO(w.Wmbej, X1(nv, wb), X3(no, wm, nv, we, no, 1), v2o2)));
     // - oovv[m,n,e,f] (t2[f,b,j,n]/2 + t1[f,j] t1[b,n])  (M=(m,e), K=(n,f), N=(tau,b,j))
     KV_TRY(kv_make_wmbej_tmp(ctx, B, nv, no, t1, t2, w.tmp4));
@@ -257,7 +259,7 @@ int kv_stanton(kvft_ctx *ctx, int nb, int nv, int no, const double *const F[4],
         // for the largest block, so index it with the v2o2 layout directly);
         // the contraction index (n, f) is contiguous in both operands
         KV_TRY(kv_gemm(ctx, no * nv, B * nv * no, no * nv, 1, -1.0,
-                       MA(oovv, X2(no, o * vv, nv, v), X2(no, vv, nv, 1), 0),
+                       MAI(oovv, X2(no, o * vv, nv, v), X2(no, vv, nv, 1)),
                        MA(w.tmp4, X2(no, v, nv, 1), X3(B, v2o2, nv, vo2, no, vo), 0),
                        1.0, MO(w.Wmbej, X2(no, wm, nv, we), X3(B, v2o2, nv, wb, no, 1), 0)));
     }
@@ -273,7 +275,7 @@ int kv_stanton(kvft_ctx *ctx, int nb, int nv, int no, const double *const F[4],
                    MO(w.Z, X2(nv, vo2, no, o), X2(nv, oo, no, 1), v2o2)));
     // Q[b,m,i,j] = vovo[b,m,e,j] t1[e,i]   (M=(b,m,j), K=e, N=i)
     KV_TRY(kv_gemm(ctx, nv * no * no, no, nv, B, 1.0,
-                   MA(vovo, X3(nv, vo2, no, vo, no, 1), X1(nv, o), 0),
+                   MAI(vovo, X3(nv, vo2, no, vo, no, 1), X1(nv, o)),
                    MA(t1, X1(nv, o), X1(no, 1), vo), 0.0,
                    MO(w.Q, X3(nv, o * oo, no, oo, no, 1), X1(no, o), vo3)));
     // Zabij += t1[a,m] Q[b,m,i,j]   (M=a, K=m, N=(b,i,j))
@@ -295,7 +297,7 @@ int kv_stanton(kvft_ctx *ctx, int nb, int nv, int no, const double *const F[4],
     // Zab += t1[a,m] vooo[b,m,i,j]   (M=a, K=m, N=(b,i,j))
     KV_TRY(kv_gemm(ctx, nv, nv * no * no, no, B, 0.5,
                    MA(t1, X1(nv, o), X1(no, 1), vo),
-                   MA(vooo, X1(no, oo), X3(nv, o * oo, no, o, no, 1), 0), 1.0,
+                   MAI(vooo, X1(no, oo), X3(nv, o * oo, no, o, no, 1)), 1.0,
                    MO(w.Z, X1(nv, vo2), X3(nv, oo, no, o, no, 1), v2o2)));
 
     // ---- Z += Zij/2: -t2 (F_mj + 1/2 t1 F_me) and vvvo t1 -----------------------
@@ -310,7 +312,7 @@ int kv_stanton(kvft_ctx *ctx, int nb, int nv, int no, const double *const F[4],
                    MO(w.Z, X3(nv, vo2, nv, oo, no, o), X1(no, 1), v2o2)));
     // Zij += vvvo[a,b,e,j] t1[e,i]   (M=(a,b,j), K=e, N=i)
     KV_TRY(kv_gemm(ctx, nv * nv * no, no, nv, B, 0.5,
-                   MA(vvvo, X3(nv, vv * o, nv, vo, no, 1), X1(nv, o), 0),
+                   MAI(vvvo, X3(nv, vv * o, nv, vo, no, 1), X1(nv, o)),
                    MA(t1, X1(nv, o), X1(no, 1), vo), 1.0,
                    MO(w.Z, X3(nv, vo2, nv, oo, no, 1), X1(no, o), v2o2)));
 

@@ -38,6 +38,7 @@
 #include <cuda_bf16.h>
 
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <mutex>
 
@@ -643,6 +644,7 @@ struct PackView {
     const double *p;
     KIdx r, c;
     long long bst;
+    int stable;         // contents fixed while the pack cache is on
 };
 
 // Operand tiles of 32 rows x 64 k go through shared memory so that global
@@ -841,21 +843,51 @@ struct Packed {
 // written: the tensor map's extent is (K, nb S R) and TMA fills out-of-range
 // boxes with zeros; rows past R inside a 128-row box belong to the next plane
 // and only reach output rows/columns that the epilogue discards.
+// Identity of a packed operand: address, view, extents and digit count.
+std::string pack_key(const PackView &v, int R, int K, int nb, int S) {
+    char b[320];
+    snprintf(b, sizeof b, "%p|%d,%d,%d:%lld,%lld,%lld|%d,%d,%d:%lld,%lld,%lld|%lld|%d,%d,%d,%d",
+             (const void *)v.p, v.r.size[0], v.r.size[1], v.r.size[2], v.r.st[0], v.r.st[1],
+             v.r.st[2], v.c.size[0], v.c.size[1], v.c.size[2], v.c.st[0], v.c.st[1], v.c.st[2],
+             v.bst, R, K, nb, S);
+    return b;
+}
+
 int pack(kvft_ctx *ctx, const char *key, const PackView &v, int R, int K, int nb, int S,
          Packed *out) {
     const int ld = (K + 63) / 64 * 64;
     const size_t plane_bytes = (size_t)R * ld * 2;
     const size_t pbytes = ((size_t)nb * S * plane_bytes + 1023) / 1024 * 1024;
     const size_t bytes = pbytes + (size_t)nb * R * sizeof(int);
-    void *buf = nullptr;
-    KV_TRY(kv_scratch(ctx, key, bytes, &buf));
-    out->planes = (__nv_bfloat16 *)buf;
-    out->ex = (int *)((uint8_t *)buf + pbytes);
     out->R = R;
     out->ld = ld;
     out->K = K;
     out->nb = nb;
     if (nb > 65535) return kv_fail(ctx, KVFT_EINVAL, "pack: batch too large");
+    void *buf = nullptr;
+    std::string ckey;
+    if (v.stable && ctx->pack_cache_on) {
+        // an integral block packed during an earlier residual evaluation
+        ckey = pack_key(v, R, K, nb, S);
+        auto it = ctx->pack_cache.find(ckey);
+        if (it != ctx->pack_cache.end()) {
+            out->planes = (__nv_bfloat16 *)it->second.first;
+            out->ex = (int *)((uint8_t *)it->second.first + pbytes);
+            return KVFT_OK;
+        }
+        // keep it only while a tenth of the device stays free
+        size_t fr = 0, tot = 0;
+        if (cudaMemGetInfo(&fr, &tot) == cudaSuccess && fr > bytes + tot / 10 &&
+            cudaMalloc(&buf, bytes) == cudaSuccess) {
+            ctx->pack_cache[ckey] = {buf, bytes};
+        } else {
+            cudaGetLastError();
+            buf = nullptr;
+        }
+    }
+    if (!buf) KV_TRY(kv_scratch(ctx, key, bytes, &buf));
+    out->planes = (__nv_bfloat16 *)buf;
+    out->ex = (int *)((uint8_t *)buf + pbytes);
     KvProfScope prof(ctx, KV_CAT_PACK, 8.0 * nb * (double)R * K + (double)nb * S * plane_bytes);
     KV_CHECK(ctx, cudaMemsetAsync(out->ex, 0x80, (size_t)nb * R * sizeof(int), ctx->stream));
     // coalesce global reads along the contiguous index
@@ -929,9 +961,9 @@ int gemm_tc_run(kvft_ctx *ctx, int M, int N, int K, int batch, double alpha, con
     const int kb = ff ? 32 : 64;
     const int nbA = A.bst ? batch : 1, nbB = B.bst ? batch : 1;
     Packed pa, pb;
-    KV_TRY(pack(ctx, "tc_pack_a", PackView{A.p, A.r, A.c, A.bst}, M, K, nbA, S, &pa));
+    KV_TRY(pack(ctx, "tc_pack_a", PackView{A.p, A.r, A.c, A.bst, A.stable}, M, K, nbA, S, &pa));
     // B is K x N; its K-major form has rows = N (B's column index), cols = K
-    KV_TRY(pack(ctx, "tc_pack_b", PackView{B.p, B.c, B.r, B.bst}, N, K, nbB, S, &pb));
+    KV_TRY(pack(ctx, "tc_pack_b", PackView{B.p, B.c, B.r, B.bst, B.stable}, N, K, nbB, S, &pb));
     CUtensorMap ma, mb;
     KV_TRY(make_map(ctx, &ma, pa.planes, pa.K, pa.ld, (long long)nbA * S * pa.R, kb, TM));
     KV_TRY(make_map(ctx, &mb, pb.planes, pb.K, pb.ld, (long long)nbB * S * pb.R, kb, tn));
@@ -1008,8 +1040,8 @@ int kv_gemm_tc(kvft_ctx *ctx, int M, int N, int K, int batch, double alpha, cons
         if (ext >= 64 || K <= 512) swap = cc;
     }
     if (swap) {
-        const KMat At{B.p, B.c, B.r, B.bst};
-        const KMat Bt{A.p, A.c, A.r, A.bst};
+        const KMat At{B.p, B.c, B.r, B.bst, B.stable};
+        const KMat Bt{A.p, A.c, A.r, A.bst, A.stable};
         const KOut Ct{C.p, C.c, C.r, C.bst};
         return gemm_tc_run(ctx, N, M, K, batch, alpha, At, Bt, beta, Ct, D);
     }
