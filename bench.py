@@ -43,10 +43,14 @@ sys.path.insert(0, ROOT)
 METRIC = "FT-CCSD solves/s"
 UNIT = "solves/s"
 
-# iters: amplitude iterations of the converged solve (FP64 path, guess 1).
+# iters: amplitude iterations of the converged solve (guess 1), by precision;
+# for 'mixed' the few-digit iterations before the REFINE refinement sweeps.
+# ueg114 was measured by full solves on a GB300 (kelvin_gb300.ccsd.ccsd(...).run()):
+# mixed 28 + 2 sweeps, Omega_cc -0.9542854151 (35.2 s); 7 levels 30, -0.9542857194.
 WORKLOADS = {
     "ueg114": dict(N=38, rs=1.0, norb=57, theta=0.25, ng=20, damp=0.5, econv=1e-10,
-                   max_iter=100, iters=None, step="iteration",
+                   max_iter=100, iters={"mixed": 28, "fp64_tc": 30, "fp64": 30},
+                   step="iteration",
                    label="UEG 38 e-, rs=1, 57 plane waves (114 spin orbitals), Theta=0.25, "
                          "ng=20, damping 0.5, econv 1e-10"),
     "ueg38": dict(N=14, rs=4.0, norb=19, theta=0.5, ng=10, damp=0.5, econv=1e-10,
@@ -56,6 +60,14 @@ WORKLOADS = {
 }
 ITERS_FALLBACK = 30
 REFINE = 2          # FP64-accurate refinement sweeps that end a mixed solve
+STEP_EVENTS = 8     # first event slot of the per-step timings (at most 50 steps)
+
+
+def iters_of(w, precision):
+    it = w["iters"]
+    if isinstance(it, dict):
+        return it.get(precision, ITERS_FALLBACK)
+    return it or ITERS_FALLBACK
 
 
 def load_peaks():
@@ -200,7 +212,7 @@ def run_reference(args, w):
     if rank != 0:
         return 0
     sysobj = build_system(w)
-    iters = w["iters"] or ITERS_FALLBACK
+    iters = iters_of(w, "fp64")                           # the reference is FP64
     cpu_iteration_seconds(w, sysobj)                      # warm-up sample
     times, sample = [], ""
     for _ in range(args.steps):
@@ -248,7 +260,7 @@ def run_gpu(args, w):
             "damp": w["damp"]}
     n, ng = en.shape[0], w["ng"]
     per_solve = w["step"] == "solve"
-    iters = w["iters"] or ITERS_FALLBACK
+    iters = iters_of(w, args.precision)
 
     ctx.set_precision(prec, digits)
     solver = DeviceSolver.from_system(ctx, en, fock, eri, beta, sysobj.mu, ti, g, G)
@@ -270,12 +282,20 @@ def run_gpu(args, w):
     l0 = ctx.launches()
     ctx.profile_begin()
     ctx.record(0)
-    results = [one_step() for _ in range(args.steps)]
+    results = []
+    for k in range(args.steps):
+        if k < 50:
+            ctx.record(STEP_EVENTS + k)
+        results.append(one_step())
+    if args.steps <= 50:
+        ctx.record(STEP_EVENTS + args.steps)
     ctx.record(1)
     ctx.sync()
     prof = ctx.profile_end()
     launches = ctx.launches() - l0
     ms = max_over_ranks(ws, ctx.elapsed_ms(0, 1))
+    lat = sorted(ctx.elapsed_ms(STEP_EVENTS + k, STEP_EVENTS + k + 1)
+                 for k in range(min(args.steps, 50))) if args.steps <= 50 else []
     clk = clocks.stop()
     step_ms = ms / args.steps
     value = ws / (step_ms / 1e3) / (1 if per_solve else iters)
@@ -353,14 +373,16 @@ def run_gpu(args, w):
                 "breakdown_ms_per_step": {c: round(prof[c][1] / args.steps, 3) for c in prof}}
 
     t_iter, sample = cpu_iteration_seconds(w, sysobj)
-    cpu_val = 1.0 / (t_iter * iters)
+    cpu_iters = iters_of(w, "fp64")                       # the CPU port is FP64
+    cpu_val = 1.0 / (t_iter * cpu_iters)
     cfg = {"workload": w["label"], "step": w["step"], "precision": args.precision,
            "digits": digits if args.precision != "fp64" else None,
            "iterations_per_solve": iters, "omega_cc_last_step": results[-1][0],
            "l2": "per-step working set > 129 MB L2 (no flush)",
            "parallelism": "replicas" if ws > 1 else "single GPU"}
-    if w["iters"] is None and not per_solve:
-        cfg["iterations_per_solve_note"] = "not yet measured for this workload; %d assumed" % iters
+    if lat:
+        q = lambda f: lat[min(len(lat) - 1, int(f * len(lat)))]
+        cfg["step_latency_ms"] = {"p50": q(0.5), "p99": q(0.99), "n": len(lat)}
     if fp64_step_ms is not None:
         cfg["fp64_tc_step_ms"] = fp64_step_ms
         cfg["fp64_tc_solves_per_s"] = ws / (fp64_step_ms / 1e3) / (1 if per_solve else iters)
@@ -371,7 +393,7 @@ def run_gpu(args, w):
             "dtype": "f64" if args.precision != "mixed" else "bf16x3-digits/f32acc + f64",
             "data": "synthetic", "config": cfg, "roofline": roofline,
             "cpu_baseline": {"value": cpu_val, "unit": UNIT, "cores": os.cpu_count(),
-                             "kind": "port", "sample": sample + "; x %d iterations" % iters},
+                             "kind": "port", "sample": sample + "; x %d iterations" % cpu_iters},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
             "gpu_launches": launches, "clocks": clk}
