@@ -4,6 +4,9 @@
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl kvft|reference]
                     [--workload ueg114|ueg38] [--precision mixed|fp64_tc|fp64]
     python bench.py --gemm M,N,K,batch [--precision ...]      # one contraction shape
+    python bench.py --system-build [--workload ...]
+        # time building the model system's integrals: dense n^4 on the host
+        # against kvft_ueg_eri on the device (closed-form Fock and E1)
     python bench.py --profile-step [--workload ...] [--precision ...]
         # one warm-up iteration, then one iteration; prints the library's
         # kernel-launch counts so that a profiler's launch list can be cut to
@@ -427,6 +430,34 @@ def run_profile_step(args, w):
     return 0
 
 
+def run_system_build(args, w):
+    """Seconds to build the workload's integrals on the host and on the device."""
+    from kelvin_gb300 import _lib, systems
+    ctx = _lib.context(0)
+    t0 = time.perf_counter()
+    s = systems.ueg_recipe(w["N"], w["rs"], w["norb"], w["theta"])
+    eri = s.g_aint_tot()
+    fock, e1 = s.g_fock_tot(), s.get_mp1()
+    t_host = time.perf_counter() - t0
+    n = eri.shape[0]
+    del eri
+    out = []
+    for _ in range(2):                 # the first also loads the module's kernels
+        ctx.sync()
+        t0 = time.perf_counter()
+        d = systems.ueg_recipe(w["N"], w["rs"], w["norb"], w["theta"], device_build=True)
+        deri = d.device_aint_tot(ctx)
+        fock_d, e1_d = d.g_fock_tot(), d.get_mp1()
+        ctx.sync()
+        out.append(time.perf_counter() - t0)
+        deri.free()
+    print(json.dumps({"system_build": args.workload, "n_spin_orbitals": n,
+                      "host_dense_s": t_host, "device_s": out[-1],
+                      "fock_max_diff": float(abs(fock - fock_d).max()),
+                      "e1_diff": float(abs(e1 - e1_d))}))
+    return 0
+
+
 def run_gemm(args):
     """Time one contraction shape through kvft_gemm (device-resident operands)."""
     import numpy
@@ -467,6 +498,8 @@ def run_gemm(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gemm", default="", help="M,N,K,batch: time one contraction shape")
+    ap.add_argument("--system-build", action="store_true",
+                    help="time the integrals' build on the host and on the device")
     ap.add_argument("--profile-step", action="store_true",
                     help="one warm-up and one profiled solver iteration")
     ap.add_argument("--gpus", type=int, default=1)
@@ -482,6 +515,8 @@ def main():
         return run_gemm(args)
     if args.profile_step:
         return run_profile_step(args, w)
+    if args.system_build:
+        return run_system_build(args, w)
     if args.impl == "reference":
         return run_reference(args, w)
     return run_gpu(args, w)

@@ -158,10 +158,27 @@ int kvft_ft_integrals(kvft_ctx *ctx, int n, const double *eps,
                       const double *fock, const double *eri, double beta,
                       double mu, double *const F[4], double *const I[9]);
 
+/* ---- model-system integrals on the device: replace the n^4 loops of
+ * kelvin/ueg_utils.py:83-138 (UEG) and kelvin/hubbard_system.py (1D Hubbard
+ * ring in the momentum basis) behind System.g_aint_tot -------------------
+ * Write the antisymmetrised spin-orbital <pq||rs> (general-spin order: nb
+ * alpha orbitals, then nb beta) into the device array eri[n][n][n][n],
+ * n = 2 nb.
+ * kvft_ueg_eri: nvec[nb][3] (host) integer plane-wave vectors, c = 4 pi / L^3
+ *   * (2 pi / L)^-2; <pq|rs> = c / |n_p - n_r|^2 for equal spins p,r and q,s,
+ *   n_p + n_q = n_r + n_s, n_p != n_r.  nb <= 512.
+ * kvft_hubbard_eri: `sites` momenta, u = U / sites; <pq|rs> = u for opposite
+ *   spins (p,r alpha and q,s beta or the reverse) and k_p + k_q = k_r + k_s
+ *   (mod sites). */
+int kvft_ueg_eri(kvft_ctx *ctx, int nb, const int *nvec, double c, double *eri);
+int kvft_hubbard_eri(kvft_ctx *ctx, int sites, double u, double *eri);
+
 /* ---- device-resident solver: replaces kelvin/ccsd.py:595-712 with
  * cc_utils.ft_integrals (569-602) and cc_utils.ft_cc_iter (111-173) -------
  * eps[n] orbital energies, fock[n][n] (System.g_fock_tot), eri[n][n][n][n]
- * (System.g_aint_tot), all HOST pointers; grid ti/g/G host pointers. */
+ * (System.g_aint_tot): host or device pointers (unified addressing; a device
+ * eri from kvft_ueg_eri / kvft_hubbard_eri skips the upload); grid ti/g/G
+ * host pointers. */
 typedef struct {
     double econv;     /* |dE| threshold */
     double tconv;     /* res1+res2 threshold */

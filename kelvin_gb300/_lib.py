@@ -97,6 +97,8 @@ _SIGS = {
                                                  ctypes.c_double, ctypes.c_int, vp]),
     "kvft_gemm": (ctypes.c_int, [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                  ctypes.c_int, ctypes.c_int, vp, vp, vp]),
+    "kvft_ueg_eri": (ctypes.c_int, [vp, ctypes.c_int, vp, ctypes.c_double, vp]),
+    "kvft_hubbard_eri": (ctypes.c_int, [vp, ctypes.c_int, ctypes.c_double, vp]),
     "kvft_ft_integrals": (ctypes.c_int, [vp, ctypes.c_int, vp, vp, vp, ctypes.c_double,
                                          ctypes.c_double, ctypes.POINTER(vp),
                                          ctypes.POINTER(vp)]),
@@ -259,10 +261,16 @@ class DeviceArray(object):
         self.ctx.check(self.ctx.L.kvft_memset(self.ctx.h, self.ptr, 0, self.nbytes),
                        "kvft_memset")
 
+    def free(self):
+        """Release the buffer now (it is released on collection otherwise)."""
+        if self._own and self.ctx.h and self.ptr:
+            self.ctx.L.kvft_free(self.ctx.h, self.ptr)
+        self.ptr = vp()
+        self._own = False
+
     def __del__(self):
         try:
-            if self._own and self.ctx.h and self.ptr:
-                self.ctx.L.kvft_free(self.ctx.h, self.ptr)
+            self.free()
         except Exception:
             pass
 

@@ -69,13 +69,19 @@ class DeviceSolver(object):
 
     @classmethod
     def from_system(cls, ctx, en, fock, eri, beta, mu, ti, g, G):
-        en, fock, eri, ti, g, G = (numpy.ascontiguousarray(a, dtype=float)
-                                   for a in (en, fock, eri, ti, g, G))
+        """``eri`` is a host array or a DeviceArray (n, n, n, n) already on the GPU."""
+        en, fock, ti, g, G = (numpy.ascontiguousarray(a, dtype=float)
+                              for a in (en, fock, ti, g, G))
+        if isinstance(eri, _lib.DeviceArray):
+            eri_ptr = eri.ptr
+        else:
+            eri = numpy.ascontiguousarray(eri, dtype=float)
+            eri_ptr = eri.ctypes.data_as(_lib.vp)
         n, ng = en.shape[0], ti.shape[0]
         h = _lib.vp()
         ctx.check(ctx.L.kvft_solver_create(
             ctx.h, n, ng, en.ctypes.data_as(_lib.vp), fock.ctypes.data_as(_lib.vp),
-            eri.ctypes.data_as(_lib.vp), float(beta), float(mu), ti.ctypes.data_as(_lib.vp),
+            eri_ptr, float(beta), float(mu), ti.ctypes.data_as(_lib.vp),
             g.ctypes.data_as(_lib.vp), G.ctypes.data_as(_lib.vp), ctypes.byref(h)),
             "kvft_solver_create")
         return cls(ctx, h, ng, n, n)

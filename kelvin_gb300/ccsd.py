@@ -120,9 +120,16 @@ class ccsd(object):
                             "which the resident solver does not run")
         prec, digits = PRECISIONS[self.precision][0], self.digits
         self.ctx.set_precision(prec, digits)
-        solver = DeviceSolver.from_system(self.ctx, en, self.sys.g_fock_tot(),
-                                          self.sys.g_aint_tot(), beta, mu, self.ti, self.g,
-                                          self.G)
+        if getattr(self.sys, "device_build", False):
+            # integrals written on the GPU; no n^4 array on the host
+            eri = self.sys.device_aint_tot(self.ctx)
+            solver = DeviceSolver.from_system(self.ctx, en, self.sys.g_fock_tot(), eri, beta,
+                                              mu, self.ti, self.g, self.G)
+            eri.free()
+        else:
+            solver = DeviceSolver.from_system(self.ctx, en, self.sys.g_fock_tot(),
+                                              self.sys.g_aint_tot(), beta, mu, self.ti,
+                                              self.g, self.G)
         self.solver = solver
         conv = {"econv": self.econv, "tconv": self.tconv, "max_iter": self.max_iter,
                 "damp": self.damp}

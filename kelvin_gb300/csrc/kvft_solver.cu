@@ -346,9 +346,10 @@ int kvft_solver_create(kvft_ctx *ctx, int n, int ng, const double *eps, const do
         st = kv_fail(ctx, KVFT_ENOMEM, "solver_create: no room for the raw integrals");
     if (st == KVFT_OK) {
         cudaStream_t str = ctx->stream;
-        if (cudaMemcpyAsync(s->eps, eps, sizeof(double) * n, cudaMemcpyHostToDevice, str) ||
-            cudaMemcpyAsync(dfock, fock, sizeof(double) * n2, cudaMemcpyHostToDevice, str) ||
-            cudaMemcpyAsync(deri, eri, sizeof(double) * n4, cudaMemcpyHostToDevice, str))
+        // host or device pointers (unified addressing picks the direction)
+        if (cudaMemcpyAsync(s->eps, eps, sizeof(double) * n, cudaMemcpyDefault, str) ||
+            cudaMemcpyAsync(dfock, fock, sizeof(double) * n2, cudaMemcpyDefault, str) ||
+            cudaMemcpyAsync(deri, eri, sizeof(double) * n4, cudaMemcpyDefault, str))
             st = kv_fail(ctx, KVFT_EDEVICE, "solver_create: upload failed");
     }
     if (st == KVFT_OK) {

@@ -80,10 +80,16 @@ class UEGSystem(object):
     ``hf_shift=True`` adds the exchange shift of the ``nref`` lowest plane
     waves (closed-shell T = 0 reference), as Kelvin's UEGSCFSystem does with
     its occupied set (ueg_scf_system.py:53-78, 280-289).
+
+    ``device_build=True``: the n^4 integrals are written on the GPU by
+    ``device_aint_tot`` (kvft_ueg_eri) and the Fock matrix, the first-order
+    energy and the exchange shift use their closed forms -- by momentum
+    conservation the direct terms vanish and each is a sum over pairs of
+    plane waves -- so no n^4 array exists on the host.
     """
 
     def __init__(self, T, L, cutoff=None, mu=None, norb=None, hf_shift=False,
-                 nref=None, N=None):
+                 nref=None, N=None, device_build=False):
         self.T = T
         self.L = L
         self.nvec = plane_waves(L, cutoff, norb)
@@ -94,6 +100,7 @@ class UEGSystem(object):
         self.ekin = 0.5 * (self.kvec ** 2).sum(1)
         self.pref = 4.0 * numpy.pi / L ** 3
         self.hf_shift = hf_shift
+        self.device_build = device_build
         e = self.ekin.copy()
         if hf_shift:
             if nref is None:
@@ -102,9 +109,13 @@ class UEGSystem(object):
                 occ = numpy.nonzero(self.ekin < mu)[0]
             else:
                 occ = numpy.arange(nref)
-            V = self._spatial()
-            e = e + 2 * numpy.einsum('pipi->p', V[:, occ][:, :, :, occ]) \
-                - numpy.einsum('piip->p', V[:, occ][:, :, occ, :])
+            if device_build:
+                # <pi|pi> = 0 (q = 0 excluded), <pi|ip> = v(n_p - n_i)
+                e = e - self._vq()[:, occ].sum(1)
+            else:
+                V = self._spatial()
+                e = e + 2 * numpy.einsum('pipi->p', V[:, occ][:, :, :, occ]) \
+                    - numpy.einsum('piip->p', V[:, occ][:, :, occ, :])
         self.e_spatial = e
         beta = 1.0 / T
         if mu is None:
@@ -115,6 +126,28 @@ class UEGSystem(object):
         self.mu = mu
         self.N = float(fermi(beta, self.g_energies_tot(), mu).sum())
         self._eri = None
+
+    def _coulomb_const(self):
+        """c of <pq|rs> = c / |n_p - n_r|^2, evaluated as in ``_spatial``."""
+        return self.pref * (2 * numpy.pi / self.L) ** -2
+
+    def _vq(self):
+        """v[p, r] = c / |n_p - n_r|^2 (0 for p = r): the nb x nb exchange kernel."""
+        n = self.nvec
+        dq = n[:, None, :] - n[None, :, :]
+        q2 = (dq * dq).sum(-1).astype(float)
+        with numpy.errstate(divide='ignore'):
+            return numpy.where(q2 > 0, self._coulomb_const() / q2, 0.0)
+
+    def device_aint_tot(self, ctx):
+        """g_aint_tot() written on the device: a DeviceArray (n, n, n, n)."""
+        from . import _lib
+        n = 2 * self.nb
+        out = _lib.DeviceArray(ctx, (n, n, n, n))
+        nv = numpy.ascontiguousarray(self.nvec, dtype=numpy.int32)
+        ctx.check(ctx.L.kvft_ueg_eri(ctx.h, self.nb, nv.ctypes.data_as(_lib.vp),
+                                     float(self._coulomb_const()), out.ptr), "kvft_ueg_eri")
+        return out
 
     def _spatial(self):
         """<pq|rs> = pref/|k_p-k_r|^2 if n_p+n_q = n_r+n_s, p != r, q != s."""
@@ -166,18 +199,35 @@ class UEGSystem(object):
         beta = 1.0 / self.T
         fo = fermi(beta, self.g_energies_tot(), self.mu)
         kin = numpy.hstack((self.ekin, self.ekin))
+        if self.device_build:
+            # F_pq = delta_pq (k_p^2/2 - sum_{r, same spin} v(n_p - n_r) f_r)
+            v = self._vq()
+            nb = self.nb
+            x = numpy.hstack((v @ fo[:nb], v @ fo[nb:]))
+            return numpy.diag(kin - x)
         return numpy.diag(kin) + numpy.einsum('prqr,r->pq', self.g_aint_tot(), fo)
 
     def get_mp1(self):
         fo = fermi(1.0 / self.T, self.g_energies_tot(), self.mu)
+        if self.device_build:
+            # 1/2 sum_ij <ij||ij> f_i f_j = -1/2 sum_{ij, same spin} v(n_i - n_j) f_i f_j
+            v = self._vq()
+            nb = self.nb
+            return -0.5 * (fo[:nb] @ v @ fo[:nb] + fo[nb:] @ v @ fo[nb:])
         return 0.5 * numpy.einsum('ijij,i,j->', self.g_aint_tot(), fo, fo)
 
 
 class HubbardRing(object):
-    """1D Hubbard ring in the momentum basis (spin orbitals: alpha k, beta k)."""
+    """1D Hubbard ring in the momentum basis (spin orbitals: alpha k, beta k).
 
-    def __init__(self, T, sites, t=1.0, U=4.0, mu=0.0):
+    ``device_build=True``: integrals written on the GPU (kvft_hubbard_eri);
+    Fock matrix and first-order energy from their closed forms (the on-site
+    U couples opposite spins only: F_pp = e_p + (U/L) N_other spin,
+    E1 = (U/L) N_alpha N_beta)."""
+
+    def __init__(self, T, sites, t=1.0, U=4.0, mu=0.0, device_build=False):
         self.T = T
+        self.device_build = device_build
         self.L = sites
         self.t = t
         self.U = U
@@ -216,16 +266,33 @@ class HubbardRing(object):
             self._eri = V - V.transpose(0, 1, 3, 2)
         return self._eri
 
+    def device_aint_tot(self, ctx):
+        """g_aint_tot() written on the device: a DeviceArray (n, n, n, n)."""
+        from . import _lib
+        n = 2 * self.L
+        out = _lib.DeviceArray(ctx, (n, n, n, n))
+        ctx.check(ctx.L.kvft_hubbard_eri(ctx.h, self.L, float(self.U / self.L), out.ptr),
+                  "kvft_hubbard_eri")
+        return out
+
     def g_fock_tot(self):
         fo = fermi(1.0 / self.T, self.g_energies_tot(), self.mu)
+        if self.device_build:
+            L = self.L
+            na, nb = fo[:L].sum(), fo[L:].sum()
+            return numpy.diag(self.g_energies_tot() + (self.U / L) *
+                              numpy.hstack((numpy.full(L, nb), numpy.full(L, na))))
         return numpy.diag(self.g_energies_tot()) + numpy.einsum('prqr,r->pq', self.g_aint_tot(), fo)
 
     def get_mp1(self):
         fo = fermi(1.0 / self.T, self.g_energies_tot(), self.mu)
+        if self.device_build:
+            L = self.L
+            return (self.U / L) * fo[:L].sum() * fo[L:].sum()
         return 0.5 * numpy.einsum('ijij,i,j->', self.g_aint_tot(), fo, fo)
 
 
-def ueg_recipe(N, rs, norb, theta, hf_shift=True):
+def ueg_recipe(N, rs, norb, theta, hf_shift=True, device_build=False):
     """UEG of N electrons at Wigner-Seitz radius rs in a cubic box
     L = (4 pi N / 3)^(1/3) rs, the norb lowest plane waves, T = theta T_F with
     T_F = k_F^2 / 2, k_F = (9 pi / 4)^(1/3) / rs, mu from non-interacting
@@ -233,9 +300,10 @@ def ueg_recipe(N, rs, norb, theta, hf_shift=True):
     L = (4.0 * numpy.pi * N / 3.0) ** (1.0 / 3.0) * rs
     kF = (9.0 * numpy.pi / 4.0) ** (1.0 / 3.0) / rs
     T = theta * 0.5 * kF * kF
-    return UEGSystem(T, L, norb=norb, N=N, hf_shift=hf_shift, nref=int(round(N)) // 2)
+    return UEGSystem(T, L, norb=norb, N=N, hf_shift=hf_shift, nref=int(round(N)) // 2,
+                     device_build=device_build)
 
 
-def hubbard_recipe(sites, t, U, beta):
+def hubbard_recipe(sites, t, U, beta, device_build=False):
     """Half-filled Hubbard ring at inverse temperature beta (mu = 0)."""
-    return HubbardRing(1.0 / beta, sites, t=t, U=U, mu=0.0)
+    return HubbardRing(1.0 / beta, sites, t=t, U=U, mu=0.0, device_build=device_build)
