@@ -62,7 +62,8 @@ WORKLOADS = {
                         "ng=10, damping 0.5, econv 1e-10"),
 }
 ITERS_FALLBACK = 30
-REFINE = 2          # FP64-accurate refinement sweeps that end a mixed solve
+REFINE = 2          # refinement sweeps that end a mixed solve
+REFINE_DIGITS = 5   # their digit levels
 STEP_EVENTS = 8     # first event slot of the per-step timings (at most 50 steps)
 
 
@@ -272,7 +273,8 @@ def run_gpu(args, w):
     def one_step():
         if per_solve:
             solver.guess(1)
-            E, info = ccsd.converge(solver, ctx, conv, args.precision, digits, REFINE)
+            E, info = ccsd.converge(solver, ctx, conv, args.precision, digits, REFINE,
+                                    REFINE_DIGITS)
             return E, info["iterations"] + info["iterations_refine"]
         return solver.step(w["damp"])[0], 1
 
@@ -305,21 +307,25 @@ def run_gpu(args, w):
     if per_solve:
         iters = results[-1][1]
 
-    # one FP64-accurate step beside the headline precision (mixed vs FP64)
-    fp64_step_ms = None
+    # an FP64-accurate (7-level) step beside the headline precision, and for a
+    # per-iteration workload the refinement sweep that ends a mixed solve
+    fp64_step_ms = refine_step_ms = None
     if args.precision == "mixed":
-        ctx.set_precision(_lib.PREC_FP64_TC, 7)
-        one_step()
-        ctx.sync()
-        ctx.record(4)
-        one_step()
-        ctx.record(5)
-        ctx.sync()
-        fp64_step_ms = ctx.elapsed_ms(4, 5)
-        ctx.set_precision(prec, digits)
+        def timed_step(levels):
+            ctx.set_precision(_lib.PREC_FP64_TC, levels)
+            one_step()                                   # warm-up at this precision
+            ctx.sync()
+            ctx.record(4)
+            one_step()
+            ctx.record(5)
+            ctx.sync()
+            return ctx.elapsed_ms(4, 5)
+        fp64_step_ms = timed_step(7)
         if not per_solve:
-            # a mixed solve = iterations at few digits + FP64-accurate refinement sweeps
-            value = ws / ((iters * step_ms + REFINE * fp64_step_ms) / 1e3)
+            refine_step_ms = timed_step(REFINE_DIGITS)
+            # a mixed solve = iterations at few digits + the refinement sweeps
+            value = ws / ((iters * step_ms + REFINE * refine_step_ms) / 1e3)
+        ctx.set_precision(prec, digits)
     solver.close()
 
     # ---- end to end through the public API (e2e) -----------------------------
@@ -334,7 +340,8 @@ def run_gpu(args, w):
     for _ in range(n_e2e):
         cc = ccsd.ccsd(sysobj, T=sysobj.T, mu=sysobj.mu, max_iter=w["max_iter"],
                        damp=w["damp"], ngrid=ng, econv=w["econv"], precision=args.precision,
-                       digits=digits, refine_sweeps=REFINE, ctx=ctx)
+                       digits=digits, refine_sweeps=REFINE, refine_digits=REFINE_DIGITS,
+                       ctx=ctx)
         cc.run()
         e2e_iters = cc.iterations + cc.iterations_refine
         cc.release()
@@ -386,6 +393,9 @@ def run_gpu(args, w):
     if lat:
         q = lambda f: lat[min(len(lat) - 1, int(f * len(lat)))]
         cfg["step_latency_ms"] = {"p50": q(0.5), "p99": q(0.99), "n": len(lat)}
+    if refine_step_ms is not None:
+        cfg["refinement"] = {"sweeps": REFINE, "digit_levels": REFINE_DIGITS,
+                             "step_ms": refine_step_ms}
     if fp64_step_ms is not None:
         cfg["fp64_tc_step_ms"] = fp64_step_ms
         cfg["fp64_tc_solves_per_s"] = ws / (fp64_step_ms / 1e3) / (1 if per_solve else iters)

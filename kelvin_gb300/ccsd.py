@@ -22,15 +22,17 @@ PRECISIONS = {'fp64': (_lib.PREC_FP64, 7), 'fp64_tc': (_lib.PREC_FP64_TC, 7),
               'mixed': (_lib.PREC_MIXED, 3)}
 
 
-def converge(solver, ctx, conv, precision, digits, refine_sweeps=2):
+def converge(solver, ctx, conv, precision, digits, refine_sweeps=2, refine_digits=5):
     """Iterate a DeviceSolver to convergence; returns (Omega_cc, info).
 
     FP64 forms use Kelvin's test (|dE| < econv and res < tconv).  The mixed
     form's few-digit update is a slightly discontinuous map (digit rounding),
     so its iteration settles at a noise floor instead of meeting econv: it
     stops at Kelvin's test or when the residual has stopped falling for three
-    sweeps, then runs `refine_sweeps` sweeps with FP64-accurate contractions
-    from that point."""
+    sweeps, then runs `refine_sweeps` sweeps from that point with
+    `refine_digits` digit levels (5: norm-wise ~1e-9 per contraction, far
+    below the 1e-6 Ha per electron the mixed form answers to, at half the
+    products of the FP64-grade 7)."""
     if precision != 'mixed':
         E = iterate(solver, conv, "CCSD")
         return E, {"iterations": solver.iterations, "iterations_refine": 0,
@@ -42,7 +44,7 @@ def converge(solver, ctx, conv, precision, digits, refine_sweeps=2):
     E = E_low
     if refine_sweeps > 0:
         prec = ctx_precision(ctx)
-        ctx.set_precision(_lib.PREC_FP64_TC, 7)
+        ctx.set_precision(_lib.PREC_FP64_TC, refine_digits)
         try:
             ref = dict(conv)
             ref["max_iter"] = refine_sweeps
@@ -64,7 +66,7 @@ class ccsd(object):
     def __init__(self, sys, T=0.0, mu=0.0, iprint=0, singles=True, econv=1e-8,
                  tconv=None, max_iter=40, damp=0.0, ngrid=10, realtime=False,
                  athresh=0.0, quad='lin', rt_iter="all", precision='fp64',
-                 digits=None, refine_sweeps=2, device=0, ctx=None):
+                 digits=None, refine_sweeps=2, refine_digits=5, device=0, ctx=None):
         self.T = T
         self.mu = mu
         self.finite_T = T != 0
@@ -86,6 +88,7 @@ class ccsd(object):
         # mixed form: sweeps re-evaluated with FP64-accurate contractions once
         # the few-digit iteration has converged (0: none)
         self.refine_sweeps = refine_sweeps
+        self.refine_digits = refine_digits
         if not sys.verify(self.T, self.mu):
             raise Exception("Sytem temperature inconsistent with CC temp")
         if not self.finite_T:
@@ -153,7 +156,7 @@ class ccsd(object):
             E2 = solver.guess(1)
         logging.info('MP2 Energy: {:.10f}'.format(E2))
         Eccn, info = converge(solver, self.ctx, conv, self.precision, digits,
-                              self.refine_sweeps)
+                              self.refine_sweeps, self.refine_digits)
         self.iterations = info["iterations"]
         self.iterations_refine = info["iterations_refine"]
         self.converged = info["converged"]
