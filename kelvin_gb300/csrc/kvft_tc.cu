@@ -68,7 +68,7 @@ struct TcParams {
     double alpha, beta;
     int alpha_pow2;       // alpha = +-2^alpha_exp: folded into the exponent field
     int alpha_exp;
-    unsigned long long alpha_sign;   // sign bit of alpha (FP64 position)
+    unsigned alpha_sign;  // sign bit of alpha (bit 31 of the FP64 high word)
     KOut C;
     int *err;
 };
@@ -112,17 +112,18 @@ __device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
     e = (a - (s - bb)) + (b - bb);
 }
 
-// FP64 value of x 2^k with sign flipped by `sgn`, built from the FP32 bit
-// pattern (exact; FP32 subnormals, below 2^-126 of the accumulator, give 0)
-__device__ __forceinline__ double f32_scaled(float x, int k, unsigned long long sgn) {
+// FP64 value of x 2^k with sign flipped by `sgn` (0 or 0x80000000), built
+// from the FP32 bit pattern in 32-bit halves: high word = sign | exponent
+// E - 127 + 1023 + k | top 20 mantissa bits, low word = the other 3 mantissa
+// bits at the top (exact; FP32 subnormals, below 2^-126 of the accumulator,
+// give 0)
+__device__ __forceinline__ double f32_scaled(float x, int k, unsigned sgn) {
     const uint32_t u = __float_as_uint(x);
     const int E = (int)((u >> 23) & 0xFF);
-    const int e64 = E - 127 + 1023 + k;
+    const int e64 = E + (1023 - 127) + k;
     if (E == 0 || e64 <= 0) return 0.0;
-    const unsigned long long bits = (((unsigned long long)(u >> 31) << 63) ^ sgn) |
-                                    ((unsigned long long)e64 << 52) |
-                                    ((unsigned long long)(u & 0x7FFFFFu) << 29);
-    return __longlong_as_double(bits);
+    const uint32_t hi = ((u & 0x80000000u) ^ sgn) | ((uint32_t)e64 << 20) | ((u >> 3) & 0xFFFFFu);
+    return __hiloint2double((int)hi, (int)(u << 29));
 }
 
 // Raw row exponents are reduced with atomicMax into an array preset to
@@ -1006,7 +1007,7 @@ int gemm_tc_run(kvft_ctx *ctx, int M, int N, int K, int batch, double alpha, con
         const double fr = std::frexp(alpha, &ex2);
         p.alpha_pow2 = (std::fabs(fr) == 0.5) ? 1 : 0;
         p.alpha_exp = p.alpha_pow2 ? ex2 - 1 : 0;
-        p.alpha_sign = (p.alpha_pow2 && alpha < 0) ? (1ull << 63) : 0ull;
+        p.alpha_sign = (p.alpha_pow2 && alpha < 0) ? 0x80000000u : 0u;
     }
     p.C = C;
     p.err = ctx->dflag;
