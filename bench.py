@@ -431,11 +431,17 @@ def run_profile_step(args, w):
     solver.step(w["damp"])
     ctx.sync()
     l0 = ctx.launches()
+    ctx.profile_begin()
     E, res = solver.step(w["damp"])
     ctx.sync()
+    recs = ctx.profile_records()
+    ctx.profile_end()
+    # the category of each contraction of the step, in launch order: one
+    # GEMM kernel (tc_gemm_kernel or gemm_f64_kernel) per contraction
+    gemm_cats = [c for c, _, _ in recs if c in ("gemm6", "gemm")]
     print(json.dumps({"profile_step": args.workload, "precision": args.precision,
                       "launches_before": l0, "launches_in_step": ctx.launches() - l0,
-                      "omega_cc": E, "res": res}))
+                      "omega_cc": E, "res": res, "gemm_categories": gemm_cats}))
     solver.close()
     return 0
 

@@ -82,6 +82,13 @@ typedef struct {
 } kvft_profile_stats;
 int kvft_profile_begin(kvft_ctx *ctx);
 int kvft_profile_end(kvft_ctx *ctx, kvft_profile_stats *out);
+/* The timed scopes of the current profile one by one, in completion order
+ * (a packing pass ends before the contraction that uses it): category,
+ * device milliseconds and algorithmic work.  *count receives the number of
+ * scopes; up to `max` are written.  Call before kvft_profile_end, which
+ * discards them. */
+int kvft_profile_records(kvft_ctx *ctx, int max, int *count, int *cat, float *ms,
+                         double *work);
 
 /* ---- quadrature: replaces kelvin/quadrature.py:292-317 ------------------
  * out[y] = sum_x G[y][x] exp(dt D) tbar[x], dt = ti[x]-ti[y] for x < y and 0

@@ -56,6 +56,8 @@ PROFILE_CATEGORIES = ("gemm6", "gemm", "quad", "energy", "elem", "pack")
 _SIGS = {
     "kvft_profile_begin": (ctypes.c_int, [vp]),
     "kvft_profile_end": (ctypes.c_int, [vp, ctypes.POINTER(ProfileStats)]),
+    "kvft_profile_records": (ctypes.c_int, [vp, ctypes.c_int, ctypes.POINTER(ctypes.c_int),
+                                            vp, vp, vp]),
     "kvft_ctx_create": (ctypes.c_int, [ctypes.c_int, vp, ctypes.POINTER(vp)]),
     "kvft_ctx_destroy": (ctypes.c_int, [vp]),
     "kvft_last_error": (ctypes.c_char_p, [vp]),
@@ -195,6 +197,20 @@ class Context(object):
 
     def profile_begin(self):
         self.check(self.L.kvft_profile_begin(self.h), "kvft_profile_begin")
+
+    def profile_records(self):
+        """[(category, device ms, algorithmic work)] of every timed scope so
+        far, in completion order (call before profile_end)."""
+        n = ctypes.c_int()
+        self.check(self.L.kvft_profile_records(self.h, 0, ctypes.byref(n), None, None, None),
+                   "kvft_profile_records")
+        cat = (ctypes.c_int * max(n.value, 1))()
+        ms = (ctypes.c_float * max(n.value, 1))()
+        work = (ctypes.c_double * max(n.value, 1))()
+        self.check(self.L.kvft_profile_records(self.h, n.value, ctypes.byref(n), cat, ms, work),
+                   "kvft_profile_records")
+        return [(PROFILE_CATEGORIES[cat[i]], float(ms[i]), float(work[i]))
+                for i in range(n.value)]
 
     def profile_end(self):
         """{category: (launches, total ms, algorithmic work)}."""

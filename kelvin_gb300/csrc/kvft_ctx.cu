@@ -220,6 +220,23 @@ extern "C" int kvft_profile_begin(kvft_ctx *c) {
     return KVFT_OK;
 }
 
+extern "C" int kvft_profile_records(kvft_ctx *c, int max, int *count, int *cat, float *ms,
+                                    double *work) {
+    if (!c || !c->prof || !count || max < 0 || (max > 0 && (!cat || !ms || !work)))
+        return KVFT_EINVAL;
+    KV_CHECK(c, cudaStreamSynchronize(c->stream));
+    const auto &recs = c->prof->recs;
+    *count = (int)recs.size();
+    for (int i = 0; i < max && i < (int)recs.size(); i++) {
+        float t = 0.f;
+        KV_CHECK(c, cudaEventElapsedTime(&t, c->prof->pool[recs[i].e0], c->prof->pool[recs[i].e1]));
+        cat[i] = recs[i].cat;
+        ms[i] = t;
+        work[i] = recs[i].work;
+    }
+    return KVFT_OK;
+}
+
 extern "C" int kvft_profile_end(kvft_ctx *c, kvft_profile_stats *out) {
     if (!c || !c->prof || !out) return KVFT_EINVAL;
     KV_CHECK(c, cudaStreamSynchronize(c->stream));

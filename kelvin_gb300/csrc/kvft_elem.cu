@@ -33,9 +33,13 @@ __device__ __forceinline__ void pair_of(int x, int n, int &p, int &q) {
 
 // One block per (batch, i0, i1, chunk of AX_CHUNK (i2, i3) positions); its
 // threads walk (i2, i3), the innermost index fastest, so only a 32-bit
-// division per element remains.
+// division per element remains.  GB300 issues about two FP64 operations per
+// clock per SM, so the common cases get their own instances: KIND 0 copies
+// with alpha = +-1 (no FP64 operation), KIND 1 scales (beta = 0: dst is not
+// read), KIND 2 is the general dst = beta dst + alpha src.
 constexpr int AX_CHUNK = 2048;
 
+template <int KIND>
 __global__ void __launch_bounds__(256)
 axpby4_kernel(long long nblk, Dims4 g, double alpha, const double *__restrict__ src,
               double beta, double *__restrict__ dst) {
@@ -56,18 +60,22 @@ axpby4_kernel(long long nblk, Dims4 g, double alpha, const double *__restrict__ 
             const int t = i3s + k;               // < d3 + AX_CHUNK: 32-bit
             const long long i2 = i2s + t / g.d[3];
             const int i3 = t % g.d[3];
-            const double v = alpha * s[i2 * g.ss[2] + i3 * g.ss[3]];
+            const double x = s[i2 * g.ss[2] + i3 * g.ss[3]];
             double *o = d + i2 * g.ds[2] + i3 * g.ds[3];
-            *o = (beta != 0.0) ? fma(beta, *o, v) : v;
+            if (KIND == 0) *o = alpha < 0.0 ? -x : x;
+            else if (KIND == 1) *o = alpha * x;
+            else *o = fma(beta, *o, alpha * x);
         }
     }
 }
 
 // out[y,a,b,i,j] = t2 + c (t1[a,i] t1[b,j] - t1[b,i] t1[a,j]); one block per
-// (y, a, b), threads over (i, j)
+// (y, a, b), threads over (i, j).  The rows c t1[a,:] and c t1[b,:] are formed
+// once per block in shared memory, so each element costs two FP64 FMAs.
 __global__ void __launch_bounds__(256)
 make_tau_kernel(long long nblk, int nv, int no, const double *__restrict__ t1,
                 const double *__restrict__ t2, double c, double *__restrict__ out) {
+    extern __shared__ double cab[];                  // [2][no]: c t1[a,:], c t1[b,:]
     const int oo = no * no;
     for (long long blk = blockIdx.x; blk < nblk; blk += gridDim.x) {
         const long long y = blk / ((long long)nv * nv);
@@ -75,10 +83,16 @@ make_tau_kernel(long long nblk, int nv, int no, const double *__restrict__ t1,
         const int a = ab / nv, b = ab % nv;
         const double *u = t1 + y * nv * no;
         const double *ua = u + a * no, *ub = u + b * no;
+        __syncthreads();
+        for (int x = threadIdx.x; x < no; x += blockDim.x) {
+            cab[x] = c * ua[x];
+            cab[no + x] = c * ub[x];
+        }
+        __syncthreads();
         const long long base = blk * oo;
         for (int e = threadIdx.x; e < oo; e += blockDim.x) {
             const int i = e / no, j = e % no;
-            out[base + e] = t2[base + e] + c * (ua[i] * ub[j] - ub[i] * ua[j]);
+            out[base + e] = fma(cab[i], ub[j], fma(-cab[no + i], ua[j], t2[base + e]));
         }
     }
 }
@@ -124,7 +138,11 @@ wmbej_tmp_kernel(int nv, int no, const double *__restrict__ t1, const double *__
 // element is read once, coalesced, and R = Q - Q^T + (L - L^T) is added to
 // T2[a,b] and subtracted from T2[b,a].  The a = b blocks of T2 get nothing.
 // Every other element of T2 receives exactly one addition, issued as a
-// fire-and-forget reduction at L2 (one rounding, like load-add-store).
+// fire-and-forget reduction at L2 (one rounding, like load-add-store); the
+// additions then cost the SM's scarce FP64 pipe nothing.
+// FS: fac is +1 (1), -1 (2) or anything else (0); the signs cost no FP64
+// operation.
+template <int FS>
 __global__ void __launch_bounds__(256)
 assemble_t2_kernel(int nv, int no, double fac, const double *__restrict__ Z,
                    const double *__restrict__ Lc, double *__restrict__ T2) {
@@ -167,14 +185,16 @@ assemble_t2_kernel(int nv, int no, double fac, const double *__restrict__ Z,
             const int r = ty + 8 * k;
             int i = i0 + r, j = j0 + tx;
             if (i < no && j < no) {
-                const double R = fac * (qa[r][tx] - qb[tx][r] + ladder(i, j));
+                const double R0 = qa[r][tx] - qb[tx][r] + ladder(i, j);
+                const double R = FS == 0 ? fac * R0 : (FS == 1 ? R0 : -R0);
                 atomicAdd(T2 + oab + i * no + j, R);
                 atomicAdd(T2 + oba + i * no + j, -R);
             }
             i = j0 + r;
             j = i0 + tx;
             if (it != jt && i < no && j < no) {
-                const double R = fac * (qb[r][tx] - qa[tx][r] + ladder(i, j));
+                const double R0 = qb[r][tx] - qa[tx][r] + ladder(i, j);
+                const double R = FS == 0 ? fac * R0 : (FS == 1 ? R0 : -R0);
                 atomicAdd(T2 + oab + i * no + j, R);
                 atomicAdd(T2 + oba + i * no + j, -R);
             }
@@ -267,8 +287,13 @@ int kv_axpby4(kvft_ctx *ctx, int batch, const int dims[4], double alpha,
     KvProfScope prof(ctx, KV_CAT_ELEM, 8.0 * total * (beta != 0.0 ? 3 : 2));
     const long long nblk = (long long)batch * dims[0] * dims[1] *
                            (((long long)dims[2] * dims[3] + AX_CHUNK - 1) / AX_CHUNK);
-    axpby4_kernel<<<(unsigned)std::min(nblk, (long long)ctx->sm_count * 16), 256, 0,
-                    ctx->stream>>>(nblk, g, alpha, src, beta, dst);
+    const unsigned grid = (unsigned)std::min(nblk, (long long)ctx->sm_count * 16);
+    if (beta == 0.0 && (alpha == 1.0 || alpha == -1.0))
+        axpby4_kernel<0><<<grid, 256, 0, ctx->stream>>>(nblk, g, alpha, src, beta, dst);
+    else if (beta == 0.0)
+        axpby4_kernel<1><<<grid, 256, 0, ctx->stream>>>(nblk, g, alpha, src, beta, dst);
+    else
+        axpby4_kernel<2><<<grid, 256, 0, ctx->stream>>>(nblk, g, alpha, src, beta, dst);
     return kv_launch_check(ctx, "axpby4");
 }
 
@@ -278,8 +303,9 @@ int kv_make_tau(kvft_ctx *ctx, int batch, int nv, int no, const double *t1,
     if (total == 0) return KVFT_OK;
     KvProfScope prof(ctx, KV_CAT_ELEM, 16.0 * total);
     const long long nblk = (long long)batch * nv * nv;
-    make_tau_kernel<<<(unsigned)std::min(nblk, (long long)ctx->sm_count * 16), 256, 0,
-                      ctx->stream>>>(nblk, nv, no, t1, t2, c, out);
+    if (no > 3072) return kv_fail(ctx, KVFT_EINVAL, "make_tau: more than 3072 occupied orbitals");
+    make_tau_kernel<<<(unsigned)std::min(nblk, (long long)ctx->sm_count * 16), 256,
+                      2 * no * sizeof(double), ctx->stream>>>(nblk, nv, no, t1, t2, c, out);
     return kv_launch_check(ctx, "make_tau");
 }
 
@@ -303,7 +329,12 @@ int kv_assemble_t2(kvft_ctx *ctx, int batch, int nv, int no, double fac, const d
     const int nt = (no + 31) / 32;
     const int pv = nv * (nv - 1) / 2;
     const dim3 grid(nt * (nt + 1) / 2, std::min(pv, 65535), batch);
-    assemble_t2_kernel<<<grid, 256, 0, ctx->stream>>>(nv, no, fac, Z, Lc, T2);
+    if (fac == 1.0)
+        assemble_t2_kernel<1><<<grid, 256, 0, ctx->stream>>>(nv, no, fac, Z, Lc, T2);
+    else if (fac == -1.0)
+        assemble_t2_kernel<2><<<grid, 256, 0, ctx->stream>>>(nv, no, fac, Z, Lc, T2);
+    else
+        assemble_t2_kernel<0><<<grid, 256, 0, ctx->stream>>>(nv, no, fac, Z, Lc, T2);
     return kv_launch_check(ctx, "assemble_t2");
 }
 

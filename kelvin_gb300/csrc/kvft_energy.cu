@@ -10,12 +10,22 @@ namespace {
 
 constexpr int TILE = 32;
 
-__global__ void __launch_bounds__(256)
+// One block per 32 x 32 tile of (a,b) x (i,j); thread (tx, ty) takes i,j =
+// ij0 + tx and the four (a,b) rows ty + 8k.  Per element and tau point two
+// FP64 FMAs: s1 += g_y T2_y and s2 += (g_y T1_y[a,i]) T1_y[b,j], the first
+// factor of the second from a shared table over the few (a, i) values of the
+// tile, filled for a chunk of tau points at a time; the element's weight is
+// then s1/4 + s2/2.
+constexpr int WTAB = 1024;                  // doubles of the (y, a, i) table
+
+__global__ void __launch_bounds__(256, 2)
 energy2_kernel(int ng, int nv, int no, const double *__restrict__ T1,
                const double *__restrict__ T2, const double *__restrict__ eri,
                const double *__restrict__ g, int qterm, double *__restrict__ partial) {
     __shared__ double E[TILE][TILE + 1];     // [ij][ab]
     __shared__ double red[256];
+    __shared__ double gs[WTAB / 4];          // g_y of the chunk
+    __shared__ double wt[WTAB];              // [y][a - a_lo][i - i_lo]: g_y T1_y[a,i]
     const long long V2 = (long long)nv * nv, O2 = (long long)no * no;
     const long long ab0 = (long long)blockIdx.y * TILE, ij0 = (long long)blockIdx.x * TILE;
     const int t = threadIdx.x, tx = t % TILE, ty = t / TILE;   // ty in [0, 8)
@@ -23,27 +33,62 @@ energy2_kernel(int ng, int nv, int no, const double *__restrict__ T1,
         long long ij = ij0 + r, ab = ab0 + tx;
         E[r][tx] = (ij < O2 && ab < V2) ? eri[ij * V2 + ab] : 0.0;
     }
-    __syncthreads();
-    double acc = 0.0;
+    const long long ab_hi = min(ab0 + TILE, V2) - 1, ij_hi = min(ij0 + TILE, O2) - 1;
+    const int a_lo = (int)(ab0 / nv), na = (int)(ab_hi / nv) - a_lo + 1;
+    const int i_lo = (int)(ij0 / no), ni = (int)(ij_hi / no) - i_lo + 1;
+    const int yc = qterm ? max(1, min(WTAB / 4, WTAB / (na * ni))) : WTAB / 4;
     const long long ij = ij0 + tx;
-    if (ij < O2) {
-        const int i = (int)(ij / no), j = (int)(ij % no);
-        for (int r = ty; r < TILE; r += 8) {
-            const long long ab = ab0 + r;
-            if (ab >= V2) break;
-            const int a = (int)(ab / nv), b = (int)(ab % nv);
-            double s = 0.0;
-            for (int y = 0; y < ng; y++) {
-                double v = 0.25 * T2[((long long)y * V2 + ab) * O2 + ij];
-                if (qterm) {
-                    const double *u = T1 + (long long)y * nv * no;
-                    v = fma(0.5 * u[a * no + i], u[b * no + j], v);
-                }
-                s = fma(g[y], v, s);
+    const bool live = ij < O2;
+    const int i = live ? (int)(ij / no) : 0, j = live ? (int)(ij % no) : 0;
+    int ka[4], kb[4];
+    long long kab[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        const long long ab = min(ab0 + ty + 8 * k, ab_hi);
+        kab[k] = ab;
+        ka[k] = (int)(ab / nv);
+        kb[k] = (int)(ab % nv);
+    }
+    double s1[4] = {0.0, 0.0, 0.0, 0.0}, s2[4] = {0.0, 0.0, 0.0, 0.0};
+    const long long sy = (long long)nv * no;
+    for (int y0 = 0; y0 < ng; y0 += yc) {
+        const int ny = min(yc, ng - y0);
+        __syncthreads();
+        for (int x = t; x < ny; x += 256) gs[x] = g[y0 + x];
+        if (qterm)
+            for (int x = t; x < ny * na * ni; x += 256) {
+                const int yy = x / (na * ni), r = x % (na * ni);
+                const int a = a_lo + r / ni, ii = i_lo + r % ni;
+                wt[x] = g[y0 + yy] * T1[(y0 + yy) * sy + (long long)a * no + ii];
             }
-            acc = fma(s, E[tx][r], acc);
+        __syncthreads();
+        if (!live) continue;
+        const double *t2 = T2 + (long long)y0 * V2 * O2 + ij;
+        for (int yy = 0; yy < ny; yy++) {
+            const double gy = gs[yy];
+#pragma unroll
+            for (int k = 0; k < 4; k++) s1[k] = fma(gy, t2[kab[k] * O2], s1[k]);
+            t2 += V2 * O2;
+        }
+        if (qterm) {
+            const double *u = T1 + (long long)y0 * sy + j;
+            const double *w = wt + (i - i_lo);
+            for (int yy = 0; yy < ny; yy++) {
+#pragma unroll
+                for (int k = 0; k < 4; k++)
+                    s2[k] = fma(w[(ka[k] - a_lo) * ni], u[(long long)kb[k] * no], s2[k]);
+                u += sy;
+                w += na * ni;
+            }
         }
     }
+    double acc = 0.0;
+    if (live)
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            const int r = ty + 8 * k;
+            if (ab0 + r < V2) acc = fma(fma(0.25, s1[k], 0.5 * s2[k]), E[tx][r], acc);
+        }
     red[t] = acc;
     __syncthreads();
     for (int s = 128; s > 0; s >>= 1) {

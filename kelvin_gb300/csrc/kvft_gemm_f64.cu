@@ -150,6 +150,7 @@ int kv_gemm_f64(kvft_ctx *ctx, int M, int N, int K, int batch, double alpha,
     }
     if ((long long)batch * nsplit > 65535)
         return kv_fail(ctx, KVFT_EINVAL, "gemm batch too large");
+    KvProfScope prof(ctx, ctx->gemm_cat, ctx->gemm_work);
     dim3 grid((N + BN - 1) / BN, (M + BM - 1) / BM, batch * nsplit);
     gemm_f64_kernel<<<grid, NT, 0, ctx->stream>>>(M, N, K, nsplit, klen, alpha, A, B,
                                                    beta, C, atomic);
@@ -202,14 +203,18 @@ void order_k(int M, int N, int batch, KMat &A, KMat &B) {
 
 }  // namespace
 
+void kv_gemm_prof_set(kvft_ctx *ctx, int M, int N, int K, int batch) {
+    // n^6-class: every GEMM dimension is a pair of orbital indices or more
+    const long long mn = std::min(std::min(M, N), K), mx = std::max(std::max(M, N), K);
+    ctx->gemm_cat = (mn * mn > mx) ? KV_CAT_GEMM6 : KV_CAT_GEMM;
+    ctx->gemm_work = 2.0 * M * N * (double)K * batch;
+}
+
 int kv_gemm(kvft_ctx *ctx, int M, int N, int K, int batch, double alpha,
             const KMat &A_in, const KMat &B_in, double beta, const KOut &C) {
     KMat A = A_in, B = B_in;
     order_k(M, N, batch, A, B);
-    // n^6-class: every GEMM dimension is a pair of orbital indices or more
-    const long long mn = std::min(std::min(M, N), K), mx = std::max(std::max(M, N), K);
-    const int cat = (mn * mn > mx) ? KV_CAT_GEMM6 : KV_CAT_GEMM;
-    KvProfScope prof(ctx, cat, 2.0 * M * N * (double)K * batch);
+    kv_gemm_prof_set(ctx, M, N, K, batch);
     // Tensor cores for everything but short sums and tiny products, which stay
     // on the FP64 pipe.  Skinny shapes (a few columns against a long K) go to
     // the tensor cores too: even with most of a 128-wide tile idle they beat

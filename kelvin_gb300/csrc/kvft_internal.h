@@ -80,6 +80,10 @@ struct kvft_ctx {
     // evaluations, emptied when a solver is destroyed.
     bool pack_cache_on = false;
     std::map<std::string, std::pair<void *, size_t>> pack_cache;
+    // profile category and algorithmic flops of the contraction being
+    // launched (its kernel is timed alone, without the operand packing)
+    int gemm_cat = 1;
+    double gemm_work = 0.0;
 };
 void kv_pack_cache_clear(kvft_ctx *ctx);
 // Turns the pack cache on for the lifetime of the guard.
@@ -140,6 +144,9 @@ int kv_gemm_f64(kvft_ctx *ctx, int M, int N, int K, int batch, double alpha,
 int kv_gemm_tc(kvft_ctx *ctx, int M, int N, int K, int batch, double alpha,
                const KMat &A, const KMat &B, double beta, const KOut &C,
                int digits);
+// Sets the profile category (n^6-class or not) and flops of the next
+// contraction launch.
+void kv_gemm_prof_set(kvft_ctx *ctx, int M, int N, int K, int batch);
 // C = beta * C over a strided output view (beta == 0 writes zeros).
 int kv_scale_view(kvft_ctx *ctx, int M, int N, int batch, double beta, const KOut &C);
 // Reads (and clears) the device status word set by bounded waits; syncs.

@@ -57,9 +57,27 @@ __device__ __forceinline__ double denom(const QuadParams &q, long long p,
 // (G[y,y-s] - G[y-s,y-s]), g1[ng] (G[y,y-1]) and gd[ng] (G[y,y]), then the
 // per-thread columns r[ng][QT] (non-uniform grids) and tb[ng][QT] (general
 // path).
+// |x| as a float (mantissa truncated), from the FP64 bit pattern with
+// integer operations: GB300's FP64 pipe, not its integer or FP32 pipes, is
+// the scarce unit of this kernel.  Below 2^-126 the result is 0; above the
+// float range it is infinity (NaN stays NaN).
+__device__ __forceinline__ float abs_to_f32(double x) {
+    const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
+    const int e = (int)((hi >> 20) & 0x7FF) - 1023 + 127;
+    if (e <= 0) return 0.f;
+    if (e >= 255) {
+        const bool nan = (hi & 0x7FF00000u) == 0x7FF00000u && (((hi & 0xFFFFFu) | lo) != 0);
+        return __int_as_float(nan ? 0x7FC00000 : 0x7F800000);
+    }
+    return __int_as_float((e << 23) | (int)((hi & 0xFFFFFu) << 3) | (int)(lo >> 29));
+}
+
 // MODE 0: out = T.  MODE 1 (fused solver update): Told = alpha Told + (1-alpha) T,
-// with block partial sums of |T - Told|^2 and |Told_new|^2.
-template <int MODE>
+// with block partial sums of |T - Told|^2 and |Told_new|^2.  Those two norms
+// only steer convergence: each element's sum over tau points is taken in
+// FP32 (relative error ~1e-7) and added to FP64 block sums.  UNI: uniform
+// grid, one step factor for every step.
+template <int MODE, bool UNI>
 __global__ void __launch_bounds__(QT)
 quad_kernel(QuadParams q, const double *__restrict__ tbar, const double *__restrict__ ti_g,
             const double *__restrict__ G_g, const double *__restrict__ D,
@@ -90,12 +108,14 @@ quad_kernel(QuadParams q, const double *__restrict__ tbar, const double *__restr
         const double d = denom(q, p, D, ev, eo);
         // step factors r_k = exp((ti[k]-ti[k+1]) d)
         double r0 = 1.0;
-        if (q.uniform) {
+        if (UNI) {
             r0 = (ng > 1) ? exp((ti[0] - ti[1]) * d) : 1.0;
         } else {
             for (int k = 0; k + 1 < ng; k++) rk[k * QT + t] = exp((ti[k] - ti[k + 1]) * d);
         }
-#define RK(k) (q.uniform ? r0 : rk[(k) * QT + t])
+        const double r02 = r0 * r0;
+        float f_diff = 0.f, f_norm = 0.f;
+#define RK(k) (UNI ? r0 : rk[(k) * QT + t])
         if (q.step > 0) {
             // chained rows; keep the last `step` outputs and inputs in registers
             double Tm1 = 0.0, Tm2 = 0.0, tbm1 = 0.0, tbm2 = 0.0;
@@ -117,7 +137,7 @@ quad_kernel(QuadParams q, const double *__restrict__ tbar, const double *__restr
                     Ty = fma(gd[y], tby, RK(y - 1) * fma(cs[y], tbm1, Tm1));
                 } else {  // step 2
                     const double w1 = RK(y - 1);
-                    const double w2 = w1 * RK(y - 2);
+                    const double w2 = UNI ? r02 : w1 * RK(y - 2);
                     Ty = fma(gd[y], tby, fma(g1[y] * w1, tbm1, w2 * fma(cs[y], tbm2, Tm2)));
                 }
                 if (MODE == 0) {
@@ -127,9 +147,10 @@ quad_kernel(QuadParams q, const double *__restrict__ tbar, const double *__restr
                     double *o = out + (long long)y * q.P + p;
                     const double told = *o;
                     const double df = Ty - told;
-                    s_diff = fma(df, df, s_diff);
                     const double nt = fma(oma, df, told);
-                    s_norm = fma(nt, nt, s_norm);
+                    const float fd = abs_to_f32(df), fn = abs_to_f32(nt);
+                    f_diff = fmaf(fd, fd, f_diff);
+                    f_norm = fmaf(fn, fn, f_norm);
                     *o = nt;
                 }
                 Tm2 = Tm1; Tm1 = Ty;
@@ -159,14 +180,19 @@ quad_kernel(QuadParams q, const double *__restrict__ tbar, const double *__restr
                     double *o = out + (long long)y * q.P + p;
                     const double told = *o;
                     const double df = Ty - told;
-                    s_diff = fma(df, df, s_diff);
                     const double nt = fma(oma, df, told);
-                    s_norm = fma(nt, nt, s_norm);
+                    const float fd = abs_to_f32(df), fn = abs_to_f32(nt);
+                    f_diff = fmaf(fd, fd, f_diff);
+                    f_norm = fmaf(fn, fn, f_norm);
                     *o = nt;
                 }
             }
         }
 #undef RK
+        if (MODE == 1) {
+            s_diff += (double)f_diff;
+            s_norm += (double)f_norm;
+        }
     }
     if (MODE == 1) {
         // block reduction of the two sums (fixed order: deterministic)
@@ -286,26 +312,34 @@ int kv_quad_launch(kvft_ctx *ctx, int mode, int ng, long long P, int rank, int n
     long long blocks = (P + QT - 1) / QT;
     long long cap = (long long)ctx->sm_count * 16;
     int grid = (int)std::min(blocks, cap);
-    static bool attr_done[2] = {false, false};
-    if (!attr_done[mode]) {
-        if (mode == 0)
-            cudaFuncSetAttribute(quad_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)quad_smem(MAXNG, 0, 0));
-        else
-            cudaFuncSetAttribute(quad_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)quad_smem(MAXNG, 0, 0));
-        attr_done[mode] = true;
+    static bool attr_done = false;
+    if (!attr_done) {
+        const int mx = (int)quad_smem(MAXNG, 0, 0);
+        cudaFuncSetAttribute(quad_kernel<0, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+        cudaFuncSetAttribute(quad_kernel<0, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+        cudaFuncSetAttribute(quad_kernel<1, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+        cudaFuncSetAttribute(quad_kernel<1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+        attr_done = true;
     }
     // algorithmic bytes: tbar in, T out (mode 0); tbar + T_old in, T_old out (mode 1)
     KvProfScope prof(ctx, KV_CAT_QUAD, 8.0 * ng * (double)P * (mode == 0 ? 2 : 3));
     if (mode == 0) {
-        quad_kernel<0><<<grid, QT, smem, ctx->stream>>>(q, tbar, ti, G, D, ev, eo, out, nullptr);
+        if (q.uniform)
+            quad_kernel<0, true><<<grid, QT, smem, ctx->stream>>>(q, tbar, ti, G, D, ev, eo, out,
+                                                                  nullptr);
+        else
+            quad_kernel<0, false><<<grid, QT, smem, ctx->stream>>>(q, tbar, ti, G, D, ev, eo,
+                                                                   out, nullptr);
         return kv_launch_check(ctx, "quad_kernel");
     }
     void *part = nullptr;
     KV_TRY(kv_scratch(ctx, "quad_partial", sizeof(double) * 2 * grid, &part));
-    quad_kernel<1><<<grid, QT, smem, ctx->stream>>>(q, tbar, ti, G, D, ev, eo, out,
-                                                    (double *)part);
+    if (q.uniform)
+        quad_kernel<1, true><<<grid, QT, smem, ctx->stream>>>(q, tbar, ti, G, D, ev, eo, out,
+                                                              (double *)part);
+    else
+        quad_kernel<1, false><<<grid, QT, smem, ctx->stream>>>(q, tbar, ti, G, D, ev, eo, out,
+                                                               (double *)part);
     KV_TRY(kv_launch_check(ctx, "quad_update_kernel"));
     reduce_pairs_kernel<<<1, 256, 0, ctx->stream>>>((const double *)part, grid, res);
     return kv_launch_check(ctx, "reduce_pairs");

@@ -763,6 +763,63 @@ __device__ __forceinline__ void digits_of(unsigned long long bits, int e, int S,
         for (int s = 0; s < S; s++) d[s] = -d[s];
 }
 
+// Up to three planes take at most 21 bits of |x| 2^-e 2^(7S): the shift
+// right is at least 33, so those bits and the rounding bit all lie in the
+// high word of the significand, and 32-bit arithmetic on it gives the digits
+// of the 64-bit form above exactly (adding the rounding bit 2^(n+31) cannot
+// carry out of bits the low word decides).
+template <int S>
+__device__ __forceinline__ void digits_of_s(unsigned long long bits, int e, int *d) {
+    if (S > 3) {
+        digits_of(bits, e, S, d);
+        return;
+    }
+#pragma unroll
+    for (int s = 0; s < S; s++) d[s] = 0;
+    const unsigned hi = (unsigned)(bits >> 32);
+    const int be = (int)((hi >> 20) & 0x7FF);
+    if (be == 0) return;
+    const int n = 52 + e - (be - 1023) - 7 * S - 32;      // >= 1 since e >= be - 1021
+    unsigned Y = n < 22 ? (((hi & 0xFFFFFu) | 0x100000u) + (1u << (n - 1))) >> n : 0u;
+#pragma unroll
+    for (int s = S - 1; s >= 1; s--) {
+        int dd = (int)(Y & 127u);
+        if (dd >= 64) dd -= 128;
+        d[s] = dd;
+        Y = (unsigned)((int)Y - dd) >> 7;
+    }
+    d[0] = (int)Y;
+    if (hi >> 31)
+#pragma unroll
+        for (int s = 0; s < S; s++) d[s] = -d[s];
+}
+
+// bf16 pair (d0 2^-7s, d1 2^-7s), |d| <= 64: the float 1.5 2^23 + d is formed
+// by an integer add on its bit pattern and the offset is removed, with the
+// scaling, by one exact FMA; one conversion then packs both values.
+template <int s>
+__device__ __forceinline__ __nv_bfloat162 digit_pair(int d0, int d1) {
+    constexpr float sc = 1.0f / (float)(1ull << (7 * s));     // 2^-7s, exact
+    const float f0 = fmaf(__int_as_float(0x4B400000 + d0), sc, -12582912.0f * sc);
+    const float f1 = fmaf(__int_as_float(0x4B400000 + d1), sc, -12582912.0f * sc);
+    return __floats2bfloat162_rn(f0, f1);
+}
+
+template <int S>
+__device__ __forceinline__ void store_digits(__nv_bfloat16 *ob, size_t plane,
+                                             unsigned long long x0, unsigned long long x1,
+                                             int e) {
+    int d0[MAXS], d1[MAXS];
+    digits_of_s<S>(x0, e, d0);
+    digits_of_s<S>(x1, e, d1);
+    *reinterpret_cast<__nv_bfloat162 *>(ob) = digit_pair<0>(d0[0], d1[0]);
+    if (S > 1) *reinterpret_cast<__nv_bfloat162 *>(ob + plane) = digit_pair<1>(d0[1], d1[1]);
+    if (S > 2) *reinterpret_cast<__nv_bfloat162 *>(ob + 2 * plane) = digit_pair<2>(d0[2], d1[2]);
+    if (S > 3) *reinterpret_cast<__nv_bfloat162 *>(ob + 3 * plane) = digit_pair<3>(d0[3], d1[3]);
+    if (S > 4) *reinterpret_cast<__nv_bfloat162 *>(ob + 4 * plane) = digit_pair<4>(d0[4], d1[4]);
+    if (S > 5) *reinterpret_cast<__nv_bfloat162 *>(ob + 5 * plane) = digit_pair<5>(d0[5], d1[5]);
+}
+
 // planes[b][s][row][k] (row stride ld) = d_s 2^-7s; each thread packs two k
 template <int S>
 __global__ void __launch_bounds__(256)
@@ -780,17 +837,100 @@ pack_digits_kernel(PackView v, int R, int K, int ld, int rows_fast, const int *_
         const int row = r0 + rr;
         if (row >= R) break;
         const int e = exp_of(ex[(long long)b * R + row]);
-        int d0[MAXS], d1[MAXS];
-        digits_of(tile.v[rr][2 * tx], e, S, d0);
-        digits_of(tile.v[rr][2 * tx + 1], e, S, d1);    // zero beyond K (tile fill)
-        __nv_bfloat16 *ob = out + (size_t)b * S * plane + (size_t)row * ld + k;
+        // the second value is zero beyond K (tile fill)
+        store_digits<S>(out + (size_t)b * S * plane + (size_t)row * ld + k, plane,
+                        tile.v[rr][2 * tx], tile.v[rr][2 * tx + 1], e);
+    }
+}
+
+// Short rows (K <= 64 KT): one pass.  A block holds 32 whole rows in shared
+// memory, takes each row's exponent from there and writes its digits, so the
+// operand is read once and no atomics are needed.  The raw exponents it
+// stores are those of the two-pass path (0x80808080 for an all-zero row).
+constexpr int PR_KMAX = 256;
+
+__host__ __device__ constexpr size_t pack_rows_smem(int kt) {
+    return (size_t)PT_R * (kt * PT_K + 1) * 8 + (size_t)(kt * PT_K + PT_R) * 8;
+}
+
+template <int S, int KT>
+__global__ void __launch_bounds__(256)
+pack_rows_kernel(PackView v, int R, int K, int ld, int rows_fast, int *__restrict__ ex,
+                 __nv_bfloat16 *__restrict__ out) {
+    constexpr int NK = KT * PT_K, LDV = NK + 1;
+    extern __shared__ unsigned long long prs[];
+    unsigned long long *val = prs;                                  // [PT_R][LDV]
+    long long *koff = reinterpret_cast<long long *>(prs + PT_R * LDV);  // [NK]
+    long long *roff = koff + NK;                                    // [PT_R]
+    __shared__ int rexp[PT_R];
+    const int b = blockIdx.z, r0 = blockIdx.y * PT_R;
+    const int tid = threadIdx.x, lane = tid % 32, w = tid / 32;
+    for (int x = tid; x < NK + PT_R; x += 256) {
+        if (x < NK) {
+            koff[x] = (x < K) ? v.c.off(x) : -1;
+        } else {
+            const int row = r0 + x - NK;
+            roff[x - NK] = (row < R) ? v.r.off(row) : -1;
+        }
+    }
+    __syncthreads();
+    const double *base = v.p + (long long)b * v.bst;
+    if (rows_fast) {
+        const long long ro = roff[lane];
 #pragma unroll
-        for (int s = 0; s < S; s++) {
-            const float sc = __int_as_float((127 - 7 * s) << 23);    // 2^-7s, exact
-            __nv_bfloat162 w2;
-            w2.x = __float2bfloat16_rn((float)d0[s] * sc);
-            w2.y = __float2bfloat16_rn((float)d1[s] * sc);
-            *reinterpret_cast<__nv_bfloat162 *>(ob + (size_t)s * plane) = w2;
+        for (int i = 0; i < NK / 8; i++) {
+            const int kk = w + 8 * i;
+            const long long ko = koff[kk];
+            val[lane * LDV + kk] = (ro >= 0 && ko >= 0)
+                                       ? (unsigned long long)__double_as_longlong(__ldg(base + ro + ko))
+                                       : 0ull;
+        }
+    } else {
+#pragma unroll
+        for (int i = 0; i < PT_R / 8; i++) {
+            const int rr = w + 8 * i;
+            const long long ro = roff[rr];
+#pragma unroll
+            for (int j = 0; j < KT * 2; j++) {
+                const long long ko = koff[lane + 32 * j];
+                val[rr * LDV + lane + 32 * j] =
+                    (ro >= 0 && ko >= 0)
+                        ? (unsigned long long)__double_as_longlong(__ldg(base + ro + ko))
+                        : 0ull;
+            }
+        }
+    }
+    __syncthreads();
+    // raw exponent of each row: warp w takes rows w, w + 8, ...
+#pragma unroll
+    for (int i = 0; i < PT_R / 8; i++) {
+        const int rr = w + 8 * i;
+        int e = -2000;
+#pragma unroll
+        for (int j = 0; j < KT * 2; j++) {
+            const unsigned long long bits = val[rr * LDV + lane + 32 * j];
+            if ((bits & 0x7FFFFFFFFFFFFFFFull) != 0) e = max(e, (int)((bits >> 52) & 0x7FF) - 1023);
+        }
+        for (int o = 16; o > 0; o >>= 1) e = max(e, __shfl_xor_sync(0xffffffffu, e, o));
+        if (lane == 0) {
+            const int raw = (e > -2000) ? e : (int)0x80808080u;
+            rexp[rr] = raw;
+            if (r0 + rr < R) ex[(long long)b * R + r0 + rr] = raw;
+        }
+    }
+    __syncthreads();
+    const size_t plane = (size_t)R * ld;
+    for (int rr = w; rr < PT_R; rr += 8) {
+        const int row = r0 + rr;
+        if (row >= R) break;
+        const int e = exp_of(rexp[rr]);
+        __nv_bfloat16 *ob = out + (size_t)b * S * plane + (size_t)row * ld;
+#pragma unroll
+        for (int j = 0; j < KT; j++) {
+            const int k = 2 * lane + 64 * j;
+            if (k >= K) break;
+            // the second value is zero beyond K
+            store_digits<S>(ob + k, plane, val[rr * LDV + k], val[rr * LDV + k + 1], e);
         }
     }
 }
@@ -854,6 +994,43 @@ std::string pack_key(const PackView &v, int R, int K, int nb, int S) {
     return b;
 }
 
+template <int S, int KT>
+int launch_pack_rows(kvft_ctx *ctx, const PackView &v, int R, int K, int ld, int nb,
+                     int rows_fast, int rtiles, Packed *out) {
+    constexpr size_t smem = pack_rows_smem(KT);
+    static bool attr = false;
+    if (!attr) {
+        KV_CHECK(ctx, cudaFuncSetAttribute(pack_rows_kernel<S, KT>,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        attr = true;
+    }
+    pack_rows_kernel<S, KT><<<dim3(1, rtiles, nb), 256, smem, ctx->stream>>>(
+        v, R, K, ld, rows_fast, out->ex, out->planes);
+    return kv_launch_check(ctx, "pack_rows");
+}
+
+template <int S>
+int pack_rows_s(kvft_ctx *ctx, const PackView &v, int R, int K, int ld, int nb, int rows_fast,
+                int rtiles, Packed *out) {
+    if (K <= PT_K) return launch_pack_rows<S, 1>(ctx, v, R, K, ld, nb, rows_fast, rtiles, out);
+    if (K <= 2 * PT_K)
+        return launch_pack_rows<S, 2>(ctx, v, R, K, ld, nb, rows_fast, rtiles, out);
+    return launch_pack_rows<S, 4>(ctx, v, R, K, ld, nb, rows_fast, rtiles, out);
+}
+
+int pack_rows(kvft_ctx *ctx, const PackView &v, int R, int K, int ld, int nb, int S,
+              int rows_fast, int rtiles, Packed *out) {
+    switch (S) {
+    case 1: return pack_rows_s<1>(ctx, v, R, K, ld, nb, rows_fast, rtiles, out);
+    case 2: return pack_rows_s<2>(ctx, v, R, K, ld, nb, rows_fast, rtiles, out);
+    case 3: return pack_rows_s<3>(ctx, v, R, K, ld, nb, rows_fast, rtiles, out);
+    case 4: return pack_rows_s<4>(ctx, v, R, K, ld, nb, rows_fast, rtiles, out);
+    case 5: return pack_rows_s<5>(ctx, v, R, K, ld, nb, rows_fast, rtiles, out);
+    case 6: return pack_rows_s<6>(ctx, v, R, K, ld, nb, rows_fast, rtiles, out);
+    default: return kv_fail(ctx, KVFT_EINVAL, "pack: digit count out of range");
+    }
+}
+
 int pack(kvft_ctx *ctx, const char *key, const PackView &v, int R, int K, int nb, int S,
          Packed *out) {
     const int ld = (K + 63) / 64 * 64;
@@ -890,11 +1067,12 @@ int pack(kvft_ctx *ctx, const char *key, const PackView &v, int R, int K, int nb
     out->planes = (__nv_bfloat16 *)buf;
     out->ex = (int *)((uint8_t *)buf + pbytes);
     KvProfScope prof(ctx, KV_CAT_PACK, 8.0 * nb * (double)R * K + (double)nb * S * plane_bytes);
-    KV_CHECK(ctx, cudaMemsetAsync(out->ex, 0x80, (size_t)nb * R * sizeof(int), ctx->stream));
     // coalesce global reads along the contiguous index
     const int rows_fast = (kidx_fast_stride(v.r) == 1 && kidx_fast_stride(v.c) != 1) ? 1 : 0;
     const long long rtiles = (R + PT_R - 1) / PT_R;
     if (rtiles > 65535) return kv_fail(ctx, KVFT_EINVAL, "pack: too many rows");
+    if (K <= PR_KMAX) return pack_rows(ctx, v, R, K, ld, nb, S, rows_fast, (int)rtiles, out);
+    KV_CHECK(ctx, cudaMemsetAsync(out->ex, 0x80, (size_t)nb * R * sizeof(int), ctx->stream));
     const dim3 g((K + PT_K - 1) / PT_K, (unsigned)rtiles, nb);
     // long rows: each exponent block walks up to 16 k tiles, so that about
     // 32 blocks per SM remain and the atomics per row drop accordingly
@@ -947,6 +1125,7 @@ int launch_tc(kvft_ctx *ctx, const CUtensorMap &ma, const CUtensorMap &mb, TcPar
         attr = true;
     }
     const int grid = std::min(p.units, ctx->sm_count);
+    KvProfScope prof(ctx, ctx->gemm_cat, ctx->gemm_work);
     kern<<<grid, NTHREADS, smem, ctx->stream>>>(ma, mb, p);
     return kv_launch_check(ctx, "tc_gemm");
 }
@@ -1074,6 +1253,7 @@ extern "C" int kvft_gemm(kvft_ctx *ctx, int M, int N, int K, int batch, int prec
     KMat a{A, kidx1(M, K), kidx1(K, 1), (long long)M * K};
     KMat b{B, kidx1(K, N), kidx1(N, 1), (long long)K * N};
     KOut c{C, kidx1(M, N), kidx1(N, 1), (long long)M * N};
+    kv_gemm_prof_set(ctx, M, N, K, batch);
     int st;
     if (precision == KVFT_PREC_FP64)
         st = kv_gemm_f64(ctx, M, N, K, batch, 1.0, a, b, 0.0, c);

@@ -76,6 +76,26 @@ def test_tc_gemm_unit_schedules(ctx, M, N, K, batch, digits):
     assert normwise(C, A, B) < TOL[digits]
 
 
+# Short contractions (K <= 256) are packed in one pass that holds whole rows
+# in shared memory: one, two and four 64-wide k tiles, odd K, rows whose
+# contiguous index is K (A) or the row index (B), all-zero rows on both sides.
+# With few terms the rounding errors of the digit products do not average
+# out against the K in the norm-wise bound, so it grows as sqrt(256 / K)
+# (an exact emulation of the digit arithmetic gives 9.1e-5 for K = 16 at
+# three levels).
+@pytest.mark.parametrize("K", [16, 57, 64, 114, 129, 200, 256])
+@pytest.mark.parametrize("digits", [3, 5, 7])
+def test_tc_gemm_short_k(ctx, K, digits):
+    rng = numpy.random.default_rng(K + 1000 * digits)
+    A = rng.standard_normal((3, 333, K)) * numpy.exp(rng.standard_normal((3, 333, 1)) * 4)
+    B = rng.standard_normal((3, K, 517)) * numpy.exp(rng.standard_normal((3, 1, 517)) * 4)
+    A[:, 5, :] = 0.0
+    B[:, :, 7] = 0.0
+    C = gemm(ctx, A, B, _lib.PREC_FP64_TC, digits)
+    assert normwise(C, A, B) < TOL[digits] * max(1.0, (256 / K) ** 0.5)
+    assert not C[:, 5, :].any() and not C[:, :, 7].any()
+
+
 @pytest.mark.parametrize("digits", [2, 3, 4, 5, 6, 7])
 def test_tc_gemm_every_digit_count(ctx, digits):
     """Each digit count is its own kernel instance (levels fixed at compile
