@@ -62,6 +62,13 @@ WORKLOADS = {
                         "ng=10, damping 0.5, econv 1e-10"),
 }
 ITERS_FALLBACK = 30
+# DRAM bytes per launch of the n^6-class contractions (dram__bytes_read.sum +
+# dram__bytes_write.sum), mean over those launches of one ueg114 iteration:
+# 22 launches (three digit levels) and 33 (seven), from the ncu launch lists
+# of `python bench.py --profile-step [--precision fp64_tc]` (one pass per
+# launch, so the full-size workload was captured).  A measured input of the
+# roofline, not computed here: re-take it when the kernel changes.
+NCU_GEMM6_TRAFFIC = {("ueg114", "mixed"): 38.204e9, ("ueg114", "fp64_tc"): 77.330e9}
 REFINE = 2          # refinement sweeps that end a mixed solve
 REFINE_DIGITS = 5   # their digit levels
 STEP_EVENTS = 8     # first event slot of the per-step timings (at most 50 steps)
@@ -377,8 +384,12 @@ def run_gpu(args, w):
         peak, unit, bound = peaks["hbm_gbs"], "GB/s", "hbm"
         psrc = "hbm_gbs of %s peaks" % peak_src
         kernel = dom
+    traffic = NCU_GEMM6_TRAFFIC.get((args.workload, args.precision)) if dom == "gemm6" else None
     roofline = {"bound": bound, "kernel": kernel, "achieved": achieved, "peak": peak,
-                "unit": unit, "frac": achieved / peak, "traffic": None, "launches": nl,
+                "unit": unit, "frac": achieved / peak, "traffic": traffic,
+                "traffic_unit": "bytes per launch (ncu dram__bytes_read.sum + "
+                                "dram__bytes_write.sum)" if traffic else None,
+                "launches": nl,
                 "avg_launch_ms": dms / max(nl, 1), "peak_source": psrc,
                 "breakdown_ms_per_step": {c: round(prof[c][1] / args.steps, 3) for c in prof}}
 

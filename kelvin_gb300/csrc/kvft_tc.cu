@@ -701,39 +701,109 @@ __device__ __forceinline__ void load_tile(const PackView &v, int b, int r0, int 
     }
 }
 
-// raw row exponents: max binary exponent over each row of `ktiles`
-// consecutive 64-wide k tiles, one atomicMax per row and block
-__global__ void __launch_bounds__(256)
-pack_exp_kernel(PackView v, int R, int K, int rows_fast, int ktiles, int *__restrict__ ex) {
-    __shared__ PackTile tile;
-    const int b = blockIdx.z, r0 = blockIdx.y * PT_R;
+// Register-prefetch form of the same tile walk: offsets of tile rows r0.. and
+// k columns k0.. in a shared table (threads 0-95), then each thread's 8
+// values -- row lane at k = w + 8 i (rows_fast), else rows w + 8 i at k = lane,
+// lane + 32 -- loaded into registers, so a block can have the next tile's
+// loads in flight while it works on the current one.
+__device__ __forceinline__ void tile_offsets(const PackView &v, int r0, int k0, int R, int K,
+                                             long long *off) {
+    const int tid = threadIdx.x;
+    if (tid < PT_R) {
+        off[tid] = (r0 + tid < R) ? v.r.off(r0 + tid) : -1;
+    } else if (tid < PT_R + PT_K) {
+        const int k = k0 + tid - PT_R;
+        off[tid] = (k < K) ? v.c.off(k) : -1;
+    }
+}
+
+__device__ __forceinline__ void tile_fetch(const double *base, const long long *off,
+                                           int rows_fast, unsigned long long (&pre)[8]) {
     const int lane = threadIdx.x % 32, w = threadIdx.x / 32;
-    int emax[PT_R / 8];
+    if (rows_fast) {
+        const long long ro = off[lane];
 #pragma unroll
-    for (int i = 0; i < PT_R / 8; i++) emax[i] = -2000;
-    for (int t = 0; t < ktiles; t++) {
-        const int k0 = (blockIdx.x * ktiles + t) * PT_K;
-        if (k0 >= K) break;
-        // the barrier inside load_tile orders these tile writes after the
-        // previous tile's reads
-        load_tile(v, b, r0, k0, R, K, rows_fast, tile);
-        __syncthreads();
+        for (int i = 0; i < 8; i++) {
+            const long long ko = off[PT_R + w + 8 * i];
+            pre[i] = (ro >= 0 && ko >= 0)
+                         ? (unsigned long long)__double_as_longlong(__ldg(base + ro + ko))
+                         : 0ull;
+        }
+    } else {
+        const long long ko0 = off[PT_R + lane], ko1 = off[PT_R + lane + 32];
 #pragma unroll
-        for (int i = 0; i < PT_R / 8; i++) {
-            const int rr = w + 8 * i;
-            for (int h = 0; h < 2; h++) {
-                const unsigned long long bits = tile.v[rr][lane + 32 * h];
-                if ((bits & 0x7FFFFFFFFFFFFFFFull) != 0)
-                    emax[i] = max(emax[i], (int)((bits >> 52) & 0x7FF) - 1023);
-            }
+        for (int i = 0; i < 4; i++) {
+            const long long ro = off[w + 8 * i];
+            pre[2 * i] = (ro >= 0 && ko0 >= 0)
+                             ? (unsigned long long)__double_as_longlong(__ldg(base + ro + ko0))
+                             : 0ull;
+            pre[2 * i + 1] = (ro >= 0 && ko1 >= 0)
+                                 ? (unsigned long long)__double_as_longlong(__ldg(base + ro + ko1))
+                                 : 0ull;
         }
     }
+}
+
+__device__ __forceinline__ int raw_exp(unsigned long long bits) {
+    return (bits & 0x7FFFFFFFFFFFFFFFull) ? (int)((bits >> 52) & 0x7FF) - 1023 : -2000;
+}
+
+// raw row exponents: max binary exponent over each row of `ktiles`
+// consecutive 64-wide k tiles, one atomicMax per row and block.  The maxima
+// are taken in registers from each thread's 8 values, and the next tile's
+// loads are issued before the current tile's values are used.
+__global__ void __launch_bounds__(256)
+pack_exp_kernel(PackView v, int R, int K, int rows_fast, int ktiles, int *__restrict__ ex) {
+    __shared__ long long off[PT_R + PT_K];
+    __shared__ int rmax[8][PT_R];
+    const int b = blockIdx.z, r0 = blockIdx.y * PT_R;
+    const int lane = threadIdx.x % 32, w = threadIdx.x / 32;
+    const double *base = v.p + (long long)b * v.bst;
+    const int kt0 = blockIdx.x * ktiles;
+    const int nkt = min(ktiles, (K + PT_K - 1) / PT_K - kt0);
+    // rows_fast: one row per thread (lane); otherwise four rows (w + 8 i)
+    int em[4] = {-2000, -2000, -2000, -2000};
+    unsigned long long pre[8];
+    tile_offsets(v, r0, kt0 * PT_K, R, K, off);
+    __syncthreads();
+    tile_fetch(base, off, rows_fast, pre);
+    for (int t = 0; t < nkt; t++) {
+        unsigned long long cur[8];
 #pragma unroll
-    for (int i = 0; i < PT_R / 8; i++) {
-        int e = emax[i];
-        for (int o = 16; o > 0; o >>= 1) e = max(e, __shfl_xor_sync(0xffffffffu, e, o));
-        const int row = r0 + w + 8 * i;
-        if (lane == 0 && e > -2000 && row < R) atomicMax(&ex[(long long)b * R + row], e);
+        for (int i = 0; i < 8; i++) cur[i] = pre[i];
+        if (t + 1 < nkt) {
+            __syncthreads();                    // every thread has read the offsets
+            tile_offsets(v, r0, (kt0 + t + 1) * PT_K, R, K, off);
+            __syncthreads();
+            tile_fetch(base, off, rows_fast, pre);
+        }
+        if (rows_fast) {
+#pragma unroll
+            for (int i = 0; i < 8; i++) em[0] = max(em[0], raw_exp(cur[i]));
+        } else {
+#pragma unroll
+            for (int i = 0; i < 4; i++)
+                em[i] = max(em[i], max(raw_exp(cur[2 * i]), raw_exp(cur[2 * i + 1])));
+        }
+    }
+    if (rows_fast) {
+        // row lane: combine the eight warps' maxima
+        rmax[w][lane] = em[0];
+        __syncthreads();
+        if (w == 0) {
+            int e = rmax[0][lane];
+#pragma unroll
+            for (int q = 1; q < 8; q++) e = max(e, rmax[q][lane]);
+            if (e > -2000 && r0 + lane < R) atomicMax(&ex[(long long)b * R + r0 + lane], e);
+        }
+    } else {
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            int e = em[i];
+            for (int o = 16; o > 0; o >>= 1) e = max(e, __shfl_xor_sync(0xffffffffu, e, o));
+            const int row = r0 + w + 8 * i;
+            if (lane == 0 && e > -2000 && row < R) atomicMax(&ex[(long long)b * R + row], e);
+        }
     }
 }
 
@@ -820,26 +890,66 @@ __device__ __forceinline__ void store_digits(__nv_bfloat16 *ob, size_t plane,
     if (S > 5) *reinterpret_cast<__nv_bfloat162 *>(ob + 5 * plane) = digit_pair<5>(d0[5], d1[5]);
 }
 
-// planes[b][s][row][k] (row stride ld) = d_s 2^-7s; each thread packs two k
+// planes[b][s][row][k] (row stride ld) = d_s 2^-7s; each thread packs two k.
+// Persistent blocks walk the 32 x 64 tiles t = blockIdx.x, + gridDim.x, ...
+// (k tile fastest, then row tile, then batch); the next tile's loads are in
+// flight in registers while the current one is converted.
 template <int S>
 __global__ void __launch_bounds__(256)
-pack_digits_kernel(PackView v, int R, int K, int ld, int rows_fast, const int *__restrict__ ex,
-                   __nv_bfloat16 *__restrict__ out) {
-    __shared__ PackTile tile;
-    const int b = blockIdx.z, r0 = blockIdx.y * PT_R, k0 = blockIdx.x * PT_K;
-    load_tile(v, b, r0, k0, R, K, rows_fast, tile);
-    __syncthreads();
+pack_digits_kernel(PackView v, int R, int K, int ld, int rows_fast, int ktn, int rtn,
+                   int ntiles, const int *__restrict__ ex, __nv_bfloat16 *__restrict__ out) {
+    __shared__ unsigned long long val[PT_R][PT_K + 1];
+    __shared__ long long off[PT_R + PT_K];
+    const int lane = threadIdx.x % 32, w = threadIdx.x / 32;
     const size_t plane = (size_t)R * ld;
-    const int tx = threadIdx.x % 32, ty = threadIdx.x / 32;
-    const int k = k0 + 2 * tx;
-    if (k >= K) return;
-    for (int rr = ty; rr < PT_R; rr += 8) {
-        const int row = r0 + rr;
-        if (row >= R) break;
-        const int e = exp_of(ex[(long long)b * R + row]);
-        // the second value is zero beyond K (tile fill)
-        store_digits<S>(out + (size_t)b * S * plane + (size_t)row * ld + k, plane,
-                        tile.v[rr][2 * tx], tile.v[rr][2 * tx + 1], e);
+    auto decode = [&](int t, int &b, int &r0, int &k0) {
+        b = t / (rtn * ktn);
+        const int rem = t - b * rtn * ktn;
+        r0 = (rem / ktn) * PT_R;
+        k0 = (rem % ktn) * PT_K;
+    };
+    unsigned long long pre[8];
+    int t = blockIdx.x;
+    if (t < ntiles) {
+        int b, r0, k0;
+        decode(t, b, r0, k0);
+        tile_offsets(v, r0, k0, R, K, off);
+        __syncthreads();
+        tile_fetch(v.p + (long long)b * v.bst, off, rows_fast, pre);
+    }
+    for (; t < ntiles; t += gridDim.x) {
+        const long long tn = (long long)t + gridDim.x;
+        int b, r0, k0;
+        decode(t, b, r0, k0);
+        __syncthreads();              // val and the offsets are free again
+        if (rows_fast) {
+#pragma unroll
+            for (int i = 0; i < 8; i++) val[lane][w + 8 * i] = pre[i];
+        } else {
+#pragma unroll
+            for (int i = 0; i < 4; i++) {
+                val[w + 8 * i][lane] = pre[2 * i];
+                val[w + 8 * i][lane + 32] = pre[2 * i + 1];
+            }
+        }
+        int bn = 0, rn = 0, kn = 0;
+        if (tn < ntiles) {
+            decode((int)tn, bn, rn, kn);
+            tile_offsets(v, rn, kn, R, K, off);
+        }
+        __syncthreads();
+        if (tn < ntiles) tile_fetch(v.p + (long long)bn * v.bst, off, rows_fast, pre);
+        const int k = k0 + 2 * lane;
+        if (k < K) {
+            for (int rr = w; rr < PT_R; rr += 8) {
+                const int row = r0 + rr;
+                if (row >= R) break;
+                const int e = exp_of(ex[(long long)b * R + row]);
+                // the second value is zero beyond K (tile fill)
+                store_digits<S>(out + (size_t)b * S * plane + (size_t)row * ld + k, plane,
+                                val[rr][2 * lane], val[rr][2 * lane + 1], e);
+            }
+        }
     }
 }
 
@@ -847,90 +957,107 @@ pack_digits_kernel(PackView v, int R, int K, int ld, int rows_fast, const int *_
 // memory, takes each row's exponent from there and writes its digits, so the
 // operand is read once and no atomics are needed.  The raw exponents it
 // stores are those of the two-pass path (0x80808080 for an all-zero row).
+// Blocks are persistent: they walk the row tiles t = blockIdx.x, + gridDim.x,
+// ... (batch-major), and while one tile is converted from shared memory the
+// global loads of the block's next tile are already in flight into
+// registers.
 constexpr int PR_KMAX = 256;
 
 __host__ __device__ constexpr size_t pack_rows_smem(int kt) {
-    return (size_t)PT_R * (kt * PT_K + 1) * 8 + (size_t)(kt * PT_K + PT_R) * 8;
+    return (size_t)PT_R * (kt * PT_K + 1) * 8 + (size_t)(kt * PT_K) * 8;
 }
 
 template <int S, int KT>
-__global__ void __launch_bounds__(256)
-pack_rows_kernel(PackView v, int R, int K, int ld, int rows_fast, int *__restrict__ ex,
-                 __nv_bfloat16 *__restrict__ out) {
-    constexpr int NK = KT * PT_K, LDV = NK + 1;
+__global__ void __launch_bounds__(256, 2)
+pack_rows_kernel(PackView v, int R, int K, int ld, int rows_fast, int rtiles, int ntiles,
+                 int *__restrict__ ex, __nv_bfloat16 *__restrict__ out) {
+    constexpr int NK = KT * PT_K, LDV = NK + 1, PER = NK / 8;   // values per thread
     extern __shared__ unsigned long long prs[];
-    unsigned long long *val = prs;                                  // [PT_R][LDV]
+    unsigned long long *val = prs;                                      // [PT_R][LDV]
     long long *koff = reinterpret_cast<long long *>(prs + PT_R * LDV);  // [NK]
-    long long *roff = koff + NK;                                    // [PT_R]
     __shared__ int rexp[PT_R];
-    const int b = blockIdx.z, r0 = blockIdx.y * PT_R;
     const int tid = threadIdx.x, lane = tid % 32, w = tid / 32;
-    for (int x = tid; x < NK + PT_R; x += 256) {
-        if (x < NK) {
-            koff[x] = (x < K) ? v.c.off(x) : -1;
-        } else {
-            const int row = r0 + x - NK;
-            roff[x - NK] = (row < R) ? v.r.off(row) : -1;
-        }
-    }
+    for (int x = tid; x < NK; x += 256) koff[x] = (x < K) ? v.c.off(x) : -1;
     __syncthreads();
-    const double *base = v.p + (long long)b * v.bst;
-    if (rows_fast) {
-        const long long ro = roff[lane];
+    // rows_fast: thread (lane, w) reads row lane at k = w + 8 i; otherwise rows
+    // w + 8 i at k = lane + 32 j.  Both cover 32 x NK values, PER per thread.
+    unsigned long long pre[PER];
+    auto fetch = [&](int t) {
+        const int b = t / rtiles, r0 = (t - b * rtiles) * PT_R;
+        const double *base = v.p + (long long)b * v.bst;
+        if (rows_fast) {
+            const long long ro = (r0 + lane < R) ? v.r.off(r0 + lane) : -1;
 #pragma unroll
-        for (int i = 0; i < NK / 8; i++) {
-            const int kk = w + 8 * i;
-            const long long ko = koff[kk];
-            val[lane * LDV + kk] = (ro >= 0 && ko >= 0)
-                                       ? (unsigned long long)__double_as_longlong(__ldg(base + ro + ko))
-                                       : 0ull;
+            for (int i = 0; i < PER; i++) {
+                const long long ko = koff[w + 8 * i];
+                pre[i] = (ro >= 0 && ko >= 0)
+                             ? (unsigned long long)__double_as_longlong(__ldg(base + ro + ko))
+                             : 0ull;
+            }
+        } else {
+#pragma unroll
+            for (int i = 0; i < PT_R / 8; i++) {
+                const int row = r0 + w + 8 * i;
+                const long long ro = (row < R) ? v.r.off(row) : -1;
+#pragma unroll
+                for (int j = 0; j < 2 * KT; j++) {
+                    const long long ko = koff[lane + 32 * j];
+                    pre[i * 2 * KT + j] =
+                        (ro >= 0 && ko >= 0)
+                            ? (unsigned long long)__double_as_longlong(__ldg(base + ro + ko))
+                            : 0ull;
+                }
+            }
         }
-    } else {
+    };
+    if (blockIdx.x < ntiles) fetch(blockIdx.x);
+    const size_t plane = (size_t)R * ld;
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        __syncthreads();                      // the previous tile's values are used up
+        if (rows_fast) {
+#pragma unroll
+            for (int i = 0; i < PER; i++) val[lane * LDV + w + 8 * i] = pre[i];
+        } else {
+#pragma unroll
+            for (int i = 0; i < PT_R / 8; i++)
+#pragma unroll
+                for (int j = 0; j < 2 * KT; j++)
+                    val[(w + 8 * i) * LDV + lane + 32 * j] = pre[i * 2 * KT + j];
+        }
+        __syncthreads();
+        if ((long long)t + gridDim.x < ntiles) fetch(t + gridDim.x);
+        const int b = t / rtiles, r0 = (t - b * rtiles) * PT_R;
+        // raw exponent of each row: warp w takes rows w, w + 8, ...
 #pragma unroll
         for (int i = 0; i < PT_R / 8; i++) {
             const int rr = w + 8 * i;
-            const long long ro = roff[rr];
+            int e = -2000;
 #pragma unroll
             for (int j = 0; j < KT * 2; j++) {
-                const long long ko = koff[lane + 32 * j];
-                val[rr * LDV + lane + 32 * j] =
-                    (ro >= 0 && ko >= 0)
-                        ? (unsigned long long)__double_as_longlong(__ldg(base + ro + ko))
-                        : 0ull;
+                const unsigned long long bits = val[rr * LDV + lane + 32 * j];
+                if ((bits & 0x7FFFFFFFFFFFFFFFull) != 0)
+                    e = max(e, (int)((bits >> 52) & 0x7FF) - 1023);
+            }
+            for (int o = 16; o > 0; o >>= 1) e = max(e, __shfl_xor_sync(0xffffffffu, e, o));
+            if (lane == 0) {
+                const int raw = (e > -2000) ? e : (int)0x80808080u;
+                rexp[rr] = raw;
+                if (r0 + rr < R) ex[(long long)b * R + r0 + rr] = raw;
             }
         }
-    }
-    __syncthreads();
-    // raw exponent of each row: warp w takes rows w, w + 8, ...
+        __syncthreads();
+        for (int rr = w; rr < PT_R; rr += 8) {
+            const int row = r0 + rr;
+            if (row >= R) break;
+            const int e = exp_of(rexp[rr]);
+            __nv_bfloat16 *ob = out + (size_t)b * S * plane + (size_t)row * ld;
 #pragma unroll
-    for (int i = 0; i < PT_R / 8; i++) {
-        const int rr = w + 8 * i;
-        int e = -2000;
-#pragma unroll
-        for (int j = 0; j < KT * 2; j++) {
-            const unsigned long long bits = val[rr * LDV + lane + 32 * j];
-            if ((bits & 0x7FFFFFFFFFFFFFFFull) != 0) e = max(e, (int)((bits >> 52) & 0x7FF) - 1023);
-        }
-        for (int o = 16; o > 0; o >>= 1) e = max(e, __shfl_xor_sync(0xffffffffu, e, o));
-        if (lane == 0) {
-            const int raw = (e > -2000) ? e : (int)0x80808080u;
-            rexp[rr] = raw;
-            if (r0 + rr < R) ex[(long long)b * R + r0 + rr] = raw;
-        }
-    }
-    __syncthreads();
-    const size_t plane = (size_t)R * ld;
-    for (int rr = w; rr < PT_R; rr += 8) {
-        const int row = r0 + rr;
-        if (row >= R) break;
-        const int e = exp_of(rexp[rr]);
-        __nv_bfloat16 *ob = out + (size_t)b * S * plane + (size_t)row * ld;
-#pragma unroll
-        for (int j = 0; j < KT; j++) {
-            const int k = 2 * lane + 64 * j;
-            if (k >= K) break;
-            // the second value is zero beyond K
-            store_digits<S>(ob + k, plane, val[rr * LDV + k], val[rr * LDV + k + 1], e);
+            for (int j = 0; j < KT; j++) {
+                const int k = 2 * lane + 64 * j;
+                if (k >= K) break;
+                // the second value is zero beyond K
+                store_digits<S>(ob + k, plane, val[rr * LDV + k], val[rr * LDV + k + 1], e);
+            }
         }
     }
 }
@@ -994,18 +1121,39 @@ std::string pack_key(const PackView &v, int R, int K, int nb, int S) {
     return b;
 }
 
+// persistent digit pass: as many blocks as fit on the SMs at once
+template <int S>
+int launch_pack_digits(kvft_ctx *ctx, const PackView &v, int R, int K, int ld, int rows_fast,
+                       int ktn, int rtn, long long tiles, Packed *out) {
+    static int per_sm = 0;
+    if (!per_sm) {
+        KV_CHECK(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                          &per_sm, pack_digits_kernel<S>, 256, 0));
+        per_sm = std::max(per_sm, 1);
+    }
+    const int grid = (int)std::min(tiles, (long long)per_sm * ctx->sm_count);
+    pack_digits_kernel<S><<<grid, 256, 0, ctx->stream>>>(v, R, K, ld, rows_fast, ktn, rtn,
+                                                        (int)tiles, out->ex, out->planes);
+    return KVFT_OK;
+}
+
 template <int S, int KT>
 int launch_pack_rows(kvft_ctx *ctx, const PackView &v, int R, int K, int ld, int nb,
                      int rows_fast, int rtiles, Packed *out) {
     constexpr size_t smem = pack_rows_smem(KT);
-    static bool attr = false;
-    if (!attr) {
+    static int per_sm = 0;
+    if (!per_sm) {
         KV_CHECK(ctx, cudaFuncSetAttribute(pack_rows_kernel<S, KT>,
                                            cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        attr = true;
+        KV_CHECK(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                          &per_sm, pack_rows_kernel<S, KT>, 256, smem));
+        per_sm = std::max(per_sm, 1);
     }
-    pack_rows_kernel<S, KT><<<dim3(1, rtiles, nb), 256, smem, ctx->stream>>>(
-        v, R, K, ld, rows_fast, out->ex, out->planes);
+    const long long ntiles = (long long)rtiles * nb;
+    if (ntiles > 0x7FFFFFFFLL) return kv_fail(ctx, KVFT_EINVAL, "pack: too many row tiles");
+    const int grid = (int)std::min(ntiles, (long long)per_sm * ctx->sm_count);
+    pack_rows_kernel<S, KT><<<grid, 256, smem, ctx->stream>>>(
+        v, R, K, ld, rows_fast, rtiles, (int)ntiles, out->ex, out->planes);
     return kv_launch_check(ctx, "pack_rows");
 }
 
@@ -1081,11 +1229,11 @@ int pack(kvft_ctx *ctx, const char *key, const PackView &v, int R, int K, int nb
     const dim3 ge((g.x + ktiles - 1) / ktiles, g.y, g.z);
     pack_exp_kernel<<<ge, 256, 0, ctx->stream>>>(v, R, K, rows_fast, ktiles, out->ex);
     KV_TRY(kv_launch_check(ctx, "pack_exp"));
+    if (tiles > 0x7FFFFFFFLL) return kv_fail(ctx, KVFT_EINVAL, "pack: too many tiles");
     switch (S) {
-#define KV_PACK_CASE(s_)                                                                    \
-    case s_:                                                                                \
-        pack_digits_kernel<s_><<<g, 256, 0, ctx->stream>>>(v, R, K, ld, rows_fast, out->ex, \
-                                                           out->planes);                    \
+#define KV_PACK_CASE(s_)                                                                   \
+    case s_:                                                                               \
+        KV_TRY(launch_pack_digits<s_>(ctx, v, R, K, ld, rows_fast, g.x, g.y, tiles, out)); \
         break;
         KV_PACK_CASE(1) KV_PACK_CASE(2) KV_PACK_CASE(3) KV_PACK_CASE(4) KV_PACK_CASE(5)
         KV_PACK_CASE(6)
