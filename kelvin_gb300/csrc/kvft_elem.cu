@@ -141,11 +141,13 @@ wmbej_tmp_kernel(int nv, int no, const double *__restrict__ t1, const double *__
 // fire-and-forget reduction at L2 (one rounding, like load-add-store); the
 // additions then cost the SM's scarce FP64 pipe nothing.
 // FS: fac is +1 (1), -1 (2) or anything else (0); the signs cost no FP64
-// operation.
-template <int FS>
+// operation.  SEED: T2 = -seed + R is stored (every a != b element once), no
+// reduction and no pre-seeded T2.
+template <int FS, bool SEED>
 __global__ void __launch_bounds__(256)
 assemble_t2_kernel(int nv, int no, double fac, const double *__restrict__ Z,
-                   const double *__restrict__ Lc, double *__restrict__ T2) {
+                   const double *__restrict__ Lc, const double *__restrict__ seed,
+                   double *__restrict__ T2) {
     __shared__ double qa[32][33], qb[32][33];
     const int tx = threadIdx.x % 32, ty = threadIdx.x / 32;
     const int nt = (no + 31) / 32;
@@ -180,6 +182,16 @@ assemble_t2_kernel(int nv, int no, double fac, const double *__restrict__ Z,
             if (!L || i == j) return 0.0;
             return i < j ? L[pair_start(i, no) + j - i - 1] : -L[pair_start(j, no) + i - j - 1];
         };
+        const long long sab = ((long long)a * nv + b) * oo, sba = ((long long)b * nv + a) * oo;
+        auto put = [&](int x, double R) {
+            if (SEED) {
+                T2[oab + x] = R - seed[sab + x];
+                T2[oba + x] = -R - seed[sba + x];
+            } else {
+                atomicAdd(T2 + oab + x, R);
+                atomicAdd(T2 + oba + x, -R);
+            }
+        };
 #pragma unroll
         for (int k = 0; k < 4; k++) {
             const int r = ty + 8 * k;
@@ -187,16 +199,14 @@ assemble_t2_kernel(int nv, int no, double fac, const double *__restrict__ Z,
             if (i < no && j < no) {
                 const double R0 = qa[r][tx] - qb[tx][r] + ladder(i, j);
                 const double R = FS == 0 ? fac * R0 : (FS == 1 ? R0 : -R0);
-                atomicAdd(T2 + oab + i * no + j, R);
-                atomicAdd(T2 + oba + i * no + j, -R);
+                put(i * no + j, R);
             }
             i = j0 + r;
             j = i0 + tx;
             if (it != jt && i < no && j < no) {
                 const double R0 = qb[r][tx] - qa[tx][r] + ladder(i, j);
                 const double R = FS == 0 ? fac * R0 : (FS == 1 ? R0 : -R0);
-                atomicAdd(T2 + oab + i * no + j, R);
-                atomicAdd(T2 + oba + i * no + j, -R);
+                put(i * no + j, R);
             }
         }
     }
@@ -321,20 +331,34 @@ int kv_make_wmbej_tmp(kvft_ctx *ctx, int batch, int nv, int no,
 }
 
 int kv_assemble_t2(kvft_ctx *ctx, int batch, int nv, int no, double fac, const double *Z,
-                   const double *Lc, double *T2) {
-    const long long total = (long long)batch * nv * nv * no * no;
-    if (total == 0 || nv < 2) return KVFT_OK;
+                   const double *Lc, double *T2, const double *seed) {
+    const long long oo = (long long)no * no, total = (long long)batch * nv * nv * oo;
+    if (total == 0) return KVFT_OK;
+    if (seed) {
+        // the a = b blocks get the seed alone: T2[y][a][a] = -seed[a][a]
+        const int d[4] = {nv, no, no, 1};
+        const long long sd[4] = {(nv + 1) * oo, no, 1, 0};
+        KV_TRY(kv_axpby4(ctx, batch, d, -1.0, seed, sd, 0, 0.0, T2, sd, nv * nv * oo));
+    }
+    if (nv < 2) return KVFT_OK;
     if (batch > 65535) return kv_fail(ctx, KVFT_EINVAL, "assemble_t2: batch too large");
     KvProfScope prof(ctx, KV_CAT_ELEM, 8.0 * total * (Lc ? 3.25 : 3.0));
     const int nt = (no + 31) / 32;
     const int pv = nv * (nv - 1) / 2;
     const dim3 grid(nt * (nt + 1) / 2, std::min(pv, 65535), batch);
-    if (fac == 1.0)
-        assemble_t2_kernel<1><<<grid, 256, 0, ctx->stream>>>(nv, no, fac, Z, Lc, T2);
-    else if (fac == -1.0)
-        assemble_t2_kernel<2><<<grid, 256, 0, ctx->stream>>>(nv, no, fac, Z, Lc, T2);
-    else
-        assemble_t2_kernel<0><<<grid, 256, 0, ctx->stream>>>(nv, no, fac, Z, Lc, T2);
+#define KV_ASM(fs_, seed_)                                                                  \
+    assemble_t2_kernel<fs_, seed_><<<grid, 256, 0, ctx->stream>>>(nv, no, fac, Z, Lc, seed, T2)
+    const int fs = fac == 1.0 ? 1 : (fac == -1.0 ? 2 : 0);
+    if (seed) {
+        if (fs == 1) KV_ASM(1, true);
+        else if (fs == 2) KV_ASM(2, true);
+        else KV_ASM(0, true);
+    } else {
+        if (fs == 1) KV_ASM(1, false);
+        else if (fs == 2) KV_ASM(2, false);
+        else KV_ASM(0, false);
+    }
+#undef KV_ASM
     return kv_launch_check(ctx, "assemble_t2");
 }
 

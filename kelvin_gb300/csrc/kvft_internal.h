@@ -170,9 +170,11 @@ int kv_make_tau(kvft_ctx *ctx, int batch, int nv, int no, const double *t1,
 int kv_make_wmbej_tmp(kvft_ctx *ctx, int batch, int nv, int no,
                       const double *t1, const double *t2, double *out);
 // T2 += fac (1 - P(ab))(1 - P(ij)) (Z + L), L = the ladder sum stored over
-// a < b, i < j (Lc, or nullptr), zero elsewhere
+// a < b, i < j (Lc, or nullptr), zero elsewhere.  With a seed (a
+// tau-independent [a][b][i][j] block) T2 is written, not updated:
+// T2 = -seed + fac (...).
 int kv_assemble_t2(kvft_ctx *ctx, int batch, int nv, int no, double fac, const double *Z,
-                   const double *Lc, double *T2);
+                   const double *Lc, double *T2, const double *seed = nullptr);
 // Antisymmetric pair compression (pairs p < q, x = p(2n-p-1)/2 + q-p-1):
 // tau_c[y][(e<f)][(i<j)] from t1, t2
 int kv_make_tau_pairs(kvft_ctx *ctx, int batch, int nv, int no, const double *t1,
@@ -194,9 +196,11 @@ int kv_energy(kvft_ctx *ctx, int ng, int nv, int no, const double *T1,
               const double *T2, const double *f, const double *eri,
               const double *g, double beta, int qterm, double *dres);
 
+// T1/T2 += fac * residual; with seed_t2, T2 = -seed_t2 + fac * residual
+// (T2 need not be initialised).
 int kv_stanton(kvft_ctx *ctx, int nb, int nv, int no,
                const double *const F[4], const double *const I[9],
                const double *t1, const double *t2, double fac, double *T1,
-               double *T2);
+               double *T2, const double *seed_t2 = nullptr);
 size_t kv_stanton_workspace(int nb, int nv, int no);
 size_t kv_chunk_bytes_per_tau(kvft_ctx *ctx, int nv, int no);

@@ -254,8 +254,8 @@ int form_tbar(kvft_solver *s) {
     kvft_ctx *ctx = s->ctx;
     if (s->chunk_prec != ctx->precision * 16 + ctx->digits) KV_TRY(pick_chunk(s));
     const long long n1 = s->s1(), n2 = s->s2();
+    // the T2 seed -I.vvoo is written by the residual's final assembly
     KV_TRY(seed_neg(ctx, s->ng, n1, s->F[2], s->T1b));
-    KV_TRY(seed_neg(ctx, s->ng, n2, s->I[3], s->T2b));
     const double *Fc[4] = {s->F[0], s->F[1], s->F[2], s->F[3]};
     const double *Ic[9];
     for (int k = 0; k < 9; k++) Ic[k] = s->I[k];
@@ -263,7 +263,7 @@ int form_tbar(kvft_solver *s) {
     for (int y0 = 0; y0 < s->ng; y0 += s->chunk) {
         int nb = std::min(s->chunk, s->ng - y0);
         KV_TRY(kv_stanton(ctx, nb, s->nv, s->no, Fc, Ic, s->T1 + y0 * n1, s->T2 + y0 * n2, -1.0,
-                          s->T1b + y0 * n1, s->T2b + y0 * n2));
+                          s->T1b + y0 * n1, s->T2b + y0 * n2, s->I[3]));
     }
     return KVFT_OK;
 }
@@ -547,10 +547,10 @@ int kvft_solver_run_point(kvft_solver *s, const kvft_solve_opts *o, kvft_result 
         int i = 0;
         while (i < o->max_iter && !conv) {
             KV_TRY(seed_neg(ctx, 1, n1, s->F[2], t1b));
-            KV_TRY(seed_neg(ctx, 1, n2, s->I[3], t2b));
             {
                 KvPackCacheScope cache(ctx);
-                KV_TRY(kv_stanton(ctx, 1, s->nv, s->no, Fc, Ic, T1g, T2g, -1.0, t1b, t2b));
+                KV_TRY(kv_stanton(ctx, 1, s->nv, s->no, Fc, Ic, T1g, T2g, -1.0, t1b, t2b,
+                                  s->I[3]));
             }
             KV_TRY(kv_quad_single(ctx, ng, ig, n1, 1, s->nv, s->no, s->T1b, s->ti, s->G, s->D1,
                                   s->eps, s->eps, u1));
@@ -649,7 +649,6 @@ int kvft_ccsd_stanton(kvft_ctx *ctx, int ng, int nv, int no, const double *const
     KV_TRY(kv_scratch(ctx, "stanton_tbar", sizeof(double) * ng * (s1 + s2), &tb));
     double *T1b = (double *)tb, *T2b = T1b + ng * s1;
     KV_TRY(seed_neg(ctx, ng, s1, F[2], T1b));
-    KV_TRY(seed_neg(ctx, ng, s2, I[3], T2b));
     size_t fr = 0, tot = 0;
     KV_CHECK(ctx, cudaMemGetInfo(&fr, &tot));
     size_t held = 0;
@@ -660,7 +659,7 @@ int kvft_ccsd_stanton(kvft_ctx *ctx, int ng, int nv, int no, const double *const
     for (int y0 = 0; y0 < ng; y0 += chunk) {
         int nb = std::min(chunk, ng - y0);
         KV_TRY(kv_stanton(ctx, nb, nv, no, F, I, T1old + y0 * s1, T2old + y0 * s2, -1.0,
-                          T1b + y0 * s1, T2b + y0 * s2));
+                          T1b + y0 * s1, T2b + y0 * s2, I[3]));
     }
     KV_TRY(kvft_int_tbar1(ctx, ng, nv, no, T1b, ti, D1, G, full, T1new));
     return kvft_int_tbar2(ctx, ng, nv, no, T2b, ti, D2, G, full, T2new);

@@ -96,7 +96,7 @@ size_t kv_chunk_bytes_per_tau(kvft_ctx *ctx, int nv, int no) {
 
 int kv_stanton(kvft_ctx *ctx, int nb, int nv, int no, const double *const F[4],
                const double *const I[9], const double *t1, const double *t2,
-               double fac, double *T1, double *T2) {
+               double fac, double *T1, double *T2, const double *seed_t2) {
     if (nb <= 0) return KVFT_OK;
     const long long v = nv, o = no;
     const long long vo = v * o, oo = o * o, vv = v * v;
@@ -317,7 +317,7 @@ int kv_stanton(kvft_ctx *ctx, int nb, int nv, int no, const double *const F[4],
                    MO(w.Z, X3(nv, vo2, nv, oo, no, 1), X1(no, o), v2o2)));
 
     // ---- T2 += fac (1 - P(ab))(1 - P(ij)) (Z + ladders) -------------------------
-    return kv_assemble_t2(ctx, B, nv, no, fac, w.Z, ladders ? w.Lc : nullptr, T2);
+    return kv_assemble_t2(ctx, B, nv, no, fac, w.Z, ladders ? w.Lc : nullptr, T2, seed_t2);
 }
 
 extern "C" int kvft_stanton_residual(kvft_ctx *ctx, int nb, int nv, int no,
