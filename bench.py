@@ -68,7 +68,7 @@ ITERS_FALLBACK = 30
 # of `python bench.py --profile-step [--precision fp64_tc]` (one pass per
 # launch, so the full-size workload was captured).  A measured input of the
 # roofline, not computed here: re-take it when the kernel changes.
-NCU_GEMM6_TRAFFIC = {("ueg114", "mixed"): 38.204e9, ("ueg114", "fp64_tc"): 77.330e9}
+NCU_GEMM6_TRAFFIC = {("ueg114", "mixed"): 36.839e9, ("ueg114", "fp64_tc"): 77.673e9}
 REFINE = 2          # refinement sweeps that end a mixed solve
 REFINE_DIGITS = 5   # their digit levels
 STEP_EVENTS = 8     # first event slot of the per-step timings (at most 50 steps)
