@@ -235,6 +235,16 @@ int kvft_solver_set_amplitudes(kvft_solver *s, const double *T1_host,
                                const double *T2_host);
 /* Device pointers of the solver's resident amplitudes (T1, T2). */
 int kvft_solver_device_amplitudes(kvft_solver *s, double **T1, double **T2);
+/* Spin blocks.  When n is even and every integral block vanishes outside the
+ * spin-conserving blocks with the alpha spin orbitals first (the general-spin
+ * ordering of the UEG and Hubbard systems), the solver finds this at creation
+ * and runs the n^6 contractions over the 10 nonzero spin-block products of
+ * 64.  on = 0 turns that off, 1 back on, -1 leaves it; *half (may be NULL)
+ * receives the alpha-half size in use (0: off).  Amplitudes given through
+ * kvft_solver_set_amplitudes that do not conserve spin turn it off; writes
+ * through kvft_solver_device_amplitudes are the caller's to keep
+ * spin-conserving. */
+int kvft_solver_set_spin_blocks(kvft_solver *s, int on, int *half);
 size_t kvft_solver_footprint(int n, int ng, int precision);
 
 #ifdef __cplusplus

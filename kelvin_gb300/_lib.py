@@ -122,6 +122,8 @@ _SIGS = {
     "kvft_solver_set_amplitudes": (ctypes.c_int, [vp, vp, vp]),
     "kvft_solver_device_amplitudes": (ctypes.c_int, [vp, ctypes.POINTER(vp),
                                                      ctypes.POINTER(vp)]),
+    "kvft_solver_set_spin_blocks": (ctypes.c_int, [vp, ctypes.c_int,
+                                                   ctypes.POINTER(ctypes.c_int)]),
     "kvft_solver_footprint": (ctypes.c_size_t, [ctypes.c_int, ctypes.c_int,
                                                 ctypes.c_int]),
 }

@@ -102,6 +102,16 @@ class DeviceSolver(object):
             G.ctypes.data_as(_lib.vp), ctypes.byref(h)), "kvft_solver_create_blocks")
         return cls(ctx, h, ng, nv, no)
 
+    def spin_blocks(self, on=None):
+        """Alpha-half size of the spin blocks the residual uses (0: none);
+        ``on`` = False / True turns them off / back on (they are found at
+        creation when the integrals are spin-blocked)."""
+        h = ctypes.c_int()
+        flag = -1 if on is None else int(bool(on))
+        self.ctx.check(self.ctx.L.kvft_solver_set_spin_blocks(self.h, flag, ctypes.byref(h)),
+                       "kvft_solver_set_spin_blocks")
+        return h.value
+
     def set_amplitudes(self, T1, T2):
         T1 = numpy.ascontiguousarray(T1, dtype=float)
         T2 = numpy.ascontiguousarray(T2, dtype=float)

@@ -84,6 +84,17 @@ struct kvft_ctx {
     // launched (its kernel is timed alone, without the operand packing)
     int gemm_cat = 1;
     double gemm_work = 0.0;
+    // Spin blocks of the residual's operands: 0, or the size h of the alpha
+    // half when every orbital index runs over [0, h) alpha then [h, 2h) beta
+    // and the integrals and amplitudes vanish outside spin-conserving blocks
+    // (set by a solver that has checked its integrals).
+    int spin_half = 0;
+};
+struct KvSpinScope {
+    kvft_ctx *ctx;
+    int prev;
+    KvSpinScope(kvft_ctx *c, int h) : ctx(c), prev(c->spin_half) { c->spin_half = h; }
+    ~KvSpinScope() { ctx->spin_half = prev; }
 };
 void kv_pack_cache_clear(kvft_ctx *ctx);
 // Turns the pack cache on for the lifetime of the guard.

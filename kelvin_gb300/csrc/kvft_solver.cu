@@ -184,6 +184,11 @@ struct kvft_solver {
     std::vector<void *> allocs;
     double nl1 = 0.1, nl2 = 0.1;
     bool norms_valid = false;
+    // spin blocks: the half h when the integrals were found spin-blocked
+    // (0: not), and whether the residual uses them (amplitudes set from
+    // outside that break the structure turn them off)
+    int spin_half = 0;
+    bool spin_on = true;
     long long s1() const { return (long long)nv * no; }
     long long s2() const { return s1() * s1(); }
 };
@@ -260,6 +265,7 @@ int form_tbar(kvft_solver *s) {
     const double *Ic[9];
     for (int k = 0; k < 9; k++) Ic[k] = s->I[k];
     KvPackCacheScope cache(ctx);          // the integral blocks are the solver's own
+    KvSpinScope spins(ctx, s->spin_on ? s->spin_half : 0);
     for (int y0 = 0; y0 < s->ng; y0 += s->chunk) {
         int nb = std::min(s->chunk, s->ng - y0);
         KV_TRY(kv_stanton(ctx, nb, s->nv, s->no, Fc, Ic, s->T1 + y0 * n1, s->T2 + y0 * n2, -1.0,
@@ -296,9 +302,70 @@ int refresh_norms(kvft_solver *s) {
     return KVFT_OK;
 }
 
+// Spin-block check: 1 in *bad if any element of the [nb][n]^rank arrays
+// outside the spin-conserving blocks is nonzero (rank 2: s_p = s_q; rank 4:
+// s_p + s_q = s_r + s_s; s = index >= h).  Blocks over (batch, p, q), threads
+// over the remaining (r, s) with 32-bit index arithmetic.
+__global__ void spin_check_kernel(const double *__restrict__ x, int n, int h, int rank,
+                                  long long rows, int *__restrict__ bad) {
+    const int inner = rank == 4 ? n * n : n;
+    for (long long row = blockIdx.x; row < rows; row += gridDim.x) {
+        int lead = 0;
+        if (rank == 4) {
+            const int pq = (int)(row % ((long long)n * n));
+            lead = (pq / n >= h) + (pq % n >= h);
+        } else {
+            lead = ((int)(row % n) >= h) ? 1 : 0;
+        }
+        const double *r = x + row * inner;
+        for (int e = threadIdx.x; e < inner; e += blockDim.x) {
+            const int tail = rank == 4 ? (e / n >= h) + (e % n >= h) : (e >= h ? 1 : 0);
+            if (tail != lead && r[e] != 0.0) *bad = 1;
+        }
+    }
+}
+
+// 1 when every listed array is spin-blocked with alpha half h
+int spin_blocked(kvft_ctx *ctx, int n, int h, int count, const double *const *arr,
+                 const int *rank, const long long *batch, int *yes) {
+    void *flag = nullptr;
+    KV_TRY(kv_scratch(ctx, "spin_check", sizeof(int), &flag));
+    KV_CHECK(ctx, cudaMemsetAsync(flag, 0, sizeof(int), ctx->stream));
+    for (int k = 0; k < count; k++) {
+        const long long rows = batch[k] * (rank[k] == 4 ? (long long)n * n : n);
+        const int grid = (int)std::min<long long>(rows, (long long)ctx->sm_count * 16);
+        spin_check_kernel<<<grid, 256, 0, ctx->stream>>>(arr[k], n, h, rank[k], rows,
+                                                         (int *)flag);
+        KV_TRY(kv_launch_check(ctx, "spin_check"));
+    }
+    int h_bad = 0;
+    KV_CHECK(ctx, cudaMemcpyAsync(&h_bad, flag, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    KV_CHECK(ctx, cudaStreamSynchronize(ctx->stream));
+    *yes = h_bad ? 0 : 1;
+    return KVFT_OK;
+}
+
+// Finds the spin blocks of the solver's integrals (general-spin ordering of
+// the model systems: alpha half, then beta half).
+int detect_spin_blocks(kvft_solver *s) {
+    s->spin_half = 0;
+    if (s->nv != s->no || s->nv % 2) return KVFT_OK;
+    const int n = s->nv, h = n / 2;
+    const double *arr[13];
+    int rank[13];
+    long long batch[13];
+    for (int k = 0; k < 4; k++) arr[k] = s->F[k], rank[k] = 2, batch[k] = 1;
+    for (int k = 0; k < 9; k++) arr[4 + k] = s->I[k], rank[4 + k] = 4, batch[4 + k] = 1;
+    int yes = 0;
+    KV_TRY(spin_blocked(s->ctx, n, h, 13, arr, rank, batch, &yes));
+    s->spin_half = yes ? h : 0;
+    return KVFT_OK;
+}
+
 int finish_create(kvft_solver *s, kvft_solver **out) {
     if (cudaStreamSynchronize(s->ctx->stream) != cudaSuccess)
         return kv_fail(s->ctx, KVFT_EDEVICE, "solver set-up kernels failed");
+    KV_TRY(detect_spin_blocks(s));
     KV_TRY(pick_chunk(s));
     *out = s;
     return KVFT_OK;
@@ -549,6 +616,7 @@ int kvft_solver_run_point(kvft_solver *s, const kvft_solve_opts *o, kvft_result 
             KV_TRY(seed_neg(ctx, 1, n1, s->F[2], t1b));
             {
                 KvPackCacheScope cache(ctx);
+                KvSpinScope spins(ctx, s->spin_on ? s->spin_half : 0);
                 KV_TRY(kv_stanton(ctx, 1, s->nv, s->no, Fc, Ic, T1g, T2g, -1.0, t1b, t2b,
                                   s->I[3]));
             }
@@ -601,6 +669,22 @@ int kvft_solver_set_amplitudes(kvft_solver *s, const double *T1h, const double *
     KV_CHECK(s->ctx, cudaMemcpyAsync(s->T2, T2h, sizeof(double) * s->ng * s->s2(),
                                      cudaMemcpyHostToDevice, s->ctx->stream));
     s->norms_valid = false;
+    if (s->spin_half && s->spin_on) {
+        // amplitudes from outside keep the spin blocks only if they conserve spin
+        const double *arr[2] = {s->T1, s->T2};
+        const int rank[2] = {2, 4};
+        const long long batch[2] = {s->ng, s->ng};
+        int yes = 0;
+        KV_TRY(spin_blocked(s->ctx, s->nv, s->spin_half, 2, arr, rank, batch, &yes));
+        if (!yes) s->spin_on = false;
+    }
+    return KVFT_OK;
+}
+
+int kvft_solver_set_spin_blocks(kvft_solver *s, int on, int *half) {
+    if (!s) return KVFT_EINVAL;
+    if (on >= 0) s->spin_on = on != 0;
+    if (half) *half = s->spin_on ? s->spin_half : 0;
     return KVFT_OK;
 }
 

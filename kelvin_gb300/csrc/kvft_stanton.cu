@@ -36,6 +36,89 @@ inline KMat MA(const double *p, KIdx r, KIdx c, long long bst) { return KMat{p, 
 inline KMat MAI(const double *p, KIdx r, KIdx c) { return KMat{p, r, c, 0, 1}; }
 inline KOut MO(double *p, KIdx r, KIdx c, long long bst) { return KOut{p, r, c, bst}; }
 
+// ---- spin-blocked contractions ----------------------------------------------
+// With spin blocks (ctx->spin_half = h > 0, nv = no = 2h) every orbital index
+// splits into an alpha half [0, h) and a beta half [h, 2h), and the integrals
+// and amplitudes vanish outside spin-conserving blocks (x_pqrs = 0 unless
+// s_p + s_q = s_r + s_s).  An n^6 contraction over six orbital indices then
+// has only 10 of its 64 spin-block products nonzero; each runs as a strided
+// GEMM on sub-views (halved index extents, offset pointers).
+
+// A view slot of an orbital index: operand (0 A, 1 B, 2 C), dimension (0
+// rows, 1 columns) and component of that composite index.
+struct Slot {
+    int op, dim, comp;
+};
+
+void halve(KIdx &x, int comp, int h, int s, long long &off) {
+    x.size[comp] = h;
+    off += (long long)s * h * x.st[comp];
+}
+
+// C = alpha A B + beta C over the block products that keep(spins) allows
+// (bit x of spins = spin of orbital index x, whose slots are idx[x]).  C
+// blocks that no product writes are scaled by beta (zeroed when C is the
+// whole contiguous buffer of `cwords` doubles and beta = 0), or left alone
+// with cwords = -1 (an intermediate whose readers skip those blocks too).
+template <class Keep>
+int spin_gemm(kvft_ctx *ctx, int h, int batch, double alpha, const KMat &A, const KMat &B,
+              double beta, const KOut &C, const std::vector<std::vector<Slot>> &idx, Keep keep,
+              long long cwords = 0) {
+    const int nx = (int)idx.size();
+    unsigned cmask = 0;
+    for (int x = 0; x < nx; x++)
+        for (const Slot &s : idx[x])
+            if (s.op == 2) cmask |= 1u << x;
+    for (int x = 0; x < nx; x++)
+        for (const Slot &s : idx[x]) {
+            const KIdx &v = s.op == 0 ? (s.dim ? A.c : A.r)
+                                      : s.op == 1 ? (s.dim ? B.c : B.r) : (s.dim ? C.c : C.r);
+            if (v.size[s.comp] != 2 * h)
+                return kv_fail(ctx, KVFT_EINVAL, "spin blocks: index extent is not 2h");
+        }
+    bool zeroed = false;
+    if (beta == 0.0 && cwords > 0) {
+        KV_CHECK(ctx, cudaMemsetAsync(C.p, 0, sizeof(double) * cwords, ctx->stream));
+        zeroed = true;
+    }
+    std::vector<char> written(1u << nx, 0);
+    for (unsigned m = 0; m < (1u << nx); m++) {
+        if (!keep(m)) continue;
+        KMat a = A, b = B;
+        KOut c = C;
+        long long oa = 0, ob = 0, oc = 0;
+        for (int x = 0; x < nx; x++) {
+            const int sp = (m >> x) & 1;
+            for (const Slot &s : idx[x]) {
+                if (s.op == 0) halve(s.dim ? a.c : a.r, s.comp, h, sp, oa);
+                else if (s.op == 1) halve(s.dim ? b.c : b.r, s.comp, h, sp, ob);
+                else halve(s.dim ? c.c : c.r, s.comp, h, sp, oc);
+            }
+        }
+        a.p += oa;
+        b.p += ob;
+        c.p += oc;
+        const unsigned key = m & cmask;
+        const double be = written[key] ? 1.0 : beta;
+        written[key] = 1;
+        KV_TRY(kv_gemm(ctx, a.r.total(), b.c.total(), a.c.total(), batch, alpha, a, b, be, c));
+    }
+    if (beta == 1.0 || zeroed || cwords < 0) return KVFT_OK;
+    for (unsigned m = 0; m < (1u << nx); m++) {
+        if ((m & ~cmask) || written[m]) continue;
+        KOut c = C;
+        long long oc = 0;
+        for (int x = 0; x < nx; x++)
+            for (const Slot &s : idx[x])
+                if (s.op == 2) halve(s.dim ? c.c : c.r, s.comp, h, (m >> x) & 1, oc);
+        c.p += oc;
+        KV_TRY(kv_scale_view(ctx, c.r.total(), c.c.total(), batch, beta, c));
+    }
+    return KVFT_OK;
+}
+
+inline int sp(unsigned m, int x) { return (m >> x) & 1; }
+
 // workspace layout (per tau point, doubles)
 struct WS {
     double *tau, *ttau, *Fae, *Fmi, *Fme, *Xbe, *Xmj, *Wmnij, *Wabef, *Wmbej,
@@ -112,6 +195,17 @@ int kv_stanton(kvft_ctx *ctx, int nb, int nv, int no, const double *const F[4],
     WS w = carve((double *)wsp, nb, v, o);
     const int B = nb;
     const KIdx one = X1(1, 0);
+    // spin blocks (nv = no = 2h): contractions whose operands all live on the
+    // spin-conserving blocks run as their nonzero spin-block products
+    const int sh = (ctx->spin_half > 0 && nv == no && nv == 2 * ctx->spin_half) ? ctx->spin_half
+                                                                               : 0;
+    typedef std::vector<std::vector<Slot>> Slots;
+    auto sgemm = [&](int M, int N, int K, int batch, double alpha, const KMat &A,
+                     const KMat &Bm, double beta, const KOut &C, const Slots &idx, auto keep,
+                     long long cwords) -> int {
+        if (sh) return spin_gemm(ctx, sh, batch, alpha, A, Bm, beta, C, idx, keep, cwords);
+        return kv_gemm(ctx, M, N, K, batch, alpha, A, Bm, beta, C);
+    };
 
     // ---- tau-tilde (tau itself is only needed pair-compressed) --------------
     KV_TRY(kv_make_tau(ctx, B, nv, no, t1, t2, 0.5, w.ttau));
@@ -242,26 +336,47 @@ int kv_stanton(kvft_ctx *ctx, int nb, int nv, int no, const double *const F[4],
         long long ds[4] = {wm, wb, we, 1};
         KV_TRY(kv_axpby4(ctx, B, d, -1.0, vovo, ss, 0, 0.0, w.Wmbej, ds, v2o2));
     }
-    // - vovv[b,m,e,f] t1[f,j]    (M=(m,b,e), K=f, N=j)
-    KV_TRY(kv_gemm(ctx, no * nv * nv, no, nv, B, -1.0,
-                   MAI(vovv, X3(no, vv, nv, o * vv, nv, v), X1(nv, 1)),
-                   MA(t1, X1(nv, o), X1(no, 1), vo), 1.0,
-                   MO(w.Wmbej, X3(no, wm, nv, wb, nv, we), X1(no, 1), v2o2)));
-    // + t1[b,n] ooov[m,n,j,e]    (M=b, K=n, N=(m,e,j))
-    KV_TRY(kv_gemm(ctx, nv, no * nv * no, no, B, 1.0,
-                   MA(t1, X1(nv, o), X1(no, 1), vo),
-                   MAI(ooov, X1(no, vo), X3(no, oo * v, nv, 1, no, v)), 1.0,
-                   MO(w.Wmbej, X1(nv, wb), X3(no, wm, nv, we, no, 1), v2o2)));
+    // - vovv[b,m,e,f] t1[f,j]    (M=(m,b,e), K=f, N=j); spins m b e f j
+    KV_TRY(sgemm(no * nv * nv, no, nv, B, -1.0,
+                 MAI(vovv, X3(no, vv, nv, o * vv, nv, v), X1(nv, 1)),
+                 MA(t1, X1(nv, o), X1(no, 1), vo), 1.0,
+                 MO(w.Wmbej, X3(no, wm, nv, wb, nv, we), X1(no, 1), v2o2),
+                 Slots{{{0, 0, 0}, {2, 0, 0}}, {{0, 0, 1}, {2, 0, 1}}, {{0, 0, 2}, {2, 0, 2}},
+                       {{0, 1, 2}, {1, 0, 2}}, {{1, 1, 2}, {2, 1, 2}}},
+                 [](unsigned m) {
+                     return sp(m, 1) + sp(m, 0) == sp(m, 2) + sp(m, 3) && sp(m, 3) == sp(m, 4);
+                 }, 0));
+    // + t1[b,n] ooov[m,n,j,e]    (M=b, K=n, N=(m,e,j)); spins b n m e j
+    KV_TRY(sgemm(nv, no * nv * no, no, B, 1.0,
+                 MA(t1, X1(nv, o), X1(no, 1), vo),
+                 MAI(ooov, X1(no, vo), X3(no, oo * v, nv, 1, no, v)), 1.0,
+                 MO(w.Wmbej, X1(nv, wb), X3(no, wm, nv, we, no, 1), v2o2),
+                 Slots{{{0, 0, 2}, {2, 0, 2}}, {{0, 1, 2}, {1, 0, 2}}, {{1, 1, 0}, {2, 1, 0}},
+                       {{1, 1, 1}, {2, 1, 1}}, {{1, 1, 2}, {2, 1, 2}}},
+                 [](unsigned m) {
+                     return sp(m, 0) == sp(m, 1) && sp(m, 2) + sp(m, 1) == sp(m, 4) + sp(m, 3);
+                 }, 0));
     // - oovv[m,n,e,f] (t2[f,b,j,n]/2 + t1[f,j] t1[b,n])  (M=(m,e), K=(n,f), N=(tau,b,j))
     KV_TRY(kv_make_wmbej_tmp(ctx, B, nv, no, t1, t2, w.tmp4));
     {
         // tmp4 holds [tau][b][j][n][f] with per-tau stride v2o2 (tmp4 is sized
         // for the largest block, so index it with the v2o2 layout directly);
         // the contraction index (n, f) is contiguous in both operands
-        KV_TRY(kv_gemm(ctx, no * nv, B * nv * no, no * nv, 1, -1.0,
-                       MAI(oovv, X2(no, o * vv, nv, v), X2(no, vv, nv, 1)),
-                       MA(w.tmp4, X2(no, v, nv, 1), X3(B, v2o2, nv, vo2, no, vo), 0),
-                       1.0, MO(w.Wmbej, X2(no, wm, nv, we), X3(B, v2o2, nv, wb, no, 1), 0)));
+        const KMat A = MAI(oovv, X2(no, o * vv, nv, v), X2(no, vv, nv, 1));
+        const KMat Bm = MA(w.tmp4, X2(no, v, nv, 1), X3(B, v2o2, nv, vo2, no, vo), 0);
+        const KOut C = MO(w.Wmbej, X2(no, wm, nv, we), X3(B, v2o2, nv, wb, no, 1), 0);
+        if (sh) {
+            // orbital indices m e n f b j; <mn||ef> and tmp[b,j,n,f] (t2[f,b,j,n])
+            const std::vector<std::vector<Slot>> idx = {
+                {{0, 0, 1}, {2, 0, 1}}, {{0, 0, 2}, {2, 0, 2}}, {{0, 1, 1}, {1, 0, 1}},
+                {{0, 1, 2}, {1, 0, 2}}, {{1, 1, 1}, {2, 1, 1}}, {{1, 1, 2}, {2, 1, 2}}};
+            KV_TRY(spin_gemm(ctx, sh, 1, -1.0, A, Bm, 1.0, C, idx, [](unsigned m) {
+                return sp(m, 0) + sp(m, 2) == sp(m, 1) + sp(m, 3) &&
+                       sp(m, 3) + sp(m, 4) == sp(m, 5) + sp(m, 2);
+            }));
+        } else {
+            KV_TRY(kv_gemm(ctx, no * nv, B * nv * no, no * nv, 1, -1.0, A, Bm, 1.0, C));
+        }
     }
     // The three doubles terms share one array Z:
     //   T2 += P(ab) Zab + P(ij) Zij + P(ab)P(ij) Zabij
@@ -269,52 +384,97 @@ int kv_stanton(kvft_ctx *ctx, int nb, int nv, int no, const double *const F[4],
     // because Zab is antisymmetric in (i,j) and Zij in (a,b) (as t2 and the
     // antisymmetrised integrals are), so the assembly reads one n^4 array.
     // Zabij[a,b,i,j] = t2[a,e,i,m] Wmbej[m,b,e,j]   (M=(a,i), K=(m,e), N=(b,j))
-    KV_TRY(kv_gemm(ctx, nv * no, nv * no, no * nv, B, 1.0,
-                   MA(t2, X2(nv, vo2, no, o), X2(no, 1, nv, oo), v2o2),
-                   MA(w.Wmbej, X2(no, wm, nv, we), X2(nv, wb, no, 1), v2o2), 0.0,
-                   MO(w.Z, X2(nv, vo2, no, o), X2(nv, oo, no, 1), v2o2)));
-    // Q[b,m,i,j] = vovo[b,m,e,j] t1[e,i]   (M=(b,m,j), K=e, N=i)
-    KV_TRY(kv_gemm(ctx, nv * no * no, no, nv, B, 1.0,
-                   MAI(vovo, X3(nv, vo2, no, vo, no, 1), X1(nv, o)),
-                   MA(t1, X1(nv, o), X1(no, 1), vo), 0.0,
-                   MO(w.Q, X3(nv, o * oo, no, oo, no, 1), X1(no, o), vo3)));
-    // Zabij += t1[a,m] Q[b,m,i,j]   (M=a, K=m, N=(b,i,j))
-    KV_TRY(kv_gemm(ctx, nv, nv * no * no, no, B, 1.0,
-                   MA(t1, X1(nv, o), X1(no, 1), vo),
-                   MA(w.Q, X1(no, oo), X3(nv, o * oo, no, o, no, 1), vo3), 1.0,
-                   MO(w.Z, X1(nv, vo2), X3(nv, oo, no, o, no, 1), v2o2)));
+    {
+        const KMat A = MA(t2, X2(nv, vo2, no, o), X2(no, 1, nv, oo), v2o2);
+        const KMat Bm = MA(w.Wmbej, X2(no, wm, nv, we), X2(nv, wb, no, 1), v2o2);
+        const KOut C = MO(w.Z, X2(nv, vo2, no, o), X2(nv, oo, no, 1), v2o2);
+        if (sh) {
+            // orbital indices a i m e b j; t2[a,e,i,m] and Wmbej[m,b,e,j]
+            const std::vector<std::vector<Slot>> idx = {
+                {{0, 0, 1}, {2, 0, 1}}, {{0, 0, 2}, {2, 0, 2}}, {{0, 1, 1}, {1, 0, 1}},
+                {{0, 1, 2}, {1, 0, 2}}, {{1, 1, 1}, {2, 1, 1}}, {{1, 1, 2}, {2, 1, 2}}};
+            KV_TRY(spin_gemm(ctx, sh, B, 1.0, A, Bm, 0.0, C, idx, [](unsigned m) {
+                return sp(m, 0) + sp(m, 3) == sp(m, 1) + sp(m, 2) &&
+                       sp(m, 2) + sp(m, 4) == sp(m, 3) + sp(m, 5);
+            }, (long long)B * v2o2));
+        } else {
+            KV_TRY(kv_gemm(ctx, nv * no, nv * no, no * nv, B, 1.0, A, Bm, 0.0, C));
+        }
+    }
+    // Q[b,m,i,j] = vovo[b,m,e,j] t1[e,i]   (M=(b,m,j), K=e, N=i); spins b m j e i.
+    // With spin blocks only Q's spin-conserving blocks are written, and they
+    // are the only ones its reader below touches.
+    KV_TRY(sgemm(nv * no * no, no, nv, B, 1.0,
+                 MAI(vovo, X3(nv, vo2, no, vo, no, 1), X1(nv, o)),
+                 MA(t1, X1(nv, o), X1(no, 1), vo), 0.0,
+                 MO(w.Q, X3(nv, o * oo, no, oo, no, 1), X1(no, o), vo3),
+                 Slots{{{0, 0, 0}, {2, 0, 0}}, {{0, 0, 1}, {2, 0, 1}}, {{0, 0, 2}, {2, 0, 2}},
+                       {{0, 1, 2}, {1, 0, 2}}, {{1, 1, 2}, {2, 1, 2}}},
+                 [](unsigned m) {
+                     return sp(m, 0) + sp(m, 1) == sp(m, 3) + sp(m, 2) && sp(m, 3) == sp(m, 4);
+                 }, -1));
+    // Zabij += t1[a,m] Q[b,m,i,j]   (M=a, K=m, N=(b,i,j)); spins a m b i j
+    KV_TRY(sgemm(nv, nv * no * no, no, B, 1.0,
+                 MA(t1, X1(nv, o), X1(no, 1), vo),
+                 MA(w.Q, X1(no, oo), X3(nv, o * oo, no, o, no, 1), vo3), 1.0,
+                 MO(w.Z, X1(nv, vo2), X3(nv, oo, no, o, no, 1), v2o2),
+                 Slots{{{0, 0, 2}, {2, 0, 2}}, {{0, 1, 2}, {1, 0, 2}}, {{1, 1, 0}, {2, 1, 0}},
+                       {{1, 1, 1}, {2, 1, 1}}, {{1, 1, 2}, {2, 1, 2}}},
+                 [](unsigned m) {
+                     return sp(m, 0) == sp(m, 1) && sp(m, 2) + sp(m, 1) == sp(m, 3) + sp(m, 4);
+                 }, 0));
 
     // ---- Z += Zab/2: t2 (F_be - 1/2 t1 F_me) and t1 vooo ----------------------
     KV_TRY(kv_bcast(ctx, 1, vv * B, w.Fae, w.Xbe));
     KV_TRY(kv_gemm(ctx, nv, nv, no, B, -0.5, MA(t1, X1(nv, o), X1(no, 1), vo),
                    MA(w.Fme, X1(no, v), X1(nv, 1), vo), 1.0,
                    MO(w.Xbe, X1(nv, v), X1(nv, 1), vv)));
-    // Zab[a,b,i,j] = t2[a,e,i,j] Xbe[b,e]   (M=(a,i,j), K=e, N=b)
-    KV_TRY(kv_gemm(ctx, nv * no * no, nv, nv, B, 0.5,
-                   MA(t2, X3(nv, vo2, no, o, no, 1), X1(nv, oo), v2o2),
-                   MA(w.Xbe, X1(nv, 1), X1(nv, v), vv), 1.0,
-                   MO(w.Z, X3(nv, vo2, no, o, no, 1), X1(nv, oo), v2o2)));
-    // Zab += t1[a,m] vooo[b,m,i,j]   (M=a, K=m, N=(b,i,j))
-    KV_TRY(kv_gemm(ctx, nv, nv * no * no, no, B, 0.5,
-                   MA(t1, X1(nv, o), X1(no, 1), vo),
-                   MAI(vooo, X1(no, oo), X3(nv, o * oo, no, o, no, 1)), 1.0,
-                   MO(w.Z, X1(nv, vo2), X3(nv, oo, no, o, no, 1), v2o2)));
+    // Zab[a,b,i,j] = t2[a,e,i,j] Xbe[b,e]   (M=(a,i,j), K=e, N=b); spins a i j e b
+    KV_TRY(sgemm(nv * no * no, nv, nv, B, 0.5,
+                 MA(t2, X3(nv, vo2, no, o, no, 1), X1(nv, oo), v2o2),
+                 MA(w.Xbe, X1(nv, 1), X1(nv, v), vv), 1.0,
+                 MO(w.Z, X3(nv, vo2, no, o, no, 1), X1(nv, oo), v2o2),
+                 Slots{{{0, 0, 0}, {2, 0, 0}}, {{0, 0, 1}, {2, 0, 1}}, {{0, 0, 2}, {2, 0, 2}},
+                       {{0, 1, 2}, {1, 0, 2}}, {{1, 1, 2}, {2, 1, 2}}},
+                 [](unsigned m) {
+                     return sp(m, 0) + sp(m, 3) == sp(m, 1) + sp(m, 2) && sp(m, 4) == sp(m, 3);
+                 }, 0));
+    // Zab += t1[a,m] vooo[b,m,i,j]   (M=a, K=m, N=(b,i,j)); spins a m b i j
+    KV_TRY(sgemm(nv, nv * no * no, no, B, 0.5,
+                 MA(t1, X1(nv, o), X1(no, 1), vo),
+                 MAI(vooo, X1(no, oo), X3(nv, o * oo, no, o, no, 1)), 1.0,
+                 MO(w.Z, X1(nv, vo2), X3(nv, oo, no, o, no, 1), v2o2),
+                 Slots{{{0, 0, 2}, {2, 0, 2}}, {{0, 1, 2}, {1, 0, 2}}, {{1, 1, 0}, {2, 1, 0}},
+                       {{1, 1, 1}, {2, 1, 1}}, {{1, 1, 2}, {2, 1, 2}}},
+                 [](unsigned m) {
+                     return sp(m, 0) == sp(m, 1) && sp(m, 2) + sp(m, 1) == sp(m, 3) + sp(m, 4);
+                 }, 0));
 
     // ---- Z += Zij/2: -t2 (F_mj + 1/2 t1 F_me) and vvvo t1 -----------------------
     KV_TRY(kv_bcast(ctx, 1, oo * B, w.Fmi, w.Xmj));
     KV_TRY(kv_gemm(ctx, no, no, nv, B, 0.5, MA(w.Fme, X1(no, v), X1(nv, 1), vo),
                    MA(t1, X1(nv, o), X1(no, 1), vo), 1.0,
                    MO(w.Xmj, X1(no, o), X1(no, 1), oo)));
-    // Zij[a,b,i,j] = - t2[a,b,i,m] Xmj[m,j]   (M=(a,b,i), K=m, N=j)
-    KV_TRY(kv_gemm(ctx, nv * nv * no, no, no, B, -0.5,
-                   MA(t2, X3(nv, vo2, nv, oo, no, o), X1(no, 1), v2o2),
-                   MA(w.Xmj, X1(no, o), X1(no, 1), oo), 1.0,
-                   MO(w.Z, X3(nv, vo2, nv, oo, no, o), X1(no, 1), v2o2)));
-    // Zij += vvvo[a,b,e,j] t1[e,i]   (M=(a,b,j), K=e, N=i)
-    KV_TRY(kv_gemm(ctx, nv * nv * no, no, nv, B, 0.5,
-                   MAI(vvvo, X3(nv, vv * o, nv, vo, no, 1), X1(nv, o)),
-                   MA(t1, X1(nv, o), X1(no, 1), vo), 1.0,
-                   MO(w.Z, X3(nv, vo2, nv, oo, no, 1), X1(no, o), v2o2)));
+    // Zij[a,b,i,j] = - t2[a,b,i,m] Xmj[m,j]   (M=(a,b,i), K=m, N=j); spins a b i m j
+    KV_TRY(sgemm(nv * nv * no, no, no, B, -0.5,
+                 MA(t2, X3(nv, vo2, nv, oo, no, o), X1(no, 1), v2o2),
+                 MA(w.Xmj, X1(no, o), X1(no, 1), oo), 1.0,
+                 MO(w.Z, X3(nv, vo2, nv, oo, no, o), X1(no, 1), v2o2),
+                 Slots{{{0, 0, 0}, {2, 0, 0}}, {{0, 0, 1}, {2, 0, 1}}, {{0, 0, 2}, {2, 0, 2}},
+                       {{0, 1, 2}, {1, 0, 2}}, {{1, 1, 2}, {2, 1, 2}}},
+                 [](unsigned m) {
+                     return sp(m, 0) + sp(m, 1) == sp(m, 2) + sp(m, 3) && sp(m, 3) == sp(m, 4);
+                 }, 0));
+    // Zij += vvvo[a,b,e,j] t1[e,i]   (M=(a,b,j), K=e, N=i); spins a b j e i
+    KV_TRY(sgemm(nv * nv * no, no, nv, B, 0.5,
+                 MAI(vvvo, X3(nv, vv * o, nv, vo, no, 1), X1(nv, o)),
+                 MA(t1, X1(nv, o), X1(no, 1), vo), 1.0,
+                 MO(w.Z, X3(nv, vo2, nv, oo, no, 1), X1(no, o), v2o2),
+                 Slots{{{0, 0, 0}, {2, 0, 0}}, {{0, 0, 1}, {2, 0, 1}}, {{0, 0, 2}, {2, 0, 2}},
+                       {{0, 1, 2}, {1, 0, 2}}, {{1, 1, 2}, {2, 1, 2}}},
+                 [](unsigned m) {
+                     return sp(m, 0) + sp(m, 1) == sp(m, 3) + sp(m, 2) && sp(m, 3) == sp(m, 4);
+                 }, 0));
 
     // ---- T2 += fac (1 - P(ab))(1 - P(ij)) (Z + ladders) -------------------------
     return kv_assemble_t2(ctx, B, nv, no, fac, w.Z, ladders ? w.Lc : nullptr, T2, seed_t2);
