@@ -62,13 +62,13 @@ WORKLOADS = {
                         "ng=10, damping 0.5, econv 1e-10"),
 }
 ITERS_FALLBACK = 30
-# DRAM bytes per launch of the n^6-class contractions (dram__bytes_read.sum +
-# dram__bytes_write.sum), mean over those launches of one ueg114 iteration:
-# 22 launches (three digit levels) and 33 (seven), from the ncu launch lists
-# of `python bench.py --profile-step [--precision fp64_tc]` (one pass per
-# launch, so the full-size workload was captured).  A measured input of the
-# roofline, not computed here: re-take it when the kernel changes.
-NCU_GEMM6_TRAFFIC = {("ueg114", "mixed"): 36.839e9, ("ueg114", "fp64_tc"): 77.673e9}
+# DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of
+# the contraction classes, mean over those launches of one ueg114 iteration,
+# from the ncu launch lists of `python bench.py --profile-step [--precision
+# fp64_tc]` (one replay pass per launch, so the full-size workload was
+# captured).  A measured input of the roofline, not computed here: re-take
+# it when the kernels change.
+NCU_TRAFFIC = {}
 REFINE = 2          # refinement sweeps that end a mixed solve
 REFINE_DIGITS = 5   # their digit levels
 STEP_EVENTS = 8     # first event slot of the per-step timings (at most 50 steps)
@@ -363,35 +363,51 @@ def run_gpu(args, w):
     if rank != 0:
         return 0
     peaks, peak_src = load_peaks()
-    dom = max(prof, key=lambda c: prof[c][1])
-    nl, dms, work = prof[dom]
-    if dom in ("gemm6", "gemm"):
-        achieved = work / (dms / 1e3) / 1e12
-        unit, bound = "TFLOP/s", "tensor"
-        if args.precision == "fp64":
-            peak = 1.25
-            psrc = "nominal GB300 FP64 1.25 TFLOP/s (MEASURED_PEAKS.json has no FP64 figure)"
-            kernel = "gemm_f64_kernel (%s contractions)" % dom
+    kernels = {"gemm6": "tc_gemm_kernel, n^6-class contractions",
+               "gemm": "tc_gemm_kernel, n^5-class contractions", "quad": "quad_kernel",
+               "energy": "energy2_kernel", "elem": "element-wise passes",
+               "pack": "digit packing (pack_rows/pack_exp/pack_digits)"}
+    if args.precision == "fp64":
+        kernels["gemm6"] = "gemm_f64_kernel, n^6-class contractions"
+        kernels["gemm"] = "gemm_f64_kernel, n^5-class contractions"
+
+    def roof(c):
+        """Achieved rate of one category against its bound: tensor flops for
+        the n^6 contractions (GB300's FP64 pipe for the FP64 form), bytes per
+        second against HBM for everything else."""
+        nl, dms, work = prof[c]
+        if nl == 0 or dms <= 0:
+            return None
+        if c == "gemm6":
+            achieved, unit, bound = work / (dms / 1e3) / 1e12, "TFLOP/s", "tensor"
+            if args.precision == "fp64":
+                peak = 1.25
+                psrc = "nominal GB300 FP64 1.25 TFLOP/s (MEASURED_PEAKS.json has no FP64 figure)"
+            else:
+                pairs = sum(l - 1 for l in range(2, digits + 1))
+                achieved *= pairs      # BF16 tensor flops issued per FP64-equivalent flop
+                peak = peaks["bf16_tflops_sustained"]
+                psrc = "bf16_tflops_sustained of %s peaks; achieved = algorithmic 2MNK flops " \
+                       "x %d digit-pair products" % (peak_src, pairs)
         else:
-            pairs = sum(l - 1 for l in range(2, digits + 1))
-            achieved *= pairs          # BF16 tensor flops issued per FP64-equivalent flop
-            peak = peaks["bf16_tflops_sustained"]
-            psrc = "bf16_tflops_sustained of %s peaks; achieved = algorithmic 2MNK flops x " \
-                   "%d digit-pair products" % (peak_src, pairs)
-            kernel = "tc_gemm_kernel (%s contractions)" % dom
-    else:
-        achieved = work / (dms / 1e3) / 1e9
-        peak, unit, bound = peaks["hbm_gbs"], "GB/s", "hbm"
-        psrc = "hbm_gbs of %s peaks" % peak_src
-        kernel = dom
-    traffic = NCU_GEMM6_TRAFFIC.get((args.workload, args.precision)) if dom == "gemm6" else None
-    roofline = {"bound": bound, "kernel": kernel, "achieved": achieved, "peak": peak,
-                "unit": unit, "frac": achieved / peak, "traffic": traffic,
-                "traffic_unit": "bytes per launch (ncu dram__bytes_read.sum + "
-                                "dram__bytes_write.sum)" if traffic else None,
-                "launches": nl,
-                "avg_launch_ms": dms / max(nl, 1), "peak_source": psrc,
-                "breakdown_ms_per_step": {c: round(prof[c][1] / args.steps, 3) for c in prof}}
+            achieved, unit, bound = work / (dms / 1e3) / 1e9, "GB/s", "hbm"
+            peak = peaks["hbm_gbs"]
+            psrc = "hbm_gbs of %s peaks; achieved = algorithmic bytes" % peak_src
+        return {"bound": bound, "kernel": kernels[c], "achieved": achieved, "peak": peak,
+                "unit": unit, "frac": achieved / peak, "launches": nl,
+                "avg_launch_ms": dms / nl, "peak_source": psrc}
+
+    cats = {c: roof(c) for c in prof}
+    dom = max(prof, key=lambda c: prof[c][1])
+    roofline = dict(cats[dom])
+    traffic = NCU_TRAFFIC.get((args.workload, args.precision, dom))
+    roofline.update({
+        "category": dom, "traffic": traffic,
+        "traffic_unit": "bytes per launch (ncu dram__bytes_read.sum + dram__bytes_write.sum)"
+                        if traffic else None,
+        "categories": {c: {k: cats[c][k] for k in ("bound", "achieved", "unit", "frac")}
+                       for c in cats if cats[c]},
+        "breakdown_ms_per_step": {c: round(prof[c][1] / args.steps, 3) for c in prof}})
 
     t_iter, sample = cpu_iteration_seconds(w, sysobj)
     cpu_iters = iters_of(w, "fp64")                       # the CPU port is FP64

@@ -75,6 +75,8 @@ enum {
     KVFT_CAT_ELEM = 4,    /* element-wise tensor passes */
     KVFT_CAT_PACK = 5     /* tensor-core operand packing */
 };
+/* Per category: launches, device milliseconds and algorithmic work --
+ * flops for KVFT_CAT_GEMM6, bytes moved for every other category. */
 typedef struct {
     uint64_t launches[6];
     double ms[6];

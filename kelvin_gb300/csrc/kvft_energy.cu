@@ -21,7 +21,7 @@ constexpr int WTAB = 1024;                  // doubles of the (y, a, i) table
 __global__ void __launch_bounds__(256, 2)
 energy2_kernel(int ng, int nv, int no, const double *__restrict__ T1,
                const double *__restrict__ T2, const double *__restrict__ eri,
-               const double *__restrict__ g, int qterm, double *__restrict__ partial) {
+               const double *__restrict__ g, int qterm, int sh, double *__restrict__ partial) {
     __shared__ double E[TILE][TILE + 1];     // [ij][ab]
     __shared__ double red[256];
     __shared__ double gs[WTAB / 4];          // g_y of the chunk
@@ -29,6 +29,25 @@ energy2_kernel(int ng, int nv, int no, const double *__restrict__ T1,
     const long long V2 = (long long)nv * nv, O2 = (long long)no * no;
     const long long ab0 = (long long)blockIdx.y * TILE, ij0 = (long long)blockIdx.x * TILE;
     const int t = threadIdx.x, tx = t % TILE, ty = t / TILE;   // ty in [0, 8)
+    if (sh > 0) {
+        // spin blocks: a tile whose (a,b) spin sums and (i,j) spin sums never
+        // meet holds only zero amplitudes and adds nothing
+        __shared__ int live;
+        if (t < 32) {
+            const long long ab = ab0 + t, ij = ij0 + t;
+            unsigned sab = 0, sij = 0;
+            if (ab < V2) sab = 1u << ((int)(ab / nv >= sh) + (int)(ab % nv >= sh));
+            if (ij < O2) sij = 1u << ((int)(ij / no >= sh) + (int)(ij % no >= sh));
+            sab = __reduce_or_sync(0xffffffffu, sab);
+            sij = __reduce_or_sync(0xffffffffu, sij);
+            if (t == 0) live = (sab & sij) != 0;
+        }
+        __syncthreads();
+        if (!live) {
+            if (t == 0) partial[blockIdx.y * gridDim.x + blockIdx.x] = 0.0;
+            return;
+        }
+    }
     for (int r = ty; r < TILE; r += 8) {
         long long ij = ij0 + r, ab = ab0 + tx;
         E[r][tx] = (ij < O2 && ab < V2) ? eri[ij * V2 + ab] : 0.0;
@@ -138,7 +157,7 @@ __global__ void energy_final_kernel(const double *__restrict__ partial, int n,
 // Writes Omega to dres[0] (device).  Uses context scratch.
 int kv_energy(kvft_ctx *ctx, int ng, int nv, int no, const double *T1, const double *T2,
               const double *f, const double *eri, const double *g, double beta, int qterm,
-              double *dres) {
+              double *dres, int spin_half) {
     const long long V2 = (long long)nv * nv, O2 = (long long)no * no;
     dim3 grid((unsigned)((O2 + TILE - 1) / TILE), (unsigned)((V2 + TILE - 1) / TILE));
     long long nblk = (long long)grid.x * grid.y;
@@ -148,7 +167,8 @@ int kv_energy(kvft_ctx *ctx, int ng, int nv, int no, const double *T1, const dou
     // algorithmic bytes: T2 (all tau points) + eri + T1
     KvProfScope prof(ctx, KV_CAT_ENERGY,
                      8.0 * ((double)ng * V2 * O2 + (double)V2 * O2 + (double)ng * nv * no));
-    energy2_kernel<<<grid, 256, 0, ctx->stream>>>(ng, nv, no, T1, T2, eri, g, qterm, pp);
+    const int sh = (nv == no && nv == 2 * spin_half) ? spin_half : 0;
+    energy2_kernel<<<grid, 256, 0, ctx->stream>>>(ng, nv, no, T1, T2, eri, g, qterm, sh, pp);
     KV_TRY(kv_launch_check(ctx, "energy2"));
     energy1_kernel<<<1, 256, 0, ctx->stream>>>(ng, nv, no, T1, f, g, pp + nblk);
     KV_TRY(kv_launch_check(ctx, "energy1"));
@@ -226,7 +246,7 @@ extern "C" int kvft_ft_cc_energy_noalloc(void *stream, int ng, int nv, int no,
     cudaStream_t st = (cudaStream_t)stream;
     const int nblk = (int)(gx * gy);
     energy2_kernel<<<dim3((unsigned)gx, (unsigned)gy), 256, 0, st>>>(ng, nv, no, T1, T2, eri, g,
-                                                                      qterm, scratch);
+                                                                      qterm, 0, scratch);
     energy1_kernel<<<1, 256, 0, st>>>(ng, nv, no, T1, f, g, scratch + nblk);
     energy_final_kernel<<<1, 256, 0, st>>>(scratch, nblk, scratch + nblk, 1.0 / beta,
                                            omega_dev);

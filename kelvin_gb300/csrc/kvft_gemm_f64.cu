@@ -203,24 +203,34 @@ void order_k(int M, int N, int batch, KMat &A, KMat &B) {
 
 }  // namespace
 
-void kv_gemm_prof_set(kvft_ctx *ctx, int M, int N, int K, int batch) {
-    // n^6-class: every GEMM dimension is a pair of orbital indices or more
+void kv_gemm_prof_set(kvft_ctx *ctx, int M, int N, int K, int batch, int nbA, int nbB,
+                      double beta, bool tc) {
+    // n^6-class: every GEMM dimension is a pair of orbital indices or more;
+    // its work is counted in flops, the other contractions' in the bytes the
+    // kernel must move (operands as read: BF16 digit planes on the tensor
+    // cores, FP64 otherwise; C written, or read and written when added to)
     const long long mn = std::min(std::min(M, N), K), mx = std::max(std::max(M, N), K);
     ctx->gemm_cat = (mn * mn > mx) ? KV_CAT_GEMM6 : KV_CAT_GEMM;
-    ctx->gemm_work = 2.0 * M * N * (double)K * batch;
+    if (ctx->gemm_cat == KV_CAT_GEMM6) {
+        ctx->gemm_work = 2.0 * M * N * (double)K * batch;
+    } else {
+        const double el = tc ? 2.0 * std::min(ctx->digits - 1, 6) : 8.0;
+        ctx->gemm_work = el * K * ((double)M * nbA + (double)N * nbB) +
+                         8.0 * M * (double)N * batch * (beta != 0.0 ? 2 : 1);
+    }
 }
 
 int kv_gemm(kvft_ctx *ctx, int M, int N, int K, int batch, double alpha,
             const KMat &A_in, const KMat &B_in, double beta, const KOut &C) {
     KMat A = A_in, B = B_in;
     order_k(M, N, batch, A, B);
-    kv_gemm_prof_set(ctx, M, N, K, batch);
     // Tensor cores for everything but short sums and tiny products, which stay
     // on the FP64 pipe.  Skinny shapes (a few columns against a long K) go to
     // the tensor cores too: even with most of a 128-wide tile idle they beat
     // GB300's FP64 pipe by an order of magnitude.
     const bool tc = ctx->precision != KVFT_PREC_FP64 && K >= 16 &&
                     2.0 * M * N * (double)K * batch >= 2.0e6;
+    kv_gemm_prof_set(ctx, M, N, K, batch, A.bst ? batch : 1, B.bst ? batch : 1, beta, tc);
     if (!tc) return kv_gemm_f64(ctx, M, N, K, batch, alpha, A, B, beta, C);
     return kv_gemm_tc(ctx, M, N, K, batch, alpha, A, B, beta, C, ctx->digits);
 }

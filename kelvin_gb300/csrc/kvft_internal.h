@@ -155,9 +155,10 @@ int kv_gemm_f64(kvft_ctx *ctx, int M, int N, int K, int batch, double alpha,
 int kv_gemm_tc(kvft_ctx *ctx, int M, int N, int K, int batch, double alpha,
                const KMat &A, const KMat &B, double beta, const KOut &C,
                int digits);
-// Sets the profile category (n^6-class or not) and flops of the next
-// contraction launch.
-void kv_gemm_prof_set(kvft_ctx *ctx, int M, int N, int K, int batch);
+// Sets the profile category (n^6-class or not) and work (flops, or bytes
+// for the other class) of the next contraction launch.
+void kv_gemm_prof_set(kvft_ctx *ctx, int M, int N, int K, int batch, int nbA, int nbB,
+                      double beta, bool tc);
 // C = beta * C over a strided output view (beta == 0 writes zeros).
 int kv_scale_view(kvft_ctx *ctx, int M, int N, int batch, double beta, const KOut &C);
 // Reads (and clears) the device status word set by bounded waits; syncs.
@@ -203,9 +204,11 @@ int kv_int_tbar(kvft_ctx *ctx, int ng, size_t P, const double *tbar,
                 const double *eps_o, int nv, int no, int rank,
                 const double *G, int full, double *out);
 
+// spin_half > 0: the amplitudes vanish outside the spin-conserving blocks
+// (alpha half first), whose zero tiles are skipped
 int kv_energy(kvft_ctx *ctx, int ng, int nv, int no, const double *T1,
               const double *T2, const double *f, const double *eri,
-              const double *g, double beta, int qterm, double *dres);
+              const double *g, double beta, int qterm, double *dres, int spin_half = 0);
 
 // T1/T2 += fac * residual; with seed_t2, T2 = -seed_t2 + fac * residual
 // (T2 need not be initialised).

@@ -34,6 +34,7 @@ struct QuadParams {
     int uniform;             // all ti[k+1]-ti[k] equal
     int full;
     double alpha;            // damping (fused update only)
+    int spin_half;           // fused update over the spin-conserving elements only (0: all)
 };
 
 __device__ __forceinline__ double denom(const QuadParams &q, long long p,
@@ -103,8 +104,7 @@ quad_kernel(QuadParams q, const double *__restrict__ tbar, const double *__restr
 
     double s_diff = 0.0, s_norm = 0.0;
     const int t = threadIdx.x;
-    for (long long p = blockIdx.x * (long long)QT + t; p < q.P;
-         p += (long long)gridDim.x * QT) {
+    auto element = [&](long long p) {
         const double d = denom(q, p, D, ev, eo);
         // step factors r_k = exp((ti[k]-ti[k+1]) d)
         double r0 = 1.0;
@@ -193,6 +193,28 @@ quad_kernel(QuadParams q, const double *__restrict__ tbar, const double *__restr
             s_diff += (double)f_diff;
             s_norm += (double)f_norm;
         }
+    };
+    if (MODE == 1 && q.spin_half > 0) {
+        // spin blocks: only the spin-conserving elements move (the others
+        // are zero and stay zero); each (a, b, i) row holds them as one run
+        // of h consecutive j or none, and one warp takes one run
+        const int h = q.spin_half, n = q.no;
+        const long long rows = q.P / n;
+        const int lane = t % 32;
+        const long long tw = (long long)gridDim.x * (QT / 32);
+        for (long long u = blockIdx.x * (long long)(QT / 32) + t / 32; u < 2 * rows; u += tw) {
+            const long long r = u >> 1;
+            const int jh = (int)(u & 1);
+            const int i = (int)(r % n);
+            const long long ab = r / n;
+            const int b = (int)(ab % n), a = (int)(ab / n);
+            if ((a >= h) + (b >= h) != (i >= h) + jh) continue;
+            for (int jj = lane; jj < h; jj += 32) element(r * n + (long long)jh * h + jj);
+        }
+    } else {
+        for (long long p = blockIdx.x * (long long)QT + t; p < q.P;
+             p += (long long)gridDim.x * QT)
+            element(p);
     }
     if (MODE == 1) {
         // block reduction of the two sums (fixed order: deterministic)
@@ -296,7 +318,7 @@ int kv_quad_launch(kvft_ctx *ctx, int mode, int ng, long long P, int rank, int n
                    int no, const double *tbar, const double *ti, const double *hti,
                    const double *G, const double *hG, const double *D,
                    const double *ev, const double *eo, int full, double alpha,
-                   double *out, double *res) {
+                   double *out, double *res, int spin_half) {
     if (ng < 1 || ng > MAXNG) return kv_fail(ctx, KVFT_EINVAL, "ng must be in [1, 64]");
     if (P == 0) return KVFT_OK;
     QuadParams q;
@@ -307,6 +329,7 @@ int kv_quad_launch(kvft_ctx *ctx, int mode, int ng, long long P, int rank, int n
     q.no = no;
     q.full = full;
     q.alpha = alpha;
+    q.spin_half = (mode == 1 && rank == 2 && nv == no && nv == 2 * spin_half) ? spin_half : 0;
     analyse_grid(ng, hti, hG, full, &q.step, &q.uniform);
     size_t smem = quad_smem(ng, q.uniform, q.step);
     long long blocks = (P + QT - 1) / QT;
@@ -362,7 +385,7 @@ int int_tbar_entry(kvft_ctx *ctx, int rank, int ng, int nv, int no, const double
     KV_CHECK(ctx, cudaStreamSynchronize(ctx->stream));
     long long P = (long long)nv * no * (rank == 2 ? (long long)nv * no : 1LL);
     return kv_quad_launch(ctx, 0, ng, P, rank, nv, no, tbar, ti, hti.data(), G, hG.data(), D,
-                          nullptr, nullptr, full, 0.0, out, nullptr);
+                          nullptr, nullptr, full, 0.0, out, nullptr, 0);
 }
 
 int int_tbar_single_entry(kvft_ctx *ctx, int rank, int ng, int ig, int nv, int no,
@@ -410,7 +433,7 @@ int kv_int_tbar(kvft_ctx *ctx, int ng, size_t P, const double *tbar, const doubl
                                   cudaMemcpyDeviceToHost, ctx->stream));
     KV_CHECK(ctx, cudaStreamSynchronize(ctx->stream));
     return kv_quad_launch(ctx, 0, ng, (long long)P, rank, nv, no, tbar, ti, hti.data(), G,
-                          hG.data(), D, eps_v, eps_o, full, 0.0, out, nullptr);
+                          hG.data(), D, eps_v, eps_o, full, 0.0, out, nullptr, 0);
 }
 
 extern "C" {

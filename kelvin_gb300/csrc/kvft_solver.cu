@@ -19,7 +19,7 @@
 int kv_quad_launch(kvft_ctx *ctx, int mode, int ng, long long P, int rank, int nv, int no,
                    const double *tbar, const double *ti, const double *hti, const double *G,
                    const double *hG, const double *D, const double *ev, const double *eo,
-                   int full, double alpha, double *out, double *res);
+                   int full, double alpha, double *out, double *res, int spin_half = 0);
 int kv_quad_single(kvft_ctx *ctx, int ng, int ig, long long P, int rank, int nv, int no,
                    const double *tbar, const double *ti, const double *G, const double *D,
                    const double *ev, const double *eo, double *out);
@@ -279,9 +279,10 @@ int integrate(kvft_solver *s, int mode, double damp, const double *t1b, const do
     KV_TRY(kv_quad_launch(s->ctx, mode, s->ng, s->s1(), 1, s->nv, s->no, t1b, s->ti,
                           s->hti.data(), s->G, s->hG.data(), s->D1, s->eps, s->eps, 0, damp, o1,
                           r1));
+    // the damped update skips the zero spin blocks of T2 (they stay zero)
     return kv_quad_launch(s->ctx, mode, s->ng, s->s2(), 2, s->nv, s->no, t2b, s->ti,
                           s->hti.data(), s->G, s->hG.data(), s->D2, s->eps, s->eps, 0, damp, o2,
-                          r2);
+                          r2, s->spin_on ? s->spin_half : 0);
 }
 
 int read_scalars(kvft_solver *s, int count, double *h) {
@@ -512,7 +513,7 @@ int kvft_solver_step(kvft_solver *s, double damp, double *energy, double *res) {
     // integrate + damp in place: T <- damp T + (1-damp) int(tbar)
     KV_TRY(integrate(s, 1, damp, s->T1b, s->T2b, s->T1, s->T2, s->dsc + 0, s->dsc + 2));
     KV_TRY(kv_energy(ctx, s->ng, s->nv, s->no, s->T1, s->T2, s->F[1], s->I[5], s->g, s->beta, 1,
-                     s->dsc + 4));
+                     s->dsc + 4, s->spin_on ? s->spin_half : 0));
     double h[5];
     KV_TRY(read_scalars(s, 5, h));
     const double res1 = std::sqrt(h[0]) / s->nl1;
@@ -540,7 +541,7 @@ int kvft_solver_run(kvft_solver *s, const kvft_solve_opts *o, kvft_result *r) {
         KV_TRY(integrate(s, 0, 0.0, s->T1b, s->T2b, s->T1, s->T2, nullptr, nullptr));
     }
     KV_TRY(kv_energy(ctx, s->ng, s->nv, s->no, s->T1, s->T2, s->F[1], s->I[5], s->g, s->beta, 0,
-                     s->dsc + 6));
+                     s->dsc + 6, s->spin_on ? s->spin_half : 0));
     double h[7];
     KV_TRY(read_scalars(s, 7, h));
     r->e_guess = h[6];
@@ -638,7 +639,7 @@ int kvft_solver_run_point(kvft_solver *s, const kvft_solve_opts *o, kvft_result 
         if (!conv) all_conv = 0;
     }
     KV_TRY(kv_energy(ctx, s->ng, s->nv, s->no, s->T1, s->T2, s->F[1], s->I[5], s->g, s->beta, 1,
-                     s->dsc + 4));
+                     s->dsc + 4, s->spin_on ? s->spin_half : 0));
     double h[5];
     KV_TRY(read_scalars(s, 5, h));
     r->omega_cc = h[4];

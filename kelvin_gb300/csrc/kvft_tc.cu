@@ -1283,9 +1283,10 @@ int gemm_tc_run(kvft_ctx *ctx, int M, int N, int K, int batch, double alpha, con
     const int S = std::min(D - 1, MAXS);
     // D >= 4: three to six levels, FP32 pairs, TN = 64, and 32-deep k-blocks
     // (six digit planes per stage); D <= 3: 64-deep k-blocks, so that every
-    // TMA box row is a full 128-byte line
+    // TMA box row is a full 128-byte line, and TN = 128 unless C has at most
+    // 64 columns (then 64-wide tiles keep all eight epilogue warps busy)
     const bool ff = D >= 4;
-    const int tn = ff ? 64 : 128;
+    const int tn = (ff || N <= 64) ? 64 : 128;
     const int kb = ff ? 32 : 64;
     const int nbA = A.bst ? batch : 1, nbB = B.bst ? batch : 1;
     Packed pa, pb;
@@ -1339,8 +1340,12 @@ int gemm_tc_run(kvft_ctx *ctx, int M, int N, int K, int batch, double alpha, con
     p.C = C;
     p.err = ctx->dflag;
     switch (D) {
-    case 2: return launch_tc<128, false, 64, 2>(ctx, ma, mb, p);
-    case 3: return launch_tc<128, false, 64, 3>(ctx, ma, mb, p);
+    case 2:
+        return tn == 64 ? launch_tc<64, false, 64, 2>(ctx, ma, mb, p)
+                        : launch_tc<128, false, 64, 2>(ctx, ma, mb, p);
+    case 3:
+        return tn == 64 ? launch_tc<64, false, 64, 3>(ctx, ma, mb, p)
+                        : launch_tc<128, false, 64, 3>(ctx, ma, mb, p);
     case 4: return launch_tc<64, true, 32, 4>(ctx, ma, mb, p);
     case 5: return launch_tc<64, true, 32, 5>(ctx, ma, mb, p);
     case 6: return launch_tc<64, true, 32, 6>(ctx, ma, mb, p);
@@ -1401,7 +1406,7 @@ extern "C" int kvft_gemm(kvft_ctx *ctx, int M, int N, int K, int batch, int prec
     KMat a{A, kidx1(M, K), kidx1(K, 1), (long long)M * K};
     KMat b{B, kidx1(K, N), kidx1(N, 1), (long long)K * N};
     KOut c{C, kidx1(M, N), kidx1(N, 1), (long long)M * N};
-    kv_gemm_prof_set(ctx, M, N, K, batch);
+    kv_gemm_prof_set(ctx, M, N, K, batch, batch, batch, 0.0, precision != KVFT_PREC_FP64);
     int st;
     if (precision == KVFT_PREC_FP64)
         st = kv_gemm_f64(ctx, M, N, K, batch, 1.0, a, b, 0.0, c);

@@ -96,6 +96,20 @@ def test_tc_gemm_short_k(ctx, K, digits):
     assert not C[:, 5, :].any() and not C[:, :, 7].any()
 
 
+# Few output columns after the orientation swap (C's contiguous index on the
+# tile rows, the short extent on the columns): 64-wide tiles at two and three
+# digit levels, with one or several K chunks.
+@pytest.mark.parametrize("M,N,K,batch", [(57, 3000, 114, 2), (40, 2000, 600, 1),
+                                         (64, 1000, 2500, 1), (9, 5000, 57, 3)])
+@pytest.mark.parametrize("digits", [2, 3])
+def test_tc_gemm_narrow_tiles(ctx, M, N, K, batch, digits):
+    rng = numpy.random.default_rng(M + N + K + digits)
+    A = rng.standard_normal((batch, M, K)) * numpy.exp(rng.standard_normal((batch, M, 1)))
+    B = rng.standard_normal((batch, K, N))
+    C = gemm(ctx, A, B, _lib.PREC_FP64_TC, digits)
+    assert normwise(C, A, B) < TOL[digits] * max(1.0, (256 / K) ** 0.5)
+
+
 @pytest.mark.parametrize("digits", [2, 3, 4, 5, 6, 7])
 def test_tc_gemm_every_digit_count(ctx, digits):
     """Each digit count is its own kernel instance (levels fixed at compile
