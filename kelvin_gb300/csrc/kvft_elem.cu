@@ -31,6 +31,54 @@ __device__ __forceinline__ void pair_of(int x, int n, int &p, int &q) {
     q = x - pair_start(p, n) + p + 1;
 }
 
+// Order of the pairs p < q over n orbitals.  h = 0: row-major triangle
+// (x = pair_start(p, n) + q - p - 1).  h > 0 (spin blocks, n = 2h): the
+// alpha-alpha pairs (triangle over [0, h)), then the alpha-beta pairs
+// (p * h + q - h), then the beta-beta pairs (triangle over [h, 2h)), so each
+// pair spin type is one contiguous range and a ladder contraction, nonzero
+// only between pairs of one type, splits into three block products.
+struct PairOrder {
+    int n, h;
+    __device__ __forceinline__ int index(int p, int q) const {
+        if (!h) return pair_start(p, n) + q - p - 1;
+        const int paa = h * (h - 1) / 2;
+        if (q < h) return pair_start(p, h) + q - p - 1;
+        if (p < h) return paa + p * h + (q - h);
+        return paa + h * h + pair_start(p - h, h) + q - p - 1;
+    }
+    __device__ __forceinline__ void decode(int x, int &p, int &q) const {
+        if (!h) {
+            pair_of(x, n, p, q);
+            return;
+        }
+        const int paa = h * (h - 1) / 2;
+        if (x < paa) {
+            pair_of(x, h, p, q);
+            return;
+        }
+        x -= paa;
+        if (x < h * h) {
+            p = x / h;
+            q = h + x % h;
+            return;
+        }
+        pair_of(x - h * h, h, p, q);
+        p += h;
+        q += h;
+    }
+    // index range [lo, hi) of the pairs of spin type t = s_p + s_q
+    __device__ __forceinline__ void range(int t, int &lo, int &hi) const {
+        if (!h) {
+            lo = 0;
+            hi = n * (n - 1) / 2;
+            return;
+        }
+        const int paa = h * (h - 1) / 2;
+        lo = t == 0 ? 0 : (t == 1 ? paa : paa + h * h);
+        hi = t == 0 ? paa : (t == 1 ? paa + h * h : 2 * paa + h * h);
+    }
+};
+
 // One block per (batch, i0, i1, chunk of AX_CHUNK (i2, i3) positions); its
 // threads walk (i2, i3), the innermost index fastest, so only a 32-bit
 // division per element remains.  GB300 issues about two FP64 operations per
@@ -73,7 +121,7 @@ axpby4_kernel(long long nblk, Dims4 g, double alpha, const double *__restrict__ 
 // (y, a, b), threads over (i, j).  The rows c t1[a,:] and c t1[b,:] are formed
 // once per block in shared memory, so each element costs two FP64 FMAs.
 __global__ void __launch_bounds__(256)
-make_tau_kernel(long long nblk, int nv, int no, const double *__restrict__ t1,
+make_tau_kernel(long long nblk, int nv, int no, int sh, const double *__restrict__ t1,
                 const double *__restrict__ t2, double c, double *__restrict__ out) {
     extern __shared__ double cab[];                  // [2][no]: c t1[a,:], c t1[b,:]
     const int oo = no * no;
@@ -90,8 +138,11 @@ make_tau_kernel(long long nblk, int nv, int no, const double *__restrict__ t1,
         }
         __syncthreads();
         const long long base = blk * oo;
+        // spin blocks (sh > 0): only the spin-conserving (i, j) are read later
+        const int sab = (a >= sh) + (b >= sh);
         for (int e = threadIdx.x; e < oo; e += blockDim.x) {
             const int i = e / no, j = e % no;
+            if (sh && (i >= sh) + (j >= sh) != sab) continue;
             out[base + e] = fma(cab[i], ub[j], fma(-cab[no + i], ua[j], t2[base + e]));
         }
     }
@@ -102,8 +153,8 @@ make_tau_kernel(long long nblk, int nv, int no, const double *__restrict__ t1,
 // product.  32 x 32 (f, n) tiles go through shared memory so the reads are
 // coalesced along n and the writes along f.
 __global__ void __launch_bounds__(256)
-wmbej_tmp_kernel(int nv, int no, const double *__restrict__ t1, const double *__restrict__ t2,
-                 double *__restrict__ out) {
+wmbej_tmp_kernel(int nv, int no, int sh, const double *__restrict__ t1,
+                 const double *__restrict__ t2, double *__restrict__ out) {
     __shared__ double tile[32][33];
     const int tx = threadIdx.x % 32, ty = threadIdx.x / 32;
     const int ntn = (no + 31) / 32;
@@ -111,20 +162,32 @@ wmbej_tmp_kernel(int nv, int no, const double *__restrict__ t1, const double *__
     const long long y = blockIdx.z;
     const long long oo = (long long)no * no;
     const double *u = t1 + y * nv * no;
+    // spin blocks (sh > 0): only elements with s_f + s_b = s_j + s_n are read
+    // later; the spin sets of the tile's f and n ranges
+    const int fs0 = f0 >= sh, fs1 = min(f0 + 31, nv - 1) >= sh;
+    const int ns0 = n0 >= sh, ns1 = min(n0 + 31, no - 1) >= sh;
+    auto keep = [&](int f, int b, int j, int n) {
+        return !sh || (f >= sh) + (b >= sh) == (j >= sh) + (n >= sh);
+    };
     for (int bj = blockIdx.y; bj < nv * no; bj += gridDim.y) {
         const int b = bj / no, j = bj % no;
+        if (sh) {
+            // s_f - s_n must equal s_j - s_b for some f, n of the tile
+            const int d = (j >= sh) - (b >= sh);
+            if (fs1 - ns0 < d || fs0 - ns1 > d) continue;      // block-uniform
+        }
         __syncthreads();
 #pragma unroll
         for (int i = 0; i < 4; i++) {
             const int f = f0 + ty + 8 * i, n = n0 + tx;
-            if (f < nv && n < no)
+            if (f < nv && n < no && keep(f, b, j, n))
                 tile[ty + 8 * i][tx] = t2[((y * nv + f) * nv + b) * oo + (long long)j * no + n];
         }
         __syncthreads();
 #pragma unroll
         for (int i = 0; i < 4; i++) {
             const int n = n0 + ty + 8 * i, f = f0 + tx;
-            if (f < nv && n < no)
+            if (f < nv && n < no && keep(f, b, j, n))
                 out[(((y * nv + b) * no + j) * no + n) * nv + f] =
                     0.5 * tile[tx][ty + 8 * i] + u[f * no + j] * u[b * no + n];
         }
@@ -145,9 +208,10 @@ wmbej_tmp_kernel(int nv, int no, const double *__restrict__ t1, const double *__
 // reduction and no pre-seeded T2.
 template <int FS, bool SEED>
 __global__ void __launch_bounds__(256)
-assemble_t2_kernel(int nv, int no, double fac, const double *__restrict__ Z,
+assemble_t2_kernel(int nv, int no, int sh, double fac, const double *__restrict__ Z,
                    const double *__restrict__ Lc, const double *__restrict__ seed,
                    double *__restrict__ T2) {
+    const PairOrder ov{nv, sh}, oo_{no, sh};
     __shared__ double qa[32][33], qb[32][33];
     const int tx = threadIdx.x % 32, ty = threadIdx.x / 32;
     const int nt = (no + 31) / 32;
@@ -163,7 +227,8 @@ assemble_t2_kernel(int nv, int no, double fac, const double *__restrict__ Z,
     const long long oo = (long long)no * no, s4 = (long long)nv * nv * oo;
     for (int pab = blockIdx.y; pab < pv; pab += gridDim.y) {
         int a, b;
-        pair_of(pab, nv, a, b);
+        ov.decode(pab, a, b);
+        const int tab = (a >= sh) + (b >= sh);
         const long long oab = y * s4 + ((long long)a * nv + b) * oo;
         const long long oba = y * s4 + ((long long)b * nv + a) * oo;
         const double *L = Lc ? Lc + (y * pv + pab) * (long long)po : nullptr;
@@ -178,9 +243,11 @@ assemble_t2_kernel(int nv, int no, double fac, const double *__restrict__ Z,
             qb[r][tx] = (i < no && j < no) ? Z[oab + i * no + j] - Z[oba + i * no + j] : 0.0;
         }
         __syncthreads();
+        // L over (i < j); with spin blocks it vanishes between pair types
         auto ladder = [&](int i, int j) -> double {
             if (!L || i == j) return 0.0;
-            return i < j ? L[pair_start(i, no) + j - i - 1] : -L[pair_start(j, no) + i - j - 1];
+            if (sh && (i >= sh) + (j >= sh) != tab) return 0.0;
+            return i < j ? L[oo_.index(i, j)] : -L[oo_.index(j, i)];
         };
         const long long sab = ((long long)a * nv + b) * oo, sba = ((long long)b * nv + a) * oo;
         auto put = [&](int x, double R) {
@@ -223,20 +290,24 @@ __global__ void bcast_kernel(long long total, long long count,
 // tau_c[y][(e<f)][(i<j)] = t2[y,e,f,i,j] + t1[y,e,i] t1[y,f,j] - t1[y,f,i] t1[y,e,j];
 // one block per (y, e<f), threads over the (i<j) pairs
 __global__ void __launch_bounds__(256)
-make_tau_pairs_kernel(long long nblk, int nv, int no, int pv, int po,
+make_tau_pairs_kernel(long long nblk, int nv, int no, int pv, int po, int sh,
                       const double *__restrict__ t1, const double *__restrict__ t2,
                       double *__restrict__ out) {
     const long long s4 = (long long)nv * nv * no * no;
+    const PairOrder ov{nv, sh}, oo_{no, sh};
     for (long long blk = blockIdx.x; blk < nblk; blk += gridDim.x) {
         const long long y = blk / pv;
         int e, f;
-        pair_of((int)(blk - y * pv), nv, e, f);
+        ov.decode((int)(blk - y * pv), e, f);
         const double *u = t1 + y * nv * no;
         const double *src = t2 + y * s4 + ((long long)e * nv + f) * no * no;
         double *dst = out + blk * po;
-        for (int x = threadIdx.x; x < po; x += blockDim.x) {
+        // with spin blocks only the (i < j) of the same pair type are read
+        int lo = 0, hi = po;
+        if (sh) oo_.range((e >= sh) + (f >= sh), lo, hi);
+        for (int x = lo + threadIdx.x; x < hi; x += blockDim.x) {
             int i, j;
-            pair_of(x, no, i, j);
+            oo_.decode(x, i, j);
             dst[x] = src[i * no + j] + u[e * no + i] * u[f * no + j] - u[f * no + i] * u[e * no + j];
         }
     }
@@ -250,6 +321,7 @@ struct PairGather {
     const double *B;             // per-batch terms c1 B[p,q,r,s] + c2 B[with strides sb2]
     long long sb1[4], sb2[4], bst;
     double c1, c2;
+    int sh;                      // spin-sorted pair order; only same-type pairs written
 };
 
 // one block per (batch, p<q), threads over the (a<b) pairs
@@ -258,15 +330,18 @@ pair_gather_kernel(long long nblk, PairGather g, double *__restrict__ out) {
     for (long long blk = blockIdx.x; blk < nblk; blk += gridDim.x) {
         const long long y = blk / g.P1;
         int p, q;
-        pair_of((int)(blk - y * g.P1), g.n1, p, q);
+        const PairOrder o1{g.n1, g.sh}, o2{g.n2, g.sh};
+        o1.decode((int)(blk - y * g.P1), p, q);
         const double *Ar = g.A ? g.A + p * g.sa[0] + q * g.sa[1] : nullptr;
         const double *Bb = g.B ? g.B + y * g.bst : nullptr;
         const double *B1 = Bb ? Bb + p * g.sb1[0] + q * g.sb1[1] : nullptr;
         const double *B2 = Bb ? Bb + p * g.sb2[0] + q * g.sb2[1] : nullptr;
         double *o = out + blk * g.P2;
-        for (int x = threadIdx.x; x < g.P2; x += blockDim.x) {
+        int lo = 0, hi = g.P2;
+        if (g.sh) o2.range((p >= g.sh) + (q >= g.sh), lo, hi);
+        for (int x = lo + threadIdx.x; x < hi; x += blockDim.x) {
             int a, b;
-            pair_of(x, g.n2, a, b);
+            o2.decode(x, a, b);
             double v = 0.0;
             if (Ar) v = g.ca * Ar[a * g.sa[2] + b * g.sa[3]];
             if (Bb) {
@@ -308,30 +383,31 @@ int kv_axpby4(kvft_ctx *ctx, int batch, const int dims[4], double alpha,
 }
 
 int kv_make_tau(kvft_ctx *ctx, int batch, int nv, int no, const double *t1,
-                const double *t2, double c, double *out) {
+                const double *t2, double c, double *out, int spin_half) {
     long long total = (long long)batch * nv * nv * no * no;
     if (total == 0) return KVFT_OK;
     KvProfScope prof(ctx, KV_CAT_ELEM, 16.0 * total);
     const long long nblk = (long long)batch * nv * nv;
     if (no > 3072) return kv_fail(ctx, KVFT_EINVAL, "make_tau: more than 3072 occupied orbitals");
     make_tau_kernel<<<(unsigned)std::min(nblk, (long long)ctx->sm_count * 16), 256,
-                      2 * no * sizeof(double), ctx->stream>>>(nblk, nv, no, t1, t2, c, out);
+                      2 * no * sizeof(double), ctx->stream>>>(nblk, nv, no, spin_half, t1, t2,
+                                                              c, out);
     return kv_launch_check(ctx, "make_tau");
 }
 
 int kv_make_wmbej_tmp(kvft_ctx *ctx, int batch, int nv, int no,
-                      const double *t1, const double *t2, double *out) {
+                      const double *t1, const double *t2, double *out, int spin_half) {
     long long total = (long long)batch * nv * nv * no * no;
     if (total == 0) return KVFT_OK;
     if (batch > 65535) return kv_fail(ctx, KVFT_EINVAL, "wmbej_tmp: batch too large");
     KvProfScope prof(ctx, KV_CAT_ELEM, 16.0 * total);
     const dim3 grid(((nv + 31) / 32) * ((no + 31) / 32), std::min(nv * no, 65535), batch);
-    wmbej_tmp_kernel<<<grid, 256, 0, ctx->stream>>>(nv, no, t1, t2, out);
+    wmbej_tmp_kernel<<<grid, 256, 0, ctx->stream>>>(nv, no, spin_half, t1, t2, out);
     return kv_launch_check(ctx, "wmbej_tmp");
 }
 
 int kv_assemble_t2(kvft_ctx *ctx, int batch, int nv, int no, double fac, const double *Z,
-                   const double *Lc, double *T2, const double *seed) {
+                   const double *Lc, double *T2, const double *seed, int spin_half) {
     const long long oo = (long long)no * no, total = (long long)batch * nv * nv * oo;
     if (total == 0) return KVFT_OK;
     if (seed) {
@@ -346,8 +422,10 @@ int kv_assemble_t2(kvft_ctx *ctx, int batch, int nv, int no, double fac, const d
     const int nt = (no + 31) / 32;
     const int pv = nv * (nv - 1) / 2;
     const dim3 grid(nt * (nt + 1) / 2, std::min(pv, 65535), batch);
+    const int sh = (nv == no && nv == 2 * spin_half) ? spin_half : 0;
 #define KV_ASM(fs_, seed_)                                                                  \
-    assemble_t2_kernel<fs_, seed_><<<grid, 256, 0, ctx->stream>>>(nv, no, fac, Z, Lc, seed, T2)
+    assemble_t2_kernel<fs_, seed_><<<grid, 256, 0, ctx->stream>>>(nv, no, sh, fac, Z, Lc, seed, \
+                                                                  T2)
     const int fs = fac == 1.0 ? 1 : (fac == -1.0 ? 2 : 0);
     if (seed) {
         if (fs == 1) KV_ASM(1, true);
@@ -363,21 +441,24 @@ int kv_assemble_t2(kvft_ctx *ctx, int batch, int nv, int no, double fac, const d
 }
 
 int kv_make_tau_pairs(kvft_ctx *ctx, int batch, int nv, int no, const double *t1,
-                      const double *t2, double *out) {
+                      const double *t2, double *out, int spin_half) {
+    const int sh = (nv == no && nv == 2 * spin_half) ? spin_half : 0;
     const int pv = nv * (nv - 1) / 2, po = no * (no - 1) / 2;
     long long total = (long long)batch * pv * po;
     if (total == 0) return KVFT_OK;
     KvProfScope prof(ctx, KV_CAT_ELEM, 16.0 * total);
     const long long nblk = (long long)batch * pv;
     make_tau_pairs_kernel<<<(unsigned)std::min(nblk, (long long)ctx->sm_count * 16), 256, 0,
-                            ctx->stream>>>(nblk, nv, no, pv, po, t1, t2, out);
+                            ctx->stream>>>(nblk, nv, no, pv, po, sh, t1, t2, out);
     return kv_launch_check(ctx, "make_tau_pairs");
 }
 
 int kv_pair_gather(kvft_ctx *ctx, int batch, int n1, int n2, const double *A,
                    const long long sa[4], double ca, const double *B, const long long sb1[4],
-                   double c1, const long long sb2[4], double c2, long long bst, double *out) {
+                   double c1, const long long sb2[4], double c2, long long bst, double *out,
+                   int spin_half) {
     PairGather g;
+    g.sh = (n1 == n2 && n1 == 2 * spin_half) ? spin_half : 0;
     g.n1 = n1;
     g.n2 = n2;
     g.P1 = n1 * (n1 - 1) / 2;

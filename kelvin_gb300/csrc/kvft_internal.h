@@ -176,25 +176,30 @@ int kv_axpby4(kvft_ctx *ctx, int batch, const int dims[4], double alpha,
               double beta, double *dst, const long long ds[4], long long dbst);
 
 // tau-type amplitudes: out = t2 + c * (t1[a,i] t1[b,j] - t1[b,i] t1[a,j])
+// (spin_half > 0: the spin-conserving elements only)
 int kv_make_tau(kvft_ctx *ctx, int batch, int nv, int no, const double *t1,
-                const double *t2, double c, double *out);
-// tmp[b,j,n,f] = 0.5 t2[f,b,j,n] + t1[f,j] t1[b,n]
+                const double *t2, double c, double *out, int spin_half = 0);
+// tmp[b,j,n,f] = 0.5 t2[f,b,j,n] + t1[f,j] t1[b,n] (spin_half > 0: the
+// spin-conserving elements only)
 int kv_make_wmbej_tmp(kvft_ctx *ctx, int batch, int nv, int no,
-                      const double *t1, const double *t2, double *out);
+                      const double *t1, const double *t2, double *out, int spin_half = 0);
 // T2 += fac (1 - P(ab))(1 - P(ij)) (Z + L), L = the ladder sum stored over
 // a < b, i < j (Lc, or nullptr), zero elsewhere.  With a seed (a
 // tau-independent [a][b][i][j] block) T2 is written, not updated:
 // T2 = -seed + fac (...).
 int kv_assemble_t2(kvft_ctx *ctx, int batch, int nv, int no, double fac, const double *Z,
-                   const double *Lc, double *T2, const double *seed = nullptr);
+                   const double *Lc, double *T2, const double *seed = nullptr,
+                   int spin_half = 0);
 // Antisymmetric pair compression (pairs p < q, x = p(2n-p-1)/2 + q-p-1):
 // tau_c[y][(e<f)][(i<j)] from t1, t2
+// (spin_half > 0: spin-sorted pair order, only pairs of one spin type linked)
 int kv_make_tau_pairs(kvft_ctx *ctx, int batch, int nv, int no, const double *t1,
-                      const double *t2, double *out);
+                      const double *t2, double *out, int spin_half = 0);
 // out[y][(p<q) over n1][(r<s) over n2] = ca A[p,q,r,s] + c1 B[y][p,q,r,s] + c2 B[y](sb2)
 int kv_pair_gather(kvft_ctx *ctx, int batch, int n1, int n2, const double *A,
                    const long long sa[4], double ca, const double *B, const long long sb1[4],
-                   double c1, const long long sb2[4], double c2, long long bst, double *out);
+                   double c1, const long long sb2[4], double c2, long long bst, double *out,
+                   int spin_half = 0);
 // broadcast a tau-independent block over the batch: dst[b] = src
 int kv_bcast(kvft_ctx *ctx, int batch, size_t count, const double *src,
              double *dst);

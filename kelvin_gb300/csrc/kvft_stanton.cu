@@ -208,7 +208,9 @@ int kv_stanton(kvft_ctx *ctx, int nb, int nv, int no, const double *const F[4],
     };
 
     // ---- tau-tilde (tau itself is only needed pair-compressed) --------------
-    KV_TRY(kv_make_tau(ctx, B, nv, no, t1, t2, 0.5, w.ttau));
+    // tau-tilde feeds only F_ae and F_mi, whose contractions read its
+    // spin-conserving blocks alone
+    KV_TRY(kv_make_tau(ctx, B, nv, no, t1, t2, 0.5, w.ttau, sh));
 
     // ---- F_ae ------------------------------------------------------------
     KV_TRY(kv_bcast(ctx, B, vv, Fvv, w.Fae));
@@ -221,11 +223,17 @@ int kv_stanton(kvft_ctx *ctx, int nb, int nv, int no, const double *const F[4],
                    MAI(vovv, X2(nv, o * vv, nv, 1), X2(no, vv, nv, v)),
                    MA(t1, X2(no, 1, nv, o), X1(B, vo), 0), 1.0,
                    MO(w.Fae, X2(nv, v, nv, 1), X1(B, vv), 0)));
-    // -1/2 ttau[a,f,m,n] oovv[m,n,e,f]
-    KV_TRY(kv_gemm(ctx, nv, nv, nv * no * no, B, -0.5,
-                   MA(w.ttau, X1(nv, vo2), X3(nv, oo, no, o, no, 1), v2o2),
-                   MAI(oovv, X3(nv, 1, no, o * vv, no, vv), X1(nv, v)), 1.0,
-                   MO(w.Fae, X1(nv, v), X1(nv, 1), vv)));
+    // -1/2 ttau[a,f,m,n] oovv[m,n,e,f]; spins a f m n e
+    KV_TRY(sgemm(nv, nv, nv * no * no, B, -0.5,
+                 MA(w.ttau, X1(nv, vo2), X3(nv, oo, no, o, no, 1), v2o2),
+                 MAI(oovv, X3(nv, 1, no, o * vv, no, vv), X1(nv, v)), 1.0,
+                 MO(w.Fae, X1(nv, v), X1(nv, 1), vv),
+                 Slots{{{0, 0, 2}, {2, 0, 2}}, {{0, 1, 0}, {1, 0, 0}}, {{0, 1, 1}, {1, 0, 1}},
+                       {{0, 1, 2}, {1, 0, 2}}, {{1, 1, 2}, {2, 1, 2}}},
+                 [](unsigned m) {
+                     return sp(m, 0) + sp(m, 1) == sp(m, 2) + sp(m, 3) &&
+                            sp(m, 2) + sp(m, 3) == sp(m, 4) + sp(m, 1);
+                 }, 0));
 
     // ---- F_mi ------------------------------------------------------------
     KV_TRY(kv_bcast(ctx, B, oo, Foo, w.Fmi));
@@ -238,11 +246,17 @@ int kv_stanton(kvft_ctx *ctx, int nb, int nv, int no, const double *const F[4],
                    MAI(ooov, X2(no, oo * v, no, v), X2(no, vo, nv, 1)),
                    MA(t1, X2(no, 1, nv, o), X1(B, vo), 0), 1.0,
                    MO(w.Fmi, X2(no, o, no, 1), X1(B, oo), 0)));
-    // +1/2 oovv[m,n,e,f] ttau[e,f,i,n]
-    KV_TRY(kv_gemm(ctx, no, no, no * nv * nv, B, 0.5,
-                   MAI(oovv, X1(no, o * vv), X3(no, vv, nv, v, nv, 1)),
-                   MA(w.ttau, X3(no, 1, nv, vo2, nv, oo), X1(no, o), v2o2), 1.0,
-                   MO(w.Fmi, X1(no, o), X1(no, 1), oo)));
+    // +1/2 oovv[m,n,e,f] ttau[e,f,i,n]; spins m n e f i
+    KV_TRY(sgemm(no, no, no * nv * nv, B, 0.5,
+                 MAI(oovv, X1(no, o * vv), X3(no, vv, nv, v, nv, 1)),
+                 MA(w.ttau, X3(no, 1, nv, vo2, nv, oo), X1(no, o), v2o2), 1.0,
+                 MO(w.Fmi, X1(no, o), X1(no, 1), oo),
+                 Slots{{{0, 0, 2}, {2, 0, 2}}, {{0, 1, 0}, {1, 0, 0}}, {{0, 1, 1}, {1, 0, 1}},
+                       {{0, 1, 2}, {1, 0, 2}}, {{1, 1, 2}, {2, 1, 2}}},
+                 [](unsigned m) {
+                     return sp(m, 0) + sp(m, 1) == sp(m, 2) + sp(m, 3) &&
+                            sp(m, 2) + sp(m, 3) == sp(m, 4) + sp(m, 1);
+                 }, 0));
 
     // ---- F_me ------------------------------------------------------------
     KV_TRY(kv_bcast(ctx, B, vo, Fov, w.Fme));
@@ -258,24 +272,41 @@ int kv_stanton(kvft_ctx *ctx, int nb, int nv, int no, const double *const F[4],
                    MA(t1, X1(nv, o), X1(no, 1), vo), 1.0, T1o));
     KV_TRY(kv_gemm(ctx, nv, no, no, B, -fac, MA(t1, X1(nv, o), X1(no, 1), vo),
                    MA(w.Fmi, X1(no, o), X1(no, 1), oo), 1.0, T1o));
-    // t2[a,e,i,m] Fme[m,e]   (M=(a,i), K=(m,e), N=1)
-    KV_TRY(kv_gemm(ctx, nv * no, 1, no * nv, B, fac,
-                   MA(t2, X2(nv, vo2, no, o), X2(no, 1, nv, oo), v2o2),
-                   MA(w.Fme, X2(no, v, nv, 1), one, vo), 1.0,
-                   MO(T1, X2(nv, o, no, 1), one, vo)));
+    // t2[a,e,i,m] Fme[m,e]   (M=(a,i), K=(m,e), N=1); spins a i m e
+    KV_TRY(sgemm(nv * no, 1, no * nv, B, fac,
+                 MA(t2, X2(nv, vo2, no, o), X2(no, 1, nv, oo), v2o2),
+                 MA(w.Fme, X2(no, v, nv, 1), one, vo), 1.0,
+                 MO(T1, X2(nv, o, no, 1), one, vo),
+                 Slots{{{0, 0, 1}, {2, 0, 1}}, {{0, 0, 2}, {2, 0, 2}}, {{0, 1, 1}, {1, 0, 1}},
+                       {{0, 1, 2}, {1, 0, 2}}},
+                 [](unsigned m) {
+                     return sp(m, 0) + sp(m, 3) == sp(m, 1) + sp(m, 2) && sp(m, 2) == sp(m, 3);
+                 }, 0));
     // - vovo[a,n,f,i] t1[f,n]   (M=(a,i), K=(n,f), N=tau)
     KV_TRY(kv_gemm(ctx, nv * no, B, no * nv, 1, -fac,
                    MAI(vovo, X2(nv, vo2, no, 1), X2(no, vo, nv, o)),
                    MA(t1, X2(no, 1, nv, o), X1(B, vo), 0), 1.0,
                    MO(T1, X2(nv, o, no, 1), X1(B, vo), 0)));
-    // +1/2 vovv[a,m,e,f] t2[e,f,i,m]
-    KV_TRY(kv_gemm(ctx, nv, no, no * nv * nv, B, 0.5 * fac,
-                   MAI(vovv, X1(nv, o * vv), X3(no, vv, nv, v, nv, 1)),
-                   MA(t2, X3(no, 1, nv, vo2, nv, oo), X1(no, o), v2o2), 1.0, T1o));
-    // +1/2 t2[a,e,m,n] ooov[n,m,i,e]
-    KV_TRY(kv_gemm(ctx, nv, no, nv * no * no, B, 0.5 * fac,
-                   MA(t2, X1(nv, vo2), X3(nv, oo, no, o, no, 1), v2o2),
-                   MAI(ooov, X3(nv, 1, no, vo, no, oo * v), X1(no, v)), 1.0, T1o));
+    // +1/2 vovv[a,m,e,f] t2[e,f,i,m]; spins a m e f i
+    KV_TRY(sgemm(nv, no, no * nv * nv, B, 0.5 * fac,
+                 MAI(vovv, X1(nv, o * vv), X3(no, vv, nv, v, nv, 1)),
+                 MA(t2, X3(no, 1, nv, vo2, nv, oo), X1(no, o), v2o2), 1.0, T1o,
+                 Slots{{{0, 0, 2}, {2, 0, 2}}, {{0, 1, 0}, {1, 0, 0}}, {{0, 1, 1}, {1, 0, 1}},
+                       {{0, 1, 2}, {1, 0, 2}}, {{1, 1, 2}, {2, 1, 2}}},
+                 [](unsigned m) {
+                     return sp(m, 0) + sp(m, 1) == sp(m, 2) + sp(m, 3) &&
+                            sp(m, 2) + sp(m, 3) == sp(m, 4) + sp(m, 1);
+                 }, 0));
+    // +1/2 t2[a,e,m,n] ooov[n,m,i,e]; spins a e m n i
+    KV_TRY(sgemm(nv, no, nv * no * no, B, 0.5 * fac,
+                 MA(t2, X1(nv, vo2), X3(nv, oo, no, o, no, 1), v2o2),
+                 MAI(ooov, X3(nv, 1, no, vo, no, oo * v), X1(no, v)), 1.0, T1o,
+                 Slots{{{0, 0, 2}, {2, 0, 2}}, {{0, 1, 0}, {1, 0, 0}}, {{0, 1, 1}, {1, 0, 1}},
+                       {{0, 1, 2}, {1, 0, 2}}, {{1, 1, 2}, {2, 1, 2}}},
+                 [](unsigned m) {
+                     return sp(m, 0) + sp(m, 1) == sp(m, 2) + sp(m, 3) &&
+                            sp(m, 3) + sp(m, 2) == sp(m, 4) + sp(m, 1);
+                 }, 0));
 
     // ---- ladder terms over antisymmetric pairs ---------------------------------
     // tau, W'_mnij, W'_abef and <mn||ef> are antisymmetric in each index pair,
@@ -289,43 +320,76 @@ int kv_stanton(kvft_ctx *ctx, int nb, int nv, int no, const double *const F[4],
     const long long pvo = (long long)pv * po, poo = (long long)po * po, pvv = (long long)pv * pv;
     const bool ladders = pv > 0 && po > 0;
     if (ladders) {
-        KV_TRY(kv_make_tau_pairs(ctx, B, nv, no, t1, t2, w.tau));      // tau_c[y][ef][ij]
+        // With spin blocks the pairs are in spin-sorted order and every pair
+        // tensor links only pairs of one spin type (alpha-alpha, alpha-beta,
+        // beta-beta), so each pair contraction runs as three block products
+        // on the diagonal type blocks; the other blocks are neither written
+        // nor read.  ntype = 1 with the whole range otherwise.
+        const long long paa = (long long)sh * (sh - 1) / 2, hh = (long long)sh * sh;
+        const int ntype = sh ? 3 : 1;
+        // first index and count of the type-t pairs (virtual / occupied pairs;
+        // the same ranges when spin-blocked, since then nv = no)
+        auto rlo = [&](int t) -> long long { return sh ? (t == 0 ? 0 : t == 1 ? paa : paa + hh) : 0; };
+        auto rnv = [&](int t) -> int { return sh ? (int)(t == 1 ? hh : paa) : pv; };
+        auto rno = [&](int t) -> int { return sh ? (int)(t == 1 ? hh : paa) : po; };
+        KV_TRY(kv_make_tau_pairs(ctx, B, nv, no, t1, t2, w.tau, sh));  // tau_c[y][ef][ij]
         void *oc = nullptr;
         KV_TRY(kv_scratch(ctx, "oovv_pairs", sizeof(double) * (size_t)po * pv, &oc));
         const long long sov[4] = {o * vv, vv, v, 1};
         KV_TRY(kv_pair_gather(ctx, 1, no, nv, oovv, sov, 1.0, nullptr, nullptr, 0.0, nullptr,
-                              0.0, 0, (double *)oc));
-        // Z[m,n,i,j] = ooov[m,n,i,e] t1[e,j]
-        KV_TRY(kv_gemm(ctx, no * no * no, no, nv, B, 1.0,
-                       MAI(ooov, X3(no, oo * v, no, vo, no, v), X1(nv, 1)),
-                       MA(t1, X1(nv, o), X1(no, 1), vo), 0.0,
-                       MO(w.tmp4, X3(no, o * oo, no, oo, no, o), X1(no, 1), o4)));
+                              0.0, 0, (double *)oc, sh));
+        // Z[m,n,i,j] = ooov[m,n,i,e] t1[e,j]; spins m n i e j (the gather below
+        // reads its spin-conserving elements only)
+        KV_TRY(sgemm(no * no * no, no, nv, B, 1.0,
+                     MAI(ooov, X3(no, oo * v, no, vo, no, v), X1(nv, 1)),
+                     MA(t1, X1(nv, o), X1(no, 1), vo), 0.0,
+                     MO(w.tmp4, X3(no, o * oo, no, oo, no, o), X1(no, 1), o4),
+                     Slots{{{0, 0, 0}, {2, 0, 0}}, {{0, 0, 1}, {2, 0, 1}}, {{0, 0, 2}, {2, 0, 2}},
+                           {{0, 1, 2}, {1, 0, 2}}, {{1, 1, 2}, {2, 1, 2}}},
+                     [](unsigned m) {
+                         return sp(m, 0) + sp(m, 1) == sp(m, 2) + sp(m, 3) && sp(m, 3) == sp(m, 4);
+                     }, -1));
         // W'_c = oooo + Z - Z^(ij)
         const long long s4o[4] = {o * oo, oo, o, 1}, s4t[4] = {o * oo, oo, 1, o};
         KV_TRY(kv_pair_gather(ctx, B, no, no, oooo, s4o, 1.0, w.tmp4, s4o, 1.0, s4t, -1.0, o4,
-                              w.Wmnij));
-        // W'_c += oovv_c tau_c   (M = mn pairs, K = ef pairs, N = (tau, ij pairs))
-        KV_TRY(kv_gemm(ctx, po, B * po, pv, 1, 1.0,
-                       MA((const double *)oc, X1(po, pv), X1(pv, 1), 0),
-                       MA(w.tau, X1(pv, po), X2(B, pvo, po, 1), 0), 1.0,
-                       MO(w.Wmnij, X1(po, po), X2(B, poo, po, 1), 0)));
-        // Lc = tau_c W'_c        (M = ab pairs, K = mn pairs, N = ij pairs)
-        KV_TRY(kv_gemm(ctx, pv, po, po, B, 1.0, MA(w.tau, X1(pv, po), X1(po, 1), pvo),
-                       MA(w.Wmnij, X1(po, po), X1(po, 1), poo), 0.0,
-                       MO(w.Lc, X1(pv, po), X1(po, 1), pvo)));
-        // Y[a,b,e,f] = t1[b,m] vovv[a,m,e,f]   (M=b, K=m, N=(a,e,f))
-        KV_TRY(kv_gemm(ctx, nv, nv * nv * nv, no, B, 1.0,
-                       MA(t1, X1(nv, o), X1(no, 1), vo),
-                       MAI(vovv, X1(no, vv), X3(nv, o * vv, nv, v, nv, 1)), 0.0,
-                       MO(w.tmp4, X1(nv, vv), X3(nv, v * vv, nv, v, nv, 1), v4)));
+                              w.Wmnij, sh));
+        for (int t = 0; t < ntype; t++) {
+            const long long lo = rlo(t);          // lo applies to both pair kinds
+            const int nvt = rnv(t), not_ = rno(t);
+            // W'_c += oovv_c tau_c   (M = mn pairs, K = ef pairs, N = (tau, ij pairs))
+            KV_TRY(kv_gemm(ctx, not_, B * not_, nvt, 1, 1.0,
+                           MA((const double *)oc + lo * pv + lo, X1(not_, pv), X1(nvt, 1), 0),
+                           MA(w.tau + lo * po + lo, X1(nvt, po), X2(B, pvo, not_, 1), 0), 1.0,
+                           MO(w.Wmnij + lo * po + lo, X1(not_, po), X2(B, poo, not_, 1), 0)));
+            // Lc = tau_c W'_c        (M = ab pairs, K = mn pairs, N = ij pairs)
+            KV_TRY(kv_gemm(ctx, nvt, not_, not_, B, 1.0,
+                           MA(w.tau + lo * po + lo, X1(nvt, po), X1(not_, 1), pvo),
+                           MA(w.Wmnij + lo * po + lo, X1(not_, po), X1(not_, 1), poo), 0.0,
+                           MO(w.Lc + lo * po + lo, X1(nvt, po), X1(not_, 1), pvo)));
+        }
+        // Y[a,b,e,f] = t1[b,m] vovv[a,m,e,f]   (M=b, K=m, N=(a,e,f)); spins b m a e f
+        KV_TRY(sgemm(nv, nv * nv * nv, no, B, 1.0,
+                     MA(t1, X1(nv, o), X1(no, 1), vo),
+                     MAI(vovv, X1(no, vv), X3(nv, o * vv, nv, v, nv, 1)), 0.0,
+                     MO(w.tmp4, X1(nv, vv), X3(nv, v * vv, nv, v, nv, 1), v4),
+                     Slots{{{0, 0, 2}, {2, 0, 2}}, {{0, 1, 2}, {1, 0, 2}}, {{1, 1, 0}, {2, 1, 0}},
+                           {{1, 1, 1}, {2, 1, 1}}, {{1, 1, 2}, {2, 1, 2}}},
+                     [](unsigned m) {
+                         return sp(m, 0) == sp(m, 1) && sp(m, 2) + sp(m, 1) == sp(m, 3) + sp(m, 4);
+                     }, -1));
         // W'_abef_c = vvvv - Y + Y^(ab)
         const long long s4v[4] = {v * vv, vv, v, 1}, s4s[4] = {vv, v * vv, v, 1};
         KV_TRY(kv_pair_gather(ctx, B, nv, nv, vvvv, s4v, 1.0, w.tmp4, s4v, -1.0, s4s, 1.0, v4,
-                              w.Wabef));
+                              w.Wabef, sh));
         // Lc += W'_abef_c tau_c   (M = ab pairs, K = ef pairs, N = ij pairs)
-        KV_TRY(kv_gemm(ctx, pv, po, pv, B, 1.0, MA(w.Wabef, X1(pv, pv), X1(pv, 1), pvv),
-                       MA(w.tau, X1(pv, po), X1(po, 1), pvo), 1.0,
-                       MO(w.Lc, X1(pv, po), X1(po, 1), pvo)));
+        for (int t = 0; t < ntype; t++) {
+            const long long lo = rlo(t);
+            const int nvt = rnv(t), not_ = rno(t);
+            KV_TRY(kv_gemm(ctx, nvt, not_, nvt, B, 1.0,
+                           MA(w.Wabef + lo * pv + lo, X1(nvt, pv), X1(nvt, 1), pvv),
+                           MA(w.tau + lo * po + lo, X1(nvt, po), X1(not_, 1), pvo), 1.0,
+                           MO(w.Lc + lo * po + lo, X1(nvt, po), X1(not_, 1), pvo)));
+        }
     }
 
     // ---- W_mbej (layout [m][b][e][j]) ----------------------------------------
@@ -334,7 +398,21 @@ int kv_stanton(kvft_ctx *ctx, int nb, int nv, int no, const double *const F[4],
         int d[4] = {no, nv, nv, no};
         long long ss[4] = {vo, vo2, o, 1};          // vovo[b,m,e,j]
         long long ds[4] = {wm, wb, we, 1};
-        KV_TRY(kv_axpby4(ctx, B, d, -1.0, vovo, ss, 0, 0.0, w.Wmbej, ds, v2o2));
+        if (sh) {
+            // W_mbej is read only on its spin-conserving blocks (s_m + s_b =
+            // s_e + s_j): six of the sixteen (m, b, e, j) spin blocks
+            const int hd[4] = {sh, sh, sh, sh};
+            for (int m = 0; m < 16; m++) {
+                const int sm = m & 1, sb = (m >> 1) & 1, se = (m >> 2) & 1, sj = (m >> 3) & 1;
+                if (sm + sb != se + sj) continue;
+                const long long os = (long long)sh * (sm * ss[0] + sb * ss[1] + se * ss[2] + sj),
+                                od = (long long)sh * (sm * ds[0] + sb * ds[1] + se * ds[2] + sj);
+                KV_TRY(kv_axpby4(ctx, B, hd, -1.0, vovo + os, ss, 0, 0.0, w.Wmbej + od, ds,
+                                 v2o2));
+            }
+        } else {
+            KV_TRY(kv_axpby4(ctx, B, d, -1.0, vovo, ss, 0, 0.0, w.Wmbej, ds, v2o2));
+        }
     }
     // - vovv[b,m,e,f] t1[f,j]    (M=(m,b,e), K=f, N=j); spins m b e f j
     KV_TRY(sgemm(no * nv * nv, no, nv, B, -1.0,
@@ -357,7 +435,7 @@ int kv_stanton(kvft_ctx *ctx, int nb, int nv, int no, const double *const F[4],
                      return sp(m, 0) == sp(m, 1) && sp(m, 2) + sp(m, 1) == sp(m, 4) + sp(m, 3);
                  }, 0));
     // - oovv[m,n,e,f] (t2[f,b,j,n]/2 + t1[f,j] t1[b,n])  (M=(m,e), K=(n,f), N=(tau,b,j))
-    KV_TRY(kv_make_wmbej_tmp(ctx, B, nv, no, t1, t2, w.tmp4));
+    KV_TRY(kv_make_wmbej_tmp(ctx, B, nv, no, t1, t2, w.tmp4, sh));
     {
         // tmp4 holds [tau][b][j][n][f] with per-tau stride v2o2 (tmp4 is sized
         // for the largest block, so index it with the v2o2 layout directly);
@@ -477,7 +555,7 @@ int kv_stanton(kvft_ctx *ctx, int nb, int nv, int no, const double *const F[4],
                  }, 0));
 
     // ---- T2 += fac (1 - P(ab))(1 - P(ij)) (Z + ladders) -------------------------
-    return kv_assemble_t2(ctx, B, nv, no, fac, w.Z, ladders ? w.Lc : nullptr, T2, seed_t2);
+    return kv_assemble_t2(ctx, B, nv, no, fac, w.Z, ladders ? w.Lc : nullptr, T2, seed_t2, sh);
 }
 
 extern "C" int kvft_stanton_residual(kvft_ctx *ctx, int nb, int nv, int no,
