@@ -49,10 +49,10 @@ UNIT = "solves/s"
 # iters: amplitude iterations of the converged solve (guess 1), by precision;
 # for 'mixed' the few-digit iterations before the REFINE refinement sweeps.
 # ueg114 was measured by full solves on a GB300 (kelvin_gb300.ccsd.ccsd(...).run()):
-# mixed 28 + 2 sweeps, Omega_cc -0.9542854151 (35.2 s); 7 levels 30, -0.9542857194.
+# mixed 27 + 2 sweeps, Omega_cc -0.9542852803 (12.8 s); 7 levels 30, -0.9542857194.
 WORKLOADS = {
     "ueg114": dict(N=38, rs=1.0, norb=57, theta=0.25, ng=20, damp=0.5, econv=1e-10,
-                   max_iter=100, iters={"mixed": 28, "fp64_tc": 30, "fp64": 30},
+                   max_iter=100, iters={"mixed": 27, "fp64_tc": 30, "fp64": 30},
                    step="iteration",
                    label="UEG 38 e-, rs=1, 57 plane waves (114 spin orbitals), Theta=0.25, "
                          "ng=20, damping 0.5, econv 1e-10"),
@@ -68,7 +68,12 @@ ITERS_FALLBACK = 30
 # fp64_tc]` (one replay pass per launch, so the full-size workload was
 # captured).  A measured input of the roofline, not computed here: re-take
 # it when the kernels change.
-NCU_TRAFFIC = {}
+NCU_TRAFFIC = {
+    ("ueg114", "mixed", "gemm6"): 2.4879e9, ("ueg114", "mixed", "gemm"): 1.5869e9,
+    ("ueg114", "mixed", "elem"): 4.7672e9,
+    ("ueg114", "fp64_tc", "gemm6"): 5.0731e9, ("ueg114", "fp64_tc", "gemm"): 1.8195e9,
+    ("ueg114", "fp64_tc", "elem"): 3.1879e9,
+}
 REFINE = 2          # refinement sweeps that end a mixed solve
 REFINE_DIGITS = 5   # their digit levels
 STEP_EVENTS = 8     # first event slot of the per-step timings (at most 50 steps)

@@ -207,7 +207,7 @@ wmbej_tmp_kernel(int nv, int no, int sh, const double *__restrict__ t1,
 // operation.  SEED: T2 = -seed + R is stored (every a != b element once), no
 // reduction and no pre-seeded T2.
 template <int FS, bool SEED>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 3)
 assemble_t2_kernel(int nv, int no, int sh, double fac, const double *__restrict__ Z,
                    const double *__restrict__ Lc, const double *__restrict__ seed,
                    double *__restrict__ T2) {
@@ -401,7 +401,9 @@ int kv_make_wmbej_tmp(kvft_ctx *ctx, int batch, int nv, int no,
     if (total == 0) return KVFT_OK;
     if (batch > 65535) return kv_fail(ctx, KVFT_EINVAL, "wmbej_tmp: batch too large");
     KvProfScope prof(ctx, KV_CAT_ELEM, 16.0 * total);
-    const dim3 grid(((nv + 31) / 32) * ((no + 31) / 32), std::min(nv * no, 65535), batch);
+    // each block walks several (b, j): with spin blocks most of its tiles are
+    // skipped, and short-lived blocks would leave the SMs waiting for new ones
+    const dim3 grid(((nv + 31) / 32) * ((no + 31) / 32), std::min(nv * no, 2048), batch);
     wmbej_tmp_kernel<<<grid, 256, 0, ctx->stream>>>(nv, no, spin_half, t1, t2, out);
     return kv_launch_check(ctx, "wmbej_tmp");
 }
