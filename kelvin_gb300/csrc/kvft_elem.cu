@@ -229,6 +229,14 @@ assemble_t2_kernel(int nv, int no, int sh, double fac, const double *__restrict_
         int a, b;
         ov.decode(pab, a, b);
         const int tab = (a >= sh) + (b >= sh);
+        if (SEED && sh) {
+            // spin blocks: a tile pair without spin-conserving (i, j) holds
+            // zeros only, which nothing reads (the solver's update and the
+            // energy walk the conserving elements), so it is not written
+            const int il = i0 >= sh, ih = min(i0 + 31, no - 1) >= sh;
+            const int jl = j0 >= sh, jh = min(j0 + 31, no - 1) >= sh;
+            if (tab < il + jl || tab > ih + jh) continue;           // block-uniform
+        }
         const long long oab = y * s4 + ((long long)a * nv + b) * oo;
         const long long oba = y * s4 + ((long long)b * nv + a) * oo;
         const double *L = Lc ? Lc + (y * pv + pab) * (long long)po : nullptr;
