@@ -57,6 +57,11 @@ inline long long kidx_fast_stride(const KIdx &x) {
     return 0;
 }
 
+// Profile categories (kvft_profile_stats order): work in flops for
+// KV_CAT_GEMM6, in bytes for the others.
+enum KvCat { KV_CAT_GEMM6 = 0, KV_CAT_GEMM = 1, KV_CAT_QUAD = 2, KV_CAT_ENERGY = 3,
+             KV_CAT_ELEM = 4, KV_CAT_PACK = 5, KV_NCAT = 6 };
+
 // ---------------------------------------------------------------------------
 // Context
 // ---------------------------------------------------------------------------
@@ -80,9 +85,9 @@ struct kvft_ctx {
     // evaluations, emptied when a solver is destroyed.
     bool pack_cache_on = false;
     std::map<std::string, std::pair<void *, size_t>> pack_cache;
-    // profile category and algorithmic flops of the contraction being
+    // profile category and algorithmic work of the contraction being
     // launched (its kernel is timed alone, without the operand packing)
-    int gemm_cat = 1;
+    int gemm_cat = KV_CAT_GEMM;
     double gemm_work = 0.0;
     // Spin blocks of the residual's operands: 0, or the size h of the alpha
     // half when every orbital index runs over [0, h) alpha then [h, 2h) beta
@@ -109,8 +114,6 @@ struct KvPackCacheScope {
 
 // Live per-launch timing (enabled by kvft_profile_begin): event pairs around
 // launches of each category, with the algorithmic work they carry.
-enum KvCat { KV_CAT_GEMM6 = 0, KV_CAT_GEMM = 1, KV_CAT_QUAD = 2, KV_CAT_ENERGY = 3,
-             KV_CAT_ELEM = 4, KV_CAT_PACK = 5, KV_NCAT = 6 };
 struct KvProf {
     bool on = false;
     std::vector<cudaEvent_t> pool;

@@ -43,3 +43,20 @@ def test_device_built_solve_matches_host_built(ctx):
         cc.release()
     assert abs(res[0][1] - res[1][1]) < 1e-12
     assert abs(res[0][0] - res[1][0]) < 1e-11
+
+
+@pytest.mark.parametrize("make", CASES)
+def test_builders_are_spin_blocked(make):
+    """The solver's spin-block path needs alpha spin orbitals first and every
+    integral zero outside the spin-conserving blocks (s_p + s_q = s_r + s_s);
+    the UEG and Hubbard builders give exactly that."""
+    s = make(False)
+    eri, fock = s.g_aint_tot(), s.g_fock_tot()
+    n = eri.shape[0]
+    assert n % 2 == 0
+    sp = (numpy.arange(n) >= n // 2).astype(int)
+    cons = (sp[:, None, None, None] + sp[None, :, None, None]
+            == sp[None, None, :, None] + sp[None, None, None, :])
+    assert not eri[~cons].any()
+    assert not fock[sp[:, None] != sp[None, :]].any()
+    assert eri[cons].any()
