@@ -16,7 +16,7 @@ import numpy
 from . import _lib
 from .cc_utils import DeviceSolver, iterate
 from .quadrature import ft_quad
-from .systems import grand_potential0
+from .systems import fermi, grand_potential0
 
 PRECISIONS = {'fp64': (_lib.PREC_FP64, 7), 'fp64_tc': (_lib.PREC_FP64_TC, 7),
               'mixed': (_lib.PREC_MIXED, 3)}
@@ -167,6 +167,70 @@ class ccsd(object):
         self.Gcc = Eccn
         self.Gtot = E0 + E1 + Eccn
         return (Eccn + E0 + E1, Eccn)
+
+    def compute_ESN(self, L1=None, L2=None, gderiv=True, delta=1e-4):
+        """Energy, entropy and particle number (kelvin/ccsd.py:128-214).
+
+        Kelvin differentiates the grand potential Omega(beta, mu) through the
+        Lambda equations (an adjoint, plus the tau-grid derivative when
+        gderiv=True), with the orbital energies fixed and the mean-field Fock
+        matrix following the occupations.  Here the same derivatives are
+        central finite differences of Omega itself: four further solves at
+        (beta +- delta beta, mu) and (beta, mu +- delta T), warm-started from the
+        converged amplitudes, with the grid nodes moving with beta as in
+        Kelvin's gderiv=True form.  The few-digit mixed form is not smooth
+        enough to difference, so its difference solves use seven digit levels.
+
+            N = -dOmega/dmu,  E = d(beta Omega)/dbeta + mu N,
+            S = beta (E - mu N - Omega)
+
+        L1/L2 (given Lambda amplitudes) have no counterpart and must be None."""
+        if L1 is not None or L2 is not None:
+            raise Exception("kelvin_gb300.ccsd: Lambda amplitudes are not used "
+                            "(E, S, N come from finite differences of Omega)")
+        if not gderiv:
+            raise Exception("kelvin_gb300.ccsd: only the exact-grid derivative (gderiv=True)")
+        if self.T1 is None:
+            self.run()
+        en = self.sys.g_energies_tot()
+        fock0 = self.sys.g_fock_tot()
+        eri = self.sys.g_aint_tot()
+        W = numpy.einsum('ijij->ij', eri)
+        fo0 = fermi(self.beta, en, self.mu)
+        # the mean-field Fock matrix follows the occupations, as in Kelvin's
+        # relaxed occupation numbers (g_fock_d_den): F = h + sum_r <pr||qr> f_r
+        Gd = numpy.einsum('prqr->pqr', eri)
+        prec = 'fp64_tc' if self.precision == 'mixed' else self.precision
+        conv = {"econv": min(self.econv, 1e-12), "tconv": 1e3 * min(self.econv, 1e-12),
+                "max_iter": max(self.max_iter, 200), "damp": self.damp}
+
+        def omega(beta, mu):
+            fo = fermi(beta, en, mu)
+            fock = fock0 + Gd @ (fo - fo0)
+            E0 = grand_potential0(beta, en, mu) + self.sys.const_energy()
+            E1 = 0.5 * fo @ W @ fo
+            ti, g, G = ft_quad(self.ngrid, beta, self.quad)
+            self.ctx.set_precision(*PRECISIONS[prec])
+            solver = DeviceSolver.from_system(self.ctx, en, fock, eri, beta, mu, ti, g, G)
+            try:
+                solver.set_amplitudes(self.T1, self.T2)
+                solver.guess(2)
+                Ecc, _ = converge(solver, self.ctx, conv, prec, PRECISIONS[prec][1])
+            finally:
+                solver.close()
+            return E0 + E1 + Ecc
+
+        beta, mu = self.beta, self.mu
+        db, dm = delta * beta, delta * self.T
+        Om = omega(beta, mu)            # with the difference solves' settings
+        Np = omega(beta, mu + dm)
+        Nm = omega(beta, mu - dm)
+        Bp = omega(beta + db, mu)
+        Bm = omega(beta - db, mu)
+        self.N = -(Np - Nm) / (2.0 * dm)
+        self.E = ((beta + db) * Bp - (beta - db) * Bm) / (2.0 * db) + mu * self.N
+        self.S = beta * (self.E - mu * self.N - Om)
+        return self.E, self.S, self.N
 
     def release(self):
         """Free the device buffers of the last solve."""
