@@ -222,11 +222,15 @@ class ccsd(object):
 
         beta, mu = self.beta, self.mu
         db, dm = delta * beta, delta * self.T
-        Om = omega(beta, mu)            # with the difference solves' settings
-        Np = omega(beta, mu + dm)
-        Nm = omega(beta, mu - dm)
-        Bp = omega(beta + db, mu)
-        Bm = omega(beta - db, mu)
+        prev = ctx_precision(self.ctx)
+        try:
+            Om = omega(beta, mu)            # with the difference solves' settings
+            Np = omega(beta, mu + dm)
+            Nm = omega(beta, mu - dm)
+            Bp = omega(beta + db, mu)
+            Bm = omega(beta - db, mu)
+        finally:
+            self.ctx.set_precision(*prev)
         self.N = -(Np - Nm) / (2.0 * dm)
         self.E = ((beta + db) * Bp - (beta - db) * Bm) / (2.0 * db) + mu * self.N
         self.S = beta * (self.E - mu * self.N - Om)

@@ -733,6 +733,25 @@ int kvft_ccsd_stanton(kvft_ctx *ctx, int ng, int nv, int no, const double *const
     void *tb = nullptr;
     KV_TRY(kv_scratch(ctx, "stanton_tbar", sizeof(double) * ng * (s1 + s2), &tb));
     double *T1b = (double *)tb, *T2b = T1b + ng * s1;
+    // spin blocks: used when the integrals and the amplitudes given are all
+    // spin-blocked (alpha half first); tbar's zero blocks are then cleared
+    // here, since the residual does not write them and the integration reads
+    // every element
+    int sh = 0;
+    if (nv == no && nv % 2 == 0) {
+        const double *arr[15];
+        int rank[15];
+        long long bat[15];
+        for (int k = 0; k < 4; k++) arr[k] = F[k], rank[k] = 2, bat[k] = 1;
+        for (int k = 0; k < 9; k++) arr[4 + k] = I[k], rank[4 + k] = 4, bat[4 + k] = 1;
+        arr[13] = T1old, rank[13] = 2, bat[13] = ng;
+        arr[14] = T2old, rank[14] = 4, bat[14] = ng;
+        int yes = 0;
+        KV_TRY(spin_blocked(ctx, nv, nv / 2, 15, arr, rank, bat, &yes));
+        if (yes) sh = nv / 2;
+    }
+    if (sh) KV_CHECK(ctx, cudaMemsetAsync(T2b, 0, sizeof(double) * ng * s2, ctx->stream));
+    KvSpinScope spins(ctx, sh);
     KV_TRY(seed_neg(ctx, ng, s1, F[2], T1b));
     size_t fr = 0, tot = 0;
     KV_CHECK(ctx, cudaMemGetInfo(&fr, &tot));

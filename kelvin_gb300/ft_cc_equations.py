@@ -79,3 +79,121 @@ def stanton_residual(T1, T2, F, I, t1, t2, fac=1.0, ctx=None):
     if isinstance(T1, numpy.ndarray):
         dT1.to_host(T1)
         dT2.to_host(T2)
+
+
+# ---- unrestricted (spin-blocked) form -------------------------------------------
+# Kelvin's unrestricted update (ft_cc_equations.py:130-164) takes the alpha and
+# beta blocks separately: Fa, Fb (one_e_blocks), Ia, Ib (antisymmetrised
+# same-spin two_e_blocks), Iabab (<ab|ab> with alpha indices 1, 3 and beta 2, 4,
+# all sixteen o/v blocks), T1a, T1b, T2aa, T2ab[a,b,i,j] (a, i alpha; b, j beta),
+# T2bb and their denominators.  Here they are laid out as one general-spin
+# problem with the alpha spin orbitals first; the solver finds its spin blocks
+# and contracts only those, so the work is that of the spin-blocked equations.
+
+class _Blocks(object):
+    def __init__(self, **kw):
+        self.__dict__.update(kw)
+
+
+def u_to_g_one(Fa, Fb):
+    """General-spin one_e_blocks from the alpha and beta blocks."""
+    out = {}
+    for t in F_ORDER:
+        fa, fb = getattr(Fa, t), getattr(Fb, t)
+        na, nb = fa.shape[0], fb.shape[0]
+        g = numpy.zeros((na + nb, na + nb), dtype=fa.dtype)
+        g[:na, :na] = fa
+        g[na:, na:] = fb
+        out[t] = g
+    return _Blocks(**out)
+
+
+def u_to_g_two(Ia, Ib, Iabab):
+    """General-spin antisymmetrised blocks <pq||rs> from Ia, Ib and Iabab."""
+    out = {}
+    for t in I_ORDER:
+        ia, ib = getattr(Ia, t), getattr(Ib, t)
+        na, nb = ia.shape[0], ib.shape[0]
+        n = na + nb
+        A, B = slice(0, na), slice(na, n)
+        g = numpy.zeros((n, n, n, n), dtype=ia.dtype)
+        g[A, A, A, A] = ia
+        g[B, B, B, B] = ib
+        g[A, B, A, B] = getattr(Iabab, t)
+        # <Pq||Rs> = <qP||sR>, <pQ||Rs> = -<pQ||sR>, <Pq||rS> = -<qP||rS>
+        g[B, A, B, A] = getattr(Iabab, t[1] + t[0] + t[3] + t[2]).transpose(1, 0, 3, 2)
+        g[A, B, B, A] = -getattr(Iabab, t[0] + t[1] + t[3] + t[2]).transpose(0, 1, 3, 2)
+        g[B, A, A, B] = -getattr(Iabab, t[1] + t[0] + t[2] + t[3]).transpose(1, 0, 2, 3)
+        out[t] = g
+    return _Blocks(**out)
+
+
+def u_to_g_t1(T1a, T1b):
+    """[ng][n][n] from [ng][na][na] and [ng][nb][nb] (spin-diagonal)."""
+    ng, na, nb = T1a.shape[0], T1a.shape[1], T1b.shape[1]
+    g = numpy.zeros((ng, na + nb, na + nb), dtype=T1a.dtype)
+    g[:, :na, :na] = T1a
+    g[:, na:, na:] = T1b
+    return g
+
+
+def u_to_g_t2(T2aa, T2ab, T2bb):
+    """[ng][n]^4 from the three spin cases (antisymmetric completion)."""
+    ng, na, nb = T2aa.shape[0], T2aa.shape[1], T2bb.shape[1]
+    n = na + nb
+    A, B = slice(0, na), slice(na, n)
+    g = numpy.zeros((ng, n, n, n, n), dtype=T2aa.dtype)
+    g[:, A, A, A, A] = T2aa
+    g[:, B, B, B, B] = T2bb
+    g[:, A, B, A, B] = T2ab
+    g[:, B, A, B, A] = T2ab.transpose(0, 2, 1, 4, 3)
+    g[:, A, B, B, A] = -T2ab.transpose(0, 1, 2, 4, 3)
+    g[:, B, A, A, B] = -T2ab.transpose(0, 2, 1, 3, 4)
+    return g
+
+
+def u_to_g_d1(D1a, D1b):
+    na, nb = D1a.shape[0], D1b.shape[0]
+    g = numpy.zeros((na + nb, na + nb), dtype=D1a.dtype)
+    g[:na, :na] = D1a
+    g[na:, na:] = D1b
+    return g
+
+
+def u_to_g_d2(D2aa, D2ab, D2bb):
+    """Denominators of the spin-conserving blocks (zero elsewhere: those
+    amplitudes vanish and stay zero)."""
+    na, nb = D2aa.shape[0], D2bb.shape[0]
+    n = na + nb
+    A, B = slice(0, na), slice(na, n)
+    g = numpy.zeros((n, n, n, n), dtype=D2aa.dtype)
+    g[A, A, A, A] = D2aa
+    g[B, B, B, B] = D2bb
+    g[A, B, A, B] = D2ab
+    g[B, A, B, A] = D2ab.transpose(1, 0, 3, 2)
+    g[A, B, B, A] = D2ab.transpose(0, 1, 3, 2)
+    g[B, A, A, B] = D2ab.transpose(1, 0, 2, 3)
+    return g
+
+
+def g_to_u_t(T1, T2, na):
+    """Unrestricted blocks ((T1a, T1b), (T2aa, T2ab, T2bb)) of general-spin
+    amplitudes with the alpha spin orbitals first."""
+    A, B = slice(0, na), slice(na, T1.shape[1])
+    return ((T1[:, A, A].copy(), T1[:, B, B].copy()),
+            (T2[:, A, A, A, A].copy(), T2[:, A, B, A, B].copy(), T2[:, B, B, B, B].copy()))
+
+
+def uccsd_stanton(Fa, Fb, Ia, Ib, Iabab, T1aold, T1bold, T2aaold, T2abold, T2bbold,
+                  D1a, D1b, D2aa, D2ab, D2bb, ti, ng, G, ctx=None, precision=None):
+    """Unrestricted FT-CCSD update (ft_cc_equations.py:130-164): returns
+    ((T1a, T1b), (T2aa, T2ab, T2bb)).  Runs as one general-spin update with
+    the alpha spin orbitals first, restricted to its spin-conserving blocks."""
+    F = u_to_g_one(Fa, Fb)
+    I = u_to_g_two(Ia, Ib, Iabab)
+    T1 = u_to_g_t1(numpy.asarray(T1aold), numpy.asarray(T1bold))
+    T2 = u_to_g_t2(numpy.asarray(T2aaold), numpy.asarray(T2abold), numpy.asarray(T2bbold))
+    D1 = u_to_g_d1(D1a, D1b)
+    D2 = u_to_g_d2(D2aa, D2ab, D2bb)
+    o1, o2 = ccsd_stanton(F, I, T1, T2, D1, D2, ti, ng, G, ctx=ctx, precision=precision)
+    return g_to_u_t(o1, o2, Fa.vo.shape[0])
