@@ -1,0 +1,95 @@
+"""compute_ESN's finite differences and thermodynamic assembly, on the host:
+with the correlated part of Omega replaced by zero (fake solver), E, S and N
+must be those of Omega0 + Omega1 with the mean-field Fock matrix following
+the occupations, whose derivatives are known in closed form."""
+import numpy
+
+from kelvin_gb300 import ccsd as ccsd_mod
+from kelvin_gb300.systems import fermi
+
+
+class FakeCtx(object):
+    def __init__(self):
+        self._precision = (0, 7)
+
+    def set_precision(self, prec, digits=7):
+        self._precision = (prec, digits)
+
+
+class FakeSystem(object):
+    """n orbitals with fixed energies and a symmetric <ij||ij> matrix."""
+
+    def __init__(self, rng, n, T, mu):
+        self.T, self.mu = T, mu
+        self.en = numpy.sort(rng.standard_normal(n))
+        g = rng.standard_normal((n, n, n, n)) * 0.05
+        g = g - g.transpose(1, 0, 2, 3)
+        g = g - g.transpose(0, 1, 3, 2)
+        self.eri = 0.5 * (g + g.transpose(2, 3, 0, 1))
+
+    def verify(self, T, mu):
+        return T == self.T and mu == self.mu
+
+    def g_energies_tot(self):
+        return self.en
+
+    def g_fock_tot(self):
+        fo = fermi(1.0 / self.T, self.en, self.mu)
+        return numpy.diag(self.en) + numpy.einsum('prqr,r->pq', self.eri, fo)
+
+    def g_aint_tot(self):
+        return self.eri
+
+    def const_energy(self):
+        return 0.0
+
+
+class FakeSolver(object):
+    calls = []
+
+    @classmethod
+    def from_system(cls, ctx, en, fock, eri, beta, mu, ti, g, G):
+        cls.calls.append((beta, mu, fock.copy()))
+        return cls()
+
+    def set_amplitudes(self, T1, T2):
+        pass
+
+    def guess(self, kind):
+        return 0.0
+
+    def close(self):
+        pass
+
+
+def test_esn_of_the_mean_field_part(monkeypatch):
+    rng = numpy.random.default_rng(4)
+    T, mu = 0.3, 0.1
+    s = FakeSystem(rng, 6, T, mu)
+    monkeypatch.setattr(ccsd_mod, "DeviceSolver", FakeSolver)
+    monkeypatch.setattr(ccsd_mod, "converge", lambda *a, **k: (0.0, {}))
+    FakeSolver.calls = []
+    cc = ccsd_mod.ccsd(s, T=T, mu=mu, ngrid=4, ctx=FakeCtx(), precision='mixed')
+    cc.T1, cc.T2 = numpy.zeros(1), numpy.zeros(1)
+    E, S, N = cc.compute_ESN()
+    assert cc.ctx._precision == (0, 7)                    # restored
+
+    beta, en = 1.0 / T, s.en
+    W = numpy.einsum('ijij->ij', s.eri)
+    f = fermi(beta, en, mu)
+    df_dmu = beta * f * (1 - f)
+    df_dbeta = -(en - mu) * f * (1 - f)
+    Om1 = 0.5 * f @ W @ f
+    Om0 = ccsd_mod.grand_potential0(beta, en, mu)
+    N_ref = f.sum() - f @ W @ df_dmu
+    E_ref = (f * (en - mu)).sum() + Om1 + beta * (f @ W @ df_dbeta) + mu * N_ref
+    S_ref = beta * (E_ref - mu * N_ref - Om0 - Om1)
+    assert abs(N - N_ref) < 1e-8
+    assert abs(E - E_ref) < 1e-8
+    assert abs(S - S_ref) < 1e-7
+    # five solves; the Fock matrix of each follows its occupations
+    assert len(FakeSolver.calls) == 5
+    for b, m, fock in FakeSolver.calls:
+        fo = fermi(b, en, m)
+        assert numpy.allclose(fock, numpy.diag(en) + numpy.einsum('prqr,r->pq', s.eri, fo),
+                              rtol=0, atol=1e-13)
