@@ -15,6 +15,7 @@ import numpy
 
 from . import _lib
 from .cc_utils import DeviceSolver, iterate
+from .ft_cc_equations import g_to_u_t, u_to_g_t1, u_to_g_t2
 from .quadrature import ft_quad
 from .systems import fermi, grand_potential0
 
@@ -104,7 +105,16 @@ class ccsd(object):
         self.ctx = ctx or _lib.context(device)
         self.T1 = None
         self.T2 = None
+        self._Tg = None          # general-spin amplitudes of the last solve
         self.solver = None
+
+    def _unrestricted(self):
+        """A system in Kelvin's unrestricted form (has_u()): it is solved in its
+        general-spin form (alpha spin orbitals first, spin blocks found by the
+        solver) and the amplitudes are given and returned per spin case,
+        T1 = (T1a, T1b), T2 = (T2aa, T2ab, T2bb) (kelvin/ccsd.py:714-880)."""
+        has_u = getattr(self.sys, "has_u", None)
+        return bool(has_u and has_u() and hasattr(self.sys, "u_energies_tot"))
 
     def run(self, T1=None, T2=None):
         """Solve; returns (Omega_total, Omega_cc) like Kelvin."""
@@ -143,13 +153,20 @@ class ccsd(object):
             self.iterations_refine = 0
             self.converged = bool(r.converged)
             self.omega_low = None
-            self.T1, self.T2 = solver.amplitudes()
+            self._Tg = solver.amplitudes()
+            self.T1, self.T2 = self._Tg
+            if self._unrestricted():
+                na = self.sys.u_energies_tot()[0].shape[0]
+                self.T1, self.T2 = g_to_u_t(self._Tg[0], self._Tg[1], na)
             Eccn = r.omega_cc
             self.G0, self.G1, self.Gcc, self.Gtot = E0, E1, Eccn, E0 + E1 + Eccn
             return (Eccn + E0 + E1, Eccn)
         if self.rt_iter[0] != 'a':
             logging.warning("Convergence scheme ({}) is ignored when amplitudes are given.".format(self.rt_iter))
         if T1in is not None and T2in is not None:
+            if self._unrestricted():
+                T1in = u_to_g_t1(*[numpy.asarray(x) for x in T1in])
+                T2in = u_to_g_t2(*[numpy.asarray(x) for x in T2in])
             solver.set_amplitudes(T1in, T2in)
             E2 = solver.guess(2)
         else:
@@ -161,7 +178,11 @@ class ccsd(object):
         self.iterations_refine = info["iterations_refine"]
         self.converged = info["converged"]
         self.omega_low = info["omega_low"]
-        self.T1, self.T2 = solver.amplitudes()
+        self._Tg = solver.amplitudes()
+        self.T1, self.T2 = self._Tg
+        if self._unrestricted():
+            na = self.sys.u_energies_tot()[0].shape[0]
+            self.T1, self.T2 = g_to_u_t(self._Tg[0], self._Tg[1], na)
         self.G0 = E0
         self.G1 = E1
         self.Gcc = Eccn
@@ -192,6 +213,7 @@ class ccsd(object):
             raise Exception("kelvin_gb300.ccsd: only the exact-grid derivative (gderiv=True)")
         if self.T1 is None:
             self.run()
+        Tg = self._Tg if self._Tg is not None else (self.T1, self.T2)
         en = self.sys.g_energies_tot()
         fock0 = self.sys.g_fock_tot()
         eri = self.sys.g_aint_tot()
@@ -213,7 +235,7 @@ class ccsd(object):
             self.ctx.set_precision(*PRECISIONS[prec])
             solver = DeviceSolver.from_system(self.ctx, en, fock, eri, beta, mu, ti, g, G)
             try:
-                solver.set_amplitudes(self.T1, self.T2)
+                solver.set_amplitudes(*Tg)
                 solver.guess(2)
                 Ecc, _ = converge(solver, self.ctx, conv, prec, PRECISIONS[prec][1])
             finally:

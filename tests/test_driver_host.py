@@ -1,7 +1,9 @@
-"""compute_ESN's finite differences and thermodynamic assembly, on the host:
-with the correlated part of Omega replaced by zero (fake solver), E, S and N
+"""The ccsd driver's host logic with a fake device solver.
+
+compute_ESN: with the correlated part of Omega replaced by zero, E, S and N
 must be those of Omega0 + Omega1 with the mean-field Fock matrix following
-the occupations, whose derivatives are known in closed form."""
+the occupations, whose derivatives are known in closed form.  Unrestricted
+systems: amplitudes are returned and accepted per spin case."""
 import numpy
 
 from kelvin_gb300 import ccsd as ccsd_mod
@@ -93,3 +95,56 @@ def test_esn_of_the_mean_field_part(monkeypatch):
         fo = fermi(b, en, m)
         assert numpy.allclose(fock, numpy.diag(en) + numpy.einsum('prqr,r->pq', s.eri, fo),
                               rtol=0, atol=1e-13)
+
+
+class USystem(FakeSystem):
+    """The same system offered in Kelvin's unrestricted form (has_u)."""
+
+    def has_u(self):
+        return True
+
+    def u_energies_tot(self):
+        n = self.en.shape[0] // 2
+        return self.en[:n], self.en[n:]
+
+    def get_mp1(self):
+        f = fermi(1.0 / self.T, self.en, self.mu)
+        return 0.5 * numpy.einsum('ijij,i,j->', self.eri, f, f)
+
+
+def test_unrestricted_system_amplitudes(monkeypatch):
+    """Amplitudes of an unrestricted system come back per spin case and are
+    accepted per spin case (kelvin/ccsd.py:714-880)."""
+    rng = numpy.random.default_rng(5)
+    T, mu, ng = 0.3, 0.1, 4
+    s = USystem(rng, 6, T, mu)
+    n, na = 6, 3
+    sp = (numpy.arange(n) >= na).astype(int)
+    cons = (sp[:, None, None, None] + sp[None, :, None, None]
+            == sp[None, None, :, None] + sp[None, None, None, :])
+    T1 = rng.standard_normal((ng, n, n)) * (sp[:, None] == sp[None, :])
+    T2 = rng.standard_normal((ng, n, n, n, n))
+    T2 = (T2 - T2.transpose(0, 2, 1, 3, 4))
+    T2 = (T2 - T2.transpose(0, 1, 2, 4, 3)) * cons
+    seen = {}
+
+    class Solver(FakeSolver):
+        def amplitudes(self):
+            return T1.copy(), T2.copy()
+
+        def set_amplitudes(self, a, b):
+            seen["T1"], seen["T2"] = a, b
+
+    monkeypatch.setattr(ccsd_mod, "DeviceSolver", Solver)
+    monkeypatch.setattr(ccsd_mod, "converge", lambda *a, **k: (
+        -0.01, {"iterations": 3, "iterations_refine": 0, "converged": True,
+                "omega_low": None}))
+    cc = ccsd_mod.ccsd(s, T=T, mu=mu, ngrid=ng, ctx=FakeCtx())
+    cc.run()
+    (t1a, t1b), (t2aa, t2ab, t2bb) = cc.T1, cc.T2
+    assert numpy.array_equal(t1a, T1[:, :na, :na]) and numpy.array_equal(t1b, T1[:, na:, na:])
+    assert numpy.array_equal(t2ab, T2[:, :na, na:, :na, na:])
+    assert numpy.array_equal(t2aa, T2[:, :na, :na, :na, :na])
+    assert numpy.array_equal(t2bb, T2[:, na:, na:, na:, na:])
+    cc.run(T1=cc.T1, T2=cc.T2)
+    assert numpy.array_equal(seen["T1"], T1) and numpy.array_equal(seen["T2"], T2)
