@@ -543,6 +543,18 @@ def run_gemm(args):
     return 0
 
 
+def run_serve(args):
+    """A seeded Poisson stream of mixed requests (kelvin_gb300.serve): solves/s
+    and p50/p99 latency, completion minus arrival."""
+    from kelvin_gb300 import serve
+    reqs = serve.request_stream(args.serve, rate=args.rate, seed=0)
+    rep = serve.Server(precision=args.precision).serve(reqs)
+    rep.pop("requests")
+    print(json.dumps(dict({"serve": args.serve, "rate_per_s": args.rate,
+                           "precision": args.precision}, **rep)))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gemm", default="", help="M,N,K,batch: time one contraction shape")
@@ -557,8 +569,13 @@ def main():
     ap.add_argument("--workload", default="ueg114", choices=sorted(WORKLOADS))
     ap.add_argument("--precision", default="mixed", choices=["fp64", "fp64_tc", "mixed"])
     ap.add_argument("--digits", type=int, default=0)
+    ap.add_argument("--serve", type=int, default=0,
+                    help="serve this many requests of a seeded Poisson stream")
+    ap.add_argument("--rate", type=float, default=20.0, help="request rate of --serve (1/s)")
     args = ap.parse_args()
     w = WORKLOADS[args.workload]
+    if args.serve:
+        return run_serve(args)
     if args.gemm:
         return run_gemm(args)
     if args.profile_step:
