@@ -17,6 +17,11 @@ restatements for cqcpy).  Outputs (all small, seeded):
                       norb=7, 'g') integrals and the full ccsd(...).run()
                       (Kelvin test_ft_ccsd.py:119-133 golden -0.010750238811)
 * uegscf7.json     -- UEGSCFSystem at ng=40 (examples/ueg_ft_cc_compare.py)
+* ueg19_esn.json   -- Kelvin's published Lambda run, read from the text of
+                      examples/ueg_ft_ccsd_ESN.py (settings) and
+                      examples/ueg_ft_ccsd_ESN.out (Omega, the Lambda
+                      residual per iteration, E, S, N); nothing is executed
+                      (``--esn-only`` writes just this file)
 """
 import json
 import logging
@@ -225,5 +230,35 @@ def main(ref_root):
     print("UEG7", Ecc, "UEGSCF7", Ecc)
 
 
+def esn_example(ref_root):
+    """ueg19_esn.json from the example script and its recorded output."""
+    import re
+    ex = os.path.join(ref_root, "examples")
+    src = open(os.path.join(ex, "ueg_ft_ccsd_ESN.py")).read()
+    out = open(os.path.join(ex, "ueg_ft_ccsd_ESN.out")).read().splitlines()
+
+    def setting(name):
+        return float(re.search(r"^%s = ([0-9.eE+-]+)$" % name, src, re.M).group(1))
+    meta = {"T": setting("T"), "mu": setting("mu"), "norb": int(setting("norb")),
+            "cutoff": setting("cut"), "damp": setting("damp"),
+            "max_iter": int(setting("mi")),
+            "ngrid": int(re.search(r"ngrid=(\d+)", src).group(1)),
+            "econv": 1e-8,                      # ccsd() default; tconv = 1000 econv
+            "source": "examples/ueg_ft_ccsd_ESN.py, examples/ueg_ft_ccsd_ESN.out"}
+    start = [i for i, l in enumerate(out) if l.startswith("OmegaC:")][0]
+    stop = [i for i, l in enumerate(out) if l.startswith("Total CCSD Lambda time")][0]
+    meta["Omega"] = float([l for l in out if l.startswith("Omega:")][0].split()[1])
+    meta["Omega_cc"] = float(out[start].split()[1])
+    meta["lambda_residuals"] = [float(l.split()[1]) for l in out[start + 1:stop]]
+    for key in ("E", "S", "N"):
+        meta[key] = float([l for l in out if l.startswith(key + ": ")][0].split()[1])
+    with open(os.path.join(HERE, "ueg19_esn.json"), "w") as f:
+        json.dump(meta, f, indent=1)
+
+
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    args = [a for a in sys.argv[1:] if not a.startswith("--")]
+    root = args[0] if args else "/root/reference"
+    esn_example(root)
+    if "--esn-only" not in sys.argv:
+        main(root)
