@@ -138,3 +138,30 @@ def exact_residual(F, I, t1, t2):
         if a != b and i != j:
             R2[a - no, b - no, i, j] = sp.ad(a, sp.ad(b, sp.a(j, sp.a(i, ref)))) @ hbar
     return R1, R2
+
+
+def grand_potential(h, eri, T, mu):
+    """Exact grand potential -T ln Tr exp(-(H - mu N)/T) for
+    H = sum h[p,q] a+_p a_q + 1/4 sum <pq||rs> a+_p a+_q a_s a_r over n <= 10
+    spin orbitals, by diagonalising H - mu N in the 2^n-dimensional Fock space
+    (the finite-temperature FCI of kelvin/fci.py:88-103)."""
+    n = h.shape[0]
+    sp = _Space(n)
+    dim = sp.dim
+    H = numpy.zeros((dim, dim))
+    for col in range(dim):
+        v = numpy.zeros(dim)
+        v[col] = 1.0
+        out = numpy.zeros(dim)
+        for p in range(n):
+            for q in range(n):
+                if h[p, q] != 0.0:
+                    out += h[p, q] * sp.ad(p, sp.a(q, v))
+        for p, q, r, s in itertools.product(range(n), repeat=4):
+            if eri[p, q, r, s] != 0.0:
+                out += 0.25 * eri[p, q, r, s] * sp.ad(p, sp.ad(q, sp.a(s, sp.a(r, v))))
+        H[:, col] = out
+    N = numpy.array([bin(x).count("1") for x in range(dim)], dtype=float)
+    w = numpy.linalg.eigvalsh(0.5 * (H + H.T) - mu * numpy.diag(N))
+    w0 = w.min()
+    return w0 - T * numpy.log(numpy.exp(-(w - w0) / T).sum())

@@ -88,3 +88,38 @@ def test_ueg_golden_omega():
     assert abs(Ecc - meta["Omega_cc"]) < 1e-12
     assert abs(Et - meta["Omega_total"]) < 1e-12
     assert len(hist) == len(meta["iterations"])
+
+
+def _hubbard_atom(eps=0.0, U=1.0):
+    """One site, two spin orbitals: h = eps, <01||01> = U."""
+    h = numpy.diag([eps, eps])
+    eri = numpy.zeros((2, 2, 2, 2))
+    eri[0, 1, 0, 1] = eri[1, 0, 1, 0] = U
+    eri[0, 1, 1, 0] = eri[1, 0, 0, 1] = -U
+    return h, eri
+
+
+def test_ft_ccsd_exact_for_two_spin_orbitals():
+    """FT-CCSD is exact for two spin orbitals as the grid is refined
+    (kelvin/tests/test_ft_ccsd.py:26-47 compares with FT-FCI at ng = 200 to
+    1e-9).  The exact grand potential comes from diagonalising H - mu N in the
+    Fock space and equals the Hubbard atom's closed form."""
+    from oracle import ft_lambda, ft_utils
+    eps, U, T, mu = 0.0, 1.0, 1.0, 0.3
+    h, eri = _hubbard_atom(eps, U)
+    exact = fock_space.grand_potential(h, eri, T, mu)
+    b = 1.0 / T
+    closed = -T * numpy.log(1 + 2 * numpy.exp(-b * (eps - mu))
+                            + numpy.exp(-b * (2 * eps + U - 2 * mu)))
+    assert abs(exact - closed) < 1e-14
+    err = {}
+    for label, en in (("bare", numpy.diag(h).copy()), ("shifted", numpy.diag(h) + 0.5 * U)):
+        fock = ft_lambda.mean_field(h, eri, ft_utils.ff(b, en, mu))
+        E1 = ft_lambda.omega_ref(en, h, eri, b, mu)[1]
+        for ng in (100, 200):
+            Et = ft_ccsd.ft_ccsd(en, fock, eri, T, mu, ngrid=ng, econv=1e-11, max_iter=24,
+                                 E1=E1)[0]
+            err[label, ng] = abs(Et - exact)
+    assert err["shifted", 200] < 1e-10 and err["bare", 200] < 2e-9
+    # third-order convergence in the grid spacing (Simpson weights)
+    assert 6.0 < err["bare", 100] / err["bare", 200] < 10.0
