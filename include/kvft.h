@@ -151,6 +151,41 @@ int kvft_stanton_residual(kvft_ctx *ctx, int nb, int nv, int no,
                           const double *const F[4], const double *const I[9],
                           const double *t1, const double *t2, double fac,
                           double *T1, double *T2);
+/* Lambda terms (cqcpy _Lambda_opt, called at ft_cc_equations.py:400-401):
+ * g = R'(t)^T m, the transpose of the residual's Jacobian at (t1, t2) applied
+ * to m, batched over nb tau points, so that
+ *   sum g1 dt1 + 1/4 sum g2 dt2 = sum m1 dR1 + 1/4 sum m2 dR2
+ * for every dt1 and antisymmetric dt2.  m1[i][a], m2[i][j][a][b] are in
+ * Lambda layout, g1[a][i], g2[a][b][i][j] in amplitude layout (device
+ * pointers; F, I as for kvft_stanton_residual). */
+int kvft_lambda_residual(kvft_ctx *ctx, int nb, int nv, int no,
+                         const double *const F[4], const double *const I[9],
+                         const double *t1, const double *t2, const double *m1,
+                         const double *m2, double *g1, double *g2);
+/* The strided-GEMM form of an index-string contraction C[cix] = A[aix] B[bix]
+ * (letters a-h virtual, i-n occupied; every letter in exactly two of the
+ * three): mnk = {M, N, K}; sizes/strides hold the composite indices (three
+ * components each, slow to fast) of A rows, A columns, B rows, B columns, C
+ * rows, C columns.  Host arithmetic only. */
+int kvft_einsum_plan(int nv, int no, const char *aix, const char *bix,
+                     const char *cix, int *mnk, int *sizes, long long *strides);
+
+/* ---- dry run ---------------------------------------------------------------
+ * A context without a device whose calls record their launches (the
+ * descriptors each kernel would receive) instead of running them; pointers
+ * passed to it are host memory and its scratch is host memory filled with
+ * NaN.  Lets the index arithmetic of a call be replayed and checked on a
+ * CPU.  kvft_lambda_residual accepts it; every other call that would touch
+ * the device returns KVFT_EINVAL.  Destroy it with kvft_ctx_destroy. */
+int kvft_dryrun_create(int precision, int digits, kvft_ctx **ctx);
+int kvft_dryrun_count(const kvft_ctx *ctx, int *count);
+/* op i: ints[32], longs[32], dbls[2], ptrs[8]; kind 0 contraction (M N K
+ * batch, alpha, beta, A B C views), 1 strided axpby (dims, strides, src,
+ * dst), 3 scale of a view.  Layout in kvft_ctx.cu. */
+int kvft_dryrun_op(const kvft_ctx *ctx, int i, int *ints, long long *longs,
+                   double *dbls, const void **ptrs);
+/* scratch buffer i of a dry-run context (KVFT_EINVAL past the last one) */
+int kvft_dryrun_scratch(const kvft_ctx *ctx, int i, const void **ptr, size_t *bytes);
 
 /* ---- contraction engine: the GEMM under every einsum of the path --------
  * (Kelvin's pyscf.lib.einsum -> BLAS dgemm).  C[b] = A[b] B[b] for `batch`

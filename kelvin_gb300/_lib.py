@@ -94,6 +94,21 @@ _SIGS = {
                                              ctypes.c_int, ctypes.POINTER(vp),
                                              ctypes.POINTER(vp), vp, vp,
                                              ctypes.c_double, vp, vp]),
+    "kvft_lambda_residual": (ctypes.c_int, [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                            ctypes.POINTER(vp), ctypes.POINTER(vp), vp, vp,
+                                            vp, vp, vp, vp]),
+    "kvft_einsum_plan": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_char_p,
+                                        ctypes.c_char_p, ctypes.c_char_p,
+                                        ctypes.POINTER(ctypes.c_int),
+                                        ctypes.POINTER(ctypes.c_int),
+                                        ctypes.POINTER(ctypes.c_longlong)]),
+    "kvft_dryrun_create": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.POINTER(vp)]),
+    "kvft_dryrun_count": (ctypes.c_int, [vp, ctypes.POINTER(ctypes.c_int)]),
+    "kvft_dryrun_op": (ctypes.c_int, [vp, ctypes.c_int, ctypes.POINTER(ctypes.c_int),
+                                      ctypes.POINTER(ctypes.c_longlong),
+                                      ctypes.POINTER(ctypes.c_double), ctypes.POINTER(vp)]),
+    "kvft_dryrun_scratch": (ctypes.c_int, [vp, ctypes.c_int, ctypes.POINTER(vp),
+                                           ctypes.POINTER(ctypes.c_size_t)]),
     "kvft_ft_cc_energy_noalloc": (ctypes.c_int, [vp, ctypes.c_int, ctypes.c_int,
                                                  ctypes.c_int, vp, vp, vp, vp, vp,
                                                  ctypes.c_double, ctypes.c_int, vp]),

@@ -2,7 +2,9 @@
 #include "kvft_internal.h"
 
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
+#include <iterator>
 #include <new>
 
 int kv_fail(kvft_ctx *ctx, int code, const std::string &msg) {
@@ -32,6 +34,20 @@ int kv_scratch(kvft_ctx *ctx, const char *key, size_t bytes, void **p) {
     auto it = ctx->scratch.find(key);
     if (it != ctx->scratch.end() && it->second.second >= bytes) {
         *p = it->second.first;
+        return KVFT_OK;
+    }
+    if (ctx->dry) {
+        // host memory, every double NaN: a read before any write shows
+        if (it != ctx->scratch.end()) {
+            std::free(it->second.first);
+            ctx->scratch.erase(it);
+        }
+        size_t b = bytes ? bytes : 256;
+        void *q = std::malloc(b);
+        if (!q) return kv_fail(ctx, KVFT_ENOMEM, "dry run: host scratch");
+        std::memset(q, 0xff, b);
+        ctx->scratch[key] = {q, b};
+        *p = q;
         return KVFT_OK;
     }
     if (it != ctx->scratch.end()) {
@@ -95,6 +111,12 @@ int kvft_ctx_create(int device, void *stream, kvft_ctx **out) {
 
 int kvft_ctx_destroy(kvft_ctx *c) {
     if (!c) return KVFT_OK;
+    if (c->dry) {
+        for (auto &kv : c->scratch) std::free(kv.second.first);
+        delete c->dry;
+        delete c;
+        return KVFT_OK;
+    }
     cudaSetDevice(c->device);
     cudaStreamSynchronize(c->stream);
     for (auto &kv : c->scratch) cudaFree(kv.second.first);
@@ -113,6 +135,71 @@ int kvft_ctx_destroy(kvft_ctx *c) {
 
 const char *kvft_last_error(const kvft_ctx *c) { return c ? c->err.c_str() : "null context"; }
 
+int kvft_dryrun_create(int precision, int digits, kvft_ctx **out) {
+    if (!out) return KVFT_EINVAL;
+    *out = nullptr;
+    kvft_ctx *c = new (std::nothrow) kvft_ctx();
+    if (!c) return KVFT_ENOMEM;
+    c->dry = new (std::nothrow) std::vector<KvDryOp>();
+    if (!c->dry) {
+        delete c;
+        return KVFT_ENOMEM;
+    }
+    c->sm_count = 152;
+    c->precision = precision;
+    c->digits = digits;
+    *out = c;
+    return KVFT_OK;
+}
+
+int kvft_dryrun_count(const kvft_ctx *c, int *count) {
+    if (!c || !c->dry || !count) return KVFT_EINVAL;
+    *count = (int)c->dry->size();
+    return KVFT_OK;
+}
+
+int kvft_dryrun_scratch(const kvft_ctx *c, int i, const void **ptr, size_t *bytes) {
+    if (!c || !c->dry || !ptr || !bytes || i < 0 || i >= (int)c->scratch.size())
+        return KVFT_EINVAL;
+    auto it = c->scratch.begin();
+    std::advance(it, i);
+    *ptr = it->second.first;
+    *bytes = it->second.second;
+    return KVFT_OK;
+}
+
+int kvft_dryrun_op(const kvft_ctx *c, int i, int *ints, long long *longs, double *dbls,
+                   const void **ptrs) {
+    if (!c || !c->dry || i < 0 || i >= (int)c->dry->size() || !ints || !longs || !dbls ||
+        !ptrs)
+        return KVFT_EINVAL;
+    const KvDryOp &op = (*c->dry)[i];
+    // ints: kind M N K batch | A.r A.c B.r B.c C.r C.c sizes (18) | dims (4) | ng rank
+    //       full nv no (5) = 32
+    // longs: A.r A.c B.r B.c C.r C.c strides (18) | A.bst B.bst C.bst | ss (4) ds (4)
+    //        sbst dbst | P = 32
+    const KIdx *ix[6] = {&op.A.r, &op.A.c, &op.B.r, &op.B.c, &op.C.r, &op.C.c};
+    ints[0] = op.kind, ints[1] = op.M, ints[2] = op.N, ints[3] = op.K, ints[4] = op.batch;
+    for (int k = 0; k < 6; k++)
+        for (int d = 0; d < 3; d++) {
+            ints[5 + 3 * k + d] = ix[k]->size[d];
+            longs[3 * k + d] = ix[k]->st[d];
+        }
+    for (int d = 0; d < 4; d++) {
+        ints[23 + d] = op.dims[d];
+        longs[21 + d] = op.ss[d];
+        longs[25 + d] = op.ds[d];
+    }
+    ints[27] = op.ng, ints[28] = op.rank, ints[29] = op.full, ints[30] = op.nv,
+    ints[31] = op.no;
+    longs[18] = op.A.bst, longs[19] = op.B.bst, longs[20] = op.C.bst;
+    longs[29] = op.sbst, longs[30] = op.dbst, longs[31] = op.P;
+    dbls[0] = op.alpha, dbls[1] = op.beta;
+    const void *p[8] = {op.A.p, op.B.p, op.C.p, op.src, op.dst, op.ti, op.G, op.ev};
+    for (int k = 0; k < 8; k++) ptrs[k] = p[k];
+    return KVFT_OK;
+}
+
 int kvft_set_precision(kvft_ctx *c, int precision, int digits) {
     if (!c) return KVFT_EINVAL;
     if (precision < KVFT_PREC_FP64 || precision > KVFT_PREC_MIXED)
@@ -125,6 +212,7 @@ int kvft_set_precision(kvft_ctx *c, int precision, int digits) {
 }
 
 int kvft_alloc(kvft_ctx *c, size_t bytes, void **p) {
+    if (c && c->dry) return kv_fail(c, KVFT_EINVAL, "kvft_alloc: not on a dry-run context");
     if (!c || !p) return KVFT_EINVAL;
     cudaSetDevice(c->device);
     KV_CHECK(c, cudaMalloc(p, bytes ? bytes : 16));
@@ -132,6 +220,7 @@ int kvft_alloc(kvft_ctx *c, size_t bytes, void **p) {
 }
 
 int kvft_free(kvft_ctx *c, void *p) {
+    if (c && c->dry) return kv_fail(c, KVFT_EINVAL, "kvft_free: not on a dry-run context");
     if (!c) return KVFT_EINVAL;
     KV_CHECK(c, cudaStreamSynchronize(c->stream));
     KV_CHECK(c, cudaFree(p));
@@ -139,12 +228,14 @@ int kvft_free(kvft_ctx *c, void *p) {
 }
 
 int kvft_h2d(kvft_ctx *c, void *dst, const void *src, size_t bytes) {
+    if (c && c->dry) return kv_fail(c, KVFT_EINVAL, "kvft_h2d: not on a dry-run context");
     if (!c) return KVFT_EINVAL;
     KV_CHECK(c, cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, c->stream));
     return KVFT_OK;
 }
 
 int kvft_d2h(kvft_ctx *c, void *dst, const void *src, size_t bytes) {
+    if (c && c->dry) return kv_fail(c, KVFT_EINVAL, "kvft_d2h: not on a dry-run context");
     if (!c) return KVFT_EINVAL;
     KV_CHECK(c, cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, c->stream));
     KV_CHECK(c, cudaStreamSynchronize(c->stream));
@@ -152,24 +243,28 @@ int kvft_d2h(kvft_ctx *c, void *dst, const void *src, size_t bytes) {
 }
 
 int kvft_memset(kvft_ctx *c, void *p, int v, size_t bytes) {
+    if (c && c->dry) return kv_fail(c, KVFT_EINVAL, "kvft_memset: not on a dry-run context");
     if (!c) return KVFT_EINVAL;
     KV_CHECK(c, cudaMemsetAsync(p, v, bytes, c->stream));
     return KVFT_OK;
 }
 
 int kvft_sync(kvft_ctx *c) {
+    if (c && c->dry) return kv_fail(c, KVFT_EINVAL, "kvft_sync: not on a dry-run context");
     if (!c) return KVFT_EINVAL;
     KV_CHECK(c, cudaStreamSynchronize(c->stream));
     return KVFT_OK;
 }
 
 int kvft_event_record(kvft_ctx *c, int slot) {
+    if (c && c->dry) return kv_fail(c, KVFT_EINVAL, "kvft_event_record: not on a dry-run context");
     if (!c || slot < 0 || slot >= 64) return KVFT_EINVAL;
     KV_CHECK(c, cudaEventRecord(c->ev[slot], c->stream));
     return KVFT_OK;
 }
 
 int kvft_event_elapsed_ms(kvft_ctx *c, int s0, int s1, float *ms) {
+    if (c && c->dry) return kv_fail(c, KVFT_EINVAL, "kvft_event_elapsed_ms: not on a dry-run context");
     if (!c || s0 < 0 || s0 >= 64 || s1 < 0 || s1 >= 64 || !ms) return KVFT_EINVAL;
     KV_CHECK(c, cudaEventSynchronize(c->ev[s1]));
     KV_CHECK(c, cudaEventElapsedTime(ms, c->ev[s0], c->ev[s1]));
@@ -212,6 +307,7 @@ KvProfScope::~KvProfScope() {
 }
 
 extern "C" int kvft_profile_begin(kvft_ctx *c) {
+    if (c && c->dry) return kv_fail(c, KVFT_EINVAL, "kvft_profile_begin: not on a dry-run context");
     if (!c) return KVFT_EINVAL;
     if (!c->prof) c->prof = new KvProf();
     c->prof->on = true;
@@ -222,6 +318,7 @@ extern "C" int kvft_profile_begin(kvft_ctx *c) {
 
 extern "C" int kvft_profile_records(kvft_ctx *c, int max, int *count, int *cat, float *ms,
                                     double *work) {
+    if (c && c->dry) return kv_fail(c, KVFT_EINVAL, "kvft_profile_records: not on a dry-run context");
     if (!c || !c->prof || !count || max < 0 || (max > 0 && (!cat || !ms || !work)))
         return KVFT_EINVAL;
     KV_CHECK(c, cudaStreamSynchronize(c->stream));
@@ -238,6 +335,7 @@ extern "C" int kvft_profile_records(kvft_ctx *c, int max, int *count, int *cat, 
 }
 
 extern "C" int kvft_profile_end(kvft_ctx *c, kvft_profile_stats *out) {
+    if (c && c->dry) return kv_fail(c, KVFT_EINVAL, "kvft_profile_end: not on a dry-run context");
     if (!c || !c->prof || !out) return KVFT_EINVAL;
     KV_CHECK(c, cudaStreamSynchronize(c->stream));
     memset(out, 0, sizeof(*out));
@@ -261,6 +359,7 @@ __global__ void kv_flush_kernel(uint4 *p, size_t n, unsigned salt) {
 }
 
 extern "C" int kvft_flush_l2(kvft_ctx *c) {
+    if (c && c->dry) return kv_fail(c, KVFT_EINVAL, "kvft_flush_l2: not on a dry-run context");
     if (!c) return KVFT_EINVAL;
     const size_t bytes = 256ull << 20;  // twice the 129 MB L2
     if (!c->l2buf) KV_CHECK(c, cudaMalloc(&c->l2buf, bytes));

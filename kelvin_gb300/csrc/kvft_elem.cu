@@ -377,6 +377,15 @@ int kv_axpby4(kvft_ctx *ctx, int batch, const int dims[4], double alpha,
     g.sbst = sbst;
     g.dbst = dbst;
     if (total == 0) return KVFT_OK;
+    if (ctx->dry) {
+        KvDryOp op;
+        op.kind = 1;
+        op.batch = batch, op.alpha = alpha, op.beta = beta;
+        for (int k = 0; k < 4; k++) op.dims[k] = dims[k], op.ss[k] = ss[k], op.ds[k] = ds[k];
+        op.sbst = sbst, op.dbst = dbst, op.src = src, op.dst = dst;
+        ctx->dry->push_back(op);
+        return KVFT_OK;
+    }
     KvProfScope prof(ctx, KV_CAT_ELEM, 8.0 * total * (beta != 0.0 ? 3 : 2));
     const long long nblk = (long long)batch * dims[0] * dims[1] *
                            (((long long)dims[2] * dims[3] + AX_CHUNK - 1) / AX_CHUNK);

@@ -180,6 +180,7 @@ extern "C" int kvft_ft_cc_energy(kvft_ctx *ctx, int ng, int nv, int no, const do
                                  const double *T2, const double *f, const double *eri,
                                  const double *g, double beta, int qterm,
                                  double *omega_host) {
+    if (ctx && ctx->dry) return kv_fail(ctx, KVFT_EINVAL, "kvft_ft_cc_energy: not on a dry-run context");
     if (!ctx || ng < 1 || nv <= 0 || no <= 0 || !T1 || !T2 || !f || !eri || !g || !omega_host ||
         beta == 0.0)
         return kv_fail(ctx, KVFT_EINVAL, "ft_cc_energy: bad argument");

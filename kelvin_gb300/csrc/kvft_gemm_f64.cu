@@ -116,6 +116,13 @@ __global__ void scale_view_kernel(int M, int N, int batch, double beta, KOut C) 
 
 int kv_scale_view(kvft_ctx *ctx, int M, int N, int batch, double beta, const KOut &C) {
     if (beta == 1.0 || M <= 0 || N <= 0 || batch <= 0) return KVFT_OK;
+    if (ctx->dry) {
+        KvDryOp op;
+        op.kind = 3;
+        op.M = M, op.N = N, op.batch = batch, op.beta = beta, op.C = C;
+        ctx->dry->push_back(op);
+        return KVFT_OK;
+    }
     scale_view_kernel<<<ctx->sm_count * 4, 256, 0, ctx->stream>>>(M, N, batch, beta, C);
     return kv_launch_check(ctx, "scale_view");
 }
@@ -222,6 +229,15 @@ void kv_gemm_prof_set(kvft_ctx *ctx, int M, int N, int K, int batch, int nbA, in
 
 int kv_gemm(kvft_ctx *ctx, int M, int N, int K, int batch, double alpha,
             const KMat &A_in, const KMat &B_in, double beta, const KOut &C) {
+    if (ctx->dry) {
+        KvDryOp op;
+        op.kind = 0;
+        op.M = M, op.N = N, op.K = K, op.batch = batch;
+        op.alpha = alpha, op.beta = beta;
+        op.A = A_in, op.B = B_in, op.C = C;
+        ctx->dry->push_back(op);
+        return KVFT_OK;
+    }
     KMat A = A_in, B = B_in;
     order_k(M, N, batch, A, B);
     // Tensor cores for everything but short sums and tiny products, which stay

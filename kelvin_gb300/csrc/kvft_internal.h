@@ -62,6 +62,25 @@ inline long long kidx_fast_stride(const KIdx &x) {
 enum KvCat { KV_CAT_GEMM6 = 0, KV_CAT_GEMM = 1, KV_CAT_QUAD = 2, KV_CAT_ENERGY = 3,
              KV_CAT_ELEM = 4, KV_CAT_PACK = 5, KV_NCAT = 6 };
 
+// One recorded launch of a dry-run context (kvft_dryrun_create): the
+// descriptors a kernel would have been launched with.
+struct KvDryOp {
+    int kind;                        // 0 contraction, 1 strided axpby, 2 tau integral,
+                                     // 3 scale
+    int M = 0, N = 0, K = 0, batch = 0;
+    double alpha = 0.0, beta = 0.0;
+    KMat A{}, B{};
+    KOut C{};
+    int dims[4] = {1, 1, 1, 1};
+    long long ss[4] = {0, 0, 0, 0}, ds[4] = {0, 0, 0, 0}, sbst = 0, dbst = 0;
+    const double *src = nullptr;
+    double *dst = nullptr;
+    // tau integral: ng, P, rank, full, nv, no and its operands
+    int ng = 0, rank = 0, full = 0, nv = 0, no = 0;
+    long long P = 0;
+    const double *ti = nullptr, *G = nullptr, *ev = nullptr, *eo = nullptr;
+};
+
 // ---------------------------------------------------------------------------
 // Context
 // ---------------------------------------------------------------------------
@@ -94,6 +113,9 @@ struct kvft_ctx {
     // and the integrals and amplitudes vanish outside spin-conserving blocks
     // (set by a solver that has checked its integrals).
     int spin_half = 0;
+    // Dry run: launches are recorded here instead of executed, and scratch
+    // is host memory filled with NaN (a context without a device).
+    std::vector<KvDryOp> *dry = nullptr;
 };
 struct KvSpinScope {
     kvft_ctx *ctx;
@@ -225,4 +247,36 @@ int kv_stanton(kvft_ctx *ctx, int nb, int nv, int no,
                const double *t1, const double *t2, double fac, double *T1,
                double *T2, const double *seed_t2 = nullptr);
 size_t kv_stanton_workspace(int nb, int nv, int no);
+
+// ---- contractions named by index strings ------------------------------------
+// A tensor laid out row-major over the letters of `ix` (last fastest); a..h
+// run over the nv virtual orbitals, i..n over the no occupied ones.  bst is
+// the stride between tau points (0: shared by the batch).
+struct KvTen {
+    const double *p;
+    const char *ix;
+    long long bst;
+    int stable;                      // an integral block (fixed for a solver's lifetime)
+};
+// The strided-GEMM form of C[cix] = alpha sum A[A.ix] B[B.ix] + beta C: rows
+// are the letters of A and C, columns those of B and C, the sum runs over the
+// letters of A and B; each group keeps at most three strided components.
+int kv_einsum_desc(int nv, int no, const char *aix, const char *bix, const char *cix,
+                   int *M, int *N, int *K, KIdx *Ar, KIdx *Ac, KIdx *Br, KIdx *Bc,
+                   KIdx *Cr, KIdx *Cc, std::string *err);
+int kv_einsum(kvft_ctx *ctx, int nv, int no, int batch, double alpha, const KvTen &A,
+              const KvTen &B, double beta, double *C, const char *cix, long long cbst);
+// dst[dix] = beta dst + alpha src[src.ix] over the same letters (a transpose
+// or a copy; at most four letters)
+int kv_add(kvft_ctx *ctx, int nv, int no, int batch, double alpha, const KvTen &src,
+           double beta, double *dst, const char *dix, long long dbst);
+
+// Lambda terms of one tau batch: g = R'(t)^T m, the transpose of the
+// residual's Jacobian applied to m (m1[i,a], m2[i,j,a,b] in Lambda layout;
+// g1[a,i], g2[a,b,i,j] in amplitude layout, g2 antisymmetric), with
+//   sum g1 dt1 + 1/4 sum g2 dt2 = sum m1 dR1 + 1/4 sum m2 dR2.
+int kv_lambda_vjp(kvft_ctx *ctx, int nb, int nv, int no, const double *const F[4],
+                  const double *const I[9], const double *t1, const double *t2,
+                  const double *m1, const double *m2, double *g1, double *g2);
+size_t kv_lambda_workspace(int nb, int nv, int no);
 size_t kv_chunk_bytes_per_tau(kvft_ctx *ctx, int nv, int no);

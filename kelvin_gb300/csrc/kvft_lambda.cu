@@ -1,0 +1,453 @@
+// The Lambda terms of FT-CCSD on the device: R'(t)^T m, the transpose of the
+// CCSD residual's Jacobian applied to a Lambda-shaped tensor.  Kelvin's Lambda
+// iteration (kelvin/ft_cc_equations.py:385-409) hands these terms to
+// cqcpy.cc_equations._Lambda_opt; Lambda is the adjoint of the amplitude
+// iteration, so they are evaluated here as the reverse pass through the same
+// Stanton-Gauss intermediates the residual builds (F_ae, F_mi, F_me, W_mnij,
+// W_abef, W_mbej), term by term.
+//
+// Every contraction is written as an index-string contraction (kv_einsum),
+// which lowers to one strided GEMM (kv_gemm: tensor cores or the FP64 pipe),
+// and every permuted sum as a strided axpby (kv_add); no other kernel runs.
+// The intermediates are kept in plain (not pair-compressed) form; the spin-
+// block and pair-ladder savings of the forward residual are not applied here.
+#include "kvft_internal.h"
+
+#include <cstring>
+
+namespace {
+
+long long letter_extent(char c, int nv, int no) {
+    if (c >= 'a' && c <= 'h') return nv;
+    if (c >= 'i' && c <= 'n') return no;
+    return -1;
+}
+
+struct Layout {
+    std::string ix;
+    std::vector<long long> ext, st;
+    long long size = 1;
+};
+
+bool make_layout(const char *ix, int nv, int no, Layout *L, std::string *err) {
+    L->ix = ix ? ix : "";
+    const int n = (int)L->ix.size();
+    if (n == 0 || n > 4) {
+        *err = "einsum: a tensor needs one to four indices: " + L->ix;
+        return false;
+    }
+    L->ext.assign(n, 0);
+    L->st.assign(n, 0);
+    long long s = 1;
+    for (int k = n - 1; k >= 0; k--) {
+        const long long e = letter_extent(L->ix[k], nv, no);
+        if (e < 0) {
+            *err = "einsum: index letters are a-h (virtual) or i-n (occupied): " + L->ix;
+            return false;
+        }
+        if (L->ix.find(L->ix[k]) != (size_t)k) {
+            *err = "einsum: repeated index in " + L->ix;
+            return false;
+        }
+        L->ext[k] = e;
+        L->st[k] = s;
+        s *= e;
+    }
+    L->size = s;
+    return true;
+}
+
+long long stride_of(const Layout &L, char c) {
+    const size_t k = L.ix.find(c);
+    return k == std::string::npos ? -1 : L.st[k];
+}
+
+// One composite index (at most three strided components) per tensor for the
+// letters of group g, merging neighbours that are contiguous in every tensor.
+bool group_index(const std::string &g, const Layout *const *ts, KIdx *const *out, int nt,
+                 int nv, int no, std::string *err) {
+    struct Comp {
+        long long ext;
+        long long st[2];
+    };
+    std::vector<Comp> comps;
+    for (char c : g) {
+        Comp cp;
+        cp.ext = letter_extent(c, nv, no);
+        for (int t = 0; t < nt; t++) cp.st[t] = stride_of(*ts[t], c);
+        comps.push_back(cp);
+    }
+    while (comps.size() > 3) {
+        bool merged = false;
+        for (size_t k = 0; k + 1 < comps.size() && !merged; k++) {
+            bool ok = true;
+            for (int t = 0; t < nt; t++)
+                if (comps[k].st[t] != comps[k + 1].st[t] * comps[k + 1].ext) ok = false;
+            if (ok) {
+                comps[k].ext *= comps[k + 1].ext;
+                for (int t = 0; t < nt; t++) comps[k].st[t] = comps[k + 1].st[t];
+                comps.erase(comps.begin() + k + 1);
+                merged = true;
+            }
+        }
+        if (!merged) {
+            *err = "einsum: index group " + g + " needs more than three strided components";
+            return false;
+        }
+    }
+    const int off = 3 - (int)comps.size();
+    for (int t = 0; t < nt; t++) {
+        KIdx &x = *out[t];
+        x = KIdx{{1, 1, 1}, {0, 0, 0}};
+        for (size_t k = 0; k < comps.size(); k++) {
+            x.size[off + k] = (int)comps[k].ext;
+            x.st[off + k] = comps[k].st[t];
+        }
+    }
+    return true;
+}
+
+}  // namespace
+
+int kv_einsum_desc(int nv, int no, const char *aix, const char *bix, const char *cix, int *M,
+                   int *N, int *K, KIdx *Ar, KIdx *Ac, KIdx *Br, KIdx *Bc, KIdx *Cr, KIdx *Cc,
+                   std::string *err) {
+    Layout A, B, C;
+    if (!make_layout(aix, nv, no, &A, err) || !make_layout(bix, nv, no, &B, err) ||
+        !make_layout(cix, nv, no, &C, err))
+        return KVFT_EINVAL;
+    const size_t npos = std::string::npos;
+    std::string gm, gn, gk;
+    for (char c : A.ix) {
+        const bool inB = B.ix.find(c) != npos, inC = C.ix.find(c) != npos;
+        if (inB == inC) {
+            *err = std::string("einsum: index ") + c + " must be in exactly one of " + B.ix +
+                   " and " + C.ix;
+            return KVFT_EINVAL;
+        }
+        if (inB) gk += c;
+    }
+    for (char c : B.ix)
+        if ((A.ix.find(c) != npos) == (C.ix.find(c) != npos)) {
+            *err = std::string("einsum: index ") + c + " must be in exactly one of " + A.ix +
+                   " and " + C.ix;
+            return KVFT_EINVAL;
+        }
+    for (char c : C.ix) {
+        const bool inA = A.ix.find(c) != npos, inB = B.ix.find(c) != npos;
+        if (inA == inB) {
+            *err = std::string("einsum: output index ") + c + " must come from one input";
+            return KVFT_EINVAL;
+        }
+        (inA ? gm : gn) += c;
+    }
+    const Layout *mt[2] = {&A, &C}, *nt[2] = {&B, &C}, *kt[2] = {&A, &B};
+    KIdx *mo[2] = {Ar, Cr}, *no_[2] = {Bc, Cc}, *ko[2] = {Ac, Br};
+    if (!group_index(gm, mt, mo, 2, nv, no, err) || !group_index(gn, nt, no_, 2, nv, no, err) ||
+        !group_index(gk, kt, ko, 2, nv, no, err))
+        return KVFT_EINVAL;
+    const long long m = (long long)Ar->size[0] * Ar->size[1] * Ar->size[2];
+    const long long n = (long long)Bc->size[0] * Bc->size[1] * Bc->size[2];
+    const long long k = (long long)Ac->size[0] * Ac->size[1] * Ac->size[2];
+    if (m > 0x7fffffffLL || n > 0x7fffffffLL || k > 0x7fffffffLL) {
+        *err = "einsum: a GEMM dimension exceeds 2^31";
+        return KVFT_EINVAL;
+    }
+    *M = (int)m;
+    *N = (int)n;
+    *K = (int)k;
+    return KVFT_OK;
+}
+
+int kv_einsum(kvft_ctx *ctx, int nv, int no, int batch, double alpha, const KvTen &A,
+              const KvTen &B, double beta, double *C, const char *cix, long long cbst) {
+    int M, N, K;
+    KIdx ar, ac, br, bc, cr, cc;
+    std::string err;
+    if (kv_einsum_desc(nv, no, A.ix, B.ix, cix, &M, &N, &K, &ar, &ac, &br, &bc, &cr, &cc,
+                       &err) != KVFT_OK)
+        return kv_fail(ctx, KVFT_EINVAL, err);
+    KMat a{A.p, ar, ac, A.bst, A.stable}, b{B.p, br, bc, B.bst, B.stable};
+    KOut c{C, cr, cc, cbst};
+    return kv_gemm(ctx, M, N, K, batch, alpha, a, b, beta, c);
+}
+
+int kv_add(kvft_ctx *ctx, int nv, int no, int batch, double alpha, const KvTen &src,
+           double beta, double *dst, const char *dix, long long dbst) {
+    Layout S, D;
+    std::string err;
+    if (!make_layout(src.ix, nv, no, &S, &err) || !make_layout(dix, nv, no, &D, &err))
+        return kv_fail(ctx, KVFT_EINVAL, err);
+    if (S.ix.size() != D.ix.size())
+        return kv_fail(ctx, KVFT_EINVAL, "add: " + S.ix + " and " + D.ix + " differ");
+    int dims[4] = {1, 1, 1, 1};
+    long long ss[4] = {0, 0, 0, 0}, ds[4] = {0, 0, 0, 0};
+    const int off = 4 - (int)D.ix.size();
+    for (size_t k = 0; k < D.ix.size(); k++) {
+        const long long s = stride_of(S, D.ix[k]);
+        if (s < 0) return kv_fail(ctx, KVFT_EINVAL, "add: " + S.ix + " and " + D.ix + " differ");
+        dims[off + k] = (int)D.ext[k];
+        ds[off + k] = D.st[k];
+        ss[off + k] = s;
+    }
+    return kv_axpby4(ctx, batch, dims, alpha, src.p, ss, src.bst, beta, dst, ds, dbst);
+}
+
+// ---- the reverse pass ----------------------------------------------------------
+
+namespace {
+
+struct LWS {
+    double *tau, *ttau, *tmp, *Wmbej, *Wabef, *Wmnij, *Fae, *Fmi, *Fme, *Xbe, *Xmj;
+    double *xA, *xI, *xAI, *Y1, *Y2, *taub, *ttaub, *ttb, *t2b, *tmpb, *Wmbejb, *Wabefb,
+        *Wmnijb, *xW4, *Faeb, *Fmib, *Fmeb, *Xbeb, *Xmjb;
+};
+
+// doubles per tau point, in carve order
+void ws_sizes(long long v, long long o, long long *sz) {
+    const long long v2o2 = v * v * o * o, v4 = v * v * v * v, o4 = o * o * o * o;
+    const long long t[30] = {v2o2, v2o2, v2o2, v2o2, v4, o4, v * v, o * o, o * v, v * v,
+                             o * o, v2o2, v2o2, v2o2, v * o * o * o, v * v * v * o, v2o2, v2o2,
+                             v2o2, v2o2, v2o2, v2o2, v4, o4, std::max(v4, o4), v * v, o * o,
+                             o * v, v * v, o * o};
+    for (int k = 0; k < 30; k++) sz[k] = t[k];
+}
+
+long long per_tau(long long v, long long o) {
+    long long sz[30], s = 0;
+    ws_sizes(v, o, sz);
+    for (int k = 0; k < 30; k++) s += (sz[k] + 1) / 2 * 2;      // 16-byte aligned slices
+    return s;
+}
+
+LWS carve(double *p, int nb, long long v, long long o) {
+    long long sz[30];
+    ws_sizes(v, o, sz);
+    double **slot[30];
+    LWS w;
+    double **q[30] = {&w.tau, &w.ttau, &w.tmp, &w.Wmbej, &w.Wabef, &w.Wmnij, &w.Fae, &w.Fmi,
+                      &w.Fme, &w.Xbe, &w.Xmj, &w.xA, &w.xI, &w.xAI, &w.Y1, &w.Y2, &w.taub,
+                      &w.ttaub, &w.ttb, &w.t2b, &w.tmpb, &w.Wmbejb, &w.Wabefb, &w.Wmnijb,
+                      &w.xW4, &w.Faeb, &w.Fmib, &w.Fmeb, &w.Xbeb, &w.Xmjb};
+    for (int k = 0; k < 30; k++) slot[k] = q[k];
+    for (int k = 0; k < 30; k++) {
+        *slot[k] = p;
+        p += (long long)nb * ((sz[k] + 1) / 2 * 2);
+    }
+    return w;
+}
+
+}  // namespace
+
+size_t kv_lambda_workspace(int nb, int nv, int no) {
+    return sizeof(double) * (size_t)nb * (size_t)per_tau(nv, no);
+}
+
+int kv_lambda_vjp(kvft_ctx *ctx, int nb, int nv, int no, const double *const F[4],
+                  const double *const I[9], const double *t1, const double *t2,
+                  const double *m1, const double *m2, double *g1, double *g2) {
+    if (nb <= 0) return KVFT_OK;
+    const long long v = nv, o = no;
+    const long long vo = v * o, v2o2 = v * v * o * o;
+    const double *Foo = F[0], *Fov = F[1], *Fvv = F[3];
+    const double *vvvv = I[0], *vvvo = I[1], *vovv = I[2], *vovo = I[4], *oovv = I[5],
+                 *vooo = I[6], *ooov = I[7], *oooo = I[8];
+    void *wsp = nullptr;
+    KV_TRY(kv_scratch(ctx, "lambda", kv_lambda_workspace(nb, nv, no), &wsp));
+    long long sz[30];
+    ws_sizes(v, o, sz);
+    const LWS w = carve((double *)wsp, nb, v, o);
+    const int B = nb;
+    // per-tau strides of the workspace slices (16-byte aligned sizes)
+    auto bs = [&](int k) { return (sz[k] + 1) / 2 * 2; };
+    const long long s_tau = bs(0), s_tmp = bs(2), s_wmbej = bs(3), s_w4v = bs(4),
+                    s_w4o = bs(5), s_vv = bs(6), s_oo = bs(7), s_ov = bs(8), s_y1 = bs(14),
+                    s_y2 = bs(15), s_x4 = bs(24);
+
+    // tensors: an integral block (shared, stable), a per-tau operand
+    auto IB = [](const double *p, const char *ix) { return KvTen{p, ix, 0, 1}; };
+    auto TT = [](const double *p, const char *ix, long long bst) { return KvTen{p, ix, bst, 0}; };
+    auto E = [&](double alpha, const KvTen &A, const KvTen &Bt, double beta, double *C,
+                 const char *cix, long long cbst) {
+        return kv_einsum(ctx, nv, no, B, alpha, A, Bt, beta, C, cix, cbst);
+    };
+    auto ADD = [&](double alpha, const KvTen &S, double beta, double *D, const char *dix,
+                   long long dbst) { return kv_add(ctx, nv, no, B, alpha, S, beta, D, dix, dbst); };
+
+    // ---- forward intermediates (oracle cc_equations.intermediates) ----------
+    // ttau = t2 + 1/2 P(ab) t1 t1, tau = t2 + P(ab) t1 t1
+    KV_TRY(ADD(1.0, TT(t2, "abij", v2o2), 0.0, w.ttau, "abij", s_tau));
+    KV_TRY(E(0.5, TT(t1, "ai", vo), TT(t1, "bj", vo), 1.0, w.ttau, "abij", s_tau));
+    KV_TRY(E(-0.5, TT(t1, "bi", vo), TT(t1, "aj", vo), 1.0, w.ttau, "abij", s_tau));
+    KV_TRY(ADD(1.0, TT(t2, "abij", v2o2), 0.0, w.tau, "abij", s_tau));
+    KV_TRY(E(1.0, TT(t1, "ai", vo), TT(t1, "bj", vo), 1.0, w.tau, "abij", s_tau));
+    KV_TRY(E(-1.0, TT(t1, "bi", vo), TT(t1, "aj", vo), 1.0, w.tau, "abij", s_tau));
+    // F_ae = vv - 1/2 ov[m,e] t1[a,m] - t1[f,m] vovv[a,m,f,e] - 1/2 ttau[a,f,m,n] oovv[m,n,e,f]
+    KV_TRY(ADD(1.0, IB(Fvv, "ae"), 0.0, w.Fae, "ae", s_vv));
+    KV_TRY(E(-0.5, IB(Fov, "me"), TT(t1, "am", vo), 1.0, w.Fae, "ae", s_vv));
+    KV_TRY(E(-1.0, TT(t1, "fm", vo), IB(vovv, "amfe"), 1.0, w.Fae, "ae", s_vv));
+    KV_TRY(E(-0.5, TT(w.ttau, "afmn", s_tau), IB(oovv, "mnef"), 1.0, w.Fae, "ae", s_vv));
+    // F_mi = oo + 1/2 t1[e,i] ov[m,e] + t1[e,n] ooov[m,n,i,e] + 1/2 ttau[e,f,i,n] oovv[m,n,e,f]
+    KV_TRY(ADD(1.0, IB(Foo, "mi"), 0.0, w.Fmi, "mi", s_oo));
+    KV_TRY(E(0.5, TT(t1, "ei", vo), IB(Fov, "me"), 1.0, w.Fmi, "mi", s_oo));
+    KV_TRY(E(1.0, TT(t1, "en", vo), IB(ooov, "mnie"), 1.0, w.Fmi, "mi", s_oo));
+    KV_TRY(E(0.5, TT(w.ttau, "efin", s_tau), IB(oovv, "mnef"), 1.0, w.Fmi, "mi", s_oo));
+    // F_me = ov + t1[f,n] oovv[m,n,e,f]
+    KV_TRY(ADD(1.0, IB(Fov, "me"), 0.0, w.Fme, "me", s_ov));
+    KV_TRY(E(1.0, TT(t1, "fn", vo), IB(oovv, "mnef"), 1.0, w.Fme, "me", s_ov));
+    // W_mnij = oooo + P(ij) t1[e,j] ooov[m,n,i,e] + 1/4 tau[e,f,i,j] oovv[m,n,e,f]
+    KV_TRY(ADD(1.0, IB(oooo, "mnij"), 0.0, w.Wmnij, "mnij", s_w4o));
+    KV_TRY(E(1.0, TT(t1, "ej", vo), IB(ooov, "mnie"), 1.0, w.Wmnij, "mnij", s_w4o));
+    KV_TRY(E(-1.0, TT(t1, "ej", vo), IB(ooov, "mnie"), 1.0, w.Wmnij, "mnji", s_w4o));
+    KV_TRY(E(0.25, TT(w.tau, "efij", s_tau), IB(oovv, "mnef"), 1.0, w.Wmnij, "mnij", s_w4o));
+    // W_abef = vvvv - P(ab) t1[b,m] vovv[a,m,e,f] + 1/4 tau[a,b,m,n] oovv[m,n,e,f]
+    KV_TRY(ADD(1.0, IB(vvvv, "abef"), 0.0, w.Wabef, "abef", s_w4v));
+    KV_TRY(E(-1.0, TT(t1, "bm", vo), IB(vovv, "amef"), 1.0, w.Wabef, "abef", s_w4v));
+    KV_TRY(E(1.0, TT(t1, "bm", vo), IB(vovv, "amef"), 1.0, w.Wabef, "baef", s_w4v));
+    KV_TRY(E(0.25, TT(w.tau, "abmn", s_tau), IB(oovv, "mnef"), 1.0, w.Wabef, "abef", s_w4v));
+    // tmp = 1/2 t2[f,b,j,n] + t1[f,j] t1[b,n]
+    KV_TRY(ADD(0.5, TT(t2, "fbjn", v2o2), 0.0, w.tmp, "fbjn", s_tmp));
+    KV_TRY(E(1.0, TT(t1, "fj", vo), TT(t1, "bn", vo), 1.0, w.tmp, "fbjn", s_tmp));
+    // W_mbej = -vovo[b,m,e,j] - t1[f,j] vovv[b,m,e,f] + t1[b,n] ooov[m,n,j,e]
+    //          - tmp[f,b,j,n] oovv[m,n,e,f]
+    KV_TRY(ADD(-1.0, IB(vovo, "bmej"), 0.0, w.Wmbej, "mbej", s_wmbej));
+    KV_TRY(E(-1.0, TT(t1, "fj", vo), IB(vovv, "bmef"), 1.0, w.Wmbej, "mbej", s_wmbej));
+    KV_TRY(E(1.0, TT(t1, "bn", vo), IB(ooov, "mnje"), 1.0, w.Wmbej, "mbej", s_wmbej));
+    KV_TRY(E(-1.0, TT(w.tmp, "fbjn", s_tmp), IB(oovv, "mnef"), 1.0, w.Wmbej, "mbej", s_wmbej));
+
+    // ---- R2 terms, with R2b = m2 / 4 ------------------------------------------
+    // xA = P(ab) R2b, xI = P(ij) R2b, xAI = P(ab) P(ij) R2b (amplitude layout)
+    KV_TRY(ADD(0.25, TT(m2, "ijab", v2o2), 0.0, w.xA, "abij", s_tau));
+    KV_TRY(ADD(-0.25, TT(m2, "ijba", v2o2), 1.0, w.xA, "abij", s_tau));
+    KV_TRY(ADD(0.25, TT(m2, "ijab", v2o2), 0.0, w.xI, "abij", s_tau));
+    KV_TRY(ADD(-0.25, TT(m2, "jiab", v2o2), 1.0, w.xI, "abij", s_tau));
+    KV_TRY(ADD(1.0, TT(w.xA, "abij", s_tau), 0.0, w.xAI, "abij", s_tau));
+    KV_TRY(ADD(-1.0, TT(w.xA, "abji", s_tau), 1.0, w.xAI, "abij", s_tau));
+    // x = t1[a,m] vooo[b,m,i,j]: t1b[a,m] = xA . vooo   (first write of g1)
+    KV_TRY(E(1.0, TT(w.xA, "abij", s_tau), IB(vooo, "bmij"), 0.0, g1, "am", vo));
+    // x = t1[e,i] vvvo[a,b,e,j]
+    KV_TRY(E(1.0, TT(w.xI, "abij", s_tau), IB(vvvo, "abej"), 1.0, g1, "ei", vo));
+    // ring: x = t2[a,e,i,m] W_mbej + t1[e,i] t1[a,m] vovo[b,m,e,j]   (first write of t2b)
+    KV_TRY(E(1.0, TT(w.xAI, "abij", s_tau), TT(w.Wmbej, "mbej", s_wmbej), 0.0, w.t2b, "aeim",
+             s_tau));
+    KV_TRY(E(1.0, TT(w.xAI, "abij", s_tau), TT(t2, "aeim", v2o2), 0.0, w.Wmbejb, "mbej",
+             s_wmbej));
+    KV_TRY(E(1.0, TT(w.xAI, "abij", s_tau), TT(t1, "am", vo), 0.0, w.Y1, "bijm", s_y1));
+    KV_TRY(E(1.0, TT(w.Y1, "bijm", s_y1), IB(vovo, "bmej"), 1.0, g1, "ei", vo));
+    KV_TRY(E(1.0, TT(w.xAI, "abij", s_tau), TT(t1, "ei", vo), 0.0, w.Y2, "abej", s_y2));
+    KV_TRY(E(1.0, TT(w.Y2, "abej", s_y2), IB(vovo, "bmej"), 1.0, g1, "am", vo));
+    // R2 += 1/2 tau[e,f,i,j] W_abef and 1/2 tau[a,b,m,n] W_mnij (R2b = m2/4)
+    KV_TRY(E(0.125, TT(m2, "ijab", v2o2), TT(w.Wabef, "abef", s_w4v), 0.0, w.taub, "efij",
+             s_tau));
+    KV_TRY(E(0.125, TT(m2, "ijab", v2o2), TT(w.tau, "efij", s_tau), 0.0, w.Wabefb, "abef",
+             s_w4v));
+    KV_TRY(E(0.125, TT(m2, "ijab", v2o2), TT(w.Wmnij, "mnij", s_w4o), 1.0, w.taub, "abmn",
+             s_tau));
+    KV_TRY(E(0.125, TT(m2, "ijab", v2o2), TT(w.tau, "abmn", s_tau), 0.0, w.Wmnijb, "mnij",
+             s_w4o));
+    // x = t2[a,b,i,m] X_mj, X_mj = F_mi + 1/2 t1[e,j] F_me;  R2 -= P(ij) x
+    KV_TRY(ADD(1.0, TT(w.Fmi, "mj", s_oo), 0.0, w.Xmj, "mj", s_oo));
+    KV_TRY(E(0.5, TT(t1, "ej", vo), TT(w.Fme, "me", s_ov), 1.0, w.Xmj, "mj", s_oo));
+    KV_TRY(E(-1.0, TT(w.xI, "abij", s_tau), TT(w.Xmj, "mj", s_oo), 1.0, w.t2b, "abim", s_tau));
+    KV_TRY(E(-1.0, TT(w.xI, "abij", s_tau), TT(t2, "abim", v2o2), 0.0, w.Xmjb, "mj", s_oo));
+    // x = t2[a,e,i,j] X_be, X_be = F_ae - 1/2 t1[b,m] F_me;  R2 += P(ab) x
+    KV_TRY(ADD(1.0, TT(w.Fae, "be", s_vv), 0.0, w.Xbe, "be", s_vv));
+    KV_TRY(E(-0.5, TT(t1, "bm", vo), TT(w.Fme, "me", s_ov), 1.0, w.Xbe, "be", s_vv));
+    KV_TRY(E(1.0, TT(w.xA, "abij", s_tau), TT(w.Xbe, "be", s_vv), 1.0, w.t2b, "aeij", s_tau));
+    KV_TRY(E(1.0, TT(w.xA, "abij", s_tau), TT(t2, "aeij", v2o2), 0.0, w.Xbeb, "be", s_vv));
+    // back through X_mj and X_be
+    KV_TRY(ADD(1.0, TT(w.Xmjb, "mi", s_oo), 0.0, w.Fmib, "mi", s_oo));
+    KV_TRY(E(0.5, TT(w.Xmjb, "mj", s_oo), TT(w.Fme, "me", s_ov), 1.0, g1, "ej", vo));
+    KV_TRY(E(0.5, TT(w.Xmjb, "mj", s_oo), TT(t1, "ej", vo), 0.0, w.Fmeb, "me", s_ov));
+    KV_TRY(ADD(1.0, TT(w.Xbeb, "ae", s_vv), 0.0, w.Faeb, "ae", s_vv));
+    KV_TRY(E(-0.5, TT(w.Xbeb, "be", s_vv), TT(w.Fme, "me", s_ov), 1.0, g1, "bm", vo));
+    KV_TRY(E(-0.5, TT(w.Xbeb, "be", s_vv), TT(t1, "bm", vo), 1.0, w.Fmeb, "me", s_ov));
+
+    // ---- R1 terms, R1b = m1 ----------------------------------------------------
+    const KvTen m1v = TT(m1, "ia", vo);
+    KV_TRY(E(1.0, m1v, TT(t1, "ei", vo), 1.0, w.Faeb, "ae", s_vv));
+    KV_TRY(E(1.0, m1v, TT(w.Fae, "ae", s_vv), 1.0, g1, "ei", vo));
+    KV_TRY(E(-1.0, TT(m1, "ia", vo), TT(w.Fmi, "mi", s_oo), 1.0, g1, "am", vo));
+    KV_TRY(E(-1.0, TT(m1, "ia", vo), TT(t1, "am", vo), 1.0, w.Fmib, "mi", s_oo));
+    KV_TRY(E(1.0, m1v, TT(w.Fme, "me", s_ov), 1.0, w.t2b, "aeim", s_tau));
+    KV_TRY(E(1.0, m1v, TT(t2, "aeim", v2o2), 1.0, w.Fmeb, "me", s_ov));
+    KV_TRY(E(-1.0, m1v, IB(vovo, "anfi"), 1.0, g1, "fn", vo));
+    KV_TRY(E(0.5, m1v, IB(vovv, "amef"), 1.0, w.t2b, "efim", s_tau));
+    KV_TRY(E(0.5, m1v, IB(ooov, "nmie"), 1.0, w.t2b, "aemn", s_tau));
+
+    // ---- back through the intermediates ----------------------------------------
+    // W_abef: -P(ab) t1[b,m] vovv[a,m,e,f] and 1/4 tau[a,b,m,n] oovv[m,n,e,f]
+    KV_TRY(ADD(-1.0, TT(w.Wabefb, "abef", s_w4v), 0.0, w.xW4, "abef", s_x4));
+    KV_TRY(ADD(1.0, TT(w.Wabefb, "baef", s_w4v), 1.0, w.xW4, "abef", s_x4));
+    KV_TRY(E(1.0, TT(w.xW4, "abef", s_x4), IB(vovv, "amef"), 1.0, g1, "bm", vo));
+    KV_TRY(E(0.25, TT(w.Wabefb, "abef", s_w4v), IB(oovv, "mnef"), 1.0, w.taub, "abmn", s_tau));
+    // W_mnij: P(ij) t1[e,j] ooov[m,n,i,e] and 1/4 tau[e,f,i,j] oovv[m,n,e,f]
+    KV_TRY(ADD(1.0, TT(w.Wmnijb, "mnij", s_w4o), 0.0, w.xW4, "mnij", s_x4));
+    KV_TRY(ADD(-1.0, TT(w.Wmnijb, "mnji", s_w4o), 1.0, w.xW4, "mnij", s_x4));
+    KV_TRY(E(1.0, TT(w.xW4, "mnij", s_x4), IB(ooov, "mnie"), 1.0, g1, "ej", vo));
+    KV_TRY(E(0.25, TT(w.Wmnijb, "mnij", s_w4o), IB(oovv, "mnef"), 1.0, w.taub, "efij", s_tau));
+    // W_mbej
+    KV_TRY(E(-1.0, TT(w.Wmbejb, "mbej", s_wmbej), IB(vovv, "bmef"), 1.0, g1, "fj", vo));
+    KV_TRY(E(1.0, TT(w.Wmbejb, "mbej", s_wmbej), IB(ooov, "mnje"), 1.0, g1, "bn", vo));
+    KV_TRY(E(-1.0, TT(w.Wmbejb, "mbej", s_wmbej), IB(oovv, "mnef"), 0.0, w.tmpb, "fbjn",
+             s_tmp));
+    KV_TRY(ADD(0.5, TT(w.tmpb, "fbjn", s_tmp), 1.0, w.t2b, "fbjn", s_tau));
+    KV_TRY(E(1.0, TT(w.tmpb, "fbjn", s_tmp), TT(t1, "bn", vo), 1.0, g1, "fj", vo));
+    KV_TRY(E(1.0, TT(w.tmpb, "fbjn", s_tmp), TT(t1, "fj", vo), 1.0, g1, "bn", vo));
+    // F_me
+    KV_TRY(E(1.0, TT(w.Fmeb, "me", s_ov), IB(oovv, "mnef"), 1.0, g1, "fn", vo));
+    // F_mi
+    KV_TRY(E(0.5, TT(w.Fmib, "mi", s_oo), IB(Fov, "me"), 1.0, g1, "ei", vo));
+    KV_TRY(E(1.0, TT(w.Fmib, "mi", s_oo), IB(ooov, "mnie"), 1.0, g1, "en", vo));
+    KV_TRY(E(0.5, TT(w.Fmib, "mi", s_oo), IB(oovv, "mnef"), 0.0, w.ttaub, "efin", s_tau));
+    // F_ae
+    KV_TRY(E(-0.5, TT(w.Faeb, "ae", s_vv), IB(Fov, "me"), 1.0, g1, "am", vo));
+    KV_TRY(E(-1.0, TT(w.Faeb, "ae", s_vv), IB(vovv, "amfe"), 1.0, g1, "fm", vo));
+    KV_TRY(E(-0.5, TT(w.Faeb, "ae", s_vv), IB(oovv, "mnef"), 1.0, w.ttaub, "afmn", s_tau));
+    // tau and tau-tilde
+    KV_TRY(ADD(1.0, TT(w.taub, "abij", s_tau), 1.0, w.t2b, "abij", s_tau));
+    KV_TRY(ADD(1.0, TT(w.ttaub, "abij", s_tau), 1.0, w.t2b, "abij", s_tau));
+    KV_TRY(ADD(1.0, TT(w.taub, "abij", s_tau), 0.0, w.ttb, "abij", s_tau));
+    KV_TRY(ADD(-1.0, TT(w.taub, "baij", s_tau), 1.0, w.ttb, "abij", s_tau));
+    KV_TRY(ADD(0.5, TT(w.ttaub, "abij", s_tau), 1.0, w.ttb, "abij", s_tau));
+    KV_TRY(ADD(-0.5, TT(w.ttaub, "baij", s_tau), 1.0, w.ttb, "abij", s_tau));
+    KV_TRY(E(1.0, TT(w.ttb, "abij", s_tau), TT(t1, "bj", vo), 1.0, g1, "ai", vo));
+    KV_TRY(E(1.0, TT(w.ttb, "abij", s_tau), TT(t1, "ai", vo), 1.0, g1, "bj", vo));
+    // g2 = (1 - P(ab))(1 - P(ij)) t2b
+    KV_TRY(ADD(1.0, TT(w.t2b, "abij", s_tau), 0.0, g2, "abij", v2o2));
+    KV_TRY(ADD(-1.0, TT(w.t2b, "baij", s_tau), 1.0, g2, "abij", v2o2));
+    KV_TRY(ADD(-1.0, TT(w.t2b, "abji", s_tau), 1.0, g2, "abij", v2o2));
+    KV_TRY(ADD(1.0, TT(w.t2b, "baji", s_tau), 1.0, g2, "abij", v2o2));
+    return KVFT_OK;
+}
+
+extern "C" int kvft_lambda_residual(kvft_ctx *ctx, int nb, int nv, int no,
+                                    const double *const F[4], const double *const I[9],
+                                    const double *t1, const double *t2, const double *m1,
+                                    const double *m2, double *g1, double *g2) {
+    if (!ctx || nb < 0 || nv <= 0 || no <= 0 || !F || !I || !t1 || !t2 || !m1 || !m2 || !g1 ||
+        !g2)
+        return kv_fail(ctx, KVFT_EINVAL, "kvft_lambda_residual: bad argument");
+    for (int k = 0; k < 4; k++)
+        if (!F[k]) return kv_fail(ctx, KVFT_EINVAL, "kvft_lambda_residual: null F block");
+    for (int k = 0; k < 9; k++)
+        if (!I[k]) return kv_fail(ctx, KVFT_EINVAL, "kvft_lambda_residual: null I block");
+    if (!ctx->dry) cudaSetDevice(ctx->device);
+    return kv_lambda_vjp(ctx, nb, nv, no, F, I, t1, t2, m1, m2, g1, g2);
+}
+
+extern "C" int kvft_einsum_plan(int nv, int no, const char *aix, const char *bix,
+                                const char *cix, int *mnk, int *sizes, long long *strides) {
+    if (!aix || !bix || !cix || !mnk || !sizes || !strides) return KVFT_EINVAL;
+    KIdx x[6];
+    std::string err;
+    int st = kv_einsum_desc(nv, no, aix, bix, cix, &mnk[0], &mnk[1], &mnk[2], &x[0], &x[1],
+                            &x[2], &x[3], &x[4], &x[5], &err);
+    if (st != KVFT_OK) return st;
+    for (int k = 0; k < 6; k++)
+        for (int d = 0; d < 3; d++) {
+            sizes[3 * k + d] = x[k].size[d];
+            strides[3 * k + d] = x[k].st[d];
+        }
+    return KVFT_OK;
+}

@@ -441,24 +441,28 @@ extern "C" {
 int kvft_int_tbar1(kvft_ctx *ctx, int ng, int nv, int no, const double *t1bar,
                    const double *ti, const double *D1, const double *G, int full,
                    double *t1out) {
+    if (ctx && ctx->dry) return kv_fail(ctx, KVFT_EINVAL, "kvft_int_tbar1: not on a dry-run context");
     return int_tbar_entry(ctx, 1, ng, nv, no, t1bar, ti, D1, G, full, t1out);
 }
 
 int kvft_int_tbar2(kvft_ctx *ctx, int ng, int nv, int no, const double *t2bar,
                    const double *ti, const double *D2, const double *G, int full,
                    double *t2out) {
+    if (ctx && ctx->dry) return kv_fail(ctx, KVFT_EINVAL, "kvft_int_tbar2: not on a dry-run context");
     return int_tbar_entry(ctx, 2, ng, nv, no, t2bar, ti, D2, G, full, t2out);
 }
 
 int kvft_int_tbar1_single(kvft_ctx *ctx, int ng, int ig, int nv, int no,
                           const double *t1bar, const double *ti, const double *D1,
                           const double *G, double *t1out) {
+    if (ctx && ctx->dry) return kv_fail(ctx, KVFT_EINVAL, "kvft_int_tbar1_single: not on a dry-run context");
     return int_tbar_single_entry(ctx, 1, ng, ig, nv, no, t1bar, ti, D1, G, t1out);
 }
 
 int kvft_int_tbar2_single(kvft_ctx *ctx, int ng, int ig, int nv, int no,
                           const double *t2bar, const double *ti, const double *D2,
                           const double *G, double *t2out) {
+    if (ctx && ctx->dry) return kv_fail(ctx, KVFT_EINVAL, "kvft_int_tbar2_single: not on a dry-run context");
     return int_tbar_single_entry(ctx, 2, ng, ig, nv, no, t2bar, ti, D2, G, t2out);
 }
 

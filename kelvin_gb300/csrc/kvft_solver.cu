@@ -391,6 +391,7 @@ size_t kvft_solver_footprint(int n, int ng, int precision) {
 int kvft_solver_create(kvft_ctx *ctx, int n, int ng, const double *eps, const double *fock,
                        const double *eri, double beta, double mu, const double *ti,
                        const double *g, const double *G, kvft_solver **out) {
+    if (ctx && ctx->dry) return kv_fail(ctx, KVFT_EINVAL, "kvft_solver_create: not on a dry-run context");
     if (!ctx || !out || n <= 0 || ng < 1 || ng > 64 || !eps || !fock || !eri || !ti || !g ||
         !G || !(beta > 0.0))
         return kv_fail(ctx, KVFT_EINVAL, "solver_create: bad argument");
@@ -452,6 +453,7 @@ int kvft_solver_create_blocks(kvft_ctx *ctx, int nv, int no, int ng, const doubl
                               const double *const I[9], const double *D1, const double *D2,
                               double beta, const double *ti, const double *g, const double *G,
                               kvft_solver **out) {
+    if (ctx && ctx->dry) return kv_fail(ctx, KVFT_EINVAL, "kvft_solver_create_blocks: not on a dry-run context");
     if (!ctx || !out || nv <= 0 || no <= 0 || ng < 1 || ng > 64 || !F || !I || !D1 || !D2 ||
         !ti || !g || !G || beta == 0.0)
         return kv_fail(ctx, KVFT_EINVAL, "solver_create_blocks: bad argument");
@@ -701,6 +703,7 @@ int kvft_solver_device_amplitudes(kvft_solver *s, double **T1, double **T2) {
 int kvft_ft_integrals(kvft_ctx *ctx, int n, const double *eps, const double *fock,
                       const double *eri, double beta, double mu, double *const F[4],
                       double *const I[9]) {
+    if (ctx && ctx->dry) return kv_fail(ctx, KVFT_EINVAL, "kvft_ft_integrals: not on a dry-run context");
     if (!ctx || n <= 0 || !eps || !fock || !eri || !F || !I || !(beta > 0.0))
         return kv_fail(ctx, KVFT_EINVAL, "ft_integrals: bad argument");
     cudaSetDevice(ctx->device);
@@ -725,6 +728,7 @@ int kvft_ccsd_stanton(kvft_ctx *ctx, int ng, int nv, int no, const double *const
                       const double *const I[9], const double *T1old, const double *T2old,
                       const double *D1, const double *D2, const double *ti, const double *G,
                       int full, double *T1new, double *T2new) {
+    if (ctx && ctx->dry) return kv_fail(ctx, KVFT_EINVAL, "kvft_ccsd_stanton: not on a dry-run context");
     if (!ctx || ng < 1 || ng > 64 || nv <= 0 || no <= 0 || !F || !I || !T1old || !T2old ||
         !D1 || !D2 || !ti || !G || !T1new || !T2new)
         return kv_fail(ctx, KVFT_EINVAL, "ccsd_stanton: bad argument");

@@ -562,6 +562,7 @@ extern "C" int kvft_stanton_residual(kvft_ctx *ctx, int nb, int nv, int no,
                                      const double *const F[4], const double *const I[9],
                                      const double *t1, const double *t2, double fac,
                                      double *T1, double *T2) {
+    if (ctx && ctx->dry) return kv_fail(ctx, KVFT_EINVAL, "kvft_stanton_residual: not on a dry-run context");
     if (!ctx || nb < 0 || nv <= 0 || no <= 0 || !F || !I || !t1 || !t2 || !T1 || !T2)
         return kv_fail(ctx, KVFT_EINVAL, "kvft_stanton_residual: bad argument");
     for (int k = 0; k < 4; k++)

@@ -74,6 +74,7 @@ hubbard_eri_kernel(int L, double u, double *__restrict__ eri) {
 }  // namespace
 
 extern "C" int kvft_ueg_eri(kvft_ctx *ctx, int nb, const int *nvec, double c, double *eri) {
+    if (ctx && ctx->dry) return kv_fail(ctx, KVFT_EINVAL, "kvft_ueg_eri: not on a dry-run context");
     if (!ctx || nb <= 0 || nb > MAXNB || !nvec || !eri)
         return kv_fail(ctx, KVFT_EINVAL, "ueg_eri: bad argument (1 <= nb <= 512)");
     cudaSetDevice(ctx->device);
@@ -87,6 +88,7 @@ extern "C" int kvft_ueg_eri(kvft_ctx *ctx, int nb, const int *nvec, double c, do
 }
 
 extern "C" int kvft_hubbard_eri(kvft_ctx *ctx, int sites, double u, double *eri) {
+    if (ctx && ctx->dry) return kv_fail(ctx, KVFT_EINVAL, "kvft_hubbard_eri: not on a dry-run context");
     if (!ctx || sites <= 0 || sites > 4096 || !eri)
         return kv_fail(ctx, KVFT_EINVAL, "hubbard_eri: bad argument");
     cudaSetDevice(ctx->device);

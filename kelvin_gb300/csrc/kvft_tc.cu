@@ -1400,6 +1400,7 @@ int kv_device_status(kvft_ctx *ctx) {
 // C[M][N] = A[M][K] B[K][N] for `batch` consecutive matrices, device pointers.
 extern "C" int kvft_gemm(kvft_ctx *ctx, int M, int N, int K, int batch, int precision,
                          int digits, const double *A, const double *B, double *C) {
+    if (ctx && ctx->dry) return kv_fail(ctx, KVFT_EINVAL, "kvft_gemm: not on a dry-run context");
     if (!ctx || M <= 0 || N <= 0 || K <= 0 || batch <= 0 || !A || !B || !C)
         return kv_fail(ctx, KVFT_EINVAL, "kvft_gemm: bad argument");
     cudaSetDevice(ctx->device);

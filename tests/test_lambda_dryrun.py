@@ -1,0 +1,213 @@
+"""The device Lambda terms (kvft_lambda_residual), checked on the CPU.
+
+A dry-run context records every launch the call makes -- the strided GEMM
+and strided axpby descriptors, over host buffers and NaN-filled host scratch
+-- without a GPU.  These tests replay the recorded launches in numpy with
+the kernels' documented semantics, check that every access stays inside its
+buffer, and compare the result with the oracle's reverse pass
+(oracle/ft_lambda.residual_vjp).  What is left for the GPU is the kernels
+themselves, which the GPU tests check separately (test_gpu_tc.py,
+test_gpu_kernels.py)."""
+import ctypes
+
+import numpy
+import pytest
+
+from conftest import random_system
+from kelvin_gb300 import _lib
+from oracle import ft_lambda
+
+F_ORDER = ("oo", "ov", "vo", "vv")
+I_ORDER = ("vvvv", "vvvo", "vovv", "vvoo", "vovo", "oovv", "vooo", "ooov", "oooo")
+
+
+def _L():
+    return _lib.lib()
+
+
+def _offsets(sizes, strides):
+    s, t = sizes, strides
+    return (numpy.arange(s[0])[:, None, None] * t[0] + numpy.arange(s[1])[None, :, None] * t[1]
+            + numpy.arange(s[2])[None, None, :] * t[2]).reshape(-1)
+
+
+def _plan(nv, no, a, b, c):
+    mnk = (ctypes.c_int * 3)()
+    sizes = (ctypes.c_int * 18)()
+    strides = (ctypes.c_longlong * 18)()
+    st = _L().kvft_einsum_plan(nv, no, a.encode(), b.encode(), c.encode(), mnk, sizes, strides)
+    assert st == 0, (a, b, c)
+    views = [(list(sizes[3 * k:3 * k + 3]), list(strides[3 * k:3 * k + 3])) for k in range(6)]
+    return list(mnk), views
+
+
+SPECS = [("abij,bmij", "am"), ("ia,me", "aeim"), ("ai,bj", "abij"), ("bi,aj", "abij"),
+         ("me,am", "ae"), ("fm,amfe", "ae"), ("ej,mnie", "mnji"), ("abij,am", "bijm"),
+         ("ijab,abef", "efij"), ("mbej,mnef", "fbjn"), ("ia,nmie", "aemn"),
+         ("abef,mnef", "abmn"), ("fbjn,fj", "bn"), ("mi,mnef", "efin")]
+
+
+@pytest.mark.parametrize("ab,c", SPECS)
+def test_einsum_plan_is_the_contraction(ab, c):
+    """The strided-GEMM form of each index-string contraction reproduces
+    numpy.einsum (nv != no, so a virtual/occupied mix-up shows)."""
+    nv, no = 4, 3
+    a, b = ab.split(",")
+    ext = lambda s: tuple(nv if ch in "abcdefgh" else no for ch in s)
+    rng = numpy.random.default_rng(len(a) * 7 + len(c))
+    A = rng.standard_normal(ext(a))
+    B = rng.standard_normal(ext(b))
+    (M, N, K), v = _plan(nv, no, a, b, c)
+    ar, ac, br, bc, cr, cc = [_offsets(*x) for x in v]
+    assert (len(ar), len(ac), len(bc)) == (M, K, N)
+    Am = A.reshape(-1)[ar[:, None] + ac[None, :]]
+    Bm = B.reshape(-1)[br[:, None] + bc[None, :]]
+    C = numpy.full(int(numpy.prod(ext(c))), numpy.nan)
+    idx = cr[:, None] + cc[None, :]
+    assert len(numpy.unique(idx)) == C.size            # every element written once
+    C[idx] = Am @ Bm
+    ref = numpy.einsum("%s,%s->%s" % (a, b, c), A, B)
+    assert abs(C.reshape(ref.shape) - ref).max() < 1e-13
+
+
+def test_einsum_plan_rejects_bad_strings():
+    mnk = (ctypes.c_int * 3)()
+    sizes = (ctypes.c_int * 18)()
+    strides = (ctypes.c_longlong * 18)()
+    for a, b, c in (("abij", "bj", "abij"), ("ai", "bj", "ab"), ("az", "zb", "ab"),
+                    ("aai", "ai", "ai")):
+        assert _L().kvft_einsum_plan(3, 2, a.encode(), b.encode(), c.encode(), mnk, sizes,
+                                     strides) != 0
+
+
+class _Memory(object):
+    """Host buffers the recorded launches address, by base pointer."""
+
+    def __init__(self):
+        self.bufs = []
+
+    def add(self, arr):
+        flat = arr.reshape(-1)
+        assert flat.base is arr or flat is arr or numpy.shares_memory(flat, arr)
+        self.bufs.append((arr.ctypes.data, flat.size, flat))
+
+    def add_raw(self, ptr, nbytes):
+        n = nbytes // 8
+        flat = numpy.ctypeslib.as_array((ctypes.c_double * n).from_address(ptr))
+        self.bufs.append((ptr, n, flat))
+
+    def find(self, ptr):
+        for base, n, flat in self.bufs:
+            if base <= ptr < base + 8 * n:
+                assert (ptr - base) % 8 == 0
+                return flat, (ptr - base) // 8
+        raise AssertionError("pointer outside every buffer")
+
+    def view(self, ptr, offs):
+        flat, start = self.find(ptr)
+        idx = start + offs
+        assert idx.min() >= 0 and idx.max() < flat.size, "access out of bounds"
+        return flat, idx
+
+
+def _replay(ctx, mem):
+    L = _L()
+    n = ctypes.c_int()
+    assert L.kvft_dryrun_count(ctx, ctypes.byref(n)) == 0
+    ints = (ctypes.c_int * 32)()
+    longs = (ctypes.c_longlong * 32)()
+    dbls = (ctypes.c_double * 2)()
+    ptrs = (ctypes.c_void_p * 8)()
+    kinds = []
+    for i in range(n.value):
+        assert L.kvft_dryrun_op(ctx, i, ints, longs, dbls, ptrs) == 0
+        kind, M, N, K, batch = ints[0:5]
+        alpha, beta = dbls[0], dbls[1]
+        kinds.append(kind)
+        if kind == 0:
+            v = [_offsets(ints[5 + 3 * k:8 + 3 * k], longs[3 * k:3 * k + 3]) for k in range(6)]
+            ar, ac, br, bc, cr, cc = v
+            assert (len(ar), len(ac), len(br), len(bc), len(cr), len(cc)) == (M, K, K, N, M, N)
+            abst, bbst, cbst = longs[18], longs[19], longs[20]
+            for b in range(batch):
+                fa, ia = mem.view(ptrs[0] + 8 * b * abst, ar[:, None] + ac[None, :])
+                fb, ib = mem.view(ptrs[1] + 8 * b * bbst, br[:, None] + bc[None, :])
+                fc, ic = mem.view(ptrs[2] + 8 * b * cbst, cr[:, None] + cc[None, :])
+                prod = alpha * (fa[ia] @ fb[ib])
+                fc[ic] = prod if beta == 0.0 else prod + beta * fc[ic]
+        elif kind == 1:
+            dims = ints[23:27]
+            ss, ds = longs[21:25], longs[25:29]
+            sbst, dbst = longs[29], longs[30]
+            grid = numpy.indices(dims).reshape(4, -1)
+            so = sum(grid[k] * ss[k] for k in range(4))
+            do = sum(grid[k] * ds[k] for k in range(4))
+            for b in range(batch):
+                fs, is_ = mem.view(ptrs[3] + 8 * b * sbst, so)
+                fd, id_ = mem.view(ptrs[4] + 8 * b * dbst, do)
+                val = alpha * fs[is_]
+                fd[id_] = val if beta == 0.0 else val + beta * fd[id_]
+        elif kind == 3:
+            cr = _offsets(ints[17:20], longs[12:15])
+            cc = _offsets(ints[20:23], longs[15:18])
+            for b in range(batch):
+                fc, ic = mem.view(ptrs[2] + 8 * b * longs[20], cr[:, None] + cc[None, :])
+                fc[ic] = 0.0 if beta == 0.0 else beta * fc[ic]
+        else:
+            raise AssertionError("unexpected launch kind %d" % kind)
+    return kinds
+
+
+@pytest.mark.parametrize("no,nv,nb,prec", [(3, 4, 2, 0), (4, 3, 1, 2)])
+def test_lambda_residual_dry_run_vs_oracle(no, nv, nb, prec):
+    rng = numpy.random.default_rng(10 * no + nv)
+    F, I = random_system(rng, no, nv)
+    anti = lambda x: (x - x.swapaxes(-1, -2)) - (x - x.swapaxes(-1, -2)).swapaxes(-3, -4)
+    t1 = rng.standard_normal((nb, nv, no)) * 0.1
+    t2 = anti(rng.standard_normal((nb, nv, nv, no, no)) * 0.1)
+    m1 = rng.standard_normal((nb, no, nv))
+    m2 = anti(rng.standard_normal((nb, no, no, nv, nv)))
+    g1 = numpy.full((nb, nv, no), numpy.nan)
+    g2 = numpy.full((nb, nv, nv, no, no), numpy.nan)
+    Fb = [numpy.ascontiguousarray(getattr(F, k)) for k in F_ORDER]
+    Ib = [numpy.ascontiguousarray(getattr(I, k)) for k in I_ORDER]
+    L = _L()
+    ctx = ctypes.c_void_p()
+    assert L.kvft_dryrun_create(prec, 5, ctypes.byref(ctx)) == 0
+    try:
+        Fp = (ctypes.c_void_p * 4)(*[a.ctypes.data for a in Fb])
+        Ip = (ctypes.c_void_p * 9)(*[a.ctypes.data for a in Ib])
+        st = L.kvft_lambda_residual(ctx, nb, nv, no, Fp, Ip, t1.ctypes.data, t2.ctypes.data,
+                                    m1.ctypes.data, m2.ctypes.data, g1.ctypes.data,
+                                    g2.ctypes.data)
+        assert st == 0
+        assert numpy.isnan(g1).all() and numpy.isnan(g2).all()      # nothing ran
+        mem = _Memory()
+        for a in Fb + Ib + [t1, t2, m1, m2, g1, g2]:
+            mem.add(a)
+        i = 0
+        ptr, nbytes = ctypes.c_void_p(), ctypes.c_size_t()
+        while L.kvft_dryrun_scratch(ctx, i, ctypes.byref(ptr), ctypes.byref(nbytes)) == 0:
+            mem.add_raw(ptr.value, nbytes.value)
+            i += 1
+        assert i >= 1
+        kinds = _replay(ctx, mem)
+        assert set(kinds) <= {0, 1}
+    finally:
+        L.kvft_ctx_destroy(ctx)
+    for y in range(nb):
+        r1, r2 = ft_lambda.residual_vjp(F, I, t1[y], t2[y], m1[y].T,
+                                        m2[y].transpose(2, 3, 0, 1))
+        assert abs(g1[y] - r1).max() < 1e-12 * max(1.0, abs(r1).max())
+        assert abs(g2[y] - r2).max() < 1e-12 * max(1.0, abs(r2).max())
+
+
+def test_dry_run_context_rejects_device_calls():
+    L = _L()
+    ctx = ctypes.c_void_p()
+    assert L.kvft_dryrun_create(0, 7, ctypes.byref(ctx)) == 0
+    try:
+        assert L.kvft_sync(ctx) != 0
+        assert L.kvft_flush_l2(ctx) != 0
+    finally:
+        assert L.kvft_ctx_destroy(ctx) == 0
