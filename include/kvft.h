@@ -162,6 +162,19 @@ int kvft_lambda_residual(kvft_ctx *ctx, int nb, int nv, int no,
                          const double *const F[4], const double *const I[9],
                          const double *t1, const double *t2, const double *m1,
                          const double *m2, double *g1, double *g2);
+/* One Lambda update (kelvin/ft_cc_equations.py:385-409 ccsd_lambda_opt):
+ * Lint = int_L(L_old) (quadrature.py:320-345), then per tau point
+ *   L1 = -F.ov - I.oovv T1 - R1'^T Lint,  L2 = -I.oovv - R2'^T Lint
+ * (the terms of kvft_lambda_residual, transposed to Lambda layout).
+ * L1[ng][no][nv], L2[ng][no][no][nv][nv]; ev/eo are the orbital energies of
+ * the virtual / occupied indices (D1 = ev - eo); ti, g, G the grid.  Device
+ * pointers; L1/L2 may alias L1old/L2old. */
+int kvft_ccsd_lambda(kvft_ctx *ctx, int ng, int nv, int no,
+                     const double *const F[4], const double *const I[9],
+                     const double *T1, const double *T2, const double *L1old,
+                     const double *L2old, const double *ev, const double *eo,
+                     const double *ti, const double *g, const double *G, double *L1,
+                     double *L2);
 /* The strided-GEMM form of an index-string contraction C[cix] = A[aix] B[bix]
  * (letters a-h virtual, i-n occupied; every letter in exactly two of the
  * three): mnk = {M, N, K}; sizes/strides hold the composite indices (three
@@ -175,13 +188,14 @@ int kvft_einsum_plan(int nv, int no, const char *aix, const char *bix,
  * descriptors each kernel would receive) instead of running them; pointers
  * passed to it are host memory and its scratch is host memory filled with
  * NaN.  Lets the index arithmetic of a call be replayed and checked on a
- * CPU.  kvft_lambda_residual accepts it; every other call that would touch
- * the device returns KVFT_EINVAL.  Destroy it with kvft_ctx_destroy. */
+ * CPU.  kvft_lambda_residual and kvft_ccsd_lambda accept it; every other
+ * call that would touch the device returns KVFT_EINVAL.  Destroy it with kvft_ctx_destroy. */
 int kvft_dryrun_create(int precision, int digits, kvft_ctx **ctx);
 int kvft_dryrun_count(const kvft_ctx *ctx, int *count);
-/* op i: ints[32], longs[32], dbls[2], ptrs[8]; kind 0 contraction (M N K
+/* op i: ints[32], longs[32], dbls[2], ptrs[9]; kind 0 contraction (M N K
  * batch, alpha, beta, A B C views), 1 strided axpby (dims, strides, src,
- * dst), 3 scale of a view.  Layout in kvft_ctx.cu. */
+ * dst), 2 tau integral (ng, P, rank, full, nv, no; tbar, out, ti, G, eps
+ * pair), 3 scale of a view.  Layout in kvft_ctx.cu. */
 int kvft_dryrun_op(const kvft_ctx *ctx, int i, int *ints, long long *longs,
                    double *dbls, const void **ptrs);
 /* scratch buffer i of a dry-run context (KVFT_EINVAL past the last one) */

@@ -97,6 +97,9 @@ _SIGS = {
     "kvft_lambda_residual": (ctypes.c_int, [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                             ctypes.POINTER(vp), ctypes.POINTER(vp), vp, vp,
                                             vp, vp, vp, vp]),
+    "kvft_ccsd_lambda": (ctypes.c_int, [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                        ctypes.POINTER(vp), ctypes.POINTER(vp), vp, vp, vp,
+                                        vp, vp, vp, vp, vp, vp, vp, vp]),
     "kvft_einsum_plan": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_char_p,
                                         ctypes.c_char_p, ctypes.c_char_p,
                                         ctypes.POINTER(ctypes.c_int),

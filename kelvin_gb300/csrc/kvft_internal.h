@@ -229,6 +229,15 @@ int kv_pair_gather(kvft_ctx *ctx, int batch, int n1, int n2, const double *A,
 int kv_bcast(kvft_ctx *ctx, int batch, size_t count, const double *src,
              double *dst);
 
+// The tau integral out[y] = sum_x G[y,x] w(y,x) tbar[x] over P elements per
+// tau point, w = exp((ti[x]-ti[y]) d) for x <= y and, for x > y, 1 (the
+// reference's rule) or the same exponential (full); d from D or, when D is
+// null, ev[p]-eo[q] (rank 1) / ev[a]+ev[b]-eo[i]-eo[j] (rank 2).  ti and G on
+// the device, hti/hG their host copies.  mode 1 also damps and takes norms.
+int kv_quad_launch(kvft_ctx *ctx, int mode, int ng, long long P, int rank, int nv, int no,
+                   const double *tbar, const double *ti, const double *hti, const double *G,
+                   const double *hG, const double *D, const double *ev, const double *eo,
+                   int full, double alpha, double *out, double *res, int spin_half = 0);
 int kv_int_tbar(kvft_ctx *ctx, int ng, size_t P, const double *tbar,
                 const double *ti, const double *D, const double *eps_v,
                 const double *eps_o, int nv, int no, int rank,

@@ -436,6 +436,100 @@ extern "C" int kvft_lambda_residual(kvft_ctx *ctx, int nb, int nv, int no,
     return kv_lambda_vjp(ctx, nb, nv, no, F, I, t1, t2, m1, m2, g1, g2);
 }
 
+namespace {
+
+int to_host(kvft_ctx *ctx, double *dst, const double *src, size_t n) {
+    if (ctx->dry) {
+        std::memcpy(dst, src, sizeof(double) * n);
+        return KVFT_OK;
+    }
+    KV_CHECK(ctx, cudaMemcpyAsync(dst, src, sizeof(double) * n, cudaMemcpyDeviceToHost,
+                                  ctx->stream));
+    KV_CHECK(ctx, cudaStreamSynchronize(ctx->stream));
+    return KVFT_OK;
+}
+
+int to_device(kvft_ctx *ctx, double *dst, const double *src, size_t n) {
+    if (ctx->dry) {
+        std::memcpy(dst, src, sizeof(double) * n);
+        return KVFT_OK;
+    }
+    KV_CHECK(ctx, cudaMemcpyAsync(dst, src, sizeof(double) * n, cudaMemcpyHostToDevice,
+                                  ctx->stream));
+    KV_CHECK(ctx, cudaStreamSynchronize(ctx->stream));
+    return KVFT_OK;
+}
+
+}  // namespace
+
+// One Lambda update (kelvin/ft_cc_equations.py:385-409):
+//   Lint = int_L(L_old)                      (quadrature.py:320-345)
+//   L[y] = -(F.ov + I.oovv T1[y]) - R'(T[y])^T Lint[y],   L2[y] = -I.oovv - ...
+// int_L is the tau integral run backwards: Lint[s] = sum_{y>=s} Gf[s,y]
+// exp((t_y - t_s) d') L_old[y] with Gf[s,y] = g_y G[y,s] / g_s and d' the
+// denominator of the Lambda layout (e_i + e_j - e_a - e_b), i.e. the full-
+// exponential form of the forward integral with the roles of the orbital
+// energies swapped.  L1/L2 may alias L1old/L2old.
+extern "C" int kvft_ccsd_lambda(kvft_ctx *ctx, int ng, int nv, int no,
+                                const double *const F[4], const double *const I[9],
+                                const double *T1, const double *T2, const double *L1old,
+                                const double *L2old, const double *ev, const double *eo,
+                                const double *ti, const double *g, const double *G, double *L1,
+                                double *L2) {
+    if (!ctx || ng < 1 || ng > 64 || nv <= 0 || no <= 0 || !F || !I || !T1 || !T2 || !L1old ||
+        !L2old || !ev || !eo || !ti || !g || !G || !L1 || !L2)
+        return kv_fail(ctx, KVFT_EINVAL, "kvft_ccsd_lambda: bad argument (ng must be 1..64)");
+    for (int k = 0; k < 4; k++)
+        if (!F[k]) return kv_fail(ctx, KVFT_EINVAL, "kvft_ccsd_lambda: null F block");
+    for (int k = 0; k < 9; k++)
+        if (!I[k]) return kv_fail(ctx, KVFT_EINVAL, "kvft_ccsd_lambda: null I block");
+    if (!ctx->dry) cudaSetDevice(ctx->device);
+    const long long v = nv, o = no, vo = v * o, v2o2 = v * v * o * o;
+    std::vector<double> hti(ng), hg(ng), hG((size_t)ng * ng), hGf((size_t)ng * ng, 0.0);
+    KV_TRY(to_host(ctx, hti.data(), ti, ng));
+    KV_TRY(to_host(ctx, hg.data(), g, ng));
+    KV_TRY(to_host(ctx, hG.data(), G, (size_t)ng * ng));
+    for (int s = 0; s < ng; s++)
+        for (int y = s; y < ng; y++) hGf[(size_t)s * ng + y] = hg[y] * hG[(size_t)y * ng + s] / hg[s];
+    void *gp = nullptr, *ip = nullptr;
+    KV_TRY(kv_scratch(ctx, "lambda_grid", sizeof(double) * ng * ng, &gp));
+    KV_TRY(to_device(ctx, (double *)gp, hGf.data(), (size_t)ng * ng));
+    KV_TRY(kv_scratch(ctx, "lambda_int", sizeof(double) * ng * (vo + v2o2), &ip));
+    double *Lint1 = (double *)ip, *Lint2 = Lint1 + ng * vo;
+    const double *Gf = (const double *)gp;
+    // Lambda layout [i][a] / [i][j][a][b]: occupied energies lead
+    KV_TRY(kv_quad_launch(ctx, 0, ng, vo, 1, no, nv, L1old, ti, hti.data(), Gf, hGf.data(),
+                          nullptr, eo, ev, 1, 0.0, Lint1, nullptr));
+    KV_TRY(kv_quad_launch(ctx, 0, ng, v2o2, 2, no, nv, L2old, ti, hti.data(), Gf, hGf.data(),
+                          nullptr, eo, ev, 1, 0.0, Lint2, nullptr));
+    // tau points per pass: the reverse pass keeps ~21 n^4 doubles per point
+    int nb = ng;
+    if (!ctx->dry) {
+        size_t fr = 0, tot = 0;
+        if (cudaMemGetInfo(&fr, &tot) == cudaSuccess) {
+            const double per = (double)kv_lambda_workspace(1, nv, no) + 8.0 * (vo + v2o2);
+            nb = (int)std::max(1.0, std::min((double)ng, 0.7 * (double)fr / per));
+        }
+    }
+    void *gb = nullptr;
+    KV_TRY(kv_scratch(ctx, "lambda_g", sizeof(double) * nb * (vo + v2o2), &gb));
+    double *g1 = (double *)gb, *g2 = g1 + nb * vo;
+    const double *Fov = F[1], *oovv = I[5];
+    for (int y0 = 0; y0 < ng; y0 += nb) {
+        const int b = std::min(nb, ng - y0);
+        KV_TRY(kv_lambda_vjp(ctx, b, nv, no, F, I, T1 + y0 * vo, T2 + y0 * v2o2, Lint1 + y0 * vo,
+                             Lint2 + y0 * v2o2, g1, g2));
+        double *l1 = L1 + y0 * vo, *l2 = L2 + y0 * v2o2;
+        KV_TRY(kv_add(ctx, nv, no, b, -1.0, KvTen{Fov, "ia", 0, 1}, 0.0, l1, "ia", vo));
+        KV_TRY(kv_einsum(ctx, nv, no, b, -1.0, KvTen{oovv, "ijab", 0, 1},
+                         KvTen{T1 + y0 * vo, "bj", vo, 0}, 1.0, l1, "ia", vo));
+        KV_TRY(kv_add(ctx, nv, no, b, -1.0, KvTen{g1, "ai", vo, 0}, 1.0, l1, "ia", vo));
+        KV_TRY(kv_add(ctx, nv, no, b, -1.0, KvTen{oovv, "ijab", 0, 1}, 0.0, l2, "ijab", v2o2));
+        KV_TRY(kv_add(ctx, nv, no, b, -1.0, KvTen{g2, "abij", v2o2, 0}, 1.0, l2, "ijab", v2o2));
+    }
+    return KVFT_OK;
+}
+
 extern "C" int kvft_einsum_plan(int nv, int no, const char *aix, const char *bix,
                                 const char *cix, int *mnk, int *sizes, long long *strides) {
     if (!aix || !bix || !cix || !mnk || !sizes || !strides) return KVFT_EINVAL;

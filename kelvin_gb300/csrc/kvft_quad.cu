@@ -321,6 +321,15 @@ int kv_quad_launch(kvft_ctx *ctx, int mode, int ng, long long P, int rank, int n
                    double *out, double *res, int spin_half) {
     if (ng < 1 || ng > MAXNG) return kv_fail(ctx, KVFT_EINVAL, "ng must be in [1, 64]");
     if (P == 0) return KVFT_OK;
+    if (ctx->dry) {
+        if (mode != 0 || D) return kv_fail(ctx, KVFT_EINVAL, "dry run: tau integral mode");
+        KvDryOp op;
+        op.kind = 2;
+        op.ng = ng, op.P = P, op.rank = rank, op.full = full, op.nv = nv, op.no = no;
+        op.src = tbar, op.dst = out, op.ti = ti, op.G = G, op.ev = ev, op.eo = eo;
+        ctx->dry->push_back(op);
+        return KVFT_OK;
+    }
     QuadParams q;
     q.ng = ng;
     q.P = P;

@@ -16,10 +16,6 @@
 #include <cstdio>
 #include <vector>
 
-int kv_quad_launch(kvft_ctx *ctx, int mode, int ng, long long P, int rank, int nv, int no,
-                   const double *tbar, const double *ti, const double *hti, const double *G,
-                   const double *hG, const double *D, const double *ev, const double *eo,
-                   int full, double alpha, double *out, double *res, int spin_half = 0);
 int kv_quad_single(kvft_ctx *ctx, int ng, int ig, long long P, int rank, int nv, int no,
                    const double *tbar, const double *ti, const double *G, const double *D,
                    const double *ev, const double *eo, double *out);

@@ -1,11 +1,12 @@
-"""The device Lambda terms (kvft_lambda_residual), checked on the CPU.
+"""The device Lambda terms (kvft_lambda_residual) and the device Lambda
+update (kvft_ccsd_lambda), checked on the CPU.
 
 A dry-run context records every launch the call makes -- the strided GEMM
 and strided axpby descriptors, over host buffers and NaN-filled host scratch
 -- without a GPU.  These tests replay the recorded launches in numpy with
 the kernels' documented semantics, check that every access stays inside its
-buffer, and compare the result with the oracle's reverse pass
-(oracle/ft_lambda.residual_vjp).  What is left for the GPU is the kernels
+buffer, and compare the result with the oracle's reverse pass and Lambda
+update (oracle/ft_lambda.residual_vjp, lambda_update).  What is left for the GPU is the kernels
 themselves, which the GPU tests check separately (test_gpu_tc.py,
 test_gpu_kernels.py)."""
 import ctypes
@@ -117,7 +118,7 @@ def _replay(ctx, mem):
     ints = (ctypes.c_int * 32)()
     longs = (ctypes.c_longlong * 32)()
     dbls = (ctypes.c_double * 2)()
-    ptrs = (ctypes.c_void_p * 8)()
+    ptrs = (ctypes.c_void_p * 9)()
     kinds = []
     for i in range(n.value):
         assert L.kvft_dryrun_op(ctx, i, ints, longs, dbls, ptrs) == 0
@@ -147,6 +148,31 @@ def _replay(ctx, mem):
                 fd, id_ = mem.view(ptrs[4] + 8 * b * dbst, do)
                 val = alpha * fs[is_]
                 fd[id_] = val if beta == 0.0 else val + beta * fd[id_]
+        elif kind == 2:
+            ng, rank, full, nv, no = ints[27:32]
+            P = longs[31]
+            ft, it = mem.view(ptrs[5], numpy.arange(ng))
+            ti = ft[it]
+            fg, ig = mem.view(ptrs[6], numpy.arange(ng * ng))
+            G = fg[ig].reshape(ng, ng)
+            fev, iev = mem.view(ptrs[7], numpy.arange(nv))
+            feo, ieo = mem.view(ptrs[8], numpy.arange(no))
+            ev, eo = fev[iev], feo[ieo]
+            if rank == 1:
+                d = (ev[:, None] - eo[None, :]).reshape(-1)
+            else:
+                d = (ev[:, None, None, None] + ev[None, :, None, None]
+                     - eo[None, None, :, None] - eo[None, None, None, :]).reshape(-1)
+            assert d.size == P
+            fs, is_ = mem.view(ptrs[3], numpy.arange(ng * P))
+            tb = fs[is_].reshape(ng, P)
+            out = numpy.zeros((ng, P))
+            for y in range(ng):
+                for x in range(ng):
+                    w = numpy.exp((ti[x] - ti[y]) * d) if (x <= y or full) else 1.0
+                    out[y] += G[y, x] * w * tb[x]
+            fo, io = mem.view(ptrs[4], numpy.arange(ng * P))
+            fo[io] = out.reshape(-1)
         elif kind == 3:
             cr = _offsets(ints[17:20], longs[12:15])
             cc = _offsets(ints[20:23], longs[15:18])
@@ -211,3 +237,55 @@ def test_dry_run_context_rejects_device_calls():
         assert L.kvft_flush_l2(ctx) != 0
     finally:
         assert L.kvft_ctx_destroy(ctx) == 0
+
+
+@pytest.mark.parametrize("no,nv,ng", [(3, 4, 4), (3, 3, 5)])
+def test_ccsd_lambda_dry_run_vs_oracle(no, nv, ng):
+    """kvft_ccsd_lambda (Kelvin's ccsd_lambda_opt: int_L, the Lambda terms,
+    the energy terms) replayed against the oracle's lambda_update."""
+    from oracle import quadrature
+    rng = numpy.random.default_rng(7 * no + nv + ng)
+    F, I = random_system(rng, no, nv)
+    anti = lambda x: (x - x.swapaxes(-1, -2)) - (x - x.swapaxes(-1, -2)).swapaxes(-3, -4)
+    ev = rng.standard_normal(nv) * 0.5 + 1.0
+    eo = rng.standard_normal(no) * 0.5 - 1.0
+    D1 = ev[:, None] - eo[None, :]
+    D2 = (ev[:, None, None, None] + ev[None, :, None, None] - eo[None, None, :, None]
+          - eo[None, None, None, :])
+    beta = 2.0
+    ti, g, G = quadrature.ft_quad(ng, beta, 'lin')
+    T1 = rng.standard_normal((ng, nv, no)) * 0.1
+    T2 = anti(rng.standard_normal((ng, nv, nv, no, no)) * 0.1)
+    L1o = rng.standard_normal((ng, no, nv)) * 0.1
+    L2o = anti(rng.standard_normal((ng, no, no, nv, nv)) * 0.1)
+    L1 = numpy.full(L1o.shape, numpy.nan)
+    L2 = numpy.full(L2o.shape, numpy.nan)
+    Fb = [numpy.ascontiguousarray(getattr(F, k)) for k in F_ORDER]
+    Ib = [numpy.ascontiguousarray(getattr(I, k)) for k in I_ORDER]
+    grid = [numpy.ascontiguousarray(x) for x in (ti, g, G)]
+    L = _L()
+    ctx = ctypes.c_void_p()
+    assert L.kvft_dryrun_create(0, 7, ctypes.byref(ctx)) == 0
+    try:
+        Fp = (ctypes.c_void_p * 4)(*[a.ctypes.data for a in Fb])
+        Ip = (ctypes.c_void_p * 9)(*[a.ctypes.data for a in Ib])
+        st = L.kvft_ccsd_lambda(ctx, ng, nv, no, Fp, Ip, T1.ctypes.data, T2.ctypes.data,
+                                L1o.ctypes.data, L2o.ctypes.data, ev.ctypes.data,
+                                eo.ctypes.data, grid[0].ctypes.data, grid[1].ctypes.data,
+                                grid[2].ctypes.data, L1.ctypes.data, L2.ctypes.data)
+        assert st == 0
+        mem = _Memory()
+        for a in Fb + Ib + grid + [T1, T2, L1o, L2o, L1, L2, ev, eo]:
+            mem.add(a)
+        i = 0
+        ptr, nbytes = ctypes.c_void_p(), ctypes.c_size_t()
+        while L.kvft_dryrun_scratch(ctx, i, ctypes.byref(ptr), ctypes.byref(nbytes)) == 0:
+            mem.add_raw(ptr.value, nbytes.value)
+            i += 1
+        kinds = _replay(ctx, mem)
+        assert kinds.count(2) == 2
+    finally:
+        L.kvft_ctx_destroy(ctx)
+    r1, r2 = ft_lambda.lambda_update(F, I, T1, T2, L1o, L2o, D1, D2, ti, ng, g, G)
+    assert abs(L1 - r1).max() < 1e-12 * abs(r1).max()
+    assert abs(L2 - r2).max() < 1e-12 * abs(r2).max()
