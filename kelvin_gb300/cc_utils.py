@@ -15,7 +15,7 @@ import time
 import numpy
 
 from . import _lib
-from .ft_cc_equations import F_ORDER, I_ORDER, ccsd_stanton
+from .ft_cc_equations import F_ORDER, I_ORDER, ccsd_lambda_opt, ccsd_stanton
 
 
 class one_e_blocks(object):
@@ -241,3 +241,71 @@ def ft_cc_iter_extrap(method, F, I, D1, D2, g, G, beta, ng, ti, iprint, conv_opt
     finally:
         solver.close()
     return T1, T2
+
+
+def ft_lambda_iter(method, L1old, L2old, T1, T2, F, I, D1, D2, g, G, beta, ng, ti, iprint,
+                   conv_options, ctx=None, update=None, history=None, spin_half=None):
+    """Damped Lambda iteration (cc_utils.py:414-480); returns (L1, L2).
+
+    Each update runs on the GPU (ft_cc_equations.ccsd_lambda_opt) with the
+    amplitudes uploaded once; damping and Kelvin's residual measure,
+    res = |L - L_old| / (|L_old| + 0.1) summed over L1 and L2, are taken on
+    the host arrays, and the loop stops below tconv or at max_iter.
+    ``spin_half`` (alpha spin orbitals first) uses the unrestricted driver's
+    measure over the spin cases (cc_utils.py:482-560).  ``update`` replaces
+    the device update (ccsd_lambda_opt's signature without ctx); ``history``
+    receives the residual of each iteration."""
+    if method != "CCSD":
+        raise Exception("Unrecognized method keyword")
+    if update is None:
+        ctx = ctx or _lib.context()
+        dT1, dT2 = _lib.as_device(ctx, T1), _lib.as_device(ctx, T2)
+
+        def update(F, I, T1, T2, L1, L2, D1, D2, ti, ng, g, G, beta):
+            return ccsd_lambda_opt(F, I, dT1, dT2, L1, L2, D1, D2, ti, ng, g, G, beta, ctx=ctx)
+    tbeg = time.time()
+    thresh = conv_options["tconv"]
+    max_iter = conv_options["max_iter"]
+    alpha = conv_options["damp"]
+    L1old, L2old = numpy.array(L1old, dtype=float), numpy.array(L2old, dtype=float)
+    nl1, nl2 = _lambda_norms(L1old, L2old, spin_half)
+    converged = False
+    i = 0
+    while i < max_iter and not converged:
+        L1, L2 = update(F, I, T1, T2, L1old, L2old, D1, D2, ti, ng, g, G, beta)
+        res = _lambda_res(L1, L2, L1old, L2old, nl1, nl2, spin_half)
+        L1old = alpha * L1old + (1.0 - alpha) * L1
+        L2old = alpha * L2old + (1.0 - alpha) * L2
+        nl1, nl2 = _lambda_norms(L1old, L2old, spin_half)
+        logging.info(' %2d  %.10f' % (i + 1, res))
+        if history is not None:
+            history.append(res)
+        i += 1
+        if res < thresh:
+            converged = True
+    if not converged:
+        logging.warning("CCSD Lambda-equations did not converge!")
+    logging.info("Total CCSD Lambda time: %f s" % (time.time() - tbeg))
+    return L1old, L2old
+
+
+def _spin_cases(L1, L2, na):
+    a, b = slice(0, na), slice(na, None)
+    return ((L1[:, a, a], L1[:, b, b]),
+            (L2[:, a, a, a, a], L2[:, a, b, a, b], L2[:, b, b, b, b]))
+
+
+def _lambda_norms(L1, L2, na):
+    nrm = numpy.linalg.norm
+    if na is None:
+        return nrm(L1) + 0.1, nrm(L2) + 0.1
+    (l1a, l1b), (l2aa, l2ab, l2bb) = _spin_cases(L1, L2, na)
+    return nrm(l1a) + nrm(l1b) + 0.1, nrm(l2aa) + nrm(l2bb) + 4 * nrm(l2ab) + 0.1
+
+
+def _lambda_res(L1, L2, L1old, L2old, nl1, nl2, na):
+    nrm = numpy.linalg.norm
+    if na is None:
+        return nrm(L1 - L1old) / nl1 + nrm(L2 - L2old) / nl2
+    d1, d2 = _spin_cases(L1 - L1old, L2 - L2old, na)
+    return sum(nrm(x) for x in d1) / nl1 + sum(nrm(x) for x in d2) / nl2

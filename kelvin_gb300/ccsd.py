@@ -14,8 +14,10 @@ import logging
 import numpy
 
 from . import _lib
-from .cc_utils import DeviceSolver, iterate
-from .ft_cc_equations import g_to_u_t, u_to_g_t1, u_to_g_t2
+from .cc_utils import DeviceSolver, ft_integrals, ft_lambda_iter, iterate
+from .ft_cc_energy import ft_cc_energy
+from .ft_cc_equations import (ccsd_lambda_guess, ccsd_stanton, g_to_u_t, u_to_g_t1,
+                              u_to_g_t2)
 from .quadrature import ft_quad
 from .systems import fermi, grand_potential0
 
@@ -54,6 +56,108 @@ def converge(solver, ctx, conv, precision, digits, refine_sweeps=2, refine_digit
             ctx.set_precision(*prec)
         info["iterations_refine"] = solver.iterations
     return E, info
+
+
+def _d_integrals(h, eri, en, beta, mu, dbeta, dmu):
+    """Directional derivatives (dF, dI, dfo) of the Fermi-scaled integrals
+    (cc_utils.py:569-602) along (dbeta, dmu) at fixed orbital energies, with
+    the mean-field Fock matrix h + sum_r <pr||qr> f_r following the
+    occupations (ueg_scf_system.py:398-417, 481-493): closed forms from
+    df/dmu = beta f (1-f), df/dbeta = -(e - mu) f (1-f)."""
+    fo = fermi(beta, en, mu)
+    fv = 1.0 - fo
+    so, sv = numpy.sqrt(fo), numpy.sqrt(fv)
+    rate = beta * dmu - (en - mu) * dbeta
+    dfo = fo * fv * rate
+    s = {'o': so, 'v': sv}
+    ds = {'o': 0.5 * so * fv * rate, 'v': -0.5 * sv * fo * rate}
+    fmo = h + numpy.einsum('prqr,r->pq', eri, fo) - numpy.diag(en)
+    dfock = numpy.einsum('prqr,r->pq', eri, dfo)
+    one = {}
+    for b in ('oo', 'ov', 'vo', 'vv'):
+        p, q, dp, dq = s[b[0]], s[b[1]], ds[b[0]], ds[b[1]]
+        one[b] = dfock * numpy.outer(p, q) + fmo * (numpy.outer(dp, q) + numpy.outer(p, dq))
+    two = {}
+    for name in ('vvvv', 'vvvo', 'vovv', 'vvoo', 'vovo', 'oovv', 'vooo', 'ooov', 'oooo'):
+        f = [s[c] for c in name]
+        d = [ds[c] for c in name]
+        acc = 0.0
+        for k in range(4):
+            v = [d[m] if m == k else f[m] for m in range(4)]
+            acc = acc + numpy.einsum('p,q,r,s->pqrs', *v)
+        two[name] = eri * acc
+    from .cc_utils import one_e_blocks, two_e_blocks
+    return one_e_blocks(**one), two_e_blocks(**two), dfo
+
+
+def _lam_dot(L1, L2, X1, X2, w):
+    """sum_y w_y <L_y, X_y> with Kelvin's factor 1/4 on doubles."""
+    return (numpy.einsum('y,yia,yai->', w, L1, X1)
+            + 0.25 * numpy.einsum('y,yijab,yabij->', w, L2, X2))
+
+
+def esn_from_lambda(en, h, eri, beta, mu, ngrid, quad, T1, T2, L1, L2, omega, stanton, energy):
+    """E, S, N from converged T and Lambda (kelvin/ccsd.py:167-214 with the
+    exact grid derivative of 1075-1148).
+
+    dOmega along (dbeta, dmu) is the Lagrangian's explicit derivative.  The
+    residual and the energy are linear in the integrals, so the integral part
+    is E(T; dF, dI) - (1/beta) sum_y g_y <L_y, Phi_y(dF, dI)>, where Phi is
+    the amplitude update ``stanton`` (Kelvin's ccsd_stanton: the integrated
+    -F.vo - R) evaluated with the derivative integrals; Kelvin's L is the
+    negative adjoint and sum_s g_s <int_L(L)_s, X_s> = sum_y g_y <L_y,
+    int_tbar(X)_y>.  The grid scales with beta (g, G, t proportional to it):
+    the 1/beta of Omega_cc and the g derivative cancel, and the G and t
+    derivatives are Phi with G/beta plus D times Phi with
+    G[y,x] (t_x - t_y)/beta.  ``stanton(F, I, T1, T2, D1, D2, ti, ng, G)`` and
+    ``energy(T1, T2, f, eri, g, beta)`` are the amplitude update and
+    ft_cc_energy; ``omega`` the converged grand potential.
+        N = -dOmega/dmu,  E = Omega + beta dOmega/dbeta + mu N,
+        S = beta (E - Omega - mu N)"""
+    ti, g, G = ft_quad(ngrid, beta, quad)
+    ng = ngrid
+    fo = fermi(beta, en, mu)
+    D1 = en[:, None] - en[None, :]
+    D2 = (en[:, None, None, None] + en[None, :, None, None] - en[None, None, :, None]
+          - en[None, None, None, :])
+    W = numpy.einsum('ijij->ij', eri)
+    hd = numpy.diag(h) - en
+    x = -beta * (en - mu)
+    gp0 = -(numpy.maximum(x, 0.0) + numpy.log1p(numpy.exp(-numpy.abs(x)))) / beta
+
+    def derivative(dbeta, dmu):
+        dF, dI, dfo = _d_integrals(h, eri, en, beta, mu, dbeta, dmu)
+        d0 = (-fo * dmu + (-gp0 / beta + (en - mu) * fo / beta) * dbeta).sum()
+        d1 = hd @ dfo + fo @ W @ dfo
+        X1, X2 = stanton(dF, dI, T1, T2, D1, D2, ti, ng, G)
+        dcc = energy(T1, T2, dF.ov, dI.oovv, g, beta) - _lam_dot(L1, L2, X1, X2, g) / beta
+        if dbeta != 0.0:
+            F, I = _scaled(h, eri, en, beta, mu)
+            P1, P2 = stanton(F, I, T1, T2, D1, D2, ti, ng, G / beta)
+            Gt = G * (ti[None, :] - ti[:, None]) / beta
+            Q1, Q2 = stanton(F, I, T1, T2, D1, D2, ti, ng, Gt)
+            dcc -= dbeta * _lam_dot(L1, L2, P1 + D1[None] * Q1, P2 + D2[None] * Q2, g) / beta
+        return d0 + d1 + dcc
+
+    dO_dmu = derivative(0.0, 1.0)
+    dO_dbeta = derivative(1.0, 0.0)
+    N = -dO_dmu
+    E = omega + beta * dO_dbeta + mu * N
+    S = beta * (E - omega - mu * N)
+    return E, S, N
+
+
+def _scaled(h, eri, en, beta, mu):
+    """Fermi-scaled blocks of the mean-field Fock matrix and the integrals
+    (cc_utils.py:569-602), on the host."""
+    from .cc_utils import one_e_blocks, two_e_blocks
+    fo = fermi(beta, en, mu)
+    s = {'o': numpy.sqrt(fo), 'v': numpy.sqrt(1.0 - fo)}
+    fmo = h + numpy.einsum('prqr,r->pq', eri, fo) - numpy.diag(en)
+    one = {b: fmo * numpy.outer(s[b[0]], s[b[1]]) for b in ('oo', 'ov', 'vo', 'vv')}
+    two = {nm: eri * numpy.einsum('p,q,r,s->pqrs', *[s[c] for c in nm])
+           for nm in ('vvvv', 'vvvo', 'vovv', 'vvoo', 'vovo', 'oovv', 'vooo', 'ooov', 'oooo')}
+    return one_e_blocks(**one), two_e_blocks(**two)
 
 
 def ctx_precision(ctx):
@@ -107,6 +211,8 @@ class ccsd(object):
         self.T2 = None
         self._Tg = None          # general-spin amplitudes of the last solve
         self.solver = None
+        self.L1 = None           # Lambda amplitudes (Kelvin's layout) once solved
+        self.L2 = None
 
     def _unrestricted(self):
         """A system in Kelvin's unrestricted form (has_u()): it is solved in its
@@ -189,7 +295,37 @@ class ccsd(object):
         self.Gtot = E0 + E1 + Eccn
         return (Eccn + E0 + E1, Eccn)
 
-    def compute_ESN(self, L1=None, L2=None, gderiv=True, delta=1e-4):
+    def _ft_ccsd_lambda(self, L1=None, L2=None):
+        """Solve the Lambda equations (kelvin/ccsd.py:882-961): Kelvin's guess
+        (or the given L1, L2), then the damped iteration of
+        cc_utils.ft_lambda_iter with each update on the GPU.  The updates use
+        FP64-accurate contractions (seven digit levels on the tensor cores
+        unless the solve ran on the FP64 pipe).  Stores self.L1, self.L2."""
+        if self._unrestricted():
+            raise Exception("kelvin_gb300.ccsd: the Lambda equations of unrestricted "
+                            "systems are not built")
+        if self.T1 is None:
+            self.run()
+        T1, T2 = self._Tg if self._Tg is not None else (self.T1, self.T2)
+        beta, mu, ng = self.beta, self.mu, self.ngrid
+        en = numpy.asarray(self.sys.g_energies_tot(), dtype=float)
+        prev = ctx_precision(self.ctx)
+        prec = 'fp64_tc' if self.precision == 'mixed' else self.precision
+        self.ctx.set_precision(*PRECISIONS[prec])
+        try:
+            F, I = ft_integrals(self.sys, en, beta, mu, ctx=self.ctx)
+            if L1 is None or L2 is None:
+                L1, L2 = ccsd_lambda_guess(F, I, T1, self.beta_max, ng)
+            conv = {"tconv": self.tconv, "max_iter": self.max_iter, "damp": self.damp}
+            D1 = en[:, None] - en[None, :]
+            self.L1, self.L2 = ft_lambda_iter("CCSD", L1, L2, T1, T2, F, I, D1, None, self.g,
+                                              self.G, self.beta_max, ng, self.ti, self.iprint,
+                                              conv, ctx=self.ctx)
+        finally:
+            self.ctx.set_precision(*prev)
+        return self.L1, self.L2
+
+    def compute_ESN(self, L1=None, L2=None, gderiv=True, delta=1e-4, method='fd'):
         """Energy, entropy and particle number (kelvin/ccsd.py:128-214).
 
         Kelvin differentiates the grand potential Omega(beta, mu) through the
@@ -205,7 +341,21 @@ class ccsd(object):
             N = -dOmega/dmu,  E = d(beta Omega)/dbeta + mu N,
             S = beta (E - mu N - Omega)
 
-        L1/L2 (given Lambda amplitudes) have no counterpart and must be None."""
+        method='lambda' takes Kelvin's own route instead: the Lambda equations
+        (_ft_ccsd_lambda, started from L1/L2 when given) and the Lagrangian's
+        explicit derivative (esn_from_lambda), one adjoint solve in place of
+        four further solves.  With 'fd', L1/L2 must be None."""
+        if method == 'lambda':
+            if not gderiv:
+                raise Exception("kelvin_gb300.ccsd: only the exact-grid derivative "
+                                "(gderiv=True)")
+            if self.T1 is None:
+                self.run()
+            if self.L1 is None or L1 is not None:
+                self._ft_ccsd_lambda(L1, L2)
+            return self._esn_lambda()
+        if method != 'fd':
+            raise Exception("Unrecognized ESN method: {}".format(method))
         if L1 is not None or L2 is not None:
             raise Exception("kelvin_gb300.ccsd: Lambda amplitudes are not used "
                             "(E, S, N come from finite differences of Omega)")
@@ -256,6 +406,30 @@ class ccsd(object):
         self.N = -(Np - Nm) / (2.0 * dm)
         self.E = ((beta + db) * Bp - (beta - db) * Bm) / (2.0 * db) + mu * self.N
         self.S = beta * (self.E - mu * self.N - Om)
+        return self.E, self.S, self.N
+
+    def _esn_lambda(self):
+        """E, S, N from the stored T and Lambda; the amplitude updates and
+        energies of esn_from_lambda run on the GPU."""
+        T1, T2 = self._Tg if self._Tg is not None else (self.T1, self.T2)
+        en = numpy.asarray(self.sys.g_energies_tot(), dtype=float)
+        eri = self.sys.g_aint_tot()
+        fo0 = fermi(self.beta, en, self.mu)
+        h = self.sys.g_fock_tot() - numpy.einsum('prqr,r->pq', eri, fo0)
+        prev = ctx_precision(self.ctx)
+        prec = 'fp64_tc' if self.precision == 'mixed' else self.precision
+        self.ctx.set_precision(*PRECISIONS[prec])
+        try:
+            def stanton(F, I, T1, T2, D1, D2, ti, ng, G):
+                return ccsd_stanton(F, I, T1, T2, D1, D2, ti, ng, G, ctx=self.ctx)
+
+            def energy(T1, T2, f, eri_, g, beta):
+                return ft_cc_energy(T1, T2, f, eri_, g, beta, ctx=self.ctx)
+            self.E, self.S, self.N = esn_from_lambda(en, h, eri, self.beta, self.mu, self.ngrid,
+                                                     self.quad, T1, T2, self.L1, self.L2,
+                                                     self.Gtot, stanton, energy)
+        finally:
+            self.ctx.set_precision(*prev)
         return self.E, self.S, self.N
 
     def release(self):

@@ -167,6 +167,13 @@ int kv_einsum(kvft_ctx *ctx, int nv, int no, int batch, double alpha, const KvTe
     if (kv_einsum_desc(nv, no, A.ix, B.ix, cix, &M, &N, &K, &ar, &ac, &br, &bc, &cr, &cc,
                        &err) != KVFT_OK)
         return kv_fail(ctx, KVFT_EINVAL, err);
+    if (M == 1 && N > 1) {
+        // a single row: computed as the transposed product C^T = B^T A^T, so
+        // that the long free dimension is the GEMM's row dimension
+        KMat a{B.p, bc, br, B.bst, B.stable}, b{A.p, ac, ar, A.bst, A.stable};
+        KOut c{C, cc, cr, cbst};
+        return kv_gemm(ctx, N, M, K, batch, alpha, a, b, beta, c);
+    }
     KMat a{A.p, ar, ac, A.bst, A.stable}, b{B.p, br, bc, B.bst, B.stable};
     KOut c{C, cr, cc, cbst};
     return kv_gemm(ctx, M, N, K, batch, alpha, a, b, beta, c);

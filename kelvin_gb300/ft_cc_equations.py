@@ -197,3 +197,58 @@ def uccsd_stanton(Fa, Fb, Ia, Ib, Iabab, T1aold, T1bold, T2aaold, T2abold, T2bbo
     D2 = u_to_g_d2(D2aa, D2ab, D2bb)
     o1, o2 = ccsd_stanton(F, I, T1, T2, D1, D2, ti, ng, G, ctx=ctx, precision=precision)
     return g_to_u_t(o1, o2, Fa.vo.shape[0])
+
+
+# ---- Lambda equations -------------------------------------------------------------
+# Kelvin's Lambda update (ft_cc_equations.py:385-409) and guess (:502-512).  The
+# Lambda terms are the transpose of the residual's Jacobian, evaluated on the
+# device (kvft_ccsd_lambda) as the reverse pass through the Stanton
+# intermediates; L1[y][i][a] and L2[y][i][j][a][b] keep Kelvin's layout.
+
+
+def energies_from_d1(D1):
+    """Orbital energies (ev, eo) with ev[a] - eo[i] = D1[a, i]; the
+    exponentials of the integrals depend on these differences only."""
+    D1 = numpy.asarray(D1, dtype=float)
+    return (numpy.ascontiguousarray(D1[:, 0]),
+            numpy.ascontiguousarray(D1[0, 0] - D1[0, :]))
+
+
+def ccsd_lambda_guess(F, I, T1old, beta, ng):
+    """Kelvin's starting Lambda: (1/beta)(F.ov + I.oovv T1, I.oovv) at every
+    tau point (host arrays, ft_cc_equations.py:502-512)."""
+    T1 = numpy.asarray(T1old)
+    L1 = (numpy.asarray(F.ov)[None] + numpy.einsum('ijab,ybj->yia', I.oovv, T1)) / beta
+    L2 = numpy.repeat(numpy.asarray(I.oovv)[None] / beta, ng, axis=0)
+    return L1, L2
+
+
+def ccsd_lambda_opt(F, I, T1old, T2old, L1old, L2old, D1, D2, ti, ng, g, G, beta, ctx=None,
+                    precision=None):
+    """One Lambda update on the GPU: L = -E'(T) - R'(T)^T int_L(L_old) per
+    tau point, with Kelvin's signature (ft_cc_equations.py:385-409; beta and
+    D2 are implied by the grid and D1).  numpy Lambda gives numpy outputs,
+    DeviceArray Lambda device outputs."""
+    ctx = ctx or _lib.context()
+    if precision is not None:
+        ctx.set_precision(*precision) if isinstance(precision, tuple) \
+            else ctx.set_precision(precision)
+    host = not isinstance(L1old, _lib.DeviceArray)
+    blk = device_blocks(ctx, F, I)
+    nv, no = blk.nv, blk.no
+    if tuple(T1old.shape) != (ng, nv, no) or tuple(L1old.shape) != (ng, no, nv) or \
+            tuple(L2old.shape) != (ng, no, no, nv, nv):
+        raise Exception("ccsd_lambda_opt: amplitude shapes do not match F.vo / ng")
+    ev, eo = energies_from_d1(D1)
+    dT1, dT2 = _lib.as_device(ctx, T1old), _lib.as_device(ctx, T2old)
+    dL1, dL2 = _lib.as_device(ctx, L1old), _lib.as_device(ctx, L2old)
+    dev, deo, dti, dg, dG = (_lib.as_device(ctx, numpy.ascontiguousarray(a, dtype=float))
+                             for a in (ev, eo, ti, g, G))
+    o1 = _lib.DeviceArray(ctx, (ng, no, nv))
+    o2 = _lib.DeviceArray(ctx, (ng, no, no, nv, nv))
+    ctx.check(ctx.L.kvft_ccsd_lambda(ctx.h, ng, nv, no, blk.Fp, blk.Ip, dT1.ptr, dT2.ptr,
+                                     dL1.ptr, dL2.ptr, dev.ptr, deo.ptr, dti.ptr, dg.ptr,
+                                     dG.ptr, o1.ptr, o2.ptr), "ccsd_lambda_opt")
+    if host:
+        return o1.to_host(), o2.to_host()
+    return o1, o2

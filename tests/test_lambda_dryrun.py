@@ -129,6 +129,7 @@ def _replay(ctx, mem):
             v = [_offsets(ints[5 + 3 * k:8 + 3 * k], longs[3 * k:3 * k + 3]) for k in range(6)]
             ar, ac, br, bc, cr, cc = v
             assert (len(ar), len(ac), len(br), len(bc), len(cr), len(cc)) == (M, K, K, N, M, N)
+            assert not (M == 1 and N > 1)       # single rows go as transposed products
             abst, bbst, cbst = longs[18], longs[19], longs[20]
             for b in range(batch):
                 fa, ia = mem.view(ptrs[0] + 8 * b * abst, ar[:, None] + ac[None, :])
