@@ -175,6 +175,18 @@ int kvft_ccsd_lambda(kvft_ctx *ctx, int ng, int nv, int no,
                      const double *L2old, const double *ev, const double *eo,
                      const double *ti, const double *g, const double *G, double *L1,
                      double *L2);
+/* Integral gradients of the Lagrangian at converged T and Lambda (the
+ * ingredients of Kelvin's response densities, ft_cc_equations.py:704-753):
+ *   Fg[b], Ig[b] = sum_y g_y d/d(block) [E(T_y) + <int_L(L)_y, F.vo + I.vvoo
+ *                  + R(T_y)>]
+ * in each block's own layout (F: oo ov vo vv, I as for kvft_ccsd_lambda).
+ * Inputs as for kvft_ccsd_lambda; device pointers. */
+int kvft_lambda_densities(kvft_ctx *ctx, int ng, int nv, int no,
+                          const double *const F[4], const double *const I[9],
+                          const double *T1, const double *T2, const double *L1,
+                          const double *L2, const double *ev, const double *eo,
+                          const double *ti, const double *g, const double *G,
+                          double *const Fg[4], double *const Ig[9]);
 /* The strided-GEMM form of an index-string contraction C[cix] = A[aix] B[bix]
  * (letters a-h virtual, i-n occupied; every letter in exactly two of the
  * three): mnk = {M, N, K}; sizes/strides hold the composite indices (three
@@ -188,8 +200,9 @@ int kvft_einsum_plan(int nv, int no, const char *aix, const char *bix,
  * descriptors each kernel would receive) instead of running them; pointers
  * passed to it are host memory and its scratch is host memory filled with
  * NaN.  Lets the index arithmetic of a call be replayed and checked on a
- * CPU.  kvft_lambda_residual and kvft_ccsd_lambda accept it; every other
- * call that would touch the device returns KVFT_EINVAL.  Destroy it with kvft_ctx_destroy. */
+ * CPU.  kvft_lambda_residual, kvft_ccsd_lambda and kvft_lambda_densities
+ * accept it; every other call that would touch the device returns
+ * KVFT_EINVAL.  Destroy it with kvft_ctx_destroy. */
 int kvft_dryrun_create(int precision, int digits, kvft_ctx **ctx);
 int kvft_dryrun_count(const kvft_ctx *ctx, int *count);
 /* op i: ints[32], longs[32], dbls[2], ptrs[9]; kind 0 contraction (M N K

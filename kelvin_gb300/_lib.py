@@ -100,6 +100,10 @@ _SIGS = {
     "kvft_ccsd_lambda": (ctypes.c_int, [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                         ctypes.POINTER(vp), ctypes.POINTER(vp), vp, vp, vp,
                                         vp, vp, vp, vp, vp, vp, vp, vp]),
+    "kvft_lambda_densities": (ctypes.c_int, [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                             ctypes.POINTER(vp), ctypes.POINTER(vp), vp, vp,
+                                             vp, vp, vp, vp, vp, vp, vp, ctypes.POINTER(vp),
+                                             ctypes.POINTER(vp)]),
     "kvft_einsum_plan": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_char_p,
                                         ctypes.c_char_p, ctypes.c_char_p,
                                         ctypes.POINTER(ctypes.c_int),

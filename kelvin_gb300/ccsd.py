@@ -16,8 +16,8 @@ import numpy
 from . import _lib
 from .cc_utils import DeviceSolver, ft_integrals, ft_lambda_iter, iterate
 from .ft_cc_energy import ft_cc_energy
-from .ft_cc_equations import (ccsd_lambda_guess, ccsd_stanton, g_to_u_t, u_to_g_t1,
-                              u_to_g_t2)
+from .ft_cc_equations import (ccsd_lambda_guess, ccsd_stanton, g_to_u_t, kelvin_densities,
+                              lambda_densities, normal_ordered_rdms, u_to_g_t1, u_to_g_t2)
 from .quadrature import ft_quad
 from .systems import fermi, grand_potential0
 
@@ -407,6 +407,43 @@ class ccsd(object):
         self.E = ((beta + db) * Bp - (beta - db) * Bm) / (2.0 * db) + mu * self.N
         self.S = beta * (self.E - mu * self.N - Om)
         return self.E, self.S, self.N
+
+    def _g_ft_rdms(self):
+        """Response densities and normal-ordered RDMs from T and Lambda
+        (kelvin/ccsd.py:1333-1432 _g_ft_1rdm / _g_ft_2rdm): dia, dba, dji, dai,
+        P2, n1rdm, n2rdm.  The densities are evaluated on the GPU."""
+        if self.L1 is None:
+            self._ft_ccsd_lambda()
+        T1, T2 = self._Tg if self._Tg is not None else (self.T1, self.T2)
+        en = numpy.asarray(self.sys.g_energies_tot(), dtype=float)
+        D1 = en[:, None] - en[None, :]
+        prev = ctx_precision(self.ctx)
+        prec = 'fp64_tc' if self.precision == 'mixed' else self.precision
+        self.ctx.set_precision(*PRECISIONS[prec])
+        try:
+            Fg, Ig = lambda_densities(T1, T2, self.L1, self.L2, D1, self.ti, self.ngrid, self.g,
+                                      self.G, ctx=self.ctx)
+        finally:
+            self.ctx.set_precision(*prev)
+        (self.dia, self.dba, self.dji, self.dai), self.P2 = kelvin_densities(Fg, Ig)
+        fo = fermi(self.beta, en, self.mu)
+        self.n1rdm, self.n2rdm = normal_ordered_rdms(self.beta, fo, 1.0 - fo,
+                                                     (self.dia, self.dba, self.dji, self.dai),
+                                                     self.P2)
+
+    def _g_ft_1rdm(self):
+        self._g_ft_rdms()
+
+    def _g_ft_2rdm(self):
+        self._g_ft_rdms()
+
+    def full_1rdm(self):
+        """Unrelaxed one-particle density matrix: the normal-ordered part plus
+        the Fermi-Dirac occupations (kelvin/ccsd.py:1988-2004, orbtype 'g')."""
+        if getattr(self, "n1rdm", None) is None:
+            self._g_ft_rdms()
+        en = numpy.asarray(self.sys.g_energies_tot(), dtype=float)
+        return self.n1rdm + numpy.diag(fermi(self.beta, en, self.mu))
 
     def _esn_lambda(self):
         """E, S, N from the stored T and Lambda; the amplitude updates and

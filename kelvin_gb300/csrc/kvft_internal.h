@@ -284,8 +284,12 @@ int kv_add(kvft_ctx *ctx, int nv, int no, int batch, double alpha, const KvTen &
 // residual's Jacobian applied to m (m1[i,a], m2[i,j,a,b] in Lambda layout;
 // g1[a,i], g2[a,b,i,j] in amplitude layout, g2 antisymmetric), with
 //   sum g1 dt1 + 1/4 sum g2 dt2 = sum m1 dR1 + 1/4 sum m2 dR2.
+// With Fg[4] / Ig[9] (nb = 1) it also adds wt times the gradient of
+// sum m1 R1 + 1/4 sum m2 R2 with respect to each integral block the residual
+// reads (blocks laid out as F, I; F.vo and I.vvoo get nothing).
 int kv_lambda_vjp(kvft_ctx *ctx, int nb, int nv, int no, const double *const F[4],
                   const double *const I[9], const double *t1, const double *t2,
-                  const double *m1, const double *m2, double *g1, double *g2);
+                  const double *m1, const double *m2, double *g1, double *g2,
+                  double *const *Fg = nullptr, double *const *Ig = nullptr, double wt = 1.0);
 size_t kv_lambda_workspace(int nb, int nv, int no);
 size_t kv_chunk_bytes_per_tau(kvft_ctx *ctx, int nv, int no);

@@ -252,8 +252,11 @@ size_t kv_lambda_workspace(int nb, int nv, int no) {
 
 int kv_lambda_vjp(kvft_ctx *ctx, int nb, int nv, int no, const double *const F[4],
                   const double *const I[9], const double *t1, const double *t2,
-                  const double *m1, const double *m2, double *g1, double *g2) {
+                  const double *m1, const double *m2, double *g1, double *g2,
+                  double *const *Fg, double *const *Ig, double wt) {
     if (nb <= 0) return KVFT_OK;
+    if ((Fg || Ig) && (!Fg || !Ig || nb != 1))
+        return kv_fail(ctx, KVFT_EINVAL, "lambda: integral gradients take one tau point");
     const long long v = nv, o = no;
     const long long vo = v * o, v2o2 = v * v * o * o;
     const double *Foo = F[0], *Fov = F[1], *Fvv = F[3];
@@ -280,6 +283,13 @@ int kv_lambda_vjp(kvft_ctx *ctx, int nb, int nv, int no, const double *const F[4
     };
     auto ADD = [&](double alpha, const KvTen &S, double beta, double *D, const char *dix,
                    long long dbst) { return kv_add(ctx, nv, no, B, alpha, S, beta, D, dix, dbst); };
+    // integral gradients (one tau point, weight wt), accumulated when asked for
+    auto GE = [&](double alpha, const KvTen &A, const KvTen &Bt, double *C, const char *cix) {
+        return Fg ? kv_einsum(ctx, nv, no, 1, alpha * wt, A, Bt, 1.0, C, cix, 0) : KVFT_OK;
+    };
+    auto GA = [&](double alpha, const KvTen &S, double *D, const char *dix) {
+        return Fg ? kv_add(ctx, nv, no, 1, alpha * wt, S, 1.0, D, dix, 0) : KVFT_OK;
+    };
 
     // ---- forward intermediates (oracle cc_equations.intermediates) ----------
     // ttau = t2 + 1/2 P(ab) t1 t1, tau = t2 + P(ab) t1 t1
@@ -332,8 +342,10 @@ int kv_lambda_vjp(kvft_ctx *ctx, int nb, int nv, int no, const double *const F[4
     KV_TRY(ADD(-1.0, TT(w.xA, "abji", s_tau), 1.0, w.xAI, "abij", s_tau));
     // x = t1[a,m] vooo[b,m,i,j]: t1b[a,m] = xA . vooo   (first write of g1)
     KV_TRY(E(1.0, TT(w.xA, "abij", s_tau), IB(vooo, "bmij"), 0.0, g1, "am", vo));
+    KV_TRY(GE(1.0, TT(w.xA, "abij", s_tau), TT(t1, "am", vo), Fg ? Ig[6] : nullptr, "bmij"));
     // x = t1[e,i] vvvo[a,b,e,j]
     KV_TRY(E(1.0, TT(w.xI, "abij", s_tau), IB(vvvo, "abej"), 1.0, g1, "ei", vo));
+    KV_TRY(GE(1.0, TT(w.xI, "abij", s_tau), TT(t1, "ei", vo), Fg ? Ig[1] : nullptr, "abej"));
     // ring: x = t2[a,e,i,m] W_mbej + t1[e,i] t1[a,m] vovo[b,m,e,j]   (first write of t2b)
     KV_TRY(E(1.0, TT(w.xAI, "abij", s_tau), TT(w.Wmbej, "mbej", s_wmbej), 0.0, w.t2b, "aeim",
              s_tau));
@@ -343,6 +355,7 @@ int kv_lambda_vjp(kvft_ctx *ctx, int nb, int nv, int no, const double *const F[4
     KV_TRY(E(1.0, TT(w.Y1, "bijm", s_y1), IB(vovo, "bmej"), 1.0, g1, "ei", vo));
     KV_TRY(E(1.0, TT(w.xAI, "abij", s_tau), TT(t1, "ei", vo), 0.0, w.Y2, "abej", s_y2));
     KV_TRY(E(1.0, TT(w.Y2, "abej", s_y2), IB(vovo, "bmej"), 1.0, g1, "am", vo));
+    KV_TRY(GE(1.0, TT(w.Y2, "abej", s_y2), TT(t1, "am", vo), Fg ? Ig[4] : nullptr, "bmej"));
     // R2 += 1/2 tau[e,f,i,j] W_abef and 1/2 tau[a,b,m,n] W_mnij (R2b = m2/4)
     KV_TRY(E(0.125, TT(m2, "ijab", v2o2), TT(w.Wabef, "abef", s_w4v), 0.0, w.taub, "efij",
              s_tau));
@@ -381,36 +394,73 @@ int kv_lambda_vjp(kvft_ctx *ctx, int nb, int nv, int no, const double *const F[4
     KV_TRY(E(-1.0, m1v, IB(vovo, "anfi"), 1.0, g1, "fn", vo));
     KV_TRY(E(0.5, m1v, IB(vovv, "amef"), 1.0, w.t2b, "efim", s_tau));
     KV_TRY(E(0.5, m1v, IB(ooov, "nmie"), 1.0, w.t2b, "aemn", s_tau));
+    if (Fg) {
+        KV_TRY(GE(-1.0, m1v, TT(t1, "fn", vo), Ig[4], "anfi"));
+        KV_TRY(GE(0.5, m1v, TT(t2, "efim", v2o2), Ig[2], "amef"));
+        KV_TRY(GE(0.5, m1v, TT(t2, "aemn", v2o2), Ig[7], "nmie"));
+    }
 
     // ---- back through the intermediates ----------------------------------------
     // W_abef: -P(ab) t1[b,m] vovv[a,m,e,f] and 1/4 tau[a,b,m,n] oovv[m,n,e,f]
     KV_TRY(ADD(-1.0, TT(w.Wabefb, "abef", s_w4v), 0.0, w.xW4, "abef", s_x4));
     KV_TRY(ADD(1.0, TT(w.Wabefb, "baef", s_w4v), 1.0, w.xW4, "abef", s_x4));
     KV_TRY(E(1.0, TT(w.xW4, "abef", s_x4), IB(vovv, "amef"), 1.0, g1, "bm", vo));
+    if (Fg) {
+        KV_TRY(GA(1.0, TT(w.Wabefb, "abef", s_w4v), Ig[0], "abef"));
+        KV_TRY(GE(1.0, TT(w.xW4, "abef", s_x4), TT(t1, "bm", vo), Ig[2], "amef"));
+        KV_TRY(GE(0.25, TT(w.Wabefb, "abef", s_w4v), TT(w.tau, "abmn", s_tau), Ig[5], "mnef"));
+    }
     KV_TRY(E(0.25, TT(w.Wabefb, "abef", s_w4v), IB(oovv, "mnef"), 1.0, w.taub, "abmn", s_tau));
     // W_mnij: P(ij) t1[e,j] ooov[m,n,i,e] and 1/4 tau[e,f,i,j] oovv[m,n,e,f]
     KV_TRY(ADD(1.0, TT(w.Wmnijb, "mnij", s_w4o), 0.0, w.xW4, "mnij", s_x4));
     KV_TRY(ADD(-1.0, TT(w.Wmnijb, "mnji", s_w4o), 1.0, w.xW4, "mnij", s_x4));
     KV_TRY(E(1.0, TT(w.xW4, "mnij", s_x4), IB(ooov, "mnie"), 1.0, g1, "ej", vo));
+    if (Fg) {
+        KV_TRY(GA(1.0, TT(w.Wmnijb, "mnij", s_w4o), Ig[8], "mnij"));
+        KV_TRY(GE(1.0, TT(w.xW4, "mnij", s_x4), TT(t1, "ej", vo), Ig[7], "mnie"));
+        KV_TRY(GE(0.25, TT(w.Wmnijb, "mnij", s_w4o), TT(w.tau, "efij", s_tau), Ig[5], "mnef"));
+    }
     KV_TRY(E(0.25, TT(w.Wmnijb, "mnij", s_w4o), IB(oovv, "mnef"), 1.0, w.taub, "efij", s_tau));
     // W_mbej
     KV_TRY(E(-1.0, TT(w.Wmbejb, "mbej", s_wmbej), IB(vovv, "bmef"), 1.0, g1, "fj", vo));
     KV_TRY(E(1.0, TT(w.Wmbejb, "mbej", s_wmbej), IB(ooov, "mnje"), 1.0, g1, "bn", vo));
     KV_TRY(E(-1.0, TT(w.Wmbejb, "mbej", s_wmbej), IB(oovv, "mnef"), 0.0, w.tmpb, "fbjn",
              s_tmp));
+    if (Fg) {
+        KV_TRY(GA(-1.0, TT(w.Wmbejb, "mbej", s_wmbej), Ig[4], "bmej"));
+        KV_TRY(GE(-1.0, TT(w.Wmbejb, "mbej", s_wmbej), TT(t1, "fj", vo), Ig[2], "bmef"));
+        KV_TRY(GE(1.0, TT(w.Wmbejb, "mbej", s_wmbej), TT(t1, "bn", vo), Ig[7], "mnje"));
+        KV_TRY(GE(-1.0, TT(w.Wmbejb, "mbej", s_wmbej), TT(w.tmp, "fbjn", s_tmp), Ig[5], "mnef"));
+    }
     KV_TRY(ADD(0.5, TT(w.tmpb, "fbjn", s_tmp), 1.0, w.t2b, "fbjn", s_tau));
     KV_TRY(E(1.0, TT(w.tmpb, "fbjn", s_tmp), TT(t1, "bn", vo), 1.0, g1, "fj", vo));
     KV_TRY(E(1.0, TT(w.tmpb, "fbjn", s_tmp), TT(t1, "fj", vo), 1.0, g1, "bn", vo));
     // F_me
     KV_TRY(E(1.0, TT(w.Fmeb, "me", s_ov), IB(oovv, "mnef"), 1.0, g1, "fn", vo));
+    if (Fg) {
+        KV_TRY(GA(1.0, TT(w.Fmeb, "me", s_ov), Fg[1], "me"));
+        KV_TRY(GE(1.0, TT(w.Fmeb, "me", s_ov), TT(t1, "fn", vo), Ig[5], "mnef"));
+    }
     // F_mi
     KV_TRY(E(0.5, TT(w.Fmib, "mi", s_oo), IB(Fov, "me"), 1.0, g1, "ei", vo));
     KV_TRY(E(1.0, TT(w.Fmib, "mi", s_oo), IB(ooov, "mnie"), 1.0, g1, "en", vo));
     KV_TRY(E(0.5, TT(w.Fmib, "mi", s_oo), IB(oovv, "mnef"), 0.0, w.ttaub, "efin", s_tau));
+    if (Fg) {
+        KV_TRY(GA(1.0, TT(w.Fmib, "mi", s_oo), Fg[0], "mi"));
+        KV_TRY(GE(0.5, TT(w.Fmib, "mi", s_oo), TT(t1, "ei", vo), Fg[1], "me"));
+        KV_TRY(GE(1.0, TT(w.Fmib, "mi", s_oo), TT(t1, "en", vo), Ig[7], "mnie"));
+        KV_TRY(GE(0.5, TT(w.Fmib, "mi", s_oo), TT(w.ttau, "efin", s_tau), Ig[5], "mnef"));
+    }
     // F_ae
     KV_TRY(E(-0.5, TT(w.Faeb, "ae", s_vv), IB(Fov, "me"), 1.0, g1, "am", vo));
     KV_TRY(E(-1.0, TT(w.Faeb, "ae", s_vv), IB(vovv, "amfe"), 1.0, g1, "fm", vo));
     KV_TRY(E(-0.5, TT(w.Faeb, "ae", s_vv), IB(oovv, "mnef"), 1.0, w.ttaub, "afmn", s_tau));
+    if (Fg) {
+        KV_TRY(GA(1.0, TT(w.Faeb, "ae", s_vv), Fg[3], "ae"));
+        KV_TRY(GE(-0.5, TT(w.Faeb, "ae", s_vv), TT(t1, "am", vo), Fg[1], "me"));
+        KV_TRY(GE(-1.0, TT(w.Faeb, "ae", s_vv), TT(t1, "fm", vo), Ig[2], "amfe"));
+        KV_TRY(GE(-0.5, TT(w.Faeb, "ae", s_vv), TT(w.ttau, "afmn", s_tau), Ig[5], "mnef"));
+    }
     // tau and tau-tilde
     KV_TRY(ADD(1.0, TT(w.taub, "abij", s_tau), 1.0, w.t2b, "abij", s_tau));
     KV_TRY(ADD(1.0, TT(w.ttaub, "abij", s_tau), 1.0, w.t2b, "abij", s_tau));
@@ -467,6 +517,38 @@ int to_device(kvft_ctx *ctx, double *dst, const double *src, size_t n) {
     return KVFT_OK;
 }
 
+// Lint = int_L(L) (quadrature.py:320-345): the tau integral run backwards,
+// Lint[s] = sum_{y>=s} Gf[s,y] exp((t_y - t_s) d') L[y] with
+// Gf[s,y] = g_y G[y,s] / g_s and d' the Lambda layout's denominator
+// (e_i + e_j - e_a - e_b): the full-exponential forward integral with the
+// roles of the orbital energies swapped.  Lint lives in scratch; hg (if not
+// null) receives the host copy of g.
+int lambda_int(kvft_ctx *ctx, int ng, int nv, int no, const double *L1, const double *L2,
+               const double *ev, const double *eo, const double *ti, const double *g,
+               const double *G, double **Lint1, double **Lint2, std::vector<double> *hgout) {
+    const long long v = nv, o = no, vo = v * o, v2o2 = v * v * o * o;
+    std::vector<double> hti(ng), hg(ng), hG((size_t)ng * ng), hGf((size_t)ng * ng, 0.0);
+    KV_TRY(to_host(ctx, hti.data(), ti, ng));
+    KV_TRY(to_host(ctx, hg.data(), g, ng));
+    KV_TRY(to_host(ctx, hG.data(), G, (size_t)ng * ng));
+    for (int s = 0; s < ng; s++)
+        for (int y = s; y < ng; y++) hGf[(size_t)s * ng + y] = hg[y] * hG[(size_t)y * ng + s] / hg[s];
+    void *gp = nullptr, *ip = nullptr;
+    KV_TRY(kv_scratch(ctx, "lambda_grid", sizeof(double) * ng * ng, &gp));
+    KV_TRY(to_device(ctx, (double *)gp, hGf.data(), (size_t)ng * ng));
+    KV_TRY(kv_scratch(ctx, "lambda_int", sizeof(double) * ng * (vo + v2o2), &ip));
+    *Lint1 = (double *)ip;
+    *Lint2 = *Lint1 + ng * vo;
+    const double *Gf = (const double *)gp;
+    // Lambda layout [i][a] / [i][j][a][b]: occupied energies lead
+    KV_TRY(kv_quad_launch(ctx, 0, ng, vo, 1, no, nv, L1, ti, hti.data(), Gf, hGf.data(),
+                          nullptr, eo, ev, 1, 0.0, *Lint1, nullptr));
+    KV_TRY(kv_quad_launch(ctx, 0, ng, v2o2, 2, no, nv, L2, ti, hti.data(), Gf, hGf.data(),
+                          nullptr, eo, ev, 1, 0.0, *Lint2, nullptr));
+    if (hgout) *hgout = hg;
+    return KVFT_OK;
+}
+
 }  // namespace
 
 // One Lambda update (kelvin/ft_cc_equations.py:385-409):
@@ -492,23 +574,8 @@ extern "C" int kvft_ccsd_lambda(kvft_ctx *ctx, int ng, int nv, int no,
         if (!I[k]) return kv_fail(ctx, KVFT_EINVAL, "kvft_ccsd_lambda: null I block");
     if (!ctx->dry) cudaSetDevice(ctx->device);
     const long long v = nv, o = no, vo = v * o, v2o2 = v * v * o * o;
-    std::vector<double> hti(ng), hg(ng), hG((size_t)ng * ng), hGf((size_t)ng * ng, 0.0);
-    KV_TRY(to_host(ctx, hti.data(), ti, ng));
-    KV_TRY(to_host(ctx, hg.data(), g, ng));
-    KV_TRY(to_host(ctx, hG.data(), G, (size_t)ng * ng));
-    for (int s = 0; s < ng; s++)
-        for (int y = s; y < ng; y++) hGf[(size_t)s * ng + y] = hg[y] * hG[(size_t)y * ng + s] / hg[s];
-    void *gp = nullptr, *ip = nullptr;
-    KV_TRY(kv_scratch(ctx, "lambda_grid", sizeof(double) * ng * ng, &gp));
-    KV_TRY(to_device(ctx, (double *)gp, hGf.data(), (size_t)ng * ng));
-    KV_TRY(kv_scratch(ctx, "lambda_int", sizeof(double) * ng * (vo + v2o2), &ip));
-    double *Lint1 = (double *)ip, *Lint2 = Lint1 + ng * vo;
-    const double *Gf = (const double *)gp;
-    // Lambda layout [i][a] / [i][j][a][b]: occupied energies lead
-    KV_TRY(kv_quad_launch(ctx, 0, ng, vo, 1, no, nv, L1old, ti, hti.data(), Gf, hGf.data(),
-                          nullptr, eo, ev, 1, 0.0, Lint1, nullptr));
-    KV_TRY(kv_quad_launch(ctx, 0, ng, v2o2, 2, no, nv, L2old, ti, hti.data(), Gf, hGf.data(),
-                          nullptr, eo, ev, 1, 0.0, Lint2, nullptr));
+    double *Lint1 = nullptr, *Lint2 = nullptr;
+    KV_TRY(lambda_int(ctx, ng, nv, no, L1old, L2old, ev, eo, ti, g, G, &Lint1, &Lint2, nullptr));
     // tau points per pass: the reverse pass keeps ~21 n^4 doubles per point
     int nb = ng;
     if (!ctx->dry) {
@@ -533,6 +600,58 @@ extern "C" int kvft_ccsd_lambda(kvft_ctx *ctx, int ng, int nv, int no,
         KV_TRY(kv_add(ctx, nv, no, b, -1.0, KvTen{g1, "ai", vo, 0}, 1.0, l1, "ia", vo));
         KV_TRY(kv_add(ctx, nv, no, b, -1.0, KvTen{oovv, "ijab", 0, 1}, 0.0, l2, "ijab", v2o2));
         KV_TRY(kv_add(ctx, nv, no, b, -1.0, KvTen{g2, "abij", v2o2, 0}, 1.0, l2, "ijab", v2o2));
+    }
+    return KVFT_OK;
+}
+
+// The integral gradients of the Lagrangian (kelvin/ft_cc_equations.py:704-753
+// assembles Kelvin's response densities from the same quantities):
+//   Fg[b], Ig[b] = sum_y g_y d/d(block) [E(T_y) + <Lint_y, F.vo + I.vvoo + R(T_y)>]
+// in the blocks' own layouts (F: oo ov vo vv, I: Kelvin's nine), Lint =
+// int_L(L).  One tau point per reverse pass.
+extern "C" int kvft_lambda_densities(kvft_ctx *ctx, int ng, int nv, int no,
+                                     const double *const F[4], const double *const I[9],
+                                     const double *T1, const double *T2, const double *L1,
+                                     const double *L2, const double *ev, const double *eo,
+                                     const double *ti, const double *g, const double *G,
+                                     double *const Fg[4], double *const Ig[9]) {
+    if (!ctx || ng < 1 || ng > 64 || nv <= 0 || no <= 0 || !F || !I || !T1 || !T2 || !L1 ||
+        !L2 || !ev || !eo || !ti || !g || !G || !Fg || !Ig)
+        return kv_fail(ctx, KVFT_EINVAL, "kvft_lambda_densities: bad argument");
+    for (int k = 0; k < 4; k++)
+        if (!F[k] || !Fg[k]) return kv_fail(ctx, KVFT_EINVAL, "kvft_lambda_densities: null F");
+    for (int k = 0; k < 9; k++)
+        if (!I[k] || !Ig[k]) return kv_fail(ctx, KVFT_EINVAL, "kvft_lambda_densities: null I");
+    if (!ctx->dry) cudaSetDevice(ctx->device);
+    const long long v = nv, o = no, vo = v * o, v2o2 = v * v * o * o;
+    double *Lint1 = nullptr, *Lint2 = nullptr;
+    std::vector<double> hg;
+    KV_TRY(lambda_int(ctx, ng, nv, no, L1, L2, ev, eo, ti, g, G, &Lint1, &Lint2, &hg));
+    // zero the outputs
+    const long long fsz[4] = {o * o, o * v, v * o, v * v};
+    const long long isz[9] = {v * v * v * v, v * v * v * o, v * o * v * v, v2o2, v2o2, v2o2,
+                              v * o * o * o, o * o * o * v, o * o * o * o};
+    for (int k = 0; k < 13; k++) {
+        const long long n = k < 4 ? fsz[k] : isz[k - 4];
+        KOut c{k < 4 ? Fg[k] : Ig[k - 4], kidx1((int)n, 1), kidx1(1, 0), 0};
+        KV_TRY(kv_scale_view(ctx, (int)n, 1, 1, 0.0, c));
+    }
+    void *gb = nullptr;
+    KV_TRY(kv_scratch(ctx, "lambda_g", sizeof(double) * (vo + v2o2), &gb));
+    double *g1 = (double *)gb, *g2 = g1 + vo;
+    for (int y = 0; y < ng; y++) {
+        const double w = hg[y];
+        const double *t1 = T1 + y * vo, *t2 = T2 + y * v2o2;
+        const double *l1 = Lint1 + y * vo, *l2 = Lint2 + y * v2o2;
+        KV_TRY(kv_lambda_vjp(ctx, 1, nv, no, F, I, t1, t2, l1, l2, g1, g2, Fg, Ig, w));
+        // the energy's own integrals (ft_cc_energy.py:7-32)
+        KV_TRY(kv_add(ctx, nv, no, 1, w, KvTen{t1, "ai", 0, 0}, 1.0, Fg[1], "ia", 0));
+        KV_TRY(kv_add(ctx, nv, no, 1, 0.25 * w, KvTen{t2, "abij", 0, 0}, 1.0, Ig[5], "ijab", 0));
+        KV_TRY(kv_einsum(ctx, nv, no, 1, 0.5 * w, KvTen{t1, "ai", 0, 0}, KvTen{t1, "bj", 0, 0},
+                         1.0, Ig[5], "ijab", 0));
+        // the driving terms F.vo and I.vvoo meet Lint itself
+        KV_TRY(kv_add(ctx, nv, no, 1, w, KvTen{l1, "ia", 0, 0}, 1.0, Fg[2], "ai", 0));
+        KV_TRY(kv_add(ctx, nv, no, 1, 0.25 * w, KvTen{l2, "ijab", 0, 0}, 1.0, Ig[3], "abij", 0));
     }
     return KVFT_OK;
 }

@@ -252,3 +252,101 @@ def ccsd_lambda_opt(F, I, T1old, T2old, L1old, L2old, D1, D2, ti, ng, g, G, beta
     if host:
         return o1.to_host(), o2.to_host()
     return o1, o2
+
+
+# ---- response densities ------------------------------------------------------------
+# Kelvin's ccsd_1rdm / ccsd_2rdm (ft_cc_equations.py:704-753) from T and Lambda.
+# They are the gradients of the Lagrangian with respect to the integral blocks,
+# which do not depend on the integrals' values (the Lagrangian is linear in
+# them); kvft_lambda_densities evaluates them on the device.  Two-electron
+# densities carry Kelvin's names, weights and index orders: Omega_cc =
+# (1/beta) sum_b w_b P_b . I_b (kelvin/tests/test_ft_cc_2rdm.py:127-135),
+# antisymmetric in their same-type index pairs.
+P2_BLOCKS = (("cdab", "vvvv", 0.25, ((0, 1), (2, 3))),
+             ("ciab", "vvvo", 0.5, ((2, 3),)),
+             ("bcai", "vovv", 0.5, ((0, 1),)),
+             ("ijab", "vvoo", 0.25, ((0, 1), (2, 3))),
+             ("bjai", "vovo", 1.0, ()),
+             ("abij", "oovv", 0.25, ((0, 1), (2, 3))),
+             ("jkai", "vooo", 0.5, ((0, 1),)),
+             ("kaij", "ooov", 0.5, ((2, 3),)),
+             ("klij", "oooo", 0.25, ((0, 1), (2, 3))))
+
+
+def _antisym_pairs(x, pairs):
+    for p in pairs:
+        perm = [0, 1, 2, 3]
+        perm[p[0]], perm[p[1]] = perm[p[1]], perm[p[0]]
+        x = 0.5 * (x - x.transpose(perm))
+    return x
+
+
+def kelvin_densities(Fg, Ig):
+    """(pia, pba, pji, pai), P2 from the integral gradients Fg (oo, ov, vo,
+    vv) and Ig (Kelvin's nine blocks, I_ORDER), as dicts or sequences."""
+    Fg = Fg if isinstance(Fg, dict) else dict(zip(F_ORDER, Fg))
+    Ig = Ig if isinstance(Ig, dict) else dict(zip(I_ORDER, Ig))
+    P1 = (Fg["vo"].T.copy(), Fg["vv"].T.copy(), Fg["oo"].T.copy(), Fg["ov"].T.copy())
+    P2 = tuple(_antisym_pairs(Ig[blk].transpose(2, 3, 0, 1) / w, pairs)
+               for _, blk, w, pairs in P2_BLOCKS)
+    return P1, P2
+
+
+def lambda_densities(T1, T2, L1, L2, D1, ti, ng, g, G, ctx=None):
+    """Integral gradients (Fg, Ig) of the Lagrangian on the device."""
+    ctx = ctx or _lib.context()
+    _, nv, no = T1.shape
+    ev, eo = energies_from_d1(D1)
+    shp1 = {"oo": (no, no), "ov": (no, nv), "vo": (nv, no), "vv": (nv, nv)}
+    ext = {"o": no, "v": nv}
+    zF = [_lib.DeviceArray(ctx, shp1[b]) for b in F_ORDER]
+    zI = [_lib.DeviceArray(ctx, tuple(ext[c] for c in b)) for b in I_ORDER]
+    for a in zF + zI:
+        a.zero()
+    oF = [_lib.DeviceArray(ctx, shp1[b]) for b in F_ORDER]
+    oI = [_lib.DeviceArray(ctx, tuple(ext[c] for c in b)) for b in I_ORDER]
+    d = [_lib.as_device(ctx, a) for a in (T1, T2, L1, L2)]
+    dv = [_lib.as_device(ctx, numpy.ascontiguousarray(a, dtype=float))
+          for a in (ev, eo, ti, g, G)]
+    ctx.check(ctx.L.kvft_lambda_densities(ctx.h, ng, nv, no, _lib.ptr_array(zF),
+                                          _lib.ptr_array(zI), d[0].ptr, d[1].ptr, d[2].ptr,
+                                          d[3].ptr, dv[0].ptr, dv[1].ptr, dv[2].ptr, dv[3].ptr,
+                                          dv[4].ptr, _lib.ptr_array(oF), _lib.ptr_array(oI)),
+              "lambda_densities")
+    return [a.to_host() for a in oF], [a.to_host() for a in oI]
+
+
+def ccsd_1rdm(T1, T2, L1, L2, D1, D2, ti, ng, g, G, ctx=None):
+    """Kelvin's one-electron response densities (pia, pba, pji, pai)
+    (ft_cc_equations.py:704-722)."""
+    Fg, Ig = lambda_densities(T1, T2, L1, L2, D1, ti, ng, g, G, ctx=ctx)
+    return kelvin_densities(Fg, Ig)[0]
+
+
+def ccsd_2rdm(T1, T2, L1, L2, D1, D2, ti, ng, g, G, ctx=None):
+    """Kelvin's nine two-electron response densities (Pcdab, Pciab, Pbcai,
+    Pijab, Pbjai, Pabij, Pjkai, Pkaij, Pklij) (ft_cc_equations.py:725-753)."""
+    Fg, Ig = lambda_densities(T1, T2, L1, L2, D1, ti, ng, g, G, ctx=ctx)
+    return kelvin_densities(Fg, Ig)[1]
+
+
+def normal_ordered_rdms(beta, fo, fv, P1, P2):
+    """Normal-ordered 1- and 2-RDMs (ccsd.py:1333-1388 _g_ft_1rdm,
+    cc_utils.py:1449-1466 g_n2rdm_full): sum n1[p,q] dfock[q,p] +
+    1/4 sum n2[p,q,r,s] d<rs||pq> = dOmega_cc at fixed occupations."""
+    so, sv = numpy.sqrt(fo), numpy.sqrt(fv)
+    pia, pba, pji, pai = P1
+    n1 = (pia * numpy.outer(so, sv) + pba * numpy.outer(sv, sv)
+          + pji * numpy.outer(so, so) + pai * numpy.outer(sv, so)) / beta
+    s = {'o': so, 'v': sv}
+    n2 = 0.0
+    for (name, blk, w, pairs), P in zip(P2_BLOCKS, P2):
+        f = [s[c] for c in blk[2:] + blk[:2]]          # the density's index types
+        x = P * numpy.einsum('p,q,r,s->pqrs', *f) / beta
+        terms = [x]
+        if (0, 1) not in pairs and blk[2] != blk[3]:
+            terms += [-t.transpose(1, 0, 2, 3) for t in terms]
+        if (2, 3) not in pairs and blk[0] != blk[1]:
+            terms += [-t.transpose(0, 1, 3, 2) for t in terms]
+        n2 = n2 + sum(terms)
+    return n1, n2

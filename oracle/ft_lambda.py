@@ -457,6 +457,16 @@ def response_densities(F, I, T1, T2, L1, L2, D1, D2, ti, ng, g, G):
 
     with respect to the integral blocks, which equals Omega_cc at convergence
     and is linear in the integrals."""
+    Fs, Is = integral_gradients(F, I, T1, T2, L1, L2, D1, D2, ti, ng, g, G)
+    pia, pba, pji, pai = Fs.vo.T, Fs.vv.T, Fs.oo.T, Fs.ov.T
+    P2 = tuple(_asym(getattr(Is, blk).transpose(2, 3, 0, 1) / w, pairs)
+               for _, blk, w, pairs in P2_BLOCKS)
+    return (pia, pba, pji, pai), P2
+
+
+def integral_gradients(F, I, T1, T2, L1, L2, D1, D2, ti, ng, g, G):
+    """The Lagrangian's gradients with respect to every entry of every F and
+    I block, in the blocks' own layouts (containers like F, I)."""
     L1int = quadrature.int_L1(ng, L1, ti, D1, g, G)
     L2int = quadrature.int_L2(ng, L2, ti, D2, g, G)
     Fs, Is = _Grad(F), _Grad(I)
@@ -473,10 +483,7 @@ def response_densities(F, I, T1, T2, L1, L2, D1, D2, ti, ng, g, G):
     # the driving terms F.vo and I.vvoo enter with int_L(L) itself
     Fs.vo += einsum('y,yia->ai', g, L1int)
     Is.vvoo += 0.25 * einsum('y,yijab->abij', g, L2int)
-    pia, pba, pji, pai = Fs.vo.T, Fs.vv.T, Fs.oo.T, Fs.ov.T
-    P2 = tuple(_asym(getattr(Is, blk).transpose(2, 3, 0, 1) / w, pairs)
-               for _, blk, w, pairs in P2_BLOCKS)
-    return (pia, pba, pji, pai), P2
+    return Fs, Is
 
 
 def normal_ordered_rdms(beta, fo, fv, P1, P2):

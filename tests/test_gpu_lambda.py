@@ -100,3 +100,27 @@ def test_esn_lambda_ueg19_vs_kelvin(ctx):
     assert abs(S - meta["S"]) < 2e-5
     assert abs(N - meta["N"]) < 2e-6
     assert abs(cc.Gtot - (E - meta["T"] * S - meta["mu"] * N)) < 1e-9
+
+
+def test_lambda_densities_vs_oracle(ctx):
+    """Kelvin's ccsd_1rdm / ccsd_2rdm blocks from the device against the
+    oracle's response densities."""
+    from kelvin_gb300 import ft_cc_equations as fe
+    no, nv, ng, beta = 4, 4, 5, 2.5
+    rng = numpy.random.default_rng(8)
+    ev = rng.standard_normal(nv) * 0.5 + 1.0
+    eo = rng.standard_normal(no) * 0.5 - 1.0
+    D1 = ev[:, None] - eo[None, :]
+    D2 = (ev[:, None, None, None] + ev[None, :, None, None] - eo[None, None, :, None]
+          - eo[None, None, None, :])
+    ti, g, G = quadrature.ft_quad(ng, beta, 'lin')
+    F, I = random_system(rng, no, nv)
+    T1 = rng.standard_normal((ng, nv, no)) * 0.1
+    T2 = _anti(rng.standard_normal((ng, nv, nv, no, no)) * 0.1)
+    L1 = rng.standard_normal((ng, no, nv)) * 0.1
+    L2 = _anti(rng.standard_normal((ng, no, no, nv, nv)) * 0.1)
+    P1 = fe.ccsd_1rdm(T1, T2, L1, L2, D1, D2, ti, ng, g, G, ctx=ctx)
+    P2 = fe.ccsd_2rdm(T1, T2, L1, L2, D1, D2, ti, ng, g, G, ctx=ctx)
+    R1, R2 = ft_lambda.response_densities(F, I, T1, T2, L1, L2, D1, D2, ti, ng, g, G)
+    for a, b in zip(tuple(P1) + tuple(P2), R1 + R2):
+        assert abs(a - b).max() < 1e-11 * max(1.0, abs(b).max())

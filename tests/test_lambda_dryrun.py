@@ -290,3 +290,57 @@ def test_ccsd_lambda_dry_run_vs_oracle(no, nv, ng):
     r1, r2 = ft_lambda.lambda_update(F, I, T1, T2, L1o, L2o, D1, D2, ti, ng, g, G)
     assert abs(L1 - r1).max() < 1e-12 * abs(r1).max()
     assert abs(L2 - r2).max() < 1e-12 * abs(r2).max()
+
+
+def test_lambda_densities_dry_run_vs_oracle():
+    """kvft_lambda_densities (the Lagrangian's integral gradients) replayed
+    against the oracle's response densities (Kelvin's block names)."""
+    from oracle import quadrature
+    no, nv, ng, beta = 3, 4, 4, 2.0
+    rng = numpy.random.default_rng(5)
+    F, I = random_system(rng, no, nv)
+    anti = lambda x: (x - x.swapaxes(-1, -2)) - (x - x.swapaxes(-1, -2)).swapaxes(-3, -4)
+    ev = rng.standard_normal(nv) * 0.5 + 1.0
+    eo = rng.standard_normal(no) * 0.5 - 1.0
+    D1 = ev[:, None] - eo[None, :]
+    D2 = (ev[:, None, None, None] + ev[None, :, None, None] - eo[None, None, :, None]
+          - eo[None, None, None, :])
+    ti, g, G = quadrature.ft_quad(ng, beta, 'lin')
+    T1 = rng.standard_normal((ng, nv, no)) * 0.1
+    T2 = anti(rng.standard_normal((ng, nv, nv, no, no)) * 0.1)
+    L1 = rng.standard_normal((ng, no, nv)) * 0.1
+    L2 = anti(rng.standard_normal((ng, no, no, nv, nv)) * 0.1)
+    Fb = [numpy.ascontiguousarray(getattr(F, k)) for k in F_ORDER]
+    Ib = [numpy.ascontiguousarray(getattr(I, k)) for k in I_ORDER]
+    Fg = [numpy.full(a.shape, numpy.nan) for a in Fb]
+    Ig = [numpy.full(a.shape, numpy.nan) for a in Ib]
+    grid = [numpy.ascontiguousarray(x) for x in (ti, g, G)]
+    L = _L()
+    ctx = ctypes.c_void_p()
+    assert L.kvft_dryrun_create(0, 7, ctypes.byref(ctx)) == 0
+    try:
+        P = lambda arrs: (ctypes.c_void_p * len(arrs))(*[a.ctypes.data for a in arrs])
+        st = L.kvft_lambda_densities(ctx, ng, nv, no, P(Fb), P(Ib), T1.ctypes.data,
+                                     T2.ctypes.data, L1.ctypes.data, L2.ctypes.data,
+                                     ev.ctypes.data, eo.ctypes.data, grid[0].ctypes.data,
+                                     grid[1].ctypes.data, grid[2].ctypes.data, P(Fg), P(Ig))
+        assert st == 0
+        mem = _Memory()
+        for a in Fb + Ib + Fg + Ig + grid + [T1, T2, L1, L2, ev, eo]:
+            mem.add(a)
+        i = 0
+        ptr, nbytes = ctypes.c_void_p(), ctypes.c_size_t()
+        while L.kvft_dryrun_scratch(ctx, i, ctypes.byref(ptr), ctypes.byref(nbytes)) == 0:
+            mem.add_raw(ptr.value, nbytes.value)
+            i += 1
+        _replay(ctx, mem)
+    finally:
+        L.kvft_ctx_destroy(ctx)
+    (pia, pba, pji, pai), P2 = ft_lambda.response_densities(F, I, T1, T2, L1, L2, D1, D2, ti,
+                                                            ng, g, G)
+    Foo, Fov, Fvo, Fvv = Fg
+    for mine, ref in ((Fvo.T, pia), (Fvv.T, pba), (Foo.T, pji), (Fov.T, pai)):
+        assert abs(mine - ref).max() < 1e-12 * max(1.0, abs(ref).max())
+    for (name, blk, w, pairs), ref in zip(ft_lambda.P2_BLOCKS, P2):
+        mine = ft_lambda._asym(Ig[I_ORDER.index(blk)].transpose(2, 3, 0, 1) / w, pairs)
+        assert abs(mine - ref).max() < 1e-12 * max(1.0, abs(ref).max()), name

@@ -88,3 +88,23 @@ def test_derivative_integrals_match_differences():
         for k in ('vvvv', 'vvoo', 'vovo', 'oovv', 'oooo'):
             ref = (getattr(Ip, k) - getattr(Im, k)) / (2 * e)
             assert abs(getattr(dI, k) - ref).max() < 1e-7 * max(1.0, abs(ref).max())
+
+
+def test_density_blocks_and_rdms_match_oracle(solved):
+    """kelvin_densities / normal_ordered_rdms on the raw integral gradients
+    (what kvft_lambda_densities returns) give the oracle's densities and RDMs."""
+    en, h, eri, T, mu, ng, hist, E, S, N, Om, T1, T2, L1, L2 = solved
+    beta = 1.0 / T
+    fo = ft_utils.ff(beta, en, mu)
+    F, I = ft_ccsd.ft_integrals(ft_lambda.mean_field(h, eri, fo), eri, en, beta, mu)
+    ti, g, G = quadrature.ft_quad(ng, beta, 'lin')
+    D1, D2 = ft_utils.D1(en, en), ft_utils.D2(en, en)
+    Fs, Is = ft_lambda.integral_gradients(F, I, T1, T2, L1, L2, D1, D2, ti, ng, g, G)
+    P1, P2 = fe.kelvin_densities({k: getattr(Fs, k) for k in fe.F_ORDER},
+                                 {k: getattr(Is, k) for k in fe.I_ORDER})
+    R1, R2 = ft_lambda.response_densities(F, I, T1, T2, L1, L2, D1, D2, ti, ng, g, G)
+    for a, b in zip(P1 + P2, R1 + R2):
+        assert abs(a - b).max() == 0.0
+    n1, n2 = fe.normal_ordered_rdms(beta, fo, 1.0 - fo, P1, P2)
+    m1, m2 = ft_lambda.normal_ordered_rdms(beta, fo, 1.0 - fo, R1, R2)
+    assert abs(n1 - m1).max() < 1e-15 and abs(n2 - m2).max() < 1e-15
