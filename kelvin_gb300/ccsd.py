@@ -213,6 +213,7 @@ class ccsd(object):
         self.solver = None
         self.L1 = None           # Lambda amplitudes (Kelvin's layout) once solved
         self.L2 = None
+        self._Lg = None          # general-spin Lambda of the last Lambda solve
 
     def _unrestricted(self):
         """A system in Kelvin's unrestricted form (has_u()): it is solved in its
@@ -300,10 +301,13 @@ class ccsd(object):
         (or the given L1, L2), then the damped iteration of
         cc_utils.ft_lambda_iter with each update on the GPU.  The updates use
         FP64-accurate contractions (seven digit levels on the tensor cores
-        unless the solve ran on the FP64 pipe).  Stores self.L1, self.L2."""
-        if self._unrestricted():
-            raise Exception("kelvin_gb300.ccsd: the Lambda equations of unrestricted "
-                            "systems are not built")
+        unless the solve ran on the FP64 pipe).  Stores self.L1, self.L2 --
+        per spin case, (L1a, L1b) and (L2aa, L2ab, L2bb), for a system in the
+        unrestricted form, which is solved in its general-spin form with the
+        unrestricted driver's guess and residual measure
+        (kelvin/ccsd.py:963-1073)."""
+        u = self._unrestricted()
+        na = self.sys.u_energies_tot()[0].shape[0] if u else None
         if self.T1 is None:
             self.run()
         T1, T2 = self._Tg if self._Tg is not None else (self.T1, self.T2)
@@ -315,14 +319,20 @@ class ccsd(object):
         try:
             F, I = ft_integrals(self.sys, en, beta, mu, ctx=self.ctx)
             if L1 is None or L2 is None:
-                L1, L2 = ccsd_lambda_guess(F, I, T1, self.beta_max, ng)
+                L1, L2 = ccsd_lambda_guess(F, I, T1, self.beta_max, ng, unrestricted=u)
+            elif u:
+                L1 = u_to_g_t1(*[numpy.asarray(x) for x in L1])
+                L2 = u_to_g_t2(*[numpy.asarray(x) for x in L2])
             conv = {"tconv": self.tconv, "max_iter": self.max_iter, "damp": self.damp}
             D1 = en[:, None] - en[None, :]
-            self.L1, self.L2 = ft_lambda_iter("CCSD", L1, L2, T1, T2, F, I, D1, None, self.g,
-                                              self.G, self.beta_max, ng, self.ti, self.iprint,
-                                              conv, ctx=self.ctx)
+            self._Lg = ft_lambda_iter("CCSD", L1, L2, T1, T2, F, I, D1, None, self.g, self.G,
+                                      self.beta_max, ng, self.ti, self.iprint, conv,
+                                      ctx=self.ctx, spin_half=na)
         finally:
             self.ctx.set_precision(*prev)
+        self.L1, self.L2 = self._Lg
+        if u:
+            self.L1, self.L2 = g_to_u_t(self._Lg[0], self._Lg[1], na)
         return self.L1, self.L2
 
     def compute_ESN(self, L1=None, L2=None, gderiv=True, delta=1e-4, method='fd'):
@@ -421,8 +431,8 @@ class ccsd(object):
         prec = 'fp64_tc' if self.precision == 'mixed' else self.precision
         self.ctx.set_precision(*PRECISIONS[prec])
         try:
-            Fg, Ig = lambda_densities(T1, T2, self.L1, self.L2, D1, self.ti, self.ngrid, self.g,
-                                      self.G, ctx=self.ctx)
+            Fg, Ig = lambda_densities(T1, T2, self._Lg[0], self._Lg[1], D1, self.ti,
+                                      self.ngrid, self.g, self.G, ctx=self.ctx)
         finally:
             self.ctx.set_precision(*prev)
         (self.dia, self.dba, self.dji, self.dai), self.P2 = kelvin_densities(Fg, Ig)
@@ -463,7 +473,8 @@ class ccsd(object):
             def energy(T1, T2, f, eri_, g, beta):
                 return ft_cc_energy(T1, T2, f, eri_, g, beta, ctx=self.ctx)
             self.E, self.S, self.N = esn_from_lambda(en, h, eri, self.beta, self.mu, self.ngrid,
-                                                     self.quad, T1, T2, self.L1, self.L2,
+                                                     self.quad, T1, T2, self._Lg[0],
+                                                     self._Lg[1],
                                                      self.Gtot, stanton, energy)
         finally:
             self.ctx.set_precision(*prev)

@@ -214,21 +214,25 @@ def energies_from_d1(D1):
             numpy.ascontiguousarray(D1[0, 0] - D1[0, :]))
 
 
-def ccsd_lambda_guess(F, I, T1old, beta, ng):
+def ccsd_lambda_guess(F, I, T1old, beta, ng, unrestricted=False):
     """Kelvin's starting Lambda: (1/beta)(F.ov + I.oovv T1, I.oovv) at every
-    tau point (host arrays, ft_cc_equations.py:502-512)."""
+    tau point (host arrays, ft_cc_equations.py:502-512); ``unrestricted``
+    gives its unrestricted driver's guess, whose I.oovv T1 term has no 1/beta
+    (ft_cc_equations.py:515-526)."""
     T1 = numpy.asarray(T1old)
-    L1 = (numpy.asarray(F.ov)[None] + numpy.einsum('ijab,ybj->yia', I.oovv, T1)) / beta
+    it1 = numpy.einsum('ijab,ybj->yia', I.oovv, T1)
+    L1 = numpy.asarray(F.ov)[None] / beta + (it1 if unrestricted else it1 / beta)
     L2 = numpy.repeat(numpy.asarray(I.oovv)[None] / beta, ng, axis=0)
     return L1, L2
 
 
 def ccsd_lambda_opt(F, I, T1old, T2old, L1old, L2old, D1, D2, ti, ng, g, G, beta, ctx=None,
-                    precision=None):
+                    precision=None, energies=None):
     """One Lambda update on the GPU: L = -E'(T) - R'(T)^T int_L(L_old) per
     tau point, with Kelvin's signature (ft_cc_equations.py:385-409; beta and
     D2 are implied by the grid and D1).  numpy Lambda gives numpy outputs,
-    DeviceArray Lambda device outputs."""
+    DeviceArray Lambda device outputs.  ``energies`` = (ev, eo) replaces the
+    orbital energies read off D1."""
     ctx = ctx or _lib.context()
     if precision is not None:
         ctx.set_precision(*precision) if isinstance(precision, tuple) \
@@ -239,7 +243,7 @@ def ccsd_lambda_opt(F, I, T1old, T2old, L1old, L2old, D1, D2, ti, ng, g, G, beta
     if tuple(T1old.shape) != (ng, nv, no) or tuple(L1old.shape) != (ng, no, nv) or \
             tuple(L2old.shape) != (ng, no, no, nv, nv):
         raise Exception("ccsd_lambda_opt: amplitude shapes do not match F.vo / ng")
-    ev, eo = energies_from_d1(D1)
+    ev, eo = energies if energies is not None else energies_from_d1(D1)
     dT1, dT2 = _lib.as_device(ctx, T1old), _lib.as_device(ctx, T2old)
     dL1, dL2 = _lib.as_device(ctx, L1old), _lib.as_device(ctx, L2old)
     dev, deo, dti, dg, dG = (_lib.as_device(ctx, numpy.ascontiguousarray(a, dtype=float))
@@ -350,3 +354,46 @@ def normal_ordered_rdms(beta, fo, fv, P1, P2):
             terms += [-t.transpose(0, 1, 3, 2) for t in terms]
         n2 = n2 + sum(terms)
     return n1, n2
+
+
+# ---- unrestricted Lambda ----------------------------------------------------------
+# Kelvin's uccsd_lambda_opt / uccsd_lambda_guess (ft_cc_equations.py:412-458,
+# 515-526) take the spin cases separately; as for uccsd_stanton they are laid
+# out as one general-spin problem (alpha spin orbitals first), which the
+# unrestricted equations are the spin-blocked form of.  Lambda keeps Kelvin's
+# layout per spin case: L1a[y][i][a], L2ab[y][i][j][a][b] (i, a alpha; j, b beta).
+
+
+def uccsd_lambda_guess(Fa, Fb, Ia, Ib, Iabab, T1aold, T1bold, beta, ng):
+    """Kelvin's unrestricted starting Lambda: (1/beta) F.ov plus I.oovv T1
+    without the 1/beta (its _u_LS_TS at the default factor), and
+    (1/beta) I.oovv, per spin case."""
+    F, I = u_to_g_one(Fa, Fb), u_to_g_two(Ia, Ib, Iabab)
+    T1 = u_to_g_t1(numpy.asarray(T1aold), numpy.asarray(T1bold))
+    na = numpy.asarray(T1aold).shape[1]
+    L1 = F.ov[None] / beta + numpy.einsum('ijab,ybj->yia', I.oovv, T1)
+    L2 = numpy.repeat(I.oovv[None] / beta, ng, axis=0)
+    (l1a, l1b), (l2aa, l2ab, l2bb) = g_to_u_t(L1, L2, na)
+    return l1a, l1b, l2aa, l2ab, l2bb
+
+
+def uccsd_lambda_opt(Fa, Fb, Ia, Ib, Iabab, T1aold, T1bold, T2aaold, T2abold, T2bbold,
+                     L1aold, L1bold, L2aaold, L2abold, L2bbold, D1a, D1b, D2aa, D2ab, D2bb,
+                     ti, ng, g, G, beta, ctx=None, precision=None):
+    """One unrestricted Lambda update (ft_cc_equations.py:412-458) as the
+    general-spin update on the device; returns (L1a, L1b, L2aa, L2ab, L2bb)."""
+    na = numpy.asarray(T1aold).shape[1]
+    F, I = u_to_g_one(Fa, Fb), u_to_g_two(Ia, Ib, Iabab)
+    T1 = u_to_g_t1(numpy.asarray(T1aold), numpy.asarray(T1bold))
+    T2 = u_to_g_t2(numpy.asarray(T2aaold), numpy.asarray(T2abold), numpy.asarray(T2bbold))
+    L1 = u_to_g_t1(numpy.asarray(L1aold), numpy.asarray(L1bold))
+    L2 = u_to_g_t2(numpy.asarray(L2aaold), numpy.asarray(L2abold), numpy.asarray(L2bbold))
+    # energies per spin: D1a, D1b fix them up to one shift per spin, which
+    # cancels in every spin-conserving denominator
+    (eva, eoa), (evb, eob) = energies_from_d1(D1a), energies_from_d1(D1b)
+    en = (numpy.concatenate((eva, evb)), numpy.concatenate((eoa, eob)))
+    D1 = u_to_g_d1(numpy.asarray(D1a), numpy.asarray(D1b))
+    o1, o2 = ccsd_lambda_opt(F, I, T1, T2, L1, L2, D1, None, ti, ng, g, G, beta, ctx=ctx,
+                             precision=precision, energies=en)
+    (l1a, l1b), (l2aa, l2ab, l2bb) = g_to_u_t(o1, o2, na)
+    return l1a, l1b, l2aa, l2ab, l2bb

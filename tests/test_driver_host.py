@@ -148,3 +148,41 @@ def test_unrestricted_system_amplitudes(monkeypatch):
     assert numpy.array_equal(t2bb, T2[:, na:, na:, na:, na:])
     cc.run(T1=cc.T1, T2=cc.T2)
     assert numpy.array_equal(seen["T1"], T1) and numpy.array_equal(seen["T2"], T2)
+
+
+def test_unrestricted_lambda_driver(monkeypatch):
+    """_ft_ccsd_lambda on a system in the unrestricted form: Kelvin's
+    unrestricted guess and residual measure, the general-spin Lambda returned
+    per spin case (kelvin/ccsd.py:963-1073)."""
+    from kelvin_gb300 import ft_cc_equations as fe
+    from kelvin_gb300.cc_utils import one_e_blocks, two_e_blocks
+    rng = numpy.random.default_rng(9)
+    T, mu, ng, n, na = 0.3, 0.1, 4, 6, 3
+    s = USystem(rng, n, T, mu)
+    sp = (numpy.arange(n) >= na).astype(int)
+    same = sp[:, None] == sp[None, :]
+    cons = (sp[:, None, None, None] + sp[None, :, None, None]
+            == sp[None, None, :, None] + sp[None, None, None, :])
+    T1 = rng.standard_normal((ng, n, n)) * 0.05 * same
+    Lg = (rng.standard_normal((ng, n, n)) * same, rng.standard_normal((ng,) + (n,) * 4) * cons)
+    F = one_e_blocks(*[rng.standard_normal((n, n)) * same for _ in range(4)])
+    I = two_e_blocks(**{k: rng.standard_normal((n,) * 4) * cons for k in fe.I_ORDER})
+    seen = {}
+
+    def fake_iter(method, L1, L2, T1_, T2_, F_, I_, D1, D2, g, G, beta, ng_, ti, iprint, conv,
+                  ctx=None, spin_half=None):
+        seen.update(L1=L1, L2=L2, spin_half=spin_half)
+        return Lg
+    monkeypatch.setattr(ccsd_mod, "ft_integrals", lambda *a, **k: (F, I))
+    monkeypatch.setattr(ccsd_mod, "ft_lambda_iter", fake_iter)
+    cc = ccsd_mod.ccsd(s, T=T, mu=mu, ngrid=ng, ctx=FakeCtx())
+    cc._Tg = (T1, numpy.zeros((ng,) + (n,) * 4))
+    cc.T1 = fe.g_to_u_t(T1, cc._Tg[1], na)[0]
+    cc._ft_ccsd_lambda()
+    assert seen["spin_half"] == na
+    g1, g2 = fe.ccsd_lambda_guess(F, I, T1, cc.beta_max, ng, unrestricted=True)
+    assert abs(seen["L1"] - g1).max() == 0.0 and abs(seen["L2"] - g2).max() == 0.0
+    (l1a, l1b), (l2aa, l2ab, l2bb) = cc.L1, cc.L2
+    assert numpy.array_equal(l1b, Lg[0][:, na:, na:])
+    assert numpy.array_equal(l2ab, Lg[1][:, :na, na:, :na, na:])
+    assert cc._Lg is Lg

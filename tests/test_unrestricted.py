@@ -124,3 +124,67 @@ def test_uccsd_stanton_vs_oracle(ctx):
     (e1a, e1b), (e2aa, e2ab, e2bb) = fe.g_to_u_t(r1, r2, na)
     for x, y in ((o1a, e1a), (o1b, e1b), (o2aa, e2aa), (o2ab, e2ab), (o2bb, e2bb)):
         assert abs(x - y).max() < 1e-12
+
+
+def test_uccsd_lambda_layout(monkeypatch):
+    """Kelvin's unrestricted Lambda signatures on the general-spin update: the
+    per-spin energies read off D1a/D1b and the spin-case maps reproduce the
+    oracle's general-spin Lambda update and guess (the device update replaced
+    by the oracle here; the device update itself is checked elsewhere)."""
+    from kelvin_gb300 import quadrature
+    from oracle import ft_ccsd as oft
+    from oracle import ft_lambda
+    s, en, blk = ueg_blocks()
+    n = en.shape[0]
+    na = n // 2
+    A, Bs = slice(0, na), slice(na, n)
+    beta, ng = 1.0 / s.T, 4
+    F, I = oft.ft_integrals(s.g_fock_tot(), s.g_aint_tot(), en, beta, s.mu)
+    ti, g, G = quadrature.ft_quad(ng, beta, "lin")
+    D1, D2 = ft_utils.D1(en, en), ft_utils.D2(en, en)
+    rng = numpy.random.default_rng(12)
+    sp = (numpy.arange(n) >= na).astype(int)
+    cons = (sp[:, None, None, None] + sp[None, :, None, None]
+            == sp[None, None, :, None] + sp[None, None, None, :])
+    same = sp[:, None] == sp[None, :]
+
+    def anti(x):
+        x = x - x.transpose(0, 2, 1, 3, 4)
+        return (x - x.transpose(0, 1, 2, 4, 3)) * cons
+    T1 = rng.standard_normal((ng, n, n)) * 0.05 * same
+    T2 = anti(rng.standard_normal((ng, n, n, n, n)) * 0.05)
+    L1 = rng.standard_normal((ng, n, n)) * 0.05 * same
+    L2 = anti(rng.standard_normal((ng, n, n, n, n)) * 0.05)
+
+    def fake(F, I, T1, T2, L1, L2, D1, D2, ti, ng, g, G, beta, ctx=None, precision=None,
+             energies=None):
+        ev, eo = energies
+        d1 = ev[:, None] - eo[None, :]
+        d2 = (ev[:, None, None, None] + ev[None, :, None, None] - eo[None, None, :, None]
+              - eo[None, None, None, :])
+        return ft_lambda.lambda_update(F, I, T1, T2, L1, L2, d1, d2, ti, ng, g, G)
+    monkeypatch.setattr(fe, "ccsd_lambda_opt", fake)
+    Fa, Fb = B(), B()
+    for t in fe.F_ORDER:
+        setattr(Fa, t, getattr(F, t)[A, A])
+        setattr(Fb, t, getattr(F, t)[Bs, Bs])
+    Ia, Ib, Iabab = B(), B(), B()
+    for t in fe.I_ORDER:
+        setattr(Ia, t, blk(t)[A, A, A, A])
+        setattr(Ib, t, blk(t)[Bs, Bs, Bs, Bs])
+    for t in I16:
+        setattr(Iabab, t, blk(t)[A, Bs, A, Bs])
+    (t1a, t1b), (t2aa, t2ab, t2bb) = fe.g_to_u_t(T1, T2, na)
+    (l1a, l1b), (l2aa, l2ab, l2bb) = fe.g_to_u_t(L1, L2, na)
+    out = fe.uccsd_lambda_opt(Fa, Fb, Ia, Ib, Iabab, t1a, t1b, t2aa, t2ab, t2bb, l1a, l1b,
+                              l2aa, l2ab, l2bb, D1[A, A], D1[Bs, Bs], D2[A, A, A, A],
+                              D2[A, Bs, A, Bs], D2[Bs, Bs, Bs, Bs], ti, ng, g, G, beta)
+    r1, r2 = ft_lambda.lambda_update(F, I, T1, T2, L1, L2, D1, D2, ti, ng, g, G)
+    (e1a, e1b), (e2aa, e2ab, e2bb) = fe.g_to_u_t(r1, r2, na)
+    for x, y in zip(out, (e1a, e1b, e2aa, e2ab, e2bb)):
+        assert abs(x - y).max() < 1e-12 * max(1.0, abs(y).max())
+    gu = fe.uccsd_lambda_guess(Fa, Fb, Ia, Ib, Iabab, t1a, t1b, beta, ng)
+    q1, q2 = ft_lambda.lambda_guess(F, I, T1, beta, ng, unrestricted=True)
+    (f1a, f1b), (f2aa, f2ab, f2bb) = fe.g_to_u_t(q1, q2, na)
+    for x, y in zip(gu, (f1a, f1b, f2aa, f2ab, f2bb)):
+        assert abs(x - y).max() < 1e-14 * max(1.0, abs(y).max())
