@@ -187,6 +187,19 @@ int kvft_lambda_densities(kvft_ctx *ctx, int ng, int nv, int no,
                           const double *L2, const double *ev, const double *eo,
                           const double *ti, const double *g, const double *G,
                           double *const Fg[4], double *const Ig[9]);
+/* Kelvin's damped Lambda iteration (cc_utils.py:414-480) resident on the
+ * device: L1/L2 hold the guess on entry and the result on return; each
+ * iteration is one kvft_ccsd_lambda update, damping and Kelvin's residual
+ * (over the spin cases of an alpha-first layout when spin_half > 0, as its
+ * unrestricted driver measures, cc_utils.py:482-560).  Stops when the
+ * residual drops below tconv or after max_iter; hist (host, may be NULL)
+ * receives the residual of each iteration, *iters their count. */
+int kvft_lambda_solve(kvft_ctx *ctx, int ng, int nv, int no,
+                      const double *const F[4], const double *const I[9],
+                      const double *T1, const double *T2, const double *ev,
+                      const double *eo, const double *ti, const double *g,
+                      const double *G, double damp, double tconv, int max_iter,
+                      int spin_half, double *L1, double *L2, double *hist, int *iters);
 /* The strided-GEMM form of an index-string contraction C[cix] = A[aix] B[bix]
  * (letters a-h virtual, i-n occupied; every letter in exactly two of the
  * three): mnk = {M, N, K}; sizes/strides hold the composite indices (three
@@ -200,15 +213,16 @@ int kvft_einsum_plan(int nv, int no, const char *aix, const char *bix,
  * descriptors each kernel would receive) instead of running them; pointers
  * passed to it are host memory and its scratch is host memory filled with
  * NaN.  Lets the index arithmetic of a call be replayed and checked on a
- * CPU.  kvft_lambda_residual, kvft_ccsd_lambda and kvft_lambda_densities
- * accept it; every other call that would touch the device returns
+ * CPU.  kvft_lambda_residual, kvft_ccsd_lambda, kvft_lambda_solve and
+ * kvft_lambda_densities accept it; every other call that would touch the device returns
  * KVFT_EINVAL.  Destroy it with kvft_ctx_destroy. */
 int kvft_dryrun_create(int precision, int digits, kvft_ctx **ctx);
 int kvft_dryrun_count(const kvft_ctx *ctx, int *count);
-/* op i: ints[32], longs[32], dbls[2], ptrs[9]; kind 0 contraction (M N K
+/* op i: ints[32], longs[32], dbls[2], ptrs[11]; kind 0 contraction (M N K
  * batch, alpha, beta, A B C views), 1 strided axpby (dims, strides, src,
  * dst), 2 tau integral (ng, P, rank, full, nv, no; tbar, out, ti, G, eps
- * pair), 3 scale of a view.  Layout in kvft_ctx.cu. */
+ * pair), 3 scale of a view, 4 sum of squares (dims, strides of the two
+ * operands, a and b, result word).  Layout in kvft_ctx.cu. */
 int kvft_dryrun_op(const kvft_ctx *ctx, int i, int *ints, long long *longs,
                    double *dbls, const void **ptrs);
 /* scratch buffer i of a dry-run context (KVFT_EINVAL past the last one) */

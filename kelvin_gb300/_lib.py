@@ -104,6 +104,11 @@ _SIGS = {
                                              ctypes.POINTER(vp), ctypes.POINTER(vp), vp, vp,
                                              vp, vp, vp, vp, vp, vp, vp, ctypes.POINTER(vp),
                                              ctypes.POINTER(vp)]),
+    "kvft_lambda_solve": (ctypes.c_int, [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                         ctypes.POINTER(vp), ctypes.POINTER(vp), vp, vp, vp,
+                                         vp, vp, vp, vp, ctypes.c_double, ctypes.c_double,
+                                         ctypes.c_int, ctypes.c_int, vp, vp, vp,
+                                         ctypes.POINTER(ctypes.c_int)]),
     "kvft_einsum_plan": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_char_p,
                                         ctypes.c_char_p, ctypes.c_char_p,
                                         ctypes.POINTER(ctypes.c_int),

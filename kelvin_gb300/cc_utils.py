@@ -15,7 +15,8 @@ import time
 import numpy
 
 from . import _lib
-from .ft_cc_equations import F_ORDER, I_ORDER, ccsd_lambda_opt, ccsd_stanton
+from .ft_cc_equations import (F_ORDER, I_ORDER, ccsd_stanton, device_blocks,
+                              energies_from_d1)
 
 
 class one_e_blocks(object):
@@ -247,22 +248,19 @@ def ft_lambda_iter(method, L1old, L2old, T1, T2, F, I, D1, D2, g, G, beta, ng, t
                    conv_options, ctx=None, update=None, history=None, spin_half=None):
     """Damped Lambda iteration (cc_utils.py:414-480); returns (L1, L2).
 
-    Each update runs on the GPU (ft_cc_equations.ccsd_lambda_opt) with the
-    amplitudes uploaded once; damping and Kelvin's residual measure,
-    res = |L - L_old| / (|L_old| + 0.1) summed over L1 and L2, are taken on
-    the host arrays, and the loop stops below tconv or at max_iter.
-    ``spin_half`` (alpha spin orbitals first) uses the unrestricted driver's
-    measure over the spin cases (cc_utils.py:482-560).  ``update`` replaces
-    the device update (ccsd_lambda_opt's signature without ctx); ``history``
+    The whole loop runs on the GPU (kvft_lambda_solve): each iteration is
+    one device update, damping and Kelvin's residual measure,
+    res = |L - L_old| / (|L_old| + 0.1) summed over L1 and L2, and the loop
+    stops below tconv or at max_iter.  ``spin_half`` (alpha spin orbitals
+    first) uses the unrestricted driver's measure over the spin cases
+    (cc_utils.py:482-560).  ``update`` runs the same loop on the host around
+    a given update (ccsd_lambda_opt's signature without ctx); ``history``
     receives the residual of each iteration."""
     if method != "CCSD":
         raise Exception("Unrecognized method keyword")
     if update is None:
-        ctx = ctx or _lib.context()
-        dT1, dT2 = _lib.as_device(ctx, T1), _lib.as_device(ctx, T2)
-
-        def update(F, I, T1, T2, L1, L2, D1, D2, ti, ng, g, G, beta):
-            return ccsd_lambda_opt(F, I, dT1, dT2, L1, L2, D1, D2, ti, ng, g, G, beta, ctx=ctx)
+        return _lambda_solve_device(ctx or _lib.context(), L1old, L2old, T1, T2, F, I, D1, g,
+                                    G, ng, ti, conv_options, history, spin_half)
     tbeg = time.time()
     thresh = conv_options["tconv"]
     max_iter = conv_options["max_iter"]
@@ -309,3 +307,33 @@ def _lambda_res(L1, L2, L1old, L2old, nl1, nl2, na):
         return nrm(L1 - L1old) / nl1 + nrm(L2 - L2old) / nl2
     d1, d2 = _spin_cases(L1 - L1old, L2 - L2old, na)
     return sum(nrm(x) for x in d1) / nl1 + sum(nrm(x) for x in d2) / nl2
+
+
+def _lambda_solve_device(ctx, L1, L2, T1, T2, F, I, D1, g, G, ng, ti, conv, history,
+                         spin_half):
+    """ft_lambda_iter resident on the device (kvft_lambda_solve)."""
+    tbeg = time.time()
+    blk = device_blocks(ctx, F, I)
+    ev, eo = energies_from_d1(D1)
+    dT1, dT2 = _lib.as_device(ctx, T1), _lib.as_device(ctx, T2)
+    dL1 = _lib.DeviceArray.from_host(ctx, numpy.asarray(L1, dtype=float))
+    dL2 = _lib.DeviceArray.from_host(ctx, numpy.asarray(L2, dtype=float))
+    dv = [_lib.as_device(ctx, numpy.ascontiguousarray(a, dtype=float))
+          for a in (ev, eo, ti, g, G)]
+    max_iter = int(conv["max_iter"])
+    hist = numpy.zeros(max(max_iter, 1))
+    iters = ctypes.c_int()
+    ctx.check(ctx.L.kvft_lambda_solve(ctx.h, ng, blk.nv, blk.no, blk.Fp, blk.Ip, dT1.ptr,
+                                      dT2.ptr, dv[0].ptr, dv[1].ptr, dv[2].ptr, dv[3].ptr,
+                                      dv[4].ptr, float(conv["damp"]), float(conv["tconv"]),
+                                      max_iter, int(spin_half or 0), dL1.ptr, dL2.ptr,
+                                      hist.ctypes.data_as(ctypes.c_void_p),
+                                      ctypes.byref(iters)), "lambda_solve")
+    for i in range(iters.value):
+        logging.info(' %2d  %.10f' % (i + 1, hist[i]))
+    if history is not None:
+        history.extend(float(x) for x in hist[:iters.value])
+    if iters.value == 0 or hist[iters.value - 1] >= conv["tconv"]:
+        logging.warning("CCSD Lambda-equations did not converge!")
+    logging.info("Total CCSD Lambda time: %f s" % (time.time() - tbeg))
+    return dL1.to_host(), dL2.to_host()

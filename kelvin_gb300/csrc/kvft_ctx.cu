@@ -195,8 +195,9 @@ int kvft_dryrun_op(const kvft_ctx *c, int i, int *ints, long long *longs, double
     longs[18] = op.A.bst, longs[19] = op.B.bst, longs[20] = op.C.bst;
     longs[29] = op.sbst, longs[30] = op.dbst, longs[31] = op.P;
     dbls[0] = op.alpha, dbls[1] = op.beta;
-    const void *p[9] = {op.A.p, op.B.p, op.C.p, op.src, op.dst, op.ti, op.G, op.ev, op.eo};
-    for (int k = 0; k < 9; k++) ptrs[k] = p[k];
+    const void *p[11] = {op.A.p, op.B.p, op.C.p, op.src, op.dst, op.ti,
+                         op.G,   op.ev,  op.eo,  op.src2, op.res};
+    for (int k = 0; k < 11; k++) ptrs[k] = p[k];
     return KVFT_OK;
 }
 

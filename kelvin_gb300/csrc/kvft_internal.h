@@ -79,6 +79,9 @@ struct KvDryOp {
     int ng = 0, rank = 0, full = 0, nv = 0, no = 0;
     long long P = 0;
     const double *ti = nullptr, *G = nullptr, *ev = nullptr, *eo = nullptr;
+    // sum of squares: src2 (second operand, may be null) and the result word
+    const double *src2 = nullptr;
+    double *res = nullptr;
 };
 
 // ---------------------------------------------------------------------------
@@ -279,6 +282,11 @@ int kv_einsum(kvft_ctx *ctx, int nv, int no, int batch, double alpha, const KvTe
 // or a copy; at most four letters)
 int kv_add(kvft_ctx *ctx, int nv, int no, int batch, double alpha, const KvTen &src,
            double beta, double *dst, const char *dix, long long dbst);
+// *out = sum (a x + b y)^2 over a [batch][d0][d1][d2][d3] index space with the
+// given element strides (y may be null), in a fixed summation order
+int kv_sumsq4(kvft_ctx *ctx, int batch, const int dims[4], double a, const double *x,
+              const long long xs[4], long long xbst, double b, const double *y,
+              const long long ys[4], long long ybst, double *out);
 
 // Lambda terms of one tau batch: g = R'(t)^T m, the transpose of the
 // residual's Jacobian applied to m (m1[i,a], m2[i,j,a,b] in Lambda layout;

@@ -13,6 +13,7 @@
 // block and pair-ladder savings of the forward residual are not applied here.
 #include "kvft_internal.h"
 
+#include <cmath>
 #include <cstring>
 
 namespace {
@@ -198,6 +199,91 @@ int kv_add(kvft_ctx *ctx, int nv, int no, int batch, double alpha, const KvTen &
         ss[off + k] = s;
     }
     return kv_axpby4(ctx, batch, dims, alpha, src.p, ss, src.bst, beta, dst, ds, dbst);
+}
+
+// ---- sums of squares (the iteration's norms) ----------------------------------
+
+namespace {
+
+struct SQ {
+    int d[4];
+    long long xs[4], ys[4], xbst, ybst;
+};
+
+constexpr int SQ_T = 256;
+
+// per-block partial sums of (a x + b y)^2 over a flat walk of the index space
+__global__ void __launch_bounds__(SQ_T)
+sumsq_kernel(long long total, SQ q, double a, const double *__restrict__ x, double b,
+             const double *__restrict__ y, double *__restrict__ part) {
+    double acc = 0.0;
+    for (long long t = blockIdx.x * (long long)SQ_T + threadIdx.x; t < total;
+         t += (long long)gridDim.x * SQ_T) {
+        long long r = t;
+        const int i3 = (int)(r % q.d[3]); r /= q.d[3];
+        const int i2 = (int)(r % q.d[2]); r /= q.d[2];
+        const int i1 = (int)(r % q.d[1]); r /= q.d[1];
+        const int i0 = (int)(r % q.d[0]);
+        const long long bt = r / q.d[0];
+        double v = a * x[bt * q.xbst + i0 * q.xs[0] + i1 * q.xs[1] + i2 * q.xs[2] +
+                         i3 * q.xs[3]];
+        if (y)
+            v = fma(b, y[bt * q.ybst + i0 * q.ys[0] + i1 * q.ys[1] + i2 * q.ys[2] +
+                         i3 * q.ys[3]], v);
+        acc = fma(v, v, acc);
+    }
+    __shared__ double red[SQ_T];
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    for (int w = SQ_T / 2; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) part[blockIdx.x] = red[0];
+}
+
+__global__ void sum_parts_kernel(const double *__restrict__ part, int n, double *out) {
+    __shared__ double red[SQ_T];
+    double acc = 0.0;
+    for (int k = threadIdx.x; k < n; k += SQ_T) acc += part[k];
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    for (int w = SQ_T / 2; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *out = red[0];
+}
+
+}  // namespace
+
+int kv_sumsq4(kvft_ctx *ctx, int batch, const int dims[4], double a, const double *x,
+              const long long xs[4], long long xbst, double b, const double *y,
+              const long long ys[4], long long ybst, double *out) {
+    long long total = batch;
+    for (int k = 0; k < 4; k++) total *= dims[k];
+    if (ctx->dry) {
+        KvDryOp op;
+        op.kind = 4;
+        op.batch = batch, op.alpha = a, op.beta = b;
+        for (int k = 0; k < 4; k++) op.dims[k] = dims[k], op.ss[k] = xs[k], op.ds[k] = ys[k];
+        op.sbst = xbst, op.dbst = ybst, op.src = x, op.src2 = y, op.res = out;
+        ctx->dry->push_back(op);
+        return KVFT_OK;
+    }
+    SQ q;
+    for (int k = 0; k < 4; k++) q.d[k] = dims[k], q.xs[k] = xs[k], q.ys[k] = y ? ys[k] : 0;
+    q.xbst = xbst;
+    q.ybst = y ? ybst : 0;
+    const int grid = (int)std::max(1LL, std::min((total + SQ_T - 1) / SQ_T,
+                                                 (long long)ctx->sm_count * 8));
+    void *part = nullptr;
+    KV_TRY(kv_scratch(ctx, "sumsq_part", sizeof(double) * grid, &part));
+    KvProfScope prof(ctx, KV_CAT_ELEM, 8.0 * total * (y ? 2 : 1));
+    sumsq_kernel<<<grid, SQ_T, 0, ctx->stream>>>(total, q, a, x, b, y, (double *)part);
+    KV_TRY(kv_launch_check(ctx, "sumsq"));
+    sum_parts_kernel<<<1, SQ_T, 0, ctx->stream>>>((const double *)part, grid, out);
+    return kv_launch_check(ctx, "sum_parts");
 }
 
 // ---- the reverse pass ----------------------------------------------------------
@@ -653,6 +739,114 @@ extern "C" int kvft_lambda_densities(kvft_ctx *ctx, int ng, int nv, int no,
         KV_TRY(kv_add(ctx, nv, no, 1, w, KvTen{l1, "ia", 0, 0}, 1.0, Fg[2], "ai", 0));
         KV_TRY(kv_add(ctx, nv, no, 1, 0.25 * w, KvTen{l2, "ijab", 0, 0}, 1.0, Ig[3], "abij", 0));
     }
+    return KVFT_OK;
+}
+
+// Kelvin's damped Lambda iteration (kelvin/cc_utils.py:414-480) with every
+// array resident: per iteration one Lambda update (kvft_ccsd_lambda), the
+// norms of the change and of the damped Lambda on the device, and a read-back
+// of a few doubles.  res = |L - L_old| / (|L_old| + 0.1) summed over L1, L2,
+// or over the spin cases (alpha half h = spin_half first, the unrestricted
+// driver's measure, cc_utils.py:482-560).  L1/L2 hold the guess on entry and
+// the result on return; hist (may be null) receives res per iteration.  A
+// dry-run context runs all max_iter iterations.
+extern "C" int kvft_lambda_solve(kvft_ctx *ctx, int ng, int nv, int no,
+                                 const double *const F[4], const double *const I[9],
+                                 const double *T1, const double *T2, const double *ev,
+                                 const double *eo, const double *ti, const double *g,
+                                 const double *G, double damp, double tconv, int max_iter,
+                                 int spin_half, double *L1, double *L2, double *hist,
+                                 int *iters) {
+    if (!ctx || ng < 1 || nv <= 0 || no <= 0 || !L1 || !L2 || max_iter < 0 || !iters ||
+        (spin_half > 0 && (nv != no || nv != 2 * spin_half)))
+        return kv_fail(ctx, KVFT_EINVAL, "kvft_lambda_solve: bad argument");
+    const long long v = nv, o = no, vo = v * o, v2o2 = v * v * o * o;
+    void *np = nullptr, *wp = nullptr;
+    KV_TRY(kv_scratch(ctx, "lambda_new", sizeof(double) * ng * (vo + v2o2), &np));
+    KV_TRY(kv_scratch(ctx, "lambda_norm", sizeof(double) * 32, &wp));
+    double *N1 = (double *)np, *N2 = N1 + ng * vo, *nw = (double *)wp;
+    // the blocks the measure runs over: (rank, element offset, dims, strides)
+    struct Blk {
+        int rank;
+        long long off;
+        int d[4];
+        long long st[4];
+    };
+    std::vector<Blk> blks;
+    const int h = spin_half;
+    if (h > 0) {
+        const long long n = nv, n2 = n * n, n3 = n2 * n;
+        blks.push_back({1, 0, {1, 1, h, h}, {0, 0, n, 1}});
+        blks.push_back({1, h * n + h, {1, 1, h, h}, {0, 0, n, 1}});
+        blks.push_back({2, 0, {h, h, h, h}, {n3, n2, n, 1}});
+        blks.push_back({2, h * n2 + h, {h, h, h, h}, {n3, n2, n, 1}});
+        blks.push_back({2, h * (n3 + n2 + n + 1), {h, h, h, h}, {n3, n2, n, 1}});
+    } else {
+        blks.push_back({1, 0, {1, 1, no, nv}, {0, 0, nv, 1}});
+        blks.push_back({2, 0, {no, no, nv, nv}, {o * v * v, v * v, v, 1}});
+    }
+    const int nb = (int)blks.size();
+    // norms of a + b * x over the blocks into nw[base + k]
+    auto norms = [&](const double *x1, const double *x2, double b, const double *y1,
+                     const double *y2, int base) -> int {
+        for (int k = 0; k < nb; k++) {
+            const Blk &q = blks[k];
+            const double *x = (q.rank == 1 ? x1 : x2) + q.off;
+            const double *y = y1 ? (q.rank == 1 ? y1 : y2) + q.off : nullptr;
+            const long long bst = q.rank == 1 ? vo : v2o2;
+            KV_TRY(kv_sumsq4(ctx, ng, q.d, 1.0, x, q.st, bst, b, y, q.st, bst, nw + base + k));
+        }
+        return KVFT_OK;
+    };
+    double hw[32];
+    auto read = [&](int count) -> int {
+        if (ctx->dry) {
+            std::memcpy(hw, nw, sizeof(double) * count);
+            return KVFT_OK;
+        }
+        KV_CHECK(ctx, cudaMemcpyAsync(hw, nw, sizeof(double) * count, cudaMemcpyDeviceToHost,
+                                      ctx->stream));
+        KV_CHECK(ctx, cudaStreamSynchronize(ctx->stream));
+        return KVFT_OK;
+    };
+    // Kelvin's normalisers: singles and doubles, the ab case weighted 4
+    auto normalisers = [&](const double *w, double *n1, double *n2) {
+        *n1 = 0.1;
+        *n2 = 0.1;
+        for (int k = 0; k < nb; k++) {
+            const double r = std::sqrt(w[k]);
+            if (blks[k].rank == 1) *n1 += r;
+            else *n2 += (h > 0 && k == 3) ? 4.0 * r : r;
+        }
+    };
+    KV_TRY(norms(L1, L2, 0.0, nullptr, nullptr, 0));
+    KV_TRY(read(nb));
+    double nl1, nl2;
+    normalisers(hw, &nl1, &nl2);
+    int it = 0;
+    for (; it < max_iter; it++) {
+        KV_TRY(kvft_ccsd_lambda(ctx, ng, nv, no, F, I, T1, T2, L1, L2, ev, eo, ti, g, G, N1, N2));
+        KV_TRY(norms(N1, N2, -1.0, L1, L2, 0));               // |L - L_old|
+        KV_TRY(kv_add(ctx, nv, no, ng, 1.0 - damp, KvTen{N1, "ia", vo, 0}, damp, L1, "ia", vo));
+        KV_TRY(kv_add(ctx, nv, no, ng, 1.0 - damp, KvTen{N2, "ijab", v2o2, 0}, damp, L2, "ijab",
+                      v2o2));
+        KV_TRY(norms(L1, L2, 0.0, nullptr, nullptr, nb));      // |L_old| after damping
+        KV_TRY(read(2 * nb));
+        double res = 0.0;
+        for (int k = 0; k < nb; k++)
+            res += std::sqrt(hw[k]) / (blks[k].rank == 1 ? nl1 : nl2);
+        normalisers(hw + nb, &nl1, &nl2);
+        if (hist) hist[it] = res;
+        if (!ctx->dry && !(res == res)) {
+            *iters = it + 1;
+            return kv_fail(ctx, KVFT_EDIVERGE, "lambda iteration: non-finite residual");
+        }
+        if (!ctx->dry && res < tconv) {
+            it++;
+            break;
+        }
+    }
+    *iters = it;
     return KVFT_OK;
 }
 

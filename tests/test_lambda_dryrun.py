@@ -111,14 +111,14 @@ class _Memory(object):
         return flat, idx
 
 
-def _replay(ctx, mem):
+def _replay(ctx, mem, sums=None):
     L = _L()
     n = ctypes.c_int()
     assert L.kvft_dryrun_count(ctx, ctypes.byref(n)) == 0
     ints = (ctypes.c_int * 32)()
     longs = (ctypes.c_longlong * 32)()
     dbls = (ctypes.c_double * 2)()
-    ptrs = (ctypes.c_void_p * 9)()
+    ptrs = (ctypes.c_void_p * 11)()
     kinds = []
     for i in range(n.value):
         assert L.kvft_dryrun_op(ctx, i, ints, longs, dbls, ptrs) == 0
@@ -174,6 +174,25 @@ def _replay(ctx, mem):
                     out[y] += G[y, x] * w * tb[x]
             fo, io = mem.view(ptrs[4], numpy.arange(ng * P))
             fo[io] = out.reshape(-1)
+        elif kind == 4:
+            dims = ints[23:27]
+            xs, ys = longs[21:25], longs[25:29]
+            xbst, ybst = longs[29], longs[30]
+            grid = numpy.indices(dims).reshape(4, -1)
+            xo = sum(grid[k] * xs[k] for k in range(4))
+            yo = sum(grid[k] * ys[k] for k in range(4))
+            acc = 0.0
+            for b in range(batch):
+                fx, ix = mem.view(ptrs[3] + 8 * b * xbst, xo)
+                val = alpha * fx[ix]
+                if ptrs[9]:
+                    fy, iy = mem.view(ptrs[9] + 8 * b * ybst, yo)
+                    val = val + beta * fy[iy]
+                acc += float((val * val).sum())
+            fr, ir = mem.view(ptrs[10], numpy.arange(1))
+            fr[ir] = acc
+            if sums is not None:
+                sums.append(acc)
         elif kind == 3:
             cr = _offsets(ints[17:20], longs[12:15])
             cc = _offsets(ints[20:23], longs[15:18])
@@ -344,3 +363,75 @@ def test_lambda_densities_dry_run_vs_oracle():
     for (name, blk, w, pairs), ref in zip(ft_lambda.P2_BLOCKS, P2):
         mine = ft_lambda._asym(Ig[I_ORDER.index(blk)].transpose(2, 3, 0, 1) / w, pairs)
         assert abs(mine - ref).max() < 1e-12 * max(1.0, abs(ref).max()), name
+
+
+@pytest.mark.parametrize("spin", [False, True])
+def test_lambda_solve_dry_run_vs_oracle(spin):
+    """kvft_lambda_solve (the resident damped loop) for three iterations,
+    replayed: the Lambda it leaves and the residual history rebuilt from its
+    recorded norms equal the oracle's loop (Kelvin's measure, or its
+    unrestricted driver's over the spin cases)."""
+    from oracle import ft_ccsd as oft, ft_utils, quadrature, systems
+    b = systems.UEGBasis(2 * numpy.pi, 1.2, norb=3)
+    eri = systems.g2e_loop(b)
+    en = systems.ueg_g_energies(b)
+    n, h, ng, beta, mu, damp, its = en.shape[0], en.shape[0] // 2, 4, 10.0, 0.1, 0.2, 3
+    fock = systems.g_fock_tot(b, eri, en, 1.0 / beta, mu)
+    F, I = oft.ft_integrals(fock, eri, en, beta, mu)
+    ti, g, G = quadrature.ft_quad(ng, beta, 'lin')
+    D1, D2 = ft_utils.D1(en, en), ft_utils.D2(en, en)
+    _, T1, T2 = oft.ft_ccsd(en, fock, eri, 1.0 / beta, mu, ngrid=ng, damp=damp, max_iter=30,
+                            return_amplitudes=True)
+    L10, L20 = ft_lambda.lambda_guess(F, I, T1, beta, ng, unrestricted=spin)
+    hist = []
+    R1, R2 = ft_lambda.ft_lambda_iter(L10.copy(), L20.copy(), T1, T2, F, I, D1, D2, g, G, beta,
+                                      ng, ti, {"tconv": 0.0, "max_iter": its, "damp": damp},
+                                      history=hist, spin_half=h if spin else None)
+    L1, L2 = numpy.ascontiguousarray(L10), numpy.ascontiguousarray(L20)
+    Fb = [numpy.ascontiguousarray(getattr(F, k)) for k in F_ORDER]
+    Ib = [numpy.ascontiguousarray(getattr(I, k)) for k in I_ORDER]
+    ev = numpy.ascontiguousarray(en)
+    grid = [numpy.ascontiguousarray(x) for x in (ti, g, G, T1, T2)]
+    Lib = _L()
+    ctx = ctypes.c_void_p()
+    iters = ctypes.c_int()
+    assert Lib.kvft_dryrun_create(0, 7, ctypes.byref(ctx)) == 0
+    sums = []
+    try:
+        P = lambda arrs: (ctypes.c_void_p * len(arrs))(*[a.ctypes.data for a in arrs])
+        st = Lib.kvft_lambda_solve(ctx, ng, n, n, P(Fb), P(Ib), grid[3].ctypes.data,
+                                   grid[4].ctypes.data, ev.ctypes.data, ev.ctypes.data,
+                                   grid[0].ctypes.data, grid[1].ctypes.data,
+                                   grid[2].ctypes.data, damp, 0.0, its, h if spin else 0,
+                                   L1.ctypes.data, L2.ctypes.data, None, ctypes.byref(iters))
+        assert st == 0 and iters.value == its
+        mem = _Memory()
+        for a in Fb + Ib + grid + [L1, L2, ev]:
+            mem.add(a)
+        i = 0
+        ptr, nbytes = ctypes.c_void_p(), ctypes.c_size_t()
+        while Lib.kvft_dryrun_scratch(ctx, i, ctypes.byref(ptr), ctypes.byref(nbytes)) == 0:
+            mem.add_raw(ptr.value, nbytes.value)
+            i += 1
+        _replay(ctx, mem, sums)
+    finally:
+        Lib.kvft_ctx_destroy(ctx)
+    assert abs(L1 - R1).max() < 1e-12 * abs(R1).max()
+    assert abs(L2 - R2).max() < 1e-12 * abs(R2).max()
+    # the residual history from the recorded norms: nb initial norms, then per
+    # iteration nb change norms and nb norms of the damped Lambda
+    nb = 5 if spin else 2
+    rank1 = [True, True, False, False, False] if spin else [True, False]
+
+    def normalisers(w):
+        n1 = 0.1 + sum(numpy.sqrt(x) for x, r in zip(w, rank1) if r)
+        n2 = 0.1 + sum((4.0 if spin and k == 3 else 1.0) * numpy.sqrt(x)
+                       for k, (x, r) in enumerate(zip(w, rank1)) if not r)
+        return n1, n2
+    assert len(sums) == nb + 2 * nb * its
+    nl = normalisers(sums[:nb])
+    for it in range(its):
+        blk = sums[nb + 2 * nb * it: nb + 2 * nb * (it + 1)]
+        res = sum(numpy.sqrt(x) / (nl[0] if r else nl[1]) for x, r in zip(blk[:nb], rank1))
+        assert abs(res - hist[it]) < 1e-12 * hist[it]
+        nl = normalisers(blk[nb:])
