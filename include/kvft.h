@@ -200,6 +200,12 @@ int kvft_lambda_solve(kvft_ctx *ctx, int ng, int nv, int no,
                       const double *eo, const double *ti, const double *g,
                       const double *G, double damp, double tconv, int max_iter,
                       int spin_half, double *L1, double *L2, double *hist, int *iters);
+/* Spin blocks of the Lambda path (kvft_lambda_residual, kvft_ccsd_lambda,
+ * kvft_lambda_solve, kvft_lambda_densities): half = h > 0 asserts that every
+ * operand vanishes outside the spin-conserving blocks of an alpha-first
+ * layout with nv = no = 2h, so that each contraction runs over its nonzero
+ * spin-block products only; 0 turns it off (the default). */
+int kvft_set_lambda_spin_blocks(kvft_ctx *ctx, int half);
 /* The strided-GEMM form of an index-string contraction C[cix] = A[aix] B[bix]
  * (letters a-h virtual, i-n occupied; every letter in exactly two of the
  * three): mnk = {M, N, K}; sizes/strides hold the composite indices (three

@@ -109,6 +109,7 @@ _SIGS = {
                                          vp, vp, vp, vp, ctypes.c_double, ctypes.c_double,
                                          ctypes.c_int, ctypes.c_int, vp, vp, vp,
                                          ctypes.POINTER(ctypes.c_int)]),
+    "kvft_set_lambda_spin_blocks": (ctypes.c_int, [vp, ctypes.c_int]),
     "kvft_einsum_plan": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_char_p,
                                         ctypes.c_char_p, ctypes.c_char_p,
                                         ctypes.POINTER(ctypes.c_int),

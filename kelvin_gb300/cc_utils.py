@@ -15,8 +15,8 @@ import time
 import numpy
 
 from . import _lib
-from .ft_cc_equations import (F_ORDER, I_ORDER, ccsd_stanton, device_blocks,
-                              energies_from_d1)
+from .ft_cc_equations import (F_ORDER, I_ORDER, _SpinBlocks, ccsd_stanton, device_blocks,
+                              energies_from_d1, spin_half_of)
 
 
 class one_e_blocks(object):
@@ -323,12 +323,15 @@ def _lambda_solve_device(ctx, L1, L2, T1, T2, F, I, D1, g, G, ng, ti, conv, hist
     max_iter = int(conv["max_iter"])
     hist = numpy.zeros(max(max_iter, 1))
     iters = ctypes.c_int()
-    ctx.check(ctx.L.kvft_lambda_solve(ctx.h, ng, blk.nv, blk.no, blk.Fp, blk.Ip, dT1.ptr,
-                                      dT2.ptr, dv[0].ptr, dv[1].ptr, dv[2].ptr, dv[3].ptr,
-                                      dv[4].ptr, float(conv["damp"]), float(conv["tconv"]),
-                                      max_iter, int(spin_half or 0), dL1.ptr, dL2.ptr,
-                                      hist.ctypes.data_as(ctypes.c_void_p),
-                                      ctypes.byref(iters)), "lambda_solve")
+    blocks = [getattr(F, b) for b in F_ORDER] + [getattr(I, b) for b in I_ORDER]
+    h = spin_half_of(blk.nv, blk.no, blocks + [T1, T2, L1, L2])
+    with _SpinBlocks(ctx, h):
+        ctx.check(ctx.L.kvft_lambda_solve(ctx.h, ng, blk.nv, blk.no, blk.Fp, blk.Ip, dT1.ptr,
+                                          dT2.ptr, dv[0].ptr, dv[1].ptr, dv[2].ptr, dv[3].ptr,
+                                          dv[4].ptr, float(conv["damp"]), float(conv["tconv"]),
+                                          max_iter, int(spin_half or 0), dL1.ptr, dL2.ptr,
+                                          hist.ctypes.data_as(ctypes.c_void_p),
+                                          ctypes.byref(iters)), "lambda_solve")
     for i in range(iters.value):
         logging.info(' %2d  %.10f' % (i + 1, hist[i]))
     if history is not None:

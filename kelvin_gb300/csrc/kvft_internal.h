@@ -119,6 +119,10 @@ struct kvft_ctx {
     // Dry run: launches are recorded here instead of executed, and scratch
     // is host memory filled with NaN (a context without a device).
     std::vector<KvDryOp> *dry = nullptr;
+    // Spin blocks of the Lambda path's operands (kvft_set_lambda_spin_blocks):
+    // 0, or h when every index-string contraction may run over its nonzero
+    // spin-block products only (nv = no = 2h, alpha half first).
+    int lam_spin = 0;
 };
 struct KvSpinScope {
     kvft_ctx *ctx;
@@ -269,13 +273,16 @@ struct KvTen {
     const char *ix;
     long long bst;
     int stable;                      // an integral block (fixed for a solver's lifetime)
+    // spin rule over the axes of ix: '+'/'-' signs with sum sign * spin = 0 on
+    // every nonzero element ("+-" for two axes, "++--" for four when null)
+    const char *spin = nullptr;
 };
 // The strided-GEMM form of C[cix] = alpha sum A[A.ix] B[B.ix] + beta C: rows
 // are the letters of A and C, columns those of B and C, the sum runs over the
 // letters of A and B; each group keeps at most three strided components.
 int kv_einsum_desc(int nv, int no, const char *aix, const char *bix, const char *cix,
                    int *M, int *N, int *K, KIdx *Ar, KIdx *Ac, KIdx *Br, KIdx *Bc,
-                   KIdx *Cr, KIdx *Cc, std::string *err);
+                   KIdx *Cr, KIdx *Cc, std::string *err, int sub = 0);
 int kv_einsum(kvft_ctx *ctx, int nv, int no, int batch, double alpha, const KvTen &A,
               const KvTen &B, double beta, double *C, const char *cix, long long cbst);
 // dst[dix] = beta dst + alpha src[src.ix] over the same letters (a transpose

@@ -66,7 +66,7 @@ long long stride_of(const Layout &L, char c) {
 // One composite index (at most three strided components) per tensor for the
 // letters of group g, merging neighbours that are contiguous in every tensor.
 bool group_index(const std::string &g, const Layout *const *ts, KIdx *const *out, int nt,
-                 int nv, int no, std::string *err) {
+                 int nv, int no, std::string *err, int sub = 0) {
     struct Comp {
         long long ext;
         long long st[2];
@@ -74,7 +74,7 @@ bool group_index(const std::string &g, const Layout *const *ts, KIdx *const *out
     std::vector<Comp> comps;
     for (char c : g) {
         Comp cp;
-        cp.ext = letter_extent(c, nv, no);
+        cp.ext = sub > 0 ? sub : letter_extent(c, nv, no);
         for (int t = 0; t < nt; t++) cp.st[t] = stride_of(*ts[t], c);
         comps.push_back(cp);
     }
@@ -112,7 +112,7 @@ bool group_index(const std::string &g, const Layout *const *ts, KIdx *const *out
 
 int kv_einsum_desc(int nv, int no, const char *aix, const char *bix, const char *cix, int *M,
                    int *N, int *K, KIdx *Ar, KIdx *Ac, KIdx *Br, KIdx *Bc, KIdx *Cr, KIdx *Cc,
-                   std::string *err) {
+                   std::string *err, int sub) {
     Layout A, B, C;
     if (!make_layout(aix, nv, no, &A, err) || !make_layout(bix, nv, no, &B, err) ||
         !make_layout(cix, nv, no, &C, err))
@@ -144,8 +144,9 @@ int kv_einsum_desc(int nv, int no, const char *aix, const char *bix, const char 
     }
     const Layout *mt[2] = {&A, &C}, *nt[2] = {&B, &C}, *kt[2] = {&A, &B};
     KIdx *mo[2] = {Ar, Cr}, *no_[2] = {Bc, Cc}, *ko[2] = {Ac, Br};
-    if (!group_index(gm, mt, mo, 2, nv, no, err) || !group_index(gn, nt, no_, 2, nv, no, err) ||
-        !group_index(gk, kt, ko, 2, nv, no, err))
+    if (!group_index(gm, mt, mo, 2, nv, no, err, sub) ||
+        !group_index(gn, nt, no_, 2, nv, no, err, sub) ||
+        !group_index(gk, kt, ko, 2, nv, no, err, sub))
         return KVFT_EINVAL;
     const long long m = (long long)Ar->size[0] * Ar->size[1] * Ar->size[2];
     const long long n = (long long)Bc->size[0] * Bc->size[1] * Bc->size[2];
@@ -160,6 +161,48 @@ int kv_einsum_desc(int nv, int no, const char *aix, const char *bix, const char 
     return KVFT_OK;
 }
 
+namespace {
+
+// One strided GEMM for a contraction already in GEMM form; a single row goes
+// as the transposed product C^T = B^T A^T, so that the long free dimension
+// is the GEMM's row dimension.
+int gemm_piece(kvft_ctx *ctx, int M, int N, int K, int batch, double alpha, const KvTen &A,
+               const KvTen &B, const KIdx &ar, const KIdx &ac, const KIdx &br, const KIdx &bc,
+               double beta, double *C, const KIdx &cr, const KIdx &cc, long long cbst) {
+    if (M == 1 && N > 1) {
+        KMat a{B.p, bc, br, B.bst, B.stable}, b{A.p, ac, ar, A.bst, A.stable};
+        KOut c{C, cc, cr, cbst};
+        return kv_gemm(ctx, N, M, K, batch, alpha, a, b, beta, c);
+    }
+    KMat a{A.p, ar, ac, A.bst, A.stable}, b{B.p, br, bc, B.bst, B.stable};
+    KOut c{C, cr, cc, cbst};
+    return kv_gemm(ctx, M, N, K, batch, alpha, a, b, beta, c);
+}
+
+// true when the spin assignment (bit of each letter in `spins`) satisfies
+// the tensor's rule
+bool spin_ok(const KvTen &T, const unsigned char *bit) {
+    const size_t n = std::strlen(T.ix);
+    const char *rule = T.spin ? T.spin : (n == 2 ? "+-" : "++--");
+    if (std::strlen(rule) != n) return true;
+    int sum = 0;
+    for (size_t k = 0; k < n; k++)
+        sum += (rule[k] == '+' ? 1 : -1) * bit[(unsigned char)T.ix[k]];
+    return sum == 0;
+}
+
+long long spin_offset(const char *ix, const unsigned char *bit, int h, int nv, int no) {
+    const size_t n = std::strlen(ix);
+    long long st = 1, off = 0;
+    for (size_t k = n; k-- > 0;) {
+        off += (long long)bit[(unsigned char)ix[k]] * h * st;
+        st *= letter_extent(ix[k], nv, no);
+    }
+    return off;
+}
+
+}  // namespace
+
 int kv_einsum(kvft_ctx *ctx, int nv, int no, int batch, double alpha, const KvTen &A,
               const KvTen &B, double beta, double *C, const char *cix, long long cbst) {
     int M, N, K;
@@ -168,16 +211,36 @@ int kv_einsum(kvft_ctx *ctx, int nv, int no, int batch, double alpha, const KvTe
     if (kv_einsum_desc(nv, no, A.ix, B.ix, cix, &M, &N, &K, &ar, &ac, &br, &bc, &cr, &cc,
                        &err) != KVFT_OK)
         return kv_fail(ctx, KVFT_EINVAL, err);
-    if (M == 1 && N > 1) {
-        // a single row: computed as the transposed product C^T = B^T A^T, so
-        // that the long free dimension is the GEMM's row dimension
-        KMat a{B.p, bc, br, B.bst, B.stable}, b{A.p, ac, ar, A.bst, A.stable};
-        KOut c{C, cc, cr, cbst};
-        return kv_gemm(ctx, N, M, K, batch, alpha, a, b, beta, c);
+    const int h = ctx->lam_spin;
+    if (h <= 0 || nv != no || nv != 2 * h)
+        return gemm_piece(ctx, M, N, K, batch, alpha, A, B, ar, ac, br, bc, beta, C, cr, cc,
+                          cbst);
+    // Spin blocks: every letter runs over an alpha half and a beta half, and
+    // only the products whose operands satisfy their spin rules are nonzero.
+    // C is scaled by beta first; the products then add into it.
+    if (beta != 1.0) KV_TRY(kv_scale_view(ctx, M, N, batch, beta, KOut{C, cr, cc, cbst}));
+    std::string letters;
+    for (const char *p : {A.ix, B.ix})
+        for (const char *q = p; *q; q++)
+            if (letters.find(*q) == std::string::npos) letters += *q;
+    int sM, sN, sK;
+    KIdx sar, sac, sbr, sbc, scr, scc;
+    if (kv_einsum_desc(nv, no, A.ix, B.ix, cix, &sM, &sN, &sK, &sar, &sac, &sbr, &sbc, &scr,
+                       &scc, &err, h) != KVFT_OK)
+        return kv_fail(ctx, KVFT_EINVAL, err);
+    unsigned char bit[128] = {0};
+    const int L = (int)letters.size();
+    for (unsigned m = 0; m < (1u << L); m++) {
+        for (int k = 0; k < L; k++) bit[(unsigned char)letters[k]] = (m >> k) & 1;
+        if (!spin_ok(A, bit) || !spin_ok(B, bit)) continue;
+        KvTen a = A, b = B;
+        a.p += spin_offset(A.ix, bit, h, nv, no);
+        b.p += spin_offset(B.ix, bit, h, nv, no);
+        double *c = C + spin_offset(cix, bit, h, nv, no);
+        KV_TRY(gemm_piece(ctx, sM, sN, sK, batch, alpha, a, b, sar, sac, sbr, sbc, 1.0, c, scr,
+                          scc, cbst));
     }
-    KMat a{A.p, ar, ac, A.bst, A.stable}, b{B.p, br, bc, B.bst, B.stable};
-    KOut c{C, cr, cc, cbst};
-    return kv_gemm(ctx, M, N, K, batch, alpha, a, b, beta, c);
+    return KVFT_OK;
 }
 
 int kv_add(kvft_ctx *ctx, int nv, int no, int batch, double alpha, const KvTen &src,
@@ -438,7 +501,8 @@ int kv_lambda_vjp(kvft_ctx *ctx, int nb, int nv, int no, const double *const F[4
     KV_TRY(E(1.0, TT(w.xAI, "abij", s_tau), TT(t2, "aeim", v2o2), 0.0, w.Wmbejb, "mbej",
              s_wmbej));
     KV_TRY(E(1.0, TT(w.xAI, "abij", s_tau), TT(t1, "am", vo), 0.0, w.Y1, "bijm", s_y1));
-    KV_TRY(E(1.0, TT(w.Y1, "bijm", s_y1), IB(vovo, "bmej"), 1.0, g1, "ei", vo));
+    // Y1[b,i,j,m] conserves b + m = i + j
+    KV_TRY(E(1.0, KvTen{w.Y1, "bijm", s_y1, 0, "+--+"}, IB(vovo, "bmej"), 1.0, g1, "ei", vo));
     KV_TRY(E(1.0, TT(w.xAI, "abij", s_tau), TT(t1, "ei", vo), 0.0, w.Y2, "abej", s_y2));
     KV_TRY(E(1.0, TT(w.Y2, "abej", s_y2), IB(vovo, "bmej"), 1.0, g1, "am", vo));
     KV_TRY(GE(1.0, TT(w.Y2, "abej", s_y2), TT(t1, "am", vo), Fg ? Ig[4] : nullptr, "bmej"));
@@ -847,6 +911,12 @@ extern "C" int kvft_lambda_solve(kvft_ctx *ctx, int ng, int nv, int no,
         }
     }
     *iters = it;
+    return KVFT_OK;
+}
+
+extern "C" int kvft_set_lambda_spin_blocks(kvft_ctx *ctx, int half) {
+    if (!ctx || half < 0) return kv_fail(ctx, KVFT_EINVAL, "lambda spin blocks: bad argument");
+    ctx->lam_spin = half;
     return KVFT_OK;
 }
 

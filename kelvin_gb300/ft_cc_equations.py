@@ -214,6 +214,44 @@ def energies_from_d1(D1):
             numpy.ascontiguousarray(D1[0, 0] - D1[0, :]))
 
 
+def spin_half_of(nv, no, arrays):
+    """h when every array (host arrays: integral blocks, or amplitudes with a
+    leading tau axis) vanishes outside the spin-conserving blocks of an
+    alpha-first layout with nv = no = 2h, else 0: the condition under which
+    the Lambda path may run its contractions over spin-block products only."""
+    if nv != no or nv % 2 or nv == 0:
+        return 0
+    h = nv // 2
+    sp = (numpy.arange(nv) >= h).astype(int)
+    one = sp[:, None] != sp[None, :]
+    two = (sp[:, None, None, None] + sp[None, :, None, None]
+           != sp[None, None, :, None] + sp[None, None, None, :])
+    for a in arrays:
+        if isinstance(a, _lib.DeviceArray):
+            return 0
+        a = numpy.asarray(a)
+        mask = one if a.ndim in (2, 3) else two
+        if a.ndim in (3, 5):
+            a = numpy.abs(a).max(axis=0)
+        if numpy.any(a[mask] != 0.0):
+            return 0
+    return h
+
+
+class _SpinBlocks(object):
+    """Spin blocks of the Lambda path for the duration of a call."""
+
+    def __init__(self, ctx, h):
+        self.ctx, self.h = ctx, h
+
+    def __enter__(self):
+        self.ctx.check(self.ctx.L.kvft_set_lambda_spin_blocks(self.ctx.h, self.h),
+                       "set_lambda_spin_blocks")
+
+    def __exit__(self, *exc):
+        self.ctx.L.kvft_set_lambda_spin_blocks(self.ctx.h, 0)
+
+
 def ccsd_lambda_guess(F, I, T1old, beta, ng, unrestricted=False):
     """Kelvin's starting Lambda: (1/beta)(F.ov + I.oovv T1, I.oovv) at every
     tau point (host arrays, ft_cc_equations.py:502-512); ``unrestricted``
@@ -250,9 +288,11 @@ def ccsd_lambda_opt(F, I, T1old, T2old, L1old, L2old, D1, D2, ti, ng, g, G, beta
                              for a in (ev, eo, ti, g, G))
     o1 = _lib.DeviceArray(ctx, (ng, no, nv))
     o2 = _lib.DeviceArray(ctx, (ng, no, no, nv, nv))
-    ctx.check(ctx.L.kvft_ccsd_lambda(ctx.h, ng, nv, no, blk.Fp, blk.Ip, dT1.ptr, dT2.ptr,
-                                     dL1.ptr, dL2.ptr, dev.ptr, deo.ptr, dti.ptr, dg.ptr,
-                                     dG.ptr, o1.ptr, o2.ptr), "ccsd_lambda_opt")
+    blocks = [getattr(F, b) for b in F_ORDER] + [getattr(I, b) for b in I_ORDER]
+    with _SpinBlocks(ctx, spin_half_of(nv, no, blocks + [T1old, T2old, L1old, L2old])):
+        ctx.check(ctx.L.kvft_ccsd_lambda(ctx.h, ng, nv, no, blk.Fp, blk.Ip, dT1.ptr, dT2.ptr,
+                                         dL1.ptr, dL2.ptr, dev.ptr, deo.ptr, dti.ptr, dg.ptr,
+                                         dG.ptr, o1.ptr, o2.ptr), "ccsd_lambda_opt")
     if host:
         return o1.to_host(), o2.to_host()
     return o1, o2
@@ -312,11 +352,12 @@ def lambda_densities(T1, T2, L1, L2, D1, ti, ng, g, G, ctx=None):
     d = [_lib.as_device(ctx, a) for a in (T1, T2, L1, L2)]
     dv = [_lib.as_device(ctx, numpy.ascontiguousarray(a, dtype=float))
           for a in (ev, eo, ti, g, G)]
-    ctx.check(ctx.L.kvft_lambda_densities(ctx.h, ng, nv, no, _lib.ptr_array(zF),
-                                          _lib.ptr_array(zI), d[0].ptr, d[1].ptr, d[2].ptr,
-                                          d[3].ptr, dv[0].ptr, dv[1].ptr, dv[2].ptr, dv[3].ptr,
-                                          dv[4].ptr, _lib.ptr_array(oF), _lib.ptr_array(oI)),
-              "lambda_densities")
+    with _SpinBlocks(ctx, spin_half_of(nv, no, [T1, T2, L1, L2])):
+        ctx.check(ctx.L.kvft_lambda_densities(ctx.h, ng, nv, no, _lib.ptr_array(zF),
+                                              _lib.ptr_array(zI), d[0].ptr, d[1].ptr, d[2].ptr,
+                                              d[3].ptr, dv[0].ptr, dv[1].ptr, dv[2].ptr,
+                                              dv[3].ptr, dv[4].ptr, _lib.ptr_array(oF),
+                                              _lib.ptr_array(oI)), "lambda_densities")
     return [a.to_host() for a in oF], [a.to_host() for a in oI]
 
 

@@ -365,12 +365,14 @@ def test_lambda_densities_dry_run_vs_oracle():
         assert abs(mine - ref).max() < 1e-12 * max(1.0, abs(ref).max()), name
 
 
-@pytest.mark.parametrize("spin", [False, True])
-def test_lambda_solve_dry_run_vs_oracle(spin):
+@pytest.mark.parametrize("spin,blocks", [(False, False), (True, False), (False, True),
+                                         (True, True)])
+def test_lambda_solve_dry_run_vs_oracle(spin, blocks):
     """kvft_lambda_solve (the resident damped loop) for three iterations,
     replayed: the Lambda it leaves and the residual history rebuilt from its
     recorded norms equal the oracle's loop (Kelvin's measure, or its
-    unrestricted driver's over the spin cases)."""
+    unrestricted driver's over the spin cases), with the contractions dense or
+    over their nonzero spin-block products."""
     from oracle import ft_ccsd as oft, ft_utils, quadrature, systems
     b = systems.UEGBasis(2 * numpy.pi, 1.2, norb=3)
     eri = systems.g2e_loop(b)
@@ -398,6 +400,7 @@ def test_lambda_solve_dry_run_vs_oracle(spin):
     assert Lib.kvft_dryrun_create(0, 7, ctypes.byref(ctx)) == 0
     sums = []
     try:
+        assert Lib.kvft_set_lambda_spin_blocks(ctx, h if blocks else 0) == 0
         P = lambda arrs: (ctypes.c_void_p * len(arrs))(*[a.ctypes.data for a in arrs])
         st = Lib.kvft_lambda_solve(ctx, ng, n, n, P(Fb), P(Ib), grid[3].ctypes.data,
                                    grid[4].ctypes.data, ev.ctypes.data, ev.ctypes.data,
@@ -413,7 +416,8 @@ def test_lambda_solve_dry_run_vs_oracle(spin):
         while Lib.kvft_dryrun_scratch(ctx, i, ctypes.byref(ptr), ctypes.byref(nbytes)) == 0:
             mem.add_raw(ptr.value, nbytes.value)
             i += 1
-        _replay(ctx, mem, sums)
+        kinds = _replay(ctx, mem, sums)
+        assert (3 in kinds) == blocks            # spin blocks scale C, then add pieces
     finally:
         Lib.kvft_ctx_destroy(ctx)
     assert abs(L1 - R1).max() < 1e-12 * abs(R1).max()

@@ -108,3 +108,20 @@ def test_density_blocks_and_rdms_match_oracle(solved):
     n1, n2 = fe.normal_ordered_rdms(beta, fo, 1.0 - fo, P1, P2)
     m1, m2 = ft_lambda.normal_ordered_rdms(beta, fo, 1.0 - fo, R1, R2)
     assert abs(n1 - m1).max() < 1e-15 and abs(n2 - m2).max() < 1e-15
+
+
+def test_spin_half_detection():
+    """The Lambda path's spin blocks are used only when every operand
+    vanishes outside the spin-conserving blocks."""
+    n, h, ng = 6, 3, 2
+    sp = (numpy.arange(n) >= h).astype(int)
+    cons = (sp[:, None, None, None] + sp[None, :, None, None]
+            == sp[None, None, :, None] + sp[None, None, None, :])
+    rng = numpy.random.default_rng(2)
+    I4 = rng.standard_normal((n,) * 4) * cons
+    F2 = rng.standard_normal((n, n)) * (sp[:, None] == sp[None, :])
+    T2 = rng.standard_normal((ng,) + (n,) * 4) * cons
+    assert fe.spin_half_of(n, n, [F2, I4, T2]) == h
+    T2[1, 0, h, 0, 0] = 1e-300
+    assert fe.spin_half_of(n, n, [F2, I4, T2]) == 0
+    assert fe.spin_half_of(n, n - 2, [F2]) == 0
