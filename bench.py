@@ -543,6 +543,35 @@ def run_gemm(args):
     return 0
 
 
+def run_esn(args):
+    """The differentiation workload (UEG, 14 electrons, rs = 2, 33 plane waves
+    = 66 spin orbitals, Theta = 0.5, ng = 16): E, S, N from the Lambda
+    equations (one adjoint solve) and from central differences of Omega
+    (four further solves), each timed end to end after the same FP64-grade
+    solve, with their differences."""
+    from kelvin_gb300 import _lib, ccsd as kccsd, systems
+    ctx = _lib.context(0)
+    s = systems.ueg_recipe(14, 2.0, 33, 0.5, device_build=True)
+    out = {"workload": "ueg66_esn", "n_spin_orbitals": 66, "ngrid": 16}
+
+    def solve():
+        cc = kccsd.ccsd(s, T=s.T, mu=s.mu, ngrid=16, damp=0.5, econv=1e-10, max_iter=200,
+                        precision="fp64_tc", ctx=ctx)
+        cc.run()
+        return cc
+    for method in ("lambda", "fd"):
+        cc = solve()
+        t0 = time.perf_counter()
+        E, S, N = cc.compute_ESN(method=method)
+        out[method] = {"E": E, "S": S, "N": N, "seconds": time.perf_counter() - t0}
+        cc.release()
+    out["dE"] = out["lambda"]["E"] - out["fd"]["E"]
+    out["dS"] = out["lambda"]["S"] - out["fd"]["S"]
+    out["dN"] = out["lambda"]["N"] - out["fd"]["N"]
+    print(json.dumps(out))
+    return 0
+
+
 def run_serve(args):
     """A seeded Poisson stream of mixed requests (kelvin_gb300.serve): solves/s
     and p50/p99 latency, completion minus arrival."""
@@ -572,10 +601,14 @@ def main():
     ap.add_argument("--serve", type=int, default=0,
                     help="serve this many requests of a seeded Poisson stream")
     ap.add_argument("--rate", type=float, default=20.0, help="request rate of --serve (1/s)")
+    ap.add_argument("--esn", action="store_true",
+                    help="E, S, N of the 66-spin-orbital UEG: Lambda route against differences")
     args = ap.parse_args()
     w = WORKLOADS[args.workload]
     if args.serve:
         return run_serve(args)
+    if args.esn:
+        return run_esn(args)
     if args.gemm:
         return run_gemm(args)
     if args.profile_step:
