@@ -382,6 +382,8 @@ class ccsd(object):
         # the mean-field Fock matrix follows the occupations, as in Kelvin's
         # relaxed occupation numbers (g_fock_d_den): F = h + sum_r <pr||qr> f_r
         Gd = numpy.einsum('prqr->pqr', eri)
+        # E1 = sum_i (h_ii - e_i) f_i + 1/2 f W f with h = F - sum_r <pr||qr> f_r
+        hd = numpy.diag(fock0) - Gd.diagonal(axis1=0, axis2=1).T @ fo0 - en
         prec = 'fp64_tc' if self.precision == 'mixed' else self.precision
         conv = {"econv": min(self.econv, 1e-12), "tconv": 1e3 * min(self.econv, 1e-12),
                 "max_iter": max(self.max_iter, 200), "damp": self.damp}
@@ -390,7 +392,7 @@ class ccsd(object):
             fo = fermi(beta, en, mu)
             fock = fock0 + Gd @ (fo - fo0)
             E0 = grand_potential0(beta, en, mu) + self.sys.const_energy()
-            E1 = 0.5 * fo @ W @ fo
+            E1 = hd @ fo + 0.5 * fo @ W @ fo
             ti, g, G = ft_quad(self.ngrid, beta, self.quad)
             self.ctx.set_precision(*PRECISIONS[prec])
             solver = DeviceSolver.from_system(self.ctx, en, fock, eri, beta, mu, ti, g, G)

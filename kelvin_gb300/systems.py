@@ -208,13 +208,19 @@ class UEGSystem(object):
         return numpy.diag(kin) + numpy.einsum('prqr,r->pq', self.g_aint_tot(), fo)
 
     def get_mp1(self):
-        fo = fermi(1.0 / self.T, self.g_energies_tot(), self.mu)
+        """First-order grand potential sum_i (h_ii - e_i) f_i +
+        1/2 sum_ij <ij||ij> f_i f_j, h the kinetic energy (ueg_scf_system.py:
+        146-157; the first sum is the exchange shift's and vanishes without
+        it)."""
+        en = self.g_energies_tot()
+        fo = fermi(1.0 / self.T, en, self.mu)
+        e1 = (numpy.hstack((self.ekin, self.ekin)) - en) @ fo
         if self.device_build:
             # 1/2 sum_ij <ij||ij> f_i f_j = -1/2 sum_{ij, same spin} v(n_i - n_j) f_i f_j
             v = self._vq()
             nb = self.nb
-            return -0.5 * (fo[:nb] @ v @ fo[:nb] + fo[nb:] @ v @ fo[nb:])
-        return 0.5 * numpy.einsum('ijij,i,j->', self.g_aint_tot(), fo, fo)
+            return e1 - 0.5 * (fo[:nb] @ v @ fo[:nb] + fo[nb:] @ v @ fo[nb:])
+        return e1 + 0.5 * numpy.einsum('ijij,i,j->', self.g_aint_tot(), fo, fo)
 
 
 class HubbardRing(object):

@@ -43,6 +43,7 @@ def test_uegscf7_ng40_vs_kelvin(ctx):
     Et, Ecc = cc.run()
     assert abs(Ecc - meta["Omega_cc"]) < OMEGA_TOL
     assert abs(Ecc - meta["kelvin_example_golden_u"]) < 1e-11
+    assert abs(Et - meta["Omega_total"]) < OMEGA_TOL
 
 
 def test_ueg19_vs_kelvin_example(ctx):

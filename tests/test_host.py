@@ -2,6 +2,7 @@
 C ABI of libkvft.so (it loads and exports every symbol include/kvft.h
 declares)."""
 import ctypes
+import json
 import os
 import re
 import subprocess
@@ -9,7 +10,7 @@ import subprocess
 import numpy
 import pytest
 
-from conftest import ROOT, golden
+from conftest import GOLDEN, ROOT, golden
 from kelvin_gb300 import quadrature, systems
 from oracle import quadrature as oq
 from oracle import systems as osys
@@ -116,3 +117,17 @@ def test_library_status_strings_without_gpu():
     assert L.kvft_status_string(0) == b"ok"
     assert L.kvft_status_string(6) == b"not converged"
     assert L.kvft_solver_footprint(38, 10, 0) > 8 * 38 ** 4 * 10
+
+
+@pytest.mark.parametrize("device_build", [False, True])
+def test_hf_shifted_first_order_energy(device_build):
+    """With HF-shifted orbital energies the first-order grand potential has
+    Kelvin's sum_i (h_ii - e_i) f_i term (ueg_scf_system.py:146-157): E1 and
+    Omega equal the UEGSCFSystem values of examples/ueg_ft_cc_compare."""
+    meta = json.load(open(os.path.join(GOLDEN, "uegscf7.json")))
+    s = systems.UEGSystem(meta["T"], meta["L"], meta["cutoff"], mu=meta["mu"], norb=7,
+                          hf_shift=True, device_build=device_build)
+    E0 = systems.grand_potential0(1.0 / meta["T"], s.g_energies_tot(), meta["mu"]) \
+        + s.const_energy()
+    assert abs(s.get_mp1() - meta["G1"]) < 1e-15
+    assert abs(E0 + s.get_mp1() + meta["Omega_cc"] - meta["Omega_total"]) < 1e-14
