@@ -198,3 +198,32 @@ def test_lambda_ueg19_vs_kelvin():
     assert abs(E - meta["E"]) < 1e-12
     assert abs(S - meta["S"]) < 1e-12
     assert abs(N - meta["N"]) < 1e-12
+
+
+def test_lambda_esn_hf_shifted_vs_finite_differences():
+    """The same check with HF-shifted orbital energies (the UEGSCFSystem form,
+    ueg_scf_system.py:280-297), where E1 has the sum_i (h_ii - e_i) f_i term
+    and the Fock matrix's diagonal differs from the energies; Kelvin's test
+    suite runs this comparison for its SCF systems (test_ft_deriv.py:56-110)."""
+    T, mu, ng, damp = 0.1, 0.12, 6, 0.2
+    b = systems.UEGBasis(2 * numpy.pi, 1.2, norb=7)
+    eri = systems.g2e_loop(b)
+    en = systems.uegscf_g_energies(b, mu)
+    h = numpy.diag(numpy.hstack((b.Es, b.Es)))
+    assert abs(numpy.diag(h) - en).max() > 1e-3
+    E, S, N, Om, T1, T2, L1, L2 = ft_lambda.solve(en, h, eri, T, mu, ngrid=ng, damp=damp,
+                                                  econv=1e-12, lconv=1e-11, max_iter=200)
+
+    def omega(T, mu):
+        beta = 1.0 / T
+        fock = ft_lambda.mean_field(h, eri, ft_utils.ff(beta, en, mu))
+        O0, O1 = ft_lambda.omega_ref(en, h, eri, beta, mu)
+        return ft_ccsd.ft_ccsd(en, fock, eri, T, mu, ngrid=ng, econv=1e-13, max_iter=200,
+                               damp=damp, E1=O1, T1in=T1, T2in=T2)[0]
+    d = 2e-5
+    Nx = -(omega(T, mu + d) - omega(T, mu - d)) / (2 * d)
+    Sx = -(omega(T + d, mu) - omega(T - d, mu)) / (2 * d)
+    Ex = Om + T * Sx + mu * Nx
+    assert abs(N - Nx) < 2e-9
+    assert abs(E - Ex) < 2e-9
+    assert abs(S - Sx) < 2e-8

@@ -125,3 +125,24 @@ def test_spin_half_detection():
     T2[1, 0, h, 0, 0] = 1e-300
     assert fe.spin_half_of(n, n, [F2, I4, T2]) == 0
     assert fe.spin_half_of(n, n - 2, [F2]) == 0
+
+
+def test_esn_from_lambda_hf_shifted_matches_oracle():
+    """The driver's assembly with HF-shifted energies (E1's linear term, a
+    Fock diagonal that differs from the energies) against the oracle."""
+    T, mu, ng = 0.1, 0.12, 4
+    b = systems.UEGBasis(2 * numpy.pi, 1.2, norb=7)
+    eri = systems.g2e_loop(b)
+    en = systems.uegscf_g_energies(b, mu)
+    h = numpy.diag(numpy.hstack((b.Es, b.Es)))
+    E, S, N, Om, T1, T2, L1, L2 = ft_lambda.solve(en, h, eri, T, mu, ngrid=ng, damp=0.2,
+                                                  econv=1e-12, lconv=1e-11, max_iter=200)
+
+    def stanton(F, I, T1, T2, D1, D2, ti, ng, G):
+        return ft_ccsd.ccsd_stanton(F, I, T1, T2, D1, D2, ti, ng, G)
+
+    def energy(T1, T2, f, eri_, g, beta):
+        return ft_ccsd.ft_cc_energy(T1, T2, f, eri_, g, beta)
+    e, s, n = kccsd.esn_from_lambda(en, h, eri, 1.0 / T, mu, ng, 'lin', T1, T2, L1, L2, Om,
+                                    stanton, energy)
+    assert abs(e - E) < 1e-12 and abs(n - N) < 1e-12 and abs(s - S) < 1e-11
