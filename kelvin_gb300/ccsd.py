@@ -418,6 +418,7 @@ class ccsd(object):
         self.N = -(Np - Nm) / (2.0 * dm)
         self.E = ((beta + db) * Bp - (beta - db) * Bm) / (2.0 * db) + mu * self.N
         self.S = beta * (self.E - mu * self.N - Om)
+        self._esn_parts()
         return self.E, self.S, self.N
 
     def _g_ft_rdms(self):
@@ -480,7 +481,34 @@ class ccsd(object):
                                                      self.Gtot, stanton, energy)
         finally:
             self.ctx.set_precision(*prev)
+        self._esn_parts()
         return self.E, self.S, self.N
+
+    def _esn_parts(self):
+        """Kelvin's split of E, S, N (kelvin/ccsd.py:193-214): the
+        non-interacting part (E0, S0, N0) of Omega0 and the first-order part
+        (E1, S1, N1) of Omega1 = sum_i (h_ii - e_i) f_i + 1/2 f W f, in closed
+        form with the Fock matrix following the occupations; the CC part is
+        the rest."""
+        beta, mu = self.beta, self.mu
+        en = numpy.asarray(self.sys.g_energies_tot(), dtype=float)
+        eri = self.sys.g_aint_tot()
+        fo = fermi(beta, en, mu)
+        fv = 1.0 - fo
+        W = numpy.einsum('ijij->ij', eri)
+        hd = numpy.diag(self.sys.g_fock_tot()) - W @ fo - en
+        G0 = grand_potential0(beta, en, mu) + self.sys.const_energy()
+        G1 = hd @ fo + 0.5 * fo @ W @ fo
+        self.N0 = fo.sum()
+        self.E0 = en @ fo + self.sys.const_energy()
+        self.S0 = beta * (self.E0 - G0 - mu * self.N0)
+        grad = hd + W @ fo                       # dOmega1 / df
+        self.N1 = -grad @ (beta * fo * fv)
+        self.E1 = G1 + beta * (grad @ (-(en - mu) * fo * fv)) + mu * self.N1
+        self.S1 = beta * (self.E1 - G1 - mu * self.N1)
+        self.Ncc = self.N - self.N0 - self.N1
+        self.Ecc = self.E - self.E0 - self.E1
+        self.Scc = self.S - self.S0 - self.S1
 
     def release(self):
         """Free the device buffers of the last solve."""

@@ -89,6 +89,10 @@ def test_esn_of_the_mean_field_part(monkeypatch):
     assert abs(N - N_ref) < 1e-8
     assert abs(E - E_ref) < 1e-8
     assert abs(S - S_ref) < 1e-7
+    # Kelvin's split: with no correlation the CC parts vanish
+    assert abs(cc.N0 - f.sum()) < 1e-14
+    assert abs(cc.Ncc) < 1e-8 and abs(cc.Ecc) < 1e-8 and abs(cc.Scc) < 1e-7
+    assert abs(cc.E0 + cc.E1 + cc.Ecc - E) < 1e-14
     # five solves; the Fock matrix of each follows its occupations
     assert len(FakeSolver.calls) == 5
     for b, m, fock in FakeSolver.calls:
