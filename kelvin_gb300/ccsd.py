@@ -450,13 +450,33 @@ class ccsd(object):
     def _g_ft_2rdm(self):
         self._g_ft_rdms()
 
-    def full_1rdm(self):
+    def full_1rdm(self, relax=False):
         """Unrelaxed one-particle density matrix: the normal-ordered part plus
         the Fermi-Dirac occupations (kelvin/ccsd.py:1988-2004, orbtype 'g')."""
+        if relax:
+            raise Exception("kelvin_gb300.ccsd: relaxed densities are not built")
         if getattr(self, "n1rdm", None) is None:
             self._g_ft_rdms()
         en = numpy.asarray(self.sys.g_energies_tot(), dtype=float)
         return self.n1rdm + numpy.diag(fermi(self.beta, en, self.mu))
+
+    def full_2rdm(self, relax=False):
+        """Unrelaxed two-particle density matrix (kelvin/ccsd.py:2008-2058,
+        orbtype 'g'; cc_utils.py:2018-2024): the normal-ordered part plus the
+        antisymmetrised products of the occupations with themselves and, with
+        weight 1/2 each way, with the normal-ordered 1-RDM."""
+        if relax:
+            raise Exception("Relaxed 2-RDM is not implemented")
+        if getattr(self, "n2rdm", None) is None:
+            self._g_ft_rdms()
+        en = numpy.asarray(self.sys.g_energies_tot(), dtype=float)
+        f = numpy.diag(fermi(self.beta, en, self.mu))
+        n1 = self.n1rdm
+        rdm2 = self.n2rdm.copy()
+        for a, b, w in ((f, f, 1.0), (f, n1, 0.5), (n1, f, 0.5)):
+            x = numpy.einsum('pr,qs->pqrs', a, b)
+            rdm2 += w * (x - x.transpose(0, 1, 3, 2))
+        return rdm2
 
     def _esn_lambda(self):
         """E, S, N from the stored T and Lambda; the amplitude updates and

@@ -190,3 +190,20 @@ def test_unrestricted_lambda_driver(monkeypatch):
     assert numpy.array_equal(l1b, Lg[0][:, na:, na:])
     assert numpy.array_equal(l2ab, Lg[1][:, :na, na:, :na, na:])
     assert cc._Lg is Lg
+
+
+def test_full_rdms_of_the_reference():
+    """With no correlation (zero normal-ordered parts) the full RDMs are the
+    grand-canonical mean-field ones: gamma = diag(f), and
+    sum_pq Gamma[p,q,p,q] = (sum f)^2 - sum f^2 (kelvin/cc_utils.py:2018-2024)."""
+    rng = numpy.random.default_rng(6)
+    T, mu = 0.3, 0.1
+    s = FakeSystem(rng, 6, T, mu)
+    cc = ccsd_mod.ccsd(s, T=T, mu=mu, ngrid=4, ctx=FakeCtx())
+    n = s.en.shape[0]
+    cc.n1rdm, cc.n2rdm = numpy.zeros((n, n)), numpy.zeros((n,) * 4)
+    f = fermi(1.0 / T, s.en, mu)
+    assert numpy.allclose(cc.full_1rdm(), numpy.diag(f), rtol=0, atol=1e-15)
+    g2 = cc.full_2rdm()
+    assert abs(numpy.einsum('pqpq->', g2) - (f.sum() ** 2 - (f * f).sum())) < 1e-13
+    assert abs(g2 + g2.transpose(1, 0, 2, 3)).max() < 1e-15
