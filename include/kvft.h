@@ -200,6 +200,14 @@ int kvft_lambda_solve(kvft_ctx *ctx, int ng, int nv, int no,
                       const double *eo, const double *ti, const double *g,
                       const double *G, double damp, double tconv, int max_iter,
                       int spin_half, double *L1, double *L2, double *hist, int *iters);
+/* Kelvin's starting Lambda (ft_cc_equations.py:502-512): L1 = F.ov/beta +
+ * I.oovv T1/beta, L2 = I.oovv/beta at every tau point; unrestricted != 0
+ * drops the 1/beta of the T1 term as Kelvin's unrestricted guess does
+ * (:515-526).  Device pointers. */
+int kvft_lambda_guess(kvft_ctx *ctx, int ng, int nv, int no,
+                      const double *const F[4], const double *const I[9],
+                      const double *T1, double beta, int unrestricted, double *L1,
+                      double *L2);
 /* Spin blocks of the Lambda path (kvft_lambda_residual, kvft_ccsd_lambda,
  * kvft_lambda_solve, kvft_lambda_densities): half = h > 0 asserts that every
  * operand vanishes outside the spin-conserving blocks of an alpha-first
@@ -219,9 +227,10 @@ int kvft_einsum_plan(int nv, int no, const char *aix, const char *bix,
  * descriptors each kernel would receive) instead of running them; pointers
  * passed to it are host memory and its scratch is host memory filled with
  * NaN.  Lets the index arithmetic of a call be replayed and checked on a
- * CPU.  kvft_lambda_residual, kvft_ccsd_lambda, kvft_lambda_solve and
- * kvft_lambda_densities accept it; every other call that would touch the device returns
- * KVFT_EINVAL.  Destroy it with kvft_ctx_destroy. */
+ * CPU.  kvft_lambda_residual, kvft_ccsd_lambda, kvft_lambda_solve,
+ * kvft_lambda_guess and kvft_lambda_densities accept it; every other call
+ * that would touch the device returns KVFT_EINVAL.  Destroy it with
+ * kvft_ctx_destroy. */
 int kvft_dryrun_create(int precision, int digits, kvft_ctx **ctx);
 int kvft_dryrun_count(const kvft_ctx *ctx, int *count);
 /* op i: ints[32], longs[32], dbls[2], ptrs[11]; kind 0 contraction (M N K
@@ -329,6 +338,17 @@ int kvft_solver_device_amplitudes(kvft_solver *s, double **T1, double **T2);
  * through kvft_solver_device_amplitudes are the caller's to keep
  * spin-conserving. */
 int kvft_solver_set_spin_blocks(kvft_solver *s, int on, int *half);
+/* Lambda on the solver's resident integrals and amplitudes (the converged T
+ * of its last solve): guess 1 forms Kelvin's starting Lambda in L1/L2, 2 its
+ * unrestricted driver's, 0 keeps the one given; then kvft_lambda_solve
+ * (damp, tconv, max_iter, measure_half as there).  L1[ng][no][nv],
+ * L2[ng][no][no][nv][nv] are device buffers; the solver's spin blocks carry
+ * over to the Lambda contractions. */
+int kvft_solver_lambda(kvft_solver *s, int guess, double damp, double tconv, int max_iter,
+                       int measure_half, double *L1, double *L2, double *hist, int *iters);
+/* kvft_lambda_densities on the solver's integrals and amplitudes. */
+int kvft_solver_lambda_densities(kvft_solver *s, const double *L1, const double *L2,
+                                 double *const Fg[4], double *const Ig[9]);
 size_t kvft_solver_footprint(int n, int ng, int precision);
 
 #ifdef __cplusplus

@@ -110,6 +110,9 @@ _SIGS = {
                                          ctypes.c_int, ctypes.c_int, vp, vp, vp,
                                          ctypes.POINTER(ctypes.c_int)]),
     "kvft_set_lambda_spin_blocks": (ctypes.c_int, [vp, ctypes.c_int]),
+    "kvft_lambda_guess": (ctypes.c_int, [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                         ctypes.POINTER(vp), ctypes.POINTER(vp), vp,
+                                         ctypes.c_double, ctypes.c_int, vp, vp]),
     "kvft_einsum_plan": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_char_p,
                                         ctypes.c_char_p, ctypes.c_char_p,
                                         ctypes.POINTER(ctypes.c_int),
@@ -152,6 +155,11 @@ _SIGS = {
                                                      ctypes.POINTER(vp)]),
     "kvft_solver_set_spin_blocks": (ctypes.c_int, [vp, ctypes.c_int,
                                                    ctypes.POINTER(ctypes.c_int)]),
+    "kvft_solver_lambda": (ctypes.c_int, [vp, ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                                          ctypes.c_int, ctypes.c_int, vp, vp, vp,
+                                          ctypes.POINTER(ctypes.c_int)]),
+    "kvft_solver_lambda_densities": (ctypes.c_int, [vp, vp, vp, ctypes.POINTER(vp),
+                                                    ctypes.POINTER(vp)]),
     "kvft_solver_footprint": (ctypes.c_size_t, [ctypes.c_int, ctypes.c_int,
                                                 ctypes.c_int]),
 }

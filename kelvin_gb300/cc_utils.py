@@ -128,6 +128,51 @@ class DeviceSolver(object):
             "kvft_solver_get_amplitudes")
         return T1, T2
 
+    def lambda_solve(self, conv_options, guess=1, L1=None, L2=None, measure_half=None,
+                     history=None):
+        """Kelvin's Lambda iteration (cc_utils.py:414-480) on the solver's
+        resident integrals and converged amplitudes; guess 1 is Kelvin's
+        starting Lambda, 2 its unrestricted driver's, 0 takes L1/L2.  Returns
+        host (L1, L2)."""
+        ng, nv, no = self.ng, self.nv, self.no
+        if guess == 0:
+            dL1 = _lib.DeviceArray.from_host(self.ctx, L1)
+            dL2 = _lib.DeviceArray.from_host(self.ctx, L2)
+        else:
+            dL1 = _lib.DeviceArray(self.ctx, (ng, no, nv))
+            dL2 = _lib.DeviceArray(self.ctx, (ng, no, no, nv, nv))
+        max_iter = int(conv_options["max_iter"])
+        hist = numpy.zeros(max(max_iter, 1))
+        iters = ctypes.c_int()
+        tbeg = time.time()
+        self.ctx.check(self.ctx.L.kvft_solver_lambda(
+            self.h, int(guess), float(conv_options["damp"]), float(conv_options["tconv"]),
+            max_iter, int(measure_half or 0), dL1.ptr, dL2.ptr,
+            hist.ctypes.data_as(_lib.vp), ctypes.byref(iters)), "kvft_solver_lambda")
+        for i in range(iters.value):
+            logging.info(' %2d  %.10f' % (i + 1, hist[i]))
+        if history is not None:
+            history.extend(float(x) for x in hist[:iters.value])
+        if iters.value == 0 or hist[iters.value - 1] >= conv_options["tconv"]:
+            logging.warning("CCSD Lambda-equations did not converge!")
+        logging.info("Total CCSD Lambda time: %f s" % (time.time() - tbeg))
+        return dL1.to_host(), dL2.to_host()
+
+    def lambda_densities(self, L1, L2):
+        """Integral gradients (Fg, Ig) of the Lagrangian at the solver's
+        amplitudes and the given Lambda (kvft_solver_lambda_densities)."""
+        nv, no = self.nv, self.no
+        shp1 = {"oo": (no, no), "ov": (no, nv), "vo": (nv, no), "vv": (nv, nv)}
+        ext = {"o": no, "v": nv}
+        oF = [_lib.DeviceArray(self.ctx, shp1[b]) for b in F_ORDER]
+        oI = [_lib.DeviceArray(self.ctx, tuple(ext[c] for c in b)) for b in I_ORDER]
+        dL1 = _lib.as_device(self.ctx, L1)
+        dL2 = _lib.as_device(self.ctx, L2)
+        self.ctx.check(self.ctx.L.kvft_solver_lambda_densities(
+            self.h, dL1.ptr, dL2.ptr, _lib.ptr_array(oF), _lib.ptr_array(oI)),
+            "kvft_solver_lambda_densities")
+        return [a.to_host() for a in oF], [a.to_host() for a in oI]
+
     def guess(self, kind, damp=0.0):
         """kind 0: zeros, 1: Kelvin's first-order guess, 2: keep.  Runs zero
         iterations and returns the guess energy (Qterm = False)."""

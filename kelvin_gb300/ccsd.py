@@ -316,14 +316,28 @@ class ccsd(object):
         prev = ctx_precision(self.ctx)
         prec = 'fp64_tc' if self.precision == 'mixed' else self.precision
         self.ctx.set_precision(*PRECISIONS[prec])
+        conv = {"tconv": self.tconv, "max_iter": self.max_iter, "damp": self.damp}
         try:
-            F, I = ft_integrals(self.sys, en, beta, mu, ctx=self.ctx)
+            if self.solver is not None and (L1 is None or L2 is None):
+                # the last solve's integrals and amplitudes are still resident
+                self._Lg = self.solver.lambda_solve(conv, guess=2 if u else 1, measure_half=na)
+                L1 = None
+            else:
+                F, I = ft_integrals(self.sys, en, beta, mu, ctx=self.ctx)
+        finally:
+            self.ctx.set_precision(*prev)
+        if self.solver is not None and L1 is None:
+            self.L1, self.L2 = self._Lg
+            if u:
+                self.L1, self.L2 = g_to_u_t(self._Lg[0], self._Lg[1], na)
+            return self.L1, self.L2
+        self.ctx.set_precision(*PRECISIONS[prec])
+        try:
             if L1 is None or L2 is None:
                 L1, L2 = ccsd_lambda_guess(F, I, T1, self.beta_max, ng, unrestricted=u)
             elif u:
                 L1 = u_to_g_t1(*[numpy.asarray(x) for x in L1])
                 L2 = u_to_g_t2(*[numpy.asarray(x) for x in L2])
-            conv = {"tconv": self.tconv, "max_iter": self.max_iter, "damp": self.damp}
             D1 = en[:, None] - en[None, :]
             self._Lg = ft_lambda_iter("CCSD", L1, L2, T1, T2, F, I, D1, None, self.g, self.G,
                                       self.beta_max, ng, self.ti, self.iprint, conv,
@@ -434,8 +448,11 @@ class ccsd(object):
         prec = 'fp64_tc' if self.precision == 'mixed' else self.precision
         self.ctx.set_precision(*PRECISIONS[prec])
         try:
-            Fg, Ig = lambda_densities(T1, T2, self._Lg[0], self._Lg[1], D1, self.ti,
-                                      self.ngrid, self.g, self.G, ctx=self.ctx)
+            if self.solver is not None:
+                Fg, Ig = self.solver.lambda_densities(self._Lg[0], self._Lg[1])
+            else:
+                Fg, Ig = lambda_densities(T1, T2, self._Lg[0], self._Lg[1], D1, self.ti,
+                                          self.ngrid, self.g, self.G, ctx=self.ctx)
         finally:
             self.ctx.set_precision(*prev)
         (self.dia, self.dba, self.dji, self.dai), self.P2 = kelvin_densities(Fg, Ig)

@@ -914,6 +914,25 @@ extern "C" int kvft_lambda_solve(kvft_ctx *ctx, int ng, int nv, int no,
     return KVFT_OK;
 }
 
+// Kelvin's starting Lambda (ft_cc_equations.py:502-512; unrestricted:
+// 515-526, whose I.oovv T1 term has no 1/beta): L1 = F.ov / beta +
+// c I.oovv T1, L2 = I.oovv / beta at every tau point, c = 1/beta or 1.
+extern "C" int kvft_lambda_guess(kvft_ctx *ctx, int ng, int nv, int no,
+                                 const double *const F[4], const double *const I[9],
+                                 const double *T1, double beta, int unrestricted, double *L1,
+                                 double *L2) {
+    if (!ctx || ng < 1 || nv <= 0 || no <= 0 || !F || !I || !F[1] || !I[5] || !T1 || !L1 ||
+        !L2 || !(beta > 0.0))
+        return kv_fail(ctx, KVFT_EINVAL, "kvft_lambda_guess: bad argument");
+    if (!ctx->dry) cudaSetDevice(ctx->device);
+    const long long vo = (long long)nv * no, v2o2 = vo * vo;
+    const double c = unrestricted ? 1.0 : 1.0 / beta;
+    KV_TRY(kv_add(ctx, nv, no, ng, 1.0 / beta, KvTen{F[1], "ia", 0, 1}, 0.0, L1, "ia", vo));
+    KV_TRY(kv_einsum(ctx, nv, no, ng, c, KvTen{I[5], "ijab", 0, 1}, KvTen{T1, "bj", vo, 0}, 1.0,
+                     L1, "ia", vo));
+    return kv_add(ctx, nv, no, ng, 1.0 / beta, KvTen{I[5], "ijab", 0, 1}, 0.0, L2, "ijab", v2o2);
+}
+
 extern "C" int kvft_set_lambda_spin_blocks(kvft_ctx *ctx, int half) {
     if (!ctx || half < 0) return kv_fail(ctx, KVFT_EINVAL, "lambda spin blocks: bad argument");
     ctx->lam_spin = half;

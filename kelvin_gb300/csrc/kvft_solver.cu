@@ -680,6 +680,75 @@ int kvft_solver_set_amplitudes(kvft_solver *s, const double *T1h, const double *
     return KVFT_OK;
 }
 
+// Lambda on the solver's resident integrals and amplitudes: the guess
+// (guess 1: Kelvin's, 2: its unrestricted driver's; 0: L1/L2 already hold
+// one), then the resident damped iteration; L1/L2 are device buffers.  The
+// orbital energies are the solver's or, for the explicit-denominator form,
+// read off D1 (ev[a] = D1[a,0], eo[i] = D1[0,0] - D1[0,i]).
+namespace {
+
+int solver_energies(kvft_solver *s, const double **ev, const double **eo) {
+    if (s->eps) {
+        *ev = *eo = s->eps;
+        return KVFT_OK;
+    }
+    const int nv = s->nv, no = s->no;
+    std::vector<double> d1((size_t)nv * no), h((size_t)nv + no);
+    KV_CHECK(s->ctx, cudaMemcpy(d1.data(), s->D1, sizeof(double) * d1.size(),
+                                cudaMemcpyDeviceToHost));
+    for (int a = 0; a < nv; a++) h[a] = d1[(size_t)a * no];
+    for (int i = 0; i < no; i++) h[nv + i] = d1[0] - d1[i];
+    void *p = nullptr;
+    KV_TRY(kv_scratch(s->ctx, "solver_energies", sizeof(double) * h.size(), &p));
+    KV_CHECK(s->ctx, cudaMemcpy(p, h.data(), sizeof(double) * h.size(), cudaMemcpyHostToDevice));
+    *ev = (const double *)p;
+    *eo = (const double *)p + nv;
+    return KVFT_OK;
+}
+
+struct LamSpinScope {
+    kvft_ctx *ctx;
+    int prev;
+    LamSpinScope(kvft_ctx *c, int h) : ctx(c), prev(c->lam_spin) { c->lam_spin = h; }
+    ~LamSpinScope() { ctx->lam_spin = prev; }
+};
+
+}  // namespace
+
+int kvft_solver_lambda(kvft_solver *s, int guess, double damp, double tconv, int max_iter,
+                       int measure_half, double *L1, double *L2, double *hist, int *iters) {
+    if (!s || !L1 || !L2 || !iters || guess < 0 || guess > 2)
+        return kv_fail(s ? s->ctx : nullptr, KVFT_EINVAL, "solver_lambda: bad argument");
+    cudaSetDevice(s->ctx->device);
+    const double *ev = nullptr, *eo = nullptr;
+    KV_TRY(solver_energies(s, &ev, &eo));
+    LamSpinScope spin(s->ctx, (s->spin_half > 0 && s->spin_on) ? s->spin_half : 0);
+    const double *F[4] = {s->F[0], s->F[1], s->F[2], s->F[3]};
+    const double *I[9];
+    for (int k = 0; k < 9; k++) I[k] = s->I[k];
+    if (guess)
+        KV_TRY(kvft_lambda_guess(s->ctx, s->ng, s->nv, s->no, F, I, s->T1, s->beta, guess == 2,
+                                 L1, L2));
+    return kvft_lambda_solve(s->ctx, s->ng, s->nv, s->no, F, I, s->T1, s->T2, ev, eo, s->ti,
+                             s->g, s->G, damp, tconv, max_iter, measure_half, L1, L2, hist,
+                             iters);
+}
+
+int kvft_solver_lambda_densities(kvft_solver *s, const double *L1, const double *L2,
+                                 double *const Fg[4], double *const Ig[9]) {
+    if (!s || !L1 || !L2 || !Fg || !Ig)
+        return kv_fail(s ? s->ctx : nullptr, KVFT_EINVAL, "solver_lambda_densities: bad argument");
+    cudaSetDevice(s->ctx->device);
+    const double *ev = nullptr, *eo = nullptr;
+    KV_TRY(solver_energies(s, &ev, &eo));
+    LamSpinScope spin(s->ctx, (s->spin_half > 0 && s->spin_on) ? s->spin_half : 0);
+    const double *F[4] = {s->F[0], s->F[1], s->F[2], s->F[3]};
+    const double *I[9];
+    for (int k = 0; k < 9; k++) I[k] = s->I[k];
+    return kvft_lambda_densities(s->ctx, s->ng, s->nv, s->no, F, I, s->T1, s->T2, L1, L2, ev,
+                                 eo, s->ti, s->g, s->G, Fg, Ig);
+}
+
 int kvft_solver_set_spin_blocks(kvft_solver *s, int on, int *half) {
     if (!s) return KVFT_EINVAL;
     if (on >= 0) s->spin_on = on != 0;

@@ -207,3 +207,31 @@ def test_full_rdms_of_the_reference():
     g2 = cc.full_2rdm()
     assert abs(numpy.einsum('pqpq->', g2) - (f.sum() ** 2 - (f * f).sum())) < 1e-13
     assert abs(g2 + g2.transpose(1, 0, 2, 3)).max() < 1e-15
+
+
+def test_lambda_on_the_resident_solver():
+    """After a solve the Lambda equations run on the solver's resident
+    integrals and amplitudes, with Kelvin's unrestricted guess and measure for
+    a system in the unrestricted form."""
+    from kelvin_gb300 import ft_cc_equations as fe
+    rng = numpy.random.default_rng(10)
+    T, mu, ng, n, na = 0.3, 0.1, 3, 6, 3
+    s = USystem(rng, n, T, mu)
+    Lg = (rng.standard_normal((ng, n, n)), rng.standard_normal((ng,) + (n,) * 4))
+    seen = {}
+
+    class Solver(object):
+        def lambda_solve(self, conv, guess=1, L1=None, L2=None, measure_half=None,
+                         history=None):
+            seen.update(conv=conv, guess=guess, measure_half=measure_half)
+            return Lg
+    cc = ccsd_mod.ccsd(s, T=T, mu=mu, ngrid=ng, ctx=FakeCtx(), damp=0.3, max_iter=17)
+    cc._Tg = (numpy.zeros((ng, n, n)), numpy.zeros((ng,) + (n,) * 4))
+    cc.T1 = "set"
+    cc.solver = Solver()
+    cc._ft_ccsd_lambda()
+    assert seen["guess"] == 2 and seen["measure_half"] == na
+    assert seen["conv"]["damp"] == 0.3 and seen["conv"]["max_iter"] == 17
+    assert cc._Lg is Lg
+    assert numpy.array_equal(cc.L2[1], Lg[1][:, :na, na:, :na, na:])
+    assert cc.ctx._precision == (0, 7)

@@ -124,3 +124,21 @@ def test_lambda_densities_vs_oracle(ctx):
     R1, R2 = ft_lambda.response_densities(F, I, T1, T2, L1, L2, D1, D2, ti, ng, g, G)
     for a, b in zip(tuple(P1) + tuple(P2), R1 + R2):
         assert abs(a - b).max() < 1e-11 * max(1.0, abs(b).max())
+
+
+def test_resident_and_host_lambda_agree(ctx):
+    """Lambda from the solver's resident integrals equals Lambda from
+    integrals rebuilt on the host, and both equal the oracle's."""
+    from kelvin_gb300 import ccsd, systems
+    s = systems.UEGSystem(0.1, 2 * numpy.pi, 1.2, mu=0.1, norb=7)
+    cc = ccsd.ccsd(s, T=0.1, mu=0.1, max_iter=100, damp=0.2, ngrid=8, econv=1e-12,
+                   precision="fp64_tc", ctx=ctx)
+    try:
+        cc.run()
+        a1, a2 = cc._ft_ccsd_lambda()
+        cc.release()
+        b1, b2 = cc._ft_ccsd_lambda()
+    finally:
+        ctx.set_precision(_lib.PREC_FP64, 7)
+    assert abs(a1 - b1).max() < 1e-10 * abs(a1).max()
+    assert abs(a2 - b2).max() < 1e-10 * abs(a2).max()

@@ -439,3 +439,30 @@ def test_lambda_solve_dry_run_vs_oracle(spin, blocks):
         res = sum(numpy.sqrt(x) / (nl[0] if r else nl[1]) for x, r in zip(blk[:nb], rank1))
         assert abs(res - hist[it]) < 1e-12 * hist[it]
         nl = normalisers(blk[nb:])
+
+
+@pytest.mark.parametrize("unrestricted", [0, 1])
+def test_lambda_guess_dry_run_vs_oracle(unrestricted):
+    no, nv, ng, beta = 3, 4, 3, 2.0
+    rng = numpy.random.default_rng(4 + unrestricted)
+    F, I = random_system(rng, no, nv)
+    T1 = rng.standard_normal((ng, nv, no)) * 0.1
+    L1 = numpy.full((ng, no, nv), numpy.nan)
+    L2 = numpy.full((ng, no, no, nv, nv), numpy.nan)
+    Fb = [numpy.ascontiguousarray(getattr(F, k)) for k in F_ORDER]
+    Ib = [numpy.ascontiguousarray(getattr(I, k)) for k in I_ORDER]
+    Lib = _L()
+    ctx = ctypes.c_void_p()
+    assert Lib.kvft_dryrun_create(0, 7, ctypes.byref(ctx)) == 0
+    try:
+        P = lambda arrs: (ctypes.c_void_p * len(arrs))(*[a.ctypes.data for a in arrs])
+        assert Lib.kvft_lambda_guess(ctx, ng, nv, no, P(Fb), P(Ib), T1.ctypes.data, beta,
+                                     unrestricted, L1.ctypes.data, L2.ctypes.data) == 0
+        mem = _Memory()
+        for a in Fb + Ib + [T1, L1, L2]:
+            mem.add(a)
+        _replay(ctx, mem)
+    finally:
+        Lib.kvft_ctx_destroy(ctx)
+    r1, r2 = ft_lambda.lambda_guess(F, I, T1, beta, ng, unrestricted=bool(unrestricted))
+    assert abs(L1 - r1).max() < 1e-14 and abs(L2 - r2).max() < 1e-15
