@@ -466,3 +466,53 @@ def test_lambda_guess_dry_run_vs_oracle(unrestricted):
         Lib.kvft_ctx_destroy(ctx)
     r1, r2 = ft_lambda.lambda_guess(F, I, T1, beta, ng, unrestricted=bool(unrestricted))
     assert abs(L1 - r1).max() < 1e-14 and abs(L2 - r2).max() < 1e-15
+
+
+def test_lambda_densities_spin_blocked_dry_run_vs_oracle():
+    """kvft_lambda_densities over spin-block products on a spin-blocked UEG
+    (T and Lambda from the oracle's solves) against the oracle's densities."""
+    from oracle import ft_ccsd as oft, ft_utils, quadrature, systems
+    b = systems.UEGBasis(2 * numpy.pi, 1.2, norb=3)
+    eri = systems.g2e_loop(b)
+    en = systems.ueg_g_energies(b)
+    n, h, ng, T, mu = en.shape[0], en.shape[0] // 2, 4, 0.1, 0.1
+    E, S, N, Om, T1, T2, L1, L2 = ft_lambda.solve(en, numpy.diag(numpy.hstack((b.Es, b.Es))),
+                                                  eri, T, mu, ngrid=ng, damp=0.2,
+                                                  econv=1e-11, lconv=1e-10, max_iter=100)
+    beta = 1.0 / T
+    fock = systems.g_fock_tot(b, eri, en, T, mu)
+    F, I = oft.ft_integrals(fock, eri, en, beta, mu)
+    ti, g, G = quadrature.ft_quad(ng, beta, 'lin')
+    D1, D2 = ft_utils.D1(en, en), ft_utils.D2(en, en)
+    Fb = [numpy.ascontiguousarray(getattr(F, k)) for k in F_ORDER]
+    Ib = [numpy.ascontiguousarray(getattr(I, k)) for k in I_ORDER]
+    Fg = [numpy.full(a.shape, numpy.nan) for a in Fb]
+    Ig = [numpy.full(a.shape, numpy.nan) for a in Ib]
+    arrs = [numpy.ascontiguousarray(x) for x in (T1, T2, L1, L2, en, ti, g, G)]
+    Lib = _L()
+    ctx = ctypes.c_void_p()
+    assert Lib.kvft_dryrun_create(0, 7, ctypes.byref(ctx)) == 0
+    try:
+        assert Lib.kvft_set_lambda_spin_blocks(ctx, h) == 0
+        P = lambda a: (ctypes.c_void_p * len(a))(*[x.ctypes.data for x in a])
+        d = [a.ctypes.data for a in arrs]
+        assert Lib.kvft_lambda_densities(ctx, ng, n, n, P(Fb), P(Ib), d[0], d[1], d[2], d[3],
+                                         d[4], d[4], d[5], d[6], d[7], P(Fg), P(Ig)) == 0
+        mem = _Memory()
+        for a in Fb + Ib + Fg + Ig + arrs:
+            mem.add(a)
+        i = 0
+        ptr, nbytes = ctypes.c_void_p(), ctypes.c_size_t()
+        while Lib.kvft_dryrun_scratch(ctx, i, ctypes.byref(ptr), ctypes.byref(nbytes)) == 0:
+            mem.add_raw(ptr.value, nbytes.value)
+            i += 1
+        assert 3 in _replay(ctx, mem)
+    finally:
+        Lib.kvft_ctx_destroy(ctx)
+    R1, R2 = ft_lambda.response_densities(F, I, T1, T2, L1, L2, D1, D2, ti, ng, g, G)
+    Foo, Fov, Fvo, Fvv = Fg
+    for mine, ref in zip((Fvo.T, Fvv.T, Foo.T, Fov.T), R1):
+        assert abs(mine - ref).max() < 1e-12 * max(1.0, abs(ref).max())
+    for (name, blk, w, pairs), ref in zip(ft_lambda.P2_BLOCKS, R2):
+        mine = ft_lambda._asym(Ig[I_ORDER.index(blk)].transpose(2, 3, 0, 1) / w, pairs)
+        assert abs(mine - ref).max() < 1e-12 * max(1.0, abs(ref).max()), name
