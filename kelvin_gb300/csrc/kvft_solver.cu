@@ -698,6 +698,15 @@ int solver_energies(kvft_solver *s, const double **ev, const double **eo) {
                                 cudaMemcpyDeviceToHost));
     for (int a = 0; a < nv; a++) h[a] = d1[(size_t)a * no];
     for (int i = 0; i < no; i++) h[nv + i] = d1[0] - d1[i];
+    // the backward integral needs D1 of that form (a block-diagonal D1 with
+    // zeros between spin cases is not)
+    for (int a = 0; a < nv; a++)
+        for (int i = 0; i < no; i++) {
+            const double d = d1[(size_t)a * no + i], r = h[a] - h[nv + i];
+            if (std::fabs(d - r) > 1e-12 * (1.0 + std::fabs(d)))
+                return kv_fail(s->ctx, KVFT_EINVAL,
+                               "solver_lambda: D1 is not a difference of orbital energies");
+        }
     void *p = nullptr;
     KV_TRY(kv_scratch(s->ctx, "solver_energies", sizeof(double) * h.size(), &p));
     KV_CHECK(s->ctx, cudaMemcpy(p, h.data(), sizeof(double) * h.size(), cudaMemcpyHostToDevice));
