@@ -210,8 +210,10 @@ def energies_from_d1(D1):
     """Orbital energies (ev, eo) with ev[a] - eo[i] = D1[a, i]; the
     exponentials of the integrals depend on these differences only."""
     D1 = numpy.asarray(D1, dtype=float)
-    return (numpy.ascontiguousarray(D1[:, 0]),
-            numpy.ascontiguousarray(D1[0, 0] - D1[0, :]))
+    ev, eo = D1[:, 0].copy(), D1[0, 0] - D1[0, :]
+    if abs(ev[:, None] - eo[None, :] - D1).max() > 1e-12 * (1.0 + abs(D1).max()):
+        raise Exception("D1 is not a difference of orbital energies")
+    return numpy.ascontiguousarray(ev), numpy.ascontiguousarray(eo)
 
 
 def spin_half_of(nv, no, arrays):

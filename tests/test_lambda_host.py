@@ -34,6 +34,10 @@ def test_energies_from_d1():
     D1 = ev[:, None] - eo[None, :]
     a, b = fe.energies_from_d1(D1)
     assert abs((a[:, None] - b[None, :]) - D1).max() < 1e-15
+    bad = D1.copy()
+    bad[1, 1] += 1.0
+    with pytest.raises(Exception):
+        fe.energies_from_d1(bad)
 
 
 def test_lambda_guess_and_loop_match_oracle(solved):
