@@ -142,3 +142,34 @@ def test_resident_and_host_lambda_agree(ctx):
         ctx.set_precision(_lib.PREC_FP64, 7)
     assert abs(a1 - b1).max() < 1e-10 * abs(a1).max()
     assert abs(a2 - b2).max() < 1e-10 * abs(a2).max()
+
+
+@pytest.mark.parametrize("spin_half", [None, 3])
+def test_lambda_iteration_vs_oracle(ctx, spin_half):
+    """ft_lambda_iter resident on the device (kvft_lambda_solve, with the
+    spin-blocked contractions this system allows) against the oracle's loop:
+    the residual history and the converged Lambda."""
+    from kelvin_gb300 import cc_utils
+    from oracle import ft_ccsd as oft, ft_utils, systems
+    b = systems.UEGBasis(2 * numpy.pi, 1.2, norb=3)
+    eri = systems.g2e_loop(b)
+    en = systems.ueg_g_energies(b)
+    T, mu, ng, beta = 0.1, 0.1, 5, 10.0
+    fock = systems.g_fock_tot(b, eri, en, T, mu)
+    F, I = oft.ft_integrals(fock, eri, en, beta, mu)
+    ti, g, G = quadrature.ft_quad(ng, beta, 'lin')
+    D1, D2 = ft_utils.D1(en, en), ft_utils.D2(en, en)
+    _, T1, T2 = oft.ft_ccsd(en, fock, eri, T, mu, ngrid=ng, damp=0.2, max_iter=60,
+                            econv=1e-11, return_amplitudes=True)
+    L1, L2 = ft_lambda.lambda_guess(F, I, T1, beta, ng, unrestricted=spin_half is not None)
+    conv = {"tconv": 1e-9, "max_iter": 60, "damp": 0.2}
+    ref, mine = [], []
+    R1, R2 = ft_lambda.ft_lambda_iter(L1.copy(), L2.copy(), T1, T2, F, I, D1, D2, g, G, beta,
+                                      ng, ti, conv, history=ref, spin_half=spin_half)
+    ctx.set_precision(_lib.PREC_FP64, 7)
+    M1, M2 = cc_utils.ft_lambda_iter("CCSD", L1, L2, T1, T2, F, I, D1, D2, g, G, beta, ng, ti,
+                                     0, conv, ctx=ctx, history=mine, spin_half=spin_half)
+    assert len(mine) == len(ref)
+    assert max(abs(a - b) / b for a, b in zip(mine, ref)) < 1e-9
+    assert abs(M1 - R1).max() < 1e-10 * abs(R1).max()
+    assert abs(M2 - R2).max() < 1e-10 * abs(R2).max()
