@@ -127,7 +127,9 @@ int kvft_ft_cc_energy(kvft_ctx *ctx, int ng, int nv, int no, const double *T1,
  * of the current device), with no context and no allocation.  Scratch is a
  * fixed 256 KiB static device array held by every GPU that loads the library
  * until exit.  The first call on a device looks up that array's address (do it
- * before any stream capture).  Calls share the array: calls that overlap on
+ * before any stream capture) and keeps it for the life of the process: after a
+ * cudaDeviceReset that address is stale, so do not call this entry point on a
+ * device that has been reset.  Calls share the array: calls that overlap on
  * the GPU race.  Limit: ceil(no*no/32) * ceil(nv*nv/32) <= 32767 tiles (up
  * to nv = no = 76); larger problems return KVFT_EINVAL without launching. */
 int kvft_ft_cc_energy_noalloc(void *stream, int ng, int nv, int no,

@@ -246,10 +246,23 @@ extern "C" int kvft_ft_cc_energy_noalloc(void *stream, int ng, int nv, int no,
     }
     cudaStream_t st = (cudaStream_t)stream;
     const int nblk = (int)(gx * gy);
-    energy2_kernel<<<dim3((unsigned)gx, (unsigned)gy), 256, 0, st>>>(ng, nv, no, T1, T2, eri, g,
-                                                                      qterm, 0, scratch);
-    energy1_kernel<<<1, 256, 0, st>>>(ng, nv, no, T1, f, g, scratch + nblk);
-    energy_final_kernel<<<1, 256, 0, st>>>(scratch, nblk, scratch + nblk, 1.0 / beta,
-                                           omega_dev);
-    return cudaGetLastError() == cudaSuccess ? KVFT_OK : KVFT_EDEVICE;
+    // each launch's own status (cudaLaunchKernel reports that launch), so
+    // that an earlier unrelated error left on the thread is not returned as
+    // this call's
+    int sh = 0;
+    double *part1 = scratch + nblk;
+    double inv_beta = 1.0 / beta;
+    void *a2[] = {&ng, &nv, &no, (void *)&T1, (void *)&T2, (void *)&eri, (void *)&g, &qterm,
+                  &sh, &scratch};
+    void *a1[] = {&ng, &nv, &no, (void *)&T1, (void *)&f, (void *)&g, &part1};
+    int nb = nblk;
+    void *af[] = {&scratch, &nb, &part1, &inv_beta, &omega_dev};
+    if (cudaLaunchKernel((const void *)energy2_kernel, dim3((unsigned)gx, (unsigned)gy),
+                         dim3(256), a2, 0, st) != cudaSuccess ||
+        cudaLaunchKernel((const void *)energy1_kernel, dim3(1), dim3(256), a1, 0, st) !=
+            cudaSuccess ||
+        cudaLaunchKernel((const void *)energy_final_kernel, dim3(1), dim3(256), af, 0, st) !=
+            cudaSuccess)
+        return KVFT_EDEVICE;
+    return KVFT_OK;
 }

@@ -901,7 +901,7 @@ extern "C" int kvft_lambda_solve(kvft_ctx *ctx, int ng, int nv, int no,
             res += std::sqrt(hw[k]) / (blks[k].rank == 1 ? nl1 : nl2);
         normalisers(hw + nb, &nl1, &nl2);
         if (hist) hist[it] = res;
-        if (!ctx->dry && !(res == res)) {
+        if (!ctx->dry && !std::isfinite(res)) {
             *iters = it + 1;
             return kv_fail(ctx, KVFT_EDIVERGE, "lambda iteration: non-finite residual");
         }

@@ -699,11 +699,15 @@ int solver_energies(kvft_solver *s, const double **ev, const double **eo) {
     for (int a = 0; a < nv; a++) h[a] = d1[(size_t)a * no];
     for (int i = 0; i < no; i++) h[nv + i] = d1[0] - d1[i];
     // the backward integral needs D1 of that form (a block-diagonal D1 with
-    // zeros between spin cases is not)
+    // zeros between spin cases is not).  The rebuilt h[a] - h[nv+i] carries
+    // rounding of the size of the largest |D1|, so the bar is relative to
+    // that maximum, not to the element (the test of energies_from_d1)
+    double dmax = 0.0;
+    for (double d : d1) dmax = std::max(dmax, std::fabs(d));
     for (int a = 0; a < nv; a++)
         for (int i = 0; i < no; i++) {
             const double d = d1[(size_t)a * no + i], r = h[a] - h[nv + i];
-            if (std::fabs(d - r) > 1e-12 * (1.0 + std::fabs(d)))
+            if (std::fabs(d - r) > 1e-12 * (1.0 + dmax))
                 return kv_fail(s->ctx, KVFT_EINVAL,
                                "solver_lambda: D1 is not a difference of orbital energies");
         }

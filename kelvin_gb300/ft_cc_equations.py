@@ -7,6 +7,8 @@ residual with Stanton-Gauss intermediates gives tbar = -F.vo - R1(t),
 never modified; new arrays are returned.  numpy inputs give numpy outputs;
 ``DeviceArray`` amplitudes give device outputs.
 """
+import zlib
+
 import numpy
 
 from . import _lib
@@ -30,15 +32,31 @@ class DeviceBlocks(object):
 _cache = {}
 
 
+def _fingerprint(F, I):
+    """Content key of the host blocks of (F, I): shape and a CRC of the bytes
+    of every block, so that a block changed in place is uploaded again.  Device blocks are used where they lie and need no key beyond
+    their address."""
+    key = []
+    for c, order in ((F, F_ORDER), (I, I_ORDER)):
+        for b in order:
+            a = getattr(c, b)
+            if isinstance(a, _lib.DeviceArray):
+                key.append(("d", a.ptr.value))
+                continue
+            a = numpy.ascontiguousarray(a, dtype=float)
+            key.append((a.shape, zlib.crc32(memoryview(a).cast("B"))))
+    return tuple(key)
+
+
 def device_blocks(ctx, F, I):
-    """Device blocks for (F, I), reused while the same objects are passed."""
-    key = (id(F), id(I), ctx.device)
+    """Device blocks for (F, I), reused while the same contents are passed."""
+    key = (ctx.device, _fingerprint(F, I))
     hit = _cache.get(key)
-    if hit is not None and hit[0] is F and hit[1] is I:
-        return hit[2]
+    if hit is not None:
+        return hit
     blk = DeviceBlocks(ctx, F, I)
     _cache.clear()
-    _cache[key] = (F, I, blk)
+    _cache[key] = blk
     return blk
 
 

@@ -1,8 +1,8 @@
 """Generate the golden fixtures in this folder by running Kelvin's own code.
 
-Usage (needs the read-only Kelvin checkout; never run on the GPU host):
+Usage (needs a read-only Kelvin checkout; never run on the GPU host):
 
-    python tests/golden/make_golden.py /root/reference
+    python tests/golden/make_golden.py <path of the Kelvin checkout>
 
 Kelvin's modules are imported unmodified; its absent dependencies are
 replaced by ``kelvin_stubs`` (numpy einsum for pyscf, the oracle's

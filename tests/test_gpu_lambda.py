@@ -1,7 +1,6 @@
 """The device Lambda path on a GPU, against the oracle and Kelvin's published
 Lambda run.  Its launch descriptors are checked on the CPU by dry-run replay
-(test_lambda_dryrun.py); these tests run the kernels themselves.  They are
-opt-in (KVFT_GPU_LAMBDA=1) until their first run on a GB300."""
+(test_lambda_dryrun.py); these tests run the kernels themselves."""
 import os
 
 import numpy
@@ -11,9 +10,7 @@ from conftest import random_system
 from kelvin_gb300 import _lib
 from oracle import ft_lambda, quadrature
 
-pytestmark = [pytest.mark.gpu,
-              pytest.mark.skipif(not os.environ.get("KVFT_GPU_LAMBDA"),
-                                 reason="first GB300 run pending: set KVFT_GPU_LAMBDA=1")]
+pytestmark = pytest.mark.gpu
 
 F_ORDER = ("oo", "ov", "vo", "vv")
 I_ORDER = ("vvvv", "vvvo", "vovv", "vvoo", "vovo", "oovv", "vooo", "ooov", "oooo")
@@ -170,6 +167,9 @@ def test_lambda_iteration_vs_oracle(ctx, spin_half):
     M1, M2 = cc_utils.ft_lambda_iter("CCSD", L1, L2, T1, T2, F, I, D1, D2, g, G, beta, ng, ti,
                                      0, conv, ctx=ctx, history=mine, spin_half=spin_half)
     assert len(mine) == len(ref)
-    assert max(abs(a - b) / b for a, b in zip(mine, ref)) < 1e-9
+    # res = |L - L_old| / (|L_old| + 0.1): near convergence it is a difference
+    # of nearly equal iterates, so rounding of the contractions (~1e-16 of
+    # |L|) is amplified in relative terms; the bar is relative plus that floor
+    assert max(abs(a - b) - 1e-9 * b for a, b in zip(mine, ref)) < 1e-14
     assert abs(M1 - R1).max() < 1e-10 * abs(R1).max()
     assert abs(M2 - R2).max() < 1e-10 * abs(R2).max()

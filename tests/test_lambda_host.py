@@ -38,6 +38,15 @@ def test_energies_from_d1():
     bad[1, 1] += 1.0
     with pytest.raises(Exception):
         fe.energies_from_d1(bad)
+    # large orbital energies: an element near zero carries the rounding of
+    # the large ones, and D1 must still be accepted (the bar is relative to
+    # max |D1|, as in the solver's own check)
+    ev = 1e4 + rng.standard_normal(6)
+    eo = 1e4 + rng.standard_normal(4)
+    eo[0] = ev[2] - 1e-13
+    D1 = ev[:, None] - eo[None, :]
+    a, b = fe.energies_from_d1(D1)
+    assert abs((a[:, None] - b[None, :]) - D1).max() < 1e-11
 
 
 def test_lambda_guess_and_loop_match_oracle(solved):
