@@ -3,6 +3,7 @@
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl kvft|reference]
                     [--workload ueg114|ueg38] [--precision mixed|fp64_tc|fp64]
+                    [--quad gl|lin]
     python bench.py --gemm M,N,K,batch [--precision ...]      # one contraction shape
     python bench.py --system-build [--workload ...]
         # time building the model system's integrals: dense n^4 on the host
@@ -11,25 +12,43 @@
         # one warm-up iteration, then one iteration; prints the library's
         # kernel-launch counts so that a profiler's launch list can be cut to
         # exactly the second iteration
+    python bench.py --accuracy
+        # mixed against FP64-accurate on the smaller configurations: the
+        # 38-spin-orbital UEG (Simpson and Gauss-Legendre grids), the 16-site
+        # Hubbard ring at beta 1, 4, 10 and the 66-spin-orbital UEG:
+        # |dOmega|, |dE|, |dS|
 
 Workloads are seeded synthetic uniform electron gases (the benchmark configs):
 
 * ueg114 (default): 38 electrons, rs = 1, the 57 lowest plane waves (114 spin
-  orbitals), Theta = 0.25, ng = 20, damping 0.5, econv 1e-10.  A full solve
-  takes minutes, so a step is ONE amplitude iteration (CCSD update of all tau
-  points + integration + damping + norms + energy) and
-  solves/s = iterations/s / iterations_per_solve.
+  orbitals), Theta = 0.25, ng = 20 Gauss-Legendre points, damping 0.5, econv
+  1e-10.  A solve takes seconds, so a timed step is ONE amplitude iteration
+  (CCSD update of all tau points + integration + damping + norms + energy)
+  and solves/s = 1 / sum over the solve's phases of (iterations x seconds per
+  iteration at that phase's digit levels), the iteration counts taken from a
+  complete solve in the same run.
 * ueg38: 14 electrons, rs = 4, 19 plane waves (38 spin orbitals), Theta = 0.5,
   ng = 10: a step is a complete solve (first-order guess to convergence).
 
-``value`` times K steps with the integrals and buffers already resident in HBM;
-``e2e`` times the same through the public drop-in API
+``value`` times the steps with the integrals and buffers already resident in
+HBM; ``e2e`` times complete solves through the public drop-in API
 (``kelvin_gb300.ccsd.ccsd(sys, ...).run()``) from host arrays, including the
 host->device upload of the integrals and the read-back of the amplitudes.
-The headline precision is 'mixed' (three BF16 digit levels on tensor cores;
-FP64 quadrature, damping and energy); one FP64-accurate step is timed beside
-it.  With N > 1 (torchrun) every rank runs an independent replica: only the
-timings are reduced (gloo).  One JSON line is printed by rank 0.
+The headline precision is 'mixed': three BF16 digit levels on tensor cores
+until the iteration's noise floor, five levels to theirs, then FP64-accurate
+(seven-level) sweeps until Kelvin's convergence test passes; quadrature,
+damping and energy are FP64 throughout.  Beside it the same run measures the
+FP64-accurate solve (|dOmega| of the mixed solve against it) and one
+iteration of the plain FP64 path (FP64 FMA contractions).  With N > 1
+(torchrun) every rank runs an independent replica: only the timings are
+reduced (gloo).  One JSON line is printed by rank 0.
+
+The reference arm (--impl reference) runs the oracle -- the numpy FP64
+restatement of Kelvin's iteration (ccsd_stanton at every tau point,
+int_tbar, damping, ft_cc_energy) -- on the host cores: a complete solve of the
+38-spin-orbital configuration, its iterations timed one by one.  A solve of
+the 114-spin-orbital configuration needs tens of minutes per iteration on the
+host, so its rate appears only as a labelled estimate.
 """
 import argparse
 import json
@@ -46,44 +65,21 @@ sys.path.insert(0, ROOT)
 METRIC = "FT-CCSD solves/s"
 UNIT = "solves/s"
 
-# iters: amplitude iterations of the converged solve (guess 1), by precision;
-# for 'mixed' the few-digit iterations before the REFINE refinement sweeps.
-# ueg114 was measured by full solves on a GB300 (kelvin_gb300.ccsd.ccsd(...).run()):
-# mixed 27 + 2 sweeps, Omega_cc -0.9542852803 (12.8 s); 7 levels 30, -0.9542857194.
 WORKLOADS = {
     "ueg114": dict(N=38, rs=1.0, norb=57, theta=0.25, ng=20, damp=0.5, econv=1e-10,
-                   max_iter=100, iters={"mixed": 27, "fp64_tc": 30, "fp64": 30},
-                   step="iteration",
+                   max_iter=100, step="iteration",
                    label="UEG 38 e-, rs=1, 57 plane waves (114 spin orbitals), Theta=0.25, "
                          "ng=20, damping 0.5, econv 1e-10"),
     "ueg38": dict(N=14, rs=4.0, norb=19, theta=0.5, ng=10, damp=0.5, econv=1e-10,
-                  max_iter=100, iters=30, step="solve",
+                  max_iter=100, step="solve",
                   label="UEG 14 e-, rs=4, 19 plane waves (38 spin orbitals), Theta=0.5, "
                         "ng=10, damping 0.5, econv 1e-10"),
 }
-ITERS_FALLBACK = 30
-# DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of
-# the contraction classes, mean over those launches of one ueg114 iteration,
-# from the ncu launch lists of `python bench.py --profile-step [--precision
-# fp64_tc]` (one replay pass per launch, so the full-size workload was
-# captured).  A measured input of the roofline, not computed here: re-take
-# it when the kernels change.
-NCU_TRAFFIC = {
-    ("ueg114", "mixed", "gemm6"): 2.4163e9, ("ueg114", "mixed", "gemm"): 1.5885e9,
-    ("ueg114", "mixed", "elem"): 4.0275e9,
-    ("ueg114", "fp64_tc", "gemm6"): 5.0731e9, ("ueg114", "fp64_tc", "gemm"): 1.8195e9,
-    ("ueg114", "fp64_tc", "elem"): 3.1879e9,
-}
-REFINE = 2          # refinement sweeps that end a mixed solve
-REFINE_DIGITS = 5   # their digit levels
+# per-launch DRAM traffic of the dominant kernel category, measured by ncu
+# on a small case and scaled to this workload: see profiles/ (read at run time
+# from the committed summary, so that a re-taken capture updates it)
+TRAFFIC_FILE = os.path.join(ROOT, "profiles", "traffic.json")
 STEP_EVENTS = 8     # first event slot of the per-step timings (at most 50 steps)
-
-
-def iters_of(w, precision):
-    it = w["iters"]
-    if isinstance(it, dict):
-        return it.get(precision, ITERS_FALLBACK)
-    return it or ITERS_FALLBACK
 
 
 def load_peaks():
@@ -180,78 +176,112 @@ def max_over_ranks(ws, x):
 
 
 # ---------------------------------------------------------------------------
-# CPU reference: the oracle (numpy FP64 port of Kelvin's path) on host cores
+# CPU reference: the oracle (numpy FP64 restatement of Kelvin's path) on the
+# host cores
 # ---------------------------------------------------------------------------
-def cpu_iteration_seconds(w, sysobj):
-    """(seconds per amplitude iteration of the numpy FP64 path, sample text).
-
-    n <= 40: one full iteration (ccsd_stanton over all tau points, int_tbar,
-    damping, ft_cc_energy).  Larger n (a numpy iteration is many minutes):
-    the W_abef ladder contraction of one tau point (2 n^6 flops, Kelvin's
-    einsum 'efij,abef->abij'), scaled by the iteration's 10 n^6 ng flops."""
+def oracle_c1_iterations(quad, max_iters, until_converged):
+    """The oracle's FT-CCSD loop (Kelvin's ccsd_stanton over all tau points,
+    int_tbar, damping, residual norms, ft_cc_energy; cc_utils.py:111-173)
+    on the 38-spin-orbital configuration, each iteration timed.  Stops after
+    `max_iters` iterations or, with until_converged, at Kelvin's test if that
+    comes later.  Returns (seconds of the first-order guess, per-iteration
+    seconds, the iteration at which Kelvin's test passed or None, Omega_cc)."""
     import numpy
     from oracle import ft_ccsd, ft_utils, quadrature
+    w = WORKLOADS["ueg38"]
+    sysobj = build_system(w)
     beta = 1.0 / sysobj.T
     en = sysobj.g_energies_tot()
-    n, ng = en.shape[0], w["ng"]
-    threads = os.cpu_count()
-    if n <= 40:
-        ti, g, G = quadrature.ft_quad(ng, beta, "lin")
-        F, I = ft_ccsd.ft_integrals(sysobj.g_fock_tot(), sysobj.g_aint_tot(), en, beta,
-                                    sysobj.mu)
-        D1, D2 = ft_utils.D1(en, en), ft_utils.D2(en, en)
-        T1 = numpy.zeros((ng, n, n))
-        T2 = numpy.zeros((ng, n, n, n, n))
-        t0 = time.perf_counter()
-        T1n, T2n = ft_ccsd.ccsd_stanton(F, I, T1, T2, D1, D2, ti, ng, G)
-        T1 = w["damp"] * T1 + (1 - w["damp"]) * T1n
-        T2 = w["damp"] * T2 + (1 - w["damp"]) * T2n
-        ft_ccsd.ft_cc_energy(T1, T2, F.ov, I.oovv, g, beta)
-        dt = time.perf_counter() - t0
-        return dt, "1 full amplitude iteration (numpy FP64 oracle port, %d threads, %.2f s)" % (
-            threads, dt)
-    rng = numpy.random.default_rng(0)
-    W = rng.standard_normal((n * n, n * n))
-    tau = rng.standard_normal((n * n, n * n))
+    ng, alpha = w["ng"], w["damp"]
+    full = quad == "gl"
+    ti, g, G = quadrature.ft_quad(ng, beta, quad)
+    F, I = ft_ccsd.ft_integrals(sysobj.g_fock_tot(), sysobj.g_aint_tot(), en, beta, sysobj.mu)
+    D1, D2 = ft_utils.D1(en, en), ft_utils.D2(en, en)
     t0 = time.perf_counter()
-    W @ tau
-    dt = time.perf_counter() - t0
-    it = dt * 5.0 * ng
-    return it, ("one n^6 contraction of the iteration (W_abef ladder of one tau point, "
-                "%d^2 x %d^2 x %d^2 FP64 BLAS via numpy, %d threads, %.2f s) scaled by "
-                "10 n^6 ng / 2 n^6 = %d (n^5 terms and quadrature not counted: a lower "
-                "bound on the CPU time)" % (n, n, n, threads, dt, 5 * ng))
+    T1 = quadrature.int_tbar1(ng, numpy.repeat(-F.vo[None], ng, 0), ti, D1, G, full=full)
+    T2 = quadrature.int_tbar2(ng, numpy.repeat(-I.vvoo[None], ng, 0), ti, D2, G, full=full)
+    t_guess = time.perf_counter() - t0
+    nl1, nl2 = numpy.linalg.norm(T1) + 0.1, numpy.linalg.norm(T2) + 0.1
+    Eold, times, conv_at, i = 888888888.888888888, [], None, 0
+    while True:
+        t0 = time.perf_counter()
+        T1n, T2n = ft_ccsd.ccsd_stanton(F, I, T1, T2, D1, D2, ti, ng, G, full=full)
+        res = (numpy.linalg.norm(T1n - T1) / nl1 + numpy.linalg.norm(T2n - T2) / nl2)
+        T1 = alpha * T1 + (1.0 - alpha) * T1n
+        T2 = alpha * T2 + (1.0 - alpha) * T2n
+        nl1, nl2 = numpy.linalg.norm(T1) + 0.1, numpy.linalg.norm(T2) + 0.1
+        E = ft_ccsd.ft_cc_energy(T1, T2, F.ov, I.oovv, g, beta)
+        times.append(time.perf_counter() - t0)
+        i += 1
+        if conv_at is None and abs(E - Eold) < w["econv"] and res < 1e3 * w["econv"]:
+            conv_at = i
+        Eold = E
+        if i >= max_iters and (conv_at is not None or not until_converged):
+            break
+        if i >= 200:
+            break
+    return t_guess, times, conv_at, E
+
+
+def c2_estimate(t_iter_c1, iters):
+    """solves/s of the 114-spin-orbital configuration ESTIMATED from a
+    38-spin-orbital iteration: contraction work scales as n^6 ng, so
+    t_114 = t_38 (114/38)^6 (20/10)."""
+    t = t_iter_c1 * (114.0 / 38.0) ** 6 * 2.0
+    return {"value": 1.0 / (t * iters), "unit": UNIT, "seconds_per_iteration": t,
+            "iterations": iters,
+            "how": "ESTIMATE, not measured: the measured 38-spin-orbital oracle iteration "
+                   "scaled by the contraction work n^6 ng to 114 spin orbitals, ng = 20, "
+                   "times the iteration count of the FP64 solve"}
 
 
 def run_reference(args, w):
     ws, rank, _ = dist_setup()
     if rank != 0:
         return 0
-    sysobj = build_system(w)
-    iters = iters_of(w, "fp64")                           # the reference is FP64
-    cpu_iteration_seconds(w, sysobj)                      # warm-up sample
-    times, sample = [], ""
-    for _ in range(args.steps):
-        t, sample = cpu_iteration_seconds(w, sysobj)
-        times.append(t)
-    t_iter = statistics.median(times)
-    value = 1.0 / (t_iter * iters)
+    threads = os.cpu_count()
+    t_guess, times, conv_at, E = oracle_c1_iterations(args.quad, args.warmup + args.steps,
+                                                      until_converged=True)
+    timed = times[args.warmup:args.warmup + args.steps]
+    t_iter = statistics.median(timed)
+    iters = conv_at or len(times)
+    t_solve = t_guess + sum(times[:iters])
+    value = 1.0 / t_solve
+    wl = WORKLOADS["ueg38"]
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": t_iter * 1e3 * (iters if w["step"] == "solve" else 1),
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic",
-            "config": {"workload": w["label"], "step": w["step"],
-                       "iterations_per_solve": iters,
-                       "impl": "oracle numpy FP64 port of Kelvin's path (Kelvin is pure "
-                               "Python and cannot run on the GPU host)"},
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": os.cpu_count(),
-                             "kind": "port", "sample": "%d x %s; solves/s = 1 / (median "
-                             "s/iteration x %d iterations)" % (args.steps, sample, iters)},
+            "ms_per_step": t_iter * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": wl["label"] + " (%s tau grid)" % args.quad,
+                       "step": "one amplitude iteration of the oracle's complete solve",
+                       "iterations_per_solve": iters, "converged": conv_at is not None,
+                       "omega_cc": E, "guess_s": t_guess, "solve_s": t_solve,
+                       "impl": "oracle: numpy FP64 restatement of Kelvin's FT-CCSD iteration "
+                               "(Kelvin is pure Python with an un-vendored dependency and "
+                               "cannot run on the GPU host); BLAS threads = all host cores",
+                       "note": "value = 1 / measured wall time of the complete 38-spin-"
+                               "orbital solve; the 114-spin-orbital rate is only estimated"},
+            "estimate_ueg114": c2_estimate(t_iter, iters),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": "complete oracle solve of the 38-spin-orbital UEG "
+                                       "(%d iterations, %.1f s)" % (iters, t_solve)},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
     return 0
+
+
+def load_traffic(workload, precision, category):
+    """Per-launch DRAM bytes of a kernel category from the committed ncu
+    summary (small-case capture scaled to the workload), or None."""
+    try:
+        t = json.load(open(TRAFFIC_FILE))
+    except (OSError, ValueError):
+        return None, None
+    e = t.get(workload, {}).get(precision, {}).get(category)
+    if not e:
+        return None, None
+    return e.get("bytes_per_launch"), e.get("how")
 
 
 # ---------------------------------------------------------------------------
@@ -271,22 +301,23 @@ def run_gpu(args, w):
     beta = 1.0 / sysobj.T
     en = sysobj.g_energies_tot()
     fock, eri = sysobj.g_fock_tot(), sysobj.g_aint_tot()
-    ti, g, G = ft_quad(w["ng"], beta, "lin")
+    full = args.quad == "gl"
+    ti, g, G = ft_quad(w["ng"], beta, args.quad)
     conv = {"econv": w["econv"], "tconv": 1000.0 * w["econv"], "max_iter": w["max_iter"],
             "damp": w["damp"]}
     n, ng = en.shape[0], w["ng"]
     per_solve = w["step"] == "solve"
-    iters = iters_of(w, args.precision)
+    mixed = args.precision == "mixed"
 
     ctx.set_precision(prec, digits)
     solver = DeviceSolver.from_system(ctx, en, fock, eri, beta, sysobj.mu, ti, g, G)
+    solver.full = full
     solver.guess(1)
 
     def one_step():
         if per_solve:
             solver.guess(1)
-            E, info = ccsd.converge(solver, ctx, conv, args.precision, digits, REFINE,
-                                    REFINE_DIGITS)
+            E, info = ccsd.converge(solver, ctx, conv, args.precision, digits)
             return E, info["iterations"] + info["iterations_refine"]
         return solver.step(w["damp"])[0], 1
 
@@ -315,55 +346,76 @@ def run_gpu(args, w):
                  for k in range(min(args.steps, 50))) if args.steps <= 50 else []
     clk = clocks.stop()
     step_ms = ms / args.steps
-    value = ws / (step_ms / 1e3) / (1 if per_solve else iters)
-    if per_solve:
-        iters = results[-1][1]
 
-    # an FP64-accurate (7-level) step beside the headline precision, and for a
-    # per-iteration workload the refinement sweep that ends a mixed solve
-    fp64_step_ms = refine_step_ms = None
-    if args.precision == "mixed":
-        def timed_step(levels):
-            ctx.set_precision(_lib.PREC_FP64_TC, levels)
-            one_step()                                   # warm-up at this precision
-            ctx.sync()
-            ctx.record(4)
-            one_step()
-            ctx.record(5)
-            ctx.sync()
-            return ctx.elapsed_ms(4, 5)
-        fp64_step_ms = timed_step(7)
-        if not per_solve:
-            refine_step_ms = timed_step(REFINE_DIGITS)
-            # a mixed solve = iterations at few digits + the refinement sweeps
-            value = ws / ((iters * step_ms + REFINE * refine_step_ms) / 1e3)
+    def timed_steps(precision, levels, count, warm=1):
+        """Device milliseconds of one iteration at a precision (mean of
+        `count` after `warm` untimed ones), on the resident solver."""
+        ctx.set_precision(precision, levels)
+        for _ in range(warm):
+            solver.step(w["damp"])
+        ctx.sync()
+        ctx.record(4)
+        for _ in range(count):
+            solver.step(w["damp"])
+        ctx.record(5)
+        ctx.sync()
+        return ctx.elapsed_ms(4, 5) / count
+
+    level_ms = {}
+    dfma_ms = None
+    if not per_solve:
+        level_ms[digits if args.precision != "fp64" else 0] = step_ms
+        if mixed:
+            for lv in (5, 7):
+                level_ms[lv] = timed_steps(_lib.PREC_FP64_TC, lv, 2)
+        elif args.precision == "fp64_tc":
+            level_ms[7] = step_ms
+        # the plain FP64 path: FP64 FMA contractions on the FP64 pipe (one
+        # iteration; tens of seconds at 114 spin orbitals)
+        dfma_ms = step_ms if args.precision == "fp64" else \
+            timed_steps(_lib.PREC_FP64, 7, 1, warm=0)
         ctx.set_precision(prec, digits)
     solver.close()
 
-    # ---- end to end through the public API (e2e) -----------------------------
-    barrier(ws)
-    ctx.sync()
-    t0 = time.perf_counter()
-    ctx.record(2)
-    # complete solves (one for the per-iteration workload) through the drop-in
-    # driver from host arrays: integral upload, guess, iterations, refinement
-    # sweeps and the read-back of all amplitudes
-    n_e2e = args.steps if per_solve else 1
-    for _ in range(n_e2e):
+    # ---- complete solves through the public drop-in API (e2e) -------------
+    # from host arrays: integral upload, guess, all phases of the iteration,
+    # and the read-back of the amplitudes
+    def solve(precision, lv):
         cc = ccsd.ccsd(sysobj, T=sysobj.T, mu=sysobj.mu, max_iter=w["max_iter"],
-                       damp=w["damp"], ngrid=ng, econv=w["econv"], precision=args.precision,
-                       digits=digits, refine_sweeps=REFINE, refine_digits=REFINE_DIGITS,
-                       ctx=ctx)
+                       damp=w["damp"], ngrid=ng, econv=w["econv"], quad=args.quad,
+                       precision=precision, digits=lv, ctx=ctx)
+        ctx.sync()
+        ctx.record(2)
+        t0 = time.perf_counter()
         cc.run()
-        e2e_iters = cc.iterations + cc.iterations_refine
+        ctx.record(3)
+        ctx.sync()
+        wall = max(ctx.elapsed_ms(2, 3), (time.perf_counter() - t0) * 1e3)
+        out = {"omega_cc": cc.Gcc, "iterations": cc.iterations + cc.iterations_refine,
+               "phases": cc.phases, "converged": bool(cc.converged), "ms": wall}
         cc.release()
-    ctx.record(3)
-    ctx.sync()
-    e2e_ms = max(ctx.elapsed_ms(2, 3), (time.perf_counter() - t0) * 1e3)
-    e2e_ms = max_over_ranks(ws, e2e_ms)
+        return out
+
+    barrier(ws)
+    n_e2e = args.steps if per_solve else 1
+    e2e_runs = [solve(args.precision, digits) for _ in range(n_e2e)]
+    e2e_ms = max_over_ranks(ws, sum(r["ms"] for r in e2e_runs))
     e2e_value = ws * n_e2e / (e2e_ms / 1e3)
+    sol = e2e_runs[-1]
+    ref64 = solve("fp64_tc", 7) if args.precision != "fp64_tc" else sol
     h2d = 8 * (n + n * n + n ** 4 + 2 * ng + ng * ng)
-    d2h = 8 * ng * (n * n + n ** 4) + 8 * 7 * (e2e_iters + 2)
+    d2h = 8 * ng * (n * n + n ** 4) + 8 * 7 * (sol["iterations"] + 2)
+
+    # solves/s with everything resident: per-phase iterations of the measured
+    # solve times that phase's measured seconds per iteration
+    if per_solve:
+        value = ws / (step_ms / 1e3)
+        t_solve_ms = step_ms
+    else:
+        t_solve_ms = 0.0
+        for lv, it, _ in sol["phases"]:
+            t_solve_ms += it * level_ms.get(lv if args.precision != "fp64" else 0, step_ms)
+        value = ws / (t_solve_ms / 1e3)
 
     if rank != 0:
         return 0
@@ -387,13 +439,13 @@ def run_gpu(args, w):
             achieved, unit, bound = work / (dms / 1e3) / 1e12, "TFLOP/s", "tensor"
             if args.precision == "fp64":
                 peak = 1.25
-                psrc = "nominal GB300 FP64 1.25 TFLOP/s (MEASURED_PEAKS.json has no FP64 figure)"
+                psrc = "nominal GB300 FP64 1.25 TFLOP/s (no measured FP64 figure)"
             else:
                 pairs = sum(l - 1 for l in range(2, digits + 1))
                 achieved *= pairs      # BF16 tensor flops issued per FP64-equivalent flop
                 peak = peaks["bf16_tflops_sustained"]
-                psrc = "bf16_tflops_sustained of %s peaks; achieved = algorithmic 2MNK flops " \
-                       "x %d digit-pair products" % (peak_src, pairs)
+                psrc = "bf16_tflops_sustained of %s peaks; achieved = the spin-blocked " \
+                       "algorithmic 2MNK flops x %d digit-pair products" % (peak_src, pairs)
         else:
             achieved, unit, bound = work / (dms / 1e3) / 1e9, "GB/s", "hbm"
             peak = peaks["hbm_gbs"]
@@ -405,43 +457,77 @@ def run_gpu(args, w):
     cats = {c: roof(c) for c in prof}
     dom = max(prof, key=lambda c: prof[c][1])
     roofline = dict(cats[dom])
-    traffic = NCU_TRAFFIC.get((args.workload, args.precision, dom))
+    traffic, thow = load_traffic(args.workload, args.precision, dom)
     roofline.update({
         "category": dom, "traffic": traffic,
         "traffic_unit": "bytes per launch (ncu dram__bytes_read.sum + dram__bytes_write.sum)"
-                        if traffic else None,
-        "categories": {c: {k: cats[c][k] for k in ("bound", "achieved", "unit", "frac")}
+                        if traffic else None, "traffic_how": thow,
+        "categories": {c: {k: cats[c][k] for k in ("bound", "achieved", "unit", "frac",
+                                                   "avg_launch_ms", "launches")}
                        for c in cats if cats[c]},
         "breakdown_ms_per_step": {c: round(prof[c][1] / args.steps, 3) for c in prof}})
 
-    t_iter, sample = cpu_iteration_seconds(w, sysobj)
-    cpu_iters = iters_of(w, "fp64")                       # the CPU port is FP64
-    cpu_val = 1.0 / (t_iter * cpu_iters)
-    cfg = {"workload": w["label"], "step": w["step"], "precision": args.precision,
+    # CPU baseline: a bounded sample of the oracle's iteration (guess and three
+    # iterations of the 38-spin-orbital solve) on the host cores
+    t_guess, times, _, _ = oracle_c1_iterations(args.quad, 3, until_converged=False)
+    t_iter_c1 = statistics.median(times)
+    cfg = {"workload": w["label"].replace("ng=%d" % ng, "ng=%d %s" % (
+               ng, "Gauss-Legendre" if full else "Simpson ('lin')")),
+           "step": w["step"], "precision": args.precision,
            "digits": digits if args.precision != "fp64" else None,
-           "iterations_per_solve": iters, "omega_cc_last_step": results[-1][0],
+           "solve": {k: sol[k] for k in ("iterations", "phases", "converged", "omega_cc")},
            "l2": "per-step working set > 129 MB L2 (no flush)",
            "parallelism": "replicas" if ws > 1 else "single GPU"}
+    if not per_solve:
+        cfg["ms_per_iteration"] = {("fp64_fma" if k == 0 else "%d_levels" % k): v
+                                   for k, v in sorted(level_ms.items())}
+        cfg["ms_per_solve_resident"] = t_solve_ms
     if lat:
         q = lambda f: lat[min(len(lat) - 1, int(f * len(lat)))]
         cfg["step_latency_ms"] = {"p50": q(0.5), "p99": q(0.99), "n": len(lat)}
-    if refine_step_ms is not None:
-        cfg["refinement"] = {"sweeps": REFINE, "digit_levels": REFINE_DIGITS,
-                             "step_ms": refine_step_ms}
-    if fp64_step_ms is not None:
-        cfg["fp64_tc_step_ms"] = fp64_step_ms
-        cfg["fp64_tc_solves_per_s"] = ws / (fp64_step_ms / 1e3) / (1 if per_solve else iters)
-        cfg["mixed_over_fp64_tc"] = fp64_step_ms / step_ms
+    if ref64 is not sol:
+        d = abs(sol["omega_cc"] - ref64["omega_cc"])
+        cfg["fp64_tc_solve"] = {k: ref64[k] for k in ("iterations", "converged", "omega_cc",
+                                                     "ms")}
+        cfg["accuracy"] = {"abs_dOmega": d, "abs_dOmega_per_electron": d / w["N"],
+                           "bar_per_electron": 1e-6, "against": "FP64-accurate solve, same run"}
+        if not per_solve and 7 in level_ms:
+            fp64tc = 1.0 / (ref64["iterations"] * level_ms[7] / 1e3)
+            cfg["fp64_tc_solves_per_s"] = fp64tc
+            cfg["mixed_over_fp64_tc"] = value / fp64tc
+    if dfma_ms is not None:
+        it64 = ref64["iterations"]
+        plain = 1.0 / (it64 * dfma_ms / 1e3)
+        cfg["plain_fp64_solves_per_s"] = plain
+        cfg["plain_fp64_how"] = ("one measured iteration of the FP64 FMA path x the "
+                                 "iteration count of the FP64-accurate solve (%d)" % it64)
+        cfg["over_plain_fp64"] = value / plain
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f64" if args.precision != "mixed" else "bf16x3-digits/f32acc + f64",
+            "dtype": {"fp64": "f64", "fp64_tc": "f64 (7 BF16 digit levels, tensor cores)",
+                      "mixed": "bf16 digits/f32 acc (3, 5 levels) + f64 refinement"}[
+                          args.precision],
             "data": "synthetic", "config": cfg, "roofline": roofline,
-            "cpu_baseline": {"value": cpu_val, "unit": UNIT, "cores": os.cpu_count(),
-                             "kind": "port", "sample": sample + "; x %d iterations" % cpu_iters},
+            "cpu_baseline": {"value": None, "unit": UNIT, "cores": os.cpu_count(),
+                             "kind": "port"},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
             "gpu_launches": launches, "clocks": clk}
+    est = c2_estimate(t_iter_c1, ref64["iterations"])
+    if per_solve:
+        line["cpu_baseline"].update({
+            "value": 1.0 / (t_guess + t_iter_c1 * ref64["iterations"]),
+            "sample": "oracle guess + 3 iterations of the same solve on the host (median "
+                      "%.2f s/iteration) x the %d iterations of the FP64 solve"
+                      % (t_iter_c1, ref64["iterations"])})
+    else:
+        line["cpu_baseline"].update({
+            "value": est["value"],
+            "sample": "oracle guess + 3 iterations of the 38-spin-orbital solve on the host "
+                      "(median %.2f s/iteration), SCALED by the contraction work n^6 ng to "
+                      "this workload (an estimate; a measured 114-spin-orbital iteration takes "
+                      "tens of minutes)" % t_iter_c1})
     print(json.dumps(line))
     return 0
 
@@ -456,9 +542,10 @@ def run_profile_step(args, w):
     ctx.set_precision(prec, args.digits or digits)
     s = build_system(w)
     beta = 1.0 / s.T
-    ti, g, G = ft_quad(w["ng"], beta, "lin")
+    ti, g, G = ft_quad(w["ng"], beta, args.quad)
     solver = DeviceSolver.from_system(ctx, s.g_energies_tot(), s.g_fock_tot(), s.g_aint_tot(),
                                       beta, s.mu, ti, g, G)
+    solver.full = args.quad == "gl"
     solver.guess(1)
     solver.step(w["damp"])
     ctx.sync()
@@ -467,7 +554,13 @@ def run_profile_step(args, w):
     E, res = solver.step(w["damp"])
     ctx.sync()
     recs = ctx.profile_records()
+    shapes = ctx.profile_shapes()
     ctx.profile_end()
+    if args.records:
+        # every timed scope of the iteration: category, ms, work, GEMM shape
+        with open(args.records, "w") as f:
+            for (c, ms, wk), sh in zip(recs, shapes):
+                f.write("%s %.4f %.4e %d %d %d %d\n" % ((c, ms, wk) + tuple(sh)))
     # the category of each contraction of the step, in launch order: one
     # GEMM kernel (tc_gemm_kernel or gemm_f64_kernel) per contraction
     gemm_cats = [c for c, _, _ in recs if c in ("gemm6", "gemm")]
@@ -572,6 +665,60 @@ def run_esn(args):
     return 0
 
 
+def run_accuracy(args):
+    """|dOmega|, |dE|, |dS| of the mixed form against the FP64-accurate form
+    on the configurations small enough to differentiate in seconds: E, S from
+    the Lambda equations on Kelvin's Simpson grid, from central differences
+    of Omega on a Gauss-Legendre grid (both evaluate the derivative with
+    FP64-accurate contractions, so the differences measure the mixed solve's
+    amplitudes).  Also |dOmega| where the few-digit phases ended."""
+    from kelvin_gb300 import _lib, ccsd as kccsd, systems
+    ctx = _lib.context(0)
+    cases = [
+        ("ueg38 Simpson", systems.ueg_recipe(14, 4.0, 19, 0.5, device_build=True), 10, "lin",
+         0.5),
+        ("ueg38 Gauss-Legendre", systems.ueg_recipe(14, 4.0, 19, 0.5, device_build=True), 10,
+         "gl", 0.5),
+        ("ueg66 (differentiation config)", systems.ueg_recipe(14, 2.0, 33, 0.5,
+                                                               device_build=True), 16, "lin",
+         0.5),
+    ]
+    for beta in (1.0, 4.0, 10.0):
+        cases.append(("hubbard16 beta=%g" % beta,
+                      systems.hubbard_mf_recipe(16, 1.0, 4.0, beta, device_build=True), 40,
+                      "lin", 0.5))
+    out = []
+    for name, s, ng, quad, damp in cases:
+        res = {}
+        for prec in ("fp64_tc", "mixed"):
+            cc = kccsd.ccsd(s, T=s.T, mu=s.mu, max_iter=300, damp=damp, ngrid=ng,
+                            econv=1e-10, quad=quad, precision=prec, ctx=ctx)
+            t0 = time.perf_counter()
+            try:
+                cc.run()
+                E, S, N = cc.compute_ESN(method="lambda" if quad == "lin" else "fd")
+                res[prec] = {"omega": cc.Gtot, "omega_low": cc.omega_low, "E": E, "S": S,
+                             "N": N, "iterations": cc.iterations + cc.iterations_refine,
+                             "phases": getattr(cc, "phases", None),
+                             "converged": bool(cc.converged),
+                             "seconds": time.perf_counter() - t0}
+            except Exception as e:          # a solve that diverges is reported as such
+                res[prec] = {"error": str(e)}
+            finally:
+                cc.release()
+                ctx.set_precision(_lib.PREC_FP64, 7)
+        a, b = res["fp64_tc"], res["mixed"]
+        row = {"config": name, "electrons": float(getattr(s, "N", 0.0)), "fp64_tc": a,
+               "mixed": b}
+        if "error" not in a and "error" not in b:
+            row.update({"abs_dOmega": abs(b["omega"] - a["omega"]),
+                        "abs_dOmega_low_phases": abs(b["omega_low"] - a["omega"]),
+                        "abs_dE": abs(b["E"] - a["E"]), "abs_dS": abs(b["S"] - a["S"])})
+        out.append(row)
+        print(json.dumps(row), flush=True)
+    return 0
+
+
 def run_serve(args):
     """A seeded Poisson stream of mixed requests (kelvin_gb300.serve): solves/s
     and p50/p99 latency, completion minus arrival."""
@@ -603,8 +750,16 @@ def main():
     ap.add_argument("--rate", type=float, default=20.0, help="request rate of --serve (1/s)")
     ap.add_argument("--esn", action="store_true",
                     help="E, S, N of the 66-spin-orbital UEG: Lambda route against differences")
+    ap.add_argument("--quad", default="gl", choices=["gl", "lin"],
+                    help="tau grid: Gauss-Legendre (the configurations') or Kelvin's Simpson")
+    ap.add_argument("--accuracy", action="store_true",
+                    help="mixed against FP64-accurate on the smaller configurations")
+    ap.add_argument("--records", default="",
+                    help="--profile-step: write every timed scope (with GEMM shapes) here")
     args = ap.parse_args()
     w = WORKLOADS[args.workload]
+    if args.accuracy:
+        return run_accuracy(args)
     if args.serve:
         return run_serve(args)
     if args.esn:

@@ -63,6 +63,12 @@ int kvft_event_record(kvft_ctx *ctx, int slot);            /* slot < 64 */
 int kvft_event_elapsed_ms(kvft_ctx *ctx, int s0, int s1, float *ms);
 int kvft_launch_count(kvft_ctx *ctx, uint64_t *count);     /* own kernels */
 int kvft_flush_l2(kvft_ctx *ctx);                          /* writes 256 MB */
+/* Free and total device memory of the context's device (cudaMemGetInfo). */
+int kvft_mem_info(kvft_ctx *ctx, size_t *free_bytes, size_t *total_bytes);
+/* Cap on the tau-chunk workspace of solvers on this context (bytes; 0: the
+ * default, 60% of the free device memory), so that several resident solvers
+ * share one device. */
+int kvft_set_workspace_limit(kvft_ctx *ctx, size_t bytes);
 
 /* Live launch timing: between begin and end every library launch of the
  * categories below is bracketed by CUDA events on the context's stream.
@@ -91,6 +97,10 @@ int kvft_profile_end(kvft_ctx *ctx, kvft_profile_stats *out);
  * discards them. */
 int kvft_profile_records(kvft_ctx *ctx, int max, int *count, int *cat, float *ms,
                          double *work);
+/* The GEMM shape (M, N, K, batch) behind each record of the current profile
+ * (four ints per record; zeros for scopes that are not a contraction or its
+ * operand packing).  Call before kvft_profile_end. */
+int kvft_profile_shapes(kvft_ctx *ctx, int max, int *count, int *shapes);
 
 /* ---- quadrature: replaces kelvin/quadrature.py:292-317 ------------------
  * out[y] = sum_x G[y][x] exp(dt D) tbar[x], dt = ti[x]-ti[y] for x < y and 0
@@ -153,6 +163,14 @@ int kvft_stanton_residual(kvft_ctx *ctx, int nb, int nv, int no,
                           const double *const F[4], const double *const I[9],
                           const double *t1, const double *t2, double fac,
                           double *T1, double *T2);
+/* Spin blocks of kvft_stanton_residual and kvft_ccsd_stanton (the blocking a
+ * solver finds and uses by itself, kvft_solver_set_spin_blocks): half = h > 0
+ * asserts that the integrals and amplitudes vanish outside the
+ * spin-conserving blocks of an alpha-first layout with nv = no = 2h, so that
+ * the residual's contractions run over their nonzero spin-block products
+ * only; 0 turns it off (the default).  Calls whose nv, no are not 2h ignore
+ * it. */
+int kvft_set_residual_spin_blocks(kvft_ctx *ctx, int half);
 /* Lambda terms (cqcpy _Lambda_opt, called at ft_cc_equations.py:400-401):
  * g = R'(t)^T m, the transpose of the residual's Jacobian at (t1, t2) applied
  * to m, batched over nb tau points, so that
@@ -324,6 +342,12 @@ int kvft_solver_run_point(kvft_solver *s, const kvft_solve_opts *opts,
 /* one amplitude iteration (update + damping + norms + energy) */
 int kvft_solver_step(kvft_solver *s, double damp, double *energy,
                      double *res);
+/* The same iteration split in two: _begin queues it on the context's stream
+ * and returns at once; _end waits for it and returns the energy and residual.
+ * Solvers on different contexts (streams) overlap on the device between the
+ * two calls; one step may be pending per solver. */
+int kvft_solver_step_begin(kvft_solver *s, double damp);
+int kvft_solver_step_end(kvft_solver *s, double *energy, double *res);
 int kvft_solver_get_amplitudes(kvft_solver *s, double *T1_host,
                                double *T2_host);
 int kvft_solver_set_amplitudes(kvft_solver *s, const double *T1_host,

@@ -58,6 +58,7 @@ _SIGS = {
     "kvft_profile_end": (ctypes.c_int, [vp, ctypes.POINTER(ProfileStats)]),
     "kvft_profile_records": (ctypes.c_int, [vp, ctypes.c_int, ctypes.POINTER(ctypes.c_int),
                                             vp, vp, vp]),
+    "kvft_profile_shapes": (ctypes.c_int, [vp, ctypes.c_int, ctypes.POINTER(ctypes.c_int), vp]),
     "kvft_ctx_create": (ctypes.c_int, [ctypes.c_int, vp, ctypes.POINTER(vp)]),
     "kvft_ctx_destroy": (ctypes.c_int, [vp]),
     "kvft_last_error": (ctypes.c_char_p, [vp]),
@@ -110,6 +111,12 @@ _SIGS = {
                                          ctypes.c_int, ctypes.c_int, vp, vp, vp,
                                          ctypes.POINTER(ctypes.c_int)]),
     "kvft_set_lambda_spin_blocks": (ctypes.c_int, [vp, ctypes.c_int]),
+    "kvft_set_residual_spin_blocks": (ctypes.c_int, [vp, ctypes.c_int]),
+    "kvft_set_workspace_limit": (ctypes.c_int, [vp, ctypes.c_size_t]),
+    "kvft_solver_step_begin": (ctypes.c_int, [vp, ctypes.c_double]),
+    "kvft_solver_step_end": (ctypes.c_int, [vp, c_double_p, c_double_p]),
+    "kvft_mem_info": (ctypes.c_int, [vp, ctypes.POINTER(ctypes.c_size_t),
+                                     ctypes.POINTER(ctypes.c_size_t)]),
     "kvft_lambda_guess": (ctypes.c_int, [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                          ctypes.POINTER(vp), ctypes.POINTER(vp), vp,
                                          ctypes.c_double, ctypes.c_int, vp, vp]),
@@ -233,6 +240,24 @@ class Context(object):
     def flush_l2(self):
         self.check(self.L.kvft_flush_l2(self.h), "kvft_flush_l2")
 
+    def mem_info(self):
+        """(free, total) bytes of the context's device."""
+        f, t = ctypes.c_size_t(), ctypes.c_size_t()
+        self.check(self.L.kvft_mem_info(self.h, ctypes.byref(f), ctypes.byref(t)),
+                   "kvft_mem_info")
+        return int(f.value), int(t.value)
+
+    def set_workspace_limit(self, nbytes):
+        """Cap the tau-chunk workspace of this context's solvers (0: default)."""
+        self.check(self.L.kvft_set_workspace_limit(self.h, int(nbytes)),
+                   "kvft_set_workspace_limit")
+
+    def set_residual_spin_blocks(self, half):
+        """Assert spin blocks (alpha half h) for kvft_stanton_residual /
+        kvft_ccsd_stanton on this context; 0 turns them off."""
+        self.check(self.L.kvft_set_residual_spin_blocks(self.h, int(half)),
+                   "kvft_set_residual_spin_blocks")
+
     def profile_begin(self):
         self.check(self.L.kvft_profile_begin(self.h), "kvft_profile_begin")
 
@@ -249,6 +274,17 @@ class Context(object):
                    "kvft_profile_records")
         return [(PROFILE_CATEGORIES[cat[i]], float(ms[i]), float(work[i]))
                 for i in range(n.value)]
+
+    def profile_shapes(self):
+        """[(M, N, K, batch)] of the contraction behind each record (zeros for
+        scopes that are not a contraction or its packing)."""
+        n = ctypes.c_int()
+        self.check(self.L.kvft_profile_shapes(self.h, 0, ctypes.byref(n), None),
+                   "kvft_profile_shapes")
+        sh = (ctypes.c_int * max(4 * n.value, 4))()
+        self.check(self.L.kvft_profile_shapes(self.h, n.value, ctypes.byref(n), sh),
+                   "kvft_profile_shapes")
+        return [tuple(sh[4 * i:4 * i + 4]) for i in range(n.value)]
 
     def profile_end(self):
         """{category: (launches, total ms, algorithmic work)}."""

@@ -67,6 +67,9 @@ class DeviceSolver(object):
         self.ctx = ctx
         self.h = handle
         self.ng, self.nv, self.no = ng, nv, no
+        # tau-integral convention: False, Kelvin's (exp factor for x < y);
+        # True, the dense-G convention of Gauss-Legendre grids (every x)
+        self.full = False
 
     @classmethod
     def from_system(cls, ctx, en, fock, eri, beta, mu, ti, g, G):
@@ -176,7 +179,7 @@ class DeviceSolver(object):
     def guess(self, kind, damp=0.0):
         """kind 0: zeros, 1: Kelvin's first-order guess, 2: keep.  Runs zero
         iterations and returns the guess energy (Qterm = False)."""
-        o = _lib.SolveOpts(econv=0.0, tconv=0.0, damp=damp, max_iter=0, full=0,
+        o = _lib.SolveOpts(econv=0.0, tconv=0.0, damp=damp, max_iter=0, full=int(self.full),
                            guess=int(kind), verbose=0)
         r = _lib.Result()
         st = self.ctx.L.kvft_solver_run(self.h, ctypes.byref(o), ctypes.byref(r))
@@ -186,6 +189,8 @@ class DeviceSolver(object):
 
     def run_point(self, conv_options, verbose=False):
         """Kelvin's tau-pointwise schedule on the device; returns the Result."""
+        if self.full:
+            raise Exception("the pointwise schedule needs a lower-triangular G")
         o = _lib.SolveOpts(econv=float(conv_options["econv"]), tconv=float(conv_options["tconv"]),
                            damp=float(conv_options["damp"]),
                            max_iter=int(conv_options["max_iter"]), full=0, guess=0,
@@ -205,6 +210,20 @@ class DeviceSolver(object):
         res = ctypes.c_double()
         self.ctx.check(self.ctx.L.kvft_solver_step(self.h, float(damp), ctypes.byref(E),
                                                    ctypes.byref(res)), "kvft_solver_step")
+        return E.value, res.value
+
+    def step_begin(self, damp):
+        """Queue one iteration on the context's stream and return at once."""
+        self.ctx.check(self.ctx.L.kvft_solver_step_begin(self.h, float(damp)),
+                       "kvft_solver_step_begin")
+
+    def step_end(self):
+        """Wait for the queued iteration; (energy, residual)."""
+        E = ctypes.c_double()
+        res = ctypes.c_double()
+        self.ctx.check(self.ctx.L.kvft_solver_step_end(self.h, ctypes.byref(E),
+                                                       ctypes.byref(res)),
+                       "kvft_solver_step_end")
         return E.value, res.value
 
     def close(self):

@@ -25,37 +25,52 @@ PRECISIONS = {'fp64': (_lib.PREC_FP64, 7), 'fp64_tc': (_lib.PREC_FP64_TC, 7),
               'mixed': (_lib.PREC_MIXED, 3)}
 
 
-def converge(solver, ctx, conv, precision, digits, refine_sweeps=2, refine_digits=5):
+def converge(solver, ctx, conv, precision, digits, refine_sweeps=None, refine_digits=7,
+             ladder=(5,)):
     """Iterate a DeviceSolver to convergence; returns (Omega_cc, info).
 
-    FP64 forms use Kelvin's test (|dE| < econv and res < tconv).  The mixed
-    form's few-digit update is a slightly discontinuous map (digit rounding),
-    so its iteration settles at a noise floor instead of meeting econv: it
-    stops at Kelvin's test or when the residual has stopped falling for three
-    sweeps, then runs `refine_sweeps` sweeps from that point with
-    `refine_digits` digit levels (5: norm-wise ~1e-9 per contraction, far
-    below the 1e-6 Ha per electron the mixed form answers to, at half the
-    products of the FP64-grade 7)."""
+    FP64 forms ('fp64', 'fp64_tc') run Kelvin's loop and test (|dE| < econv
+    and res < tconv).  The mixed form runs the same damped update in phases
+    of rising digit levels.  A few-digit update is a slightly discontinuous
+    map (digit rounding), so each low phase ends at Kelvin's test or when
+    the residual has stopped falling for three sweeps (its noise floor): first
+    `digits` levels, then each level of `ladder`.  The refinement phase then
+    re-evaluates the update with `refine_digits` levels (7: FP64-accurate)
+    and iterates until Kelvin's test passes, at most `refine_sweeps` sweeps
+    (None: the loop's max_iter).  Only that test counts as convergence: a
+    stalled low phase does not.  info: iterations (low phases),
+    iterations_refine, converged, omega_low (the energy where the low phases
+    ended) and phases, a list of (digit levels, sweeps, stalled)."""
     if precision != 'mixed':
         E = iterate(solver, conv, "CCSD")
         return E, {"iterations": solver.iterations, "iterations_refine": 0,
-                   "converged": solver.converged, "omega_low": None}
-    E_low = iterate(solver, conv, "CCSD", stall=3)
-    info = {"iterations": solver.iterations, "iterations_refine": 0,
-            "converged": solver.converged or getattr(solver, "stalled", False),
-            "omega_low": E_low}
-    E = E_low
-    if refine_sweeps > 0:
-        prec = ctx_precision(ctx)
-        ctx.set_precision(_lib.PREC_FP64_TC, refine_digits)
-        try:
-            ref = dict(conv)
+                   "converged": solver.converged, "omega_low": None,
+                   "phases": [(digits, solver.iterations, False)]}
+    prec = ctx_precision(ctx)
+    phases = []
+    low_iters = 0
+    E_low = None
+    converged = False
+    try:
+        for lv in (digits,) + tuple(l for l in ladder if digits < l < refine_digits):
+            ctx.set_precision(_lib.PREC_MIXED if lv <= 3 else _lib.PREC_FP64_TC, lv)
+            E_low = iterate(solver, conv, "CCSD (%d digit levels)" % lv, stall=3, quiet=True)
+            low_iters += solver.iterations
+            phases.append((lv, solver.iterations, bool(solver.stalled)))
+            if solver.converged:
+                break
+        ref = dict(conv)
+        if refine_sweeps is not None:
             ref["max_iter"] = refine_sweeps
-            E = iterate(solver, ref, "CCSD refinement", quiet=True)
-        finally:
-            ctx.set_precision(*prec)
-        info["iterations_refine"] = solver.iterations
-    return E, info
+        ctx.set_precision(_lib.PREC_FP64_TC, refine_digits)
+        E = iterate(solver, ref, "CCSD refinement")
+        phases.append((refine_digits, solver.iterations, False))
+        converged = solver.converged
+        refine_iters = solver.iterations
+    finally:
+        ctx.set_precision(*prec)
+    return E, {"iterations": low_iters, "iterations_refine": refine_iters,
+               "converged": converged, "omega_low": E_low, "phases": phases}
 
 
 def _d_integrals(h, eri, en, beta, mu, dbeta, dmu):
@@ -171,7 +186,8 @@ class ccsd(object):
     def __init__(self, sys, T=0.0, mu=0.0, iprint=0, singles=True, econv=1e-8,
                  tconv=None, max_iter=40, damp=0.0, ngrid=10, realtime=False,
                  athresh=0.0, quad='lin', rt_iter="all", precision='fp64',
-                 digits=None, refine_sweeps=2, refine_digits=5, device=0, ctx=None):
+                 digits=None, refine_sweeps=None, refine_digits=7, ladder=(5,), device=0,
+                 ctx=None):
         self.T = T
         self.mu = mu
         self.finite_T = T != 0
@@ -190,10 +206,12 @@ class ccsd(object):
             raise Exception("Unrecognized precision: {}".format(precision))
         self.precision = precision
         self.digits = digits if digits is not None else PRECISIONS[precision][1]
-        # mixed form: sweeps re-evaluated with FP64-accurate contractions once
-        # the few-digit iteration has converged (0: none)
+        # mixed form: after the few-digit phases (digits, then each level of
+        # `ladder`), sweeps with `refine_digits` levels (7: FP64-accurate)
+        # until Kelvin's test passes, at most refine_sweeps (None: max_iter)
         self.refine_sweeps = refine_sweeps
         self.refine_digits = refine_digits
+        self.ladder = tuple(ladder)
         if not sys.verify(self.T, self.mu):
             raise Exception("Sytem temperature inconsistent with CC temp")
         if not self.finite_T:
@@ -235,9 +253,6 @@ class ccsd(object):
         en = self.sys.g_energies_tot()
         E0 = grand_potential0(beta, en, mu) + self.sys.const_energy()
         E1 = self.sys.get_mp1()
-        if self.quad == 'gl':
-            raise Exception("the dense Gauss-Legendre G needs the full exp convention, "
-                            "which the resident solver does not run")
         prec, digits = PRECISIONS[self.precision][0], self.digits
         self.ctx.set_precision(prec, digits)
         if getattr(self.sys, "device_build", False):
@@ -250,6 +265,8 @@ class ccsd(object):
             solver = DeviceSolver.from_system(self.ctx, en, self.sys.g_fock_tot(),
                                               self.sys.g_aint_tot(), beta, mu, self.ti,
                                               self.g, self.G)
+        # a dense Gauss-Legendre G takes the exponential for every node pair
+        solver.full = self.quad == 'gl'
         self.solver = solver
         conv = {"econv": self.econv, "tconv": self.tconv, "max_iter": self.max_iter,
                 "damp": self.damp}
@@ -280,11 +297,12 @@ class ccsd(object):
             E2 = solver.guess(1)
         logging.info('MP2 Energy: {:.10f}'.format(E2))
         Eccn, info = converge(solver, self.ctx, conv, self.precision, digits,
-                              self.refine_sweeps, self.refine_digits)
+                              self.refine_sweeps, self.refine_digits, self.ladder)
         self.iterations = info["iterations"]
         self.iterations_refine = info["iterations_refine"]
         self.converged = info["converged"]
         self.omega_low = info["omega_low"]
+        self.phases = info.get("phases")
         self._Tg = solver.amplitudes()
         self.T1, self.T2 = self._Tg
         if self._unrestricted():
@@ -306,6 +324,9 @@ class ccsd(object):
         unrestricted form, which is solved in its general-spin form with the
         unrestricted driver's guess and residual measure
         (kelvin/ccsd.py:963-1073)."""
+        if self.quad == 'gl':
+            raise Exception("the Lambda equations are built for Kelvin's lower-triangular "
+                            "grids; use compute_ESN(method='fd') on a Gauss-Legendre grid")
         u = self._unrestricted()
         na = self.sys.u_energies_tot()[0].shape[0] if u else None
         if self.T1 is None:
@@ -410,6 +431,7 @@ class ccsd(object):
             ti, g, G = ft_quad(self.ngrid, beta, self.quad)
             self.ctx.set_precision(*PRECISIONS[prec])
             solver = DeviceSolver.from_system(self.ctx, en, fock, eri, beta, mu, ti, g, G)
+            solver.full = self.quad == 'gl'
             try:
                 solver.set_amplitudes(*Tg)
                 solver.guess(2)

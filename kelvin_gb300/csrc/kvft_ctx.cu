@@ -294,7 +294,10 @@ int kv_prof_mark(kvft_ctx *ctx, size_t *slot) {
 }
 
 void kv_prof_add(kvft_ctx *ctx, int cat, size_t e0, size_t e1, double work) {
-    ctx->prof->recs.push_back({cat, e0, e1, work});
+    KvProf::Rec r{cat, e0, e1, work, {0, 0, 0, 0}};
+    if (cat == KV_CAT_GEMM6 || cat == KV_CAT_GEMM || cat == KV_CAT_PACK)
+        for (int k = 0; k < 4; k++) r.shape[k] = ctx->prof->shape[k];
+    ctx->prof->recs.push_back(r);
 }
 
 KvProfScope::KvProfScope(kvft_ctx *c, int k, double w)
@@ -335,6 +338,16 @@ extern "C" int kvft_profile_records(kvft_ctx *c, int max, int *count, int *cat, 
     return KVFT_OK;
 }
 
+extern "C" int kvft_profile_shapes(kvft_ctx *c, int max, int *count, int *shapes) {
+    if (c && c->dry) return kv_fail(c, KVFT_EINVAL, "kvft_profile_shapes: not on a dry-run context");
+    if (!c || !c->prof || !count || max < 0 || (max > 0 && !shapes)) return KVFT_EINVAL;
+    const auto &recs = c->prof->recs;
+    *count = (int)recs.size();
+    for (int i = 0; i < max && i < (int)recs.size(); i++)
+        for (int k = 0; k < 4; k++) shapes[4 * i + k] = recs[i].shape[k];
+    return KVFT_OK;
+}
+
 extern "C" int kvft_profile_end(kvft_ctx *c, kvft_profile_stats *out) {
     if (c && c->dry) return kv_fail(c, KVFT_EINVAL, "kvft_profile_end: not on a dry-run context");
     if (!c || !c->prof || !out) return KVFT_EINVAL;
@@ -367,4 +380,18 @@ extern "C" int kvft_flush_l2(kvft_ctx *c) {
     static unsigned salt = 1;
     kv_flush_kernel<<<c->sm_count * 4, 512, 0, c->stream>>>((uint4 *)c->l2buf, bytes / 16, salt++);
     return kv_launch_check(c, "flush_l2");
+}
+
+extern "C" int kvft_mem_info(kvft_ctx *c, size_t *free_bytes, size_t *total_bytes) {
+    if (c && c->dry) return kv_fail(c, KVFT_EINVAL, "kvft_mem_info: not on a dry-run context");
+    if (!c || !free_bytes || !total_bytes) return kv_fail(c, KVFT_EINVAL, "kvft_mem_info: bad argument");
+    cudaSetDevice(c->device);
+    KV_CHECK(c, cudaMemGetInfo(free_bytes, total_bytes));
+    return KVFT_OK;
+}
+
+extern "C" int kvft_set_workspace_limit(kvft_ctx *c, size_t bytes) {
+    if (!c) return KVFT_EINVAL;
+    c->workspace_limit = bytes;
+    return KVFT_OK;
 }

@@ -247,6 +247,10 @@ int kv_gemm(kvft_ctx *ctx, int M, int N, int K, int batch, double alpha,
     const bool tc = ctx->precision != KVFT_PREC_FP64 && K >= 16 &&
                     2.0 * M * N * (double)K * batch >= 2.0e6;
     kv_gemm_prof_set(ctx, M, N, K, batch, A.bst ? batch : 1, B.bst ? batch : 1, beta, tc);
+    if (ctx->prof) {
+        ctx->prof->shape[0] = M, ctx->prof->shape[1] = N;
+        ctx->prof->shape[2] = K, ctx->prof->shape[3] = batch;
+    }
     if (!tc) return kv_gemm_f64(ctx, M, N, K, batch, alpha, A, B, beta, C);
     return kv_gemm_tc(ctx, M, N, K, batch, alpha, A, B, beta, C, ctx->digits);
 }

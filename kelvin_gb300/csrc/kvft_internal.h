@@ -123,6 +123,9 @@ struct kvft_ctx {
     // 0, or h when every index-string contraction may run over its nonzero
     // spin-block products only (nv = no = 2h, alpha half first).
     int lam_spin = 0;
+    // cap on the bytes a solver's tau-chunk workspace may take on this
+    // context (0: 60% of the free memory), so that several solvers fit
+    size_t workspace_limit = 0;
 };
 struct KvSpinScope {
     kvft_ctx *ctx;
@@ -147,8 +150,11 @@ struct KvProf {
     bool on = false;
     std::vector<cudaEvent_t> pool;
     size_t used = 0;
-    struct Rec { int cat; size_t e0, e1; double work; };
+    struct Rec { int cat; size_t e0, e1; double work; int shape[4]; };
     std::vector<Rec> recs;
+    // GEMM shape (M, N, K, batch) of the contraction being launched: tagged
+    // on its packing and kernel scopes
+    int shape[4] = {0, 0, 0, 0};
 };
 int kv_prof_mark(kvft_ctx *ctx, size_t *slot);            // record one event
 void kv_prof_add(kvft_ctx *ctx, int cat, size_t e0, size_t e1, double work);

@@ -33,6 +33,7 @@ struct QuadParams {
     int step;                // recurrence step (0: general path)
     int uniform;             // all ti[k+1]-ti[k] equal
     int full;
+    int symmetric;           // ti[x] + ti[ng-1-x] the same for every x
     double alpha;            // damping (fused update only)
     int spin_half;           // fused update over the spin-conserving elements only (0: all)
 };
@@ -90,7 +91,7 @@ quad_kernel(QuadParams q, const double *__restrict__ tbar, const double *__restr
     double *G = ti + ng;
     double *cs = G + ng * ng, *g1 = cs + ng, *gd = g1 + ng;
     double *rk = gd + ng;                                  // [ng][QT]
-    double *tb = rk + (q.uniform ? 0 : ng * QT);           // [ng][QT]
+    double *tb = rk + ((q.uniform || q.full) ? 0 : ng * QT);   // [ng][QT]
     for (int k = threadIdx.x; k < ng; k += QT) ti[k] = ti_g[k];
     for (int k = threadIdx.x; k < ng * ng; k += QT) G[k] = G_g[k];
     for (int y = threadIdx.x; y < ng; y += QT) {
@@ -106,6 +107,53 @@ quad_kernel(QuadParams q, const double *__restrict__ tbar, const double *__restr
     const int t = threadIdx.x;
     auto element = [&](long long p) {
         const double d = denom(q, p, D, ev, eo);
+        if (q.full) {
+            // dense G (Gauss-Legendre): exp((ti[x]-ti[y]) d) for every pair,
+            // factorised about the grid's centre tc as E_x / E_y with
+            // E_x = exp((ti[x]-tc) d).  The scaled inputs u_x = E_x tbar_x
+            // and the E_x sit in this thread's two shared-memory columns;
+            // on a grid symmetric about tc (Gauss-Legendre nodes are)
+            // E_{ng-1-x} = 1 / E_x, so ng/2 exps and ng/2 divisions, then
+            // ng^2 FMAs, per element
+            const double tc = 0.5 * (ti[0] + ti[ng - 1]);
+            double *ec = tb + ng * QT;
+            const int nx = q.symmetric ? (ng + 1) / 2 : ng;
+            for (int x = 0; x < nx; x++) {
+                const double E = exp((ti[x] - tc) * d);
+                ec[x * QT + t] = E;
+                tb[x * QT + t] = E * tbar[(long long)x * q.P + p];
+                const int xm = ng - 1 - x;
+                if (q.symmetric && xm != x) {
+                    const double Ei = 1.0 / E;
+                    ec[xm * QT + t] = Ei;
+                    tb[xm * QT + t] = Ei * tbar[(long long)xm * q.P + p];
+                }
+            }
+            float f_diff = 0.f, f_norm = 0.f;
+            for (int y = 0; y < ng; y++) {
+                double acc = 0.0;
+                for (int x = 0; x < ng; x++) acc = fma(G[y * ng + x], tb[x * QT + t], acc);
+                const double Ty = q.symmetric ? acc * ec[(ng - 1 - y) * QT + t]
+                                              : acc / ec[y * QT + t];
+                if (MODE == 0) {
+                    out[(long long)y * q.P + p] = Ty;
+                } else {
+                    double *o = out + (long long)y * q.P + p;
+                    const double told = *o;
+                    const double df = Ty - told;
+                    const double nt = fma(oma, df, told);
+                    const float fd = abs_to_f32(df), fn = abs_to_f32(nt);
+                    f_diff = fmaf(fd, fd, f_diff);
+                    f_norm = fmaf(fn, fn, f_norm);
+                    *o = nt;
+                }
+            }
+            if (MODE == 1) {
+                s_diff += (double)f_diff;
+                s_norm += (double)f_norm;
+            }
+            return;
+        }
         // step factors r_k = exp((ti[k]-ti[k+1]) d)
         double r0 = 1.0;
         if (UNI) {
@@ -167,12 +215,11 @@ quad_kernel(QuadParams q, const double *__restrict__ tbar, const double *__restr
                     const double gyx = G[y * ng + x];
                     if (gyx != 0.0) Ty = fma(gyx * w, tb[x * QT + t], Ty);
                 }
-                // x > y: factor 1 (reference) or exp((ti[x]-ti[y]) d) (full)
-                double wu = 1.0;
+                // x > y: factor 1 (the reference's rule; `full` takes the
+                // factorised branch above)
                 for (int x = y + 1; x < ng; x++) {
-                    if (q.full) wu /= RK(x - 1);
                     const double gyx = G[y * ng + x];
-                    if (gyx != 0.0) Ty = fma(gyx * wu, tb[x * QT + t], Ty);
+                    if (gyx != 0.0) Ty = fma(gyx, tb[x * QT + t], Ty);
                 }
                 if (MODE == 0) {
                     out[(long long)y * q.P + p] = Ty;
@@ -304,9 +351,21 @@ void analyse_grid(int ng, const double *ti, const double *G, int full, int *step
     }
 }
 
-size_t quad_smem(int ng, int uniform, int step) {
-    return sizeof(double) *
-           (4 * ng + ng * ng + (uniform ? 0 : ng * QT) + (step > 0 ? 0 : ng * QT));
+// ti, G, cs, g1, gd; then the per-thread columns: step factors (general
+// lower-triangular path on a non-uniform grid), inputs (general and dense
+// paths), and the dense path's scale factors
+size_t quad_smem(int ng, int uniform, int step, int full) {
+    return sizeof(double) * (4 * ng + ng * ng + ((uniform || full) ? 0 : ng * QT) +
+                             (step > 0 ? 0 : ng * QT) + (full ? ng * QT : 0));
+}
+
+// ti[x] + ti[ng-1-x] equal for every x (to rounding)
+int grid_symmetric(int ng, const double *ti) {
+    const double c = ti[0] + ti[ng - 1];
+    const double tol = 1e-13 * std::max(std::fabs(ti[ng - 1] - ti[0]), 1e-300);
+    for (int x = 0; x < ng; x++)
+        if (std::fabs(ti[x] + ti[ng - 1 - x] - c) > tol) return 0;
+    return 1;
 }
 
 }  // namespace
@@ -340,13 +399,14 @@ int kv_quad_launch(kvft_ctx *ctx, int mode, int ng, long long P, int rank, int n
     q.alpha = alpha;
     q.spin_half = (mode == 1 && rank == 2 && nv == no && nv == 2 * spin_half) ? spin_half : 0;
     analyse_grid(ng, hti, hG, full, &q.step, &q.uniform);
-    size_t smem = quad_smem(ng, q.uniform, q.step);
+    q.symmetric = grid_symmetric(ng, hti);
+    size_t smem = quad_smem(ng, q.uniform, q.step, q.full);
     long long blocks = (P + QT - 1) / QT;
     long long cap = (long long)ctx->sm_count * 16;
     int grid = (int)std::min(blocks, cap);
     static bool attr_done = false;
     if (!attr_done) {
-        const int mx = (int)quad_smem(MAXNG, 0, 0);
+        const int mx = (int)quad_smem(MAXNG, 0, 0, 1);
         cudaFuncSetAttribute(quad_kernel<0, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
         cudaFuncSetAttribute(quad_kernel<0, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
         cudaFuncSetAttribute(quad_kernel<1, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);

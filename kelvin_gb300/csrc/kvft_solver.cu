@@ -185,6 +185,14 @@ struct kvft_solver {
     // outside that break the structure turn them off)
     int spin_half = 0;
     bool spin_on = true;
+    // tau-integral convention: 0 Kelvin's (exp factor for x < y only), 1 the
+    // dense-G convention of Gauss-Legendre grids (exp factor for every x)
+    int full = 0;
+    // asynchronous steps: the step's scalars land in pinned host memory and
+    // `done` marks their arrival (kvft_solver_step_begin / _end)
+    double *hsc = nullptr;
+    cudaEvent_t done = nullptr;
+    bool pending = false;
     long long s1() const { return (long long)nv * no; }
     long long s2() const { return s1() * s1(); }
 };
@@ -244,6 +252,7 @@ int pick_chunk(kvft_solver *s) {
     for (auto &kv : s->ctx->scratch) held += kv.second.second;
     size_t per = kv_chunk_bytes_per_tau(s->ctx, s->nv, s->no);
     size_t budget = (size_t)(0.6 * (double)(fr + held));
+    if (s->ctx->workspace_limit > 0) budget = std::min(budget, s->ctx->workspace_limit);
     long long c = per ? (long long)(budget / per) : s->ng;
     s->chunk = (int)std::max(1LL, std::min((long long)s->ng, c));
     s->chunk_prec = s->ctx->precision * 16 + s->ctx->digits;
@@ -273,12 +282,12 @@ int form_tbar(kvft_solver *s) {
 int integrate(kvft_solver *s, int mode, double damp, const double *t1b, const double *t2b,
               double *o1, double *o2, double *r1, double *r2) {
     KV_TRY(kv_quad_launch(s->ctx, mode, s->ng, s->s1(), 1, s->nv, s->no, t1b, s->ti,
-                          s->hti.data(), s->G, s->hG.data(), s->D1, s->eps, s->eps, 0, damp, o1,
-                          r1));
+                          s->hti.data(), s->G, s->hG.data(), s->D1, s->eps, s->eps, s->full,
+                          damp, o1, r1));
     // the damped update skips the zero spin blocks of T2 (they stay zero)
     return kv_quad_launch(s->ctx, mode, s->ng, s->s2(), 2, s->nv, s->no, t2b, s->ti,
-                          s->hti.data(), s->G, s->hG.data(), s->D2, s->eps, s->eps, 0, damp, o2,
-                          r2, s->spin_on ? s->spin_half : 0);
+                          s->hti.data(), s->G, s->hG.data(), s->D2, s->eps, s->eps, s->full,
+                          damp, o2, r2, s->spin_on ? s->spin_half : 0);
 }
 
 int read_scalars(kvft_solver *s, int count, double *h) {
@@ -362,6 +371,8 @@ int detect_spin_blocks(kvft_solver *s) {
 int finish_create(kvft_solver *s, kvft_solver **out) {
     if (cudaStreamSynchronize(s->ctx->stream) != cudaSuccess)
         return kv_fail(s->ctx, KVFT_EDEVICE, "solver set-up kernels failed");
+    KV_CHECK(s->ctx, cudaMallocHost(&s->hsc, 16 * sizeof(double)));
+    KV_CHECK(s->ctx, cudaEventCreateWithFlags(&s->done, cudaEventDisableTiming));
     KV_TRY(detect_spin_blocks(s));
     KV_TRY(pick_chunk(s));
     *out = s;
@@ -370,6 +381,8 @@ int finish_create(kvft_solver *s, kvft_solver **out) {
 
 void destroy(kvft_solver *s) {
     for (void *p : s->allocs) cudaFree(p);
+    if (s->hsc) cudaFreeHost(s->hsc);
+    if (s->done) cudaEventDestroy(s->done);
     delete s;
 }
 
@@ -502,9 +515,13 @@ int kvft_solver_destroy(kvft_solver *s) {
     return KVFT_OK;
 }
 
-int kvft_solver_step(kvft_solver *s, double damp, double *energy, double *res) {
+// One amplitude iteration queued on the context's stream without waiting:
+// update, integration + damping + norms, energy, and the copy of the five
+// scalars to pinned host memory.  kvft_solver_step_end waits for them.
+int kvft_solver_step_begin(kvft_solver *s, double damp) {
     if (!s) return KVFT_EINVAL;
     kvft_ctx *ctx = s->ctx;
+    if (s->pending) return kv_fail(ctx, KVFT_EINVAL, "solver_step_begin: a step is pending");
     cudaSetDevice(ctx->device);
     if (!s->norms_valid) KV_TRY(refresh_norms(s));
     KV_TRY(form_tbar(s));
@@ -512,8 +529,22 @@ int kvft_solver_step(kvft_solver *s, double damp, double *energy, double *res) {
     KV_TRY(integrate(s, 1, damp, s->T1b, s->T2b, s->T1, s->T2, s->dsc + 0, s->dsc + 2));
     KV_TRY(kv_energy(ctx, s->ng, s->nv, s->no, s->T1, s->T2, s->F[1], s->I[5], s->g, s->beta, 1,
                      s->dsc + 4, s->spin_on ? s->spin_half : 0));
-    double h[5];
-    KV_TRY(read_scalars(s, 5, h));
+    KV_CHECK(ctx, cudaMemcpyAsync(s->hsc, s->dsc, 5 * sizeof(double), cudaMemcpyDeviceToHost,
+                                  ctx->stream));
+    KV_CHECK(ctx, cudaEventRecord(s->done, ctx->stream));
+    s->pending = true;
+    return KVFT_OK;
+}
+
+// Waits for the step queued by kvft_solver_step_begin; Kelvin's residual
+// measure and the energy, as kvft_solver_step returns them.
+int kvft_solver_step_end(kvft_solver *s, double *energy, double *res) {
+    if (!s) return KVFT_EINVAL;
+    kvft_ctx *ctx = s->ctx;
+    if (!s->pending) return kv_fail(ctx, KVFT_EINVAL, "solver_step_end: no step is pending");
+    s->pending = false;
+    KV_CHECK(ctx, cudaEventSynchronize(s->done));
+    const double *h = s->hsc;
     const double res1 = std::sqrt(h[0]) / s->nl1;
     const double res2 = std::sqrt(h[2]) / s->nl2;
     s->nl1 = std::sqrt(h[1]) + 0.1;
@@ -525,11 +556,18 @@ int kvft_solver_step(kvft_solver *s, double damp, double *energy, double *res) {
     return KVFT_OK;
 }
 
+int kvft_solver_step(kvft_solver *s, double damp, double *energy, double *res) {
+    KV_TRY(kvft_solver_step_begin(s, damp));
+    return kvft_solver_step_end(s, energy, res);
+}
+
 int kvft_solver_run(kvft_solver *s, const kvft_solve_opts *o, kvft_result *r) {
     if (!s || !o || !r) return KVFT_EINVAL;
     kvft_ctx *ctx = s->ctx;
     cudaSetDevice(ctx->device);
-    if (o->full) return kv_fail(ctx, KVFT_EINVAL, "solver: dense-G convention not supported");
+    if (o->full != 0 && o->full != 1) return kv_fail(ctx, KVFT_EINVAL, "solver: full must be 0 or 1");
+    // the convention holds for this run and the steps that follow it
+    s->full = o->full;
     if (o->guess == 0) {
         KV_CHECK(ctx, cudaMemsetAsync(s->T1, 0, sizeof(double) * s->ng * s->s1(), ctx->stream));
         KV_CHECK(ctx, cudaMemsetAsync(s->T2, 0, sizeof(double) * s->ng * s->s2(), ctx->stream));
@@ -572,6 +610,9 @@ int kvft_solver_run_point(kvft_solver *s, const kvft_solve_opts *o, kvft_result 
     if (!s || !o || !r) return KVFT_EINVAL;
     kvft_ctx *ctx = s->ctx;
     cudaSetDevice(ctx->device);
+    // Kelvin's pointwise schedule integrates up to each point only, which is
+    // the lower-triangular convention
+    if (o->full) return kv_fail(ctx, KVFT_EINVAL, "solver_run_point: dense-G grids are not pointwise");
     const long long n1 = s->s1(), n2 = s->s2();
     const int ng = s->ng;
     if (s->chunk_prec != ctx->precision * 16 + ctx->digits) KV_TRY(pick_chunk(s));
@@ -732,6 +773,8 @@ int kvft_solver_lambda(kvft_solver *s, int guess, double damp, double tconv, int
                        int measure_half, double *L1, double *L2, double *hist, int *iters) {
     if (!s || !L1 || !L2 || !iters || guess < 0 || guess > 2)
         return kv_fail(s ? s->ctx : nullptr, KVFT_EINVAL, "solver_lambda: bad argument");
+    // the backward integral is the adjoint of Kelvin's lower-triangular one
+    if (s->full) return kv_fail(s->ctx, KVFT_EINVAL, "solver_lambda: not on a dense-G grid");
     cudaSetDevice(s->ctx->device);
     const double *ev = nullptr, *eo = nullptr;
     KV_TRY(solver_energies(s, &ev, &eo));
@@ -751,6 +794,7 @@ int kvft_solver_lambda_densities(kvft_solver *s, const double *L1, const double 
                                  double *const Fg[4], double *const Ig[9]) {
     if (!s || !L1 || !L2 || !Fg || !Ig)
         return kv_fail(s ? s->ctx : nullptr, KVFT_EINVAL, "solver_lambda_densities: bad argument");
+    if (s->full) return kv_fail(s->ctx, KVFT_EINVAL, "solver_lambda_densities: not on a dense-G grid");
     cudaSetDevice(s->ctx->device);
     const double *ev = nullptr, *eo = nullptr;
     KV_TRY(solver_energies(s, &ev, &eo));

@@ -572,3 +572,9 @@ extern "C" int kvft_stanton_residual(kvft_ctx *ctx, int nb, int nv, int no,
     cudaSetDevice(ctx->device);
     return kv_stanton(ctx, nb, nv, no, F, I, t1, t2, fac, T1, T2);
 }
+
+extern "C" int kvft_set_residual_spin_blocks(kvft_ctx *ctx, int half) {
+    if (!ctx || half < 0) return kv_fail(ctx, KVFT_EINVAL, "residual spin blocks: bad argument");
+    ctx->spin_half = half;
+    return KVFT_OK;
+}

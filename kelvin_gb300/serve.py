@@ -1,13 +1,23 @@
-"""Serving loop for streams of FT-CCSD requests on one GPU.
+"""Serving loop for streams of FT-CCSD requests on one GPU: continuous
+batching.
 
 Requests arrive as a Poisson stream; each names a model system (a UEG recipe
-or a Hubbard ring), a reduced temperature and a tau grid.  One worker solves
-them in arrival order on the device, admitting a request only when its device
-footprint (kvft_solver_footprint) fits the memory budget, and warm-starting a
-system already solved at another temperature on the same grid from that
-solve's converged amplitudes.  A request's latency is its completion time
-minus its arrival time (queueing included); the report gives solves/s and the
-p50/p99 latencies.
+or a Hubbard ring), a reduced temperature and a tau grid.  Up to `slots`
+requests are on the device at once, each with its own resident solver
+(integrals, grid and amplitudes in HBM) on its own context and CUDA stream.
+A request is admitted as soon as it has arrived, a slot is free and its
+device footprint (kvft_solver_footprint plus the slot's capped tau-chunk
+workspace) fits the memory the active slots leave; requests that arrive
+while others run wait only for that.  The loop runs in rounds: it queues one
+amplitude iteration of every active solve (kvft_solver_step_begin, no host
+wait), so their kernels overlap on the device, then collects each result
+(kvft_solver_step_end) and advances that solve's own convergence state --
+the same phases as ccsd.converge: few-digit sweeps to their noise floor, then
+FP64-accurate sweeps to Kelvin's test.  A finished solve frees its slot at
+once.  Each solve starts from the converged amplitudes of the finished solve
+of the same system and grid whose temperature is nearest (in log Theta), when
+one is kept.  A request's latency is its completion time minus its arrival
+time; the report gives solves/s and the p50/p99 latencies.
 
     from kelvin_gb300 import serve
     reqs = serve.request_stream(64, rate=20.0, seed=0)
@@ -18,7 +28,8 @@ import time
 import numpy
 
 from . import _lib, systems
-from .ccsd import PRECISIONS, ccsd
+from .ccsd import PRECISIONS
+from .systems import grand_potential0
 
 # (electrons, plane waves) of the UEG requests; Hubbard rings take 8-16 sites
 UEG_SHAPES = ((14, 19), (14, 27), (38, 33), (38, 57))
@@ -45,7 +56,7 @@ class Request(object):
             N, norb, rs = self.params
             return systems.ueg_recipe(N, rs, norb, self.theta, device_build=True)
         sites, u = self.params
-        return systems.hubbard_recipe(sites, 1.0, u, 1.0 / self.theta, device_build=True)
+        return systems.hubbard_mf_recipe(sites, 1.0, u, 1.0 / self.theta, device_build=True)
 
 
 def request_stream(count, rate=20.0, seed=0):
@@ -71,75 +82,260 @@ def request_stream(count, rate=20.0, seed=0):
     return out
 
 
+class Solve(object):
+    """One request on the device: its solver and convergence state (the
+    phases of ccsd.converge, advanced one sweep at a time)."""
+
+    def __init__(self, req, levels, refine, conv, start, warm):
+        self.req = req
+        self.levels = list(levels)        # digit levels of the phases, last = refine
+        self.refine = refine
+        self.conv = conv
+        self.start = start
+        self.warm = warm
+        self.phase = 0
+        self.Eold = 888888888.888888888
+        self.best, self.since = float("inf"), 0
+        self.it_phase = 0
+        self.iterations = 0
+        self.omega_cc = None
+        self.done = False
+        self.converged = False
+        self.handle = None                # backend state (solver, context, ...)
+
+    def level(self):
+        return self.levels[self.phase]
+
+    def advance(self, E, res):
+        """Kelvin's test (and, in the few-digit phases, the noise-floor stop)
+        after one sweep; True when the solve is finished."""
+        self.iterations += 1
+        self.it_phase += 1
+        conv = abs(E - self.Eold) < self.conv["econv"] and res < self.conv["tconv"]
+        last = self.phase == len(self.levels) - 1
+        stalled = False
+        if not last:
+            if res < 0.9 * self.best:
+                self.best, self.since = res, 0
+            else:
+                self.since += 1
+                stalled = self.since >= 3
+        self.Eold = E
+        if last and (conv or self.it_phase >= self.conv["max_iter"]):
+            self.omega_cc, self.converged, self.done = E, conv, True
+        elif not last and (conv or stalled or self.it_phase >= self.conv["max_iter"]):
+            self.phase += 1
+            self.it_phase = 0
+            self.Eold = 888888888.888888888
+            self.best, self.since = float("inf"), 0
+        return self.done
+
+
+class DeviceBackend(object):
+    """Solves on the GPU: one context (CUDA stream) per slot, each with its
+    tau-chunk workspace capped so that the slots share the device."""
+
+    def __init__(self, slots, workspace_bytes, device=0):
+        self.free_ctx = [_lib.Context(device) for _ in range(slots)]
+        for c in self.free_ctx:
+            c.set_workspace_limit(workspace_bytes)
+        self.workspace_bytes = workspace_bytes
+
+    def mem_total(self):
+        return self.free_ctx[0].mem_info()[1] if self.free_ctx else 0
+
+    def footprint(self, req, precision):
+        prec = PRECISIONS[precision][0]
+        return int(_lib.lib().kvft_solver_footprint(req.n_spin_orbitals(), req.ng, prec)) + \
+            self.workspace_bytes
+
+    def open(self, sv, warm):
+        from .cc_utils import DeviceSolver
+        from .quadrature import ft_quad
+        ctx = self.free_ctx.pop()
+        s = sv.req.system()
+        beta = 1.0 / s.T
+        ti, g, G = ft_quad(sv.req.ng, beta, 'lin')
+        en = s.g_energies_tot()
+        ctx.set_precision(*_level_precision(sv.level()))
+        eri = s.device_aint_tot(ctx)
+        try:
+            solver = DeviceSolver.from_system(ctx, en, s.g_fock_tot(), eri, beta, s.mu, ti, g, G)
+        finally:
+            eri.free()
+        if warm is not None:
+            solver.set_amplitudes(*warm)
+            solver.guess(2)
+        else:
+            solver.guess(1)
+        sv.handle = (ctx, solver, s)
+        sv.level_set = sv.level()
+
+    def begin(self, sv, damp):
+        ctx, solver, _ = sv.handle
+        if sv.level_set != sv.level():
+            ctx.set_precision(*_level_precision(sv.level()))
+            sv.level_set = sv.level()
+        solver.step_begin(damp)
+
+    def end(self, sv):
+        return sv.handle[1].step_end()
+
+    def close(self, sv, keep):
+        """Release the slot; (Omega, the converged amplitudes on the host when
+        `keep`)."""
+        ctx, solver, s = sv.handle
+        amps = solver.amplitudes() if keep else None
+        omega = None
+        if sv.omega_cc is not None:
+            E0 = grand_potential0(1.0 / s.T, s.g_energies_tot(), s.mu) + s.const_energy()
+            omega = E0 + s.get_mp1() + sv.omega_cc
+        solver.close()
+        self.free_ctx.append(ctx)
+        sv.handle = None
+        return omega, amps
+
+
+def _level_precision(levels):
+    return (_lib.PREC_MIXED, levels) if levels <= 3 else (_lib.PREC_FP64_TC, levels)
+
+
 class Server(object):
-    """Solves requests in arrival order on one device.
+    """Continuous batching of a request stream on one device.
 
-    ``solve(req, warm)`` -> (Omega, amplitudes) and ``footprint(req)`` ->
-    bytes default to the device solver; ``clock``/``sleep`` to real time.
-    ``budget`` is the device memory a request may use (default: 90 % of the
-    device).  Warm-start amplitudes are kept per key while they take at most
-    ``warm_bytes`` on the host."""
+    ``backend`` runs the solves (default: DeviceBackend on the GPU);
+    ``clock``/``sleep`` default to real time.  ``budget``: device bytes the
+    active solves may hold (default 90 % of the device).  Converged
+    amplitudes are kept on the host per (system, grid) and temperature while
+    they take at most ``warm_bytes``; ``warm=False`` turns warm starts off."""
 
-    def __init__(self, precision='mixed', ctx=None, budget=None, solve=None, footprint=None,
-                 clock=time.perf_counter, sleep=time.sleep, warm_bytes=2 << 30):
+    def __init__(self, precision='mixed', slots=4, budget=None, backend=None,
+                 clock=time.perf_counter, sleep=time.sleep, warm_bytes=8 << 30, warm=True,
+                 damp=0.5, econv=1e-8, max_iter=200, workspace_bytes=24 << 30):
         self.precision = precision
-        self.ctx = ctx
+        self.slots = slots
         self.budget = budget
-        self.solve = solve or self._solve_on_device
-        self.footprint = footprint or self._footprint
+        self._backend = backend
+        self.workspace_bytes = workspace_bytes
         self.clock, self.sleep = clock, sleep
         self.warm_bytes = warm_bytes
-        self.cache = {}
+        self.use_warm = warm
+        self.damp = damp
+        self.conv = {"econv": econv, "tconv": 1000.0 * econv, "max_iter": max_iter}
+        self.cache = {}                   # key -> {theta: amplitudes}
+        digits = PRECISIONS[precision][1]
+        self.levels = (digits, 5, 7) if precision == 'mixed' else (digits,)
 
-    def _device(self):
-        if self.ctx is None:
-            self.ctx = _lib.context(0)
-        return self.ctx
-
-    def _footprint(self, req):
-        prec = PRECISIONS[self.precision][0]
-        return int(_lib.lib().kvft_solver_footprint(req.n_spin_orbitals(), req.ng, prec))
+    def backend(self):
+        if self._backend is None:
+            self._backend = DeviceBackend(self.slots, self.workspace_bytes)
+        return self._backend
 
     def _budget(self):
         if self.budget is None:
-            import torch
-            free, total = torch.cuda.mem_get_info(0)
-            self.budget = int(0.9 * total)
+            self.budget = int(0.9 * self.backend().mem_total())
         return self.budget
 
-    def _solve_on_device(self, req, warm):
-        s = req.system()
-        cc = ccsd(s, T=s.T, mu=s.mu, ngrid=req.ng, damp=0.5, econv=1e-8, max_iter=200,
-                  precision=self.precision, ctx=self._device())
-        try:
-            omega = cc.run(*warm)[0] if warm is not None else cc.run()[0]
-            # in the form run() takes them back (per spin case for unrestricted systems)
-            return omega, (cc.T1, cc.T2)
-        finally:
-            cc.release()
+    def _warm(self, req):
+        """Amplitudes of the finished solve of the same system and grid at the
+        temperature nearest to the request's (log Theta), or None."""
+        if not self.use_warm:
+            return None
+        kept = self.cache.get(req.key())
+        if not kept:
+            return None
+        th = min(kept, key=lambda t: abs(numpy.log(t) - numpy.log(req.theta)))
+        return kept[th]
+
+    def _keep(self, req, amps):
+        if amps is None:
+            return
+        self.cache.setdefault(req.key(), {})[req.theta] = amps
+        total = sum(_nbytes(a) for k in self.cache.values() for a in k.values())
+        while total > self.warm_bytes and self.cache:
+            # drop the oldest kept solve
+            k = next(iter(self.cache))
+            th = next(iter(self.cache[k]))
+            total -= _nbytes(self.cache[k].pop(th))
+            if not self.cache[k]:
+                del self.cache[k]
 
     def serve(self, requests):
         """Run the stream; returns the report (see `report`)."""
-        reqs = sorted(requests, key=lambda r: r.arrival)
+        be = self.backend()
+        pending = sorted(requests, key=lambda r: r.arrival)
+        budget = self._budget()
         t0 = self.clock()
-        done = []
-        for r in reqs:
+        active, done, used = [], [], 0
+        fps = {}
+        rounds = 0
+        max_active = 0
+        while pending or active:
             now = self.clock() - t0
-            if now < r.arrival:
-                self.sleep(r.arrival - now)
-            start = self.clock() - t0
-            if self.footprint(r) > self._budget():
-                done.append({"rid": r.rid, "ok": False, "arrival": r.arrival, "start": start,
-                             "end": start, "reason": "footprint above the memory budget"})
+            # admit: arrived, a free slot, and room in the memory budget
+            while pending and pending[0].arrival <= now and len(active) < self.slots:
+                r = pending[0]
+                fp = be.footprint(r, self.precision)
+                if fp > budget:
+                    pending.pop(0)
+                    done.append({"rid": r.rid, "ok": False, "arrival": r.arrival,
+                                 "start": now, "end": now,
+                                 "reason": "footprint above the memory budget"})
+                    continue
+                if used + fp > budget:
+                    break                 # waits for memory to free up
+                pending.pop(0)
+                warm = self._warm(r)
+                sv = Solve(r, self.levels, self.levels[-1], self.conv, now, warm is not None)
+                be.open(sv, warm)
+                fps[r.rid] = fp
+                used += fp
+                active.append(sv)
+            max_active = max(max_active, len(active))
+            if not active:
+                if pending:
+                    self.sleep(max(0.0, pending[0].arrival - (self.clock() - t0)))
                 continue
-            warm = self.cache.get(r.key())
-            omega, amps = self.solve(r, warm)
-            end = self.clock() - t0
-            if amps is not None and _nbytes(amps) <= self.warm_bytes:
-                self.cache[r.key()] = amps
-            done.append({"rid": r.rid, "ok": True, "arrival": r.arrival, "start": start,
-                         "end": end, "warm": warm is not None, "omega": omega})
-        return report(done, self.clock() - t0)
+            # one round: a sweep of every active solve, overlapped on the device
+            failed = {}
+            for sv in active:
+                try:
+                    be.begin(sv, self.damp)
+                except Exception as e:
+                    failed[sv.req.rid] = str(e)
+            finished = []
+            for sv in active:
+                if sv.req.rid in failed:
+                    finished.append(sv)
+                    continue
+                try:
+                    E, res = be.end(sv)
+                except Exception as e:            # e.g. a diverging solve
+                    failed[sv.req.rid] = str(e)
+                    finished.append(sv)
+                    continue
+                if sv.advance(E, res):
+                    finished.append(sv)
+            rounds += 1
+            for sv in finished:
+                active.remove(sv)
+                bad = failed.get(sv.req.rid)
+                omega, amps = be.close(sv, keep=self.use_warm and bad is None)
+                end = self.clock() - t0
+                used -= fps.pop(sv.req.rid)
+                if bad is not None:
+                    done.append({"rid": sv.req.rid, "ok": False, "arrival": sv.req.arrival,
+                                 "start": sv.start, "end": end, "reason": bad})
+                    continue
+                if amps is not None and _nbytes(amps) <= self.warm_bytes:
+                    self._keep(sv.req, amps)
+                done.append({"rid": sv.req.rid, "ok": True, "arrival": sv.req.arrival,
+                             "start": sv.start, "end": end, "warm": sv.warm,
+                             "omega": omega, "omega_cc": sv.omega_cc,
+                             "iterations": sv.iterations, "converged": sv.converged})
+        rep = report(done, self.clock() - t0)
+        rep.update({"slots": self.slots, "rounds": rounds, "max_active": max_active})
+        return rep
 
 
 def _nbytes(x):

@@ -231,13 +231,17 @@ class HubbardRing(object):
     U couples opposite spins only: F_pp = e_p + (U/L) N_other spin,
     E1 = (U/L) N_alpha N_beta)."""
 
-    def __init__(self, T, sites, t=1.0, U=4.0, mu=0.0, device_build=False):
+    def __init__(self, T, sites, t=1.0, U=4.0, mu=0.0, device_build=False, shift=0.0):
         self.T = T
         self.device_build = device_build
         self.L = sites
         self.t = t
         self.U = U
         self.mu = mu
+        # orbital energies e_k = eps_k + shift: shift = U n with n the
+        # reference density per site and spin gives the mean-field orbitals
+        # of Kelvin's HubbardSystem (hubbard_system.py:48-73), 0 the bare band
+        self.shift = float(shift)
         k = numpy.arange(sites)
         self.ek = -2.0 * t * numpy.cos(2.0 * numpy.pi * k / sites)
         self._eri = None
@@ -256,7 +260,7 @@ class HubbardRing(object):
         return 0.0
 
     def g_energies_tot(self):
-        return numpy.hstack((self.ek, self.ek))
+        return numpy.hstack((self.ek, self.ek)) + self.shift
 
     def g_aint_tot(self):
         if self._eri is None:
@@ -286,16 +290,20 @@ class HubbardRing(object):
         if self.device_build:
             L = self.L
             na, nb = fo[:L].sum(), fo[L:].sum()
-            return numpy.diag(self.g_energies_tot() + (self.U / L) *
+            return numpy.diag(numpy.hstack((self.ek, self.ek)) + (self.U / L) *
                               numpy.hstack((numpy.full(L, nb), numpy.full(L, na))))
-        return numpy.diag(self.g_energies_tot()) + numpy.einsum('prqr,r->pq', self.g_aint_tot(), fo)
+        h = numpy.diag(numpy.hstack((self.ek, self.ek)))
+        return h + numpy.einsum('prqr,r->pq', self.g_aint_tot(), fo)
 
     def get_mp1(self):
+        """sum_i (h_ii - e_i) f_i + 1/2 f W f (the first-order grand potential
+        of Kelvin's HubbardSystem.get_mp1, hubbard_system.py:120-133)."""
         fo = fermi(1.0 / self.T, self.g_energies_tot(), self.mu)
         if self.device_build:
             L = self.L
-            return (self.U / L) * fo[:L].sum() * fo[L:].sum()
-        return 0.5 * numpy.einsum('ijij,i,j->', self.g_aint_tot(), fo, fo)
+            return (self.U / L) * fo[:L].sum() * fo[L:].sum() - self.shift * fo.sum()
+        return (0.5 * numpy.einsum('ijij,i,j->', self.g_aint_tot(), fo, fo)
+                - self.shift * fo.sum())
 
 
 def ueg_recipe(N, rs, norb, theta, hf_shift=True, device_build=False):
@@ -313,3 +321,13 @@ def ueg_recipe(N, rs, norb, theta, hf_shift=True, device_build=False):
 def hubbard_recipe(sites, t, U, beta, device_build=False):
     """Half-filled Hubbard ring at inverse temperature beta (mu = 0)."""
     return HubbardRing(1.0 / beta, sites, t=t, U=U, mu=0.0, device_build=device_build)
+
+
+def hubbard_mf_recipe(sites, t, U, beta, device_build=False):
+    """Half-filled Hubbard ring in the mean-field momentum basis of Kelvin's
+    HubbardSystem: the uniform reference density 1/2 per site and spin gives
+    e_k = -2t cos(2 pi k / sites) + U/2, and mu = U/2 fills half the band at
+    every temperature (the band is symmetric about U/2, so the Fock matrix
+    equals diag(e) and F - diag(e) vanishes)."""
+    return HubbardRing(1.0 / beta, sites, t=t, U=U, mu=0.5 * U, device_build=device_build,
+                       shift=0.5 * U)

@@ -167,16 +167,19 @@ def test_ueg19_fp64_tc_vs_kelvin_example(tc_ctx):
 
 
 def test_mixed_vs_fp64_on_benchmark_system(tc_ctx):
-    """UEG 14 e-, rs=4, 38 spin orbitals, ng=10: three digit levels plus two
-    FP64-accurate refinement sweeps stay within 1e-6 Ha per electron of FP64."""
+    """UEG 14 e-, rs=4, 38 spin orbitals, ng=10: the few-digit phases end
+    within 1e-6 Ha per electron of FP64, and the FP64-accurate refinement
+    sweeps then meet Kelvin's own test, landing on the FP64 answer."""
     s = systems.ueg_recipe(14, 4.0, 19, 0.5)
     kw = dict(T=s.T, mu=s.mu, max_iter=100, damp=0.5, ngrid=10, econv=1e-10, ctx=tc_ctx)
     ref = ccsd.ccsd(s, precision="fp64_tc", **kw)
     E64 = ref.run()[1]
     mix = ccsd.ccsd(s, precision="mixed", **kw)
     Emx = mix.run()[1]
-    assert mix.iterations_refine == 2
-    assert abs(Emx - E64) < 1e-6 * s.N
+    assert mix.converged and ref.converged
+    assert mix.phases[0][0] == 3 and mix.phases[-1][0] == 7
+    assert mix.iterations_refine >= 2
+    assert abs(Emx - E64) < 1e-9
     assert abs(mix.omega_low - E64) < 1e-6 * s.N
 
 

@@ -35,48 +35,108 @@ class FakeClock(object):
         self.t += dt
 
 
-def test_service_order_latency_admission_and_warm_starts():
+class FakeBackend(object):
+    """Solves whose energy after k sweeps of a phase is known: a request
+    converges after `sweeps[rid]` sweeps of its last phase (earlier phases
+    stall at once); a round of sweeps takes 1 s of the fake clock whatever
+    the number of active solves (their work overlaps)."""
+
+    def __init__(self, clock, footprints, sweeps):
+        self.clock = clock
+        self.fp = footprints
+        self.sweeps = sweeps
+        self.opened, self.open_now, self.max_open = [], 0, 0
+        self.begun = set()
+
+    def mem_total(self):
+        return 1000
+
+    def footprint(self, req, precision):
+        return self.fp[req.rid]
+
+    def open(self, sv, warm):
+        self.opened.append((sv.req.rid, None if warm is None else float(warm[0][0])))
+        self.open_now += 1
+        self.max_open = max(self.max_open, self.open_now)
+        sv.handle = {"k": 0}
+
+    def begin(self, sv, damp):
+        if not self.begun:
+            self.clock.t += 1.0
+        self.begun.add(sv.req.rid)
+
+    def end(self, sv):
+        self.begun.discard(sv.req.rid)
+        h = sv.handle
+        h["k"] += 1
+        last = sv.phase == len(sv.levels) - 1
+        if not last:
+            return -1.0, 1.0                        # no progress: stalls after 3 sweeps
+        left = self.sweeps[sv.req.rid] - sv.it_phase
+        return -0.01 * sv.req.rid - (1e-3 if left > 1 else 0.0), 1e-9
+
+    def close(self, sv, keep):
+        self.open_now -= 1
+        amps = (numpy.array([sv.req.theta]), numpy.array([float(sv.req.rid)]))
+        return sv.omega_cc, amps if keep else None
+
+
+def test_continuous_batching_admission_overlap_and_warm_starts():
     clock = FakeClock()
     R = serve.Request
     reqs = [R(0, 0.0, 'ueg', (14, 19, 4.0), 0.5, 10),
-            R(1, 0.1, 'ueg', (14, 19, 4.0), 1.0, 10),      # same system and grid: warm
-            R(2, 0.2, 'hubbard', (16, 4.0), 0.3, 40),      # too big: rejected
-            R(3, 5.0, 'ueg', (38, 33, 2.0), 0.2, 20)]      # arrives after the queue drains
-    calls = []
-
-    def solve(r, warm):
-        calls.append((r.rid, warm is not None))
-        clock.t += 1.0                                     # every solve takes 1 s
-        return -0.01 * r.rid, (numpy.zeros(4), numpy.zeros(8))
-
-    def footprint(r):
-        return 10 if r.kind == 'ueg' else 1000
-
-    srv = serve.Server(solve=solve, footprint=footprint, budget=100, clock=clock,
+            R(1, 0.5, 'ueg', (14, 19, 4.0), 2.0, 10),      # admitted while 0 runs
+            R(2, 0.6, 'hubbard', (16, 4.0), 0.3, 40),      # too big for the device
+            R(3, 0.7, 'ueg', (38, 33, 2.0), 0.2, 20),      # waits for memory
+            R(4, 40.0, 'ueg', (14, 19, 4.0), 0.6, 10)]     # warm: nearest of 0.5, 2.0
+    fp = {0: 300, 1: 300, 2: 2000, 3: 500, 4: 300}
+    be = FakeBackend(clock, fp, {0: 4, 1: 6, 3: 2, 4: 2})
+    srv = serve.Server(precision='mixed', slots=3, budget=900, backend=be, clock=clock,
                        sleep=clock.sleep)
     rep = srv.serve(reqs)
-    assert calls == [(0, False), (1, True), (3, False)]
-    assert rep["solves"] == 3 and rep["rejected"] == 1 and rep["warm_started"] == 1
     by = {d["rid"]: d for d in rep["requests"]}
-    assert by[0]["end"] == 1.0 and by[1]["start"] == 1.0 and by[1]["end"] == 2.0
-    assert by[3]["start"] == 5.0 and by[3]["end"] == 6.0   # waited for its arrival
-    lat = numpy.array([1.0, 1.9, 1.0]) * 1e3
-    assert abs(rep["p50_ms"] - numpy.percentile(lat, 50)) < 1e-9
-    assert abs(rep["p99_ms"] - numpy.percentile(lat, 99)) < 1e-9
-    assert abs(rep["solves_per_s"] - 3 / 6.0) < 1e-12
+    assert not by[2]["ok"] and "budget" in by[2]["reason"]
+    assert rep["solves"] == 4 and rep["rejected"] == 1
+    # 0 and 1 run together; 3 needs 500 more than the 600 they hold, so it
+    # starts only when 0 has finished
+    assert be.max_open == 2 and rep["max_active"] == 2
+    assert by[1]["start"] < by[0]["end"]
+    assert by[3]["start"] >= by[0]["end"]
+    # few-digit phases stall after 3 sweeps each (3 and 5 levels), then the
+    # last phase needs the request's sweeps plus Kelvin's second energy
+    assert by[0]["iterations"] == 3 + 3 + 4 and by[0]["converged"]
+    # warm start of 4 from the kept solve at the nearest temperature (0.5)
+    assert be.opened[-1] == (4, 0.5) and by[4]["warm"]
+    assert abs(by[4]["omega_cc"] - (-0.04)) < 1e-15
+    lat = [by[r]["end"] - by[r]["arrival"] for r in (0, 1, 3, 4)]
+    assert abs(rep["p50_ms"] - numpy.percentile(numpy.array(lat) * 1e3, 50)) < 1e-9
 
 
 def test_default_footprint_is_the_solver_footprint():
-    """Admission uses kvft_solver_footprint (host arithmetic, no device): it
-    grows with the spin orbitals and the grid, and a budget below every
-    request's footprint rejects the whole stream without solving."""
-    reqs = serve.request_stream(12, rate=20.0, seed=1)
-    srv = serve.Server(budget=1 << 20, solve=lambda r, w: (_ for _ in ()).throw(AssertionError),
-                       clock=FakeClock(), sleep=lambda dt: None)
+    """Admission uses kvft_solver_footprint (host arithmetic, no device) plus
+    the slot's workspace cap: it grows with the spin orbitals and the grid,
+    and a budget below every request's footprint rejects the whole stream
+    without solving."""
+    from kelvin_gb300 import _lib
+    be = serve.DeviceBackend.__new__(serve.DeviceBackend)
+    be.workspace_bytes = 1 << 30
     small = serve.Request(0, 0.0, 'ueg', (14, 19, 1.0), 1.0, 10)
     big = serve.Request(1, 0.0, 'ueg', (38, 57, 1.0), 1.0, 10)
     wide = serve.Request(2, 0.0, 'ueg', (38, 57, 1.0), 1.0, 40)
-    assert srv.footprint(small) < srv.footprint(big) < srv.footprint(wide)
-    assert srv.footprint(big) > 8 * 114 ** 4 * 10
+    f = lambda r: be.footprint(r, 'mixed')
+    assert f(small) < f(big) < f(wide)
+    assert f(big) > 8 * 114 ** 4 * 10 + (1 << 30)
+    assert f(small) == _lib.lib().kvft_solver_footprint(38, 10, _lib.PREC_MIXED) + (1 << 30)
+
+    class NoSolve(FakeBackend):
+        def footprint(self, req, precision):
+            return f(req)
+
+        def open(self, sv, warm):
+            raise AssertionError("nothing fits")
+    reqs = serve.request_stream(12, rate=20.0, seed=1)
+    clock = FakeClock()
+    srv = serve.Server(budget=1 << 20, backend=NoSolve(clock, {}, {}), clock=clock,
+                       sleep=clock.sleep)
     rep = srv.serve(reqs)
     assert rep["solves"] == 0 and rep["rejected"] == 12 and rep["p50_ms"] is None
