@@ -70,6 +70,10 @@ WORKLOADS = {
                    max_iter=100, step="iteration",
                    label="UEG 38 e-, rs=1, 57 plane waves (114 spin orbitals), Theta=0.25, "
                          "ng=20, damping 0.5, econv 1e-10"),
+    "ueg66": dict(N=14, rs=2.0, norb=33, theta=0.5, ng=16, damp=0.5, econv=1e-10,
+                  max_iter=100, step="iteration",
+                  label="UEG 14 e-, rs=2, 33 plane waves (66 spin orbitals), Theta=0.5, "
+                        "ng=16, damping 0.5, econv 1e-10"),
     "ueg38": dict(N=14, rs=4.0, norb=19, theta=0.5, ng=10, damp=0.5, econv=1e-10,
                   max_iter=100, step="solve",
                   label="UEG 14 e-, rs=4, 19 plane waves (38 spin orbitals), Theta=0.5, "
@@ -724,10 +728,15 @@ def run_serve(args):
     and p50/p99 latency, completion minus arrival."""
     from kelvin_gb300 import serve
     reqs = serve.request_stream(args.serve, rate=args.rate, seed=0)
-    rep = serve.Server(precision=args.precision).serve(reqs)
-    rep.pop("requests")
+    rep = serve.Server(precision=args.precision, slots=args.slots).serve(reqs)
+    done = rep.pop("requests")
+    fails = {}
+    for d in done:
+        if not d["ok"]:
+            k = d.get("reason", "")[:60]
+            fails[k] = fails.get(k, 0) + 1
     print(json.dumps(dict({"serve": args.serve, "rate_per_s": args.rate,
-                           "precision": args.precision}, **rep)))
+                           "precision": args.precision, "not_solved": fails}, **rep)))
     return 0
 
 
@@ -748,6 +757,7 @@ def main():
     ap.add_argument("--serve", type=int, default=0,
                     help="serve this many requests of a seeded Poisson stream")
     ap.add_argument("--rate", type=float, default=20.0, help="request rate of --serve (1/s)")
+    ap.add_argument("--slots", type=int, default=4, help="--serve: solves on the device at once")
     ap.add_argument("--esn", action="store_true",
                     help="E, S, N of the 66-spin-orbital UEG: Lambda route against differences")
     ap.add_argument("--quad", default="gl", choices=["gl", "lin"],

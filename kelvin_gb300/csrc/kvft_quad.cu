@@ -91,7 +91,7 @@ quad_kernel(QuadParams q, const double *__restrict__ tbar, const double *__restr
     double *G = ti + ng;
     double *cs = G + ng * ng, *g1 = cs + ng, *gd = g1 + ng;
     double *rk = gd + ng;                                  // [ng][QT]
-    double *tb = rk + ((q.uniform || q.full) ? 0 : ng * QT);   // [ng][QT]
+    double *tb = rk + (q.uniform ? 0 : ng * QT);           // [ng][QT]
     for (int k = threadIdx.x; k < ng; k += QT) ti[k] = ti_g[k];
     for (int k = threadIdx.x; k < ng * ng; k += QT) G[k] = G_g[k];
     for (int y = threadIdx.x; y < ng; y += QT) {
@@ -107,53 +107,6 @@ quad_kernel(QuadParams q, const double *__restrict__ tbar, const double *__restr
     const int t = threadIdx.x;
     auto element = [&](long long p) {
         const double d = denom(q, p, D, ev, eo);
-        if (q.full) {
-            // dense G (Gauss-Legendre): exp((ti[x]-ti[y]) d) for every pair,
-            // factorised about the grid's centre tc as E_x / E_y with
-            // E_x = exp((ti[x]-tc) d).  The scaled inputs u_x = E_x tbar_x
-            // and the E_x sit in this thread's two shared-memory columns;
-            // on a grid symmetric about tc (Gauss-Legendre nodes are)
-            // E_{ng-1-x} = 1 / E_x, so ng/2 exps and ng/2 divisions, then
-            // ng^2 FMAs, per element
-            const double tc = 0.5 * (ti[0] + ti[ng - 1]);
-            double *ec = tb + ng * QT;
-            const int nx = q.symmetric ? (ng + 1) / 2 : ng;
-            for (int x = 0; x < nx; x++) {
-                const double E = exp((ti[x] - tc) * d);
-                ec[x * QT + t] = E;
-                tb[x * QT + t] = E * tbar[(long long)x * q.P + p];
-                const int xm = ng - 1 - x;
-                if (q.symmetric && xm != x) {
-                    const double Ei = 1.0 / E;
-                    ec[xm * QT + t] = Ei;
-                    tb[xm * QT + t] = Ei * tbar[(long long)xm * q.P + p];
-                }
-            }
-            float f_diff = 0.f, f_norm = 0.f;
-            for (int y = 0; y < ng; y++) {
-                double acc = 0.0;
-                for (int x = 0; x < ng; x++) acc = fma(G[y * ng + x], tb[x * QT + t], acc);
-                const double Ty = q.symmetric ? acc * ec[(ng - 1 - y) * QT + t]
-                                              : acc / ec[y * QT + t];
-                if (MODE == 0) {
-                    out[(long long)y * q.P + p] = Ty;
-                } else {
-                    double *o = out + (long long)y * q.P + p;
-                    const double told = *o;
-                    const double df = Ty - told;
-                    const double nt = fma(oma, df, told);
-                    const float fd = abs_to_f32(df), fn = abs_to_f32(nt);
-                    f_diff = fmaf(fd, fd, f_diff);
-                    f_norm = fmaf(fn, fn, f_norm);
-                    *o = nt;
-                }
-            }
-            if (MODE == 1) {
-                s_diff += (double)f_diff;
-                s_norm += (double)f_norm;
-            }
-            return;
-        }
         // step factors r_k = exp((ti[k]-ti[k+1]) d)
         double r0 = 1.0;
         if (UNI) {
@@ -215,8 +168,8 @@ quad_kernel(QuadParams q, const double *__restrict__ tbar, const double *__restr
                     const double gyx = G[y * ng + x];
                     if (gyx != 0.0) Ty = fma(gyx * w, tb[x * QT + t], Ty);
                 }
-                // x > y: factor 1 (the reference's rule; `full` takes the
-                // factorised branch above)
+                // x > y: factor 1 (the reference's rule; dense grids with
+                // the exponential for every pair run quad_dense_kernel)
                 for (int x = y + 1; x < ng; x++) {
                     const double gyx = G[y * ng + x];
                     if (gyx != 0.0) Ty = fma(gyx, tb[x * QT + t], Ty);
@@ -273,6 +226,230 @@ quad_kernel(QuadParams q, const double *__restrict__ tbar, const double *__restr
             if (t < s) {
                 red[0][t] += red[0][t + s];
                 red[1][t] += red[1][t + s];
+            }
+            __syncthreads();
+        }
+        if (t == 0) {
+            partial[2 * blockIdx.x] = red[0][0];
+            partial[2 * blockIdx.x + 1] = red[1][0];
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Dense G (Gauss-Legendre grids; the backward Lambda integral):
+//     T_y = sum_x G[y,x] exp((ti[x]-ti[y]) d) tbar_x   for every x.
+// Factorised about the grid's centre tc, exp((ti[x]-ti[y]) d) = E_x / E_y with
+// E_x = exp((ti[x]-tc) d), so T_y = (1/E_y) sum_x G[y,x] u_x, u_x = E_x tbar_x.
+// GB300 has ~64x more FP32 than FP64 throughput, so:
+//   * no exponentials per element: d = e_a + e_b - e_i - e_j, and E_x, 1/E_y
+//     are products of a pair table of the virtual indices and one of the
+//     occupied indices (quad_tables_kernel, exps of the orbital energies);
+//   * the ng^2 sum runs in compensated FP32: u (scaled by a power of two to
+//     order one) and G split into FP32 high and low parts; the high products
+//     are summed with error-free two-sums and their rounding errors, the
+//     cross terms and the sum's errors go to a second FP32 accumulator
+//     (relative error ~1e-14 of sum |G u|, far inside the parity bounds).
+// An element whose factors leave the safe range (non-finite u, or a bound on
+// |T_y| near the FP64 limit), and every element when D is given explicitly,
+// takes the FP64 path: exps, E_{ng-1-x} = 1/E_x on a grid symmetric about tc,
+// and FP64 FMAs.
+// ---------------------------------------------------------------------------
+struct DenseTabs {
+    const double *v, *vi, *o, *oi;   // [ng][NL] / [ng][NR]: E and 1/E factors
+    long long NL, NR;                // p = l NR + r
+};
+
+// tables: v[x][l] = exp((ti[x]-tc)(e_a (+ e_b))), vi = its inverse,
+// o[x][r] = exp(-(ti[x]-tc)(e_i (+ e_j))), oi = its inverse; l = a (rank 1)
+// or a nv + b (rank 2), r = i or i no + j
+__global__ void quad_tables_kernel(int ng, int rank, int nv, int no, double tc,
+                                   const double *__restrict__ ti, const double *__restrict__ ev,
+                                   const double *__restrict__ eo, long long NL, long long NR,
+                                   double *__restrict__ tab) {
+    const long long per = NL + NR;
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < ng * per;
+         k += (long long)gridDim.x * blockDim.x) {
+        const int x = (int)(k / per);
+        const long long c = k - x * per;
+        const double dt = ti[x] - tc;
+        double e;
+        if (c < NL)
+            e = (rank == 2) ? ev[c / nv] + ev[c % nv] : ev[c];
+        else
+            e = (rank == 2) ? -(eo[(c - NL) / no] + eo[(c - NL) % no]) : -eo[c - NL];
+        const double f = exp(dt * e), fi = exp(-dt * e);
+        if (c < NL) {
+            tab[x * NL + c] = f;
+            tab[ng * NL + x * NL + c] = fi;
+        } else {
+            tab[2 * ng * NL + x * NR + (c - NL)] = f;
+            tab[2 * ng * NL + ng * NR + x * NR + (c - NL)] = fi;
+        }
+    }
+}
+
+// s + e == a + b exactly (FP32 round to nearest)
+__device__ __forceinline__ void two_sum_f(float a, float b, float &s, float &e) {
+    s = a + b;
+    const float bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(QT)
+quad_dense_kernel(QuadParams q, DenseTabs tb_, const double *__restrict__ tbar,
+                  const double *__restrict__ ti_g, const double *__restrict__ G_g,
+                  const double *__restrict__ D, const double *__restrict__ ev,
+                  const double *__restrict__ eo, double *out, double *__restrict__ partial) {
+    extern __shared__ double sm[];
+    const int ng = q.ng;
+    double *ti = sm;
+    double *G = ti + ng;                                   // [ng][ng] FP64
+    float *Gh = reinterpret_cast<float *>(G + ng * ng);    // [ng][ng] FP32 high part
+    float *Gl = Gh + ng * ng;                              //          low part
+    double *c0 = G + ng * ng + ng * ng;                    // [ng][QT]: u (FP64 or FP32 pair)
+    double *c1 = c0 + ng * QT;                             // [ng][QT]: E (FP64 path)
+    for (int k = threadIdx.x; k < ng; k += QT) ti[k] = ti_g[k];
+    for (int k = threadIdx.x; k < ng * ng; k += QT) {
+        const double g = G_g[k];
+        G[k] = g;
+        const float h = (float)g;
+        Gh[k] = h;
+        Gl[k] = (float)(g - (double)h);
+    }
+    __syncthreads();
+    const double oma = 1.0 - q.alpha;
+    const double tc = 0.5 * (ti[0] + ti[ng - 1]);
+    double s_diff = 0.0, s_norm = 0.0;
+    const int t = threadIdx.x;
+    float2 *uf = reinterpret_cast<float2 *>(c0);
+
+    auto emit = [&](long long p, int y, double Ty, float &f_diff, float &f_norm) {
+        if (MODE == 0) {
+            out[(long long)y * q.P + p] = Ty;
+        } else {
+            double *o = out + (long long)y * q.P + p;
+            const double told = *o;
+            const double df = Ty - told;
+            const double nt = fma(oma, df, told);
+            const float fd = abs_to_f32(df), fn = abs_to_f32(nt);
+            f_diff = fmaf(fd, fd, f_diff);
+            f_norm = fmaf(fn, fn, f_norm);
+            *o = nt;
+        }
+    };
+
+    auto element = [&](long long p) {
+        float f_diff = 0.f, f_norm = 0.f;
+        bool table = tb_.v != nullptr;
+        if (table) {
+            const long long l = p / tb_.NR;
+            const long long r = p - l * tb_.NR;
+            // u_x = E_x tbar_x and its scale
+            double umax = 0.0;
+            for (int x = 0; x < ng; x++) {
+                const double E = __ldg(tb_.v + x * tb_.NL + l) * __ldg(tb_.o + x * tb_.NR + r);
+                const double u = E * tbar[(long long)x * q.P + p];
+                c0[x * QT + t] = u;
+                umax = fmax(umax, fabs(u));          // fmax drops a NaN; the test below sees it
+                if (!(fabs(u) <= 1e300)) table = false;
+            }
+            double eimax = 0.0;
+            for (int y = 0; y < ng && table; y++) {
+                const double Ei = __ldg(tb_.vi + y * tb_.NL + l) * __ldg(tb_.oi + y * tb_.NR + r);
+                c1[y * QT + t] = Ei;
+                if (!(Ei <= 1e300)) table = false;
+                eimax = fmax(eimax, Ei);
+            }
+            // |T_y| <= ng max|G| umax max(1/E): keep well inside FP64
+            if (table && umax * eimax > 1e290 / (double)ng) table = false;
+            if (table) {
+                if (umax == 0.0) {
+                    for (int y = 0; y < ng; y++) emit(p, y, 0.0, f_diff, f_norm);
+                } else {
+                    const int k = ilogb(umax);
+                    for (int x = 0; x < ng; x++) {
+                        const double u = scalbn(c0[x * QT + t], -k);   // exact
+                        const float h = (float)u;
+                        uf[x * QT + t] = make_float2(h, (float)(u - (double)h));
+                    }
+                    for (int y = 0; y < ng; y++) {
+                        float s = 0.f, c = 0.f;
+                        const float *gh = Gh + y * ng, *gl = Gl + y * ng;
+                        for (int x = 0; x < ng; x++) {
+                            const float2 u = uf[x * QT + t];
+                            const float pr = gh[x] * u.x;
+                            const float pe = fmaf(gh[x], u.x, -pr);      // exact
+                            float s2, e2;
+                            two_sum_f(s, pr, s2, e2);
+                            s = s2;
+                            c += e2 + pe;
+                            c = fmaf(gh[x], u.y, c);
+                            c = fmaf(gl[x], u.x, c);
+                        }
+                        const double acc = scalbn((double)s + (double)c, k);
+                        emit(p, y, acc * c1[y * QT + t], f_diff, f_norm);
+                    }
+                }
+            }
+        }
+        if (!table) {
+            // FP64 path
+            const double d = denom(q, p, D, ev, eo);
+            const int nx = q.symmetric ? (ng + 1) / 2 : ng;
+            for (int x = 0; x < nx; x++) {
+                const double E = exp((ti[x] - tc) * d);
+                c1[x * QT + t] = E;
+                c0[x * QT + t] = E * tbar[(long long)x * q.P + p];
+                const int xm = ng - 1 - x;
+                if (q.symmetric && xm != x) {
+                    const double Ei = 1.0 / E;
+                    c1[xm * QT + t] = Ei;
+                    c0[xm * QT + t] = Ei * tbar[(long long)xm * q.P + p];
+                }
+            }
+            for (int y = 0; y < ng; y++) {
+                double acc = 0.0;
+                for (int x = 0; x < ng; x++) acc = fma(G[y * ng + x], c0[x * QT + t], acc);
+                const double Ty = q.symmetric ? acc * c1[(ng - 1 - y) * QT + t]
+                                              : acc / c1[y * QT + t];
+                emit(p, y, Ty, f_diff, f_norm);
+            }
+        }
+        if (MODE == 1) {
+            s_diff += (double)f_diff;
+            s_norm += (double)f_norm;
+        }
+    };
+    if (MODE == 1 && q.spin_half > 0) {
+        const int h = q.spin_half, n = q.no;
+        const long long rows = q.P / n;
+        const int lane = t % 32;
+        const long long tw = (long long)gridDim.x * (QT / 32);
+        for (long long u = blockIdx.x * (long long)(QT / 32) + t / 32; u < 2 * rows; u += tw) {
+            const long long rr = u >> 1;
+            const int jh = (int)(u & 1);
+            const int i = (int)(rr % n);
+            const long long ab = rr / n;
+            const int b = (int)(ab % n), a = (int)(ab / n);
+            if ((a >= h) + (b >= h) != (i >= h) + jh) continue;
+            for (int jj = lane; jj < h; jj += 32) element(rr * n + (long long)jh * h + jj);
+        }
+    } else {
+        for (long long p = blockIdx.x * (long long)QT + t; p < q.P;
+             p += (long long)gridDim.x * QT)
+            element(p);
+    }
+    if (MODE == 1) {
+        __shared__ double red[2][QT];
+        red[0][t] = s_diff;
+        red[1][t] = s_norm;
+        __syncthreads();
+        for (int st = QT / 2; st > 0; st >>= 1) {
+            if (t < st) {
+                red[0][t] += red[0][t + st];
+                red[1][t] += red[1][t + st];
             }
             __syncthreads();
         }
@@ -370,6 +547,69 @@ int grid_symmetric(int ng, const double *ti) {
 
 }  // namespace
 
+namespace {
+
+size_t dense_smem(int ng) {
+    return sizeof(double) * ((size_t)ng + 2 * (size_t)ng * ng + 2 * (size_t)ng * QT);
+}
+
+// The dense-G integral: pair tables of the orbital energies (when given),
+// then quad_dense_kernel; mode 1 also damps and reduces the two norms.
+int quad_dense_launch(kvft_ctx *ctx, int mode, QuadParams &q, const double *tbar,
+                      const double *ti, const double *hti, const double *G, const double *D,
+                      const double *ev, const double *eo, double *out, double *res) {
+    const int ng = q.ng;
+    DenseTabs tabs{nullptr, nullptr, nullptr, nullptr, 1, 1};
+    if (!D && ev && eo) {
+        const long long NL = q.rank == 2 ? (long long)q.nv * q.nv : q.nv;
+        const long long NR = q.rank == 2 ? (long long)q.no * q.no : q.no;
+        if (NL * NR == q.P) {
+            void *tp = nullptr;
+            KV_TRY(kv_scratch(ctx, "quad_tables", sizeof(double) * 2 * ng * (NL + NR), &tp));
+            double *tab = (double *)tp;
+            const double tc = 0.5 * (hti[0] + hti[ng - 1]);
+            const long long work = ng * (NL + NR);
+            const int gb = (int)std::max(1LL, std::min((work + 255) / 256, 4096LL));
+            quad_tables_kernel<<<gb, 256, 0, ctx->stream>>>(ng, q.rank, q.nv, q.no, tc, ti, ev,
+                                                            eo, NL, NR, tab);
+            KV_TRY(kv_launch_check(ctx, "quad_tables"));
+            tabs = DenseTabs{tab, tab + ng * NL, tab + 2 * ng * NL, tab + 2 * ng * NL + ng * NR,
+                             NL, NR};
+        }
+    }
+    const size_t smem = dense_smem(ng);
+    static bool attr_done = false;
+    if (!attr_done) {
+        const int mx = (int)dense_smem(MAXNG);
+        cudaFuncSetAttribute(quad_dense_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+        cudaFuncSetAttribute(quad_dense_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+        attr_done = true;
+    }
+    int per_sm = 1;
+    KV_CHECK(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                      &per_sm, mode == 0 ? (const void *)quad_dense_kernel<0>
+                                         : (const void *)quad_dense_kernel<1>,
+                      QT, smem));
+    const long long blocks = (q.P + QT - 1) / QT;
+    const int grid = (int)std::max(1LL, std::min(blocks, (long long)std::max(per_sm, 1) *
+                                                             ctx->sm_count));
+    KvProfScope prof(ctx, KV_CAT_QUAD, 8.0 * ng * (double)q.P * (mode == 0 ? 2 : 3));
+    if (mode == 0) {
+        quad_dense_kernel<0><<<grid, QT, smem, ctx->stream>>>(q, tabs, tbar, ti, G, D, ev, eo,
+                                                              out, nullptr);
+        return kv_launch_check(ctx, "quad_dense_kernel");
+    }
+    void *part = nullptr;
+    KV_TRY(kv_scratch(ctx, "quad_partial", sizeof(double) * 2 * grid, &part));
+    quad_dense_kernel<1><<<grid, QT, smem, ctx->stream>>>(q, tabs, tbar, ti, G, D, ev, eo, out,
+                                                          (double *)part);
+    KV_TRY(kv_launch_check(ctx, "quad_dense_update_kernel"));
+    reduce_pairs_kernel<<<1, 256, 0, ctx->stream>>>((const double *)part, grid, res);
+    return kv_launch_check(ctx, "reduce_pairs");
+}
+
+}  // namespace
+
 // Shared launcher.  ti/G are DEVICE pointers; hti/hG are host copies used for
 // the grid analysis.  MODE 1 requires `partial` (2 doubles per block) and
 // `res` (2 doubles) device buffers.
@@ -400,6 +640,7 @@ int kv_quad_launch(kvft_ctx *ctx, int mode, int ng, long long P, int rank, int n
     q.spin_half = (mode == 1 && rank == 2 && nv == no && nv == 2 * spin_half) ? spin_half : 0;
     analyse_grid(ng, hti, hG, full, &q.step, &q.uniform);
     q.symmetric = grid_symmetric(ng, hti);
+    if (full) return quad_dense_launch(ctx, mode, q, tbar, ti, hti, G, D, ev, eo, out, res);
     size_t smem = quad_smem(ng, q.uniform, q.step, q.full);
     long long blocks = (P + QT - 1) / QT;
     long long cap = (long long)ctx->sm_count * 16;

@@ -350,6 +350,7 @@ def report(done, wall):
     ok = [d for d in done if d["ok"]]
     lat = numpy.array([d["end"] - d["arrival"] for d in ok]) * 1e3
     return {"solves": len(ok), "rejected": len(done) - len(ok),
+            "converged": sum(1 for d in ok if d.get("converged", True)),
             "solves_per_s": len(ok) / wall if wall > 0 else 0.0,
             "p50_ms": float(numpy.percentile(lat, 50)) if len(lat) else None,
             "p99_ms": float(numpy.percentile(lat, 99)) if len(lat) else None,

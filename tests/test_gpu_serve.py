@@ -1,0 +1,35 @@
+"""Continuous batching on the GPU (kelvin_gb300.serve): requests that overlap
+on the device give the grand potential each gives alone, within the mixed
+form's stated tolerance (1e-6 Ha per electron)."""
+import pytest
+
+from kelvin_gb300 import serve
+
+pytestmark = pytest.mark.gpu
+
+
+def _requests():
+    R = serve.Request
+    return [R(0, 0.00, 'ueg', (14, 19, 4.0), 0.5, 10),
+            R(1, 0.00, 'hubbard', (12, 2.0), 0.8, 20),
+            R(2, 0.01, 'ueg', (14, 27, 2.0), 1.0, 10),
+            R(3, 0.02, 'hubbard', (8, 2.0), 1.0, 10),
+            R(4, 0.03, 'ueg', (14, 19, 1.5), 2.0, 20)]
+
+
+def test_results_alone_and_in_the_mix():
+    mix = serve.Server(precision='mixed', slots=3, warm=False, workspace_bytes=4 << 30)
+    rep = mix.serve(_requests())
+    assert rep["solves"] == 5 and rep["rejected"] == 0
+    assert rep["max_active"] >= 2                    # their iterations overlapped
+    by_mix = {d["rid"]: d for d in rep["requests"]}
+    alone = serve.Server(precision='mixed', slots=1, warm=False, workspace_bytes=4 << 30)
+    for r in _requests():
+        one = alone.serve([serve.Request(r.rid, 0.0, r.kind, r.params, r.theta, r.ng)])
+        d = one["requests"][0]
+        m = by_mix[r.rid]
+        assert d["ok"] and m["ok"] and d["converged"] and m["converged"]
+        N = r.system().N
+        assert abs(d["omega"] - m["omega"]) < 1e-6 * N, (r.rid, d["omega"], m["omega"])
+        # the same arithmetic in the same order: far below the bar
+        assert abs(d["omega"] - m["omega"]) < 1e-9, (r.rid, d["omega"], m["omega"])
