@@ -79,9 +79,9 @@ WORKLOADS = {
                   label="UEG 14 e-, rs=4, 19 plane waves (38 spin orbitals), Theta=0.5, "
                         "ng=10, damping 0.5, econv 1e-10"),
 }
-# per-launch DRAM traffic of the dominant kernel category, measured by ncu
-# on a small case and scaled to this workload: see profiles/ (read at run time
-# from the committed summary, so that a re-taken capture updates it)
+# DRAM / algorithmic byte ratios per kernel category, measured by ncu on a
+# small case (read at run time from the committed summary, so that a re-taken
+# capture updates them); roofline.traffic = ratio x live algorithmic bytes
 TRAFFIC_FILE = os.path.join(ROOT, "profiles", "traffic.json")
 STEP_EVENTS = 8     # first event slot of the per-step timings (at most 50 steps)
 
@@ -275,17 +275,22 @@ def run_reference(args, w):
     return 0
 
 
-def load_traffic(workload, precision, category):
-    """Per-launch DRAM bytes of a kernel category from the committed ncu
-    summary (small-case capture scaled to the workload), or None."""
+def load_traffic(precision, category, algorithmic_per_launch):
+    """Per-launch DRAM bytes of a kernel category: the DRAM / algorithmic
+    ratio measured by ncu on a small case (profiles/traffic.json) times this
+    run's algorithmic bytes per launch of the category; (bytes, how) or
+    (None, None) where no ratio was measured."""
     try:
         t = json.load(open(TRAFFIC_FILE))
     except (OSError, ValueError):
         return None, None
-    e = t.get(workload, {}).get(precision, {}).get(category)
-    if not e:
+    e = t.get(precision, {}).get(category)
+    if not e or not algorithmic_per_launch:
         return None, None
-    return e.get("bytes_per_launch"), e.get("how")
+    r = e["dram_per_algorithmic"]
+    return r * algorithmic_per_launch, (
+        "%.3f x the live algorithmic bytes per launch; the ratio is ncu's on %s"
+        % (r, t.get("measured_on", "a small case")))
 
 
 # ---------------------------------------------------------------------------
@@ -461,7 +466,9 @@ def run_gpu(args, w):
     cats = {c: roof(c) for c in prof}
     dom = max(prof, key=lambda c: prof[c][1])
     roofline = dict(cats[dom])
-    traffic, thow = load_traffic(args.workload, args.precision, dom)
+    nl_dom = prof[dom][0]
+    traffic, thow = load_traffic(args.precision, dom,
+                                 prof[dom][2] / nl_dom if nl_dom and dom != "gemm6" else None)
     roofline.update({
         "category": dom, "traffic": traffic,
         "traffic_unit": "bytes per launch (ncu dram__bytes_read.sum + dram__bytes_write.sum)"

@@ -364,6 +364,17 @@ int kvft_solver_device_amplitudes(kvft_solver *s, double **T1, double **T2);
  * through kvft_solver_device_amplitudes are the caller's to keep
  * spin-conserving. */
 int kvft_solver_set_spin_blocks(kvft_solver *s, int on, int *half);
+/* Acceleration of the amplitude iteration (no counterpart in Kelvin, whose
+ * loop is the damped update of cc_utils.py:131-173): m = 1..3 replaces the
+ * damped update x <- x + (1 - damp)(Phi(x) - x) by Anderson mixing of depth m
+ * with the same mixing factor, over an FP32 history of 2m + 1
+ * amplitude-sized arrays allocated here (the tau chunk is re-sized for the
+ * memory left); m = 0 restores Kelvin's update (the default).  Kelvin's
+ * residual measure and convergence test apply to the accelerated iterates;
+ * the fixed point is the same.  The history restarts when the contraction
+ * precision changes, after a guess or new amplitudes, and when the residual
+ * grows a hundredfold in one step. */
+int kvft_solver_set_acceleration(kvft_solver *s, int m);
 /* Lambda on the solver's resident integrals and amplitudes (the converged T
  * of its last solve): guess 1 forms Kelvin's starting Lambda in L1/L2, 2 its
  * unrestricted driver's, 0 keeps the one given; then kvft_lambda_solve

@@ -212,6 +212,12 @@ class DeviceSolver(object):
                                                    ctypes.byref(res)), "kvft_solver_step")
         return E.value, res.value
 
+    def set_acceleration(self, depth):
+        """Anderson mixing of the given depth (1-3) in place of Kelvin's damped
+        update; 0 restores the damped update."""
+        self.ctx.check(self.ctx.L.kvft_solver_set_acceleration(self.h, int(depth)),
+                       "kvft_solver_set_acceleration")
+
     def step_begin(self, damp):
         """Queue one iteration on the context's stream and return at once."""
         self.ctx.check(self.ctx.L.kvft_solver_step_begin(self.h, float(damp)),

@@ -186,8 +186,8 @@ class ccsd(object):
     def __init__(self, sys, T=0.0, mu=0.0, iprint=0, singles=True, econv=1e-8,
                  tconv=None, max_iter=40, damp=0.0, ngrid=10, realtime=False,
                  athresh=0.0, quad='lin', rt_iter="all", precision='fp64',
-                 digits=None, refine_sweeps=None, refine_digits=7, ladder=(5,), device=0,
-                 ctx=None):
+                 digits=None, refine_sweeps=None, refine_digits=7, ladder=(5,), accel=0,
+                 device=0, ctx=None):
         self.T = T
         self.mu = mu
         self.finite_T = T != 0
@@ -212,6 +212,8 @@ class ccsd(object):
         self.refine_sweeps = refine_sweeps
         self.refine_digits = refine_digits
         self.ladder = tuple(ladder)
+        # Anderson depth of the amplitude iteration (0: Kelvin's damped update)
+        self.accel = int(accel)
         if not sys.verify(self.T, self.mu):
             raise Exception("Sytem temperature inconsistent with CC temp")
         if not self.finite_T:
@@ -267,6 +269,8 @@ class ccsd(object):
                                               self.g, self.G)
         # a dense Gauss-Legendre G takes the exponential for every node pair
         solver.full = self.quad == 'gl'
+        if self.accel:
+            solver.set_acceleration(self.accel)
         self.solver = solver
         conv = {"econv": self.econv, "tconv": self.tconv, "max_iter": self.max_iter,
                 "damp": self.damp}

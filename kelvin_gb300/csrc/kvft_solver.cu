@@ -193,6 +193,15 @@ struct kvft_solver {
     double *hsc = nullptr;
     cudaEvent_t done = nullptr;
     bool pending = false;
+    // Anderson acceleration of the damped update (depth aa_m, 0: Kelvin's
+    // update): FP32 history of steps dX and residual changes dR in slots,
+    // the last residual, the Gram matrix of the dR, steps since a restart
+    int aa_m = 0;
+    float *aa_dX[3] = {}, *aa_dR[3] = {}, *aa_rprev = nullptr;
+    double aa_G[3][3] = {};
+    long long aa_k = 0;
+    int aa_prec = -1;
+    double aa_rr = 0.0;
     long long s1() const { return (long long)nv * no; }
     long long s2() const { return s1() * s1(); }
 };
@@ -224,7 +233,7 @@ int alloc_common(kvft_solver *s) {
     KV_TRY(salloc(s, sizeof(double) * s->ng * n2, &s->T2));
     KV_TRY(salloc(s, sizeof(double) * s->ng * n1, &s->T1b));
     KV_TRY(salloc(s, sizeof(double) * s->ng * n2, &s->T2b));
-    KV_TRY(salloc(s, sizeof(double) * 16, &s->dsc));
+    KV_TRY(salloc(s, sizeof(double) * 32, &s->dsc));
     return KVFT_OK;
 }
 
@@ -379,6 +388,140 @@ int finish_create(kvft_solver *s, kvft_solver **out) {
     return KVFT_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Anderson acceleration (type II) of the fixed-point map Phi (the amplitude
+// update ccsd_stanton) with mixing beta = 1 - damp:
+//     r_k = Phi(x_k) - x_k,
+//     x_{k+1} = x_k + beta r_k - sum_i gamma_i (dX_i + beta dR_i),
+// gamma minimising |r_k - sum_i gamma_i dR_i| over the last m pairs
+// dX_i = x_{i+1} - x_i, dR_i = r_{i+1} - r_i.  With no history the step is
+// Kelvin's damped update.  The history is FP32: dX is stored as the step
+// itself and dR from the FP64 residual minus the FP32 previous residual, so
+// each keeps its precision relative to its own size.  Two fused passes per
+// iteration over T1 and the spin-conserving elements of T2 (the rest stays
+// zero), with fixed-order block reductions.
+// ---------------------------------------------------------------------------
+struct AaSeg {
+    double *x;
+    const double *phi;
+    float *rprev;
+    float *dX[3], *dR[3];
+    long long P;        // elements per tau point
+    int ng;
+    int h, n;           // h > 0: T2 spin runs (P = n^4), else every element
+};
+constexpr int AA_T = 256;
+
+// index of the e-th visited element, or -1 past the end: spin-run
+// enumeration as in the quadrature's spin path (one warp per run)
+template <class F>
+__device__ __forceinline__ void aa_visit(const AaSeg &g, F f) {
+    const int t = threadIdx.x;
+    if (g.h > 0) {
+        const int h = g.h, n = g.n;
+        const long long rows = g.P / n;
+        const int lane = t % 32;
+        const long long tw = (long long)gridDim.x * (AA_T / 32);
+        for (long long u = blockIdx.x * (long long)(AA_T / 32) + t / 32; u < 2 * rows * g.ng;
+             u += tw) {
+            const long long y = u / (2 * rows), uu = u - y * 2 * rows;
+            const long long r = uu >> 1;
+            const int jh = (int)(uu & 1);
+            const int i = (int)(r % n);
+            const long long ab = r / n;
+            const int b = (int)(ab % n), a = (int)(ab / n);
+            if ((a >= h) + (b >= h) != (i >= h) + jh) continue;
+            for (int jj = lane; jj < h; jj += 32) f(y * g.P + r * n + (long long)jh * h + jj);
+        }
+    } else {
+        const long long tot = g.P * g.ng;
+        for (long long e = blockIdx.x * (long long)AA_T + t; e < tot;
+             e += (long long)gridDim.x * AA_T)
+            f(e);
+    }
+}
+
+template <int K>
+__device__ __forceinline__ void aa_block_sum(double (&v)[K], double *part) {
+    __shared__ double red[K][AA_T / 32];
+    const int lane = threadIdx.x % 32, w = threadIdx.x / 32;
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+        double a = v[k];
+        for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
+        if (lane == 0) red[k][w] = a;
+    }
+    __syncthreads();
+    if (threadIdx.x < K) {
+        double a = 0.0;
+        for (int q = 0; q < AA_T / 32; q++) a += red[threadIdx.x][q];
+        part[blockIdx.x * K + threadIdx.x] = a;
+    }
+}
+
+// pass A: r = Phi - x; with a pending pair, dR[jnew] = r - rprev; rprev = r;
+// sums <dR_i, dR_jnew>, <dR_i, r> over the valid slots, and <r, r>
+__global__ void __launch_bounds__(AA_T)
+aa_stats_kernel(AaSeg g, int nvalid, int slot0, int m, int jnew, double *part) {
+    double v[7] = {0, 0, 0, 0, 0, 0, 0};
+    aa_visit(g, [&](long long e) {
+        const double r = g.phi[e] - g.x[e];
+        if (jnew >= 0) g.dR[jnew][e] = (float)(r - (double)g.rprev[e]);
+        g.rprev[e] = (float)r;
+        const double dn = jnew >= 0 ? (double)g.dR[jnew][e] : 0.0;
+        for (int q = 0; q < nvalid; q++) {
+            const int i = (slot0 - q + m) % m;
+            const double di = (double)g.dR[i][e];
+            v[q] = fma(di, dn, v[q]);
+            v[3 + q] = fma(di, r, v[3 + q]);
+        }
+        v[6] = fma(r, r, v[6]);
+    });
+    aa_block_sum<7>(v, part);
+}
+
+// pass B: x += beta r - sum_q gamma_q (dX_i + beta dR_i); dX[jst] = the step;
+// sums |step|^2 and |x_new|^2
+__global__ void __launch_bounds__(AA_T)
+aa_update_kernel(AaSeg g, int nvalid, int slot0, int m, int jst, double beta, double g0,
+                 double g1, double g2, double *part) {
+    double v[2] = {0, 0};
+    const double gam[3] = {g0, g1, g2};
+    aa_visit(g, [&](long long e) {
+        const double x = g.x[e];
+        const double r = g.phi[e] - x;
+        double d = beta * r;
+        for (int q = 0; q < nvalid; q++) {
+            const int i = (slot0 - q + m) % m;
+            d -= gam[q] * ((double)g.dX[i][e] + beta * (double)g.dR[i][e]);
+        }
+        const double xn = x + d;
+        g.x[e] = xn;
+        g.dX[jst][e] = (float)d;
+        v[0] = fma(d, d, v[0]);
+        v[1] = fma(xn, xn, v[1]);
+    });
+    aa_block_sum<2>(v, part);
+}
+
+// out[k] = sum over blocks of part[b K + k] (fixed order)
+__global__ void aa_reduce_kernel(const double *__restrict__ part, int nb, int K,
+                                 double *__restrict__ out) {
+    __shared__ double red[256];
+    for (int k = 0; k < K; k++) {
+        double a = 0.0;
+        for (int b = threadIdx.x; b < nb; b += 256) a += part[b * K + k];
+        red[threadIdx.x] = a;
+        __syncthreads();
+        for (int s2 = 128; s2 > 0; s2 >>= 1) {
+            if (threadIdx.x < s2) red[threadIdx.x] += red[threadIdx.x + s2];
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) out[k] = red[0];
+        __syncthreads();
+    }
+}
+
 void destroy(kvft_solver *s) {
     for (void *p : s->allocs) cudaFree(p);
     if (s->hsc) cudaFreeHost(s->hsc);
@@ -515,6 +658,148 @@ int kvft_solver_destroy(kvft_solver *s) {
     return KVFT_OK;
 }
 
+namespace {
+
+// Solves (A + lambda I) g = t for the n <= 3 valid slots (Gaussian
+// elimination with partial pivoting); false if it is singular or not finite.
+bool aa_solve(int n, double A[3][3], double *t, double *g) {
+    double tr = 0.0;
+    for (int i = 0; i < n; i++) tr += A[i][i];
+    const double lam = 1e-12 * (tr > 0.0 ? tr : 1.0) / (n > 0 ? n : 1);
+    double M[3][4];
+    for (int i = 0; i < n; i++) {
+        for (int j = 0; j < n; j++) M[i][j] = A[i][j] + (i == j ? lam : 0.0);
+        M[i][3] = t[i];
+    }
+    for (int c = 0; c < n; c++) {
+        int pv = c;
+        for (int r = c + 1; r < n; r++)
+            if (std::fabs(M[r][c]) > std::fabs(M[pv][c])) pv = r;
+        if (!(std::fabs(M[pv][c]) > 0.0)) return false;
+        if (pv != c)
+            for (int j = 0; j < 4; j++) std::swap(M[c][j], M[pv][j]);
+        for (int r = c + 1; r < n; r++) {
+            const double f = M[r][c] / M[c][c];
+            for (int j = c; j < 4; j++) M[r][j] -= f * M[c][j];
+        }
+    }
+    for (int c = n - 1; c >= 0; c--) {
+        double v = M[c][3];
+        for (int j = c + 1; j < n; j++) v -= M[c][j] * g[j];
+        g[c] = v / M[c][c];
+        if (!std::isfinite(g[c])) return false;
+    }
+    return true;
+}
+
+void aa_segments(kvft_solver *s, AaSeg *g1, AaSeg *g2) {
+    const long long n1 = s->s1(), n2 = s->s2(), ng = s->ng;
+    *g1 = AaSeg{s->T1, s->T1b, s->aa_rprev, {}, {}, n1, s->ng, 0, 0};
+    *g2 = AaSeg{s->T2, s->T2b, s->aa_rprev + ng * n1, {}, {}, n2, s->ng,
+                (s->spin_on && s->spin_half > 0 && s->nv == s->no) ? s->spin_half : 0, s->no};
+    for (int i = 0; i < s->aa_m; i++) {
+        g1->dX[i] = s->aa_dX[i];
+        g1->dR[i] = s->aa_dR[i];
+        g2->dX[i] = s->aa_dX[i] + ng * n1;
+        g2->dR[i] = s->aa_dR[i] + ng * n1;
+    }
+}
+
+// grid and partial-sum buffer of one Anderson pass over a segment
+int aa_launch_grid(kvft_ctx *ctx, const AaSeg &g) {
+    const long long work = g.h > 0 ? g.P * g.ng * 3 / 8 : g.P * g.ng;
+    return (int)std::max(1LL, std::min((long long)ctx->sm_count * 8, (work + AA_T - 1) / AA_T));
+}
+
+// The accelerated iteration up to the queued scalars (as the damped one
+// leaves them for kvft_solver_step_end: |dT1|^2, |T1|^2, |dT2|^2, |T2|^2,
+// Omega_cc).  One host wait, for the least-squares coefficients.
+int aa_step_begin(kvft_solver *s, double damp) {
+    kvft_ctx *ctx = s->ctx;
+    if (!s->norms_valid) KV_TRY(refresh_norms(s));
+    KV_TRY(form_tbar(s));
+    // Phi(x) in place of tbar
+    KV_TRY(integrate(s, 0, 0.0, s->T1b, s->T2b, s->T1b, s->T2b, nullptr, nullptr));
+    const int prec = ctx->precision * 16 + ctx->digits;
+    if (prec != s->aa_prec) {          // a new precision is a new map: restart
+        s->aa_k = 0;
+        s->aa_prec = prec;
+    }
+    const int m = s->aa_m;
+    AaSeg g[2];
+    aa_segments(s, &g[0], &g[1]);
+    long long k = s->aa_k;
+    const int jnew = k >= 1 ? (int)((k - 1) % m) : -1;
+    int nvalid = (int)std::min<long long>(k, m);
+    const int gridA[2] = {aa_launch_grid(ctx, g[0]), aa_launch_grid(ctx, g[1])};
+    void *pp = nullptr;
+    KV_TRY(kv_scratch(ctx, "aa_partial",
+                      sizeof(double) * 7 * (size_t)(gridA[0] + gridA[1]), &pp));
+    double *part = (double *)pp;
+    {
+        KvProfScope prof(ctx, KV_CAT_ELEM,
+                         (double)(s->s1() + s->s2()) * s->ng * (28.0 + 4.0 * nvalid));
+        for (int q = 0; q < 2; q++) {
+            aa_stats_kernel<<<gridA[q], AA_T, 0, ctx->stream>>>(
+                g[q], nvalid, jnew < 0 ? 0 : jnew, m, jnew, part + (q ? 7 * gridA[0] : 0));
+            KV_TRY(kv_launch_check(ctx, "aa_stats"));
+            aa_reduce_kernel<<<1, 256, 0, ctx->stream>>>(part + (q ? 7 * gridA[0] : 0),
+                                                         gridA[q], 7, s->dsc + 8 + 7 * q);
+            KV_TRY(kv_launch_check(ctx, "aa_reduce"));
+        }
+    }
+    double st[14];
+    KV_CHECK(ctx, cudaMemcpyAsync(st, s->dsc + 8, sizeof(st), cudaMemcpyDeviceToHost,
+                                  ctx->stream));
+    KV_CHECK(ctx, cudaStreamSynchronize(ctx->stream));
+    const double rr = st[6] + st[13];
+    if (!std::isfinite(rr)) return kv_fail(ctx, KVFT_EDIVERGE, "non-finite residual");
+    double gam[3] = {0.0, 0.0, 0.0};
+    if (nvalid > 0 && rr > 100.0 * s->aa_rr) nvalid = 0;     // blew up: plain step, restart
+    if (nvalid > 0) {
+        int slot[3];
+        for (int q = 0; q < nvalid; q++) slot[q] = (jnew - q + m) % m;
+        for (int q = 0; q < nvalid; q++) {
+            s->aa_G[jnew][slot[q]] = s->aa_G[slot[q]][jnew] = st[q] + st[7 + q];
+        }
+        double A[3][3], t[3];
+        for (int q = 0; q < nvalid; q++) {
+            t[q] = st[3 + q] + st[10 + q];
+            for (int p2 = 0; p2 < nvalid; p2++) A[q][p2] = s->aa_G[slot[q]][slot[p2]];
+        }
+        if (!aa_solve(nvalid, A, t, gam)) nvalid = 0;
+    }
+    if (nvalid == 0) k = 0;                // restart the history from this step
+    const int jst = (int)(k % m);
+    const int slot0 = nvalid > 0 ? jnew : 0;
+    const double beta = 1.0 - damp;
+    const int gridB[2] = {gridA[0], gridA[1]};
+    {
+        KvProfScope prof(ctx, KV_CAT_ELEM,
+                         (double)(s->s1() + s->s2()) * s->ng * (28.0 + 8.0 * nvalid));
+        for (int q = 0; q < 2; q++) {
+            aa_update_kernel<<<gridB[q], AA_T, 0, ctx->stream>>>(
+                g[q], nvalid, slot0, m, jst, beta, gam[0], gam[1], gam[2],
+                part + (q ? 2 * gridB[0] : 0));
+            KV_TRY(kv_launch_check(ctx, "aa_update"));
+            aa_reduce_kernel<<<1, 256, 0, ctx->stream>>>(part + (q ? 2 * gridB[0] : 0),
+                                                         gridB[q], 2, s->dsc + 2 * q);
+            KV_TRY(kv_launch_check(ctx, "aa_reduce"));
+        }
+    }
+    s->aa_k = k + 1;
+    s->aa_rr = rr;
+    KV_TRY(kv_energy(ctx, s->ng, s->nv, s->no, s->T1, s->T2, s->F[1], s->I[5], s->g, s->beta, 1,
+                     s->dsc + 4, s->spin_on ? s->spin_half : 0));
+    KV_CHECK(ctx, cudaMemcpyAsync(s->hsc, s->dsc, 5 * sizeof(double), cudaMemcpyDeviceToHost,
+                                  ctx->stream));
+    KV_CHECK(ctx, cudaEventRecord(s->done, ctx->stream));
+    s->pending = true;
+    return KVFT_OK;
+}
+
+}  // namespace
+
 // One amplitude iteration queued on the context's stream without waiting:
 // update, integration + damping + norms, energy, and the copy of the five
 // scalars to pinned host memory.  kvft_solver_step_end waits for them.
@@ -523,6 +808,7 @@ int kvft_solver_step_begin(kvft_solver *s, double damp) {
     kvft_ctx *ctx = s->ctx;
     if (s->pending) return kv_fail(ctx, KVFT_EINVAL, "solver_step_begin: a step is pending");
     cudaSetDevice(ctx->device);
+    if (s->aa_m > 0) return aa_step_begin(s, damp);
     if (!s->norms_valid) KV_TRY(refresh_norms(s));
     KV_TRY(form_tbar(s));
     // integrate + damp in place: T <- damp T + (1-damp) int(tbar)
@@ -568,6 +854,7 @@ int kvft_solver_run(kvft_solver *s, const kvft_solve_opts *o, kvft_result *r) {
     if (o->full != 0 && o->full != 1) return kv_fail(ctx, KVFT_EINVAL, "solver: full must be 0 or 1");
     // the convention holds for this run and the steps that follow it
     s->full = o->full;
+    if (o->guess != 2) s->aa_k = 0;
     if (o->guess == 0) {
         KV_CHECK(ctx, cudaMemsetAsync(s->T1, 0, sizeof(double) * s->ng * s->s1(), ctx->stream));
         KV_CHECK(ctx, cudaMemsetAsync(s->T2, 0, sizeof(double) * s->ng * s->s2(), ctx->stream));
@@ -709,6 +996,7 @@ int kvft_solver_set_amplitudes(kvft_solver *s, const double *T1h, const double *
     KV_CHECK(s->ctx, cudaMemcpyAsync(s->T2, T2h, sizeof(double) * s->ng * s->s2(),
                                      cudaMemcpyHostToDevice, s->ctx->stream));
     s->norms_valid = false;
+    s->aa_k = 0;
     if (s->spin_half && s->spin_on) {
         // amplitudes from outside keep the spin blocks only if they conserve spin
         const double *arr[2] = {s->T1, s->T2};
@@ -804,6 +1092,39 @@ int kvft_solver_lambda_densities(kvft_solver *s, const double *L1, const double 
     for (int k = 0; k < 9; k++) I[k] = s->I[k];
     return kvft_lambda_densities(s->ctx, s->ng, s->nv, s->no, F, I, s->T1, s->T2, L1, L2, ev,
                                  eo, s->ti, s->g, s->G, Fg, Ig);
+}
+
+// Anderson depth m (0: Kelvin's damped update).  The FP32 history (2m + 1
+// arrays of the amplitudes' size) is allocated here, and the tau chunk is
+// sized again for the memory that is left.
+int kvft_solver_set_acceleration(kvft_solver *s, int m) {
+    if (!s || m < 0 || m > 3) return kv_fail(s ? s->ctx : nullptr, KVFT_EINVAL,
+                                             "solver_set_acceleration: depth must be 0..3");
+    if (s->pending) return kv_fail(s->ctx, KVFT_EINVAL, "solver_set_acceleration: a step is pending");
+    cudaSetDevice(s->ctx->device);
+    const size_t words = (size_t)s->ng * (s->s1() + s->s2());
+    auto falloc = [&](float **p) -> int {
+        if (*p) return KVFT_OK;
+        void *q = nullptr;
+        if (cudaMalloc(&q, sizeof(float) * words) != cudaSuccess) {
+            cudaGetLastError();
+            return kv_fail(s->ctx, KVFT_ENOMEM, "solver_set_acceleration: no room for the history");
+        }
+        s->allocs.push_back(q);
+        *p = (float *)q;
+        return KVFT_OK;
+    };
+    if (m > 0) {
+        KV_TRY(falloc(&s->aa_rprev));
+        for (int i = 0; i < m; i++) {
+            KV_TRY(falloc(&s->aa_dX[i]));
+            KV_TRY(falloc(&s->aa_dR[i]));
+        }
+        s->chunk_prec = -1;            // re-size the tau chunk for the memory left
+    }
+    s->aa_m = m;
+    s->aa_k = 0;
+    return KVFT_OK;
 }
 
 int kvft_solver_set_spin_blocks(kvft_solver *s, int on, int *half) {
