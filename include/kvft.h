@@ -375,6 +375,16 @@ int kvft_solver_set_spin_blocks(kvft_solver *s, int on, int *half);
  * precision changes, after a guess or new amplitudes, and when the residual
  * grows a hundredfold in one step. */
 int kvft_solver_set_acceleration(kvft_solver *s, int m);
+/* CUDA graphs for the damped iteration (no counterpart in Kelvin): on = 1
+ * runs one eager step with the current settings, captures the next step's
+ * launches into a graph and replays it from then on (launch overhead of the
+ * several hundred launches of an iteration goes away, which matters for
+ * small systems); a change of damping, precision, spin blocks, grid
+ * convention or of any scratch buffer starts over.  A capture that fails
+ * leaves the solver eager.  Profiling (kvft_profile_begin) and Anderson
+ * acceleration run eagerly.  on = 0 turns it off, -1 leaves it; *state (may
+ * be NULL): 2 replaying, -1 a capture failed, 0 otherwise. */
+int kvft_solver_set_graph(kvft_solver *s, int on, int *state);
 /* Lambda on the solver's resident integrals and amplitudes (the converged T
  * of its last solve): guess 1 forms Kelvin's starting Lambda in L1/L2, 2 its
  * unrestricted driver's, 0 keeps the one given; then kvft_lambda_solve

@@ -115,6 +115,7 @@ _SIGS = {
     "kvft_set_workspace_limit": (ctypes.c_int, [vp, ctypes.c_size_t]),
     "kvft_solver_step_begin": (ctypes.c_int, [vp, ctypes.c_double]),
     "kvft_solver_set_acceleration": (ctypes.c_int, [vp, ctypes.c_int]),
+    "kvft_solver_set_graph": (ctypes.c_int, [vp, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]),
     "kvft_solver_step_end": (ctypes.c_int, [vp, c_double_p, c_double_p]),
     "kvft_mem_info": (ctypes.c_int, [vp, ctypes.POINTER(ctypes.c_size_t),
                                      ctypes.POINTER(ctypes.c_size_t)]),

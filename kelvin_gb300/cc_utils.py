@@ -218,6 +218,16 @@ class DeviceSolver(object):
         self.ctx.check(self.ctx.L.kvft_solver_set_acceleration(self.h, int(depth)),
                        "kvft_solver_set_acceleration")
 
+    def set_graph(self, on=None):
+        """CUDA-graph replay of the damped iteration (True / False; None
+        leaves it); returns the state: 2 replaying, -1 a capture failed, 0
+        otherwise."""
+        st = ctypes.c_int()
+        flag = -1 if on is None else int(bool(on))
+        self.ctx.check(self.ctx.L.kvft_solver_set_graph(self.h, flag, ctypes.byref(st)),
+                       "kvft_solver_set_graph")
+        return st.value
+
     def step_begin(self, damp):
         """Queue one iteration on the context's stream and return at once."""
         self.ctx.check(self.ctx.L.kvft_solver_step_begin(self.h, float(damp)),

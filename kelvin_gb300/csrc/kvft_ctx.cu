@@ -21,6 +21,7 @@ int kv_cuda(kvft_ctx *ctx, cudaError_t e, const char *what) {
 void kv_pack_cache_clear(kvft_ctx *ctx) {
     for (auto &kv : ctx->pack_cache) cudaFree(kv.second.first);
     ctx->pack_cache.clear();
+    ctx->scratch_gen++;
 }
 
 int kv_launch_check(kvft_ctx *ctx, const char *what) {
@@ -50,6 +51,7 @@ int kv_scratch(kvft_ctx *ctx, const char *key, size_t bytes, void **p) {
         *p = q;
         return KVFT_OK;
     }
+    ctx->scratch_gen++;
     if (it != ctx->scratch.end()) {
         KV_CHECK(ctx, cudaStreamSynchronize(ctx->stream));
         cudaFree(it->second.first);

@@ -126,6 +126,9 @@ struct kvft_ctx {
     // cap on the bytes a solver's tau-chunk workspace may take on this
     // context (0: 60% of the free memory), so that several solvers fit
     size_t workspace_limit = 0;
+    // bumped whenever a scratch or cached buffer is (re)allocated or freed:
+    // a captured CUDA graph holds the addresses it saw
+    uint64_t scratch_gen = 0;
 };
 struct KvSpinScope {
     kvft_ctx *ctx;

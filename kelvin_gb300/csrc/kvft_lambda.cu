@@ -911,7 +911,8 @@ extern "C" int kvft_lambda_solve(kvft_ctx *ctx, int ng, int nv, int no,
         }
     }
     *iters = it;
-    return KVFT_OK;
+    // a tensor-core wait that expired during the iteration
+    return ctx->dry ? KVFT_OK : kv_device_status(ctx);
 }
 
 // Kelvin's starting Lambda (ft_cc_equations.py:502-512; unrestricted:

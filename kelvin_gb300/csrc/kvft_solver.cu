@@ -12,6 +12,8 @@
 // undamped T never touches HBM.
 #include "kvft_internal.h"
 
+#include <cstring>
+
 #include <cmath>
 #include <cstdio>
 #include <vector>
@@ -202,6 +204,23 @@ struct kvft_solver {
     long long aa_k = 0;
     int aa_prec = -1;
     double aa_rr = 0.0;
+    // CUDA graph of the damped iteration: on when graph_on; gexec replays the
+    // launches captured for gkey (damping, precision, spin blocks, grid
+    // convention, scratch generation); gwarm: the key of the last eager step
+    struct GKey {
+        double damp = -1.0;
+        int prec = -1, spin = -1, full = -1;
+        uint64_t gen = 0;
+        bool operator==(const GKey &o) const {
+            return damp == o.damp && prec == o.prec && spin == o.spin && full == o.full &&
+                   gen == o.gen;
+        }
+    };
+    int graph_on = 0;
+    int graph_state = 0;        // 0 eager, 2 replaying, -1 capture failed (eager from then)
+    cudaGraphExec_t gexec = nullptr;
+    GKey gkey, gwarm;
+    uint64_t glaunches = 0;
     long long s1() const { return (long long)nv * no; }
     long long s2() const { return s1() * s1(); }
 };
@@ -523,6 +542,7 @@ __global__ void aa_reduce_kernel(const double *__restrict__ part, int nb, int K,
 }
 
 void destroy(kvft_solver *s) {
+    if (s->gexec) cudaGraphExecDestroy(s->gexec);
     for (void *p : s->allocs) cudaFree(p);
     if (s->hsc) cudaFreeHost(s->hsc);
     if (s->done) cudaEventDestroy(s->done);
@@ -660,6 +680,17 @@ int kvft_solver_destroy(kvft_solver *s) {
 
 namespace {
 
+// The step's five scalars and the device status word of the bounded waits
+// (a tensor-core wait that expired) into pinned host memory, on the stream.
+int queue_readback(kvft_solver *s) {
+    kvft_ctx *ctx = s->ctx;
+    KV_CHECK(ctx, cudaMemcpyAsync(s->hsc, s->dsc, 5 * sizeof(double), cudaMemcpyDeviceToHost,
+                                  ctx->stream));
+    KV_CHECK(ctx, cudaMemcpyAsync(s->hsc + 15, ctx->dflag, sizeof(int), cudaMemcpyDeviceToHost,
+                                  ctx->stream));
+    return KVFT_OK;
+}
+
 // Solves (A + lambda I) g = t for the n <= 3 valid slots (Gaussian
 // elimination with partial pivoting); false if it is singular or not finite.
 bool aa_solve(int n, double A[3][3], double *t, double *g) {
@@ -791,10 +822,83 @@ int aa_step_begin(kvft_solver *s, double damp) {
     s->aa_rr = rr;
     KV_TRY(kv_energy(ctx, s->ng, s->nv, s->no, s->T1, s->T2, s->F[1], s->I[5], s->g, s->beta, 1,
                      s->dsc + 4, s->spin_on ? s->spin_half : 0));
-    KV_CHECK(ctx, cudaMemcpyAsync(s->hsc, s->dsc, 5 * sizeof(double), cudaMemcpyDeviceToHost,
-                                  ctx->stream));
+    KV_TRY(queue_readback(s));
     KV_CHECK(ctx, cudaEventRecord(s->done, ctx->stream));
     s->pending = true;
+    return KVFT_OK;
+}
+
+}  // namespace
+
+namespace {
+
+// The damped iteration's launches on the context's stream: update,
+// integration + damping + norms, energy, read-back of the scalars.
+int enqueue_damped(kvft_solver *s, double damp) {
+    kvft_ctx *ctx = s->ctx;
+    KV_TRY(form_tbar(s));
+    // integrate + damp in place: T <- damp T + (1-damp) int(tbar)
+    KV_TRY(integrate(s, 1, damp, s->T1b, s->T2b, s->T1, s->T2, s->dsc + 0, s->dsc + 2));
+    KV_TRY(kv_energy(ctx, s->ng, s->nv, s->no, s->T1, s->T2, s->F[1], s->I[5], s->g, s->beta, 1,
+                     s->dsc + 4, s->spin_on ? s->spin_half : 0));
+    return queue_readback(s);
+}
+
+kvft_solver::GKey graph_key(kvft_solver *s, double damp) {
+    kvft_solver::GKey k;
+    k.damp = damp;
+    k.prec = s->ctx->precision * 16 + s->ctx->digits;
+    k.spin = s->spin_on ? s->spin_half : 0;
+    k.full = s->full;
+    k.gen = s->ctx->scratch_gen;
+    return k;
+}
+
+// The damped iteration through a CUDA graph: an eager step with these
+// settings first (it sizes every scratch buffer and fills the packed-integral
+// cache), then one step captured and launched, then replays.  A capture
+// that fails (or that would allocate) leaves the solver eager.
+int graph_step(kvft_solver *s, double damp) {
+    kvft_ctx *ctx = s->ctx;
+    const kvft_solver::GKey k = graph_key(s, damp);
+    if (s->gexec && !(k == s->gkey)) {
+        cudaGraphExecDestroy(s->gexec);
+        s->gexec = nullptr;
+    }
+    if (s->gexec) {
+        KV_CHECK(ctx, cudaGraphLaunch(s->gexec, ctx->stream));
+        ctx->launches += s->glaunches;
+        return KVFT_OK;
+    }
+    if (!(k == s->gwarm)) {
+        KV_TRY(enqueue_damped(s, damp));
+        s->gwarm = graph_key(s, damp);
+        return KVFT_OK;
+    }
+    const uint64_t l0 = ctx->launches, gen0 = ctx->scratch_gen;
+    bool ok = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeRelaxed) == cudaSuccess;
+    int st = ok ? enqueue_damped(s, damp) : KVFT_OK;
+    cudaGraph_t g = nullptr;
+    if (ok) ok = cudaStreamEndCapture(ctx->stream, &g) == cudaSuccess && g != nullptr;
+    ok = ok && st == KVFT_OK && ctx->scratch_gen == gen0;
+    if (ok) ok = cudaGraphInstantiate(&s->gexec, g, 0) == cudaSuccess;
+    if (g) cudaGraphDestroy(g);
+    const uint64_t captured = ctx->launches - l0;
+    ctx->launches = l0;                // nothing ran during the capture
+    if (!ok) {
+        cudaGetLastError();
+        if (s->gexec) cudaGraphExecDestroy(s->gexec);
+        s->gexec = nullptr;
+        s->graph_state = -1;
+        s->graph_on = 0;
+        ctx->err.clear();
+        return enqueue_damped(s, damp);
+    }
+    s->gkey = k;
+    s->glaunches = captured;
+    s->graph_state = 2;
+    KV_CHECK(ctx, cudaGraphLaunch(s->gexec, ctx->stream));
+    ctx->launches += captured;
     return KVFT_OK;
 }
 
@@ -810,13 +914,10 @@ int kvft_solver_step_begin(kvft_solver *s, double damp) {
     cudaSetDevice(ctx->device);
     if (s->aa_m > 0) return aa_step_begin(s, damp);
     if (!s->norms_valid) KV_TRY(refresh_norms(s));
-    KV_TRY(form_tbar(s));
-    // integrate + damp in place: T <- damp T + (1-damp) int(tbar)
-    KV_TRY(integrate(s, 1, damp, s->T1b, s->T2b, s->T1, s->T2, s->dsc + 0, s->dsc + 2));
-    KV_TRY(kv_energy(ctx, s->ng, s->nv, s->no, s->T1, s->T2, s->F[1], s->I[5], s->g, s->beta, 1,
-                     s->dsc + 4, s->spin_on ? s->spin_half : 0));
-    KV_CHECK(ctx, cudaMemcpyAsync(s->hsc, s->dsc, 5 * sizeof(double), cudaMemcpyDeviceToHost,
-                                  ctx->stream));
+    if (s->graph_on && !(ctx->prof && ctx->prof->on))
+        KV_TRY(graph_step(s, damp));
+    else
+        KV_TRY(enqueue_damped(s, damp));
     KV_CHECK(ctx, cudaEventRecord(s->done, ctx->stream));
     s->pending = true;
     return KVFT_OK;
@@ -831,6 +932,13 @@ int kvft_solver_step_end(kvft_solver *s, double *energy, double *res) {
     s->pending = false;
     KV_CHECK(ctx, cudaEventSynchronize(s->done));
     const double *h = s->hsc;
+    int flag = 0;
+    std::memcpy(&flag, h + 15, sizeof(int));
+    if (flag != 0) {
+        KV_CHECK(ctx, cudaMemsetAsync(ctx->dflag, 0, sizeof(int), ctx->stream));
+        return kv_fail(ctx, KVFT_ETIMEOUT, "solver step: a bounded device wait expired (code " +
+                                               std::to_string(flag) + ")");
+    }
     const double res1 = std::sqrt(h[0]) / s->nl1;
     const double res2 = std::sqrt(h[2]) / s->nl2;
     s->nl1 = std::sqrt(h[1]) + 0.1;
@@ -974,6 +1082,7 @@ int kvft_solver_run_point(kvft_solver *s, const kvft_solve_opts *o, kvft_result 
     r->iterations = total;
     r->converged = all_conv;
     s->norms_valid = false;
+    KV_TRY(kv_device_status(ctx));     // a tensor-core wait that expired
     return all_conv ? KVFT_OK : KVFT_ENOTCONV;
 }
 
@@ -1124,6 +1233,26 @@ int kvft_solver_set_acceleration(kvft_solver *s, int m) {
     }
     s->aa_m = m;
     s->aa_k = 0;
+    return KVFT_OK;
+}
+
+// CUDA graphs for the damped iteration: on = 1 / 0, -1 leaves it; *state
+// (may be NULL): 2 when a captured graph is being replayed, -1 when a capture
+// failed (the solver then runs eagerly), 0 otherwise.
+int kvft_solver_set_graph(kvft_solver *s, int on, int *state) {
+    if (!s || on < -1 || on > 1) return kv_fail(s ? s->ctx : nullptr, KVFT_EINVAL,
+                                                "solver_set_graph: bad argument");
+    if (on >= 0) {
+        s->graph_on = on;
+        if (!on && s->gexec) {
+            cudaSetDevice(s->ctx->device);
+            cudaStreamSynchronize(s->ctx->stream);
+            cudaGraphExecDestroy(s->gexec);
+            s->gexec = nullptr;
+        }
+        if (on && s->graph_state < 0) s->graph_state = 0;
+    }
+    if (state) *state = s->gexec ? 2 : s->graph_state < 0 ? -1 : 0;
     return KVFT_OK;
 }
 

@@ -1206,6 +1206,7 @@ int pack(kvft_ctx *ctx, const char *key, const PackView &v, int R, int K, int nb
         if (cudaMemGetInfo(&fr, &tot) == cudaSuccess && fr > bytes + tot / 10 &&
             cudaMalloc(&buf, bytes) == cudaSuccess) {
             ctx->pack_cache[ckey] = {buf, bytes};
+            ctx->scratch_gen++;
         } else {
             cudaGetLastError();
             buf = nullptr;

@@ -133,9 +133,11 @@ class Solve(object):
 
 class DeviceBackend(object):
     """Solves on the GPU: one context (CUDA stream) per slot, each with its
-    tau-chunk workspace capped so that the slots share the device."""
+    tau-chunk workspace capped so that the slots share the device, and each
+    solve's iterations captured once and replayed as a CUDA graph."""
 
-    def __init__(self, slots, workspace_bytes, device=0):
+    def __init__(self, slots, workspace_bytes, device=0, graphs=True):
+        self.graphs = graphs
         self.free_ctx = [_lib.Context(device) for _ in range(slots)]
         for c in self.free_ctx:
             c.set_workspace_limit(workspace_bytes)
@@ -168,6 +170,8 @@ class DeviceBackend(object):
             solver.guess(2)
         else:
             solver.guess(1)
+        if self.graphs:
+            solver.set_graph(True)        # iterations replayed as CUDA graphs
         sv.handle = (ctx, solver, s)
         sv.level_set = sv.level()
 
@@ -211,12 +215,13 @@ class Server(object):
 
     def __init__(self, precision='mixed', slots=4, budget=None, backend=None,
                  clock=time.perf_counter, sleep=time.sleep, warm_bytes=8 << 30, warm=True,
-                 damp=0.5, econv=1e-8, max_iter=200, workspace_bytes=24 << 30):
+                 damp=0.5, econv=1e-8, max_iter=200, workspace_bytes=24 << 30, graphs=True):
         self.precision = precision
         self.slots = slots
         self.budget = budget
         self._backend = backend
         self.workspace_bytes = workspace_bytes
+        self.graphs = graphs
         self.clock, self.sleep = clock, sleep
         self.warm_bytes = warm_bytes
         self.use_warm = warm
@@ -228,7 +233,7 @@ class Server(object):
 
     def backend(self):
         if self._backend is None:
-            self._backend = DeviceBackend(self.slots, self.workspace_bytes)
+            self._backend = DeviceBackend(self.slots, self.workspace_bytes, graphs=self.graphs)
         return self._backend
 
     def _budget(self):

@@ -33,3 +33,30 @@ def test_results_alone_and_in_the_mix():
         assert abs(d["omega"] - m["omega"]) < 1e-6 * N, (r.rid, d["omega"], m["omega"])
         # the same arithmetic in the same order: far below the bar
         assert abs(d["omega"] - m["omega"]) < 1e-9, (r.rid, d["omega"], m["omega"])
+
+
+def test_graph_replay_matches_eager(ctx):
+    """A solve whose iterations are replayed as a CUDA graph gives the eager
+    solve's grand potential, and the graph is in use."""
+    from kelvin_gb300 import _lib, systems
+    from kelvin_gb300.cc_utils import DeviceSolver, iterate
+    from kelvin_gb300.quadrature import ft_quad
+    s = systems.ueg_recipe(14, 4.0, 19, 0.5)
+    beta = 1.0 / s.T
+    ti, g, G = ft_quad(10, beta, 'lin')
+    conv = {"econv": 1e-10, "tconv": 1e-7, "max_iter": 100, "damp": 0.5}
+    out = {}
+    for graph in (False, True):
+        ctx.set_precision(_lib.PREC_FP64_TC, 7)
+        sv = DeviceSolver.from_system(ctx, s.g_energies_tot(), s.g_fock_tot(), s.g_aint_tot(),
+                                      beta, s.mu, ti, g, G)
+        try:
+            sv.guess(1)
+            sv.set_graph(graph)
+            out[graph] = (iterate(sv, conv), sv.iterations, sv.set_graph())
+        finally:
+            sv.close()
+            ctx.set_precision(_lib.PREC_FP64, 7)
+    assert out[True][2] == 2 and out[False][2] == 0
+    assert out[True][1] == out[False][1]
+    assert abs(out[True][0] - out[False][0]) < 1e-12
