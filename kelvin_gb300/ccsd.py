@@ -186,7 +186,7 @@ class ccsd(object):
     def __init__(self, sys, T=0.0, mu=0.0, iprint=0, singles=True, econv=1e-8,
                  tconv=None, max_iter=40, damp=0.0, ngrid=10, realtime=False,
                  athresh=0.0, quad='lin', rt_iter="all", precision='fp64',
-                 digits=None, refine_sweeps=None, refine_digits=7, ladder=(5,), accel=0,
+                 digits=None, refine_sweeps=None, refine_digits=7, ladder=None, accel=0,
                  device=0, ctx=None):
         self.T = T
         self.mu = mu
@@ -211,9 +211,13 @@ class ccsd(object):
         # until Kelvin's test passes, at most refine_sweeps (None: max_iter)
         self.refine_sweeps = refine_sweeps
         self.refine_digits = refine_digits
-        self.ladder = tuple(ladder)
         # Anderson depth of the amplitude iteration (0: Kelvin's damped update)
         self.accel = int(accel)
+        # intermediate digit levels of the mixed form: with Kelvin's damped
+        # update a 5-level phase shortens the FP64-accurate one; with Anderson
+        # mixing (whose history restarts at every change of precision) going
+        # straight from 3 to 7 levels takes fewer sweeps
+        self.ladder = tuple(ladder) if ladder is not None else ((5,) if not accel else ())
         if not sys.verify(self.T, self.mu):
             raise Exception("Sytem temperature inconsistent with CC temp")
         if not self.finite_T:

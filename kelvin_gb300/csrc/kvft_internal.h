@@ -129,6 +129,23 @@ struct kvft_ctx {
     // bumped whenever a scratch or cached buffer is (re)allocated or freed:
     // a captured CUDA graph holds the addresses it saw
     uint64_t scratch_gen = 0;
+    // Packed operands shared by the products of one spin-blocked contraction
+    // (on inside KvTPackScope): key -> pool slot; the slots' buffers are
+    // scratch kept for the next contraction.
+    bool tpack_on = false;
+    std::map<std::string, int> tpack;
+};
+struct KvTPackScope {
+    kvft_ctx *ctx;
+    bool prev;
+    explicit KvTPackScope(kvft_ctx *c) : ctx(c), prev(c->tpack_on) {
+        c->tpack_on = true;
+        if (!prev) c->tpack.clear();
+    }
+    ~KvTPackScope() {
+        ctx->tpack_on = prev;
+        if (!prev) ctx->tpack.clear();
+    }
 };
 struct KvSpinScope {
     kvft_ctx *ctx;

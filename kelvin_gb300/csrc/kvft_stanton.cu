@@ -76,6 +76,8 @@ int spin_gemm(kvft_ctx *ctx, int h, int batch, double alpha, const KMat &A, cons
             if (v.size[s.comp] != 2 * h)
                 return kv_fail(ctx, KVFT_EINVAL, "spin blocks: index extent is not 2h");
         }
+    // products that share an operand sub-block share its digit planes
+    KvTPackScope tpack(ctx);
     bool zeroed = false;
     if (beta == 0.0 && cwords > 0) {
         KV_CHECK(ctx, cudaMemsetAsync(C.p, 0, sizeof(double) * cwords, ctx->stream));

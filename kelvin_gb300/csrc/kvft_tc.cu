@@ -40,6 +40,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <cstdlib>
 #include <mutex>
 
 namespace {
@@ -66,6 +67,7 @@ struct TcParams {
     const int *ea, *eb;   // row exponents of A / column exponents of B
     int ea_bst, eb_bst;
     double alpha, beta;
+    int rmw1;             // beta = 1 by load-add-store (tiles owned by one CTA)
     int alpha_pow2;       // alpha = +-2^alpha_exp: folded into the exponent field
     int alpha_exp;
     unsigned alpha_sign;  // sign bit of alpha (bit 31 of the FP64 high word)
@@ -579,7 +581,7 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
                     if (!p.alpha_pow2) v *= p.alpha;
                     return v;
                 };
-                if (p.nsplit > 1 || p.beta == 1.0) {
+                if (p.nsplit > 1 || (p.beta == 1.0 && !p.rmw1)) {
                     // C += value: each element gets exactly one addition in
                     // this launch unless K chunks run as separate units, so a
                     // fire-and-forget reduction at L2 gives old + value
@@ -1212,6 +1214,20 @@ int pack(kvft_ctx *ctx, const char *key, const PackView &v, int R, int K, int nb
             buf = nullptr;
         }
     }
+    if (!buf && !v.stable && ctx->tpack_on) {
+        // an operand sub-block already packed for an earlier product of the
+        // same spin-blocked contraction
+        ckey = pack_key(v, R, K, nb, S);
+        auto it = ctx->tpack.find(ckey);
+        const int slot = (it != ctx->tpack.end()) ? it->second : (int)ctx->tpack.size();
+        char sk[32];
+        snprintf(sk, sizeof sk, "tpack%d", slot);
+        KV_TRY(kv_scratch(ctx, sk, bytes, &buf));
+        out->planes = (__nv_bfloat16 *)buf;
+        out->ex = (int *)((uint8_t *)buf + pbytes);
+        if (it != ctx->tpack.end()) return KVFT_OK;
+        ctx->tpack[ckey] = slot;
+    }
     if (!buf) KV_TRY(kv_scratch(ctx, key, bytes, &buf));
     out->planes = (__nv_bfloat16 *)buf;
     out->ex = (int *)((uint8_t *)buf + pbytes);
@@ -1331,6 +1347,14 @@ int gemm_tc_run(kvft_ctx *ctx, int M, int N, int K, int batch, double alpha, con
     p.eb_bst = (nbB > 1) ? pb.R : 0;
     p.alpha = alpha;
     p.beta = par ? 1.0 : beta;
+    {
+        static const int rmw_env = [] {
+            const char *e = std::getenv("KVFT_EPILOGUE_RMW");
+            return e ? std::atoi(e) : 0;
+        }();
+        // 1: every exclusively owned beta = 1 tile; 2: those with K <= 64
+        p.rmw1 = !par && (rmw_env == 1 || (rmw_env == 2 && K <= 64));
+    }
     {
         int ex2 = 0;
         const double fr = std::frexp(alpha, &ex2);
