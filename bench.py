@@ -484,6 +484,12 @@ def run_gpu(args, w):
                        for c in cats if cats[c]},
         "breakdown_ms_per_step": {c: round(prof[c][1] / args.steps, 3) for c in prof}})
 
+    # mixed against FP64-accurate on the 38-spin-orbital configuration as well,
+    # with E and S from the Lambda equations (Kelvin's Simpson grid, on which
+    # they are built): a few seconds
+    if mixed and not per_solve:
+        cfg["accuracy_38_spin_orbitals"] = small_accuracy(ctx, args.accel)
+
     # CPU baseline: a bounded sample of the oracle's iteration (guess and three
     # iterations of the 38-spin-orbital solve) on the host cores
     t_guess, times, _, _ = oracle_c1_iterations(args.quad, 3, until_converged=False)
@@ -689,6 +695,28 @@ def run_esn(args):
     out["dN"] = out["lambda"]["N"] - out["fd"]["N"]
     print(json.dumps(out))
     return 0
+
+
+def small_accuracy(ctx, accel):
+    """|dOmega|, |dE|, |dS| of the mixed form (as benchmarked) against Kelvin's
+    damped FP64-accurate solve: UEG 14 electrons, rs = 4, 19 plane waves,
+    Theta = 0.5, ng = 10 (Simpson), E and S from the Lambda equations."""
+    from kelvin_gb300 import _lib, ccsd as kccsd, systems
+    s = systems.ueg_recipe(14, 4.0, 19, 0.5, device_build=True)
+    out = {}
+    for prec, acc in (("fp64_tc", 0), ("mixed", accel)):
+        cc = kccsd.ccsd(s, T=s.T, mu=s.mu, max_iter=200, damp=0.5, ngrid=10, econv=1e-10,
+                        precision=prec, accel=acc, ctx=ctx)
+        try:
+            Om = cc.run()[0]
+            E, S, N = cc.compute_ESN(method="lambda")
+            out[prec] = (Om, E, S)
+        finally:
+            cc.release()
+            ctx.set_precision(_lib.PREC_FP64, 7)
+    (o0, e0, s0), (o1, e1, s1) = out["fp64_tc"], out["mixed"]
+    return {"abs_dOmega": abs(o1 - o0), "abs_dE": abs(e1 - e0), "abs_dS": abs(s1 - s0),
+            "electrons": 14, "grid": "Simpson, ng = 10"}
 
 
 def run_accuracy(args):
