@@ -194,7 +194,7 @@ quad_kernel(QuadParams q, const double *__restrict__ tbar, const double *__restr
             s_norm += (double)f_norm;
         }
     };
-    if (MODE == 1 && q.spin_half > 0) {
+    if (q.spin_half > 0) {
         // spin blocks: only the spin-conserving elements move (the others
         // are zero and stay zero); each (a, b, i) row holds them as one run
         // of h consecutive j or none, and one warp takes one run
@@ -422,7 +422,7 @@ quad_dense_kernel(QuadParams q, DenseTabs tb_, const double *__restrict__ tbar,
             s_norm += (double)f_norm;
         }
     };
-    if (MODE == 1 && q.spin_half > 0) {
+    if (q.spin_half > 0) {
         const int h = q.spin_half, n = q.no;
         const long long rows = q.P / n;
         const int lane = t % 32;
@@ -637,7 +637,9 @@ int kv_quad_launch(kvft_ctx *ctx, int mode, int ng, long long P, int rank, int n
     q.no = no;
     q.full = full;
     q.alpha = alpha;
-    q.spin_half = (mode == 1 && rank == 2 && nv == no && nv == 2 * spin_half) ? spin_half : 0;
+    // spin blocks: only the spin-conserving elements are integrated (the
+    // solver's passes, which read no other; callers pass 0 otherwise)
+    q.spin_half = (rank == 2 && nv == no && nv == 2 * spin_half) ? spin_half : 0;
     analyse_grid(ng, hti, hG, full, &q.step, &q.uniform);
     q.symmetric = grid_symmetric(ng, hti);
     if (full) return quad_dense_launch(ctx, mode, q, tbar, ti, hti, G, D, ev, eo, out, res);

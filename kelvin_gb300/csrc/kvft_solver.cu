@@ -478,19 +478,33 @@ __device__ __forceinline__ void aa_block_sum(double (&v)[K], double *part) {
     }
 }
 
-// pass A: r = Phi - x; with a pending pair, dR[jnew] = r - rprev; rprev = r;
-// sums <dR_i, dR_jnew>, <dR_i, r> over the valid slots, and <r, r>
+// The history pointers of one pass, newest first (q = 0 .. NV-1), resolved
+// on the host so that the kernels index nothing at run time.
+struct AaHist {
+    const float *dX[3];
+    const float *dR[3];
+    float *dRnew;        // pass A: the slot completed now (null: none)
+    float *dXst;         // pass B: the slot the step goes to
+};
+
+// pass A: r = Phi - x; dRnew = r - rprev; rprev = r; sums <dR_q, dRnew>,
+// <dR_q, r> over the NV valid slots, and <r, r>
+template <int NV>
 __global__ void __launch_bounds__(AA_T)
-aa_stats_kernel(AaSeg g, int nvalid, int slot0, int m, int jnew, double *part) {
+aa_stats_kernel(AaSeg g, AaHist hs, double *part) {
     double v[7] = {0, 0, 0, 0, 0, 0, 0};
     aa_visit(g, [&](long long e) {
         const double r = g.phi[e] - g.x[e];
-        if (jnew >= 0) g.dR[jnew][e] = (float)(r - (double)g.rprev[e]);
+        double dn = 0.0;
+        if (hs.dRnew) {
+            const float d = (float)(r - (double)g.rprev[e]);
+            hs.dRnew[e] = d;
+            dn = (double)d;
+        }
         g.rprev[e] = (float)r;
-        const double dn = jnew >= 0 ? (double)g.dR[jnew][e] : 0.0;
-        for (int q = 0; q < nvalid; q++) {
-            const int i = (slot0 - q + m) % m;
-            const double di = (double)g.dR[i][e];
+#pragma unroll
+        for (int q = 0; q < NV; q++) {
+            const double di = (q == 0 && hs.dRnew) ? dn : (double)hs.dR[q][e];
             v[q] = fma(di, dn, v[q]);
             v[3 + q] = fma(di, r, v[3 + q]);
         }
@@ -499,24 +513,24 @@ aa_stats_kernel(AaSeg g, int nvalid, int slot0, int m, int jnew, double *part) {
     aa_block_sum<7>(v, part);
 }
 
-// pass B: x += beta r - sum_q gamma_q (dX_i + beta dR_i); dX[jst] = the step;
+// pass B: x += beta r - sum_q gamma_q (dX_q + beta dR_q); dXst = the step;
 // sums |step|^2 and |x_new|^2
+template <int NV>
 __global__ void __launch_bounds__(AA_T)
-aa_update_kernel(AaSeg g, int nvalid, int slot0, int m, int jst, double beta, double g0,
-                 double g1, double g2, double *part) {
+aa_update_kernel(AaSeg g, AaHist hs, double beta, double g0, double g1, double g2,
+                 double *part) {
     double v[2] = {0, 0};
     const double gam[3] = {g0, g1, g2};
     aa_visit(g, [&](long long e) {
         const double x = g.x[e];
         const double r = g.phi[e] - x;
         double d = beta * r;
-        for (int q = 0; q < nvalid; q++) {
-            const int i = (slot0 - q + m) % m;
-            d -= gam[q] * ((double)g.dX[i][e] + beta * (double)g.dR[i][e]);
-        }
+#pragma unroll
+        for (int q = 0; q < NV; q++)
+            d -= gam[q] * ((double)hs.dX[q][e] + beta * (double)hs.dR[q][e]);
         const double xn = x + d;
         g.x[e] = xn;
-        g.dX[jst][e] = (float)d;
+        hs.dXst[e] = (float)d;
         v[0] = fma(d, d, v[0]);
         v[1] = fma(xn, xn, v[1]);
     });
@@ -749,7 +763,8 @@ int aa_step_begin(kvft_solver *s, double damp) {
     kvft_ctx *ctx = s->ctx;
     if (!s->norms_valid) KV_TRY(refresh_norms(s));
     KV_TRY(form_tbar(s));
-    // Phi(x) in place of tbar
+    // Phi(x) in place of tbar (spin-conserving elements only: the passes
+    // below read no other)
     KV_TRY(integrate(s, 0, 0.0, s->T1b, s->T2b, s->T1b, s->T2b, nullptr, nullptr));
     const int prec = ctx->precision * 16 + ctx->digits;
     if (prec != s->aa_prec) {          // a new precision is a new map: restart
@@ -771,8 +786,20 @@ int aa_step_begin(kvft_solver *s, double damp) {
         KvProfScope prof(ctx, KV_CAT_ELEM,
                          (double)(s->s1() + s->s2()) * s->ng * (28.0 + 4.0 * nvalid));
         for (int q = 0; q < 2; q++) {
-            aa_stats_kernel<<<gridA[q], AA_T, 0, ctx->stream>>>(
-                g[q], nvalid, jnew < 0 ? 0 : jnew, m, jnew, part + (q ? 7 * gridA[0] : 0));
+            AaHist hs{};
+            for (int t = 0; t < nvalid; t++) {
+                const int i = (jnew - t + m) % m;
+                hs.dX[t] = g[q].dX[i];
+                hs.dR[t] = g[q].dR[i];
+            }
+            hs.dRnew = jnew >= 0 ? g[q].dR[jnew] : nullptr;
+            double *pq = part + (q ? 7 * gridA[0] : 0);
+            switch (nvalid) {
+            case 0: aa_stats_kernel<0><<<gridA[q], AA_T, 0, ctx->stream>>>(g[q], hs, pq); break;
+            case 1: aa_stats_kernel<1><<<gridA[q], AA_T, 0, ctx->stream>>>(g[q], hs, pq); break;
+            case 2: aa_stats_kernel<2><<<gridA[q], AA_T, 0, ctx->stream>>>(g[q], hs, pq); break;
+            default: aa_stats_kernel<3><<<gridA[q], AA_T, 0, ctx->stream>>>(g[q], hs, pq); break;
+            }
             KV_TRY(kv_launch_check(ctx, "aa_stats"));
             aa_reduce_kernel<<<1, 256, 0, ctx->stream>>>(part + (q ? 7 * gridA[0] : 0),
                                                          gridA[q], 7, s->dsc + 8 + 7 * q);
@@ -809,9 +836,32 @@ int aa_step_begin(kvft_solver *s, double damp) {
         KvProfScope prof(ctx, KV_CAT_ELEM,
                          (double)(s->s1() + s->s2()) * s->ng * (28.0 + 8.0 * nvalid));
         for (int q = 0; q < 2; q++) {
-            aa_update_kernel<<<gridB[q], AA_T, 0, ctx->stream>>>(
-                g[q], nvalid, slot0, m, jst, beta, gam[0], gam[1], gam[2],
-                part + (q ? 2 * gridB[0] : 0));
+            AaHist hs{};
+            for (int t = 0; t < nvalid; t++) {
+                const int i = (slot0 - t + m) % m;
+                hs.dX[t] = g[q].dX[i];
+                hs.dR[t] = g[q].dR[i];
+            }
+            hs.dXst = g[q].dX[jst];
+            double *pq = part + (q ? 2 * gridB[0] : 0);
+            switch (nvalid) {
+            case 0:
+                aa_update_kernel<0><<<gridB[q], AA_T, 0, ctx->stream>>>(g[q], hs, beta, gam[0],
+                                                                       gam[1], gam[2], pq);
+                break;
+            case 1:
+                aa_update_kernel<1><<<gridB[q], AA_T, 0, ctx->stream>>>(g[q], hs, beta, gam[0],
+                                                                       gam[1], gam[2], pq);
+                break;
+            case 2:
+                aa_update_kernel<2><<<gridB[q], AA_T, 0, ctx->stream>>>(g[q], hs, beta, gam[0],
+                                                                       gam[1], gam[2], pq);
+                break;
+            default:
+                aa_update_kernel<3><<<gridB[q], AA_T, 0, ctx->stream>>>(g[q], hs, beta, gam[0],
+                                                                       gam[1], gam[2], pq);
+                break;
+            }
             KV_TRY(kv_launch_check(ctx, "aa_update"));
             aa_reduce_kernel<<<1, 256, 0, ctx->stream>>>(part + (q ? 2 * gridB[0] : 0),
                                                          gridB[q], 2, s->dsc + 2 * q);
