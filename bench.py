@@ -753,7 +753,8 @@ def run_accuracy(args):
             try:
                 cc.run()
                 E, S, N = cc.compute_ESN(method="lambda" if quad == "lin" else "fd")
-                res[prec] = {"omega": cc.Gtot, "omega_low": cc.omega_low, "E": E, "S": S,
+                res[prec] = {"omega": cc.Gtot, "omega_cc": cc.Gcc, "omega_low": cc.omega_low,
+                             "E": E, "S": S,
                              "N": N, "iterations": cc.iterations + cc.iterations_refine,
                              "phases": getattr(cc, "phases", None),
                              "converged": bool(cc.converged),
@@ -768,7 +769,7 @@ def run_accuracy(args):
                "mixed": b}
         if "error" not in a and "error" not in b:
             row.update({"abs_dOmega": abs(b["omega"] - a["omega"]),
-                        "abs_dOmega_low_phases": abs(b["omega_low"] - a["omega"]),
+                        "abs_dOmega_low_phases": abs(b["omega_low"] - a["omega_cc"]),
                         "abs_dE": abs(b["E"] - a["E"]), "abs_dS": abs(b["S"] - a["S"])})
         out.append(row)
         print(json.dumps(row), flush=True)
