@@ -492,9 +492,12 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
         for (int u = blockIdx.x; u < p.units && ok; u += gridDim.x) {
             const Unit w = unit_of(p, u, TN);
             if (w.kb0 >= w.kb1) continue;
-            // C addresses of this unit; with beta != 0 the old values are
-            // prefetched into L2 now, while the MMAs run, so the read-modify-
-            // write below is not bound by the few loads a warp keeps in flight
+            // C addresses of this unit; for the read-modify-write of a
+            // general beta the old values are prefetched into L2 now, while
+            // the MMAs run, so that it is not bound by the few loads a warp
+            // keeps in flight (the L2 reductions of beta = 1 fetch their lines
+            // at L2 themselves: prefetching them too cost 6 of 82 ms per
+            // 114-spin-orbital iteration in issue slots)
             const int nw = w.n0 + h * WCOLS;          // first column of this warp
             for (int i = lane; i < WCOLS; i += 32) {
                 const int n = nw + i;
@@ -507,7 +510,7 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
             double *Cr = p.C.p + (long long)w.b * p.C.bst + (m < p.M ? p.C.r.off(m) : 0);
             const int krow =
                 (m < p.M) ? exp_of(p.ea[(long long)w.b * p.ea_bst + m]) - 14 + p.alpha_exp : 0;
-            if (m < p.M && p.nsplit == 1 && p.beta != 0.0) {
+            if (m < p.M && p.nsplit == 1 && p.beta != 0.0 && p.beta != 1.0) {
                 for (int i = 0; i < min(WCOLS, nlim); i++)
                     asm volatile("prefetch.global.L2 [%0];" ::"l"(Cr + coff[i]));
             }
