@@ -484,12 +484,6 @@ def run_gpu(args, w):
                        for c in cats if cats[c]},
         "breakdown_ms_per_step": {c: round(prof[c][1] / args.steps, 3) for c in prof}})
 
-    # mixed against FP64-accurate on the 38-spin-orbital configuration as well,
-    # with E and S from the Lambda equations (Kelvin's Simpson grid, on which
-    # they are built): a few seconds
-    if mixed and not per_solve:
-        cfg["accuracy_38_spin_orbitals"] = small_accuracy(ctx, args.accel)
-
     # CPU baseline: a bounded sample of the oracle's iteration (guess and three
     # iterations of the 38-spin-orbital solve) on the host cores
     t_guess, times, _, _ = oracle_c1_iterations(args.quad, 3, until_converged=False)
@@ -510,6 +504,11 @@ def run_gpu(args, w):
     if lat:
         q = lambda f: lat[min(len(lat) - 1, int(f * len(lat)))]
         cfg["step_latency_ms"] = {"p50": q(0.5), "p99": q(0.99), "n": len(lat)}
+    # mixed against FP64-accurate on the 38-spin-orbital configuration as well,
+    # with E and S from the Lambda equations (Kelvin's Simpson grid, on which
+    # they are built): a few seconds
+    if mixed and not per_solve:
+        cfg["accuracy_38_spin_orbitals"] = small_accuracy(ctx, args.accel)
     if ref64 is not sol:
         d = abs(sol["omega_cc"] - ref64["omega_cc"])
         cfg["fp64_tc_solve"] = {k: ref64[k] for k in ("iterations", "converged", "omega_cc",
@@ -538,7 +537,9 @@ def run_gpu(args, w):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": {"fp64": "f64", "fp64_tc": "f64 (7 BF16 digit levels, tensor cores)",
-                      "mixed": "bf16 digits/f32 acc (3, 5 levels) + f64 refinement"}[
+                      "mixed": "bf16 digits/f32 acc (%s levels) + FP64-accurate 7-level "
+                               "refinement; f64 quadrature, update, energy"
+                               % ", ".join(str(x) for x in (digits,) + ladder)}[
                           args.precision],
             "data": "synthetic", "config": cfg, "roofline": roofline,
             "cpu_baseline": {"value": None, "unit": UNIT, "cores": os.cpu_count(),
