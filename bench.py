@@ -580,7 +580,11 @@ def run_profile_step(args, w):
                                       beta, s.mu, ti, g, G)
     solver.full = args.quad == "gl"
     solver.guess(1)
-    solver.step(w["damp"])
+    if args.accel:
+        solver.set_acceleration(args.accel)
+    # enough warm-up iterations for a full Anderson history
+    for _ in range(1 + (args.accel if args.accel else 0)):
+        solver.step(w["damp"])
     ctx.sync()
     l0 = ctx.launches()
     ctx.profile_begin()
@@ -598,7 +602,7 @@ def run_profile_step(args, w):
     # GEMM kernel (tc_gemm_kernel or gemm_f64_kernel) per contraction
     gemm_cats = [c for c, _, _ in recs if c in ("gemm6", "gemm")]
     print(json.dumps({"profile_step": args.workload, "precision": args.precision,
-                      "launches_before": l0, "launches_in_step": ctx.launches() - l0,
+                      "accel": args.accel, "launches_before": l0, "launches_in_step": ctx.launches() - l0,
                       "omega_cc": E, "res": res, "gemm_categories": gemm_cats}))
     solver.close()
     return 0

@@ -430,33 +430,58 @@ struct AaSeg {
     int h, n;           // h > 0: T2 spin runs (P = n^4), else every element
 };
 constexpr int AA_T = 256;
+constexpr int AA_U = 4;     // elements per thread per batch (all loads before any store)
+constexpr int AA_BLOCKS = 3; // resident blocks per SM (at most 85 registers a thread)
 
-// index of the e-th visited element, or -1 past the end: spin-run
-// enumeration as in the quadrature's spin path (one warp per run)
+// The six spin patterns (sa, sb, si, sj) with sa + sb = si + sj (0 = alpha,
+// 1 = beta), four bits each: sa | sb << 1 | si << 2 | sj << 3.
+constexpr unsigned AA_PATTERNS = 0u | 15u << 4 | 10u << 8 | 6u << 12 | 9u << 16 | 5u << 20;
+
+// Calls f(base, o, cnt) with batches of up to AA_U element indices
+// base + o[u] of the segment (u < cnt valid).  T2 with spin runs: one warp per (tau, spin pattern,
+// a, b) quadrant of h x h elements (i, j in their halves), lanes along j;
+// only the spin-conserving elements are visited.  Otherwise every element.
 template <class F>
 __device__ __forceinline__ void aa_visit(const AaSeg &g, F f) {
-    const int t = threadIdx.x;
+    const int t = threadIdx.x, lane = t % 32;
+    int o[AA_U];
     if (g.h > 0) {
-        const int h = g.h, n = g.n;
-        const long long rows = g.P / n;
-        const int lane = t % 32;
-        const long long tw = (long long)gridDim.x * (AA_T / 32);
-        for (long long u = blockIdx.x * (long long)(AA_T / 32) + t / 32; u < 2 * rows * g.ng;
-             u += tw) {
-            const long long y = u / (2 * rows), uu = u - y * 2 * rows;
-            const long long r = uu >> 1;
-            const int jh = (int)(uu & 1);
-            const int i = (int)(r % n);
-            const long long ab = r / n;
-            const int b = (int)(ab % n), a = (int)(ab / n);
-            if ((a >= h) + (b >= h) != (i >= h) + jh) continue;
-            for (int jj = lane; jj < h; jj += 32) f(y * g.P + r * n + (long long)jh * h + jj);
+        const int h = g.h, n = g.n, hh = h * h;
+        const long long items = (long long)g.ng * 6 * hh;
+        const long long nw = (long long)gridDim.x * (AA_T / 32);
+        for (long long it = blockIdx.x * (long long)(AA_T / 32) + t / 32; it < items; it += nw) {
+            const long long y = it / (6 * hh);
+            const int rem = (int)(it - y * 6 * hh);
+            const int pat = rem / hh, ab = rem - pat * hh;
+            const int a1 = ab / h, b1 = ab - a1 * h;
+            const unsigned c = AA_PATTERNS >> (4 * pat);
+            const int a = a1 + (int)(c & 1u) * h, b = b1 + (int)((c >> 1) & 1u) * h;
+            const long long base = y * g.P + (((long long)a * n + b) * n + (long long)((c >> 2) & 1u) * h) * n +
+                                   (long long)((c >> 3) & 1u) * h;
+            for (int k0 = 0; k0 < hh; k0 += 32 * AA_U) {
+                int cnt = 0;
+#pragma unroll
+                for (int u = 0; u < AA_U; u++) {
+                    const int k = k0 + u * 32 + lane;
+                    const int i1 = k / h;
+                    o[u] = i1 * n + (k - i1 * h);
+                    if (k < hh) cnt = u + 1;
+                }
+                f(base, o, cnt);
+            }
         }
     } else {
         const long long tot = g.P * g.ng;
-        for (long long e = blockIdx.x * (long long)AA_T + t; e < tot;
-             e += (long long)gridDim.x * AA_T)
-            f(e);
+        const long long stride = (long long)gridDim.x * AA_T;
+        for (long long e0 = blockIdx.x * (long long)AA_T + t; e0 < tot; e0 += stride * AA_U) {
+            int cnt = 0;
+#pragma unroll
+            for (int u = 0; u < AA_U; u++) {
+                o[u] = (int)(u * stride);
+                if (e0 + o[u] < tot) cnt = u + 1;
+            }
+            f(e0, o, cnt);
+        }
     }
 }
 
@@ -487,54 +512,94 @@ struct AaHist {
     float *dXst;         // pass B: the slot the step goes to
 };
 
+// GB300 has ~64x more FP32 than FP64 throughput, so the passes keep FP64
+// only where the iterate needs it (r = Phi - x and the update of x); the
+// history, the dot products (which only steer the mixing coefficients) and
+// the norms of Kelvin's residual measure run in FP32 per thread and are
+// summed in FP64 per block.
+
 // pass A: r = Phi - x; dRnew = r - rprev; rprev = r; sums <dR_q, dRnew>,
 // <dR_q, r> over the NV valid slots, and <r, r>
 template <int NV>
-__global__ void __launch_bounds__(AA_T)
+__global__ void __launch_bounds__(AA_T, AA_BLOCKS)
 aa_stats_kernel(AaSeg g, AaHist hs, double *part) {
-    double v[7] = {0, 0, 0, 0, 0, 0, 0};
-    aa_visit(g, [&](long long e) {
-        const double r = g.phi[e] - g.x[e];
-        double dn = 0.0;
-        if (hs.dRnew) {
-            const float d = (float)(r - (double)g.rprev[e]);
-            hs.dRnew[e] = d;
-            dn = (double)d;
-        }
-        g.rprev[e] = (float)r;
+    float v[7] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    const bool has_new = hs.dRnew != nullptr;
+    aa_visit(g, [&](long long base, const int (&o)[AA_U], int cnt) {
+        const double *phi = g.phi + base, *x = g.x + base;
+        float *rprev = g.rprev + base;
+        double ph[AA_U], xx[AA_U];
+        float rp[AA_U], dh[NV > 0 ? NV : 1][AA_U];
 #pragma unroll
-        for (int q = 0; q < NV; q++) {
-            const double di = (q == 0 && hs.dRnew) ? dn : (double)hs.dR[q][e];
-            v[q] = fma(di, dn, v[q]);
-            v[3 + q] = fma(di, r, v[3 + q]);
+        for (int u = 0; u < AA_U; u++) {
+            if (u >= cnt) break;
+            ph[u] = phi[o[u]];
+            xx[u] = x[o[u]];
+            rp[u] = has_new ? rprev[o[u]] : 0.f;
+#pragma unroll
+            for (int q = 0; q < NV; q++)
+                dh[q][u] = (q == 0 && has_new) ? 0.f : hs.dR[q][base + o[u]];
         }
-        v[6] = fma(r, r, v[6]);
+#pragma unroll
+        for (int u = 0; u < AA_U; u++) {
+            if (u >= cnt) break;
+            const float r = (float)(ph[u] - xx[u]);
+            const float dn = has_new ? r - rp[u] : 0.f;
+            if (has_new) hs.dRnew[base + o[u]] = dn;
+            rprev[o[u]] = r;
+#pragma unroll
+            for (int q = 0; q < NV; q++) {
+                const float di = (q == 0 && has_new) ? dn : dh[q][u];
+                v[q] = fmaf(di, dn, v[q]);
+                v[3 + q] = fmaf(di, r, v[3 + q]);
+            }
+            v[6] = fmaf(r, r, v[6]);
+        }
     });
-    aa_block_sum<7>(v, part);
+    double w[7];
+#pragma unroll
+    for (int k = 0; k < 7; k++) w[k] = (double)v[k];
+    aa_block_sum<7>(w, part);
 }
 
 // pass B: x += beta r - sum_q gamma_q (dX_q + beta dR_q); dXst = the step;
 // sums |step|^2 and |x_new|^2
 template <int NV>
-__global__ void __launch_bounds__(AA_T)
-aa_update_kernel(AaSeg g, AaHist hs, double beta, double g0, double g1, double g2,
+__global__ void __launch_bounds__(AA_T, AA_BLOCKS)
+aa_update_kernel(AaSeg g, AaHist hs, double beta, float g0, float g1, float g2,
                  double *part) {
-    double v[2] = {0, 0};
-    const double gam[3] = {g0, g1, g2};
-    aa_visit(g, [&](long long e) {
-        const double x = g.x[e];
-        const double r = g.phi[e] - x;
-        double d = beta * r;
+    float v[2] = {0.f, 0.f};
+    const float gam[3] = {g0, g1, g2};
+    const float bf = (float)beta;
+    aa_visit(g, [&](long long base, const int (&o)[AA_U], int cnt) {
+        const double *phi = g.phi + base;
+        double *x = g.x + base;
+        double ph[AA_U], xx[AA_U];
+        float hsum[AA_U];
 #pragma unroll
-        for (int q = 0; q < NV; q++)
-            d -= gam[q] * ((double)hs.dX[q][e] + beta * (double)hs.dR[q][e]);
-        const double xn = x + d;
-        g.x[e] = xn;
-        hs.dXst[e] = (float)d;
-        v[0] = fma(d, d, v[0]);
-        v[1] = fma(xn, xn, v[1]);
+        for (int u = 0; u < AA_U; u++) {
+            if (u >= cnt) break;
+            ph[u] = phi[o[u]];
+            xx[u] = x[o[u]];
+            float a = 0.f;
+#pragma unroll
+            for (int q = 0; q < NV; q++) a = fmaf(gam[q], fmaf(bf, hs.dR[q][base + o[u]], hs.dX[q][base + o[u]]), a);
+            hsum[u] = a;
+        }
+#pragma unroll
+        for (int u = 0; u < AA_U; u++) {
+            if (u >= cnt) break;
+            const double d = fma(beta, ph[u] - xx[u], -(double)hsum[u]);
+            const double xn = xx[u] + d;
+            x[o[u]] = xn;
+            const float df = (float)d, xf = (float)xn;
+            hs.dXst[base + o[u]] = df;
+            v[0] = fmaf(df, df, v[0]);
+            v[1] = fmaf(xf, xf, v[1]);
+        }
     });
-    aa_block_sum<2>(v, part);
+    double w[2] = {(double)v[0], (double)v[1]};
+    aa_block_sum<2>(w, part);
 }
 
 // out[k] = sum over blocks of part[b K + k] (fixed order)
@@ -751,9 +816,18 @@ void aa_segments(kvft_solver *s, AaSeg *g1, AaSeg *g2) {
 }
 
 // grid and partial-sum buffer of one Anderson pass over a segment
+// (one wave: AA_BLOCKS resident blocks per SM, every block striding over
+// the segment)
 int aa_launch_grid(kvft_ctx *ctx, const AaSeg &g) {
-    const long long work = g.h > 0 ? g.P * g.ng * 3 / 8 : g.P * g.ng;
-    return (int)std::max(1LL, std::min((long long)ctx->sm_count * 8, (work + AA_T - 1) / AA_T));
+    const long long wanted = g.h > 0 ? ((long long)g.ng * 6 * g.h * g.h + AA_T / 32 - 1) / (AA_T / 32)
+                                     : (g.P * g.ng + AA_T * AA_U - 1) / (AA_T * AA_U);
+    return (int)std::max(1LL, std::min((long long)ctx->sm_count * AA_BLOCKS, wanted));
+}
+
+// elements one pass visits (the spin-conserving sixth-of-16 of T2 with
+// spin runs)
+double aa_visited(const AaSeg &g) {
+    return g.h > 0 ? (double)g.ng * 6.0 * g.h * g.h * g.h * g.h : (double)g.P * g.ng;
 }
 
 // The accelerated iteration up to the queued scalars (as the damped one
@@ -784,7 +858,7 @@ int aa_step_begin(kvft_solver *s, double damp) {
     double *part = (double *)pp;
     {
         KvProfScope prof(ctx, KV_CAT_ELEM,
-                         (double)(s->s1() + s->s2()) * s->ng * (28.0 + 4.0 * nvalid));
+                         (aa_visited(g[0]) + aa_visited(g[1])) * (28.0 + 4.0 * nvalid));
         for (int q = 0; q < 2; q++) {
             AaHist hs{};
             for (int t = 0; t < nvalid; t++) {
@@ -831,10 +905,11 @@ int aa_step_begin(kvft_solver *s, double damp) {
     const int jst = (int)(k % m);
     const int slot0 = nvalid > 0 ? jnew : 0;
     const double beta = 1.0 - damp;
+    const float gf[3] = {(float)gam[0], (float)gam[1], (float)gam[2]};
     const int gridB[2] = {gridA[0], gridA[1]};
     {
         KvProfScope prof(ctx, KV_CAT_ELEM,
-                         (double)(s->s1() + s->s2()) * s->ng * (28.0 + 8.0 * nvalid));
+                         (aa_visited(g[0]) + aa_visited(g[1])) * (28.0 + 8.0 * nvalid));
         for (int q = 0; q < 2; q++) {
             AaHist hs{};
             for (int t = 0; t < nvalid; t++) {
@@ -846,20 +921,20 @@ int aa_step_begin(kvft_solver *s, double damp) {
             double *pq = part + (q ? 2 * gridB[0] : 0);
             switch (nvalid) {
             case 0:
-                aa_update_kernel<0><<<gridB[q], AA_T, 0, ctx->stream>>>(g[q], hs, beta, gam[0],
-                                                                       gam[1], gam[2], pq);
+                aa_update_kernel<0><<<gridB[q], AA_T, 0, ctx->stream>>>(g[q], hs, beta, gf[0],
+                                                                       gf[1], gf[2], pq);
                 break;
             case 1:
-                aa_update_kernel<1><<<gridB[q], AA_T, 0, ctx->stream>>>(g[q], hs, beta, gam[0],
-                                                                       gam[1], gam[2], pq);
+                aa_update_kernel<1><<<gridB[q], AA_T, 0, ctx->stream>>>(g[q], hs, beta, gf[0],
+                                                                       gf[1], gf[2], pq);
                 break;
             case 2:
-                aa_update_kernel<2><<<gridB[q], AA_T, 0, ctx->stream>>>(g[q], hs, beta, gam[0],
-                                                                       gam[1], gam[2], pq);
+                aa_update_kernel<2><<<gridB[q], AA_T, 0, ctx->stream>>>(g[q], hs, beta, gf[0],
+                                                                       gf[1], gf[2], pq);
                 break;
             default:
-                aa_update_kernel<3><<<gridB[q], AA_T, 0, ctx->stream>>>(g[q], hs, beta, gam[0],
-                                                                       gam[1], gam[2], pq);
+                aa_update_kernel<3><<<gridB[q], AA_T, 0, ctx->stream>>>(g[q], hs, beta, gf[0],
+                                                                       gf[1], gf[2], pq);
                 break;
             }
             KV_TRY(kv_launch_check(ctx, "aa_update"));
