@@ -325,11 +325,14 @@ def run_gpu(args, w):
         solver.set_acceleration(args.accel)
     solver.guess(1)
     ladder = (5,) if not args.accel else ()
+    low_tconv = args.low_tconv if args.accel else None
 
     def one_step():
         if per_solve:
             solver.guess(1)
-            E, info = ccsd.converge(solver, ctx, conv, args.precision, digits, ladder=ladder)
+            E, info = ccsd.converge(solver, ctx, dict(conv, damp=1.0 - args.mix)
+                                    if args.accel else conv, args.precision, digits,
+                                    ladder=ladder, low_tconv=low_tconv)
             return E, info["iterations"] + info["iterations_refine"]
         return solver.step(w["damp"])[0], 1
 
@@ -395,7 +398,9 @@ def run_gpu(args, w):
     def solve(precision, lv, accel):
         cc = ccsd.ccsd(sysobj, T=sysobj.T, mu=sysobj.mu, max_iter=w["max_iter"],
                        damp=w["damp"], ngrid=ng, econv=w["econv"], quad=args.quad,
-                       precision=precision, digits=lv, accel=accel, ctx=ctx)
+                       precision=precision, digits=lv, accel=accel,
+                       mix=args.mix if accel else None,
+                       low_tconv=low_tconv if accel else None, ctx=ctx)
         ctx.sync()
         ctx.record(2)
         t0 = time.perf_counter()
@@ -491,7 +496,11 @@ def run_gpu(args, w):
     cfg = {"workload": w["label"].replace("ng=%d" % ng, "ng=%d %s" % (
                ng, "Gauss-Legendre" if full else "Simpson ('lin')")),
            "step": w["step"], "precision": args.precision,
-           "update": ("Anderson mixing, depth %d, mixing factor 1 - damping" % args.accel
+           "update": ("Anderson mixing, depth %d, mixing factor %g (the damped update's "
+                      "fixed point; Kelvin's test)%s" % (
+                          args.accel, args.mix,
+                          "; few-digit phase until Kelvin's residual < %g or its noise floor"
+                          % low_tconv if mixed and low_tconv else "")
                       if args.accel else "Kelvin's damped update"),
            "digits": digits if args.precision != "fp64" else None,
            "solve": {k: sol[k] for k in ("iterations", "phases", "converged", "omega_cc")},
@@ -508,7 +517,7 @@ def run_gpu(args, w):
     # with E and S from the Lambda equations (Kelvin's Simpson grid, on which
     # they are built): a few seconds
     if mixed and not per_solve:
-        cfg["accuracy_38_spin_orbitals"] = small_accuracy(ctx, args.accel)
+        cfg["accuracy_38_spin_orbitals"] = small_accuracy(ctx, args)
     if ref64 is not sol:
         d = abs(sol["omega_cc"] - ref64["omega_cc"])
         cfg["fp64_tc_solve"] = {k: ref64[k] for k in ("iterations", "converged", "omega_cc",
@@ -702,16 +711,17 @@ def run_esn(args):
     return 0
 
 
-def small_accuracy(ctx, accel):
+def small_accuracy(ctx, args):
     """|dOmega|, |dE|, |dS| of the mixed form (as benchmarked) against Kelvin's
     damped FP64-accurate solve: UEG 14 electrons, rs = 4, 19 plane waves,
     Theta = 0.5, ng = 10 (Simpson), E and S from the Lambda equations."""
     from kelvin_gb300 import _lib, ccsd as kccsd, systems
     s = systems.ueg_recipe(14, 4.0, 19, 0.5, device_build=True)
     out = {}
-    for prec, acc in (("fp64_tc", 0), ("mixed", accel)):
+    for prec, acc in (("fp64_tc", 0), ("mixed", args.accel)):
         cc = kccsd.ccsd(s, T=s.T, mu=s.mu, max_iter=200, damp=0.5, ngrid=10, econv=1e-10,
-                        precision=prec, accel=acc, ctx=ctx)
+                        precision=prec, accel=acc, mix=args.mix if acc else None,
+                        low_tconv=args.low_tconv if acc else None, ctx=ctx)
         try:
             Om = cc.run()[0]
             E, S, N = cc.compute_ESN(method="lambda")
@@ -753,7 +763,10 @@ def run_accuracy(args):
             # the reference: Kelvin's damped loop; the mixed form: as benchmarked
             cc = kccsd.ccsd(s, T=s.T, mu=s.mu, max_iter=300, damp=damp, ngrid=ng,
                             econv=1e-10, quad=quad, precision=prec,
-                            accel=args.accel if prec == "mixed" else 0, ctx=ctx)
+                            accel=args.accel if prec == "mixed" else 0,
+                            mix=args.mix if prec == "mixed" and args.accel else None,
+                            low_tconv=args.low_tconv if prec == "mixed" and args.accel
+                            else None, ctx=ctx)
             t0 = time.perf_counter()
             try:
                 cc.run()
@@ -818,8 +831,13 @@ def main():
     ap.add_argument("--slots", type=int, default=4, help="--serve: solves on the device at once")
     ap.add_argument("--esn", action="store_true",
                     help="E, S, N of the 66-spin-orbital UEG: Lambda route against differences")
-    ap.add_argument("--accel", type=int, default=2,
+    ap.add_argument("--accel", type=int, default=3,
                     help="Anderson depth of the iteration (0: Kelvin's damped update)")
+    ap.add_argument("--mix", type=float, default=0.7,
+                    help="Anderson mixing factor (with --accel)")
+    ap.add_argument("--low-tconv", type=float, default=1e-4,
+                    help="mixed form with --accel: end the few-digit phase once Kelvin's "
+                         "residual measure is below this")
     ap.add_argument("--quad", default="gl", choices=["gl", "lin"],
                     help="tau grid: Gauss-Legendre (the configurations') or Kelvin's Simpson")
     ap.add_argument("--accuracy", action="store_true",

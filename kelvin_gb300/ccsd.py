@@ -26,7 +26,7 @@ PRECISIONS = {'fp64': (_lib.PREC_FP64, 7), 'fp64_tc': (_lib.PREC_FP64_TC, 7),
 
 
 def converge(solver, ctx, conv, precision, digits, refine_sweeps=None, refine_digits=7,
-             ladder=(5,)):
+             ladder=(5,), low_tconv=None):
     """Iterate a DeviceSolver to convergence; returns (Omega_cc, info).
 
     FP64 forms ('fp64', 'fp64_tc') run Kelvin's loop and test (|dE| < econv
@@ -38,7 +38,10 @@ def converge(solver, ctx, conv, precision, digits, refine_sweeps=None, refine_di
     re-evaluates the update with `refine_digits` levels (7: FP64-accurate)
     and iterates until Kelvin's test passes, at most `refine_sweeps` sweeps
     (None: the loop's max_iter).  Only that test counts as convergence: a
-    stalled low phase does not.  info: iterations (low phases),
+    stalled low phase does not.  `low_tconv` also ends each low phase once
+    Kelvin's residual measure falls below it (the few-digit map's own fixed
+    point is off the FP64 one by about its rounding, so sweeps below that
+    level are not needed).  info: iterations (low phases),
     iterations_refine, converged, omega_low (the energy where the low phases
     ended) and phases, a list of (digit levels, sweeps, stalled)."""
     if precision != 'mixed':
@@ -54,10 +57,11 @@ def converge(solver, ctx, conv, precision, digits, refine_sweeps=None, refine_di
     try:
         for lv in (digits,) + tuple(l for l in ladder if digits < l < refine_digits):
             ctx.set_precision(_lib.PREC_MIXED if lv <= 3 else _lib.PREC_FP64_TC, lv)
-            E_low = iterate(solver, conv, "CCSD (%d digit levels)" % lv, stall=3, quiet=True)
+            low = conv if low_tconv is None else dict(conv, econv=float("inf"), tconv=low_tconv)
+            E_low = iterate(solver, low, "CCSD (%d digit levels)" % lv, stall=3, quiet=True)
             low_iters += solver.iterations
             phases.append((lv, solver.iterations, bool(solver.stalled)))
-            if solver.converged:
+            if solver.converged and low_tconv is None:
                 break
         ref = dict(conv)
         if refine_sweeps is not None:
@@ -187,7 +191,7 @@ class ccsd(object):
                  tconv=None, max_iter=40, damp=0.0, ngrid=10, realtime=False,
                  athresh=0.0, quad='lin', rt_iter="all", precision='fp64',
                  digits=None, refine_sweeps=None, refine_digits=7, ladder=None, accel=0,
-                 device=0, ctx=None):
+                 mix=None, low_tconv=None, device=0, ctx=None):
         self.T = T
         self.mu = mu
         self.finite_T = T != 0
@@ -212,7 +216,13 @@ class ccsd(object):
         self.refine_sweeps = refine_sweeps
         self.refine_digits = refine_digits
         # Anderson depth of the amplitude iteration (0: Kelvin's damped update)
+        # and its mixing factor (None: 1 - damp, the damped update's); the
+        # fixed point does not depend on either
         self.accel = int(accel)
+        self.mix = mix
+        # mixed form: end each few-digit phase once Kelvin's residual measure
+        # is below this (None: at its noise floor only)
+        self.low_tconv = low_tconv
         # intermediate digit levels of the mixed form: with Kelvin's damped
         # update a 5-level phase shortens the FP64-accurate one; with Anderson
         # mixing (whose history restarts at every change of precision) going
@@ -304,8 +314,11 @@ class ccsd(object):
         else:
             E2 = solver.guess(1)
         logging.info('MP2 Energy: {:.10f}'.format(E2))
+        if self.accel and self.mix is not None:
+            conv["damp"] = 1.0 - self.mix
         Eccn, info = converge(solver, self.ctx, conv, self.precision, digits,
-                              self.refine_sweeps, self.refine_digits, self.ladder)
+                              self.refine_sweeps, self.refine_digits, self.ladder,
+                              self.low_tconv)
         self.iterations = info["iterations"]
         self.iterations_refine = info["iterations_refine"]
         self.converged = info["converged"]

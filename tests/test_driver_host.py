@@ -235,3 +235,56 @@ def test_lambda_on_the_resident_solver():
     assert cc._Lg is Lg
     assert numpy.array_equal(cc.L2[1], Lg[1][:, :na, na:, :na, na:])
     assert cc.ctx._precision == (0, 7)
+
+
+class ScriptSolver(object):
+    """Steps through scripted (E, res) pairs per digit-level setting and
+    records the mixing factor each step was given."""
+
+    def __init__(self, ctx, script):
+        self.ctx, self.script, self.pos, self.damps = ctx, script, {}, []
+
+    def step(self, damp):
+        lv = self.ctx._precision[1]
+        k = self.pos.get(lv, 0)
+        self.pos[lv] = k + 1
+        self.damps.append(damp)
+        seq = self.script[lv]
+        return seq[min(k, len(seq) - 1)]
+
+
+def test_converge_phases_and_residual_cut():
+    """Few-digit phases end at their noise floor (three sweeps without a new
+    best below 0.9 of it) or, with low_tconv, once the residual is below it;
+    the ladder continues after a cut; only the refinement's Kelvin test
+    counts as convergence."""
+    three = [(-1.0, 1e-1), (-0.9, 1e-2), (-0.95, 5e-5), (-0.95, 8e-5), (-0.95, 6e-5),
+             (-0.95, 7e-5), (-0.95, 9e-5)]
+    five = [(-0.95, 1e-4), (-0.95, 4e-5), (-0.95, 5e-5), (-0.95, 6e-5), (-0.95, 7e-5)]
+    seven = [(-0.9500001, 1e-5), (-0.95000001, 1e-6), (-0.950000010001, 1e-8)]
+    conv = {"econv": 1e-10, "tconv": 1e-7, "max_iter": 50, "damp": 0.3}
+
+    ctx = FakeCtx()
+    s = ScriptSolver(ctx, {3: three, 5: five, 7: seven})
+    E, info = ccsd_mod.converge(s, ctx, conv, 'mixed', 3, ladder=(5,))
+    assert info["phases"] == [(3, 6, True), (5, 5, True), (7, 3, False)]
+    assert info["converged"] and abs(E + 0.950000010001) < 1e-15
+
+    ctx = FakeCtx()
+    s = ScriptSolver(ctx, {3: three, 5: five, 7: seven})
+    E, info = ccsd_mod.converge(s, ctx, conv, 'mixed', 3, ladder=(5,), low_tconv=1e-4)
+    # 3 levels: cut at the third sweep; 5 levels: 1e-4 is not below the cut,
+    # 4e-5 is; then the refinement
+    assert info["phases"] == [(3, 3, False), (5, 2, False), (7, 3, False)]
+    assert info["iterations"] == 5 and info["iterations_refine"] == 3
+    assert info["converged"]
+    assert set(s.damps) == {0.3}
+    assert ctx._precision == (0, 7)           # the caller's setting is restored
+
+    # a refinement that never meets Kelvin's test is not converged, even when
+    # every few-digit phase met its cut
+    ctx = FakeCtx()
+    s = ScriptSolver(ctx, {3: three, 7: [(-0.95, 1e-5), (-0.96, 1e-5)]})
+    E, info = ccsd_mod.converge(s, ctx, dict(conv, max_iter=4), 'mixed', 3, ladder=(),
+                                low_tconv=1e-4)
+    assert not info["converged"] and info["iterations_refine"] == 4

@@ -58,3 +58,24 @@ def test_anderson_gauss_legendre_vs_oracle(ctx, prec, tol):
     assert acc.converged
     assert abs(Ecc - meta["omega_cc"]) < tol
     assert n_acc <= n_ref
+
+
+def test_benchmarked_scheme_vs_oracle(ctx):
+    """The mixed form as benchmarked (depth 3, mixing factor 0.7, the
+    three-level phase cut at residual 1e-4) on the 38-spin-orbital
+    Gauss-Legendre configuration: Kelvin's test passes at the oracle's
+    fixed point."""
+    meta = json.load(open(os.path.join(GOLDEN, "configs.json")))["ueg38_gl"]
+    s = systems.ueg_recipe(14, 4.0, 19, 0.5)
+    try:
+        cc = ccsd.ccsd(s, T=s.T, mu=s.mu, max_iter=100, damp=0.5, ngrid=meta["ngrid"],
+                       econv=1e-10, quad="gl", precision="mixed", accel=3, mix=0.7,
+                       low_tconv=1e-4, ctx=ctx)
+        Et, Ecc = cc.run()
+        cc.release()
+    finally:
+        ctx.set_precision(_lib.PREC_FP64, 7)
+    print("benchmarked scheme: phases %s, Omega_cc %.12f oracle %.12f"
+          % (cc.phases, Ecc, meta["omega_cc"]))
+    assert cc.converged
+    assert abs(Ecc - meta["omega_cc"]) < 1e-8
