@@ -350,6 +350,14 @@ int kvft_solver_step_begin(kvft_solver *s, double damp);
 int kvft_solver_step_end(kvft_solver *s, double *energy, double *res);
 int kvft_solver_get_amplitudes(kvft_solver *s, double *T1_host,
                                double *T2_host);
+/* The same read-back through the context's pinned staging buffer (2 x 256
+ * MiB, allocated on first use and kept), with the host-side copy spread over
+ * the host's threads.  dst_zeroed = 1 promises that T2_host holds zeros (a
+ * fresh calloc): with spin blocks only the spin-conserving elements are
+ * copied and the pages of the rest are never touched.  Replaces the host
+ * arrays Kelvin's solve leaves in ccsd.T1 / ccsd.T2 (kelvin/ccsd.py:704-712). */
+int kvft_solver_read_amplitudes(kvft_solver *s, double *T1_host, double *T2_host,
+                                int dst_zeroed);
 int kvft_solver_set_amplitudes(kvft_solver *s, const double *T1_host,
                                const double *T2_host);
 /* Device pointers of the solver's resident amplitudes (T1, T2). */

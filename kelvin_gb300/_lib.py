@@ -159,6 +159,7 @@ _SIGS = {
     "kvft_solver_run_point": (ctypes.c_int, [vp, ctypes.POINTER(SolveOpts),
                                              ctypes.POINTER(Result)]),
     "kvft_solver_get_amplitudes": (ctypes.c_int, [vp, vp, vp]),
+    "kvft_solver_read_amplitudes": (ctypes.c_int, [vp, vp, vp, ctypes.c_int]),
     "kvft_solver_set_amplitudes": (ctypes.c_int, [vp, vp, vp]),
     "kvft_solver_device_amplitudes": (ctypes.c_int, [vp, ctypes.POINTER(vp),
                                                      ctypes.POINTER(vp)]),

@@ -125,10 +125,12 @@ class DeviceSolver(object):
 
     def amplitudes(self):
         T1 = numpy.empty((self.ng, self.nv, self.no))
-        T2 = numpy.empty((self.ng, self.nv, self.nv, self.no, self.no))
-        self.ctx.check(self.ctx.L.kvft_solver_get_amplitudes(
-            self.h, T1.ctypes.data_as(_lib.vp), T2.ctypes.data_as(_lib.vp)),
-            "kvft_solver_get_amplitudes")
+        # zero pages until written: with spin blocks only the
+        # spin-conserving elements are copied
+        T2 = numpy.zeros((self.ng, self.nv, self.nv, self.no, self.no))
+        self.ctx.check(self.ctx.L.kvft_solver_read_amplitudes(
+            self.h, T1.ctypes.data_as(_lib.vp), T2.ctypes.data_as(_lib.vp), 1),
+            "kvft_solver_read_amplitudes")
         return T1, T2
 
     def lambda_solve(self, conv_options, guess=1, L1=None, L2=None, measure_half=None,

@@ -129,6 +129,7 @@ int kvft_ctx_destroy(kvft_ctx *c) {
     }
     if (c->l2buf) cudaFree(c->l2buf);
     if (c->dflag) cudaFree(c->dflag);
+    if (c->hstage) cudaFreeHost(c->hstage);
     for (int i = 0; i < 64; i++) cudaEventDestroy(c->ev[i]);
     if (c->own_stream) cudaStreamDestroy(c->stream);
     delete c;

@@ -134,6 +134,10 @@ struct kvft_ctx {
     // scratch kept for the next contraction.
     bool tpack_on = false;
     std::map<std::string, int> tpack;
+    // Pinned, device-mapped host staging of the amplitude read-back (two
+    // halves), kept for the context's lifetime.
+    void *hstage = nullptr;
+    size_t hstage_bytes = 0;
 };
 struct KvTPackScope {
     kvft_ctx *ctx;

@@ -16,6 +16,7 @@
 
 #include <cmath>
 #include <cstdio>
+#include <thread>
 #include <vector>
 
 int kv_quad_single(kvft_ctx *ctx, int ng, int ig, long long P, int rank, int nv, int no,
@@ -620,6 +621,54 @@ __global__ void aa_reduce_kernel(const double *__restrict__ part, int nb, int K,
     }
 }
 
+// ---------------------------------------------------------------------------
+// Amplitude read-back through pinned staging.  A chunk of T2 goes to one half
+// of the context's pinned, device-mapped staging buffer (written by a gather
+// kernel over the C2C / PCIe link), and host threads copy it on into the
+// caller's array while the device fills the other half, so that the first
+// touch of the destination pages is spread over the host cores.  With spin
+// blocks and a destination known to be zero, only the spin-conserving
+// elements travel, in the quadrant order of the Anderson passes (tau, spin
+// pattern, a, b, then the h x h block of (i, j)).
+// ---------------------------------------------------------------------------
+__host__ __device__ __forceinline__ long long spin_item_base(long long it, long long P, int n,
+                                                            int h) {
+    const int hh = h * h;
+    const long long y = it / (6 * hh);
+    const int rem = (int)(it - y * 6 * hh);
+    const int pat = rem / hh, ab = rem - pat * hh;
+    const int a1 = ab / h, b1 = ab - a1 * h;
+    const unsigned c = AA_PATTERNS >> (4 * pat);
+    const long long a = a1 + (long long)(c & 1u) * h, b = b1 + (long long)((c >> 1) & 1u) * h;
+    return y * P + ((a * n + b) * n + (long long)((c >> 2) & 1u) * h) * n +
+           (long long)((c >> 3) & 1u) * h;
+}
+
+// out[t] = T2 at the t-th element of items [it0, it0 + nit)
+__global__ void __launch_bounds__(256)
+amp_gather_kernel(const double *__restrict__ T2, long long P, int n, int h, long long it0,
+                  long long nit, double *__restrict__ out) {
+    const int hh = h * h;
+    const long long tot = nit * hh;
+    for (long long t = blockIdx.x * 256LL + threadIdx.x; t < tot; t += (long long)gridDim.x * 256) {
+        const long long it = t / hh;
+        const int k = (int)(t - it * hh), i1 = k / h;
+        out[t] = T2[spin_item_base(it0 + it, P, n, h) + (long long)i1 * n + (k - i1 * h)];
+    }
+}
+
+// runs f(lo, hi) over [0, n) split across the host threads
+template <class F>
+void host_parallel(long long n, F f) {
+    const unsigned hw = std::thread::hardware_concurrency();
+    const int nt = (int)std::max(1LL, std::min<long long>(hw ? hw : 4, (n + 1023) / 1024));
+    std::vector<std::thread> th;
+    for (int t = 1; t < nt; t++)
+        th.emplace_back(f, n * t / nt, n * (t + 1) / nt);
+    f(0, n / nt);
+    for (auto &x : th) x.join();
+}
+
 void destroy(kvft_solver *s) {
     if (s->gexec) cudaGraphExecDestroy(s->gexec);
     for (void *p : s->allocs) cudaFree(p);
@@ -1221,6 +1270,84 @@ int kvft_solver_get_amplitudes(kvft_solver *s, double *T1h, double *T2h) {
                                          cudaMemcpyDeviceToHost, s->ctx->stream));
     KV_CHECK(s->ctx, cudaStreamSynchronize(s->ctx->stream));
     return KVFT_OK;
+}
+
+int kvft_solver_read_amplitudes(kvft_solver *s, double *T1h, double *T2h, int dst_zeroed) {
+    if (!s || !T1h || !T2h) return KVFT_EINVAL;
+    kvft_ctx *ctx = s->ctx;
+    cudaSetDevice(ctx->device);
+    KV_CHECK(ctx, cudaMemcpyAsync(T1h, s->T1, sizeof(double) * s->ng * s->s1(),
+                                  cudaMemcpyDeviceToHost, ctx->stream));
+    constexpr size_t HALF = (size_t)32 << 20;          // doubles per staging half
+    if (ctx->hstage_bytes < 2 * HALF * sizeof(double)) {
+        if (ctx->hstage) cudaFreeHost(ctx->hstage);
+        ctx->hstage = nullptr;
+        ctx->hstage_bytes = 0;
+        KV_CHECK(ctx, cudaHostAlloc(&ctx->hstage, 2 * HALF * sizeof(double),
+                                    cudaHostAllocMapped));
+        ctx->hstage_bytes = 2 * HALF * sizeof(double);
+    }
+    double *hs = (double *)ctx->hstage;
+    double *ds = nullptr;
+    KV_CHECK(ctx, cudaHostGetDevicePointer((void **)&ds, ctx->hstage, 0));
+    const int h = (s->spin_on && s->spin_half > 0 && s->nv == s->no) ? s->spin_half : 0;
+    const bool sparse = dst_zeroed && h > 0;
+    const long long P = s->s2(), n = s->no, hh = (long long)h * h;
+    // chunks: whole items of the spin order, or plain ranges of T2
+    const long long per = sparse ? (long long)(HALF / hh) : (long long)HALF;
+    const long long total = sparse ? (long long)s->ng * 6 * hh : (long long)s->ng * P;
+    const long long nch = (total + per - 1) / per;
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+    int st = KVFT_OK;
+    for (int q = 0; q < 2 && st == KVFT_OK; q++)
+        if (cudaEventCreateWithFlags(&ev[q], cudaEventDisableTiming) != cudaSuccess)
+            st = kv_fail(ctx, KVFT_EDEVICE, "read_amplitudes: event");
+    auto fill = [&](long long k) -> int {
+        const long long c0 = k * per, cnt = std::min(per, total - c0);
+        double *dst = ds + (k % 2) * HALF;
+        if (sparse) {
+            const long long el = cnt * hh;
+            const int grid = (int)std::min<long long>((el + 255) / 256, (long long)ctx->sm_count * 8);
+            amp_gather_kernel<<<grid, 256, 0, ctx->stream>>>(s->T2, P, (int)n, h, c0, cnt, dst);
+            KV_TRY(kv_launch_check(ctx, "amp_gather"));
+        } else {
+            KV_CHECK(ctx, cudaMemcpyAsync(dst, s->T2 + c0, sizeof(double) * cnt,
+                                          cudaMemcpyDeviceToHost, ctx->stream));
+        }
+        KV_CHECK(ctx, cudaEventRecord(ev[k % 2], ctx->stream));
+        return KVFT_OK;
+    };
+    if (st == KVFT_OK && nch > 0) st = fill(0);
+    for (long long k = 0; k < nch && st == KVFT_OK; k++) {
+        if (k + 1 < nch) st = fill(k + 1);     // the other half was drained at k - 1
+        if (st != KVFT_OK) break;
+        if (cudaEventSynchronize(ev[k % 2]) != cudaSuccess) {
+            st = kv_fail(ctx, KVFT_EDEVICE, "read_amplitudes: device copy failed");
+            break;
+        }
+        const double *src = hs + (k % 2) * HALF;
+        const long long c0 = k * per, cnt = std::min(per, total - c0);
+        if (sparse) {
+            host_parallel(cnt, [&](long long lo, long long hi) {
+                for (long long it = lo; it < hi; it++) {
+                    double *d = T2h + spin_item_base(c0 + it, P, (int)n, h);
+                    const double *q = src + it * hh;
+                    for (int i1 = 0; i1 < h; i1++)
+                        std::memcpy(d + (long long)i1 * n, q + (long long)i1 * h,
+                                    sizeof(double) * h);
+                }
+            });
+        } else {
+            host_parallel(cnt, [&](long long lo, long long hi) {
+                std::memcpy(T2h + c0 + lo, src + lo, sizeof(double) * (hi - lo));
+            });
+        }
+    }
+    if (st == KVFT_OK && cudaStreamSynchronize(ctx->stream) != cudaSuccess)
+        st = kv_fail(ctx, KVFT_EDEVICE, "read_amplitudes: T1 copy failed");
+    for (int q = 0; q < 2; q++)
+        if (ev[q]) cudaEventDestroy(ev[q]);
+    return st;
 }
 
 int kvft_solver_set_amplitudes(kvft_solver *s, const double *T1h, const double *T2h) {

@@ -96,3 +96,31 @@ def test_spin_breaking_amplitudes_turn_blocks_off(ctx):
         assert sv.spin_blocks() == 0
     finally:
         sv.close()
+
+
+@pytest.mark.parametrize("spin", [True, False])
+def test_staged_read_back_is_exact(ctx, spin):
+    """kvft_solver_read_amplitudes (pinned staging, host threads; with spin
+    blocks and a zeroed destination only the spin-conserving elements) gives
+    the bytes of the plain copy, and with dst_zeroed = 0 overwrites every
+    element of a dirty destination."""
+    ctx.set_precision(_lib.PREC_FP64, 7)
+    sv = solver_for(ctx, UEG())
+    try:
+        assert (sv.spin_blocks(spin) > 0) == spin
+        sv.guess(1)
+        for _ in range(3):
+            sv.step(0.5)
+        shp1, shp2 = (sv.ng, sv.nv, sv.no), (sv.ng, sv.nv, sv.nv, sv.no, sv.no)
+        P1, P2 = numpy.empty(shp1), numpy.empty(shp2)
+        ctx.check(ctx.L.kvft_solver_get_amplitudes(sv.h, P1.ctypes.data_as(_lib.vp),
+                                                    P2.ctypes.data_as(_lib.vp)), "get")
+        T1, T2 = sv.amplitudes()
+        assert numpy.array_equal(T1, P1) and numpy.array_equal(T2, P2)
+        D1, D2 = numpy.full(shp1, numpy.nan), numpy.full(shp2, numpy.nan)
+        ctx.check(ctx.L.kvft_solver_read_amplitudes(sv.h, D1.ctypes.data_as(_lib.vp),
+                                                     D2.ctypes.data_as(_lib.vp), 0), "read")
+        assert numpy.array_equal(D1, P1) and numpy.array_equal(D2, P2)
+        assert numpy.count_nonzero(P2) > 0
+    finally:
+        sv.close()
