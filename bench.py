@@ -424,7 +424,11 @@ def run_gpu(args, w):
     acc64 = solve("fp64_tc", 7, args.accel) if args.precision != "fp64_tc" else sol
     ref64 = solve("fp64_tc", 7, 0) if args.accel else acc64
     h2d = 8 * (n + n * n + n ** 4 + 2 * ng + ng * ng)
-    d2h = 8 * ng * (n * n + n ** 4) + 8 * 7 * (sol["iterations"] + 2)
+    # the amplitudes Kelvin's solve leaves on the instance: T1 and the
+    # spin-conserving elements of T2 cross the link (the host array's other
+    # blocks are zero pages); plus the scalars each iteration reads back
+    h = n // 2
+    d2h = 8 * ng * (n * n + 6 * h ** 4) + 8 * 7 * (sol["iterations"] + 2)
 
     # solves/s with everything resident: per-phase iterations of the measured
     # solve times that phase's measured seconds per iteration
@@ -554,7 +558,9 @@ def run_gpu(args, w):
             "cpu_baseline": {"value": None, "unit": UNIT, "cores": os.cpu_count(),
                              "kind": "port"},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
-                    "d2h_bytes_per_step": d2h},
+                    "d2h_bytes_per_step": d2h,
+                    "how": "ccsd(...).run() from host arrays: integral upload, solve, "
+                           "amplitudes read back into ccsd.T1 / ccsd.T2 (numpy)"},
             "gpu_launches": launches, "clocks": clk}
     est = c2_estimate(t_iter_c1, ref64["iterations"])     # the reference's damped loop
     if per_solve:
@@ -799,7 +805,9 @@ def run_serve(args):
     and p50/p99 latency, completion minus arrival."""
     from kelvin_gb300 import serve
     reqs = serve.request_stream(args.serve, rate=args.rate, seed=0)
-    rep = serve.Server(precision=args.precision, slots=args.slots).serve(reqs)
+    rep = serve.Server(precision=args.precision, slots=args.slots, accel=args.accel,
+                       mix=args.mix if args.accel else None,
+                       low_tconv=args.low_tconv if args.accel else None).serve(reqs)
     done = rep.pop("requests")
     fails = {}
     for d in done:
@@ -807,7 +815,8 @@ def run_serve(args):
             k = d.get("reason", "")[:60]
             fails[k] = fails.get(k, 0) + 1
     print(json.dumps(dict({"serve": args.serve, "rate_per_s": args.rate,
-                           "precision": args.precision, "not_solved": fails}, **rep)))
+                           "precision": args.precision, "accel": args.accel,
+                           "not_solved": fails}, **rep)))
     return 0
 
 

@@ -205,6 +205,16 @@ struct kvft_solver {
     long long aa_k = 0;
     int aa_prec = -1;
     double aa_rr = 0.0;
+    // an accelerated step split at its host decision: the first half (update
+    // map and statistics) is queued and its statistics land in hsc + 16;
+    // aa_step_finish waits for them, solves for the mixing coefficients and
+    // queues the second half
+    bool aa_mid = false;
+    int aa_h = -1;              // spin layout of the history (0: every element)
+    cudaEvent_t aa_ev = nullptr;
+    double aa_damp = 0.0;
+    int aa_nvalid = 0, aa_jnew = -1, aa_grid[2] = {0, 0};
+    double *aa_part = nullptr;
     // CUDA graph of the damped iteration: on when graph_on; gexec replays the
     // launches captured for gkey (damping, precision, spin blocks, grid
     // convention, scratch generation); gwarm: the key of the last eager step
@@ -400,8 +410,9 @@ int detect_spin_blocks(kvft_solver *s) {
 int finish_create(kvft_solver *s, kvft_solver **out) {
     if (cudaStreamSynchronize(s->ctx->stream) != cudaSuccess)
         return kv_fail(s->ctx, KVFT_EDEVICE, "solver set-up kernels failed");
-    KV_CHECK(s->ctx, cudaMallocHost(&s->hsc, 16 * sizeof(double)));
+    KV_CHECK(s->ctx, cudaMallocHost(&s->hsc, 32 * sizeof(double)));
     KV_CHECK(s->ctx, cudaEventCreateWithFlags(&s->done, cudaEventDisableTiming));
+    KV_CHECK(s->ctx, cudaEventCreateWithFlags(&s->aa_ev, cudaEventDisableTiming));
     KV_TRY(detect_spin_blocks(s));
     KV_TRY(pick_chunk(s));
     *out = s;
@@ -424,7 +435,7 @@ int finish_create(kvft_solver *s, kvft_solver **out) {
 struct AaSeg {
     double *x;
     const double *phi;
-    float *rprev;
+    float *rprev;       // rprev and the history: the visit order (compact)
     float *dX[3], *dR[3];
     long long P;        // elements per tau point
     int ng;
@@ -438,10 +449,13 @@ constexpr int AA_BLOCKS = 3; // resident blocks per SM (at most 85 registers a t
 // 1 = beta), four bits each: sa | sb << 1 | si << 2 | sj << 3.
 constexpr unsigned AA_PATTERNS = 0u | 15u << 4 | 10u << 8 | 6u << 12 | 9u << 16 | 5u << 20;
 
-// Calls f(base, o, cnt) with batches of up to AA_U element indices
-// base + o[u] of the segment (u < cnt valid).  T2 with spin runs: one warp per (tau, spin pattern,
-// a, b) quadrant of h x h elements (i, j in their halves), lanes along j;
-// only the spin-conserving elements are visited.  Otherwise every element.
+// Calls f(base, o, cb, cs, cnt) with batches of up to AA_U elements: the
+// amplitude index base + o[u] and the compact index cb + u cs (the position
+// in the visit order, which the FP32 history uses), u < cnt valid.  T2 with
+// spin runs: one warp per (tau, spin pattern, a, b) quadrant of h x h
+// elements (i, j in their halves), lanes along j; only the spin-conserving
+// elements are visited and the compact order holds only them (6/16 of T2).
+// Otherwise every element, the compact index the amplitude index.
 template <class F>
 __device__ __forceinline__ void aa_visit(const AaSeg &g, F f) {
     const int t = threadIdx.x, lane = t % 32;
@@ -468,7 +482,7 @@ __device__ __forceinline__ void aa_visit(const AaSeg &g, F f) {
                     o[u] = i1 * n + (k - i1 * h);
                     if (k < hh) cnt = u + 1;
                 }
-                f(base, o, cnt);
+                f(base, o, it * hh + k0 + lane, 32, cnt);
             }
         }
     } else {
@@ -481,7 +495,7 @@ __device__ __forceinline__ void aa_visit(const AaSeg &g, F f) {
                 o[u] = (int)(u * stride);
                 if (e0 + o[u] < tot) cnt = u + 1;
             }
-            f(e0, o, cnt);
+            f(e0, o, e0, (int)stride, cnt);
         }
     }
 }
@@ -526,9 +540,9 @@ __global__ void __launch_bounds__(AA_T, AA_BLOCKS)
 aa_stats_kernel(AaSeg g, AaHist hs, double *part) {
     float v[7] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
     const bool has_new = hs.dRnew != nullptr;
-    aa_visit(g, [&](long long base, const int (&o)[AA_U], int cnt) {
+    aa_visit(g, [&](long long base, const int (&o)[AA_U], long long cb, int cs, int cnt) {
         const double *phi = g.phi + base, *x = g.x + base;
-        float *rprev = g.rprev + base;
+        float *rprev = g.rprev + cb;
         double ph[AA_U], xx[AA_U];
         float rp[AA_U], dh[NV > 0 ? NV : 1][AA_U];
 #pragma unroll
@@ -536,18 +550,18 @@ aa_stats_kernel(AaSeg g, AaHist hs, double *part) {
             if (u >= cnt) break;
             ph[u] = phi[o[u]];
             xx[u] = x[o[u]];
-            rp[u] = has_new ? rprev[o[u]] : 0.f;
+            rp[u] = has_new ? rprev[u * cs] : 0.f;
 #pragma unroll
             for (int q = 0; q < NV; q++)
-                dh[q][u] = (q == 0 && has_new) ? 0.f : hs.dR[q][base + o[u]];
+                dh[q][u] = (q == 0 && has_new) ? 0.f : hs.dR[q][cb + u * cs];
         }
 #pragma unroll
         for (int u = 0; u < AA_U; u++) {
             if (u >= cnt) break;
             const float r = (float)(ph[u] - xx[u]);
             const float dn = has_new ? r - rp[u] : 0.f;
-            if (has_new) hs.dRnew[base + o[u]] = dn;
-            rprev[o[u]] = r;
+            if (has_new) hs.dRnew[cb + u * cs] = dn;
+            rprev[u * cs] = r;
 #pragma unroll
             for (int q = 0; q < NV; q++) {
                 const float di = (q == 0 && has_new) ? dn : dh[q][u];
@@ -572,7 +586,7 @@ aa_update_kernel(AaSeg g, AaHist hs, double beta, float g0, float g1, float g2,
     float v[2] = {0.f, 0.f};
     const float gam[3] = {g0, g1, g2};
     const float bf = (float)beta;
-    aa_visit(g, [&](long long base, const int (&o)[AA_U], int cnt) {
+    aa_visit(g, [&](long long base, const int (&o)[AA_U], long long cb, int cs, int cnt) {
         const double *phi = g.phi + base;
         double *x = g.x + base;
         double ph[AA_U], xx[AA_U];
@@ -584,7 +598,8 @@ aa_update_kernel(AaSeg g, AaHist hs, double beta, float g0, float g1, float g2,
             xx[u] = x[o[u]];
             float a = 0.f;
 #pragma unroll
-            for (int q = 0; q < NV; q++) a = fmaf(gam[q], fmaf(bf, hs.dR[q][base + o[u]], hs.dX[q][base + o[u]]), a);
+            for (int q = 0; q < NV; q++)
+                a = fmaf(gam[q], fmaf(bf, hs.dR[q][cb + u * cs], hs.dX[q][cb + u * cs]), a);
             hsum[u] = a;
         }
 #pragma unroll
@@ -594,7 +609,7 @@ aa_update_kernel(AaSeg g, AaHist hs, double beta, float g0, float g1, float g2,
             const double xn = xx[u] + d;
             x[o[u]] = xn;
             const float df = (float)d, xf = (float)xn;
-            hs.dXst[base + o[u]] = df;
+            hs.dXst[cb + u * cs] = df;
             v[0] = fmaf(df, df, v[0]);
             v[1] = fmaf(xf, xf, v[1]);
         }
@@ -674,6 +689,7 @@ void destroy(kvft_solver *s) {
     for (void *p : s->allocs) cudaFree(p);
     if (s->hsc) cudaFreeHost(s->hsc);
     if (s->done) cudaEventDestroy(s->done);
+    if (s->aa_ev) cudaEventDestroy(s->aa_ev);
     delete s;
 }
 
@@ -851,11 +867,53 @@ bool aa_solve(int n, double A[3][3], double *t, double *g) {
     return true;
 }
 
+// The T2 spin half the Anderson passes visit by (0: every element).
+int aa_half(const kvft_solver *s) {
+    return (s->spin_on && s->spin_half > 0 && s->nv == s->no) ? s->spin_half : 0;
+}
+
+// FP32 history of depth m in the visit order of the current spin layout:
+// ng (nv no + 6 h^4) words per array with spin runs, ng (nv no + (nv no)^2)
+// without; arrays of another layout are freed first.
+int aa_alloc(kvft_solver *s, int m) {
+    const int h = aa_half(s);
+    float **arr[7] = {&s->aa_rprev, &s->aa_dX[0], &s->aa_dR[0], &s->aa_dX[1], &s->aa_dR[1],
+                      &s->aa_dX[2], &s->aa_dR[2]};
+    if (s->aa_h != h) {
+        cudaStreamSynchronize(s->ctx->stream);
+        for (float **p : arr) {
+            if (!*p) continue;
+            for (size_t i = 0; i < s->allocs.size(); i++)
+                if (s->allocs[i] == (void *)*p) {
+                    s->allocs.erase(s->allocs.begin() + i);
+                    break;
+                }
+            cudaFree(*p);
+            *p = nullptr;
+        }
+        s->aa_h = h;
+        s->chunk_prec = -1;
+    }
+    if (m == 0) return KVFT_OK;
+    const size_t words = (size_t)s->ng * (s->s1() + (h ? 6 * (size_t)h * h * h * h : s->s2()));
+    for (int i = 0; i < 1 + 2 * m; i++) {
+        if (*arr[i]) continue;
+        void *q = nullptr;
+        if (cudaMalloc(&q, sizeof(float) * words) != cudaSuccess) {
+            cudaGetLastError();
+            return kv_fail(s->ctx, KVFT_ENOMEM, "solver_set_acceleration: no room for the history");
+        }
+        s->allocs.push_back(q);
+        *arr[i] = (float *)q;
+        s->chunk_prec = -1;            // re-size the tau chunk for the memory left
+    }
+    return KVFT_OK;
+}
+
 void aa_segments(kvft_solver *s, AaSeg *g1, AaSeg *g2) {
     const long long n1 = s->s1(), n2 = s->s2(), ng = s->ng;
     *g1 = AaSeg{s->T1, s->T1b, s->aa_rprev, {}, {}, n1, s->ng, 0, 0};
-    *g2 = AaSeg{s->T2, s->T2b, s->aa_rprev + ng * n1, {}, {}, n2, s->ng,
-                (s->spin_on && s->spin_half > 0 && s->nv == s->no) ? s->spin_half : 0, s->no};
+    *g2 = AaSeg{s->T2, s->T2b, s->aa_rprev + ng * n1, {}, {}, n2, s->ng, aa_half(s), s->no};
     for (int i = 0; i < s->aa_m; i++) {
         g1->dX[i] = s->aa_dX[i];
         g1->dR[i] = s->aa_dR[i];
@@ -884,6 +942,10 @@ double aa_visited(const AaSeg &g) {
 // Omega_cc).  One host wait, for the least-squares coefficients.
 int aa_step_begin(kvft_solver *s, double damp) {
     kvft_ctx *ctx = s->ctx;
+    if (aa_half(s) != s->aa_h) {       // the spin layout changed: a new history
+        KV_TRY(aa_alloc(s, s->aa_m));
+        s->aa_k = 0;
+    }
     if (!s->norms_valid) KV_TRY(refresh_norms(s));
     KV_TRY(form_tbar(s));
     // Phi(x) in place of tbar (spin-conserving elements only: the passes
@@ -929,10 +991,37 @@ int aa_step_begin(kvft_solver *s, double damp) {
             KV_TRY(kv_launch_check(ctx, "aa_reduce"));
         }
     }
-    double st[14];
-    KV_CHECK(ctx, cudaMemcpyAsync(st, s->dsc + 8, sizeof(st), cudaMemcpyDeviceToHost,
-                                  ctx->stream));
-    KV_CHECK(ctx, cudaStreamSynchronize(ctx->stream));
+    KV_CHECK(ctx, cudaMemcpyAsync(s->hsc + 16, s->dsc + 8, 14 * sizeof(double),
+                                  cudaMemcpyDeviceToHost, ctx->stream));
+    KV_CHECK(ctx, cudaEventRecord(s->aa_ev, ctx->stream));
+    s->aa_mid = true;
+    s->aa_damp = damp;
+    s->aa_nvalid = nvalid;
+    s->aa_jnew = jnew;
+    s->aa_grid[0] = gridA[0];
+    s->aa_grid[1] = gridA[1];
+    s->aa_part = part;
+    s->pending = true;
+    return KVFT_OK;
+}
+
+// The second half of an accelerated step: the host's least-squares solve on
+// the statistics of the first, then the update pass, the energy and the
+// step's scalars (as the damped step leaves them).
+int aa_step_finish(kvft_solver *s) {
+    kvft_ctx *ctx = s->ctx;
+    s->aa_mid = false;
+    KV_CHECK(ctx, cudaEventSynchronize(s->aa_ev));
+    const double *st = s->hsc + 16;
+    const int m = s->aa_m;
+    AaSeg g[2];
+    aa_segments(s, &g[0], &g[1]);
+    long long k = s->aa_k;
+    const int jnew = s->aa_jnew;
+    int nvalid = s->aa_nvalid;
+    const int gridA[2] = {s->aa_grid[0], s->aa_grid[1]};
+    double *part = s->aa_part;
+    const double damp = s->aa_damp;
     const double rr = st[6] + st[13];
     if (!std::isfinite(rr)) return kv_fail(ctx, KVFT_EDIVERGE, "non-finite residual");
     double gam[3] = {0.0, 0.0, 0.0};
@@ -998,7 +1087,6 @@ int aa_step_begin(kvft_solver *s, double damp) {
                      s->dsc + 4, s->spin_on ? s->spin_half : 0));
     KV_TRY(queue_readback(s));
     KV_CHECK(ctx, cudaEventRecord(s->done, ctx->stream));
-    s->pending = true;
     return KVFT_OK;
 }
 
@@ -1104,6 +1192,7 @@ int kvft_solver_step_end(kvft_solver *s, double *energy, double *res) {
     kvft_ctx *ctx = s->ctx;
     if (!s->pending) return kv_fail(ctx, KVFT_EINVAL, "solver_step_end: no step is pending");
     s->pending = false;
+    if (s->aa_mid) KV_TRY(aa_step_finish(s));
     KV_CHECK(ctx, cudaEventSynchronize(s->done));
     const double *h = s->hsc;
     int flag = 0;
@@ -1463,26 +1552,7 @@ int kvft_solver_set_acceleration(kvft_solver *s, int m) {
                                              "solver_set_acceleration: depth must be 0..3");
     if (s->pending) return kv_fail(s->ctx, KVFT_EINVAL, "solver_set_acceleration: a step is pending");
     cudaSetDevice(s->ctx->device);
-    const size_t words = (size_t)s->ng * (s->s1() + s->s2());
-    auto falloc = [&](float **p) -> int {
-        if (*p) return KVFT_OK;
-        void *q = nullptr;
-        if (cudaMalloc(&q, sizeof(float) * words) != cudaSuccess) {
-            cudaGetLastError();
-            return kv_fail(s->ctx, KVFT_ENOMEM, "solver_set_acceleration: no room for the history");
-        }
-        s->allocs.push_back(q);
-        *p = (float *)q;
-        return KVFT_OK;
-    };
-    if (m > 0) {
-        KV_TRY(falloc(&s->aa_rprev));
-        for (int i = 0; i < m; i++) {
-            KV_TRY(falloc(&s->aa_dX[i]));
-            KV_TRY(falloc(&s->aa_dR[i]));
-        }
-        s->chunk_prec = -1;            // re-size the tau chunk for the memory left
-    }
+    KV_TRY(aa_alloc(s, m));
     s->aa_m = m;
     s->aa_k = 0;
     return KVFT_OK;

@@ -86,8 +86,9 @@ class Solve(object):
     """One request on the device: its solver and convergence state (the
     phases of ccsd.converge, advanced one sweep at a time)."""
 
-    def __init__(self, req, levels, refine, conv, start, warm):
+    def __init__(self, req, levels, refine, conv, start, warm, low_tconv=None):
         self.req = req
+        self.low_tconv = low_tconv        # few-digit phases also end below it
         self.levels = list(levels)        # digit levels of the phases, last = refine
         self.refine = refine
         self.conv = conv
@@ -120,6 +121,8 @@ class Solve(object):
             else:
                 self.since += 1
                 stalled = self.since >= 3
+            if self.low_tconv is not None:
+                conv = res < self.low_tconv
         self.Eold = E
         if last and (conv or self.it_phase >= self.conv["max_iter"]):
             self.omega_cc, self.converged, self.done = E, conv, True
@@ -136,8 +139,9 @@ class DeviceBackend(object):
     tau-chunk workspace capped so that the slots share the device, and each
     solve's iterations captured once and replayed as a CUDA graph."""
 
-    def __init__(self, slots, workspace_bytes, device=0, graphs=True):
+    def __init__(self, slots, workspace_bytes, device=0, graphs=True, accel=0):
         self.graphs = graphs
+        self.accel = accel
         self.free_ctx = [_lib.Context(device) for _ in range(slots)]
         for c in self.free_ctx:
             c.set_workspace_limit(workspace_bytes)
@@ -148,8 +152,15 @@ class DeviceBackend(object):
 
     def footprint(self, req, precision):
         prec = PRECISIONS[precision][0]
-        return int(_lib.lib().kvft_solver_footprint(req.n_spin_orbitals(), req.ng, prec)) + \
+        fp = int(_lib.lib().kvft_solver_footprint(req.n_spin_orbitals(), req.ng, prec)) + \
             self.workspace_bytes
+        if self.accel:
+            # the FP32 Anderson history (1 + 2 depth arrays) over T1 and the
+            # spin-conserving elements of T2 (the model systems are spin-blocked)
+            n = req.n_spin_orbitals()
+            h = n // 2
+            fp += 4 * (1 + 2 * self.accel) * req.ng * (n * n + 6 * h ** 4)
+        return fp
 
     def open(self, sv, warm):
         from .cc_utils import DeviceSolver
@@ -170,7 +181,9 @@ class DeviceBackend(object):
             solver.guess(2)
         else:
             solver.guess(1)
-        if self.graphs:
+        if self.accel:
+            solver.set_acceleration(self.accel)
+        elif self.graphs:
             solver.set_graph(True)        # iterations replayed as CUDA graphs
         sv.handle = (ctx, solver, s)
         sv.level_set = sv.level()
@@ -211,11 +224,17 @@ class Server(object):
     ``clock``/``sleep`` default to real time.  ``budget``: device bytes the
     active solves may hold (default 90 % of the device).  Converged
     amplitudes are kept on the host per (system, grid) and temperature while
-    they take at most ``warm_bytes``; ``warm=False`` turns warm starts off."""
+    they take at most ``warm_bytes``; ``warm=False`` turns warm starts off.
+    ``accel`` > 0: Anderson mixing of that depth with mixing factor ``mix``
+    (None: 1 - damp), the few-digit phase going straight to the
+    FP64-accurate one and ending once Kelvin's residual is below
+    ``low_tconv`` (as ccsd.converge); the split step keeps the solves
+    overlapped on the device."""
 
     def __init__(self, precision='mixed', slots=4, budget=None, backend=None,
                  clock=time.perf_counter, sleep=time.sleep, warm_bytes=8 << 30, warm=True,
-                 damp=0.5, econv=1e-8, max_iter=200, workspace_bytes=24 << 30, graphs=True):
+                 damp=0.5, econv=1e-8, max_iter=200, workspace_bytes=24 << 30, graphs=True,
+                 accel=0, mix=None, low_tconv=None):
         self.precision = precision
         self.slots = slots
         self.budget = budget
@@ -225,15 +244,19 @@ class Server(object):
         self.clock, self.sleep = clock, sleep
         self.warm_bytes = warm_bytes
         self.use_warm = warm
-        self.damp = damp
+        self.accel = accel
+        self.low_tconv = low_tconv if accel else None
+        self.damp = 1.0 - mix if accel and mix is not None else damp
         self.conv = {"econv": econv, "tconv": 1000.0 * econv, "max_iter": max_iter}
         self.cache = {}                   # key -> {theta: amplitudes}
         digits = PRECISIONS[precision][1]
-        self.levels = (digits, 5, 7) if precision == 'mixed' else (digits,)
+        self.levels = ((digits, 7) if accel else (digits, 5, 7)) if precision == 'mixed' \
+            else (digits,)
 
     def backend(self):
         if self._backend is None:
-            self._backend = DeviceBackend(self.slots, self.workspace_bytes, graphs=self.graphs)
+            self._backend = DeviceBackend(self.slots, self.workspace_bytes, graphs=self.graphs,
+                                          accel=self.accel)
         return self._backend
 
     def _budget(self):
@@ -291,7 +314,8 @@ class Server(object):
                     break                 # waits for memory to free up
                 pending.pop(0)
                 warm = self._warm(r)
-                sv = Solve(r, self.levels, self.levels[-1], self.conv, now, warm is not None)
+                sv = Solve(r, self.levels, self.levels[-1], self.conv, now, warm is not None,
+                           self.low_tconv)
                 be.open(sv, warm)
                 fps[r.rid] = fp
                 used += fp

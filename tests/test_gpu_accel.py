@@ -79,3 +79,34 @@ def test_benchmarked_scheme_vs_oracle(ctx):
           % (cc.phases, Ecc, meta["omega_cc"]))
     assert cc.converged
     assert abs(Ecc - meta["omega_cc"]) < 1e-8
+
+
+def test_history_layouts_agree(ctx):
+    """The FP32 history in the compact spin order (spin blocks on) and over
+    every element (off) give the same accelerated iterates; turning the spin
+    blocks off mid-solve starts a new history in the full layout."""
+    from kelvin_gb300.cc_utils import DeviceSolver
+    from kelvin_gb300.quadrature import ft_quad
+    s = systems.ueg_recipe(14, 4.0, 19, 0.5)
+    beta = 1.0 / s.T
+    ti, g, G = ft_quad(10, beta, "lin")
+    ctx.set_precision(_lib.PREC_FP64, 7)
+    hist = {}
+    for on in (True, False):
+        sv = DeviceSolver.from_system(ctx, s.g_energies_tot(), s.g_fock_tot(), s.g_aint_tot(),
+                                      beta, s.mu, ti, g, G)
+        try:
+            assert (sv.spin_blocks(on) > 0) == on
+            sv.set_acceleration(3)
+            sv.guess(1)
+            hist[on] = [sv.step(0.3) for _ in range(8)]
+            if on:
+                sv.spin_blocks(False)
+                E, res = sv.step(0.3)
+                assert numpy.isfinite(E) and res < hist[on][-1][1] * 10
+        finally:
+            sv.close()
+    # the FP32 sums run in another order (the full layout adds the zero
+    # elements), so the mixing coefficients agree to FP32 rounding only
+    for (e1, r1), (e2, r2) in zip(hist[True], hist[False]):
+        assert abs(e1 - e2) < 1e-8 and abs(r1 - r2) < 1e-4 * r2

@@ -17,13 +17,19 @@ def _requests():
             R(4, 0.03, 'ueg', (14, 19, 1.5), 2.0, 20)]
 
 
-def test_results_alone_and_in_the_mix():
-    mix = serve.Server(precision='mixed', slots=3, warm=False, workspace_bytes=4 << 30)
+@pytest.mark.parametrize("accel", [0, 3])
+def test_results_alone_and_in_the_mix(accel):
+    """Kelvin's damped update with CUDA-graph replay, and the accelerated
+    scheme (depth 3, mixing factor 0.7, residual cut 1e-4) whose split step
+    keeps the solves overlapped."""
+    kw = dict(accel=accel, mix=0.7, low_tconv=1e-4) if accel else {}
+    mix = serve.Server(precision='mixed', slots=3, warm=False, workspace_bytes=4 << 30, **kw)
     rep = mix.serve(_requests())
     assert rep["solves"] == 5 and rep["rejected"] == 0
     assert rep["max_active"] >= 2                    # their iterations overlapped
     by_mix = {d["rid"]: d for d in rep["requests"]}
-    alone = serve.Server(precision='mixed', slots=1, warm=False, workspace_bytes=4 << 30)
+    alone = serve.Server(precision='mixed', slots=1, warm=False, workspace_bytes=4 << 30,
+                         **kw)
     for r in _requests():
         one = alone.serve([serve.Request(r.rid, 0.0, r.kind, r.params, r.theta, r.ng)])
         d = one["requests"][0]

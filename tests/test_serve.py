@@ -120,6 +120,7 @@ def test_default_footprint_is_the_solver_footprint():
     from kelvin_gb300 import _lib
     be = serve.DeviceBackend.__new__(serve.DeviceBackend)
     be.workspace_bytes = 1 << 30
+    be.accel = 0
     small = serve.Request(0, 0.0, 'ueg', (14, 19, 1.0), 1.0, 10)
     big = serve.Request(1, 0.0, 'ueg', (38, 57, 1.0), 1.0, 10)
     wide = serve.Request(2, 0.0, 'ueg', (38, 57, 1.0), 1.0, 40)
@@ -127,6 +128,12 @@ def test_default_footprint_is_the_solver_footprint():
     assert f(small) < f(big) < f(wide)
     assert f(big) > 8 * 114 ** 4 * 10 + (1 << 30)
     assert f(small) == _lib.lib().kvft_solver_footprint(38, 10, _lib.PREC_MIXED) + (1 << 30)
+    # with Anderson mixing of depth 3: seven FP32 arrays over T1 and the
+    # spin-conserving elements of T2
+    be.accel = 3
+    assert f(small) == _lib.lib().kvft_solver_footprint(38, 10, _lib.PREC_MIXED) + (1 << 30) \
+        + 4 * 7 * 10 * (38 * 38 + 6 * 19 ** 4)
+    be.accel = 0
 
     class NoSolve(FakeBackend):
         def footprint(self, req, precision):
@@ -140,3 +147,42 @@ def test_default_footprint_is_the_solver_footprint():
                        sleep=clock.sleep)
     rep = srv.serve(reqs)
     assert rep["solves"] == 0 and rep["rejected"] == 12 and rep["p50_ms"] is None
+
+
+class CutBackend(FakeBackend):
+    """The few-digit phase's residual falls by 10x a sweep from 1 (so a cut at
+    1e-2 ends it after three sweeps); records the mixing factor it is given."""
+
+    def begin(self, sv, damp):
+        self.damps = getattr(self, "damps", set()) | {damp}
+        FakeBackend.begin(self, sv, damp)
+
+    def end(self, sv):
+        if sv.phase < len(sv.levels) - 1:
+            self.begun.discard(sv.req.rid)
+            return -1.0, 10.0 ** -(sv.it_phase + 1)
+        return FakeBackend.end(self, sv)
+
+
+def test_accelerated_scheme_phases():
+    """With accel the mixed form goes from 3 digit levels straight to 7, the
+    few-digit phase ends at the residual cut, and the solves step with the
+    mixing factor's damp = 1 - mix."""
+    clock = FakeClock()
+    R = serve.Request
+    reqs = [R(0, 0.0, 'ueg', (14, 19, 4.0), 0.5, 10)]
+    be = CutBackend(clock, {0: 100}, {0: 4})
+    srv = serve.Server(precision='mixed', slots=2, budget=900, backend=be, clock=clock,
+                       sleep=clock.sleep, accel=3, mix=0.7, low_tconv=1e-2)
+    assert srv.levels == (3, 7)
+    rep = srv.serve(reqs)
+    d = rep["requests"][0]
+    # the cut ends the few-digit phase at its third sweep (1e-3 < 1e-2; a
+    # stall would take four); the fake's last phase meets Kelvin's test at
+    # its second sweep (an unchanged energy)
+    assert d["ok"] and d["converged"] and d["iterations"] == 3 + 2
+    assert be.damps == {1.0 - 0.7}
+    # without accel: Kelvin's damping and the 3, 5, 7 ladder
+    srv = serve.Server(precision='mixed', slots=2, budget=900, backend=FakeBackend(
+        FakeClock(), {0: 100}, {0: 4}), clock=clock, sleep=clock.sleep)
+    assert srv.levels == (3, 5, 7) and srv.damp == 0.5 and srv.low_tconv is None
