@@ -213,8 +213,13 @@ struct kvft_solver {
     int aa_h = -1;              // spin layout of the history (0: every element)
     cudaEvent_t aa_ev = nullptr;
     double aa_damp = 0.0;
-    int aa_nvalid = 0, aa_jnew = -1, aa_grid[2] = {0, 0};
+    int aa_nvalid = 0, aa_grid[2] = {0, 0};
     double *aa_part = nullptr;
+    // history slots: aa_ord the complete pairs, newest first; aa_pend the
+    // slot whose step dX the last update wrote (its dR completes at the next
+    // statistics pass; -1: none); aa_slots the pairs of the step in flight
+    int aa_ord[3] = {0, 0, 0}, aa_nord = 0, aa_pend = -1, aa_slots[3] = {0, 0, 0};
+    bool aa_has_new = false;
     // CUDA graph of the damped iteration: on when graph_on; gexec replays the
     // launches captured for gkey (damping, precision, spin blocks, grid
     // convention, scratch generation); gwarm: the key of the last eager step
@@ -952,16 +957,25 @@ int aa_step_begin(kvft_solver *s, double damp) {
     // below read no other)
     KV_TRY(integrate(s, 0, 0.0, s->T1b, s->T2b, s->T1b, s->T2b, nullptr, nullptr));
     const int prec = ctx->precision * 16 + ctx->digits;
-    if (prec != s->aa_prec) {          // a new precision is a new map: restart
+    // a new precision is a new map: restart (keeping the earlier map's pairs
+    // doubled the FP64-accurate sweeps of the 114-spin-orbital mixed solve)
+    if (prec != s->aa_prec) {
         s->aa_k = 0;
         s->aa_prec = prec;
+    }
+    if (s->aa_k == 0) {
+        s->aa_nord = 0;
+        s->aa_pend = -1;
     }
     const int m = s->aa_m;
     AaSeg g[2];
     aa_segments(s, &g[0], &g[1]);
-    long long k = s->aa_k;
-    const int jnew = k >= 1 ? (int)((k - 1) % m) : -1;
-    int nvalid = (int)std::min<long long>(k, m);
+    // the pairs of this step, newest first: the pending one (completed by
+    // this pass) and the complete ones
+    const bool has_new = s->aa_pend >= 0;
+    int slots[3], nvalid = 0;
+    if (has_new) slots[nvalid++] = s->aa_pend;
+    for (int i = 0; i < s->aa_nord && nvalid < m; i++) slots[nvalid++] = s->aa_ord[i];
     const int gridA[2] = {aa_launch_grid(ctx, g[0]), aa_launch_grid(ctx, g[1])};
     void *pp = nullptr;
     KV_TRY(kv_scratch(ctx, "aa_partial",
@@ -973,11 +987,10 @@ int aa_step_begin(kvft_solver *s, double damp) {
         for (int q = 0; q < 2; q++) {
             AaHist hs{};
             for (int t = 0; t < nvalid; t++) {
-                const int i = (jnew - t + m) % m;
-                hs.dX[t] = g[q].dX[i];
-                hs.dR[t] = g[q].dR[i];
+                hs.dX[t] = g[q].dX[slots[t]];
+                hs.dR[t] = g[q].dR[slots[t]];
             }
-            hs.dRnew = jnew >= 0 ? g[q].dR[jnew] : nullptr;
+            hs.dRnew = has_new ? g[q].dR[slots[0]] : nullptr;
             double *pq = part + (q ? 7 * gridA[0] : 0);
             switch (nvalid) {
             case 0: aa_stats_kernel<0><<<gridA[q], AA_T, 0, ctx->stream>>>(g[q], hs, pq); break;
@@ -997,7 +1010,8 @@ int aa_step_begin(kvft_solver *s, double damp) {
     s->aa_mid = true;
     s->aa_damp = damp;
     s->aa_nvalid = nvalid;
-    s->aa_jnew = jnew;
+    s->aa_has_new = has_new;
+    for (int t = 0; t < nvalid; t++) s->aa_slots[t] = slots[t];
     s->aa_grid[0] = gridA[0];
     s->aa_grid[1] = gridA[1];
     s->aa_part = part;
@@ -1016,9 +1030,11 @@ int aa_step_finish(kvft_solver *s) {
     const int m = s->aa_m;
     AaSeg g[2];
     aa_segments(s, &g[0], &g[1]);
-    long long k = s->aa_k;
-    const int jnew = s->aa_jnew;
+    const long long k = s->aa_k;
+    const bool has_new = s->aa_has_new;
     int nvalid = s->aa_nvalid;
+    int slot[3];
+    for (int t = 0; t < nvalid; t++) slot[t] = s->aa_slots[t];
     const int gridA[2] = {s->aa_grid[0], s->aa_grid[1]};
     double *part = s->aa_part;
     const double damp = s->aa_damp;
@@ -1027,11 +1043,9 @@ int aa_step_finish(kvft_solver *s) {
     double gam[3] = {0.0, 0.0, 0.0};
     if (nvalid > 0 && rr > 100.0 * s->aa_rr) nvalid = 0;     // blew up: plain step, restart
     if (nvalid > 0) {
-        int slot[3];
-        for (int q = 0; q < nvalid; q++) slot[q] = (jnew - q + m) % m;
-        for (int q = 0; q < nvalid; q++) {
-            s->aa_G[jnew][slot[q]] = s->aa_G[slot[q]][jnew] = st[q] + st[7 + q];
-        }
+        if (has_new)                   // the completed pair against every pair
+            for (int q = 0; q < nvalid; q++)
+                s->aa_G[slot[0]][slot[q]] = s->aa_G[slot[q]][slot[0]] = st[q] + st[7 + q];
         double A[3][3], t[3];
         for (int q = 0; q < nvalid; q++) {
             t[q] = st[3 + q] + st[10 + q];
@@ -1039,9 +1053,18 @@ int aa_step_finish(kvft_solver *s) {
         }
         if (!aa_solve(nvalid, A, t, gam)) nvalid = 0;
     }
-    if (nvalid == 0) k = 0;                // restart the history from this step
-    const int jst = (int)(k % m);
-    const int slot0 = nvalid > 0 ? jnew : 0;
+    // complete pairs after this step (none: the history restarts here), and
+    // the slot this step's dX goes to: a free one, else the oldest pair's
+    // (read by this update before each element is overwritten)
+    s->aa_nord = nvalid;
+    for (int t = 0; t < nvalid; t++) s->aa_ord[t] = slot[t];
+    bool used[3] = {false, false, false};
+    for (int t = 0; t < s->aa_nord; t++) used[s->aa_ord[t]] = true;
+    int jst = -1;
+    for (int j = 0; j < m && jst < 0; j++)
+        if (!used[j]) jst = j;
+    if (jst < 0) jst = s->aa_ord[--s->aa_nord];
+    s->aa_pend = jst;
     const double beta = 1.0 - damp;
     const float gf[3] = {(float)gam[0], (float)gam[1], (float)gam[2]};
     const int gridB[2] = {gridA[0], gridA[1]};
@@ -1051,9 +1074,8 @@ int aa_step_finish(kvft_solver *s) {
         for (int q = 0; q < 2; q++) {
             AaHist hs{};
             for (int t = 0; t < nvalid; t++) {
-                const int i = (slot0 - t + m) % m;
-                hs.dX[t] = g[q].dX[i];
-                hs.dR[t] = g[q].dR[i];
+                hs.dX[t] = g[q].dX[slot[t]];
+                hs.dR[t] = g[q].dR[slot[t]];
             }
             hs.dXst = g[q].dX[jst];
             double *pq = part + (q ? 2 * gridB[0] : 0);
