@@ -403,7 +403,7 @@ int kv_make_tau(kvft_ctx *ctx, int batch, int nv, int no, const double *t1,
                 const double *t2, double c, double *out, int spin_half) {
     long long total = (long long)batch * nv * nv * no * no;
     if (total == 0) return KVFT_OK;
-    KvProfScope prof(ctx, KV_CAT_ELEM, 16.0 * total);
+    KvProfScope prof(ctx, KV_CAT_ELEM, 16.0 * total * kv_spin_frac(nv, no, spin_half));
     const long long nblk = (long long)batch * nv * nv;
     if (no > 3072) return kv_fail(ctx, KVFT_EINVAL, "make_tau: more than 3072 occupied orbitals");
     make_tau_kernel<<<(unsigned)std::min(nblk, (long long)ctx->sm_count * 16), 256,
@@ -417,7 +417,7 @@ int kv_make_wmbej_tmp(kvft_ctx *ctx, int batch, int nv, int no,
     long long total = (long long)batch * nv * nv * no * no;
     if (total == 0) return KVFT_OK;
     if (batch > 65535) return kv_fail(ctx, KVFT_EINVAL, "wmbej_tmp: batch too large");
-    KvProfScope prof(ctx, KV_CAT_ELEM, 16.0 * total);
+    KvProfScope prof(ctx, KV_CAT_ELEM, 16.0 * total * kv_spin_frac(nv, no, spin_half));
     // each block walks several (b, j): with spin blocks most of its tiles are
     // skipped, and short-lived blocks would leave the SMs waiting for new ones
     const dim3 grid(((nv + 31) / 32) * ((no + 31) / 32), std::min(nv * no, 2048), batch);
@@ -437,11 +437,12 @@ int kv_assemble_t2(kvft_ctx *ctx, int batch, int nv, int no, double fac, const d
     }
     if (nv < 2) return KVFT_OK;
     if (batch > 65535) return kv_fail(ctx, KVFT_EINVAL, "assemble_t2: batch too large");
-    KvProfScope prof(ctx, KV_CAT_ELEM, 8.0 * total * (Lc ? 3.25 : 3.0));
+    const int sh = (nv == no && nv == 2 * spin_half) ? spin_half : 0;
+    KvProfScope prof(ctx, KV_CAT_ELEM,
+                     8.0 * total * (Lc ? 3.25 : 3.0) * kv_spin_frac(nv, no, sh));
     const int nt = (no + 31) / 32;
     const int pv = nv * (nv - 1) / 2;
     const dim3 grid(nt * (nt + 1) / 2, std::min(pv, 65535), batch);
-    const int sh = (nv == no && nv == 2 * spin_half) ? spin_half : 0;
 #define KV_ASM(fs_, seed_)                                                                  \
     assemble_t2_kernel<fs_, seed_><<<grid, 256, 0, ctx->stream>>>(nv, no, sh, fac, Z, Lc, seed, \
                                                                   T2)
@@ -465,7 +466,7 @@ int kv_make_tau_pairs(kvft_ctx *ctx, int batch, int nv, int no, const double *t1
     const int pv = nv * (nv - 1) / 2, po = no * (no - 1) / 2;
     long long total = (long long)batch * pv * po;
     if (total == 0) return KVFT_OK;
-    KvProfScope prof(ctx, KV_CAT_ELEM, 16.0 * total);
+    KvProfScope prof(ctx, KV_CAT_ELEM, 16.0 * total * kv_spin_frac(nv, no, sh));
     const long long nblk = (long long)batch * pv;
     make_tau_pairs_kernel<<<(unsigned)std::min(nblk, (long long)ctx->sm_count * 16), 256, 0,
                             ctx->stream>>>(nblk, nv, no, pv, po, sh, t1, t2, out);
@@ -495,7 +496,8 @@ int kv_pair_gather(kvft_ctx *ctx, int batch, int n1, int n2, const double *A,
     }
     long long total = (long long)batch * g.P1 * g.P2;
     if (total == 0) return KVFT_OK;
-    KvProfScope prof(ctx, KV_CAT_ELEM, 8.0 * total * (B ? 3 : 2));
+    KvProfScope prof(ctx, KV_CAT_ELEM,
+                     8.0 * total * (B ? 3 : 2) * kv_spin_frac(n1, n2, g.sh));
     const long long nblk = (long long)batch * g.P1;
     pair_gather_kernel<<<(unsigned)std::min(nblk, (long long)ctx->sm_count * 16), 256, 0,
                          ctx->stream>>>(nblk, g, out);

@@ -164,10 +164,12 @@ int kv_energy(kvft_ctx *ctx, int ng, int nv, int no, const double *T1, const dou
     void *part = nullptr;
     KV_TRY(kv_scratch(ctx, "energy_partial", sizeof(double) * (nblk + 1), &part));
     double *pp = (double *)part;
-    // algorithmic bytes: T2 (all tau points) + eri + T1
-    KvProfScope prof(ctx, KV_CAT_ENERGY,
-                     8.0 * ((double)ng * V2 * O2 + (double)V2 * O2 + (double)ng * nv * no));
+    // algorithmic bytes: T2 (all tau points) + eri + T1; with spin blocks the
+    // spin-conserving elements of T2 and eri
     const int sh = (nv == no && nv == 2 * spin_half) ? spin_half : 0;
+    KvProfScope prof(ctx, KV_CAT_ENERGY,
+                     8.0 * (((double)ng * V2 * O2 + (double)V2 * O2) * kv_spin_frac(nv, no, sh) +
+                            (double)ng * nv * no));
     energy2_kernel<<<grid, 256, 0, ctx->stream>>>(ng, nv, no, T1, T2, eri, g, qterm, sh, pp);
     KV_TRY(kv_launch_check(ctx, "energy2"));
     energy1_kernel<<<1, 256, 0, ctx->stream>>>(ng, nv, no, T1, f, g, pp + nblk);

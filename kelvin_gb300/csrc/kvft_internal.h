@@ -151,6 +151,13 @@ struct KvTPackScope {
         if (!prev) ctx->tpack.clear();
     }
 };
+// Fraction of a T2-shaped tensor (nv nv no no) that the spin-conserving
+// blocks hold: 6 of the 16 spin blocks when nv = no = 2 sh, else all.  The
+// profiled algorithmic bytes of a pass that touches only those elements are
+// scaled by it.
+inline double kv_spin_frac(int nv, int no, int sh) {
+    return (sh > 0 && nv == no && nv == 2 * sh) ? 6.0 / 16.0 : 1.0;
+}
 struct KvSpinScope {
     kvft_ctx *ctx;
     int prev;

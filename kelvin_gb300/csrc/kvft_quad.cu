@@ -593,7 +593,8 @@ int quad_dense_launch(kvft_ctx *ctx, int mode, QuadParams &q, const double *tbar
     const long long blocks = (q.P + QT - 1) / QT;
     const int grid = (int)std::max(1LL, std::min(blocks, (long long)std::max(per_sm, 1) *
                                                              ctx->sm_count));
-    KvProfScope prof(ctx, KV_CAT_QUAD, 8.0 * ng * (double)q.P * (mode == 0 ? 2 : 3));
+    KvProfScope prof(ctx, KV_CAT_QUAD, 8.0 * ng * (double)q.P * (mode == 0 ? 2 : 3) *
+                                           kv_spin_frac(q.nv, q.no, q.spin_half));
     if (mode == 0) {
         quad_dense_kernel<0><<<grid, QT, smem, ctx->stream>>>(q, tabs, tbar, ti, G, D, ev, eo,
                                                               out, nullptr);
@@ -656,8 +657,10 @@ int kv_quad_launch(kvft_ctx *ctx, int mode, int ng, long long P, int rank, int n
         cudaFuncSetAttribute(quad_kernel<1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
         attr_done = true;
     }
-    // algorithmic bytes: tbar in, T out (mode 0); tbar + T_old in, T_old out (mode 1)
-    KvProfScope prof(ctx, KV_CAT_QUAD, 8.0 * ng * (double)P * (mode == 0 ? 2 : 3));
+    // algorithmic bytes: tbar in, T out (mode 0); tbar + T_old in, T_old out
+    // (mode 1); with spin blocks, of the spin-conserving elements
+    KvProfScope prof(ctx, KV_CAT_QUAD, 8.0 * ng * (double)P * (mode == 0 ? 2 : 3) *
+                                           kv_spin_frac(nv, no, q.spin_half));
     if (mode == 0) {
         if (q.uniform)
             quad_kernel<0, true><<<grid, QT, smem, ctx->stream>>>(q, tbar, ti, G, D, ev, eo, out,
