@@ -296,6 +296,45 @@ __device__ __forceinline__ void two_sum_f(float a, float b, float &s, float &e) 
     e = (a - (s - bb)) + (b - bb);
 }
 
+// Biased exponent field of x (0: zero or subnormal, 0x7FF: inf or NaN).
+__device__ __forceinline__ int dexp(double x) {
+    return (__double2hiint(x) >> 20) & 0x7FF;
+}
+
+// x 2^-k as an FP32 pair hi + lo, from the bit pattern with integer
+// operations (hi: the sign, exponent and top 23 mantissa bits; lo: the
+// remaining 29 bits, rounded to 24), |x 2^-k - hi - lo| <= 2^-47 |x 2^-k|.
+// For |x 2^-k| < 2: parts below 2^-126 are dropped (absolute error below
+// 2^-126 of the scale 1).
+__device__ __forceinline__ float2 dsplit_scaled(double x, int k) {
+    const unsigned hw = (unsigned)__double2hiint(x), lw = (unsigned)__double2loint(x);
+    const int e = (int)((hw >> 20) & 0x7FF) - 1023 - k;      // unbiased exponent of x 2^-k
+    if (((hw >> 20) & 0x7FF) == 0 || e < -126) return make_float2(0.f, 0.f);
+    const unsigned sg = hw & 0x80000000u;
+    const float hi = __uint_as_float(sg | ((unsigned)(e + 127) << 23) | ((hw & 0xFFFFFu) << 3) |
+                                     (lw >> 29));
+    const unsigned rem = lw & 0x1FFFFFFFu;                   // 29 low mantissa bits
+    float lo = 0.f;
+    if (rem != 0 && e - 52 >= -126)
+        lo = __uint_as_float(sg | __float_as_uint(__uint2float_rn(rem) *
+                                                  __uint_as_float((unsigned)(e - 52 + 127) << 23)));
+    return make_float2(hi, lo);
+}
+
+// (double) f 2^k for a finite float f, by integer operations on the bit
+// pattern: 0 stays 0, a result below 2^-1022 is 0 (an absolute error far
+// below anything the integral resolves), one above the FP64 range infinite.
+__device__ __forceinline__ double f32_to_f64_scaled(float f, int k) {
+    const unsigned u = __float_as_uint(f);
+    const int E = (int)((u >> 23) & 0xFF);
+    const int eb = E - 127 + 1023 + k;                       // biased FP64 exponent
+    if (E == 0 || eb <= 0) return 0.0;                       // zero, float subnormals, underflow
+    const unsigned sg = u & 0x80000000u;
+    if (eb >= 0x7FF) return __hiloint2double((int)(sg | 0x7FF00000u), 0);
+    const unsigned hw = sg | ((unsigned)eb << 20) | ((u >> 3) & 0xFFFFFu);
+    return __hiloint2double((int)hw, (int)(u << 29));
+}
+
 template <int MODE>
 __global__ void __launch_bounds__(QT)
 quad_dense_kernel(QuadParams q, DenseTabs tb_, const double *__restrict__ tbar,
@@ -346,34 +385,34 @@ quad_dense_kernel(QuadParams q, DenseTabs tb_, const double *__restrict__ tbar,
         if (table) {
             const long long l = p / tb_.NR;
             const long long r = p - l * tb_.NR;
-            // u_x = E_x tbar_x and its scale
-            double umax = 0.0;
+            // u_x = E_x tbar_x and the largest binary exponent among them.
+            // Range tests and the scale are integer operations on exponent
+            // fields: the FP64 pipe, GB300's scarce unit here, only takes the
+            // products
+            int umax_e = 0, eimax_e = 0;
             for (int x = 0; x < ng; x++) {
                 const double E = __ldg(tb_.v + x * tb_.NL + l) * __ldg(tb_.o + x * tb_.NR + r);
                 const double u = E * tbar[(long long)x * q.P + p];
                 c0[x * QT + t] = u;
-                umax = fmax(umax, fabs(u));          // fmax drops a NaN; the test below sees it
-                if (!(fabs(u) <= 1e300)) table = false;
+                umax_e = max(umax_e, dexp(u));        // inf / NaN: 0x7FF, refused below
             }
-            double eimax = 0.0;
-            for (int y = 0; y < ng && table; y++) {
+            for (int y = 0; y < ng; y++) {
                 const double Ei = __ldg(tb_.vi + y * tb_.NL + l) * __ldg(tb_.oi + y * tb_.NR + r);
                 c1[y * QT + t] = Ei;
-                if (!(Ei <= 1e300)) table = false;
-                eimax = fmax(eimax, Ei);
+                eimax_e = max(eimax_e, dexp(Ei));
             }
-            // |T_y| <= ng max|G| umax max(1/E): keep well inside FP64
-            if (table && umax * eimax > 1e290 / (double)ng) table = false;
+            // |u|, 1/E < 2^996 (< 1e300), and |T_y| <= ng max|G| max|u| max(1/E)
+            // < 2^(umax_e + eimax_e - 2044 + 8) kept below 2^956 (~1e288):
+            // well inside FP64
+            if (umax_e > 1023 + 995 || eimax_e > 1023 + 995 ||
+                umax_e + eimax_e - 2044 + 8 > 956)
+                table = false;
             if (table) {
-                if (umax == 0.0) {
+                if (umax_e == 0) {          // all u zero (or below 2^-1022)
                     for (int y = 0; y < ng; y++) emit(p, y, 0.0, f_diff, f_norm);
                 } else {
-                    const int k = ilogb(umax);
-                    for (int x = 0; x < ng; x++) {
-                        const double u = scalbn(c0[x * QT + t], -k);   // exact
-                        const float h = (float)u;
-                        uf[x * QT + t] = make_float2(h, (float)(u - (double)h));
-                    }
+                    const int k = umax_e - 1023;     // |u 2^-k| < 2
+                    for (int x = 0; x < ng; x++) uf[x * QT + t] = dsplit_scaled(c0[x * QT + t], k);
                     for (int y = 0; y < ng; y++) {
                         float s = 0.f, c = 0.f;
                         const float *gh = Gh + y * ng, *gl = Gl + y * ng;
@@ -388,7 +427,7 @@ quad_dense_kernel(QuadParams q, DenseTabs tb_, const double *__restrict__ tbar,
                             c = fmaf(gh[x], u.y, c);
                             c = fmaf(gl[x], u.x, c);
                         }
-                        const double acc = scalbn((double)s + (double)c, k);
+                        const double acc = f32_to_f64_scaled(s, k) + f32_to_f64_scaled(c, k);
                         emit(p, y, acc * c1[y * QT + t], f_diff, f_norm);
                     }
                 }
