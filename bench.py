@@ -326,13 +326,16 @@ def run_gpu(args, w):
     solver.guess(1)
     ladder = (5,) if not args.accel else ()
     low_tconv = args.low_tconv if args.accel else None
+    # the mixed form's refinement levels (the driver's default for the update)
+    refine = 6 if args.accel else 7
 
     def one_step():
         if per_solve:
             solver.guess(1)
             E, info = ccsd.converge(solver, ctx, dict(conv, damp=1.0 - args.mix)
                                     if args.accel else conv, args.precision, digits,
-                                    ladder=ladder, low_tconv=low_tconv)
+                                    ladder=ladder, low_tconv=low_tconv,
+                                    refine_digits=refine)
             return E, info["iterations"] + info["iterations_refine"]
         return solver.step(w["damp"])[0], 1
 
@@ -381,7 +384,7 @@ def run_gpu(args, w):
     if not per_solve:
         level_ms[digits if args.precision != "fp64" else 0] = step_ms
         if mixed:
-            for lv in ladder + (7,):
+            for lv in sorted(set(ladder + (refine, 7))):
                 level_ms[lv] = timed_steps(_lib.PREC_FP64_TC, lv, 2)
         elif args.precision == "fp64_tc":
             level_ms[7] = step_ms
@@ -550,9 +553,9 @@ def run_gpu(args, w):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": {"fp64": "f64", "fp64_tc": "f64 (7 BF16 digit levels, tensor cores)",
-                      "mixed": "bf16 digits/f32 acc (%s levels) + FP64-accurate 7-level "
-                               "refinement; f64 quadrature, update, energy"
-                               % ", ".join(str(x) for x in (digits,) + ladder)}[
+                      "mixed": "bf16 digits/f32 acc (%s levels) + %d-level refinement "
+                               "(FP64-accurate: 7); f64 quadrature, update, energy"
+                               % (", ".join(str(x) for x in (digits,) + ladder), refine)}[
                           args.precision],
             "data": "synthetic", "config": cfg, "roofline": roofline,
             "cpu_baseline": {"value": None, "unit": UNIT, "cores": os.cpu_count(),

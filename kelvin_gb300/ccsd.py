@@ -190,7 +190,7 @@ class ccsd(object):
     def __init__(self, sys, T=0.0, mu=0.0, iprint=0, singles=True, econv=1e-8,
                  tconv=None, max_iter=40, damp=0.0, ngrid=10, realtime=False,
                  athresh=0.0, quad='lin', rt_iter="all", precision='fp64',
-                 digits=None, refine_sweeps=None, refine_digits=7, ladder=None, accel=0,
+                 digits=None, refine_sweeps=None, refine_digits=None, ladder=None, accel=0,
                  mix=None, low_tconv=None, device=0, ctx=None):
         self.T = T
         self.mu = mu
@@ -211,10 +211,14 @@ class ccsd(object):
         self.precision = precision
         self.digits = digits if digits is not None else PRECISIONS[precision][1]
         # mixed form: after the few-digit phases (digits, then each level of
-        # `ladder`), sweeps with `refine_digits` levels (7: FP64-accurate)
-        # until Kelvin's test passes, at most refine_sweeps (None: max_iter)
+        # `ladder`), sweeps with `refine_digits` levels until Kelvin's test
+        # passes, at most refine_sweeps (None: max_iter).  Default 7
+        # (FP64-accurate) with Kelvin's damped update; 6 with Anderson mixing,
+        # whose refinement sweeps cost 13 % less at 6 levels and land on the
+        # same Omega (1.2e-14 Ha apart at 114 spin orbitals; 6-level
+        # contractions are within ~1e-11 of FP64 norm-wise)
         self.refine_sweeps = refine_sweeps
-        self.refine_digits = refine_digits
+        self.refine_digits = refine_digits if refine_digits is not None else (6 if accel else 7)
         # Anderson depth of the amplitude iteration (0: Kelvin's damped update)
         # and its mixing factor (None: 1 - damp, the damped update's); the
         # fixed point does not depend on either

@@ -228,13 +228,14 @@ class Server(object):
     ``accel`` > 0: Anderson mixing of that depth with mixing factor ``mix``
     (None: 1 - damp), the few-digit phase going straight to the
     FP64-accurate one and ending once Kelvin's residual is below
-    ``low_tconv`` (as ccsd.converge); the split step keeps the solves
-    overlapped on the device."""
+    ``low_tconv`` (as ccsd.converge), and the refinement at
+    ``refine_digits`` levels (None: 6 with accel, else 7, as ccsd.ccsd); the
+    split step keeps the solves overlapped on the device."""
 
     def __init__(self, precision='mixed', slots=4, budget=None, backend=None,
                  clock=time.perf_counter, sleep=time.sleep, warm_bytes=8 << 30, warm=True,
                  damp=0.5, econv=1e-8, max_iter=200, workspace_bytes=24 << 30, graphs=True,
-                 accel=0, mix=None, low_tconv=None):
+                 accel=0, mix=None, low_tconv=None, refine_digits=None):
         self.precision = precision
         self.slots = slots
         self.budget = budget
@@ -250,8 +251,9 @@ class Server(object):
         self.conv = {"econv": econv, "tconv": 1000.0 * econv, "max_iter": max_iter}
         self.cache = {}                   # key -> {theta: amplitudes}
         digits = PRECISIONS[precision][1]
-        self.levels = ((digits, 7) if accel else (digits, 5, 7)) if precision == 'mixed' \
-            else (digits,)
+        refine = refine_digits if refine_digits is not None else (6 if accel else 7)
+        self.levels = ((digits, refine) if accel else (digits, 5, refine)) \
+            if precision == 'mixed' else (digits,)
 
     def backend(self):
         if self._backend is None:

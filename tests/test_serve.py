@@ -165,16 +165,16 @@ class CutBackend(FakeBackend):
 
 
 def test_accelerated_scheme_phases():
-    """With accel the mixed form goes from 3 digit levels straight to 7, the
-    few-digit phase ends at the residual cut, and the solves step with the
-    mixing factor's damp = 1 - mix."""
+    """With accel the mixed form goes from 3 digit levels straight to the
+    6-level refinement (as ccsd.ccsd), the few-digit phase ends at the
+    residual cut, and the solves step with the mixing factor's damp = 1 - mix."""
     clock = FakeClock()
     R = serve.Request
     reqs = [R(0, 0.0, 'ueg', (14, 19, 4.0), 0.5, 10)]
     be = CutBackend(clock, {0: 100}, {0: 4})
     srv = serve.Server(precision='mixed', slots=2, budget=900, backend=be, clock=clock,
                        sleep=clock.sleep, accel=3, mix=0.7, low_tconv=1e-2)
-    assert srv.levels == (3, 7)
+    assert srv.levels == (3, 6)
     rep = srv.serve(reqs)
     d = rep["requests"][0]
     # the cut ends the few-digit phase at its third sweep (1e-3 < 1e-2; a
@@ -182,6 +182,7 @@ def test_accelerated_scheme_phases():
     # its second sweep (an unchanged energy)
     assert d["ok"] and d["converged"] and d["iterations"] == 3 + 2
     assert be.damps == {1.0 - 0.7}
+    assert serve.Server(precision='mixed', accel=3, refine_digits=7).levels == (3, 7)
     # without accel: Kelvin's damping and the 3, 5, 7 ladder
     srv = serve.Server(precision='mixed', slots=2, budget=900, backend=FakeBackend(
         FakeClock(), {0: 100}, {0: 4}), clock=clock, sleep=clock.sleep)
