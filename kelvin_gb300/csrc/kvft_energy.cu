@@ -117,6 +117,69 @@ energy2_kernel(int ng, int nv, int no, const double *__restrict__ T1,
     if (t == 0) partial[blockIdx.y * gridDim.x + blockIdx.x] = red[0];
 }
 
+// Spin blocks (nv = no = 2h): only the spin-conserving (a, b, i, j) carry
+// amplitudes and integrals.  Item (a, i, q) is one h x h block of (b, j): with
+// s_a = s_i the blocks s_b = s_j = q (q = 0, 1), otherwise the one block
+// s_b = s_i, s_j = s_a (q = 0; q = 1 is empty).  The block's integrals
+// eri[i][j][a][b] are read along b into shared memory and its amplitudes
+// T2_y[a][b][i][j] along j, so both streams are coalesced and no element
+// outside the conserving blocks is read.  The T1 T1 term vanishes unless s_b
+// = s_j (T1 is spin-diagonal), i.e. on the s_a = s_i items.  One partial sum
+// per item, reduced in a fixed order.
+constexpr int ESP_HMAX = 96;                 // h x (h + 1) doubles of shared memory
+
+__global__ void __launch_bounds__(256)
+energy2_spin_kernel(int ng, int n, int h, const double *__restrict__ T1,
+                    const double *__restrict__ T2, const double *__restrict__ eri,
+                    const double *__restrict__ g, int qterm, long long items,
+                    double *__restrict__ partial) {
+    extern __shared__ double E[];            // [h][h + 1]: E[j1][b1]
+    __shared__ double red[256];
+    __shared__ double gs[64], w[64];         // g_y and g_y T1_y[a][i]
+    const int t = threadIdx.x, hh = h * h, ld = h + 1;
+    const long long n2 = (long long)n * n, P = n2 * n2;
+    for (long long it = blockIdx.x; it < items; it += gridDim.x) {
+        const int q = (int)(it & 1);
+        const long long ai = it >> 1;
+        const int a = (int)(ai / n), i = (int)(ai - (long long)a * n);
+        const int sa = a >= h, si = i >= h;
+        double acc = 0.0;
+        if (sa == si || q == 0) {            // block-uniform
+            const int sb = sa == si ? q : si, sj = sa == si ? q : sa;
+            const bool tt = qterm && sa == si;
+            __syncthreads();                 // E, gs, w of the last item are used up
+            for (int x = t; x < ng; x += 256) {
+                gs[x] = g[x];
+                w[x] = tt ? g[x] * T1[(long long)x * n2 + (long long)a * n + i] : 0.0;
+            }
+            for (int x = t; x < hh; x += 256) {
+                const int j1 = x / h, b1 = x - j1 * h;
+                E[j1 * ld + b1] = eri[(((long long)i * n + sj * h + j1) * n + a) * n + sb * h + b1];
+            }
+            __syncthreads();
+            const long long base = ((long long)a * n + sb * h) * n2 + (long long)i * n + sj * h;
+            for (int x = t; x < hh; x += 256) {
+                const int b1 = x / h, j1 = x - b1 * h;
+                const double *t2 = T2 + base + (long long)b1 * n2 + j1;
+                double s1 = 0.0, s2 = 0.0;
+                for (int y = 0; y < ng; y++) s1 = fma(gs[y], t2[(long long)y * P], s1);
+                if (tt) {
+                    const double *u = T1 + (long long)(sb * h + b1) * n + sj * h + j1;
+                    for (int y = 0; y < ng; y++) s2 = fma(w[y], u[(long long)y * n2], s2);
+                }
+                acc = fma(fma(0.25, s1, 0.5 * s2), E[j1 * ld + b1], acc);
+            }
+        }
+        red[t] = acc;
+        __syncthreads();
+        for (int st = 128; st > 0; st >>= 1) {
+            if (t < st) red[t] += red[t + st];
+            __syncthreads();
+        }
+        if (t == 0) partial[it] = red[0];
+    }
+}
+
 __global__ void energy1_kernel(int ng, int nv, int no, const double *__restrict__ T1,
                                const double *__restrict__ f, const double *__restrict__ g,
                                double *__restrict__ out) {
@@ -160,18 +223,35 @@ int kv_energy(kvft_ctx *ctx, int ng, int nv, int no, const double *T1, const dou
               double *dres, int spin_half) {
     const long long V2 = (long long)nv * nv, O2 = (long long)no * no;
     dim3 grid((unsigned)((O2 + TILE - 1) / TILE), (unsigned)((V2 + TILE - 1) / TILE));
-    long long nblk = (long long)grid.x * grid.y;
+    const int sh = (nv == no && nv == 2 * spin_half) ? spin_half : 0;
+    const bool spin = sh > 0 && sh <= ESP_HMAX && ng <= 64;
+    // spin items (a, i, q), or the 32 x 32 tiles of the dense kernel
+    const long long nblk = spin ? 2LL * nv * nv : (long long)grid.x * grid.y;
     void *part = nullptr;
     KV_TRY(kv_scratch(ctx, "energy_partial", sizeof(double) * (nblk + 1), &part));
     double *pp = (double *)part;
     // algorithmic bytes: T2 (all tau points) + eri + T1; with spin blocks the
     // spin-conserving elements of T2 and eri
-    const int sh = (nv == no && nv == 2 * spin_half) ? spin_half : 0;
     KvProfScope prof(ctx, KV_CAT_ENERGY,
                      8.0 * (((double)ng * V2 * O2 + (double)V2 * O2) * kv_spin_frac(nv, no, sh) +
                             (double)ng * nv * no));
-    energy2_kernel<<<grid, 256, 0, ctx->stream>>>(ng, nv, no, T1, T2, eri, g, qterm, sh, pp);
-    KV_TRY(kv_launch_check(ctx, "energy2"));
+    if (spin) {
+        const size_t smem = sizeof(double) * (size_t)sh * (sh + 1);
+        static bool attr = false;
+        if (!attr) {
+            KV_CHECK(ctx, cudaFuncSetAttribute(energy2_spin_kernel,
+                                               cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                               (int)(sizeof(double) * ESP_HMAX * (ESP_HMAX + 1))));
+            attr = true;
+        }
+        const int gb = (int)std::min<long long>(nblk, (long long)ctx->sm_count * 8);
+        energy2_spin_kernel<<<gb, 256, smem, ctx->stream>>>(ng, nv, sh, T1, T2, eri, g, qterm,
+                                                           nblk, pp);
+        KV_TRY(kv_launch_check(ctx, "energy2_spin"));
+    } else {
+        energy2_kernel<<<grid, 256, 0, ctx->stream>>>(ng, nv, no, T1, T2, eri, g, qterm, sh, pp);
+        KV_TRY(kv_launch_check(ctx, "energy2"));
+    }
     energy1_kernel<<<1, 256, 0, ctx->stream>>>(ng, nv, no, T1, f, g, pp + nblk);
     KV_TRY(kv_launch_check(ctx, "energy1"));
     energy_final_kernel<<<1, 256, 0, ctx->stream>>>(pp, (int)nblk, pp + nblk, 1.0 / beta, dres);
