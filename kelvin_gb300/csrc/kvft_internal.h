@@ -151,6 +151,33 @@ struct KvTPackScope {
         if (!prev) ctx->tpack.clear();
     }
 };
+// FP64 <-> FP32 by integer operations on the bit patterns, for values that
+// only steer the iteration (norms, the Anderson history): GB300's FP64 pipe
+// runs conversions at its FP64 rate.  To FP32: mantissa truncated, below
+// 2^-126 zero, above the FP32 range infinite (NaN stays NaN).  To FP64:
+// exact (FP32 subnormals become zero).
+__device__ __forceinline__ float kv_d2f(double x) {
+    const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
+    const unsigned sg = hi & 0x80000000u;
+    const int e = (int)((hi >> 20) & 0x7FF) - 1023 + 127;
+    if (e <= 0) return __uint_as_float(sg);
+    if (e >= 255) {
+        const bool nan = (hi & 0x7FF00000u) == 0x7FF00000u && (((hi & 0xFFFFFu) | lo) != 0);
+        return __uint_as_float(nan ? 0x7FC00000u : (sg | 0x7F800000u));
+    }
+    return __uint_as_float(sg | ((unsigned)e << 23) | ((hi & 0xFFFFFu) << 3) | (lo >> 29));
+}
+__device__ __forceinline__ double kv_f2d(float f) {
+    const unsigned u = __float_as_uint(f);
+    const int E = (int)((u >> 23) & 0xFF);
+    if (E == 0) return __hiloint2double((int)(u & 0x80000000u), 0);
+    if (E == 255) return __hiloint2double((int)((u & 0x80000000u) | 0x7FF00000u | ((u >> 3) & 0xFFFFFu)),
+                                          (int)(u << 29));
+    return __hiloint2double((int)((u & 0x80000000u) | ((unsigned)(E - 127 + 1023) << 20) |
+                                  ((u >> 3) & 0xFFFFFu)),
+                            (int)(u << 29));
+}
+
 // Fraction of a T2-shaped tensor (nv nv no no) that the spin-conserving
 // blocks hold: 6 of the 16 spin blocks when nv = no = 2 sh, else all.  The
 // profiled algorithmic bytes of a pass that touches only those elements are

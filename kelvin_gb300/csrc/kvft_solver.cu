@@ -536,7 +536,8 @@ struct AaHist {
 // only where the iterate needs it (r = Phi - x and the update of x); the
 // history, the dot products (which only steer the mixing coefficients) and
 // the norms of Kelvin's residual measure run in FP32 per thread and are
-// summed in FP64 per block.
+// summed in FP64 per block; the conversions between the two are integer
+// operations on the bit patterns (kv_d2f, kv_f2d), not FP64-pipe ones.
 
 // pass A: r = Phi - x; dRnew = r - rprev; rprev = r; sums <dR_q, dRnew>,
 // <dR_q, r> over the NV valid slots, and <r, r>
@@ -563,7 +564,7 @@ aa_stats_kernel(AaSeg g, AaHist hs, double *part) {
 #pragma unroll
         for (int u = 0; u < AA_U; u++) {
             if (u >= cnt) break;
-            const float r = (float)(ph[u] - xx[u]);
+            const float r = kv_d2f(ph[u] - xx[u]);
             const float dn = has_new ? r - rp[u] : 0.f;
             if (has_new) hs.dRnew[cb + u * cs] = dn;
             rprev[u * cs] = r;
@@ -610,10 +611,10 @@ aa_update_kernel(AaSeg g, AaHist hs, double beta, float g0, float g1, float g2,
 #pragma unroll
         for (int u = 0; u < AA_U; u++) {
             if (u >= cnt) break;
-            const double d = fma(beta, ph[u] - xx[u], -(double)hsum[u]);
+            const double d = fma(beta, ph[u] - xx[u], -kv_f2d(hsum[u]));
             const double xn = xx[u] + d;
             x[o[u]] = xn;
-            const float df = (float)d, xf = (float)xn;
+            const float df = kv_d2f(d), xf = kv_d2f(xn);
             hs.dXst[cb + u * cs] = df;
             v[0] = fmaf(df, df, v[0]);
             v[1] = fmaf(xf, xf, v[1]);
@@ -983,7 +984,8 @@ int aa_step_begin(kvft_solver *s, double damp) {
     double *part = (double *)pp;
     {
         KvProfScope prof(ctx, KV_CAT_ELEM,
-                         (aa_visited(g[0]) + aa_visited(g[1])) * (28.0 + 4.0 * nvalid));
+                         (aa_visited(g[0]) + aa_visited(g[1])) *
+                             (28.0 + 4.0 * (nvalid - (has_new ? 1 : 0))));
         for (int q = 0; q < 2; q++) {
             AaHist hs{};
             for (int t = 0; t < nvalid; t++) {
