@@ -287,6 +287,91 @@ assemble_t2_kernel(int nv, int no, int sh, double fac, const double *__restrict_
     }
 }
 
+// The seeded assembly with spin blocks (nv = no = n = 2h): for the pair
+// (a < b) of spin sum t = s_a + s_b only the (i, j) with s_i + s_j = t are
+// written -- the alpha-alpha quadrant (t = 0), the beta-beta one (t = 2), or
+// the alpha-beta quadrant with its mirror beta-alpha (t = 1).  Tiles are laid
+// out from each quadrant's origin, so no tile straddles the spin boundary:
+// tile pairs (it <= jt) of a diagonal quadrant, every (it, jt) of the
+// alpha-beta one with its mirror tile in the beta-alpha one.  The other
+// elements of T2 are left as they are (zero: nothing writes or reads them).
+template <int FS>
+__global__ void __launch_bounds__(256, 3)
+assemble_t2_spin_kernel(int n, int h, double fac, const double *__restrict__ Z,
+                        const double *__restrict__ Lc, const double *__restrict__ seed,
+                        double *__restrict__ T2) {
+    const PairOrder ov{n, h};
+    __shared__ double qa[32][33], qb[32][33];
+    const int tx = threadIdx.x % 32, ty = threadIdx.x / 32;
+    const int nth = (h + 31) / 32;
+    const long long y = blockIdx.z;
+    const int pv = n * (n - 1) / 2;
+    const long long oo = (long long)n * n, s4 = oo * oo;
+    for (int pab = blockIdx.y; pab < pv; pab += gridDim.y) {
+        int a, b;
+        ov.decode(pab, a, b);
+        const int tab = (a >= h) + (b >= h);
+        int it, jt;
+        if (tab == 1) {
+            if ((int)blockIdx.x >= nth * nth) continue;              // block-uniform
+            it = blockIdx.x / nth;
+            jt = blockIdx.x % nth;
+        } else {
+            if ((int)blockIdx.x >= nth * (nth + 1) / 2) continue;
+            it = 0;
+            int rem = blockIdx.x;
+            while (rem >= nth - it) {
+                rem -= nth - it;
+                it++;
+            }
+            jt = it + rem;
+        }
+        const int ilo = tab == 2 ? h : 0, jlo = tab == 0 ? 0 : h;   // quadrant origins
+        const int ihi = ilo + h, jhi = jlo + h;
+        const int i0 = ilo + 32 * it, j0 = jlo + 32 * jt;
+        const bool mirror = tab == 1 || it != jt;
+        const long long oab = y * s4 + ((long long)a * n + b) * oo;
+        const long long oba = y * s4 + ((long long)b * n + a) * oo;
+        const double *L = Lc ? Lc + (y * pv + pab) * (long long)pv : nullptr;
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            const int r = ty + 8 * k;
+            int i = i0 + r, j = j0 + tx;
+            qa[r][tx] = (i < ihi && j < jhi) ? Z[oab + i * n + j] - Z[oba + i * n + j] : 0.0;
+            i = j0 + r;
+            j = i0 + tx;
+            qb[r][tx] = (i < jhi && j < ihi) ? Z[oab + i * n + j] - Z[oba + i * n + j] : 0.0;
+        }
+        __syncthreads();
+        // L over (i < j); both indices of a written element have the pair's type
+        auto ladder = [&](int i, int j) -> double {
+            if (!L || i == j) return 0.0;
+            return i < j ? L[ov.index(i, j)] : -L[ov.index(j, i)];
+        };
+        const long long sab = ((long long)a * n + b) * oo, sba = ((long long)b * n + a) * oo;
+        auto put = [&](int x, double R) {
+            T2[oab + x] = R - seed[sab + x];
+            T2[oba + x] = -R - seed[sba + x];
+        };
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            const int r = ty + 8 * k;
+            int i = i0 + r, j = j0 + tx;
+            if (i < ihi && j < jhi) {
+                const double R0 = qa[r][tx] - qb[tx][r] + ladder(i, j);
+                put(i * n + j, FS == 0 ? fac * R0 : (FS == 1 ? R0 : -R0));
+            }
+            i = j0 + r;
+            j = i0 + tx;
+            if (mirror && i < jhi && j < ihi) {
+                const double R0 = qb[r][tx] - qa[tx][r] + ladder(i, j);
+                put(i * n + j, FS == 0 ? fac * R0 : (FS == 1 ? R0 : -R0));
+            }
+        }
+    }
+}
+
 __global__ void bcast_kernel(long long total, long long count,
                              const double *__restrict__ src,
                              double *__restrict__ dst) {
@@ -447,6 +532,17 @@ int kv_assemble_t2(kvft_ctx *ctx, int batch, int nv, int no, double fac, const d
     assemble_t2_kernel<fs_, seed_><<<grid, 256, 0, ctx->stream>>>(nv, no, sh, fac, Z, Lc, seed, \
                                                                   T2)
     const int fs = fac == 1.0 ? 1 : (fac == -1.0 ? 2 : 0);
+    if (seed && sh) {
+        const int nth = (sh + 31) / 32;
+        const dim3 gs(nth * nth, std::min(pv, 65535), batch);
+        if (fs == 1)
+            assemble_t2_spin_kernel<1><<<gs, 256, 0, ctx->stream>>>(nv, sh, fac, Z, Lc, seed, T2);
+        else if (fs == 2)
+            assemble_t2_spin_kernel<2><<<gs, 256, 0, ctx->stream>>>(nv, sh, fac, Z, Lc, seed, T2);
+        else
+            assemble_t2_spin_kernel<0><<<gs, 256, 0, ctx->stream>>>(nv, sh, fac, Z, Lc, seed, T2);
+        return kv_launch_check(ctx, "assemble_t2_spin");
+    }
     if (seed) {
         if (fs == 1) KV_ASM(1, true);
         else if (fs == 2) KV_ASM(2, true);
