@@ -138,12 +138,24 @@ make_tau_kernel(long long nblk, int nv, int no, int sh, const double *__restrict
         }
         __syncthreads();
         const long long base = blk * oo;
-        // spin blocks (sh > 0): only the spin-conserving (i, j) are read later
-        const int sab = (a >= sh) + (b >= sh);
-        for (int e = threadIdx.x; e < oo; e += blockDim.x) {
-            const int i = e / no, j = e % no;
-            if (sh && (i >= sh) + (j >= sh) != sab) continue;
-            out[base + e] = fma(cab[i], ub[j], fma(-cab[no + i], ua[j], t2[base + e]));
+        if (sh) {
+            // spin blocks (nv = no = 2 sh): only the spin-conserving (i, j) are
+            // read later -- the quadrant(s) with s_i + s_j = s_a + s_b, walked
+            // directly (j fastest)
+            const int sab = (a >= sh) + (b >= sh), hh = sh * sh;
+            const int nq = sab == 1 ? 2 : 1;
+            for (int x = threadIdx.x; x < nq * hh; x += blockDim.x) {
+                const int qq = x / hh, r = x - qq * hh;
+                const int i1 = r / sh, j1 = r - i1 * sh;
+                const int si = sab == 1 ? qq : sab / 2, sj = sab == 1 ? 1 - qq : sab / 2;
+                const int i = si * sh + i1, j = sj * sh + j1, e = i * no + j;
+                out[base + e] = fma(cab[i], ub[j], fma(-cab[no + i], ua[j], t2[base + e]));
+            }
+        } else {
+            for (int e = threadIdx.x; e < oo; e += blockDim.x) {
+                const int i = e / no, j = e % no;
+                out[base + e] = fma(cab[i], ub[j], fma(-cab[no + i], ua[j], t2[base + e]));
+            }
         }
     }
 }
@@ -283,6 +295,46 @@ assemble_t2_kernel(int nv, int no, int sh, double fac, const double *__restrict_
                 const double R = FS == 0 ? fac * R0 : (FS == 1 ? R0 : -R0);
                 put(i * no + j, R);
             }
+        }
+    }
+}
+
+// The same with spin blocks (nv = no = n = 2h): for each (b, j) only the
+// (f, n) with s_f - s_n = s_j - s_b are written -- the alpha-alpha and
+// beta-beta quadrants, or the one mixed quadrant -- in 32 x 32 tiles laid out
+// from each quadrant's origin (no tile straddles the spin boundary; block x
+// = quadrant and tile).
+__global__ void __launch_bounds__(256)
+wmbej_tmp_spin_kernel(int n, int h, const double *__restrict__ t1,
+                      const double *__restrict__ t2, double *__restrict__ out) {
+    __shared__ double tile[32][33];
+    const int tx = threadIdx.x % 32, ty = threadIdx.x / 32;
+    const int nth = (h + 31) / 32, nt2 = nth * nth;
+    const int q = blockIdx.x / nt2, tt = blockIdx.x % nt2;
+    const long long y = blockIdx.z;
+    const long long oo = (long long)n * n;
+    const double *u = t1 + y * oo;
+    for (int bj = blockIdx.y; bj < n * n; bj += gridDim.y) {
+        const int b = bj / n, j = bj % n;
+        const int d = (j >= h) - (b >= h);          // s_f - s_n
+        if (d != 0 && q) continue;                  // block-uniform
+        const int sf = d == 0 ? q : (d > 0), sn = d == 0 ? q : (d < 0);
+        const int f0 = sf * h + 32 * (tt / nth), n0 = sn * h + 32 * (tt % nth);
+        const int fhi = sf * h + h, nhi = sn * h + h;
+        __syncthreads();
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            const int f = f0 + ty + 8 * i, m = n0 + tx;
+            if (f < fhi && m < nhi)
+                tile[ty + 8 * i][tx] = t2[((y * n + f) * n + b) * oo + (long long)j * n + m];
+        }
+        __syncthreads();
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            const int m = n0 + ty + 8 * i, f = f0 + tx;
+            if (f < fhi && m < nhi)
+                out[(((y * n + b) * n + j) * n + m) * n + f] =
+                    0.5 * tile[tx][ty + 8 * i] + u[f * n + j] * u[b * n + m];
         }
     }
 }
@@ -491,9 +543,9 @@ int kv_make_tau(kvft_ctx *ctx, int batch, int nv, int no, const double *t1,
     KvProfScope prof(ctx, KV_CAT_ELEM, 16.0 * total * kv_spin_frac(nv, no, spin_half));
     const long long nblk = (long long)batch * nv * nv;
     if (no > 3072) return kv_fail(ctx, KVFT_EINVAL, "make_tau: more than 3072 occupied orbitals");
+    const int sh = (nv == no && nv == 2 * spin_half) ? spin_half : 0;
     make_tau_kernel<<<(unsigned)std::min(nblk, (long long)ctx->sm_count * 16), 256,
-                      2 * no * sizeof(double), ctx->stream>>>(nblk, nv, no, spin_half, t1, t2,
-                                                              c, out);
+                      2 * no * sizeof(double), ctx->stream>>>(nblk, nv, no, sh, t1, t2, c, out);
     return kv_launch_check(ctx, "make_tau");
 }
 
@@ -503,8 +555,14 @@ int kv_make_wmbej_tmp(kvft_ctx *ctx, int batch, int nv, int no,
     if (total == 0) return KVFT_OK;
     if (batch > 65535) return kv_fail(ctx, KVFT_EINVAL, "wmbej_tmp: batch too large");
     KvProfScope prof(ctx, KV_CAT_ELEM, 16.0 * total * kv_spin_frac(nv, no, spin_half));
-    // each block walks several (b, j): with spin blocks most of its tiles are
-    // skipped, and short-lived blocks would leave the SMs waiting for new ones
+    if (spin_half > 0 && nv == no && nv == 2 * spin_half) {
+        const int nth = (spin_half + 31) / 32;
+        const dim3 gs(2 * nth * nth, std::min(nv * no, 2048), batch);
+        wmbej_tmp_spin_kernel<<<gs, 256, 0, ctx->stream>>>(nv, spin_half, t1, t2, out);
+        return kv_launch_check(ctx, "wmbej_tmp_spin");
+    }
+    // each block walks several (b, j): short-lived blocks would leave the SMs
+    // waiting for new ones
     const dim3 grid(((nv + 31) / 32) * ((no + 31) / 32), std::min(nv * no, 2048), batch);
     wmbej_tmp_kernel<<<grid, 256, 0, ctx->stream>>>(nv, no, spin_half, t1, t2, out);
     return kv_launch_check(ctx, "wmbej_tmp");
