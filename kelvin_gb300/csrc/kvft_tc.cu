@@ -53,6 +53,25 @@ constexpr int TMEM_COLS = 512;               // all of an SM's TMEM (one CTA per
 constexpr int GROUP_M = 8;                    // m-tiles per raster group (L2 reuse)
 constexpr unsigned long long WAIT_NS = 2000000000ull;   // 2 s per wait
 
+// x / d for 0 <= x < 2^31 by a multiply and a shift (Granlund-Montgomery:
+// m = ceil(2^(31+l) / d) with 2^l >= d), in place of the ~20 instructions of
+// an integer division by a run-time divisor in the per-tile index arithmetic.
+struct FastDiv {
+    unsigned long long m;
+    int s;
+    __device__ __forceinline__ int div(int x) const {
+        return (int)(((unsigned long long)(unsigned)x * m) >> s);
+    }
+};
+inline FastDiv fastdiv(int d) {
+    int l = 0;
+    while ((1LL << l) < d) l++;
+    FastDiv f;
+    f.s = 31 + l;
+    f.m = ((1ULL << f.s) + (unsigned long long)d - 1) / (unsigned long long)d;
+    return f;
+}
+
 struct TcParams {
     int M, N;             // output extent
     int mt, nt;           // output tiles along M and N
@@ -71,6 +90,8 @@ struct TcParams {
     unsigned alpha_sign;  // sign bit of alpha (bit 31 of the FP64 high word)
     KOut C;
     int *err;
+    FastDiv dv_split, dv_perb, dv_gsz;    // nsplit, mt nt, GROUP_M nt
+    FastDiv dv_cr2, dv_cr1;               // C's row index: sizes of its fast components
 };
 
 // A work unit: one output tile of one batch entry over a k-block range.
@@ -82,19 +103,25 @@ struct Unit {
 // (n-tiles walk inside a group), then by batch entry, so the CTAs that run
 // at the same time share a few A row panels and sweep B once per group.
 __device__ __forceinline__ Unit unit_of(const TcParams &p, int u, int tn) {
+    static_assert(GROUP_M == 8, "raster groups of 8 m-tiles (shift and mask below)");
     Unit w;
-    const int split = u % p.nsplit;
-    const int t = u / p.nsplit;
+    const int t = p.dv_split.div(u);
+    const int split = u - t * p.nsplit;
     const int per_b = p.mt * p.nt;
-    w.b = t / per_b;
+    w.b = p.dv_perb.div(t);
     const int r = t - w.b * per_b;
     const int gsz = GROUP_M * p.nt;
-    const int g = r / gsz;
+    const int g = p.dv_gsz.div(r);
     const int first = g * GROUP_M;
     const int gm = min(GROUP_M, p.mt - first);
     const int rr = r - g * gsz;
-    w.m0 = (first + rr % gm) * TM;
-    w.n0 = (rr / gm) * tn;
+    if (gm == GROUP_M) {
+        w.m0 = (first + (rr & 7)) * TM;
+        w.n0 = (rr >> 3) * tn;
+    } else {                              // the last, short group
+        w.m0 = (first + rr % gm) * TM;
+        w.n0 = (rr / gm) * tn;
+    }
     if (p.nsplit > 1) {
         w.kb0 = split * p.chunk_kb;
         w.kb1 = min(w.kb0 + p.chunk_kb, p.nkb_total);
@@ -489,6 +516,7 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
         float rlo[FF ? WCOLS : 1];
         int gc = 0;
         bool ok = true;
+        int cached_n = -1, cached_b = -1;   // the columns coff / cexp hold (warp-uniform)
         for (int u = blockIdx.x; u < p.units && ok; u += gridDim.x) {
             const Unit w = unit_of(p, u, TN);
             if (w.kb0 >= w.kb1) continue;
@@ -499,15 +527,30 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
             // at L2 themselves: prefetching them too cost 6 of 82 ms per
             // 114-spin-orbital iteration in issue slots)
             const int nw = w.n0 + h * WCOLS;          // first column of this warp
-            for (int i = lane; i < WCOLS; i += 32) {
-                const int n = nw + i;
-                coff[i] = (n < p.N) ? p.C.c.off(n) : 0;
-                cexp[i] = (n < p.N) ? exp_of(p.eb[(long long)w.b * p.eb_bst + n]) : 0;
+            // column offsets and exponents: the same for every tile of this
+            // column range (and batch entry, when B is per batch)
+            const int bkey = p.eb_bst ? w.b : 0;
+            if (nw != cached_n || bkey != cached_b) {
+                __syncwarp();                            // the last tile's reads are done
+                for (int i = lane; i < WCOLS; i += 32) {
+                    const int n = nw + i;
+                    coff[i] = (n < p.N) ? p.C.c.off(n) : 0;
+                    cexp[i] = (n < p.N) ? exp_of(p.eb[(long long)bkey * p.eb_bst + n]) : 0;
+                }
+                cached_n = nw;
+                cached_b = bkey;
             }
             __syncwarp();
             const int m = w.m0 + row;
             const int nlim = p.N - nw;
-            double *Cr = p.C.p + (long long)w.b * p.C.bst + (m < p.M ? p.C.r.off(m) : 0);
+            long long roff = 0;
+            if (m < p.M) {                               // p.C.r.off(m), fast divisions
+                const int r1 = p.dv_cr2.div(m), i2 = m - r1 * p.C.r.size[2];
+                const int i0 = p.dv_cr1.div(r1), i1 = r1 - i0 * p.C.r.size[1];
+                roff = (long long)i0 * p.C.r.st[0] + (long long)i1 * p.C.r.st[1] +
+                       (long long)i2 * p.C.r.st[2];
+            }
+            double *Cr = p.C.p + (long long)w.b * p.C.bst + roff;
             const int krow =
                 (m < p.M) ? exp_of(p.ea[(long long)w.b * p.ea_bst + m]) - 14 + p.alpha_exp : 0;
             if (m < p.M && p.nsplit == 1 && p.beta != 0.0 && p.beta != 1.0) {
@@ -1359,6 +1402,11 @@ int gemm_tc_run(kvft_ctx *ctx, int M, int N, int K, int batch, double alpha, con
     }
     p.C = C;
     p.err = ctx->dflag;
+    p.dv_split = fastdiv(p.nsplit);
+    p.dv_perb = fastdiv(p.mt * p.nt);
+    p.dv_gsz = fastdiv(GROUP_M * p.nt);
+    p.dv_cr2 = fastdiv(C.r.size[2]);
+    p.dv_cr1 = fastdiv(C.r.size[1]);
     switch (D) {
     case 2:
         return tn == 64 ? launch_tc<64, false, 64, 2>(ctx, ma, mb, p)
