@@ -96,6 +96,21 @@ def test_tc_gemm_short_k(ctx, K, digits):
     assert not C[:, 5, :].any() and not C[:, :, 7].any()
 
 
+# FP32-pair levels (four or more digits) with a short K run on 32-wide tiles
+# with two accumulator sets: partial and exact tile widths, one or several
+# n-tiles, partial m-tiles, a batch.
+@pytest.mark.parametrize("M,N,K,batch", [(300, 20, 57, 2), (333, 57, 57, 1),
+                                         (128, 64, 100, 3), (57, 900, 57, 2)])
+@pytest.mark.parametrize("digits", [4, 6, 7])
+def test_tc_gemm_short_k_narrow_pair_levels(ctx, M, N, K, batch, digits):
+    rng = numpy.random.default_rng(M + 7 * N + K + digits)
+    A = rng.standard_normal((batch, M, K)) * numpy.exp(rng.standard_normal((batch, M, 1)) * 3)
+    B = rng.standard_normal((batch, K, N)) * numpy.exp(rng.standard_normal((batch, 1, N)) * 3)
+    C = gemm(ctx, A, B, _lib.PREC_FP64_TC, digits)
+    tol = TOL.get(digits, 5e-11 if digits == 6 else None)
+    assert normwise(C, A, B) < tol * max(1.0, (256 / K) ** 0.5)
+
+
 # Few output columns after the orientation swap (C's contiguous index on the
 # tile rows, the short extent on the columns): 64-wide tiles at two and three
 # digit levels, with one or several K chunks.
