@@ -123,15 +123,54 @@ class DeviceSolver(object):
             self.h, T1.ctypes.data_as(_lib.vp), T2.ctypes.data_as(_lib.vp)),
             "kvft_solver_set_amplitudes")
 
-    def amplitudes(self):
-        T1 = numpy.empty((self.ng, self.nv, self.no))
-        # zero pages until written: with spin blocks only the
-        # spin-conserving elements are copied
-        T2 = numpy.zeros((self.ng, self.nv, self.nv, self.no, self.no))
+    def amplitudes(self, out=None):
+        """Host copies (T1, T2).  ``out``: a (T1, T2) pair of C-contiguous
+        float64 arrays of these shapes whose T2 holds zeros (e.g. from
+        prepare_amplitudes), filled in place."""
+        if out is None:
+            T1 = numpy.empty((self.ng, self.nv, self.no))
+            # zero pages until written: with spin blocks only the
+            # spin-conserving elements are copied
+            T2 = numpy.zeros((self.ng, self.nv, self.nv, self.no, self.no))
+        else:
+            T1, T2 = out
         self.ctx.check(self.ctx.L.kvft_solver_read_amplitudes(
             self.h, T1.ctypes.data_as(_lib.vp), T2.ctypes.data_as(_lib.vp), 1),
             "kvft_solver_read_amplitudes")
         return T1, T2
+
+    def prepare_amplitudes(self):
+        """Start a host thread that allocates the (T1, T2) arrays for
+        amplitudes(out=...) and faults in the pages the read-back will write
+        (the spin-conserving blocks of T2, or all of it), so that the first
+        touch of tens of GB overlaps the iteration on the device instead of
+        following it.  Returns a function that waits and returns the pair."""
+        import threading
+        shp1 = (self.ng, self.nv, self.no)
+        shp2 = (self.ng, self.nv, self.nv, self.no, self.no)
+        h = self.spin_blocks() if self.nv == self.no else 0
+        box = {}
+
+        def work():
+            T1 = numpy.empty(shp1)
+            T2 = numpy.zeros(shp2)
+            if h:
+                lo, hi = slice(0, h), slice(h, 2 * h)
+                half = (lo, hi)
+                for sa, sb, si, sj in ((0, 0, 0, 0), (1, 1, 1, 1), (0, 1, 0, 1),
+                                       (0, 1, 1, 0), (1, 0, 0, 1), (1, 0, 1, 0)):
+                    T2[:, half[sa], half[sb], half[si], half[sj]] = 0.0
+            else:
+                T2[...] = 0.0
+            box["out"] = (T1, T2)
+
+        th = threading.Thread(target=work, daemon=True)
+        th.start()
+
+        def wait():
+            th.join()
+            return box["out"]
+        return wait
 
     def lambda_solve(self, conv_options, guess=1, L1=None, L2=None, measure_half=None,
                      history=None):

@@ -320,6 +320,9 @@ class ccsd(object):
         logging.info('MP2 Energy: {:.10f}'.format(E2))
         if self.accel and self.mix is not None:
             conv["damp"] = 1.0 - self.mix
+        # the host arrays of the amplitudes, their pages faulted in while the
+        # device iterates
+        ready = solver.prepare_amplitudes()
         Eccn, info = converge(solver, self.ctx, conv, self.precision, digits,
                               self.refine_sweeps, self.refine_digits, self.ladder,
                               self.low_tconv)
@@ -328,7 +331,7 @@ class ccsd(object):
         self.converged = info["converged"]
         self.omega_low = info["omega_low"]
         self.phases = info.get("phases")
-        self._Tg = solver.amplitudes()
+        self._Tg = solver.amplitudes(out=ready())
         self.T1, self.T2 = self._Tg
         if self._unrestricted():
             na = self.sys.u_energies_tot()[0].shape[0]

@@ -60,6 +60,9 @@ class FakeSolver(object):
     def guess(self, kind):
         return 0.0
 
+    def prepare_amplitudes(self):
+        return lambda: None
+
     def close(self):
         pass
 
@@ -133,7 +136,7 @@ def test_unrestricted_system_amplitudes(monkeypatch):
     seen = {}
 
     class Solver(FakeSolver):
-        def amplitudes(self):
+        def amplitudes(self, out=None):
             return T1.copy(), T2.copy()
 
         def set_amplitudes(self, a, b):
