@@ -525,6 +525,36 @@ def run_gpu(args, w):
     # they are built): a few seconds
     if mixed and not per_solve:
         cfg["accuracy_38_spin_orbitals"] = small_accuracy(ctx, args)
+    # the reference arm's workload (the 38-spin-orbital configuration on this
+    # run's grid), end to end through the same driver: the like-for-like
+    # rate beside the reference's (median of three solves each)
+    if not per_solve and ws == 1:
+        w38 = WORKLOADS["ueg38"]
+        s38 = build_system(w38)
+
+        def solve38(precision, accel):
+            runs = []
+            for _ in range(3):
+                cc = ccsd.ccsd(s38, T=s38.T, mu=s38.mu, max_iter=w38["max_iter"],
+                               damp=w38["damp"], ngrid=w38["ng"], econv=w38["econv"],
+                               quad=args.quad, precision=precision, accel=accel,
+                               mix=args.mix if accel else None,
+                               low_tconv=low_tconv if accel else None, ctx=ctx)
+                ctx.sync()
+                t0 = time.perf_counter()
+                cc.run()
+                ctx.sync()
+                runs.append((time.perf_counter() - t0,
+                             cc.iterations + cc.iterations_refine, cc.Gcc))
+                cc.release()
+            t, it, E = sorted(runs)[1]
+            return {"solves_per_s": 1.0 / t, "iterations": it, "omega_cc": E}
+        cfg["reference_workload_e2e"] = {
+            "workload": w38["label"] + " (%s tau grid)" % args.quad,
+            "mixed": solve38(args.precision, args.accel),
+            "fp64_tc_damped": solve38("fp64_tc", 0),
+            "how": "ccsd(...).run() from host arrays, wall clock, median of three; the "
+                   "reference arm times the oracle's complete solve of this workload"}
     if ref64 is not sol:
         d = abs(sol["omega_cc"] - ref64["omega_cc"])
         cfg["fp64_tc_solve"] = {k: ref64[k] for k in ("iterations", "converged", "omega_cc",
