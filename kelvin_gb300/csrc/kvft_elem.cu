@@ -163,9 +163,9 @@ make_tau_kernel(long long nblk, int nv, int no, int sh, const double *__restrict
 // out[y][b][j][n][f] = 0.5 t2[y][f][b][j][n] + t1[y][f][j] t1[y][b][n]: the
 // contraction index (n, f) ends up contiguous, matching <mn||ef> of the W_mbej
 // product.  32 x 32 (f, n) tiles go through shared memory so the reads are
-// coalesced along n and the writes along f.
+// coalesced along n and the writes along f.  (Spin blocks: the kernel below.)
 __global__ void __launch_bounds__(256)
-wmbej_tmp_kernel(int nv, int no, int sh, const double *__restrict__ t1,
+wmbej_tmp_kernel(int nv, int no, const double *__restrict__ t1,
                  const double *__restrict__ t2, double *__restrict__ out) {
     __shared__ double tile[32][33];
     const int tx = threadIdx.x % 32, ty = threadIdx.x / 32;
@@ -174,32 +174,20 @@ wmbej_tmp_kernel(int nv, int no, int sh, const double *__restrict__ t1,
     const long long y = blockIdx.z;
     const long long oo = (long long)no * no;
     const double *u = t1 + y * nv * no;
-    // spin blocks (sh > 0): only elements with s_f + s_b = s_j + s_n are read
-    // later; the spin sets of the tile's f and n ranges
-    const int fs0 = f0 >= sh, fs1 = min(f0 + 31, nv - 1) >= sh;
-    const int ns0 = n0 >= sh, ns1 = min(n0 + 31, no - 1) >= sh;
-    auto keep = [&](int f, int b, int j, int n) {
-        return !sh || (f >= sh) + (b >= sh) == (j >= sh) + (n >= sh);
-    };
     for (int bj = blockIdx.y; bj < nv * no; bj += gridDim.y) {
         const int b = bj / no, j = bj % no;
-        if (sh) {
-            // s_f - s_n must equal s_j - s_b for some f, n of the tile
-            const int d = (j >= sh) - (b >= sh);
-            if (fs1 - ns0 < d || fs0 - ns1 > d) continue;      // block-uniform
-        }
         __syncthreads();
 #pragma unroll
         for (int i = 0; i < 4; i++) {
             const int f = f0 + ty + 8 * i, n = n0 + tx;
-            if (f < nv && n < no && keep(f, b, j, n))
+            if (f < nv && n < no)
                 tile[ty + 8 * i][tx] = t2[((y * nv + f) * nv + b) * oo + (long long)j * no + n];
         }
         __syncthreads();
 #pragma unroll
         for (int i = 0; i < 4; i++) {
             const int n = n0 + ty + 8 * i, f = f0 + tx;
-            if (f < nv && n < no && keep(f, b, j, n))
+            if (f < nv && n < no)
                 out[(((y * nv + b) * no + j) * no + n) * nv + f] =
                     0.5 * tile[tx][ty + 8 * i] + u[f * no + j] * u[b * no + n];
         }
@@ -241,14 +229,6 @@ assemble_t2_kernel(int nv, int no, int sh, double fac, const double *__restrict_
         int a, b;
         ov.decode(pab, a, b);
         const int tab = (a >= sh) + (b >= sh);
-        if (SEED && sh) {
-            // spin blocks: a tile pair without spin-conserving (i, j) holds
-            // zeros only, which nothing reads (the solver's update and the
-            // energy walk the conserving elements), so it is not written
-            const int il = i0 >= sh, ih = min(i0 + 31, no - 1) >= sh;
-            const int jl = j0 >= sh, jh = min(j0 + 31, no - 1) >= sh;
-            if (tab < il + jl || tab > ih + jh) continue;           // block-uniform
-        }
         const long long oab = y * s4 + ((long long)a * nv + b) * oo;
         const long long oba = y * s4 + ((long long)b * nv + a) * oo;
         const double *L = Lc ? Lc + (y * pv + pab) * (long long)po : nullptr;
@@ -564,7 +544,7 @@ int kv_make_wmbej_tmp(kvft_ctx *ctx, int batch, int nv, int no,
     // each block walks several (b, j): short-lived blocks would leave the SMs
     // waiting for new ones
     const dim3 grid(((nv + 31) / 32) * ((no + 31) / 32), std::min(nv * no, 2048), batch);
-    wmbej_tmp_kernel<<<grid, 256, 0, ctx->stream>>>(nv, no, spin_half, t1, t2, out);
+    wmbej_tmp_kernel<<<grid, 256, 0, ctx->stream>>>(nv, no, t1, t2, out);
     return kv_launch_check(ctx, "wmbej_tmp");
 }
 
