@@ -633,9 +633,29 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
                     // thread waiting for the old value (measured on the
                     // 114-spin-orbital n^5 class: 82 ms per iteration
                     // against 120 ms for the load-add-store ring below)
+                    if constexpr (FF) {
+                        if (p.alpha_pow2) {
+                            // the FP32 pair as two reductions at L2: no FP64
+                            // add on the SM (GB300's FP64 pipe bounded this
+                            // write); C gets old + hi + lo in two roundings
 #pragma unroll
-                    for (int i = 0; i < WCOLS; i++)
-                        if (i < nlim) atomicAdd(Cr + coff[i], value(i));
+                            for (int i = 0; i < WCOLS; i++) {
+                                if (i < nlim) {
+                                    const int k = krow + cexp[i];
+                                    atomicAdd(Cr + coff[i], f32_scaled(rhi[i], k, p.alpha_sign));
+                                    atomicAdd(Cr + coff[i], f32_scaled(rlo[i], k, p.alpha_sign));
+                                }
+                            }
+                        } else {
+#pragma unroll
+                            for (int i = 0; i < WCOLS; i++)
+                                if (i < nlim) atomicAdd(Cr + coff[i], value(i));
+                        }
+                    } else {
+#pragma unroll
+                        for (int i = 0; i < WCOLS; i++)
+                            if (i < nlim) atomicAdd(Cr + coff[i], value(i));
+                    }
                 } else if (p.beta == 0.0) {
 #pragma unroll
                     for (int i = 0; i < WCOLS; i++)
