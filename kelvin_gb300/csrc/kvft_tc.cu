@@ -657,9 +657,23 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
                             if (i < nlim) atomicAdd(Cr + coff[i], value(i));
                     }
                 } else if (p.beta == 0.0) {
+                    if (FF && p.alpha_pow2) {
+                        // hi stored, lo added at L2: hi + lo rounded once,
+                        // as the FP64 add gave, without it on the SM
 #pragma unroll
-                    for (int i = 0; i < WCOLS; i++)
-                        if (i < nlim) Cr[coff[i]] = value(i);
+                        for (int i = 0; i < WCOLS; i++) {
+                            if (i < nlim) {
+                                const int k = krow + cexp[i];
+                                Cr[coff[i]] = f32_scaled(rhi[i], k, p.alpha_sign);
+                                if constexpr (FF)
+                                    atomicAdd(Cr + coff[i], f32_scaled(rlo[i], k, p.alpha_sign));
+                            }
+                        }
+                    } else {
+#pragma unroll
+                        for (int i = 0; i < WCOLS; i++)
+                            if (i < nlim) Cr[coff[i]] = value(i);
+                    }
                 } else {
                     // read-modify-write: the old values of the next RING
                     // groups of WG columns are in flight while one group is
