@@ -291,3 +291,17 @@ def test_converge_phases_and_residual_cut():
     E, info = ccsd_mod.converge(s, ctx, dict(conv, max_iter=4), 'mixed', 3, ladder=(),
                                 low_tconv=1e-4)
     assert not info["converged"] and info["iterations_refine"] == 4
+
+
+def test_prepared_amplitude_arrays():
+    """DeviceSolver.prepare_amplitudes: the host thread returns zeroed arrays
+    of the amplitude shapes (the read-back writes only the spin-conserving
+    blocks into them)."""
+    from kelvin_gb300.cc_utils import DeviceSolver
+    for h in (0, 2):
+        sv = DeviceSolver.__new__(DeviceSolver)
+        sv.ng, sv.nv, sv.no = 3, 4, 4
+        sv.spin_blocks = lambda on=None, h=h: h
+        T1, T2 = sv.prepare_amplitudes()()
+        assert T1.shape == (3, 4, 4) and T2.shape == (3, 4, 4, 4, 4)
+        assert T2.flags.c_contiguous and not T2.any()
