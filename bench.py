@@ -877,7 +877,7 @@ def main():
                     help="Anderson depth of the iteration (0: Kelvin's damped update)")
     ap.add_argument("--mix", type=float, default=0.7,
                     help="Anderson mixing factor (with --accel)")
-    ap.add_argument("--low-tconv", type=float, default=1e-4,
+    ap.add_argument("--low-tconv", type=float, default=3e-4,
                     help="mixed form with --accel: end the few-digit phase once Kelvin's "
                          "residual measure is below this")
     ap.add_argument("--quad", default="gl", choices=["gl", "lin"],
