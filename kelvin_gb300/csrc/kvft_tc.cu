@@ -739,55 +739,11 @@ struct PackView {
 // view.
 constexpr int PT_R = 32, PT_K = 64;
 
-struct PackTile {
-    unsigned long long v[PT_R][PT_K + 1];
-    long long roff[PT_R];
-    long long koff[PT_K];
-};
-
-__device__ __forceinline__ void load_tile(const PackView &v, int b, int r0, int k0, int R, int K,
-                                          bool rows_fast, PackTile &t) {
-    const int tid = threadIdx.x, tx = tid % 32, ty = tid / 32;
-    if (tid < PT_R) {
-        const int row = r0 + tid;
-        t.roff[tid] = (row < R) ? v.r.off(row) : -1;
-    } else if (tid < PT_R + PT_K) {
-        const int k = k0 + tid - PT_R;
-        t.koff[tid - PT_R] = (k < K) ? v.c.off(k) : -1;
-    }
-    __syncthreads();
-    const double *base = v.p + (long long)b * v.bst;
-    if (rows_fast) {
-        const long long ro = t.roff[tx];
-#pragma unroll
-        for (int i = 0; i < PT_K / 8; i++) {
-            const int kk = ty + 8 * i;
-            const long long ko = t.koff[kk];
-            t.v[tx][kk] = (ro >= 0 && ko >= 0)
-                              ? (unsigned long long)__double_as_longlong(__ldg(base + ro + ko))
-                              : 0ull;
-        }
-    } else {
-        const long long ko0 = t.koff[tx], ko1 = t.koff[tx + 32];
-#pragma unroll
-        for (int i = 0; i < PT_R / 8; i++) {
-            const int rr = ty + 8 * i;
-            const long long ro = t.roff[rr];
-            t.v[rr][tx] = (ro >= 0 && ko0 >= 0)
-                              ? (unsigned long long)__double_as_longlong(__ldg(base + ro + ko0))
-                              : 0ull;
-            t.v[rr][tx + 32] = (ro >= 0 && ko1 >= 0)
-                                   ? (unsigned long long)__double_as_longlong(__ldg(base + ro + ko1))
-                                   : 0ull;
-        }
-    }
-}
-
-// Register-prefetch form of the same tile walk: offsets of tile rows r0.. and
-// k columns k0.. in a shared table (threads 0-95), then each thread's 8
-// values -- row lane at k = w + 8 i (rows_fast), else rows w + 8 i at k = lane,
-// lane + 32 -- loaded into registers, so a block can have the next tile's
-// loads in flight while it works on the current one.
+// The tile walk: offsets of tile rows r0.. and k columns k0.. in a shared
+// table (threads 0-95), then each thread's 8 values -- row lane at k = w + 8 i
+// (rows_fast), else rows w + 8 i at k = lane, lane + 32 -- loaded into
+// registers, so a block can have the next tile's loads in flight while it
+// works on the current one.
 __device__ __forceinline__ void tile_offsets(const PackView &v, int r0, int k0, int R, int K,
                                              long long *off) {
     const int tid = threadIdx.x;
