@@ -136,7 +136,7 @@ def test_unrestricted_system_amplitudes(monkeypatch):
     seen = {}
 
     class Solver(FakeSolver):
-        def amplitudes(self, out=None):
+        def amplitudes(self, out=None, resident=False):
             return T1.copy(), T2.copy()
 
         def set_amplitudes(self, a, b):
