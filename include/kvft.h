@@ -354,13 +354,8 @@ int kvft_solver_get_amplitudes(kvft_solver *s, double *T1_host,
  * MiB, allocated on first use and kept), with the host-side copy spread over
  * the host's threads.  dst_zeroed = 1 promises that T2_host holds zeros (a
  * fresh calloc): with spin blocks only the spin-conserving elements are
- * copied and the pages of the rest are never touched.  dst_zeroed = 2 also
- * promises that the pages of the spin-conserving blocks are resident
- * (written once by the host): where the device can store to pageable host
- * memory (cudaDevAttrPageableMemoryAccess, e.g. NVLink-C2C with the host
- * page tables), it writes those blocks in place, without staging.  Replaces
- * the host arrays Kelvin's solve leaves in ccsd.T1 / ccsd.T2
- * (kelvin/ccsd.py:704-712). */
+ * copied and the pages of the rest are never touched.  Replaces the host
+ * arrays Kelvin's solve leaves in ccsd.T1 / ccsd.T2 (kelvin/ccsd.py:704-712). */
 int kvft_solver_read_amplitudes(kvft_solver *s, double *T1_host, double *T2_host,
                                 int dst_zeroed);
 int kvft_solver_set_amplitudes(kvft_solver *s, const double *T1_host,

@@ -123,23 +123,20 @@ class DeviceSolver(object):
             self.h, T1.ctypes.data_as(_lib.vp), T2.ctypes.data_as(_lib.vp)),
             "kvft_solver_set_amplitudes")
 
-    def amplitudes(self, out=None, resident=False):
+    def amplitudes(self, out=None):
         """Host copies (T1, T2).  ``out``: a (T1, T2) pair of C-contiguous
         float64 arrays of these shapes whose T2 holds zeros (e.g. from
-        prepare_amplitudes), filled in place; ``resident``: its spin-block
-        pages are faulted in (prepare_amplitudes does that), so the device may
-        store them itself."""
+        prepare_amplitudes), filled in place."""
         if out is None:
             T1 = numpy.empty((self.ng, self.nv, self.no))
             # zero pages until written: with spin blocks only the
             # spin-conserving elements are copied
             T2 = numpy.zeros((self.ng, self.nv, self.nv, self.no, self.no))
-            resident = False
         else:
             T1, T2 = out
         self.ctx.check(self.ctx.L.kvft_solver_read_amplitudes(
-            self.h, T1.ctypes.data_as(_lib.vp), T2.ctypes.data_as(_lib.vp),
-            2 if resident else 1), "kvft_solver_read_amplitudes")
+            self.h, T1.ctypes.data_as(_lib.vp), T2.ctypes.data_as(_lib.vp), 1),
+            "kvft_solver_read_amplitudes")
         return T1, T2
 
     def prepare_amplitudes(self):

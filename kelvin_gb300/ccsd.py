@@ -331,7 +331,7 @@ class ccsd(object):
         self.converged = info["converged"]
         self.omega_low = info["omega_low"]
         self.phases = info.get("phases")
-        self._Tg = solver.amplitudes(out=ready(), resident=True)
+        self._Tg = solver.amplitudes(out=ready())
         self.T1, self.T2 = self._Tg
         if self._unrestricted():
             na = self.sys.u_energies_tot()[0].shape[0]

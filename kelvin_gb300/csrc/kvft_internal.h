@@ -138,7 +138,6 @@ struct kvft_ctx {
     // halves), kept for the context's lifetime.
     void *hstage = nullptr;
     size_t hstage_bytes = 0;
-    int pageable_access = -1;   // device stores to pageable host memory (-1: not asked yet)
 };
 struct KvTPackScope {
     kvft_ctx *ctx;

@@ -678,37 +678,6 @@ amp_gather_kernel(const double *__restrict__ T2, long long P, int n, int h, long
     }
 }
 
-// Direct read-back: items [0, nit) of the spin order copied in place into a
-// host array of T2's layout, stored to by the device itself (pageable host
-// memory reached through the host page tables over NVLink-C2C).  A warp per
-// row (item, i1) of h contiguous elements.
-__global__ void __launch_bounds__(256)
-amp_place_kernel(const double *__restrict__ T2, long long P, int n, int h, long long nit,
-                 double *__restrict__ out) {
-    const long long rows = nit * h;
-    const int lane = threadIdx.x % 32;
-    for (long long r = blockIdx.x * 8LL + threadIdx.x / 32; r < rows;
-         r += (long long)gridDim.x * 8) {
-        const long long it = r / h;
-        const int i1 = (int)(r - it * h);
-        const long long o = spin_item_base(it, P, n, h) + (long long)i1 * n;
-        for (int i2 = lane; i2 < h; i2 += 32) out[o + i2] = T2[o + i2];
-    }
-}
-
-bool pageable_access(kvft_ctx *ctx) {
-    if (ctx->pageable_access < 0) {
-        int v = 0;
-        if (cudaDeviceGetAttribute(&v, cudaDevAttrPageableMemoryAccess, ctx->device) !=
-            cudaSuccess) {
-            cudaGetLastError();
-            v = 0;
-        }
-        ctx->pageable_access = v ? 1 : 0;
-    }
-    return ctx->pageable_access == 1;
-}
-
 // runs f(lo, hi) over [0, n) split across the host threads
 template <class F>
 void host_parallel(long long n, F f) {
@@ -1422,19 +1391,6 @@ int kvft_solver_read_amplitudes(kvft_solver *s, double *T1h, double *T2h, int ds
     cudaSetDevice(ctx->device);
     KV_CHECK(ctx, cudaMemcpyAsync(T1h, s->T1, sizeof(double) * s->ng * s->s1(),
                                   cudaMemcpyDeviceToHost, ctx->stream));
-    const int h = (s->spin_on && s->spin_half > 0 && s->nv == s->no) ? s->spin_half : 0;
-    const bool sparse = dst_zeroed && h > 0;
-    const long long P = s->s2(), n = s->no, hh = (long long)h * h;
-    if (sparse && dst_zeroed == 2 && pageable_access(ctx)) {
-        // the caller's spin-block pages are resident: the device writes them
-        const long long items = (long long)s->ng * 6 * hh, rows = items * h;
-        const int grid = (int)std::min<long long>((rows + 7) / 8, (long long)ctx->sm_count * 16);
-        amp_place_kernel<<<grid, 256, 0, ctx->stream>>>(s->T2, P, (int)n, h, items, T2h);
-        KV_TRY(kv_launch_check(ctx, "amp_place"));
-        if (cudaStreamSynchronize(ctx->stream) != cudaSuccess)
-            return kv_fail(ctx, KVFT_EDEVICE, "read_amplitudes: device copy failed");
-        return KVFT_OK;
-    }
     constexpr size_t HALF = (size_t)32 << 20;          // doubles per staging half
     if (ctx->hstage_bytes < 2 * HALF * sizeof(double)) {
         if (ctx->hstage) cudaFreeHost(ctx->hstage);
@@ -1447,6 +1403,9 @@ int kvft_solver_read_amplitudes(kvft_solver *s, double *T1h, double *T2h, int ds
     double *hs = (double *)ctx->hstage;
     double *ds = nullptr;
     KV_CHECK(ctx, cudaHostGetDevicePointer((void **)&ds, ctx->hstage, 0));
+    const int h = (s->spin_on && s->spin_half > 0 && s->nv == s->no) ? s->spin_half : 0;
+    const bool sparse = dst_zeroed && h > 0;
+    const long long P = s->s2(), n = s->no, hh = (long long)h * h;
     // chunks: whole items of the spin order, or plain ranges of T2
     const long long per = sparse ? (long long)(HALF / hh) : (long long)HALF;
     const long long total = sparse ? (long long)s->ng * 6 * hh : (long long)s->ng * P;

@@ -136,7 +136,7 @@ def test_unrestricted_system_amplitudes(monkeypatch):
     seen = {}
 
     class Solver(FakeSolver):
-        def amplitudes(self, out=None, resident=False):
+        def amplitudes(self, out=None):
             return T1.copy(), T2.copy()
 
         def set_amplitudes(self, a, b):
