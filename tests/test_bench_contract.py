@@ -136,3 +136,28 @@ def test_bench_line_contract(monkeypatch, capsys):
     assert c["kind"] in ("port", "reference") and c["cores"] >= 1 and c["value"] > 0
     assert c["unit"] == d["unit"] and c["sample"]
     assert isinstance(d["gpu_launches"], int) and d["gpu_launches"] >= 0
+
+
+def test_reference_arm_contract(monkeypatch, capsys):
+    """--impl reference: rank 0 times the oracle's complete solve of the
+    38-spin-orbital workload and prints the same metric with impl, its CPU
+    baseline (the line's own value) and an e2e entry with no device bytes;
+    other ranks print nothing."""
+    monkeypatch.setattr(bench, "oracle_c1_iterations",
+                        lambda q, n, until_converged: (1.0, [3.0, 3.1, 3.2, 3.3], 3, -0.127))
+
+    class A(Args):
+        gpus = 1
+    monkeypatch.setattr(bench, "dist_setup", lambda: (2, 1, 1))
+    assert bench.run_reference(A(), bench.WORKLOADS["ueg38"]) == 0
+    assert not [ln for ln in capsys.readouterr().out.splitlines() if ln.startswith("{")]
+    monkeypatch.setattr(bench, "dist_setup", lambda: (1, 0, 0))
+    assert bench.run_reference(A(), bench.WORKLOADS["ueg38"]) == 0
+    d = json.loads([ln for ln in capsys.readouterr().out.splitlines() if ln.startswith("{")][-1])
+    assert d["impl"] == "reference" and d["metric"] == bench.METRIC and d["unit"] == "solves/s"
+    # guess 1 s + the three iterations to convergence
+    assert abs(d["value"] - 1.0 / (1.0 + 3.0 + 3.1 + 3.2)) < 1e-12
+    assert d["cpu_baseline"]["value"] == d["value"] and d["cpu_baseline"]["kind"] == "port"
+    assert d["e2e"] == {"value": d["value"], "unit": "solves/s", "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}
+    assert "38 spin orbitals" in d["config"]["workload"]
