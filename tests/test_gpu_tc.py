@@ -1,7 +1,6 @@
 """The digit-sliced BF16 tensor-core contraction engine (tcgen05) against
 FP64.  Error bounds are norm-wise: |C - A B| <= tol * K * max_k|A_mk| max_k|B_kn|,
 with tol from the digit count (7 levels: FP64-grade)."""
-import ctypes
 import json
 import os
 

@@ -5,7 +5,6 @@ import ctypes
 import json
 import os
 import re
-import subprocess
 
 import numpy
 import pytest
